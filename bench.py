@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark: Newton steps/s of the batched mixed-precision GB300 solver.
+
+Workload (one bench step): 256 independent beam models (element counts
+log-uniform in [10, 4000], +/-20 % properties around the 5 m cantilever pipe,
+random clamp and load triads, 0.1-10 kN step loads, HHT-alpha alpha = -0.1,
+dt = 1 ms) each advanced through 500 time steps.  Synthetic, seeded inputs.
+A "Newton step" is one Newton iteration of one model (forces, residual,
+tangent assembly and factorisation when updated, solve, update, norms).
+
+value: Newton iterations of all models / device time of the batched run,
+       state already resident in HBM (restored device-to-device between steps).
+e2e:   the same through the C ABI from host buffers: upload (fgpu_batch_create),
+       run, download of every triad position, per step.
+Also reported: the plain per-model FP64 GPU path on a sample of models, the
+max relative displacement error of the mixed path against the FP64 path, the
+CPU oracle on a bounded sample (cpu_baseline), sampled phase roofline, clocks.
+
+--impl reference: the CPU oracle (restatement of the reference algorithm; the
+reference itself does not build here) on a bounded sample with all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fedem-solvers_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton steps/s batched+served vs plain GPU at 1e-8 rel err; p50/p99 latency"
+UNIT = "Newton steps/s"
+# algorithmic work of the element pass per beam element and launch
+ELEM_BYTES = 4040          # K, M, frames, triads, velocities in; frame, deformation, forces out
+ELEM_FP64_FLOPS = 1400     # corotation, deformation, 2 matvecs 12x12, rotations
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--models", type=int, default=256)
+    ap.add_argument("--sim-steps", type=int, default=500)
+    ap.add_argument("--sweeps", type=int, default=3)
+    ap.add_argument("--plain-sample", type=int, default=24, help="models timed on the plain FP64 per-model path")
+    ap.add_argument("--cpu-sample-steps", type=int, default=40)
+    ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu legs (profiling runs)")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world <= 1:
+        return None, 0, 1
+    import torch
+    import torch.distributed as dist
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    dist.init_process_group("nccl")
+    return dist, rank, world
+
+
+def shard(cases, rank, world):
+    """Models are independent: balance by element count, no data-path collective."""
+    order = sorted(range(len(cases)), key=lambda k: -cases[k][2])
+    loads = [0] * world
+    mine = []
+    for k in order:
+        r = min(range(world), key=lambda q: loads[q])
+        loads[r] += cases[k][2]
+        if r == rank:
+            mine.append(k)
+    return sorted(mine)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9 or (vis.isdigit() and p[0] != vis):
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(cases, sample_steps, threads):
+    """Oracle Newton iterations/s over the first `sample_steps` steps of every model."""
+    from oracle.oracle import OracleModel
+
+    def one(case):
+        fsi, opts, _ = case
+        o = OracleModel(fsi, opts)
+        for _ in range(sample_steps):
+            if not o.solve_next():
+                break
+        it = o.iterations()
+        o.close()
+        return it
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        iters = sum(ex.map(one, cases))
+    dt = time.perf_counter() - t0
+    return iters / dt, iters, dt
+
+
+def run_reference(args, dist, rank, world):
+    """The CPU oracle on a bounded sample of the same workload, all host threads."""
+    from fedem_gb300 import models
+
+    if rank != 0:
+        return
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    cases = models.batch_c4(args.models, seed=4, steps=args.sim_steps)
+    threads = os.cpu_count() or 1
+    steps = max(1, args.cpu_sample_steps // 4)
+    for _ in range(args.warmup):
+        cpu_oracle_rate(cases[:8], 2, threads)
+    rates, tot_it, tot_t = [], 0, 0.0
+    for _ in range(args.steps):
+        r, it, dt = cpu_oracle_rate(cases, steps, threads)
+        rates.append(r)
+        tot_it += it
+        tot_t += dt
+    value = tot_it / tot_t
+    sample = f"all {args.models} models, first {steps} time steps each, per bench step"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator of the 256-model beam batch)",
+            "config": {"workload": f"{args.models} beam models x {args.sim_steps} HHT steps (bounded sample)",
+                       "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist, rank, world = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, dist, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+    import numpy as np
+
+    import fedem_gb300
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+
+    fedem_gb300.load_library()
+    cases_all = models.batch_c4(args.models, seed=4, steps=args.sim_steps)
+    mine = shard(cases_all, rank, world)
+    cases = [cases_all[k] for k in mine]
+    t_setup = time.perf_counter()
+    mods = [Model(f, o) for f, o, _ in cases]
+    setup_s = time.perf_counter() - t_setup
+    n_el = sum(m.nel for m in mods)
+
+    # ---- device-resident timed runs (mixed precision, batched) ----------------------
+    b = Batch(mods, mixed=True, sweeps=args.sweeps)
+    b.snapshot()
+    for _ in range(args.warmup):
+        b.restore()
+        b.run(max_batched=200000)
+    b.phase_timings(reset=True)
+    clocks = ClockSampler()
+    if dist:
+        dist.barrier()
+    clocks.start()
+    iters, dev_s, wall_s, kernels, batched = 0, 0.0, 0.0, 0, 0
+    failed = 0
+    for _ in range(args.steps):
+        b.restore()
+        st = b.run(max_batched=200000)
+        iters += st["newton_iterations"]
+        dev_s += st["device_us"] * 1e-6
+        wall_s += st["wall_us"] * 1e-6
+        kernels = st["kernels_per_iteration"]
+        batched += st["batched_iterations"]
+        failed += st["models_failed"]
+    clocks_info = clocks.stop()
+    if dist:
+        import torch
+
+        t = torch.tensor([dev_s, float(iters)], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        dev_s_max, iters_tot = float(tmax[0]), float(t[1])
+    else:
+        dev_s_max, iters_tot = dev_s, float(iters)
+    value = iters_tot / dev_s_max
+    nsamp, ms3, el_s = b.phase_timings()
+    final_mixed = b.all_triads().copy()
+    b.close()
+
+    # ---- e2e through the C ABI from host buffers ------------------------------------
+    e2e_iters, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+    out = np.zeros(12 * sum(m.ntri for m in mods))
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        be = Batch(mods, mixed=True, sweeps=args.sweeps)
+        st = be.run()
+        be.all_triads(out)
+        e2e_s += time.perf_counter() - t0
+        e2e_iters += st["newton_iterations"]
+        h2d = st["h2d_bytes"]
+        d2h = out.nbytes
+        be.close()
+    e2e_value = e2e_iters / e2e_s
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # ---- accuracy of the mixed path against the plain FP64 path ------------------
+        bf = Batch(mods, mixed=False)
+        bf.run()
+        final_fp64 = bf.all_triads().copy()
+        bf.close()
+        off, worst = 0, 0.0
+        for m, (fsi, opts, n) in zip(mods, cases):
+            nt = m.ntri
+            a = final_mixed[off:off + 12 * nt].reshape(nt, 4, 3)[:, 3, :]
+            c = final_fp64[off:off + 12 * nt].reshape(nt, 4, 3)[:, 3, :]
+            x0 = np.stack([np.arange(nt) * 0.25, np.zeros(nt), np.zeros(nt)], 1)
+            denom = max(np.abs(c - x0).max(), 1e-300)
+            worst = max(worst, float(np.abs(a - c).max() / denom))
+            off += 12 * nt
+        extras["max_rel_disp_err_mixed_vs_fp64"] = worst
+        # ---- plain per-model FP64 GPU path on a sample --------------------------------
+        idx = np.linspace(0, len(mods) - 1, min(args.plain_sample, len(mods))).astype(int)
+        p_it, p_s = 0, 0.0
+        for k in idx:
+            bp = Batch([mods[k]], mixed=False)
+            st = bp.run()
+            p_it += st["newton_iterations"]
+            p_s += st["device_us"] * 1e-6
+            bp.close()
+        plain_rate = p_it / p_s
+        extras["plain_fp64_per_model"] = {"value": plain_rate, "unit": UNIT,
+                                          "sample": f"{len(idx)} of {len(mods)} models run one at a time"}
+        extras["speedup_vs_plain"] = value / plain_rate
+        # ---- CPU oracle on a bounded sample ---------------------------------------------
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        threads = os.cpu_count() or 1
+        c_rate, c_it, c_dt = cpu_oracle_rate(cases, args.cpu_sample_steps, threads)
+        extras["cpu_baseline"] = {"value": c_rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": f"all {len(cases)} models, first {args.cpu_sample_steps} "
+                                            f"time steps each ({c_it} Newton iterations, {c_dt:.1f} s)"}
+
+    hbm_peak, peak_kind = measured_peaks()
+    roof = None
+    if nsamp > 0 and ms3[0] > 0:
+        achieved = el_s * ELEM_BYTES / (ms3[0] * 1e-3) / 1e9
+        fp64 = el_s * ELEM_FP64_FLOPS / (ms3[0] * 1e-3) / 1e12
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "kernel": "kElements (element pass after the increment)",
+                "peak_source": peak_kind, "fp64_tflops": fp64, "samples": nsamp,
+                "phase_ms_per_iteration": {"elements": ms3[0] / nsamp, "factor": ms3[1] / nsamp,
+                                           "solve": ms3[2] / nsamp}}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+                "data": "synthetic (seeded generator of the 256-model beam batch)",
+                "config": {"workload": f"{args.models} beam models (10-4000 elements, log-uniform) x "
+                                       f"{args.sim_steps} HHT-alpha steps, batched mixed precision "
+                                       f"(FP32 fronts + FP64 refinement, {args.sweeps} solves/iteration)",
+                           "elements": n_el, "models_on_rank0": len(mods), "l2": "inputs larger than L2 "
+                           "(element matrices and state of all models ~%.2f GB)" % (n_el * 5200 / 1e9),
+                           "host_setup_s": setup_s},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": kernels * batched, "kernels_per_batched_iteration": kernels,
+                "batched_iterations": batched, "models_failed": failed,
+                "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,443 @@
+// capi.cpp -- the exported C ABI: the reference's solver-core entry points
+// (src/vpmSolver/solverInterface.h, one model per process) and the batched
+// fgpu_* API.  Both drive the same GPU engine; there is no CPU solver path.
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/fedem_solver_core.h"
+#include "../../include/fgpu.h"
+#include "engine.h"
+#include "host_model.h"
+
+using namespace fgpu;
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg) {
+  g_lastError = msg;
+  return code;
+}
+
+// ---------------------------------------------------------------------------
+// legacy singleton (solverInterface.C:49 keeps the same kind of global state)
+// ---------------------------------------------------------------------------
+struct Singleton {
+  std::unique_ptr<HostModel> model;
+  std::unique_ptr<Engine> engine;
+  bool finished = false;
+  int ierr = 0;
+};
+std::unique_ptr<Singleton> g_core;
+
+bool readFileText(const std::string& path, std::string& text) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return false;
+  std::stringstream ss;
+  ss << in.rdbuf();
+  text = ss.str();
+  return true;
+}
+
+std::string optionValue(int argc, char** argv, const char* key) {
+  std::string k = std::string("-") + key + "=";
+  for (int a = 0; a < argc; ++a) {
+    if (!argv || !argv[a]) continue;
+    std::string s(argv[a]);
+    if (s.compare(0, k.size(), k) == 0) {
+      std::string v = s.substr(k.size());
+      if (v.size() >= 2 && (v[0] == '"' || v[0] == '\'') && v.back() == v[0]) v = v.substr(1, v.size() - 2);
+      return v;
+    }
+  }
+  return std::string();
+}
+
+bool hasFlag(int argc, char** argv, const char* key) {
+  std::string k = std::string("-") + key;
+  for (int a = 0; a < argc; ++a)
+    if (argv && argv[a] && (k == argv[a] || k + "+" == argv[a])) return true;
+  return false;
+}
+
+int triadIndex(const HostModel& m, int id) {
+  for (int t = 0; t < m.ntri; ++t)
+    if (m.triId[t] == id) return t;
+  return -1;
+}
+
+bool hasReachedEnd(const Singleton& s) {
+  const Control& c = s.model->ctl;
+  double t = s.engine->modelTime(0);
+  return c.tStart <= c.tEnd && t + 0.1 * c.minInc > c.tEnd;
+}
+
+}  // namespace
+
+struct fgpu_model {
+  HostModel m;
+};
+
+struct fgpu_batch {
+  Engine engine;
+  std::vector<const HostModel*> models;
+  RunStats stats;
+};
+
+extern "C" {
+
+// ===========================================================================
+// solverInterface.h entry points
+// ===========================================================================
+
+int solverInit(int argc, char** argv, const char* cfsi, const double* stateData, int ndat,
+               const double* /*gagesData*/, int /*ngda*/, const double* /*extInput*/, int* nxinp) {
+  if (nxinp) *nxinp = 0;
+  if (stateData && ndat > 0) return fail(-1, "restart from state data is not supported");
+  g_core.reset();
+  std::string text;
+  if (cfsi) {
+    text = cfsi;
+  } else {
+    std::string path = optionValue(argc, argv, "fsifile");
+    if (path.empty()) return fail(-1, "no model: give cfsi or -fsifile");
+    if (!readFileText(path, text)) return fail(-2, "cannot read " + path);
+  }
+  auto s = std::make_unique<Singleton>();
+  s->model = std::make_unique<HostModel>();
+  std::string err;
+  const char* const* cargv = const_cast<const char* const*>(argv);
+  int rc = buildModel(text.c_str(), argc, cargv, *s->model, err);
+  if (rc) return fail(rc < 0 ? rc : -100 - rc, err);
+  EngineOptions opt;
+  opt.fp32Factor = hasFlag(argc, argv, "gpuMixed");
+  opt.refineSweeps = opt.fp32Factor ? 4 : 1;
+  s->engine = std::make_unique<Engine>();
+  std::vector<const HostModel*> ms{s->model.get()};
+  rc = s->engine->upload(ms, opt, err);
+  if (!rc) rc = s->engine->initialState(err);
+  if (rc) return fail(rc, err);
+  g_core = std::move(s);
+  return 0;
+}
+
+int restartFromState(const double*, const int, const int) { return fail(-1, "restart is not supported"); }
+
+bool solveWindow(int, int, int, int, const int*, const double*, const double*, double*, int, double*, int* ierr) {
+  if (ierr) *ierr = -1;
+  return false;
+}
+
+int getStateSize(void) { return 0; }
+int getTransformationStateSize(void) { return 0; }
+int getPartDeformationStateSize(int) { return 0; }
+int getPartStressStateSize(int) { return 0; }
+int getGagesSize(void) { return 0; }
+bool saveState(double*, const int) { return false; }
+bool saveTransformationState(double*, const int) { return false; }
+bool saveGages(double*, const int) { return false; }
+bool savePartDeformationState(int, double*, const int) { return false; }
+bool savePartStressState(int, double*, const int) { return false; }
+bool getStrainsFromDisp(const double*, const int*, double*, const int, const int) { return false; }
+bool getBeamForcesFromDisp(const double*, const int*, double*, const int, const int) { return false; }
+bool getRelDisp(const double*, const int*, double*, const int, const int) { return false; }
+bool getRespVars(const double*, const int*, double*, const int, const int) { return false; }
+
+bool solveNext(int* ierr) {
+  if (ierr) *ierr = 0;
+  if (!g_core) {
+    if (ierr) *ierr = -1;
+    return false;
+  }
+  Singleton& s = *g_core;
+  if (s.ierr) {
+    if (ierr) *ierr = s.ierr;
+    return false;
+  }
+  if (hasReachedEnd(s)) return false;
+  int state = 0;
+  int rc = s.engine->advanceOneStep(0, &state);
+  if (rc || state == ST_ERROR) {
+    int st = s.engine->modelStatus(0);
+    s.ierr = rc ? rc : (st & SS_SINGULAR) ? -3 : (st & SS_MAXIT) ? 1 : -1;
+    if (ierr) *ierr = s.ierr;
+    return false;
+  }
+  s.finished = hasReachedEnd(s);
+  return !s.finished;
+}
+
+bool startStep(int* ierr) {
+  if (ierr) *ierr = -1;
+  return false;
+}
+bool solveIteration(int* ierr, bool) {
+  if (ierr) *ierr = -1;
+  return false;
+}
+bool solveEigenModes(const int, double*, double*, bool, int, int* ierr) {
+  if (ierr) *ierr = -1;
+  return false;
+}
+bool solveInverse(const double*, const int*, const int*, int, int, int* ierr) {
+  if (ierr) *ierr = -1;
+  return false;
+}
+
+int solverDone(bool) {
+  g_core.reset();
+  return 0;
+}
+void solverClose(void) { g_core.reset(); }
+
+bool setExtFunc(int, double) { return false; }
+
+double getTime(bool nextStep, int* ierr) {
+  if (!g_core) {
+    if (ierr) *ierr = -1;
+    return 0.0;
+  }
+  if (ierr) *ierr = 0;
+  double t = g_core->engine->modelTime(0);
+  return nextStep ? t + g_core->model->ctl.tInc : t;
+}
+
+bool setTime(double) { return false; }
+
+double evalFunc(int, const char*, double, int* ierr) {
+  if (ierr) *ierr = -1;
+  return 0.0;
+}
+int getFuncId(const char*) { return -1; }
+
+int getEquations(int bid, int* meqn) {
+  if (!g_core) return 0;
+  const HostModel& m = *g_core->model;
+  int t = triadIndex(m, bid);
+  if (t < 0) return 0;
+  for (int k = 0; k < m.triNdof[t]; ++k) meqn[k] = m.meqn[m.triFirstDof[t] + k] + 1;
+  return m.triNdof[t];
+}
+
+int getStateVar(int bid, double* var) {
+  if (!g_core) return 0;
+  const HostModel& m = *g_core->model;
+  int t = triadIndex(m, bid);
+  if (t < 0 || m.triNdof[t] < 3) return 0;
+  std::vector<double> ur(12 * (size_t)m.ntri);
+  g_core->engine->getTriadUr(0, ur.data());
+  for (int r = 0; r < 3; ++r) var[r] = ur[12 * (size_t)t + 9 + r];
+  return 3;
+}
+
+int getSystemSize(bool dofs) {
+  if (!g_core) return 0;
+  return dofs ? g_core->model->ndof : g_core->model->neq;
+}
+
+bool getSystemMatrix(double* Smat, int iMat) {
+  if (!g_core || iMat != 0) return false;
+  const HostModel& m = *g_core->model;
+  std::vector<double> v(m.colInd.size());
+  g_core->engine->getCsrValues(0, v.data());
+  std::memset(Smat, 0, sizeof(double) * (size_t)m.neq * m.neq);
+  for (int i = 0; i < m.neq; ++i)
+    for (int k = m.rowPtr[i]; k < m.rowPtr[i + 1]; ++k) Smat[(size_t)i + (size_t)m.neq * m.colInd[k]] = v[k];
+  return true;
+}
+bool getNewtonMatrix(double* Nmat) { return getSystemMatrix(Nmat, 0); }
+bool getStiffnessMatrix(double*) { return false; }
+bool getMassMatrix(double*) { return false; }
+bool getDampingMatrix(double*) { return false; }
+
+bool getElementStiffnessMatrix(double* Kmat, int bid) {
+  if (!g_core) return false;
+  const HostModel& m = *g_core->model;
+  for (int e = 0; e < m.nel; ++e)
+    if (m.elId[e] == bid) {
+      std::memcpy(Kmat, &m.K[144 * (size_t)e], sizeof(double) * 144);
+      return true;
+    }
+  return false;
+}
+
+bool getRhsVector(double* Rvec, int iVec) {
+  if (!g_core || iVec != 0) return false;
+  g_core->engine->getEqVector(0, 4, Rvec);
+  return true;
+}
+bool setRhsVector(const double*) { return false; }
+bool addRhsVector(const double*) { return false; }
+bool getJointSprCoeff(double*, int) { return false; }
+
+// ===========================================================================
+// fgpu.h batched API
+// ===========================================================================
+
+int fgpu_model_create(const char* fsi, int argc, const char* const* argv, fgpu_model** out) {
+  if (!out) return fail(-1, "null output handle");
+  *out = nullptr;
+  auto h = std::make_unique<fgpu_model>();
+  std::string err;
+  int rc = buildModel(fsi, argc, argv, h->m, err);
+  if (rc) return fail(rc, err);
+  *out = h.release();
+  return 0;
+}
+
+void fgpu_model_destroy(fgpu_model* m) { delete m; }
+
+int fgpu_model_sizes(const fgpu_model* h, long long* s) {
+  if (!h || !s) return fail(-1, "null argument");
+  const HostModel& m = h->m;
+  s[0] = m.ntri; s[1] = m.ndof; s[2] = m.neq; s[3] = m.nel; s[4] = (long long)m.colInd.size();
+  s[5] = (long long)m.fronts.size(); s[6] = m.maxFront; s[7] = m.maxHeight + 1;
+  return 0;
+}
+
+int fgpu_model_meqn(const fgpu_model* h, int* meqn) {
+  if (!h || !meqn) return fail(-1, "null argument");
+  for (int i = 0; i < h->m.ndof; ++i) meqn[i] = h->m.meqn[i] + 1;
+  return 0;
+}
+
+int fgpu_model_csr_pattern(const fgpu_model* h, int* rowptr, int* cols) {
+  if (!h) return fail(-1, "null argument");
+  if (rowptr) std::memcpy(rowptr, h->m.rowPtr.data(), sizeof(int) * h->m.rowPtr.size());
+  if (cols) std::memcpy(cols, h->m.colInd.data(), sizeof(int) * h->m.colInd.size());
+  return 0;
+}
+
+int fgpu_model_symbolic(const fgpu_model* h, int* perm, int* info4) {
+  if (!h) return fail(-1, "null argument");
+  if (perm) std::memcpy(perm, h->m.perm.data(), sizeof(int) * h->m.perm.size());
+  if (info4)
+    for (size_t f = 0; f < h->m.fronts.size(); ++f) {
+      const Front& fr = h->m.fronts[f];
+      info4[4 * f] = fr.npiv; info4[4 * f + 1] = fr.nrow; info4[4 * f + 2] = fr.parent; info4[4 * f + 3] = fr.height;
+    }
+  return 0;
+}
+
+int fgpu_model_element_matrix(const fgpu_model* h, int iel, int which, double* mat) {
+  if (!h || !mat || iel < 0 || iel >= h->m.nel || which < 0 || which > 2) return fail(-1, "bad argument");
+  const std::vector<double>& src = which == 0 ? h->m.K : which == 1 ? h->m.M : h->m.C;
+  std::memcpy(mat, &src[144 * (size_t)iel], sizeof(double) * 144);
+  return 0;
+}
+
+int fgpu_batch_create(int n, fgpu_model* const* models, int mixed, int sweeps, fgpu_batch** out) {
+  if (!out || !models || n <= 0) return fail(-1, "bad argument");
+  *out = nullptr;
+  auto b = std::make_unique<fgpu_batch>();
+  for (int k = 0; k < n; ++k) {
+    if (!models[k]) return fail(-1, "null model handle");
+    b->models.push_back(&models[k]->m);
+  }
+  EngineOptions opt;
+  opt.fp32Factor = mixed != 0;
+  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 3 : 1);
+  std::string err;
+  int rc = b->engine.upload(b->models, opt, err);
+  if (!rc) rc = b->engine.initialState(err);
+  if (rc) return fail(rc, err);
+  *out = b.release();
+  return 0;
+}
+
+void fgpu_batch_destroy(fgpu_batch* b) { delete b; }
+
+int fgpu_batch_run(fgpu_batch* b, long long maxBatched, long long* s8) {
+  if (!b) return fail(-1, "null batch");
+  RunStats st;
+  b->engine.setStepLimit(1LL << 62);
+  int rc = b->engine.run(maxBatched > 0 ? maxBatched : (1LL << 40), &st);
+  if (rc) return fail(rc, "batched run failed (CUDA error)");
+  if (s8) {
+    s8[0] = st.newtonIterations; s8[1] = st.timeSteps; s8[2] = st.batchedIterations;
+    s8[3] = st.modelsDone; s8[4] = st.modelsFailed; s8[5] = b->engine.launchesPerIteration();
+    s8[6] = (long long)(b->engine.lastRunSeconds() * 1.0e6);
+    s8[7] = (long long)(b->engine.lastRunDeviceSeconds() * 1.0e6);
+    s8[8] = b->engine.uploadedBytes();
+    s8[9] = 0;
+  }
+  return 0;
+}
+
+int fgpu_batch_model_info(fgpu_batch* b, int k, int* state, int* status, double* time, long long* steps,
+                          long long* iters) {
+  if (!b || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad model index");
+  if (state) *state = b->engine.modelState(k);
+  if (status) *status = b->engine.modelStatus(k);
+  if (time) *time = b->engine.modelTime(k);
+  if (steps) *steps = b->engine.modelSteps(k);
+  if (iters) *iters = b->engine.modelIterations(k);
+  return 0;
+}
+
+int fgpu_batch_get_triads(fgpu_batch* b, int k, double* ur) {
+  if (!b || !ur || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  b->engine.getTriadUr(k, ur);
+  return 0;
+}
+
+long long fgpu_batch_get_all_triads(fgpu_batch* b, double* ur) {
+  if (!b || !ur) return fail(-1, "bad argument");
+  long long off = 0;
+  for (int k = 0; k < b->engine.numModels(); ++k) off += 12LL * b->engine.getTriadUr(k, ur + off);
+  return off;
+}
+
+int fgpu_batch_get_newton_values(fgpu_batch* b, int k, double* vals) {
+  if (!b || !vals || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  b->engine.getCsrValues(k, vals);
+  return 0;
+}
+
+int fgpu_batch_get_vector(fgpu_batch* b, int k, int which, double* v) {
+  if (!b || !v || k < 0 || k >= b->engine.numModels() || which < 0 || which > 5) return fail(-1, "bad argument");
+  b->engine.getEqVector(k, which, v);
+  return 0;
+}
+
+int fgpu_batch_get_norms(fgpu_batch* b, int k, double* n18) {
+  if (!b || !n18 || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  b->engine.getNorms(k, n18);
+  return 0;
+}
+
+int fgpu_batch_step(fgpu_batch* b, int k, int* state) {
+  if (!b || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad model index");
+  int rc = b->engine.advanceOneStep(k, state);
+  return rc ? fail(rc, "step failed") : 0;
+}
+
+int fgpu_batch_snapshot(fgpu_batch* b) {
+  if (!b) return fail(-1, "null batch");
+  int rc = b->engine.snapshot();
+  return rc ? fail(rc, "snapshot failed") : 0;
+}
+
+int fgpu_batch_restore(fgpu_batch* b) {
+  if (!b) return fail(-1, "null batch");
+  int rc = b->engine.restore();
+  return rc ? fail(rc, "restore failed (no snapshot?)") : 0;
+}
+
+long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems, int reset) {
+  if (!b || !ms3) return fail(-1, "bad argument");
+  long long n = b->engine.phaseTimings(ms3, elems);
+  if (reset) b->engine.resetPhaseTimings();
+  return n;
+}
+
+const char* fgpu_last_error(void) { return g_lastError.c_str(); }
+
+}  // extern "C"

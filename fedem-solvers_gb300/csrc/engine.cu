@@ -1,0 +1,616 @@
+// engine.cu -- host orchestration of the batched GB300 Newton engine.
+//
+// One batched iteration performs, for every active model, exactly one Newton
+// iteration of the reference's NewmarkInt loop
+// (src/vpmSolver/newmarkRoutinesModule.f90:711-1024):
+//   begin-step control -> predictor vectors -> predictor element pass ->
+//   force gather + residual -> [tangent: element Newton matrices -> CSR ->
+//   multifrontal factor] -> solve (+ FP64 refinement) -> increment (vectors,
+//   triads) -> element pass with the new positions -> norms + convergence.
+// The sequence is a fixed list of launches, captured once in a CUDA graph
+// and replayed; models that are idle or in another phase early-exit on their
+// per-model flags, so models of uneven size and iteration count share launches.
+
+#include <chrono>
+#include <climits>
+#include <cstring>
+
+#include "engine.h"
+
+namespace fgpu {
+
+#define FG_CHECK(call)                                            \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) {                                      \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);  \
+      return -900;                                                \
+    }                                                             \
+  } while (0)
+
+Engine::~Engine() {
+  if (graphExec_) cudaGraphExecDestroy(graphExec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (cudaEvent_t ev : ev_)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : evRun_)
+    if (ev) cudaEventDestroy(ev);
+  for (void* p : allocs_) cudaFree(p);
+  if (hActive_) cudaFreeHost(hActive_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <typename T>
+T* Engine::alloc(size_t n) {
+  if (n == 0) n = 1;
+  void* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+    allocFailed_ = true;
+    return nullptr;
+  }
+  cudaMemsetAsync(p, 0, n * sizeof(T), stream_);
+  allocs_.push_back(p);
+  return static_cast<T*>(p);
+}
+
+namespace {
+thread_local long long t_putBytes = 0;  // host -> device bytes of the current upload
+
+template <typename T>
+cudaError_t put(T* dst, const std::vector<T>& src, cudaStream_t s) {
+  if (src.empty()) return cudaSuccess;
+  t_putBytes += (long long)(src.size() * sizeof(T));
+  return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+}  // namespace
+
+int Engine::upload(const std::vector<const HostModel*>& models, const EngineOptions& opt, std::string& err) {
+  hm_ = models;
+  opt_ = opt;
+  t_putBytes = 0;
+  if (!opt_.fp32Factor) opt_.refineSweeps = 1;
+  if (opt_.refineSweeps < 1) opt_.refineSweeps = 1;
+  FG_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  const int nm = (int)models.size();
+  // ---- global offsets --------------------------------------------------------
+  modelTriOff_.assign(nm, 0);
+  modelDofOff_.assign(nm, 0);
+  modelEqOff_.assign(nm, 0);
+  modelElOff_.assign(nm, 0);
+  modelSlotOff_.assign(nm, 0);
+  std::vector<int> frontOff(nm, 0);
+  std::vector<int64_t> contribOff(nm, 0), eqContribOff(nm, 0), rowsOff(nm, 0), lOff(nm, 0), uOff(nm, 0),
+      wOff(nm, 0), childOff(nm, 0), relOff(nm, 0), asmOff(nm, 0);
+  int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, maxH = 0;
+  int64_t nslot = 0, ncontrib = 0, neqc = 0, nrows = 0, nl = 0, nu = 0, nw = 0, nch = 0, nrel = 0, nasm = 0;
+  bool anyC = false;
+  for (int k = 0; k < nm; ++k) {
+    const HostModel& h = *models[k];
+    modelTriOff_[k] = ntri; modelDofOff_[k] = ndof; modelEqOff_[k] = neq; modelElOff_[k] = nel;
+    modelSlotOff_[k] = nslot; frontOff[k] = nfr; contribOff[k] = ncontrib; eqContribOff[k] = neqc;
+    rowsOff[k] = nrows; lOff[k] = nl; uOff[k] = nu; wOff[k] = nw; childOff[k] = nch; relOff[k] = nrel;
+    asmOff[k] = nasm;
+    ntri += h.ntri; ndof += h.ndof; neq += h.neq; nel += h.nel; nfr += (int)h.fronts.size();
+    nslot += (int64_t)h.colInd.size(); ncontrib += (int64_t)h.slotSrc.size(); neqc += (int64_t)h.eqSrc.size();
+    nrows += (int64_t)h.frontRows.size(); nl += h.lSize; nu += h.uSize; nw += h.wSize;
+    nch += (int64_t)h.childList.size(); nrel += (int64_t)h.relIndex.size(); nasm += (int64_t)h.asmSlot.size();
+    maxH = std::max(maxH, h.maxHeight);
+    for (uint8_t c : h.hasC) anyC |= c != 0;
+  }
+  if (12LL * nel > INT_MAX || neqc > INT_MAX) { err = "batch too large for 32-bit gather indices"; return -901; }
+  d_.ntriTot = ntri; d_.ndofTot = ndof; d_.neqTot = neq; d_.nelTot = nel; d_.nslotTot = nslot;
+  d_.nfrontTot = nfr;
+  // ---- per-model control -------------------------------------------------------
+  DevModels& M = d_.m;
+  M.n = nm;
+  auto iv = [&](std::vector<int>& v) { v.assign(nm, 0); };
+  std::vector<int> triOff(nm), ntriV(nm), dofOff(nm), ndofV(nm), eqOff(nm), neqV(nm), elOff(nm), nelV(nm);
+  std::vector<double> tStart(nm), tEnd(nm), dt(nm), minInc(nm), alpha(nm), beta(nm), gamma(nm), wD(3 * nm),
+      wF(3 * nm), grav(3 * nm), tolV(18 * nm), scaleN(3 * nm, -1.0), equTol(nm), equLim(nm);
+  std::vector<int> tolC(18 * nm), maxIt(nm), minIt(nm), fixedIt(nm), nUpdat(nm), maxSeq(nm), staticMode(nm),
+      staticDone(nm);
+  std::vector<long long> stepLimit(nm, LLONG_MAX);
+  iv(maxIt);
+  for (int k = 0; k < nm; ++k) {
+    const HostModel& h = *models[k];
+    const Control& c = h.ctl;
+    triOff[k] = modelTriOff_[k]; ntriV[k] = h.ntri; dofOff[k] = modelDofOff_[k]; ndofV[k] = h.ndof;
+    eqOff[k] = modelEqOff_[k]; neqV[k] = h.neq; elOff[k] = modelElOff_[k]; nelV[k] = h.nel;
+    tStart[k] = c.tStart; tEnd[k] = c.tEnd; dt[k] = c.tInc; minInc[k] = c.minInc;
+    alpha[k] = c.alpha; beta[k] = c.beta; gamma[k] = c.gamma;
+    for (int q = 0; q < 3; ++q) { wD[3 * k + q] = c.wDisp[q]; wF[3 * k + q] = c.wForce[q]; grav[3 * k + q] = c.gravity[q]; }
+    for (int q = 0; q < 18; ++q) { tolC[18 * k + q] = c.tolCode[q]; tolV[18 * k + q] = c.tolVal[q]; }
+    maxIt[k] = c.maxIt; minIt[k] = c.minIt; fixedIt[k] = c.fixedIt; nUpdat[k] = c.nUpdat; maxSeq[k] = c.maxSeqNoUpdate;
+    double eqTol = c.initEquilibrium ? c.tolInitEquil : 0.0, eqLim = c.initEquilibrium ? c.limInitEquilStep : 0.0;
+    equTol[k] = eqTol; equLim[k] = eqLim;
+    staticMode[k] = (eqLim > 0.0 && h.neq > 0) ? (eqTol > 0.0 ? 2 : 1) : 0;
+    staticDone[k] = staticMode[k] == 0 ? 1 : 0;
+  }
+#define UP_I(field, vec) if (!(M.field = alloc<int>(nm)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
+#define UP_D(field, vec, n) if (!(M.field = alloc<double>(n)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
+  UP_I(triOff, triOff); UP_I(ntri, ntriV); UP_I(dofOff, dofOff); UP_I(ndof, ndofV);
+  UP_I(eqOff, eqOff); UP_I(neq, neqV); UP_I(elOff, elOff); UP_I(nel, nelV);
+  UP_D(time, tStart, nm); UP_D(dt, dt, nm); UP_D(tStart, tStart, nm); UP_D(tEnd, tEnd, nm);
+  UP_D(minInc, minInc, nm); UP_D(alpha, alpha, nm); UP_D(beta, beta, nm); UP_D(gamma, gamma, nm);
+  UP_D(scaleN, scaleN, 3 * nm); UP_D(wDisp, wD, 3 * nm); UP_D(wForce, wF, 3 * nm); UP_D(gravity, grav, 3 * nm);
+  UP_D(tolVal, tolV, 18 * nm); UP_D(equTol, equTol, nm); UP_D(equLim, equLim, nm);
+  if (!(M.tolCode = alloc<int>(18 * nm)) || put(M.tolCode, tolC, stream_) != cudaSuccess) { err = "alloc tolCode"; return -902; }
+  UP_I(maxIt, maxIt); UP_I(minIt, minIt); UP_I(fixedIt, fixedIt); UP_I(nUpdat, nUpdat); UP_I(maxSeq, maxSeq);
+  UP_I(staticMode, staticMode); UP_I(staticDone, staticDone);
+#undef UP_I
+#undef UP_D
+  M.sacc = alloc<double>(nm); M.svel = alloc<double>(nm); M.pc = alloc<double>(4 * nm);
+  M.normVal = alloc<double>(18 * nm); M.deln = alloc<double>(nm); M.staticScale = alloc<double>(nm);
+  M.state = alloc<int>(nm); M.flags = alloc<int>(nm); M.status = alloc<int>(nm); M.iter = alloc<int>(nm);
+  M.nSeqNoUpd = alloc<int>(nm); M.negPiv = alloc<int>(nm); M.staticIter = alloc<int>(nm); M.staticNinc = alloc<int>(nm);
+  M.nStep = alloc<long long>(nm); M.nIter = alloc<long long>(nm); M.stepLimit = alloc<long long>(nm);
+  if (put(M.stepLimit, stepLimit, stream_) != cudaSuccess) { err = "upload stepLimit"; return -902; }
+
+  // ---- triads, DOFs, equations ---------------------------------------------------
+  std::vector<double> ur;
+  ur.reserve(12 * (size_t)ntri);
+  std::vector<int> triFirst, triNd, triModel, meqn, dofType, dofModel, eqModel;
+  std::vector<double> qext;
+  for (int k = 0; k < nm; ++k) {
+    const HostModel& h = *models[k];
+    ur.insert(ur.end(), h.ur.begin(), h.ur.end());
+    for (int t = 0; t < h.ntri; ++t) {
+      triFirst.push_back(h.triFirstDof[t] + modelDofOff_[k]);
+      triNd.push_back(h.triNdof[t]);
+      triModel.push_back(k);
+    }
+    for (int i = 0; i < h.ndof; ++i) {
+      meqn.push_back(h.meqn[i] >= 0 ? h.meqn[i] + modelEqOff_[k] : -1);
+      dofType.push_back(h.dofType[i]);
+      dofModel.push_back(k);
+    }
+    for (int i = 0; i < h.neq; ++i) eqModel.push_back(k);
+    qext.insert(qext.end(), h.qext.begin(), h.qext.end());
+  }
+#define UPV(ptr, T, vec) if (!(ptr = alloc<T>(vec.size())) || put(ptr, vec, stream_) != cudaSuccess) { err = "upload " #ptr; return -903; }
+  UPV(d_.ur, double, ur);
+  UPV(d_.triFirstDof, int, triFirst); UPV(d_.triNdof, int, triNd); UPV(d_.triModel, int, triModel);
+  UPV(d_.meqn, int, meqn); UPV(d_.dofType, int, dofType); UPV(d_.dofModel, int, dofModel);
+  UPV(d_.eqModel, int, eqModel); UPV(d_.qext, double, qext);
+  d_.urd = alloc<double>(ndof); d_.urdd = alloc<double>(ndof); d_.dk = alloc<double>(ndof); d_.ak = alloc<double>(ndof);
+  d_.rinc = alloc<double>(ndof); d_.sinc0 = alloc<double>(ndof); d_.sinc1 = alloc<double>(ndof); d_.sinc2 = alloc<double>(ndof);
+  d_.FSk = alloc<double>(neq); d_.FDk = alloc<double>(neq); d_.FIk = alloc<double>(neq); d_.Qk = alloc<double>(neq);
+  d_.FIact = alloc<double>(neq); d_.res = alloc<double>(neq); d_.del = alloc<double>(neq);
+  d_.x64 = alloc<double>(neq); d_.xref = alloc<double>(neq); d_.rref = alloc<double>(neq); d_.x32 = alloc<float>(neq);
+  d_.rhs32 = nullptr;
+
+  // ---- elements (SoA) -------------------------------------------------------------
+  auto soa = [&](int width, auto getter) {
+    std::vector<double> v((size_t)width * nel);
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      for (int e = 0; e < h.nel; ++e)
+        for (int c = 0; c < width; ++c) v[(size_t)c * nel + modelElOff_[k] + e] = getter(h, e, c);
+    }
+    return v;
+  };
+  {
+    auto K = soa(144, [](const HostModel& h, int e, int c) { return h.K[144 * (size_t)e + c]; });
+    UPV(d_.K, double, K);
+  }
+  {
+    auto Mm = soa(144, [](const HostModel& h, int e, int c) { return h.M[144 * (size_t)e + c]; });
+    UPV(d_.M, double, Mm);
+  }
+  if (anyC) {
+    auto C = soa(144, [](const HostModel& h, int e, int c) { return h.C[144 * (size_t)e + c]; });
+    UPV(d_.C, double, C);
+  } else {
+    d_.C = alloc<double>(1);
+  }
+  {
+    auto fg = soa(36, [](const HostModel& h, int e, int c) { return h.fg[36 * (size_t)e + c]; });
+    UPV(d_.fg, double, fg);
+    auto S = soa(12, [](const HostModel& h, int e, int c) { return h.supTr[12 * (size_t)e + c]; });
+    UPV(d_.supTr, double, S);
+    auto R = soa(12, [](const HostModel& h, int e, int c) { return h.triRelSup[12 * (size_t)e + c]; });
+    UPV(d_.triRelSup, double, R);
+    auto T = soa(24, [](const HostModel& h, int e, int c) { return h.trUnd[24 * (size_t)e + c]; });
+    UPV(d_.trUnd, double, T);
+    auto O = soa(9, [](const HostModel& h, int e, int c) { return h.elOffset[9 * (size_t)e + c]; });
+    UPV(d_.offset, double, O);
+  }
+  d_.N = alloc<double>(144 * (size_t)nel);
+  d_.elMat = alloc<double>(144 * (size_t)nel);
+  d_.finit = alloc<double>(12 * (size_t)nel);
+  d_.finitPrev = alloc<double>(12 * (size_t)nel);
+  d_.Fel = alloc<double>(48 * (size_t)nel);
+  {
+    std::vector<int> elTri(2 * (size_t)nel), elRef(3 * (size_t)nel), elModel(nel);
+    std::vector<double> ss(nel), kd(nel);
+    std::vector<uint8_t> hc(nel), hv(nel);
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      for (int e = 0; e < h.nel; ++e) {
+        int g = modelElOff_[k] + e;
+        for (int n = 0; n < 2; ++n) elTri[(size_t)n * nel + g] = h.elTri[2 * e + n] + modelTriOff_[k];
+        for (int j = 0; j < 3; ++j) elRef[(size_t)j * nel + g] = h.elRef[3 * e + j];
+        elModel[g] = k;
+        ss[g] = h.stifScl[e];
+        kd[g] = h.kDmp[e];
+        hc[g] = h.hasC[e];
+        hv[g] = h.hasVld[e];
+      }
+    }
+    UPV(d_.elTri, int, elTri); UPV(d_.elRef, int, elRef); UPV(d_.elModel, int, elModel);
+    UPV(d_.stifScl, double, ss); UPV(d_.kDmp, double, kd); UPV(d_.hasC, uint8_t, hc); UPV(d_.hasVld, uint8_t, hv);
+  }
+  // ---- CSR and gather maps -----------------------------------------------------------
+  {
+    std::vector<int64_t> rowPtr(neq + 1, 0), slotPtr(nslot + 1, 0), slotSrc;
+    std::vector<int> colInd, slotModel, eqPtr(neq + 1, 0), eqSrc;
+    colInd.reserve(nslot);
+    slotModel.reserve(nslot);
+    slotSrc.reserve(ncontrib);
+    eqSrc.reserve(neqc);
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      for (int i = 0; i < h.neq; ++i) {
+        rowPtr[modelEqOff_[k] + i + 1] = modelSlotOff_[k] + h.rowPtr[i + 1];
+        eqPtr[modelEqOff_[k] + i + 1] = (int)(eqContribOff[k] + h.eqPtr[i + 1]);
+      }
+      for (size_t s = 0; s < h.colInd.size(); ++s) {
+        colInd.push_back(h.colInd[s] + modelEqOff_[k]);
+        slotModel.push_back(k);
+        slotPtr[modelSlotOff_[k] + s + 1] = contribOff[k] + h.slotPtr[s + 1];
+      }
+      for (int src : h.slotSrc) {
+        int e = src / 144, entry = src % 144;
+        slotSrc.push_back((int64_t)entry * nel + modelElOff_[k] + e);
+      }
+      for (int src : h.eqSrc) {
+        int e = src / 12, loc = src % 12;
+        eqSrc.push_back(loc * nel + modelElOff_[k] + e);
+      }
+    }
+    UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int64_t, slotPtr);
+    UPV(d_.slotSrc, int64_t, slotSrc); UPV(d_.slotModel, int, slotModel); UPV(d_.eqPtr, int, eqPtr);
+    UPV(d_.eqSrc, int, eqSrc);
+    d_.csrVal = alloc<double>(nslot);
+  }
+  // ---- fronts ------------------------------------------------------------------------------
+  {
+    std::vector<int> npiv, nrow, parent, fmodel, nchild, nasmv, frontRows, childList, relIndex, asmPos;
+    std::vector<int64_t> rowOffV, lOffV, uOffV, wOffV, childOffV, relOffV, asmOffV, asmSlot;
+    std::vector<std::vector<int>> byHeight(maxH + 1);
+    std::vector<int> maxRowH(maxH + 1, 0);
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      for (size_t f = 0; f < h.fronts.size(); ++f) {
+        const Front& fr = h.fronts[f];
+        npiv.push_back(fr.npiv);
+        nrow.push_back(fr.nrow);
+        parent.push_back(fr.parent >= 0 ? fr.parent + frontOff[k] : -1);
+        fmodel.push_back(k);
+        nchild.push_back(fr.nchild);
+        nasmv.push_back(fr.nasm);
+        rowOffV.push_back(fr.rowOff + rowsOff[k]);
+        lOffV.push_back(fr.lOff + lOff[k]);
+        uOffV.push_back(fr.uOff + uOff[k]);
+        wOffV.push_back(fr.wOff + wOff[k]);
+        childOffV.push_back(fr.childOff + childOff[k]);
+        relOffV.push_back(fr.relOff + relOff[k]);
+        asmOffV.push_back(fr.asmOff + asmOff[k]);
+        byHeight[fr.height].push_back(frontOff[k] + (int)f);
+        maxRowH[fr.height] = std::max(maxRowH[fr.height], fr.nrow);
+      }
+      for (int r : h.frontRows) frontRows.push_back(r + modelEqOff_[k]);
+      for (int c : h.childList) childList.push_back(c + frontOff[k]);
+      relIndex.insert(relIndex.end(), h.relIndex.begin(), h.relIndex.end());
+      for (int s : h.asmSlot) asmSlot.push_back((int64_t)s + modelSlotOff_[k]);
+      asmPos.insert(asmPos.end(), h.asmPos.begin(), h.asmPos.end());
+    }
+    UPV(d_.fNpiv, int, npiv); UPV(d_.fNrow, int, nrow); UPV(d_.fParent, int, parent); UPV(d_.fModel, int, fmodel);
+    UPV(d_.fNchild, int, nchild); UPV(d_.fNasm, int, nasmv);
+    UPV(d_.fRowOff, int64_t, rowOffV); UPV(d_.fLOff, int64_t, lOffV); UPV(d_.fUOff, int64_t, uOffV);
+    UPV(d_.fWOff, int64_t, wOffV); UPV(d_.fChildOff, int64_t, childOffV); UPV(d_.fRelOff, int64_t, relOffV);
+    UPV(d_.fAsmOff, int64_t, asmOffV);
+    UPV(d_.frontRows, int, frontRows); UPV(d_.childList, int, childList); UPV(d_.relIndex, int, relIndex);
+    UPV(d_.asmSlot, int64_t, asmSlot); UPV(d_.asmPos, int, asmPos);
+    if (opt_.fp32Factor) {
+      d_.L32 = alloc<float>(nl); d_.U32 = alloc<float>(nu); d_.w32 = alloc<float>(nw);
+      if (!d_.L32 || !d_.U32 || !d_.w32) { err = "out of device memory (factor)"; return -904; }
+    } else {
+      d_.L64 = alloc<double>(nl); d_.U64 = alloc<double>(nu); d_.w64 = alloc<double>(nw);
+      if (!d_.L64 || !d_.U64 || !d_.w64) { err = "out of device memory (factor)"; return -904; }
+    }
+    std::vector<int> flat;
+    std::vector<size_t> starts;
+    for (int hgt = 0; hgt <= maxH; ++hgt) {
+      starts.push_back(flat.size());
+      flat.insert(flat.end(), byHeight[hgt].begin(), byHeight[hgt].end());
+    }
+    int* dFlat = nullptr;
+    UPV(dFlat, int, flat);
+    levels_.clear();
+    for (int hgt = 0; hgt <= maxH; ++hgt) {
+      LevelPlan lp;
+      lp.fronts = dFlat + starts[hgt];
+      lp.count = (int)byHeight[hgt].size();
+      lp.maxRow = maxRowH[hgt];
+      size_t perWarpBytes = ((size_t)lp.maxRow * lp.maxRow + 2 * lp.maxRow) * (opt_.fp32Factor ? 4 : 8);
+      if (perWarpBytes > 200 * 1024) { err = "front too large for the shared-memory front kernels"; return -905; }
+      levels_.push_back(lp);
+    }
+  }
+#undef UPV
+  if (allocFailed_) { err = "out of device memory"; return -906; }
+  dActive_ = alloc<int>(1);
+  dActiveEl_ = alloc<long long>(1);
+  FG_CHECK(cudaMallocHost(&hActive_, sizeof(int)));
+  FG_CHECK(cudaMallocHost(&hActiveEl_, sizeof(long long)));
+  for (cudaEvent_t& ev : ev_) FG_CHECK(cudaEventCreate(&ev));
+  // mutable state for snapshot/restore (everything a run changes that is read
+  // before it is rewritten)
+  auto reg = [&](void* p, size_t bytes) { mutable_.push_back({p, bytes}); };
+  const size_t D = sizeof(double);
+  reg(d_.ur, D * 12 * (size_t)ntri);
+  for (double* p : {d_.urd, d_.urdd, d_.dk, d_.ak, d_.rinc, d_.sinc0, d_.sinc1, d_.sinc2}) reg(p, D * (size_t)ndof);
+  for (double* p : {d_.FSk, d_.FDk, d_.FIk, d_.Qk, d_.FIact, d_.res, d_.del}) reg(p, D * (size_t)neq);
+  reg(d_.supTr, D * 12 * (size_t)nel);
+  reg(d_.finit, D * 12 * (size_t)nel);
+  reg(d_.finitPrev, D * 12 * (size_t)nel);
+  reg(d_.Fel, D * 48 * (size_t)nel);
+  for (double* p : {M.time, M.sacc, M.svel, M.deln, M.staticScale}) reg(p, D * nm);
+  for (double* p : {M.scaleN, M.gravity}) reg(p, D * 3 * nm);
+  reg(M.pc, D * 4 * nm);
+  reg(M.normVal, D * 18 * nm);
+  for (int* p : {M.state, M.flags, M.status, M.iter, M.nSeqNoUpd, M.negPiv, M.staticIter, M.staticNinc,
+                 M.staticDone})
+    reg(p, sizeof(int) * nm);
+  for (long long* p : {M.nStep, M.nIter, M.stepLimit}) reg(p, sizeof(long long) * nm);
+  uploadedBytes_ = t_putBytes;
+  FG_CHECK(cudaStreamSynchronize(stream_));
+  FG_CHECK(cudaGetLastError());
+  return 0;
+}
+
+int Engine::snapshot() {
+  size_t total = 0;
+  for (auto& m : mutable_) total += (m.second + 255) & ~size_t(255);
+  if (!backup_) {
+    backup_ = alloc<char>(total);
+    if (!backup_) return -930;
+  }
+  size_t off = 0;
+  for (auto& m : mutable_) {
+    cudaMemcpyAsync(backup_ + off, m.first, m.second, cudaMemcpyDeviceToDevice, stream_);
+    off += (m.second + 255) & ~size_t(255);
+  }
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -931;
+}
+
+int Engine::restore() {
+  if (!backup_) return -932;
+  size_t off = 0;
+  for (auto& m : mutable_) {
+    cudaMemcpyAsync(m.first, backup_ + off, m.second, cudaMemcpyDeviceToDevice, stream_);
+    off += (m.second + 255) & ~size_t(255);
+  }
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -933;
+}
+
+long long Engine::phaseTimings(double* ms3, long long* elems) {
+  for (int k = 0; k < 3; ++k) ms3[k] = phaseMs_[k];
+  if (elems) *elems = phaseElems_;
+  return phaseSamples_;
+}
+
+void Engine::resetPhaseTimings() {
+  phaseMs_[0] = phaseMs_[1] = phaseMs_[2] = 0.0;
+  phaseSamples_ = phaseElems_ = 0;
+}
+
+void Engine::enqueueFactor(cudaStream_t s) {
+  for (const LevelPlan& lv : levels_) launchFactorLevel(d_, lv, opt_.fp32Factor, s);
+}
+
+void Engine::enqueueSolve(cudaStream_t s) {
+  const bool f32 = opt_.fp32Factor;
+  for (int sweep = 0; sweep < opt_.refineSweeps; ++sweep) {
+    if (sweep > 0) launchRefineResidual(d_, s);
+    launchSolveSetup(d_, f32, sweep, s);
+    for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
+    for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);
+    launchSolveAccumulate(d_, f32, s);
+  }
+  if (f32) launchSolveFinalize(d_, s);
+}
+
+void Engine::enqueueIteration(cudaStream_t s) {
+  cudaMemsetAsync(dActive_, 0, sizeof(int), s);
+  cudaMemsetAsync(dActiveEl_, 0, sizeof(long long), s);
+  launchBeginStep(d_, dActive_, dActiveEl_, s);
+  launchPredictDofs(d_, s);
+  launchElements(d_, EM_PRED, s);
+  launchResidual(d_, s);
+  launchBuildElementNewton(d_, s);
+  launchRotateElementNewton(d_, s);
+  launchCsrGather(d_, s);
+  cudaEventRecordWithFlags(ev_[0], s, cudaEventRecordExternal);
+  enqueueFactor(s);
+  cudaEventRecordWithFlags(ev_[1], s, cudaEventRecordExternal);
+  enqueueSolve(s);
+  cudaEventRecordWithFlags(ev_[2], s, cudaEventRecordExternal);
+  launchIncrement(d_, s);
+  cudaEventRecordWithFlags(ev_[3], s, cudaEventRecordExternal);
+  launchElements(d_, EM_INC, s);
+  cudaEventRecordWithFlags(ev_[4], s, cudaEventRecordExternal);
+  launchNormsControl(d_, s);
+  const int nl = (int)levels_.size(), sw = opt_.refineSweeps;
+  // kernels per batched iteration: 10 fixed + factor levels + per sweep (setup, accumulate,
+  // forward and backward levels) + refinement residuals + mixed-precision finalise
+  launchesPerIter_ = 10 + nl + sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
+}
+
+int Engine::readActive() {
+  cudaMemcpyAsync(hActive_, dActive_, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return *hActive_;
+}
+
+int Engine::initialState(std::string& err) {
+  // staticEquilibriumModule.f90:50-437: iterate the models that asked for it
+  launchStaticBegin(d_, dActive_, stream_);
+  launchElements(d_, EM_STATIC_INIT, stream_);
+  launchBuildElementNewton(d_, stream_);
+  for (int guard = 0; guard < 100000; ++guard) {
+    cudaMemsetAsync(dActive_, 0, sizeof(int), stream_);
+    launchStaticBegin(d_, dActive_, stream_);
+    if (readActive() == 0) break;
+    launchStaticResidual(d_, stream_);
+    launchBuildElementNewton(d_, stream_);
+    launchRotateElementNewton(d_, stream_);
+    launchCsrGather(d_, stream_);
+    enqueueFactor(stream_);
+    enqueueSolve(stream_);
+    launchStaticNorm(d_, stream_);
+    launchStaticIncrement(d_, stream_);
+    launchElements(d_, EM_STATIC, stream_);
+    launchStaticFinish(d_, stream_);
+  }
+  // finalStaticUpdate: zero velocities, corotated update and forces of every model
+  cudaMemsetAsync(d_.m.flags, 0, sizeof(int) * d_.m.n, stream_);
+  launchElements(d_, EM_FINAL, stream_);
+  FG_CHECK(cudaMemcpyAsync(d_.finitPrev, d_.finit, sizeof(double) * 12 * (size_t)d_.nelTot,
+                           cudaMemcpyDeviceToDevice, stream_));
+  FG_CHECK(cudaMemsetAsync(d_.rinc, 0, sizeof(double) * (size_t)d_.ndofTot, stream_));
+  FG_CHECK(cudaStreamSynchronize(stream_));
+  FG_CHECK(cudaGetLastError());
+  for (int k = 0; k < d_.m.n; ++k)
+    if (modelState(k) == ST_ERROR) { err = "initial static equilibrium failed"; return -910; }
+  return 0;
+}
+
+int Engine::run(long long maxBatched, RunStats* stats) {
+  if (opt_.useGraph && !graphExec_) {
+    cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+    enqueueIteration(stream_);
+    if (cudaStreamEndCapture(stream_, &graph_) != cudaSuccess) return -920;
+    if (cudaGraphInstantiate(&graphExec_, graph_, 0) != cudaSuccess) return -921;
+  }
+  if (!evRun_[0]) {
+    cudaEventCreate(&evRun_[0]);
+    cudaEventCreate(&evRun_[1]);
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  cudaEventRecord(evRun_[0], stream_);
+  long long done = 0;
+  const int chunk = 8;
+  while (done < maxBatched) {
+    int n = (int)std::min<long long>(chunk, maxBatched - done);
+    for (int k = 0; k < n; ++k) {
+      if (opt_.useGraph) cudaGraphLaunch(graphExec_, stream_);
+      else enqueueIteration(stream_);
+    }
+    done += n;
+    cudaMemcpyAsync(hActiveEl_, dActiveEl_, sizeof(long long), cudaMemcpyDeviceToHost, stream_);
+    int active = readActive();
+    // sample the phase durations of the last iteration of this chunk
+    float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+    if (cudaEventElapsedTime(&t0, ev_[3], ev_[4]) == cudaSuccess &&
+        cudaEventElapsedTime(&t1, ev_[0], ev_[1]) == cudaSuccess &&
+        cudaEventElapsedTime(&t2, ev_[1], ev_[2]) == cudaSuccess && *hActiveEl_ > 0) {
+      phaseMs_[0] += t0;
+      phaseMs_[1] += t1;
+      phaseMs_[2] += t2;
+      phaseElems_ += *hActiveEl_;
+      ++phaseSamples_;
+    }
+    if (active == 0) break;
+  }
+  cudaEventRecord(evRun_[1], stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -922;
+  if (cudaGetLastError() != cudaSuccess) return -923;
+  lastRunSec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  float devMs = 0.f;
+  cudaEventElapsedTime(&devMs, evRun_[0], evRun_[1]);
+  lastRunDevSec_ = 1.0e-3 * devMs;
+  if (stats) {
+    std::vector<long long> it(d_.m.n), st(d_.m.n);
+    std::vector<int> state(d_.m.n);
+    cudaMemcpy(it.data(), d_.m.nIter, sizeof(long long) * d_.m.n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(st.data(), d_.m.nStep, sizeof(long long) * d_.m.n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(state.data(), d_.m.state, sizeof(int) * d_.m.n, cudaMemcpyDeviceToHost);
+    stats->newtonIterations = 0;
+    stats->timeSteps = 0;
+    stats->modelsDone = stats->modelsFailed = 0;
+    for (int k = 0; k < d_.m.n; ++k) {
+      stats->newtonIterations += it[k];
+      stats->timeSteps += st[k];
+      stats->modelsDone += state[k] == ST_DONE;
+      stats->modelsFailed += state[k] == ST_ERROR;
+    }
+    stats->batchedIterations += done;
+  }
+  return 0;
+}
+
+void Engine::setStepLimit(long long lim) {
+  std::vector<long long> v(d_.m.n, lim);
+  cudaMemcpyAsync(d_.m.stepLimit, v.data(), sizeof(long long) * v.size(), cudaMemcpyHostToDevice, stream_);
+  cudaStreamSynchronize(stream_);
+}
+
+int Engine::advanceOneStep(int m, int* state) {
+  long long s0 = modelSteps(m);
+  std::vector<long long> lim(d_.m.n, 0);
+  lim[m] = s0 + 1;
+  cudaMemcpyAsync(d_.m.stepLimit, lim.data(), sizeof(long long) * lim.size(), cudaMemcpyHostToDevice, stream_);
+  int rc = run(1000000, nullptr);
+  if (state) *state = modelState(m);
+  return rc;
+}
+
+namespace {
+template <typename T>
+T readOne(const T* p, cudaStream_t s) {
+  T v{};
+  cudaMemcpyAsync(&v, p, sizeof(T), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  return v;
+}
+}  // namespace
+
+int Engine::modelState(int m) { return readOne(d_.m.state + m, stream_); }
+int Engine::modelStatus(int m) { return readOne(d_.m.status + m, stream_); }
+double Engine::modelTime(int m) { return readOne(d_.m.time + m, stream_); }
+long long Engine::modelSteps(int m) { return readOne(d_.m.nStep + m, stream_); }
+long long Engine::modelIterations(int m) { return readOne(d_.m.nIter + m, stream_); }
+
+int Engine::getTriadUr(int m, double* ur) {
+  int n = hm_[m]->ntri;
+  cudaMemcpyAsync(ur, d_.ur + 12 * (size_t)modelTriOff_[m], sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return n;
+}
+
+int Engine::getNorms(int m, double* n18) {
+  cudaMemcpyAsync(n18, d_.m.normVal + 18 * m, sizeof(double) * 18, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return 18;
+}
+
+int Engine::getCsrValues(int m, double* vals) {
+  size_t n = hm_[m]->colInd.size();
+  cudaMemcpyAsync(vals, d_.csrVal + modelSlotOff_[m], sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return (int)n;
+}
+
+int Engine::getEqVector(int m, int which, double* v) {
+  const double* src = which == 0 ? d_.FSk : which == 1 ? d_.FDk : which == 2 ? d_.FIk : which == 3 ? d_.Qk
+                      : which == 4 ? d_.res : d_.del;
+  int n = hm_[m]->neq;
+  cudaMemcpyAsync(v, src + modelEqOff_[m], sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return n;
+}
+
+}  // namespace fgpu

@@ -1,0 +1,111 @@
+// engine.h -- the batched GB300 Newton engine: many FEDEM models resident in
+// HBM, advanced one Newton iteration per model per batched iteration.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "engine_dev.cuh"
+#include "host_model.h"
+#include "kernels.h"
+
+namespace fgpu {
+
+struct EngineOptions {
+  bool fp32Factor = false;  // mixed precision: FP32 fronts + FP64 iterative refinement
+  int refineSweeps = 3;     // solves per Newton iteration in mixed precision (1 + refinements)
+  bool useGraph = true;     // capture the batched iteration in a CUDA graph
+};
+
+struct RunStats {
+  long long newtonIterations = 0;  // sum over models of Newton iterations performed
+  long long timeSteps = 0;         // sum over models of completed time steps
+  long long batchedIterations = 0;
+  int modelsDone = 0, modelsFailed = 0;
+};
+
+class Engine {
+ public:
+  Engine() = default;
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  // Uploads the models (host arrays -> HBM) and prepares the level schedule.
+  int upload(const std::vector<const HostModel*>& models, const EngineOptions& opt, std::string& err);
+  // Initial static equilibrium (when requested) and the final static update.
+  int initialState(std::string& err);
+  // Runs batched iterations until no model is active or maxBatched is reached.
+  int run(long long maxBatched, RunStats* stats);
+  // Advances model `m` by exactly one time step (other models may advance too).
+  int advanceOneStep(int m, int* state);
+
+  // accessors (blocking device -> host copies)
+  int numModels() const { return (int)hm_.size(); }
+  int modelState(int m);
+  int modelStatus(int m);
+  double modelTime(int m);
+  long long modelSteps(int m);
+  long long modelIterations(int m);
+  int getTriadUr(int m, double* ur);  // 12 per triad of the model
+  int getNorms(int m, double* norms18);
+  int getCsrValues(int m, double* vals);  // full symmetric CSR values of the last tangent
+  int getEqVector(int m, int which, double* v);  // 0 FS, 1 FD, 2 FI, 3 Q, 4 residual, 5 del
+  const HostModel& host(int m) const { return *hm_[m]; }
+  cudaStream_t stream() const { return stream_; }
+  // Device counters for the launch count claim: kernels enqueued per batched iteration.
+  int launchesPerIteration() const { return launchesPerIter_; }
+  double lastRunSeconds() const { return lastRunSec_; }
+  double lastRunDeviceSeconds() const { return lastRunDevSec_; }  // CUDA events on the engine stream
+  long long uploadedBytes() const { return uploadedBytes_; }
+  void setStepLimit(long long lim);
+  // Saves / restores the mutable device state (device-to-device copies), so a
+  // timed run can start again from the initial state already resident in HBM.
+  int snapshot();
+  int restore();
+  // Phase timings sampled with CUDA events inside the captured iteration:
+  // phase 0 = element pass after the increment, 1 = factorisation, 2 = solve.
+  // Returns samples; ms[3] = summed milliseconds, elems = summed active elements.
+  long long phaseTimings(double* ms3, long long* activeElems);
+  void resetPhaseTimings();
+
+ private:
+  template <typename T>
+  T* alloc(size_t n);
+  void enqueueIteration(cudaStream_t s);
+  void enqueueSolve(cudaStream_t s);
+  void enqueueFactor(cudaStream_t s);
+  int readActive();
+
+  std::vector<const HostModel*> hm_;
+  EngineOptions opt_;
+  DevData d_{};
+  std::vector<void*> allocs_;
+  std::vector<LevelPlan> levels_;
+  int* dActive_ = nullptr;
+  int* hActive_ = nullptr;  // pinned
+  cudaStream_t stream_ = nullptr;
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graphExec_ = nullptr;
+  std::vector<int> modelTriOff_, modelDofOff_, modelEqOff_, modelElOff_;
+  std::vector<int64_t> modelSlotOff_;
+  int launchesPerIter_ = 0;
+  double lastRunSec_ = 0.0;
+  bool allocFailed_ = false;
+  // snapshot of mutable arrays: (device pointer, bytes) and the backup buffer
+  std::vector<std::pair<void*, size_t>> mutable_;
+  char* backup_ = nullptr;
+  // phase timing events (recorded as external event nodes inside the graph)
+  cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  long long* dActiveEl_ = nullptr;
+  long long* hActiveEl_ = nullptr;
+  cudaEvent_t evRun_[2] = {nullptr, nullptr};
+  double lastRunDevSec_ = 0.0;
+  long long uploadedBytes_ = 0;
+  double phaseMs_[3] = {0, 0, 0};
+  long long phaseSamples_ = 0, phaseElems_ = 0;
+};
+
+}  // namespace fgpu

@@ -1,0 +1,684 @@
+// host_model.cpp -- reading a FEDEM solver input (.fsi subset) and the
+// solver options, and building the flat model arrays the GPU engine uploads.
+//
+// Reference behaviour restated here (paths relative to fedem-solvers):
+//   namelist records   src/vpmCommon/triadTypeModule.f90:1264, supElTypeModule.f90:1301-1365,
+//                      src/vpmSolver/finiteElementModule.f90:151-205, forceTypeModule.f90:157-260
+//   options/defaults   src/vpmSolver/solverInterface.C:195-554
+//   Newmark constants  src/vpmSolver/initiateSystemTypeModule.f90:74-92
+//   beam matrices      src/vpmSolver/finiteElementModule.f90:283-541 -> src/Femlib/beam.f
+//                      (BEAM31 :11, BELS31 :619, BEAM35 :396), src/Femlib/beamaux.f
+//   offsets/corot init src/vpmSolver/initiateSupElTypeModule.f90:354-371, supElTypeModule.f90:779-992
+//   SAM numbering      src/vpmSolver/samSolverModule.f90:95-250 (triads in input order, MSC = BC)
+//   damping/scaling    src/vpmSolver/initiateSupElTypeModule.f90:549-599, :785-811
+
+#include "host_model.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+
+namespace fgpu {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Namelist text -> records of key -> raw value tokens
+// ---------------------------------------------------------------------------
+struct NmlRecord {
+  std::string name;
+  std::map<std::string, std::vector<std::string>> vals;
+};
+
+std::string lowerCase(const std::string& s) {
+  std::string r(s);
+  std::transform(r.begin(), r.end(), r.begin(), [](unsigned char c) { return (char)std::tolower(c); });
+  return r;
+}
+
+double toDouble(const std::string& tok) {
+  std::string t(tok);
+  for (char& c : t)
+    if (c == 'd' || c == 'D') c = 'e';
+  return std::strtod(t.c_str(), nullptr);
+}
+
+std::vector<NmlRecord> readNamelists(const char* text) {
+  std::vector<NmlRecord> out;
+  const size_t n = std::strlen(text);
+  size_t p = 0;
+  while (p < n) {
+    while (p < n && text[p] != '&') ++p;
+    if (p >= n) break;
+    size_t q = ++p;
+    while (q < n && (std::isalnum((unsigned char)text[q]) || text[q] == '_')) ++q;
+    NmlRecord rec;
+    rec.name = lowerCase(std::string(text + p, q - p));
+    p = q;
+    struct Tok { std::string s; char kind; };  // 'w' word, '=' assign, 's' string
+    std::vector<Tok> toks;
+    while (p < n) {
+      char c = text[p];
+      if (c == '/') { ++p; break; }
+      if (std::isspace((unsigned char)c) || c == ',') { ++p; continue; }
+      if (c == '!') { while (p < n && text[p] != '\n') ++p; continue; }
+      if (c == '=') { toks.push_back({"=", '='}); ++p; continue; }
+      if (c == '\'' || c == '"') {
+        size_t s0 = ++p;
+        while (p < n && text[p] != c) ++p;
+        toks.push_back({std::string(text + s0, p - s0), 's'});
+        if (p < n) ++p;
+        continue;
+      }
+      size_t s0 = p;
+      while (p < n && !std::isspace((unsigned char)text[p]) && text[p] != ',' && text[p] != '=' &&
+             text[p] != '/' && text[p] != '\'' && text[p] != '"')
+        ++p;
+      toks.push_back({std::string(text + s0, p - s0), 'w'});
+    }
+    std::string key;
+    for (size_t k = 0; k < toks.size(); ++k) {
+      if (toks[k].kind == 'w' && k + 1 < toks.size() && toks[k + 1].kind == '=') {
+        key = lowerCase(toks[k].s);
+        rec.vals[key];
+        ++k;
+      } else if (!key.empty()) {
+        const std::string& s = toks[k].s;
+        size_t star = toks[k].kind == 'w' ? s.find('*') : std::string::npos;
+        if (star != std::string::npos && star > 0) {
+          int rep = std::atoi(s.substr(0, star).c_str());
+          for (int r = 0; r < rep; ++r) rec.vals[key].push_back(s.substr(star + 1));
+        } else {
+          rec.vals[key].push_back(s);
+        }
+      }
+    }
+    out.push_back(std::move(rec));
+  }
+  return out;
+}
+
+struct Rec {
+  const NmlRecord& r;
+  std::vector<double> nums(const char* k) const {
+    std::vector<double> v;
+    auto it = r.vals.find(k);
+    if (it != r.vals.end())
+      for (const auto& s : it->second) v.push_back(toDouble(s));
+    return v;
+  }
+  double num(const char* k, double def) const {
+    auto v = nums(k);
+    return v.empty() ? def : v[0];
+  }
+  int inum(const char* k, int def) const { return (int)std::lround(num(k, (double)def)); }
+};
+
+// ---------------------------------------------------------------------------
+// Options: -name=value, -name, -name-, -name+
+// ---------------------------------------------------------------------------
+struct Opts {
+  std::map<std::string, std::string> kv;
+  explicit Opts(int argc, const char* const* argv) {
+    for (int a = 0; a < argc; ++a) {
+      if (!argv || !argv[a] || argv[a][0] != '-') continue;
+      std::string s(argv[a] + 1), key, val = "true";
+      size_t eq = s.find('=');
+      if (eq != std::string::npos) {
+        key = s.substr(0, eq);
+        val = s.substr(eq + 1);
+        if (val.size() >= 2 && (val[0] == '"' || val[0] == '\'') && val.back() == val[0])
+          val = val.substr(1, val.size() - 2);
+      } else if (!s.empty() && (s.back() == '-' || s.back() == '+')) {
+        val = s.back() == '-' ? "false" : "true";
+        key = s.substr(0, s.size() - 1);
+      } else {
+        key = s;
+      }
+      kv[lowerCase(key)] = val;
+    }
+  }
+  double d(const char* k, double def) const {
+    auto it = kv.find(lowerCase(k));
+    return it == kv.end() ? def : toDouble(it->second);
+  }
+  int i(const char* k, int def) const { return (int)std::lround(d(k, (double)def)); }
+  bool b(const char* k, bool def) const {
+    auto it = kv.find(lowerCase(k));
+    if (it == kv.end()) return def;
+    std::string v = lowerCase(it->second);
+    return v == "true" || v == "1" || v == "t" || v == "yes" || v == "on";
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Small dense helpers. P34 is a 3x4 position matrix, column-major (12 doubles).
+// ---------------------------------------------------------------------------
+inline double& at34(double* T, int r, int c) { return T[r + 3 * c]; }
+inline double at34(const double* T, int r, int c) { return T[r + 3 * c]; }
+
+void compose34(const double* a, const double* b, double* out) {  // a o b
+  double r[12];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double s = at34(a, i, 0) * at34(b, 0, j) + at34(a, i, 1) * at34(b, 1, j) + at34(a, i, 2) * at34(b, 2, j);
+      if (j == 3) s += at34(a, i, 3);
+      r[i + 3 * j] = s;
+    }
+  std::memcpy(out, r, sizeof(r));
+}
+
+void inverse34(const double* a, double* out) {
+  double r[12];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r[i + 3 * j] = at34(a, j, i);
+  for (int i = 0; i < 3; ++i)
+    r[i + 9] = -(r[i] * a[9] + r[i + 3] * a[10] + r[i + 6] * a[11]);
+  std::memcpy(out, r, sizeof(r));
+}
+
+void crossp(const double* a, const double* b, double* c) {
+  double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+  c[0] = x; c[1] = y; c[2] = z;
+}
+
+// Frame through three points: x along p1->p2, z normal to the plane, origin p1.
+int frameFrom3Points(const double* p1, const double* p2, const double* p3, double* T) {
+  double ex[3], v2[3], ez[3], ey[3];
+  for (int k = 0; k < 3; ++k) { ex[k] = p2[k] - p1[k]; v2[k] = p3[k] - p1[k]; }
+  crossp(ex, v2, ez);
+  double lx = ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2];
+  if (!(lx > 1.0e-16)) return -1;
+  lx = std::sqrt(lx);
+  for (double& v : ex) v /= lx;
+  double lz = ez[0] * ez[0] + ez[1] * ez[1] + ez[2] * ez[2];
+  if (!(lz > 1.0e-16)) return -2;
+  lz = std::sqrt(lz);
+  for (double& v : ez) v /= lz;
+  crossp(ez, ex, ey);
+  for (int k = 0; k < 3; ++k) { T[k] = ex[k]; T[3 + k] = ey[k]; T[6 + k] = ez[k]; T[9 + k] = p1[k]; }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// 12-DOF beam element matrices in superelement axes (Femlib BEAM31/BEAM35).
+// E is column-major; e(i,j) uses 1-based indices like the element library.
+// ---------------------------------------------------------------------------
+struct Mat12 {
+  double* a;
+  double& operator()(int i, int j) const { return a[(i - 1) + 12 * (j - 1)]; }
+};
+
+// Rows of G are the local unit axes in superelement coordinates (DCOS30).
+void localAxes(const double* X1, const double* X2, const double* X3, double G[3][3]) {
+  double d[3] = {X2[0] - X1[0], X2[1] - X1[1], X2[2] - X1[2]};
+  double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  for (int k = 0; k < 3; ++k) G[0][k] = d[k] / l;
+  double w[3] = {X3[0] - X1[0], X3[1] - X1[1], X3[2] - X1[2]};
+  double y[3] = {G[0][2] * w[1] - G[0][1] * w[2], G[0][0] * w[2] - G[0][2] * w[0], G[0][1] * w[0] - G[0][0] * w[1]};
+  l = std::sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+  for (int k = 0; k < 3; ++k) G[1][k] = y[k] / l;
+  double z[3] = {G[0][1] * G[1][2] - G[0][2] * G[1][1], G[0][2] * G[1][0] - G[0][0] * G[1][2],
+                 G[0][0] * G[1][1] - G[0][1] * G[1][0]};
+  l = std::sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+  for (int k = 0; k < 3; ++k) G[2][k] = z[k] / l;
+}
+
+// E := blockdiag(G)^T E blockdiag(G), 3x3 blocks, then symmetrised from the lower part.
+void congruence(double* E, const double G[3][3]) {
+  Mat12 e{E};
+  for (int bi = 0; bi < 12; bi += 3)
+    for (int bj = 0; bj < 12; bj += 3) {
+      double B[3][3] = {{0.0}};
+      for (int ia = 1; ia <= 3; ++ia)
+        for (int ka = 1; ka <= 3; ++ka)
+          for (int ja = 1; ja <= 3; ++ja) B[ja - 1][ia - 1] += G[ka - 1][ja - 1] * e(bj + ka, bi + ia);
+      for (int ia = 1; ia <= 3; ++ia)
+        for (int ka = 1; ka <= 3; ++ka) {
+          double s = 0.0;
+          for (int ja = 1; ja <= 3; ++ja) s += B[ka - 1][ja - 1] * G[ja - 1][ia - 1];
+          e(bj + ka, bi + ia) = s;
+        }
+    }
+  for (int i = 1; i <= 12; ++i)
+    for (int j = i; j <= 12; ++j) e(i, j) = e(j, i);
+}
+
+// Move the element ends to eccentric nodes (TRIX30); zero eccentricity is a no-op
+// apart from exact zero additions, kept for bitwise agreement with the library.
+void eccentricNodes(double* E, const double* e1, const double* e2) {
+  Mat12 a{E};
+  for (int i = 1; i <= 12; ++i) {
+    a(4, i) += e1[2] * a(2, i) - e1[1] * a(3, i);
+    a(5, i) += -e1[2] * a(1, i) + e1[0] * a(3, i);
+    a(6, i) += e1[1] * a(1, i) - e1[0] * a(2, i);
+    a(10, i) += e2[2] * a(8, i) - e2[1] * a(9, i);
+    a(11, i) += -e2[2] * a(7, i) + e2[0] * a(9, i);
+    a(12, i) += e2[1] * a(7, i) - e2[0] * a(8, i);
+  }
+  for (int i = 1; i <= 12; ++i) {
+    a(i, 4) += e1[2] * a(i, 2) - e1[1] * a(i, 3);
+    a(i, 5) += -e1[2] * a(i, 1) + e1[0] * a(i, 3);
+    a(i, 6) += e1[1] * a(i, 1) - e1[0] * a(i, 2);
+    a(i, 10) += e2[2] * a(i, 8) - e2[1] * a(i, 9);
+    a(i, 11) += -e2[2] * a(i, 7) + e2[0] * a(i, 9);
+    a(i, 12) += e2[1] * a(i, 7) - e2[0] * a(i, 8);
+  }
+}
+
+// Timoshenko beam stiffness, local axes (BELS31): EP = E,G,A,Iy,Iz,It.
+void beamStiffnessLocal(double* E, double L, const double* EP, const double* CA, const double* XS) {
+  double EA, EIy, EIz, GIt, phiY, phiZ;
+  if (EP[0] < -1.0e-16) {  // generic section data: EA, EI, GAs, GIt given directly
+    EA = EP[2]; EIy = EP[3]; EIz = EP[4]; GIt = EP[5];
+    phiY = CA[0] > 1.0e-16 ? 12.0 * EIy / (CA[0] * L * L) : 0.0;
+    phiZ = CA[1] > 1.0e-16 ? 12.0 * EIz / (CA[1] * L * L) : 0.0;
+  } else {
+    EA = EP[0] * EP[2]; EIy = EP[0] * EP[3]; EIz = EP[0] * EP[4]; GIt = EP[1] * EP[5];
+    phiY = 12.0 * CA[0] * EIy / (EP[2] * EP[1] * L * L);
+    phiZ = 12.0 * CA[1] * EIz / (EP[2] * EP[1] * L * L);
+  }
+  std::fill(E, E + 144, 0.0);
+  Mat12 k{E};
+  k(1, 1) = EA / L;
+  k(2, 2) = 12. * EIy / (L * L * L * (1. + phiY));
+  k(3, 3) = 12. * EIz / (L * L * L * (1. + phiZ));
+  k(4, 4) = GIt / L;
+  k(3, 5) = -.5 * L * k(3, 3);
+  k(2, 6) = .5 * L * k(2, 2);
+  k(5, 5) = EIz * (4. + phiZ) / (L * (1. + phiZ));
+  k(6, 6) = EIy * (4. + phiY) / (L * (1. + phiY));
+  k(1, 7) = -k(1, 1);
+  k(7, 7) = k(1, 1);
+  k(2, 8) = -k(2, 2);
+  k(6, 8) = -k(2, 6);
+  k(8, 8) = k(2, 2);
+  k(3, 9) = -k(3, 3);
+  k(5, 9) = -k(3, 5);
+  k(9, 9) = k(3, 3);
+  k(4, 10) = -k(4, 4);
+  k(10, 10) = k(4, 4);
+  k(3, 11) = k(3, 5);
+  k(5, 11) = EIz * (2. - phiZ) / (L * (1. + phiZ));
+  k(9, 11) = -k(3, 5);
+  k(11, 11) = k(5, 5);
+  k(2, 12) = k(2, 6);
+  k(6, 12) = EIy * (2. - phiY) / (L * (1. + phiY));
+  k(8, 12) = -k(2, 6);
+  k(12, 12) = k(6, 6);
+  for (int i = 1; i <= 12; ++i)
+    for (int j = 1; j < i; ++j) k(i, j) = k(j, i);
+  if (.00001 * std::sqrt(EP[2]) < std::fabs(XS[0]) + std::fabs(XS[1])) {  // shear centre offset
+    double ys = XS[0], zs = XS[1];
+    for (int i = 1; i <= 12; ++i) {
+      k(4, i) = k(4, i) - zs * k(2, i) + ys * k(3, i);
+      k(10, i) = k(10, i) - zs * k(8, i) + ys * k(9, i);
+    }
+    for (int i = 1; i <= 12; ++i) {
+      k(i, 4) = k(i, 4) - k(i, 2) * zs + k(i, 3) * ys;
+      k(i, 10) = k(i, 10) - k(i, 8) * zs + k(i, 9) * ys;
+    }
+  }
+}
+
+// Consistent mass, local axes (BEAM35, IOP = 3).
+void beamMassLocal(double* E, double L, double A, double rho, double Ix) {
+  std::fill(E, E + 144, 0.0);
+  Mat12 m{E};
+  double am = L * A * rho, am2 = L * am, am3 = L * am2, rm = Ix * rho;
+  m(1, 1) = am / 3.;
+  m(1, 7) = am / 6.;
+  m(2, 2) = 13. * am / 35.;
+  m(2, 6) = 11. * am2 / 210.;
+  m(2, 8) = 9. * am / 70.;
+  m(2, 12) = -13. * am2 / 420.;
+  m(3, 3) = m(2, 2);
+  m(3, 5) = -m(2, 6);
+  m(3, 9) = m(2, 8);
+  m(3, 11) = -m(2, 12);
+  m(4, 4) = L * rm / 3.;
+  m(4, 10) = L * rm / 6.;
+  m(5, 5) = am3 / 105.;
+  m(5, 9) = m(2, 12);
+  m(5, 11) = -am3 / 140.;
+  m(6, 6) = m(5, 5);
+  m(6, 8) = m(3, 11);
+  m(6, 12) = m(5, 11);
+  m(7, 7) = m(1, 1);
+  m(8, 8) = m(2, 2);
+  m(8, 12) = m(3, 5);
+  m(9, 9) = m(8, 8);
+  m(9, 11) = m(2, 6);
+  m(10, 10) = m(4, 4);
+  m(11, 11) = m(5, 5);
+  m(12, 12) = m(6, 6);
+  for (int i = 1; i <= 12; ++i)
+    for (int j = i; j <= 12; ++j) m(j, i) = m(i, j);
+}
+
+struct Prop { int id; double geo[8]; double mat[4]; double zvec[3]; };
+
+int beamMatrices(const Prop& p, const double* und1, const double* und2, double* K, double* M, double* fg,
+                 std::string& err) {
+  // node positions in superelement axes; no eccentricity (ends at the nodes)
+  double X1[3] = {und1[9], und1[10], und1[11]}, X2[3] = {und2[9], und2[10], und2[11]}, X3[3];
+  bool hasZ = std::fabs(p.zvec[0]) > 1e-16 || std::fabs(p.zvec[1]) > 1e-16 || std::fabs(p.zvec[2]) > 1e-16;
+  if (hasZ) {
+    for (int k = 0; k < 3; ++k) X3[k] = X1[k] + p.zvec[k];
+  } else {
+    // local Z from the default orientation of the beam axis (trans1V)
+    double v[3] = {X2[0] - X1[0], X2[1] - X1[1], X2[2] - X1[2]};
+    double s2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    if (!(std::fabs(s2) > 1e-16)) { err = "degenerated beam element (zero length)"; return -1; }
+    double s = std::sqrt(s2), t1[3] = {v[0] / s, v[1] / s, v[2] / s}, t2[3], t3[3];
+    if (std::fabs(t1[2]) > std::fabs(t1[1])) {
+      t2[0] = -t1[1] * t1[0]; t2[1] = t1[0] * t1[0] + t1[2] * t1[2]; t2[2] = -t1[1] * t1[2];
+      double l = std::sqrt(t2[0] * t2[0] + t2[1] * t2[1] + t2[2] * t2[2]);
+      for (double& q : t2) q /= l;
+      crossp(t1, t2, t3);
+    } else {
+      t3[0] = -t1[2] * t1[0]; t3[1] = -t1[2] * t1[1]; t3[2] = t1[0] * t1[0] + t1[1] * t1[1];
+      double l = std::sqrt(t3[0] * t3[0] + t3[1] * t3[1] + t3[2] * t3[2]);
+      for (double& q : t3) q /= l;
+    }
+    for (int k = 0; k < 3; ++k) X3[k] = X1[k] + t3[k];
+  }
+  double dx = X2[0] - X1[0], dy = X2[1] - X1[1], dz = X2[2] - X1[2];
+  double L = std::sqrt(dx * dx + dy * dy + dz * dz);
+  double tolL = 1.0e-6 * (std::fabs(X1[0]) + std::fabs(X2[0]) + std::fabs(X1[1]) + std::fabs(X2[1]) +
+                          std::fabs(X1[2]) + std::fabs(X2[2]));
+  if (L - tolL <= 0.0) { err = "degenerated beam element"; return -1; }
+  double EP[6] = {p.mat[1], p.mat[2], p.geo[0], p.geo[1], p.geo[2], p.geo[3]};
+  double CA[2] = {p.geo[4], p.geo[5]}, XS[2] = {p.geo[6], p.geo[7]};
+  if (EP[1] <= 1.0e-16 || EP[2] <= 1.0e-16) { err = "invalid beam property parameters"; return -3; }
+  double G[3][3];
+  localAxes(X1, X2, X3, G);
+  const double zero[3] = {0.0, 0.0, 0.0};
+  beamStiffnessLocal(K, L, EP, CA, XS);
+  congruence(K, G);
+  eccentricNodes(K, zero, zero);
+  double rho = p.mat[0], Ix = p.geo[1] + p.geo[2];
+  if (Ix <= 0.0) Ix = p.geo[3];
+  double area = EP[2], rix = Ix;
+  if (EP[0] <= 1.0e-16 && rho > 1.0e-16) { area = 1.0; rix = Ix / rho; }
+  beamMassLocal(M, L, area, rho, rix);
+  congruence(M, G);
+  eccentricNodes(M, zero, zero);
+  for (int i = 0; i < 12; ++i)
+    for (int c = 0; c < 3; ++c) fg[i + 12 * c] = M[i + 12 * c] + M[i + 12 * (c + 6)];
+  return 0;
+}
+
+void setTol(const Opts& o, const char* key, Control& c, int idx) {
+  double v = o.d(key, 0.0);
+  c.tolCode[idx] = v > 0.0 ? 1 : v < 0.0 ? 2 : 0;
+  c.tolVal[idx] = std::fabs(v);
+}
+
+}  // namespace
+
+int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m, std::string& err) {
+  if (!fsi) { err = "no model text"; return -1; }
+  Opts o(argc, argv);
+  Control& c = m.ctl;
+  double a = o.d("alphaNewmark", 0.1);
+  a = std::min(std::max(a, 0.0), 1.0 / 3.0);
+  c.alpha = -a;
+  c.beta = (1.0 - c.alpha) * (1.0 - c.alpha) / 4.0;
+  c.gamma = 0.5 - c.alpha;
+  c.tStart = o.d("timeStart", 0.0);
+  c.tEnd = o.d("timeEnd", 0.0);
+  c.tInc = std::max(o.d("timeInc", 0.0), 1.0e-6);
+  c.minInc = o.d("minInc", 0.001);
+  c.maxIt = o.i("maxit", 15);
+  c.minIt = o.i("minit", 1);
+  c.fixedIt = o.i("numit", 0);
+  c.nUpdat = o.i("nupdat", 0);
+  c.maxSeqNoUpdate = o.i("maxSeqNoUpdate", 100);
+  c.stiffDampFiltering = o.i("stiffDampFiltering", 1);
+  c.initEquilibrium = o.b("initEquilibrium", false);
+  c.tolInitEquil = o.d("tolInitEquil", 1.0e-3);
+  c.limInitEquilStep = o.d("limInitEquilStep", 1.0);
+  c.tolFactorize = o.d("tolFactorize", 1.0e-12);
+  const char* tolKeys[18] = {"tolDispNorm", "tolDispTra", "tolDispRot", "tolDispGen", "tolVelNorm", "tolVelTra",
+                             "tolVelRot",   "tolVelGen",  "tolAccNorm", "tolAccTra",  "tolAccRot",  "tolAccGen",
+                             "tolResNorm",  "tolResTra",  "tolResRot",  "tolResGen",  "tolEnerMax", "tolEnerSum"};
+  for (int k = 0; k < 18; ++k) setTol(o, tolKeys[k], c, k);
+
+  std::vector<NmlRecord> recs = readNamelists(fsi);
+  std::vector<Prop> props;
+  std::map<int, int> triIndex;
+  // pass 1: mechanism, environment, triads, properties
+  for (const NmlRecord& nr : recs) {
+    Rec r{nr};
+    if (nr.name == "mechanism") {
+      c.wDisp[0] = r.num("weighttranslation", 1.0);
+      c.wDisp[1] = r.num("weightrotation", 1.0);
+      c.wDisp[2] = r.num("weightgeneralized", 1.0);
+    } else if (nr.name == "environment") {
+      auto g = r.nums("gravity");
+      for (size_t k = 0; k < 3 && k < g.size(); ++k) c.gravity[k] = g[k];
+    } else if (nr.name == "triad") {
+      int id = r.inum("id", 0);
+      triIndex[id] = m.ntri++;
+      m.triId.push_back(id);
+      m.triNdof.push_back(r.inum("ndofs", 6));
+      auto u = r.nums("ur");  // 3x4, row by row in the file
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 3; ++row) {
+          size_t k = (size_t)(4 * row + col);
+          m.ur.push_back(k < u.size() ? u[k] : 0.0);
+        }
+      auto bc = r.nums("bc");
+      for (int k = 0; k < 6; ++k) m.dofType.push_back(k < (int)bc.size() ? (int)std::lround(bc[k]) : 1);
+    } else if (nr.name == "element_property") {
+      Prop p{};
+      p.id = r.inum("id", 0);
+      auto g = r.nums("geometry");
+      for (size_t k = 0; k < 8 && k < g.size(); ++k) p.geo[k] = g[k];
+      auto mt = r.nums("material");
+      for (size_t k = 0; k < 4 && k < mt.size(); ++k) p.mat[k] = mt[k];
+      auto z = r.nums("orientation");
+      for (size_t k = 0; k < 3 && k < z.size(); ++k) p.zvec[k] = z[k];
+      props.push_back(p);
+    }
+  }
+  for (double w = 0; w < 3; ++w) {
+    int k = (int)w;
+    c.wForce[k] = c.wDisp[k] > 0.0 ? 1.0 / c.wDisp[k] : 0.0;
+  }
+  // SAM: DOFs per triad in input order; status code BC: 0 fixed, 1 free
+  std::vector<int> bcs = m.dofType;  // temporarily holds the BC codes, 6 per triad
+  m.dofType.clear();
+  m.triFirstDof.resize(m.ntri);
+  for (int t = 0; t < m.ntri; ++t) {
+    m.triFirstDof[t] = m.ndof;
+    for (int k = 0; k < m.triNdof[t]; ++k) {
+      int bc = bcs[6 * t + k];
+      if (bc != 0 && bc != 1) { err = "prescribed triad DOFs are not supported"; return -30; }
+      m.meqn.push_back(bc == 1 ? m.neq++ : -1);
+      m.dofType.push_back(k < 3 ? 1 : 2);
+    }
+    m.ndof += m.triNdof[t];
+  }
+  // pass 2: superelements, undeformed positions, loads
+  std::vector<int> elProp;
+  std::map<int, int> elIndex;
+  m.qext.assign(m.neq, 0.0);
+  for (const NmlRecord& nr : recs) {
+    Rec r{nr};
+    if (nr.name == "sup_el") {
+      auto tids = r.nums("triadids");
+      if (r.inum("numtriads", 2) != 2 || tids.size() < 2) { err = "only 2-noded beam superelements"; return -10; }
+      int e = m.nel++;
+      elIndex[r.inum("id", 0)] = e;
+      m.elId.push_back(r.inum("id", 0));
+      int tri[2];
+      for (int k = 0; k < 2; ++k) {
+        auto it = triIndex.find((int)std::lround(tids[k]));
+        if (it == triIndex.end()) { err = "superelement refers to unknown triad"; return -11; }
+        tri[k] = it->second;
+        if (m.triNdof[tri[k]] != 6) { err = "beam triads need 6 DOFs"; return -12; }
+        m.elTri.push_back(tri[k]);
+      }
+      const char* refKey[3] = {"reftriad1id", "reftriad2id", "reftriad3id"};
+      const char* offKey[3] = {"offset1", "offset2", "offset3"};
+      auto sp = r.nums("suppos");
+      double S[12];
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 3; ++row) {
+          size_t k = (size_t)(4 * row + col);
+          S[row + 3 * col] = k < sp.size() ? sp[k] : 0.0;
+        }
+      for (int j = 0; j < 3; ++j) {
+        int rid = r.inum(refKey[j], 0), node = -1;
+        for (int k = 0; k < 2; ++k)
+          if (m.triId[tri[k]] == rid) node = k;
+        if (node < 0) { err = "invalid reference triad"; return -13; }
+        m.elRef.push_back(node);
+        // offset expressed in the reference triad axes: ur^T * (supPos * offset)
+        auto ov = r.nums(offKey[j]);
+        double off[3] = {0, 0, 0}, so[3];
+        for (size_t k = 0; k < 3 && k < ov.size(); ++k) off[k] = ov[k];
+        for (int q = 0; q < 3; ++q) so[q] = S[q] * off[0] + S[q + 3] * off[1] + S[q + 6] * off[2];
+        const double* U = &m.ur[12 * tri[node]];
+        for (int col = 0; col < 3; ++col)
+          m.elOffset.push_back(so[0] * U[3 * col] + so[1] * U[3 * col + 1] + so[2] * U[3 * col + 2]);
+      }
+      for (double v : S) m.supTr.push_back(v);
+      double ss = r.num("stiffscale", 1.0), ms = r.num("massscale", 1.0);
+      double a1 = r.num("alpha1", 0.0), a2 = r.num("alpha2", 0.0);
+      m.stifScl.push_back(ss);  // temporarily: stiffness scale, replaced below
+      m.kDmp.push_back(a2);
+      m.C.push_back(ms);        // temporarily: mass scale
+      m.C.push_back(a1);        // temporarily: alpha1
+      int pid = r.inum("elpropid", 0), pidx = -1;
+      for (size_t k = 0; k < props.size(); ++k)
+        if (props[k].id == pid) pidx = (int)k;
+      if (pidx < 0) { err = "superelement refers to unknown element property"; return -14; }
+      elProp.push_back(pidx);
+      m.trUnd.resize(24 * (size_t)m.nel, 0.0);
+    } else if (nr.name == "triad_undpos") {
+      auto it = elIndex.find(r.inum("supelid", 0));
+      if (it == elIndex.end()) { err = "undeformed position for unknown superelement"; return -15; }
+      int e = it->second, tid = r.inum("triadid", 0), node = -1;
+      for (int k = 0; k < 2; ++k)
+        if (m.triId[m.elTri[2 * e + k]] == tid) node = k;
+      if (node < 0) { err = "undeformed position for unconnected triad"; return -16; }
+      auto u = r.nums("undposinsupelsystem");
+      // stored transposed in the rotation part (initiateSupElTypeModule.f90:312): file rows -> columns
+      double* T = &m.trUnd[24 * (size_t)e + 12 * node];
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 3; ++row) {
+          size_t k = (size_t)(4 * row + col);
+          T[row + 3 * col] = k < u.size() ? u[k] : 0.0;
+        }
+    } else if (nr.name == "load") {
+      auto it = triIndex.find(r.inum("triadid", 0));
+      if (it == triIndex.end()) { err = "load on unknown triad"; return -17; }
+      int dof = r.inum("ldof", 0);
+      if (dof < 1 || dof > m.triNdof[it->second]) { err = "load DOF must be 1..6"; return -18; }
+      int eq = m.meqn[m.triFirstDof[it->second] + dof - 1];
+      if (eq >= 0) m.qext[eq] += r.num("f0", 0.0);
+    }
+  }
+  // element matrices, damping, scaling, corotation initialisation
+  std::vector<double> tmpC = m.C;
+  m.K.assign(144 * (size_t)m.nel, 0.0);
+  m.M.assign(144 * (size_t)m.nel, 0.0);
+  m.C.assign(144 * (size_t)m.nel, 0.0);
+  m.fg.assign(36 * (size_t)m.nel, 0.0);
+  m.triRelSup.assign(12 * (size_t)m.nel, 0.0);
+  m.hasC.assign(m.nel, 0);
+  m.hasVld.assign(m.nel, 0);
+  for (int e = 0; e < m.nel; ++e) {
+    double* K = &m.K[144 * (size_t)e];
+    double* M = &m.M[144 * (size_t)e];
+    double* C = &m.C[144 * (size_t)e];
+    double* fg = &m.fg[36 * (size_t)e];
+    const double* und = &m.trUnd[24 * (size_t)e];
+    if (int rc = beamMatrices(props[elProp[e]], und, und + 12, K, M, fg, err)) return rc;
+    double ss = m.stifScl[e], ms = tmpC[2 * e], a1 = tmpC[2 * e + 1], a2 = m.kDmp[e];
+    bool damp = a1 > 0.0 || a2 > 0.0;
+    if (damp) {
+      for (int k = 0; k < 144; ++k) C[k] = a1 * M[k] + a2 * K[k];
+      m.hasC[e] = 1;
+    }
+    if (std::fabs(ss - 1.0) > 1.0e-16)
+      for (int k = 0; k < 144; ++k) K[k] *= ss;
+    if (std::fabs(ms - 1.0) > 1.0e-16) {
+      for (int k = 0; k < 144; ++k) M[k] *= ms;
+      for (int k = 0; k < 36; ++k) fg[k] *= ms;
+    }
+    if (damp && std::fabs(ss - 1.0) > 1.0e-16) a2 /= ss;
+    m.kDmp[e] = a2;
+    m.stifScl[e] = 1.0;
+    m.hasVld[e] = (a2 > 0.0 && c.stiffDampFiltering > 0) ? 1 : 0;
+    // triangle frame through the reference points (supElTypeModule.f90:912-950, stat = 1)
+    double pts[3][3];
+    for (int j = 0; j < 3; ++j) {
+      const double* U = &m.ur[12 * m.elTri[2 * e + m.elRef[3 * e + j]]];
+      const double* o = &m.elOffset[9 * (size_t)e + 3 * j];
+      for (int q = 0; q < 3; ++q) pts[j][q] = U[q] * o[0] + U[q + 3] * o[1] + U[q + 6] * o[2] + U[q + 9];
+    }
+    double tri[12], inv[12];
+    if (frameFrom3Points(pts[0], pts[1], pts[2], tri)) { err = "cannot build corotated frame"; return -22; }
+    inverse34(tri, inv);
+    compose34(inv, &m.supTr[12 * (size_t)e], &m.triRelSup[12 * (size_t)e]);
+  }
+  // element equation lists
+  m.elEq.resize(12 * (size_t)m.nel);
+  for (int e = 0; e < m.nel; ++e)
+    for (int n = 0; n < 2; ++n)
+      for (int d = 0; d < 6; ++d) m.elEq[12 * e + 6 * n + d] = m.meqn[m.triFirstDof[m.elTri[2 * e + n]] + d];
+  // full symmetric CSR pattern (union of element cliques, diagonal always present)
+  std::vector<std::vector<int>> rows(m.neq);
+  for (int i = 0; i < m.neq; ++i) rows[i].push_back(i);
+  for (int e = 0; e < m.nel; ++e) {
+    const int* q = &m.elEq[12 * e];
+    for (int i = 0; i < 12; ++i) {
+      if (q[i] < 0) continue;
+      for (int j = 0; j < 12; ++j)
+        if (q[j] >= 0) rows[q[i]].push_back(q[j]);
+    }
+  }
+  m.rowPtr.assign(m.neq + 1, 0);
+  for (int i = 0; i < m.neq; ++i) {
+    std::sort(rows[i].begin(), rows[i].end());
+    rows[i].erase(std::unique(rows[i].begin(), rows[i].end()), rows[i].end());
+    m.rowPtr[i + 1] = m.rowPtr[i] + (int)rows[i].size();
+  }
+  m.colInd.reserve(m.rowPtr[m.neq]);
+  for (int i = 0; i < m.neq; ++i) m.colInd.insert(m.colInd.end(), rows[i].begin(), rows[i].end());
+  // slot <- (element, entry) lists, in element order (deterministic summation order)
+  std::vector<std::vector<int>> slotList(m.colInd.size());
+  for (int e = 0; e < m.nel; ++e) {
+    const int* q = &m.elEq[12 * e];
+    for (int i = 0; i < 12; ++i) {
+      if (q[i] < 0) continue;
+      const int* b = &m.colInd[m.rowPtr[q[i]]];
+      const int* en = &m.colInd[0] + m.rowPtr[q[i] + 1];
+      for (int j = 0; j < 12; ++j) {
+        if (q[j] < 0) continue;
+        int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
+        slotList[slot].push_back(144 * e + i + 12 * j);
+      }
+    }
+  }
+  m.slotPtr.assign(m.colInd.size() + 1, 0);
+  for (size_t s = 0; s < slotList.size(); ++s) m.slotPtr[s + 1] = m.slotPtr[s] + (int)slotList[s].size();
+  for (auto& l : slotList) m.slotSrc.insert(m.slotSrc.end(), l.begin(), l.end());
+  // equation <- (element, local DOF) lists
+  std::vector<std::vector<int>> eqList(m.neq);
+  for (int e = 0; e < m.nel; ++e)
+    for (int i = 0; i < 12; ++i)
+      if (m.elEq[12 * e + i] >= 0) eqList[m.elEq[12 * e + i]].push_back(12 * e + i);
+  m.eqPtr.assign(m.neq + 1, 0);
+  for (int i = 0; i < m.neq; ++i) m.eqPtr[i + 1] = m.eqPtr[i] + (int)eqList[i].size();
+  for (auto& l : eqList) m.eqSrc.insert(m.eqSrc.end(), l.begin(), l.end());
+  return symbolicAnalysis(m, err);
+}
+
+}  // namespace fgpu

@@ -1,0 +1,83 @@
+// host_model.h -- host-side set-up of one FEDEM beam model for the GB300
+// solver: input reading, element matrices, SAM numbering, sparsity pattern,
+// deterministic gather maps and the multifrontal symbolic analysis.
+//
+// Everything here runs once per model (set-up); the per-iteration work is in
+// engine.cu.  Arrays are flat so they upload to HBM without repacking.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace fgpu {
+
+// Integration and convergence control (initiateSystemTypeModule.f90:41-185,
+// normTypeModule.f90:93-193).  Norm test codes: 1 = all-of, 2 = one-of, 0 = off.
+struct Control {
+  double alpha = -0.1, beta = 0.3025, gamma = 0.6;
+  double tStart = 0.0, tEnd = 0.0, tInc = 0.0, minInc = 0.001;
+  int maxIt = 15, minIt = 1, fixedIt = 0, nUpdat = 0, maxSeqNoUpdate = 100;
+  int stiffDampFiltering = 1;
+  bool initEquilibrium = false;
+  double tolInitEquil = 1.0e-3, limInitEquilStep = 1.0;
+  double tolFactorize = 1.0e-12;
+  // 18 convergence tests: dis[4], vel[4], acc[4], res[4], ener[2] (max, sum)
+  int tolCode[18] = {0};
+  double tolVal[18] = {0.0};
+  double wDisp[3] = {1, 1, 1}, wForce[3] = {1, 1, 1};
+  double gravity[3] = {0, 0, 0};
+};
+
+struct Front {            // one supernode of the assembly tree
+  int npiv = 0, nrow = 0; // pivots p and front size f (p pivots first)
+  int parent = -1;        // front index within the model, -1 for a root
+  int height = 0;         // 0 for leaves
+  int64_t rowOff = 0;     // offset into frontRows (f entries: equation numbers)
+  int64_t lOff = 0;       // offset of the f x p factor block (column-major)
+  int64_t uOff = 0;       // offset of the (f-p)^2 update matrix
+  int64_t wOff = 0;       // offset of the (f-p) forward-solve update vector
+  int64_t childOff = 0;   // offset into childList
+  int nchild = 0;
+  int64_t relOff = 0;     // offset into relIndex (f-p entries: row in parent front)
+  int64_t asmOff = 0;     // offset into asmSlot/asmPos (original entries)
+  int nasm = 0;
+};
+
+struct HostModel {
+  Control ctl;
+  // triads (initiateTriadTypeModule.f90): ur is 3x4 column-major
+  int ntri = 0;
+  std::vector<int> triId, triNdof, triFirstDof;
+  std::vector<double> ur;
+  // DOFs and equations (samSolverModule.f90:95-250): meqn 0-based, -1 fixed
+  int ndof = 0, neq = 0;
+  std::vector<int> meqn, dofType;
+  // beam superelements: matrices column-major 12x12 in superelement axes
+  int nel = 0;
+  std::vector<int> elId, elTri, elRef, elEq;  // elTri: triad index x2, elRef x3, elEq x12
+  std::vector<double> elOffset, supTr, triRelSup, trUnd;  // 9, 12, 12, 24 per element
+  std::vector<double> K, M, C, fg;                        // 144, 144, 144, 36 per element
+  std::vector<double> stifScl, kDmp;
+  std::vector<uint8_t> hasC, hasVld;
+  // external point loads in equation order (constant f0; forceRoutinesModule.f90)
+  std::vector<double> qext;
+  // full symmetric CSR pattern of the Newton matrix, equation order
+  std::vector<int> rowPtr, colInd;
+  // deterministic gather maps: CSR slot <- (element, entry); equation <- (element, local dof)
+  std::vector<int> slotPtr, slotSrc;   // slotSrc = 144*element + entry
+  std::vector<int> eqPtr, eqSrc;       // eqSrc = 12*element + local dof
+  // multifrontal symbolic factorisation
+  std::vector<Front> fronts;
+  std::vector<int> frontRows, childList, relIndex, asmSlot, asmPos;
+  int maxHeight = 0, maxFront = 0;
+  int64_t lSize = 0, uSize = 0, wSize = 0;
+  std::vector<int> perm;  // elimination position -> equation
+};
+
+// Parses the solver-input text and command-line options; returns 0 or < 0.
+int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m, std::string& err);
+// Nested-dissection ordering, assembly tree and front maps (symbolic.cpp).
+int symbolicAnalysis(HostModel& m, std::string& err);
+
+}  // namespace fgpu

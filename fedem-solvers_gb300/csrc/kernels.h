@@ -1,0 +1,51 @@
+// kernels.h -- launch wrappers of the batched FEDEM Newton engine kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine_dev.cuh"
+
+namespace fgpu {
+
+// element pass modes
+enum ElemMode : int {
+  EM_PRED = 0,         // predictor: velocities from dk/ak, no position update
+  EM_INC = 1,          // after an increment: corotation, deformation, forces
+  EM_STATIC_INIT = 2,  // static, initial frame kept (linInc = 1)
+  EM_STATIC = 3,       // static after an increment (corotated update)
+  EM_FINAL = 4         // final static update: corotation, zero velocities, no vld
+};
+
+// --- element_kernels.cu ----------------------------------------------------
+void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, cudaStream_t s);
+void launchPredictDofs(const DevData& d, cudaStream_t s);
+void launchElements(const DevData& d, int mode, cudaStream_t s);
+void launchResidual(const DevData& d, cudaStream_t s);
+void launchBuildElementNewton(const DevData& d, cudaStream_t s);
+void launchRotateElementNewton(const DevData& d, cudaStream_t s);
+void launchCsrGather(const DevData& d, cudaStream_t s);
+void launchIncrement(const DevData& d, cudaStream_t s);
+void launchNormsControl(const DevData& d, cudaStream_t s);
+// static equilibrium helpers
+void launchStaticBegin(const DevData& d, int* activeCount, cudaStream_t s);
+void launchStaticResidual(const DevData& d, cudaStream_t s);
+void launchStaticNorm(const DevData& d, cudaStream_t s);
+void launchStaticIncrement(const DevData& d, cudaStream_t s);
+void launchStaticFinish(const DevData& d, cudaStream_t s);
+
+// --- front_kernels.cu --------------------------------------------------------
+struct LevelPlan {
+  const int* fronts;  // device list of global front indices at this height
+  int count;
+  int maxRow;         // largest front at this height
+};
+void launchFactorLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
+void launchForwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
+void launchBackwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
+// vector glue for the solves
+void launchSolveSetup(const DevData& d, bool fp32, int sweep, cudaStream_t s);
+void launchSolveAccumulate(const DevData& d, bool fp32, cudaStream_t s);
+void launchSolveFinalize(const DevData& d, cudaStream_t s);
+void launchRefineResidual(const DevData& d, cudaStream_t s);
+
+}  // namespace fgpu

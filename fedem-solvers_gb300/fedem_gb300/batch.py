@@ -1,0 +1,155 @@
+"""Batched GPU execution of many FEDEM models (the ``fgpu_*`` C ABI).
+
+``Model`` holds the host-side set-up of one model (parse, element matrices,
+numbering, multifrontal symbolic analysis); ``Batch`` uploads models to HBM
+and advances all of them to their end time together, one Newton iteration
+per model per batched iteration.
+"""
+import ctypes
+
+import numpy as np
+
+from . import FedemException, _argv, load_library
+
+_P = ctypes.POINTER
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(_P(ctype))
+
+
+class Model:
+    """Host set-up of one model from solver-input text and solver options."""
+
+    def __init__(self, fsi, options=(), lib=None):
+        self._lib = lib or load_library()
+        argc, argv = _argv(["fedem_solver"] + list(options))
+        h = ctypes.c_void_p()
+        rc = self._lib.fgpu_model_create(fsi.encode() if isinstance(fsi, str) else fsi, argc, argv, ctypes.byref(h))
+        if rc != 0:
+            raise FedemException(f"model set-up failed ({rc}): " + self._lib.fgpu_last_error().decode())
+        self._h = h
+        s = np.zeros(8, dtype=np.int64)
+        self._lib.fgpu_model_sizes(self._h, _ptr(s, ctypes.c_longlong))
+        (self.ntri, self.ndof, self.neq, self.nel, self.nnz, self.nfront, self.max_front,
+         self.levels) = (int(v) for v in s)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fgpu_model_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def meqn(self):
+        v = np.zeros(self.ndof, dtype=np.int32)
+        self._lib.fgpu_model_meqn(self._h, _ptr(v, ctypes.c_int))
+        return v
+
+    def csr_pattern(self):
+        rp = np.zeros(self.neq + 1, dtype=np.int32)
+        ci = np.zeros(self.nnz, dtype=np.int32)
+        self._lib.fgpu_model_csr_pattern(self._h, _ptr(rp, ctypes.c_int), _ptr(ci, ctypes.c_int))
+        return rp, ci
+
+    def symbolic(self):
+        perm = np.zeros(self.neq, dtype=np.int32)
+        info = np.zeros((self.nfront, 4), dtype=np.int32)
+        self._lib.fgpu_model_symbolic(self._h, _ptr(perm, ctypes.c_int), _ptr(info, ctypes.c_int))
+        return perm, info
+
+    def element_matrix(self, iel, which):
+        m = np.zeros(144)
+        rc = self._lib.fgpu_model_element_matrix(self._h, iel, which, _ptr(m, ctypes.c_double))
+        if rc != 0:
+            raise FedemException("element_matrix: bad argument")
+        return m.reshape((12, 12), order="F")
+
+
+class Batch:
+    """Models resident on the GPU, advanced together (mixed or FP64)."""
+
+    def __init__(self, models, mixed=False, sweeps=0, lib=None):
+        self._lib = lib or load_library()
+        self.models = list(models)
+        arr = (ctypes.c_void_p * len(self.models))(*[m._h for m in self.models])
+        h = ctypes.c_void_p()
+        rc = self._lib.fgpu_batch_create(len(self.models), arr, 1 if mixed else 0, int(sweeps), ctypes.byref(h))
+        if rc != 0:
+            raise FedemException(f"batch create failed ({rc}): " + self._lib.fgpu_last_error().decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fgpu_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def run(self, max_batched=0):
+        """Runs every model to its end time; returns the run statistics."""
+        s = np.zeros(10, dtype=np.int64)
+        rc = self._lib.fgpu_batch_run(self._h, int(max_batched), _ptr(s, ctypes.c_longlong))
+        if rc != 0:
+            raise FedemException(f"batch run failed ({rc}): " + self._lib.fgpu_last_error().decode())
+        keys = ("newton_iterations", "time_steps", "batched_iterations", "models_done", "models_failed",
+                "kernels_per_iteration", "wall_us", "device_us", "h2d_bytes")
+        return {k: int(v) for k, v in zip(keys, s)}
+
+    def step(self, model):
+        st = ctypes.c_int()
+        rc = self._lib.fgpu_batch_step(self._h, model, ctypes.byref(st))
+        if rc != 0:
+            raise FedemException("step failed: " + self._lib.fgpu_last_error().decode())
+        return st.value
+
+    def info(self, model):
+        st, ss, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        steps, its = ctypes.c_longlong(), ctypes.c_longlong()
+        self._lib.fgpu_batch_model_info(self._h, model, ctypes.byref(st), ctypes.byref(ss), ctypes.byref(t),
+                                        ctypes.byref(steps), ctypes.byref(its))
+        return {"state": st.value, "status": ss.value, "time": t.value, "steps": steps.value,
+                "iterations": its.value}
+
+    def triads(self, model):
+        ur = np.zeros(12 * self.models[model].ntri)
+        self._lib.fgpu_batch_get_triads(self._h, model, _ptr(ur, ctypes.c_double))
+        return ur.reshape((-1, 4, 3)).transpose(0, 2, 1)  # (ntri, 3, 4)
+
+    def all_triads(self, out=None):
+        n = 12 * sum(m.ntri for m in self.models)
+        if out is None:
+            out = np.zeros(n)
+        self._lib.fgpu_batch_get_all_triads(self._h, _ptr(out, ctypes.c_double))
+        return out
+
+    def newton_values(self, model):
+        v = np.zeros(self.models[model].nnz)
+        self._lib.fgpu_batch_get_newton_values(self._h, model, _ptr(v, ctypes.c_double))
+        return v
+
+    def vector(self, model, which):
+        v = np.zeros(self.models[model].neq)
+        self._lib.fgpu_batch_get_vector(self._h, model, which, _ptr(v, ctypes.c_double))
+        return v
+
+    def snapshot(self):
+        if self._lib.fgpu_batch_snapshot(self._h) != 0:
+            raise FedemException("snapshot failed: " + self._lib.fgpu_last_error().decode())
+
+    def restore(self):
+        if self._lib.fgpu_batch_restore(self._h) != 0:
+            raise FedemException("restore failed: " + self._lib.fgpu_last_error().decode())
+
+    def phase_timings(self, reset=False):
+        """(samples, [element ms, factor ms, solve ms], active elements) sampled inside run()."""
+        ms = np.zeros(3)
+        el = ctypes.c_longlong()
+        n = self._lib.fgpu_batch_phase_timings(self._h, _ptr(ms, ctypes.c_double), ctypes.byref(el),
+                                               1 if reset else 0)
+        return int(n), ms, int(el.value)
+
+    def norms(self, model):
+        v = np.zeros(18)
+        self._lib.fgpu_batch_get_norms(self._h, model, _ptr(v, ctypes.c_double))
+        return v

@@ -1,0 +1,134 @@
+"""Synthetic FEDEM models written as solver-input (.fsi) text.
+
+The generators produce the workloads of the benchmark configurations with
+seeded random properties; the text uses the record subset the reference
+solver reads for beam models (&MECHANISM, &TRIAD, &SUP_EL, &TRIAD_UNDPOS,
+&ELEMENT_PROPERTY, &LOAD; see src/vpmSolver/vpmSolverTests/models/
+cantilever-pipe.fsi for the layout).  Every model is a straight chain of
+2-noded beam superelements along the global X axis.
+"""
+import math
+
+import numpy as np
+
+STEEL = {"E": 2.1e11, "G": 8.1e10, "rho": 7850.0}
+
+
+def pipe_section(od, wall):
+    """Area, Iy, Iz, It of a circular pipe."""
+    di = od - 2.0 * wall
+    area = math.pi / 4.0 * (od * od - di * di)
+    inertia = math.pi / 64.0 * (od ** 4 - di ** 4)
+    return area, inertia, inertia, 2.0 * inertia
+
+
+def _f(x):
+    return repr(float(x))
+
+
+def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof, load,
+                   shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x"):
+    """Solver-input text for a straight chain of `n_el` beams along X (or Z).
+
+    Triad k sits at k*el_len on the axis; triad `clamp` has all six DOFs
+    fixed; a constant (step) load `load` acts on DOF `load_dof` (1..6) of
+    triad `load_node`.  shear_factor = 0 gives Euler-Bernoulli beams.
+    `section` = (A, Iy, Iz, It) overrides the pipe section from od/wall.
+    """
+    if axis == "z":
+        return _chain_along_z(n_el, el_len, section or pipe_section(od, wall), E, G, rho, clamp, load_node,
+                              load_dof, load, shear_factor, weights, title)
+    area, iy, iz, it = section or pipe_section(od, wall)
+    out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
+           f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
+           f"  weightRotation = {_f(weights[1])}\n  weightGeneralized = {_f(weights[2])}\n/\n"]
+    for k in range(n_el + 1):
+        x = _f(k * el_len)
+        bc = "  BC = 0 0 0 0 0 0\n" if k == clamp else ""
+        out.append(f"&TRIAD\n  id = {k + 1}\n  nDOFs = 6\n  ur = 1.0 0.0 0.0 {x} 0.0 1.0 0.0 0.0 "
+                   f"0.0 0.0 1.0 0.0\n{bc}/\n")
+    L = _f(el_len)
+    for e in range(n_el):
+        a, b = e + 1, e + 2
+        x0 = _f(e * el_len)
+        sid = n_el + 2 + e
+        out.append(
+            f"&SUP_EL\n  id = {sid}\n  numTriads = 2\n  triadIds = {a} {b}\n  elPropId = 1\n  shadowPosAlg = 1\n"
+            f"  refTriad1Id = {a}, offset1 = 0.0 0.0 0.0\n  refTriad2Id = {b}, offset2 = 0.0 0.0 0.0\n"
+            f"  refTriad3Id = {a}, offset3 = 0.0 {L} 0.0\n"
+            f"  supPos = 1.0 0.0 0.0 {x0} 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {a}\n"
+            f"  undPosInSupElSystem = 1.0 0.0 0.0 0.0 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {b}\n"
+            f"  undPosInSupElSystem = 1.0 0.0 0.0 {L} 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n")
+    out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
+               f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
+    out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
+               f"  f0 = {_f(load)}\n/\n")
+    return "".join(out)
+
+
+def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof, load, shear_factor, weights,
+                   title):
+    """Chain along global Z; the superelement X axis is the beam axis, so the
+    superelement frame rotates global Z onto local X."""
+    area, iy, iz, it = section
+    rot = "0.0 0.0 -1.0 {p0} 0.0 1.0 0.0 {p1} 1.0 0.0 0.0 {p2}"
+    out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
+           f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
+           f"  weightRotation = {_f(weights[1])}\n  weightGeneralized = {_f(weights[2])}\n/\n"]
+    for k in range(n_el + 1):
+        bc = "  BC = 0 0 0 0 0 0\n" if k == clamp else ""
+        out.append(f"&TRIAD\n  id = {k + 1}\n  nDOFs = 6\n  ur = 1.0 0.0 0.0 0.0 0.0 1.0 0.0 0.0 "
+                   f"0.0 0.0 1.0 {_f(k * el_len)}\n{bc}/\n")
+    L = _f(el_len)
+    for e in range(n_el):
+        a, b = e + 1, e + 2
+        sid = n_el + 2 + e
+        out.append(
+            f"&SUP_EL\n  id = {sid}\n  numTriads = 2\n  triadIds = {a} {b}\n  elPropId = 1\n  shadowPosAlg = 1\n"
+            f"  refTriad1Id = {a}, offset1 = 0.0 0.0 0.0\n  refTriad2Id = {b}, offset2 = 0.0 0.0 0.0\n"
+            f"  refTriad3Id = {a}, offset3 = 0.0 {L} 0.0\n"
+            f"  supPos = {rot.format(p0='0.0', p1='0.0', p2=_f(e * el_len))}\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {a}\n"
+            f"  undPosInSupElSystem = {rot.format(p0='0.0', p1='0.0', p2='0.0')}\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {b}\n"
+            f"  undPosInSupElSystem = {rot.format(p0=L, p1='0.0', p2='0.0')}\n/\n")
+    out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
+               f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
+    out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
+               f"  f0 = {_f(load)}\n/\n")
+    return "".join(out)
+
+
+def cantilever_c1():
+    """Plain method, FP64: 5 m cantilever pipe, 20 Euler-Bernoulli beams, 1 kN tip step load."""
+    fsi = beam_chain_fsi(20, 0.25, 0.1, 0.01, clamp=0, load_node=20, load_dof=2, load=1000.0, **STEEL,
+                         title="cantilever pipe, 20 beams")
+    opts = ["-timeInc=0.001", "-timeEnd=1.0", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
+    return fsi, opts
+
+
+def batch_c4(n_models=256, seed=4, n_min=10, n_max=4000, steps=500):
+    """Batched workload: chains with log-uniform element counts, +/-20% properties,
+    random clamp and load triads, step loads uniform in [0.1, 10] kN.
+    Returns a list of (fsi text, options, element count)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_models):
+        n_el = int(math.floor(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        n_el = max(n_min, min(n_max, n_el))
+        s = rng.uniform(0.8, 1.2, size=5)
+        od = 0.1 * s[0]
+        clamp = int(rng.integers(0, n_el + 1))
+        load_node = int(rng.integers(0, n_el))
+        if load_node >= clamp:
+            load_node += 1
+        load_dof = int(rng.choice([2, 3]))
+        load = float(rng.uniform(100.0, 10000.0)) * (1.0 if rng.random() < 0.5 else -1.0)
+        fsi = beam_chain_fsi(n_el, 0.25, od, od / 10.0, E=STEEL["E"] * s[1], G=STEEL["G"] * s[2],
+                             rho=STEEL["rho"] * s[3], clamp=clamp, load_node=load_node, load_dof=load_dof,
+                             load=load, title=f"batch model, {n_el} beams")
+        opts = ["-timeInc=0.001", f"-timeEnd={steps * 0.001!r}", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
+        out.append((fsi, opts, n_el))
+    return out

@@ -1,0 +1,91 @@
+/*
+ * fgpu.h -- batched and served GB300 FEDEM Newton engine (handle-based C ABI,
+ * exported by libfedem_solver_core.so next to the legacy ABI).
+ *
+ * The reference core is a process-wide singleton (src/vpmSolver/solverModule.f90:
+ * 40-49, solverInterface.C:49) and has no batch or serving interface, so these
+ * entry points have no direct reference counterpart.  Their per-model semantics
+ * are exactly solverInit + solveNext-until-the-end of the reference
+ * (src/vpmSolver/solverInterface.h:65, :247): same input text, same options,
+ * same time integration; only many models advance together on one GPU.
+ *
+ * All pointers are caller-owned host memory, read or written during the call.
+ * Return codes: 0 success, < 0 error (fgpu_last_error() gives the text).
+ */
+#ifndef FGPU_H
+#define FGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fgpu_model fgpu_model;  /* host-side set-up of one model */
+typedef struct fgpu_batch fgpu_batch;  /* models resident on the GPU    */
+
+/* Host set-up of one model (the preprocessing part of solverInit,
+ * solverInterface.h:65): parses the solver-input text and options, builds
+ * the element matrices, equation numbering, sparsity pattern, gather maps and
+ * the multifrontal symbolic factorisation.  No GPU work. */
+int fgpu_model_create(const char* fsi, int argc, const char* const* argv, fgpu_model** out);
+void fgpu_model_destroy(fgpu_model* m);
+/* ntri, ndof, neq, nel, nnz (full CSR), nfront, max front rows, tree height */
+int fgpu_model_sizes(const fgpu_model* m, long long* sizes8);
+/* equation numbering (1-based, 0 = fixed), ndof entries */
+int fgpu_model_meqn(const fgpu_model* m, int* meqn);
+/* full symmetric CSR pattern in equation order: rowptr[neq+1], cols[nnz] (0-based) */
+int fgpu_model_csr_pattern(const fgpu_model* m, int* rowptr, int* cols);
+/* elimination order (position -> 0-based equation) and front partition:
+ * for each front: npiv, nrow, parent (-1 root), height */
+int fgpu_model_symbolic(const fgpu_model* m, int* perm, int* frontInfo4);
+/* element matrix (0 = K, 1 = M, 2 = C), 12x12 column-major, superelement axes */
+int fgpu_model_element_matrix(const fgpu_model* m, int iel, int which, double* mat);
+
+/* Uploads the models to the GPU (host -> HBM copies), solves each model's
+ * initial static equilibrium if requested and prepares the batched iteration.
+ * mixed != 0: FP32 frontal factorisation + FP64 iterative refinement with
+ * `sweeps` solves per Newton iteration; mixed == 0: plain FP64. */
+int fgpu_batch_create(int nmodels, fgpu_model* const* models, int mixed, int sweeps, fgpu_batch** out);
+void fgpu_batch_destroy(fgpu_batch* b);
+/* Runs batched Newton iterations until every model reached its end time (or
+ * maxBatched iterations).  stats10: newton iterations, time steps, batched
+ * iterations, models done, models failed, kernels per batched iteration,
+ * wall microseconds, device microseconds (CUDA events), bytes uploaded by
+ * fgpu_batch_create, 0. */
+int fgpu_batch_run(fgpu_batch* b, long long maxBatched, long long* stats10);
+/* per-model results: state (0 stepping, 1 iterating, 2 done, 3 error),
+ * status bits (1 singular, 2 max iterations, 4 NaN, 8 corotation), time,
+ * steps, Newton iterations */
+int fgpu_batch_model_info(fgpu_batch* b, int model, int* state, int* status, double* time, long long* steps,
+                          long long* iters);
+/* triad position matrices of one model, 12 doubles (3x4 column-major) each */
+int fgpu_batch_get_triads(fgpu_batch* b, int model, double* ur);
+/* triad position matrices of all models, concatenated in model order */
+long long fgpu_batch_get_all_triads(fgpu_batch* b, double* ur);
+/* FP64 Newton matrix values (full CSR, last tangent update) of one model */
+int fgpu_batch_get_newton_values(fgpu_batch* b, int model, double* vals);
+/* equation vectors of one model: 0 FS, 1 FD, 2 FI, 3 Q, 4 residual, 5 last solution */
+int fgpu_batch_get_vector(fgpu_batch* b, int model, int which, double* v);
+/* last iteration norms (18: displacement, velocity, acceleration, residual
+ * L2 + inf per DOF type, energy max/sum) */
+int fgpu_batch_get_norms(fgpu_batch* b, int model, double* norms18);
+/* Advances only `model` by one time step (step-at-a-time driving). */
+int fgpu_batch_step(fgpu_batch* b, int model, int* state);
+/* Saves / restores the batch's mutable device state with device-to-device
+ * copies (a rerun from the initial state without host transfers). */
+int fgpu_batch_snapshot(fgpu_batch* b);
+int fgpu_batch_restore(fgpu_batch* b);
+/* CUDA-event samples of three phases of the batched iteration, taken inside
+ * fgpu_batch_run: ms3 = summed milliseconds of {element pass after the
+ * increment, multifrontal factorisation, triangular solves incl. refinement};
+ * elems = summed active elements of the sampled iterations.  Returns the
+ * number of samples; reset != 0 clears the accumulators afterwards. */
+long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems, int reset);
+
+/* Text of the last error of this thread. */
+const char* fgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,152 @@
+"""GPU solver against the oracle (FP64 path within 1e-10, mixed precision
+within 1e-8 relative displacement error) and against the reference's goldens,
+all through the C ABI."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_DIR
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1.0e-10   # relative displacement error of the plain FP64 path
+MIXED_TOL = 1.0e-8   # relative displacement error of FP32 factor + FP64 refinement
+
+
+def _golden_cases():
+    with open(os.path.join(GOLDEN_DIR, "golden.json")) as f:
+        return json.load(f)["cases"]
+
+
+def rel_disp_error(ur_gpu, ur_ref, ur0):
+    dg = ur_gpu[:, :, 3] - ur0[:, :, 3]
+    dr = ur_ref[:, :, 3] - ur0[:, :, 3]
+    scale = max(np.abs(dr).max(), 1e-300)
+    return np.abs(dg - dr).max() / scale
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("case", _golden_cases(), ids=lambda c: c["name"])
+def test_reference_goldens_through_solver_abi(gpu, case, mixed):
+    from fedem_gb300.solver import FedemSolver
+
+    with open(os.path.join(GOLDEN_DIR, case["model"])) as f:
+        fsi = f.read()
+    opts = list(case["options"]) + (["-gpuMixed"] if mixed else [])
+    s = FedemSolver(solver_options=opts, fsi=fsi)
+    got = [s.get_state_var(case["triad"])]
+    while len(got) < len(case["expected"]):
+        s.solve_next()
+        got.append(s.get_state_var(case["triad"]))
+    assert s.ierr.value == 0
+    assert s.solver_done() == 0
+    for g, e in zip(got, case["expected"]):
+        for a, b in zip(g, e):
+            assert abs(a - b) <= case["abs_tol"], (g, e)
+
+
+def _run_pair(fsi, opts, mixed):
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    o = OracleModel(fsi, opts)
+    ur0 = o.triads()
+    o.run_all()
+    m = Model(fsi, opts)
+    b = Batch([m], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0, (st, b.info(0))
+    return b, o, ur0
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_cantilever_1000_steps_matches_oracle(gpu, oracle_lib, mixed):
+    from fedem_gb300 import models
+
+    fsi, opts = models.cantilever_c1()
+    b, o, ur0 = _run_pair(fsi, opts, mixed)
+    err = rel_disp_error(b.triads(0), o.triads(), ur0)
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    info = b.info(0)
+    assert info["steps"] == 1000 and abs(info["time"] - 1.0) < 1e-9
+    if not mixed:
+        assert info["iterations"] == o.iterations()
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_batch_of_uneven_models_matches_oracle(gpu, oracle_lib, mixed):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    cases = models.batch_c4(6, seed=21, n_max=400, steps=60)
+    mods = [Model(f, op) for f, op, _ in cases]
+    b = Batch(mods, mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 6 and st["models_failed"] == 0
+    for k, (f, op, _) in enumerate(cases):
+        o = OracleModel(f, op)
+        ur0 = o.triads()
+        o.run_all()
+        err = rel_disp_error(b.triads(k), o.triads(), ur0)
+        assert err <= (MIXED_TOL if mixed else FP64_TOL), (k, err)
+        if not mixed:
+            assert b.info(k)["iterations"] == o.iterations()
+
+
+def test_newton_matrix_matches_oracle(gpu, oracle_lib):
+    """FP64 Newton matrix of the first tangent update vs the oracle's assembly."""
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi, opts, _ = models.batch_c4(1, seed=7, n_max=60, steps=1)[0]
+    o = OracleModel(fsi, opts)
+    beta, gamma, dt, alpha = 0.3025, 0.6, 1.0e-3, -0.1
+    sM, sK = 1.0 / (beta * dt * dt), 1.0 + alpha
+    rp_u, ci_u, v_u = o.newton_upper(sM, gamma / (beta * dt) * sK, sK)
+    m = Model(fsi, opts)
+    b = Batch([m])
+    b.step(0)
+    vals = b.newton_values(0)
+    rp, ci = m.csr_pattern()
+    dense_gpu = np.zeros((m.neq, m.neq))
+    for i in range(m.neq):
+        dense_gpu[i, ci[rp[i]:rp[i + 1]]] = vals[rp[i]:rp[i + 1]]
+    dense_ref = np.zeros((m.neq, m.neq))
+    for i in range(m.neq):
+        dense_ref[i, ci_u[rp_u[i]:rp_u[i + 1]]] = v_u[rp_u[i]:rp_u[i + 1]]
+    dense_ref = np.triu(dense_ref) + np.triu(dense_ref, 1).T
+    scale = np.abs(dense_ref).max()
+    assert np.abs(dense_gpu - dense_ref).max() <= 1e-13 * scale
+    assert np.array_equal(dense_gpu, dense_gpu.T)
+
+
+def test_each_model_same_alone_and_in_the_mix(gpu):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+
+    cases = models.batch_c4(5, seed=33, n_max=200, steps=40)
+    mix = Batch([Model(f, op) for f, op, _ in cases])
+    mix.run()
+    for k in (0, 3):
+        f, op, _ = cases[k]
+        alone = Batch([Model(f, op)])
+        alone.run()
+        assert np.array_equal(alone.triads(0), mix.triads(k))
+
+
+def test_runs_are_bitwise_reproducible(gpu):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+
+    cases = models.batch_c4(3, seed=44, n_max=300, steps=30)
+    res = []
+    for _ in range(2):
+        b = Batch([Model(f, op) for f, op, _ in cases], mixed=True)
+        b.run()
+        res.append([b.triads(k) for k in range(3)])
+    for a, c in zip(res[0], res[1]):
+        assert np.array_equal(a, c)

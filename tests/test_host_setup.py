@@ -1,0 +1,137 @@
+"""Host-side set-up of the GPU solver (no GPU): element matrices, equation
+numbering, sparsity pattern and symbolic factorisation, checked bit-exactly
+against the oracle and for internal consistency."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_DIR, ROOT
+
+
+def _models():
+    from fedem_gb300 import models
+
+    out = [models.cantilever_c1()]
+    for fsi, opts, _ in models.batch_c4(6, seed=11, n_max=300):
+        out.append((fsi, opts))
+    with open(os.path.join(GOLDEN_DIR, "cantilever_pipe.fsi")) as f:
+        out.append((f.read(), ["-initEquilibrium"]))
+    return out
+
+
+@pytest.mark.parametrize("idx", range(8))
+def test_setup_matches_oracle_bitwise(gpu_lib, oracle_lib, idx):
+    from fedem_gb300.batch import Model
+    from oracle.oracle import OracleModel
+
+    fsi, opts = _models()[idx]
+    m = Model(fsi, opts)
+    o = OracleModel(fsi, opts)
+    assert (m.ntri, m.ndof, m.neq, m.nel) == (o.ntri, o.ndof, o.neq, o.nel)
+    # equation numbering (MEQN): bit-exact
+    assert np.array_equal(m.meqn(), o.meqn())
+    # element stiffness and mass matrices: bit-exact
+    for e in range(m.nel):
+        for which in (0, 1):
+            assert np.array_equal(m.element_matrix(e, which), o.element_matrix(e, which)), (e, which)
+    # sparsity pattern: the upper triangle of the GPU's full pattern is the oracle's pattern
+    rp, ci = m.csr_pattern()
+    orp, oci = o.csr_upper_pattern()
+    upper_rows = [ci[rp[i]:rp[i + 1]] for i in range(m.neq)]
+    for i in range(m.neq):
+        r = upper_rows[i]
+        assert np.array_equal(r[r >= i], oci[orp[i]:orp[i + 1]])
+    # full pattern is symmetric
+    a = set()
+    for i in range(m.neq):
+        for j in ci[rp[i]:rp[i + 1]]:
+            a.add((i, int(j)))
+    assert all((j, i) in a for (i, j) in a)
+
+
+@pytest.mark.parametrize("idx", range(8))
+def test_symbolic_factorisation_is_consistent(gpu_lib, idx):
+    from fedem_gb300.batch import Model
+
+    fsi, opts = _models()[idx]
+    m = Model(fsi, opts)
+    perm, info = m.symbolic()
+    assert sorted(perm.tolist()) == list(range(m.neq))
+    npiv, nrow, parent, height = info[:, 0], info[:, 1], info[:, 2], info[:, 3]
+    assert npiv.sum() == m.neq
+    assert np.all(npiv >= 1) and np.all(nrow >= npiv)
+    for f in range(m.nfront):
+        if parent[f] >= 0:
+            assert parent[f] > f  # post-order
+            assert height[parent[f]] > height[f]
+        else:
+            assert nrow[f] == npiv[f]  # roots have no update rows
+    assert nrow.max() == m.max_front
+    assert height.max() + 1 == m.levels
+
+
+def test_symbolic_is_deterministic(gpu_lib):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Model
+
+    fsi, opts, _ = models.batch_c4(1, seed=3, n_min=500, n_max=600)[0]
+    a, b = Model(fsi, opts), Model(fsi, opts)
+    pa, ia = a.symbolic()
+    pb, ib = b.symbolic()
+    assert np.array_equal(pa, pb) and np.array_equal(ia, ib)
+
+
+def test_nested_dissection_depth_is_logarithmic_for_chains(gpu_lib):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Model
+
+    fsi, opts, n = models.batch_c4(1, seed=5, n_min=4000, n_max=4000)[0]
+    m = Model(fsi, opts)
+    assert m.levels <= 2 * int(np.ceil(np.log2(n))) and m.max_front <= 36
+
+
+def _declared_functions():
+    names = []
+    for h in ("fedem_solver_core.h", "fgpu.h"):
+        with open(os.path.join(ROOT, "include", h)) as f:
+            text = f.read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for mt in re.finditer(r"^\s*(?!static)[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M):
+            names.append(mt.group(1))
+    return sorted(set(names) - {"if", "return"})
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    from fedem_gb300 import LIB_PATH
+
+    import subprocess
+
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    declared = _declared_functions()
+    assert len(declared) >= 60
+    missing = [n for n in declared if n not in exported]
+    assert not missing, missing
+
+
+def test_fedempy_symbol_set_is_exported(gpu_lib):
+    """Every symbol fedempy binds (PythonAPI/src/fedempy/solver.py:154-191) is present."""
+    fedempy = ["solverInit", "restartFromState", "solveWindow", "getStateSize", "getTransformationStateSize",
+               "getPartDeformationStateSize", "getPartStressStateSize", "getGagesSize", "saveState",
+               "saveTransformationState", "savePartDeformationState", "savePartStressState", "saveGages",
+               "solveNext", "startStep", "solveIteration", "solveEigenModes", "solveInverse", "solverDone",
+               "setExtFunc", "getTime", "evalFunc", "getEquations", "getStateVar", "getSystemSize",
+               "getSystemMatrix", "getElementStiffnessMatrix", "getRhsVector", "setRhsVector", "addRhsVector",
+               "getBeamForcesFromDisp", "getStrainsFromDisp", "getRelDisp", "getRespVars", "getJointSprCoeff"]
+    for name in fedempy:
+        assert hasattr(gpu_lib, name), name
+
+
+def test_invalid_model_fails_loudly(gpu_lib):
+    from fedem_gb300 import FedemException
+    from fedem_gb300.batch import Model
+
+    with pytest.raises(FedemException):
+        Model("&TRIAD\n id = 1\n/\n&SUP_EL\n id = 2\n numTriads = 2\n triadIds = 1 9\n/\n", [])
