@@ -51,7 +51,12 @@ def parse():
     ap.add_argument("--sweeps", type=int, default=3)
     ap.add_argument("--plain-sample", type=int, default=24, help="models timed on the plain FP64 per-model path")
     ap.add_argument("--cpu-sample-steps", type=int, default=40)
-    ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu legs (profiling runs)")
+    ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu/served legs (profiling runs)")
+    ap.add_argument("--timed-only", action="store_true", help="one timed run, no warm-up, e2e or extras (ncu)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-pool", type=int, default=48)
+    ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     return ap.parse_args()
 
 
@@ -168,6 +173,46 @@ def cpu_oracle_rate(cases, sample_steps, threads):
     return iters / dt, iters, dt
 
 
+def served_leg(args):
+    """Poisson request stream served with continuous batching; p50/p99 latency."""
+    import numpy as np
+
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Model, Server
+
+    pool = models.served_pool_c5(args.serve_pool, seed=5, steps_scale=args.serve_steps_scale)
+    mods = [Model(f, o) for f, o, _, _ in pool]
+    rng = np.random.default_rng(55)
+    n_req = max(1, int(round(args.serve_rate * args.serve_seconds)))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n_req))
+    pick = rng.integers(0, len(mods), n_req)
+    srv = Server(budget_bytes=120e9, mixed=True, sweeps=args.sweeps, min_batch=8, max_wait=0.02)
+    t0 = srv.now()
+    ids, k, overlap = [], 0, 0
+    while True:
+        now = srv.now() - t0
+        while k < n_req and arrivals[k] <= now:
+            ids.append(srv.submit(mods[pick[k]]))
+            k += 1
+        srv.pump()
+        st = srv.status()
+        overlap = max(overlap, st["live_batches"])
+        if k == n_req and st["pending"] == 0 and st["live_batches"] == 0:
+            break
+    recs = [srv.request(i) for i in ids]
+    lat = np.array([r["finished"] - r["arrival"] for r in recs])
+    its = sum(r["iterations"] for r in recs)
+    span = max(r["finished"] for r in recs) - min(r["arrival"] for r in recs)
+    failed = sum(1 for r in recs if r["state"] != 2)
+    srv.close()
+    return {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "throughput": its / span, "unit": UNIT, "requests": n_req, "failed": failed,
+            "arrival_rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
+            "max_concurrent_batches": overlap,
+            "pool": f"{len(mods)} models, 1k-200k DOF log-uniform, 100-2000 steps log-uniform x "
+                    f"{args.serve_steps_scale}"}
+
+
 def run_reference(args, dist, rank, world):
     """The CPU oracle on a bounded sample of the same workload, all host threads."""
     from fedem_gb300 import models
@@ -225,6 +270,8 @@ def main():
     # ---- device-resident timed runs (mixed precision, batched) ----------------------
     b = Batch(mods, mixed=True, sweeps=args.sweeps)
     b.snapshot()
+    if args.timed_only:
+        args.warmup, args.steps, args.no_extras = 0, 1, True
     for _ in range(args.warmup):
         b.restore()
         b.run(max_batched=200000)
@@ -263,7 +310,7 @@ def main():
     # ---- e2e through the C ABI from host buffers ------------------------------------
     e2e_iters, e2e_s, h2d, d2h = 0, 0.0, 0, 0
     out = np.zeros(12 * sum(m.ntri for m in mods))
-    for k in range(args.steps):
+    for k in range(0 if args.timed_only else args.steps):
         t0 = time.perf_counter()
         be = Batch(mods, mixed=True, sweeps=args.sweeps)
         st = be.run()
@@ -273,7 +320,7 @@ def main():
         h2d = st["h2d_bytes"]
         d2h = out.nbytes
         be.close()
-    e2e_value = e2e_iters / e2e_s
+    e2e_value = e2e_iters / e2e_s if e2e_s > 0 else None
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -312,6 +359,8 @@ def main():
         extras["cpu_baseline"] = {"value": c_rate, "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": f"all {len(cases)} models, first {args.cpu_sample_steps} "
                                             f"time steps each ({c_it} Newton iterations, {c_dt:.1f} s)"}
+        # ---- served: Poisson request stream with continuous batching ----------------------
+        extras["served"] = served_leg(args)
 
     hbm_peak, peak_kind = measured_peaks()
     roof = None

@@ -14,6 +14,7 @@
 #include "../../include/fgpu.h"
 #include "engine.h"
 #include "host_model.h"
+#include "server.h"
 
 using namespace fgpu;
 
@@ -89,6 +90,10 @@ struct fgpu_batch {
   Engine engine;
   std::vector<const HostModel*> models;
   RunStats stats;
+};
+
+struct fgpu_server {
+  Server srv;
 };
 
 extern "C" {
@@ -436,6 +441,62 @@ long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems,
   long long n = b->engine.phaseTimings(ms3, elems);
   if (reset) b->engine.resetPhaseTimings();
   return n;
+}
+
+int fgpu_server_create(double budget, int mixed, int sweeps, int maxModels, int minBatch, double maxWait,
+                       fgpu_server** out) {
+  if (!out) return fail(-1, "null output handle");
+  EngineOptions opt;
+  opt.fp32Factor = mixed != 0;
+  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 3 : 1);
+  auto* s = new fgpu_server{Server((size_t)(budget > 0 ? budget : 64.0e9), opt, maxModels, 4)};
+  s->srv.setBatchingWindow(minBatch, maxWait);
+  *out = s;
+  return 0;
+}
+
+void fgpu_server_destroy(fgpu_server* s) { delete s; }
+
+int fgpu_server_submit(fgpu_server* s, fgpu_model* m, int* id) {
+  if (!s || !m) return fail(-1, "bad argument");
+  int r = s->srv.submit(&m->m);
+  if (id) *id = r;
+  return 0;
+}
+
+int fgpu_server_pump(fgpu_server* s) {
+  if (!s) return fail(-1, "null server");
+  int rc = s->srv.pump();
+  return rc < 0 ? fail(rc, "server pump failed") : rc;
+}
+
+int fgpu_server_status(fgpu_server* s, long long* st) {
+  if (!s || !st) return fail(-1, "bad argument");
+  st[0] = s->srv.numRequests();
+  st[1] = s->srv.pending();
+  st[2] = s->srv.liveEngines();
+  st[3] = (long long)s->srv.bytesInUse();
+  return 0;
+}
+
+double fgpu_server_now(fgpu_server* s) { return s ? s->srv.now() : 0.0; }
+
+int fgpu_server_request(fgpu_server* s, int id, int* state, double* t3, long long* iters, long long* steps) {
+  if (!s || id < 0 || id >= s->srv.numRequests()) return fail(-1, "bad request id");
+  const Request& r = s->srv.request(id);
+  if (state) *state = r.state;
+  if (t3) { t3[0] = r.arrival; t3[1] = r.admitted; t3[2] = r.finished; }
+  if (iters) *iters = r.iterations;
+  if (steps) *steps = r.steps;
+  return 0;
+}
+
+int fgpu_server_result(fgpu_server* s, int id, double* ur) {
+  if (!s || !ur || id < 0 || id >= s->srv.numRequests()) return fail(-1, "bad argument");
+  const Request& r = s->srv.request(id);
+  if (r.state != 2) return fail(-2, "request not finished");
+  std::memcpy(ur, r.ur.data(), sizeof(double) * r.ur.size());
+  return 0;
 }
 
 const char* fgpu_last_error(void) { return g_lastError.c_str(); }

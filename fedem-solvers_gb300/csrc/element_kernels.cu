@@ -189,7 +189,7 @@ __device__ inline void matvecSoA(const double* __restrict__ A, int nel, int e, c
                                  double* y) {
 #pragma unroll
   for (int r = 0; r < 12; ++r) y[r] = 0.0;
-#pragma unroll 2
+#pragma unroll
   for (int c = 0; c < 12; ++c) {
     double xc = x[c];
 #pragma unroll
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       int node = d.elRef[(size_t)j * nel + e];
-      const double* U = d.ur + 12 * (size_t)tri[node];
+      const double* U = d.ur + 12 * (size_t)(node ? tri[1] : tri[0]);
       double o0 = d.offset[(size_t)(3 * j) * nel + e], o1 = d.offset[(size_t)(3 * j + 1) * nel + e],
              o2 = d.offset[(size_t)(3 * j + 2) * nel + e];
 #pragma unroll
@@ -320,9 +320,14 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   double* FDo = d.Fel + (size_t)12 * nel;
   double* FIo = d.Fel + (size_t)24 * nel;
   double* Qo = d.Fel + (size_t)36 * nel;
-  // Fs = stifScl * K * finit
-  matvecSoA(d.K, nel, e, fin, ss, y);
-  rotateStore(S, y, FSo, nel, e);
+  // Fs = stifScl * K * finit.  The predictor pass keeps the frame and the
+  // deformation of the converged previous step, so FS and Q stored by the
+  // last pass are already the values UpdateSupEls would recompute.
+  const bool keepFsQ = mode == EM_PRED;
+  if (!keepFsQ) {
+    matvecSoA(d.K, nel, e, fin, ss, y);
+    rotateStore(S, y, FSo, nel, e);
+  }
   if (isStatic) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) { FDo[(size_t)k * nel + e] = 0.0; FIo[(size_t)k * nel + e] = 0.0; }
@@ -330,27 +335,39 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
     // Fi = M * uldd
     matvecSoA(d.M, nel, e, uldd, 1.0, y);
     rotateStore(S, y, FIo, nel, e);
-    // Fd = stifScl * C * uld  (- kDmp * stifScl * K * (uld - vld))
-    if (d.hasC[e]) {
-      matvecSoA(d.C, nel, e, uld, ss, y);
+    // Fd = stifScl * C * uld  (- kDmp * stifScl * K * (uld - vld)); exactly zero without damping
+    const double dt = d.m.dt[m];
+    const bool vldActive = mode == EM_INC && d.hasVld[e] && dt > 0.0;
+    if (d.hasC[e] || vldActive) {
+      if (d.hasC[e]) {
+        matvecSoA(d.C, nel, e, uld, ss, y);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) y[k] = 0.0;
+      }
+      if (vldActive) {
+        double tmp[12], yk[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) tmp[k] = uld[k] - (fin[k] - d.finitPrev[(size_t)k * nel + e]) / dt;
+        matvecSoA(d.K, nel, e, tmp, ss, yk);
+        double kd = d.kDmp[e];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) y[k] -= kd * yk[k];
+      }
+      rotateStore(S, y, FDo, nel, e);
     } else {
 #pragma unroll
-      for (int k = 0; k < 12; ++k) y[k] = 0.0;
+      for (int k = 0; k < 12; ++k) FDo[(size_t)k * nel + e] = 0.0;
     }
-    double dt = d.m.dt[m];
-    if (mode == EM_INC && d.hasVld[e] && dt > 0.0) {
-      double tmp[12], yk[12];
-#pragma unroll
-      for (int k = 0; k < 12; ++k) tmp[k] = uld[k] - (fin[k] - d.finitPrev[(size_t)k * nel + e]) / dt;
-      matvecSoA(d.K, nel, e, tmp, ss, yk);
-      double kd = d.kDmp[e];
-#pragma unroll
-      for (int k = 0; k < 12; ++k) y[k] -= kd * yk[k];
-    }
-    rotateStore(S, y, FDo, nel, e);
   }
-  // gravity: Q = stifScl * fg * (supTr^T g)
+  if (keepFsQ) return;
+  // gravity: Q = stifScl * fg * (supTr^T g); exactly zero without gravity
   const double* gv = d.m.gravity + 3 * m;
+  if (gv[0] == 0.0 && gv[1] == 0.0 && gv[2] == 0.0) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) Qo[(size_t)k * nel + e] = 0.0;
+    return;
+  }
   double gl0 = gv[0] * S[0] + gv[1] * S[1] + gv[2] * S[2];
   double gl1 = gv[0] * S[3] + gv[1] * S[4] + gv[2] * S[5];
   double gl2 = gv[0] * S[6] + gv[1] * S[7] + gv[2] * S[8];
@@ -525,112 +542,148 @@ __device__ inline double blockMax(double v, double* sh) {
 
 __device__ inline bool isBad(double v) { return !(fabs(v) <= 1.0e300); }
 
-// iteration norms, convergence test and step bookkeeping, one block per model
-__global__ void __launch_bounds__(NTPB) kNormsControl(DevData d) {
-  __shared__ double sh[NTPB];
-  __shared__ int stepDone;
-  int m = blockIdx.x;
-  int fl = d.m.flags[m];
-  if (!(fl & FL_ACTIVE)) return;
-  const int d0 = d.m.dofOff[m], nd = d.m.ndof[m];
+// Iteration norms in two deterministic stages: every chunk of DOFs (one model
+// each) reduces 21 partial values with a fixed tree; one thread per model then
+// combines its chunks in order, applies the convergence test and the step-end
+// bookkeeping flags.  Partials: 0 sw, 1 swf, 2-4 disp/vel/acc sums of squares,
+// 5 residual, 6 energy sum, 7 energy max, 8-19 inf norms (4 vectors x 3 DOF
+// types), 20 NaN/Inf seen.
+constexpr int NPART = 21;
+constexpr int CHUNK_TPB = 256;
+
+__global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
+  __shared__ double sh[CHUNK_TPB / 32][NPART];
+  const int c = blockIdx.x;
+  const int m = d.chunkModel[c];
+  if (!(d.m.flags[m] & FL_ACTIVE)) return;
   const double* wD = d.m.wDisp + 3 * m;
   const double* wF = d.m.wForce + 3 * m;
-  double sw = 0, swf = 0, q0 = 0, q1 = 0, q2 = 0, qr = 0, es = 0, em = 0;
-  double inf[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  bool bad = false;
-  for (int k = threadIdx.x; k < nd; k += NTPB) {
-    int i = d0 + k, eq = d.meqn[i];
+  double v[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) v[k] = 0.0;
+  for (int i = d.chunkStart[c] + threadIdx.x; i < d.chunkEnd[c]; i += CHUNK_TPB) {
+    int eq = d.meqn[i];
     if (eq < 0) continue;
     int t = d.dofType[i] - 1;
     double wd = wD[t], wf = wF[t];
     double s0 = d.sinc0[i], s1 = d.sinc1[i], s2 = d.sinc2[i], r = d.res[eq];
-    bad |= isBad(s0) || isBad(r);
-    sw += wd * wd;
-    swf += wf * wf;
-    q0 += (wd * s0) * (wd * s0);
-    q1 += (wd * s1) * (wd * s1);
-    q2 += (wd * s2) * (wd * s2);
-    qr += (wf * r) * (wf * r);
-    inf[t] = fmax(inf[t], fabs(s0));
-    inf[3 + t] = fmax(inf[3 + t], fabs(s1));
-    inf[6 + t] = fmax(inf[6 + t], fabs(s2));
-    inf[9 + t] = fmax(inf[9 + t], fabs(r));
+    if (isBad(s0) || isBad(r)) v[20] = 1.0;
+    v[0] += wd * wd;
+    v[1] += wf * wf;
+    v[2] += (wd * s0) * (wd * s0);
+    v[3] += (wd * s1) * (wd * s1);
+    v[4] += (wd * s2) * (wd * s2);
+    v[5] += (wf * r) * (wf * r);
     double en = fabs(s0 * r);
-    es += en;
-    em = fmax(em, en);
+    v[6] += en;
+    v[7] = fmax(v[7], en);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (q != t) continue;
+      v[8 + q] = fmax(v[8 + q], fabs(s0));
+      v[11 + q] = fmax(v[11 + q], fabs(s1));
+      v[14 + q] = fmax(v[14 + q], fabs(s2));
+      v[17 + q] = fmax(v[17 + q], fabs(r));
+    }
   }
-  sw = blockSum(sw, sh);
-  swf = blockSum(swf, sh);
-  q0 = blockSum(q0, sh);
-  q1 = blockSum(q1, sh);
-  q2 = blockSum(q2, sh);
-  qr = blockSum(qr, sh);
-  es = blockSum(es, sh);
-  em = blockMax(em, sh);
-  for (int k = 0; k < 12; ++k) inf[k] = blockMax(inf[k], sh);
-  double anyBad = blockMax(bad ? 1.0 : 0.0, sh);
-  if (threadIdx.x == 0) {
-    double* nv = d.m.normVal + 18 * m;
-    nv[0] = sw > 0 ? sqrt(q0 / sw) : 0.0;
-    nv[4] = sw > 0 ? sqrt(q1 / sw) : 0.0;
-    nv[8] = sw > 0 ? sqrt(q2 / sw) : 0.0;
-    nv[12] = swf > 0 ? sqrt(qr / swf) : 0.0;
-    for (int t = 0; t < 3; ++t) {
-      nv[1 + t] = inf[t];
-      nv[5 + t] = inf[3 + t];
-      nv[9 + t] = inf[6 + t];
-      nv[13 + t] = inf[9 + t];
+  // warp tree (fixed pattern), then warps in order
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = (k <= 6) ? x + y : fmax(x, y);
     }
-    int neq = d.m.neq[m];
-    nv[16] = em;
-    nv[17] = (nd > 1 && neq > 0) ? es / (double)neq : es;
-    int it = d.m.iter[m] + 1;
-    d.m.iter[m] = it;
-    d.m.nIter[m] += 1;
-    if (fl & FL_TANGENT) d.m.nSeqNoUpd[m] = 0;
-    else d.m.nSeqNoUpd[m] += 1;
-    bool conv = false;
-    int done = 0;
-    if (anyBad > 0.0 || (d.m.status[m] & (SS_SINGULAR | SS_COROT))) {
-      d.m.status[m] |= anyBad > 0.0 ? SS_NAN : 0;
-      d.m.state[m] = ST_ERROR;
-    } else if (d.m.fixedIt[m] > 0) {
-      conv = it == d.m.fixedIt[m];
-    } else if (it > d.m.maxIt[m]) {
-      d.m.status[m] |= SS_MAXIT;
-      d.m.state[m] = ST_ERROR;
-    } else if (it >= max(2, d.m.minIt[m])) {
-      // normTypeModule.f90:196-249
-      bool exists1 = false, exists2 = false, oneOf = false, allOf = true;
-      const int* code = d.m.tolCode + 18 * m;
-      const double* tol = d.m.tolVal + 18 * m;
-      for (int k = 0; k < 18; ++k) {
-        if (code[k] == 2) { exists2 = true; if (nv[k] < tol[k]) oneOf = true; }
-        else if (code[k] == 1) { exists1 = true; if (nv[k] >= tol[k]) allOf = false; }
-      }
-      conv = true;
-      if (exists2) conv = conv && oneOf;
-      if (exists1) conv = conv && allOf;
-    }
-    if (conv) {
-      d.m.nStep[m] += 1;
-      d.m.state[m] = ST_NEED_STEP;
-      done = 1;
-    }
-    stepDone = done;
+    v[k] = x;
   }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NPART; ++k) sh[w][k] = v[k];
   __syncthreads();
-  if (stepDone) {
-    // terminateStep: orthonormalise the triad rotations; keep the deformation for the next step
-    const int t0 = d.m.triOff[m], nt = d.m.ntri[m];
-    for (int k = threadIdx.x; k < nt; k += NTPB) {
-      if (d.triNdof[t0 + k] != 6) continue;
-      orthonormRot(d.ur + 12 * (size_t)(t0 + k));
+  if (threadIdx.x < NPART) {
+    const int k = threadIdx.x;
+    double x = sh[0][k];
+    for (int ww = 1; ww < CHUNK_TPB / 32; ++ww) x = (k <= 6) ? x + sh[ww][k] : fmax(x, sh[ww][k]);
+    d.partial[(size_t)c * NPART + k] = x;
+  }
+}
+
+// norms, convergence test (normTypeModule.f90:196-249) and iteration counters
+__global__ void kControl(DevData d) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= d.m.n) return;
+  const int fl = d.m.flags[m];
+  if (!(fl & FL_ACTIVE)) return;
+  double v[NPART];
+  const int c0 = d.modelChunkOff[m], nc = d.modelNchunk[m];
+  for (int k = 0; k < NPART; ++k) v[k] = nc > 0 ? d.partial[(size_t)c0 * NPART + k] : 0.0;
+  for (int c = 1; c < nc; ++c)
+    for (int k = 0; k < NPART; ++k) {
+      double x = d.partial[(size_t)(c0 + c) * NPART + k];
+      v[k] = (k <= 6) ? v[k] + x : fmax(v[k], x);
     }
-    const int e0 = d.m.elOff[m], ne = d.m.nel[m];
-    for (int k = threadIdx.x; k < ne; k += NTPB)
+  double* nv = d.m.normVal + 18 * m;
+  nv[0] = v[0] > 0 ? sqrt(v[2] / v[0]) : 0.0;
+  nv[4] = v[0] > 0 ? sqrt(v[3] / v[0]) : 0.0;
+  nv[8] = v[0] > 0 ? sqrt(v[4] / v[0]) : 0.0;
+  nv[12] = v[1] > 0 ? sqrt(v[5] / v[1]) : 0.0;
+  for (int t = 0; t < 3; ++t) {
+    nv[1 + t] = v[8 + t];
+    nv[5 + t] = v[11 + t];
+    nv[9 + t] = v[14 + t];
+    nv[13 + t] = v[17 + t];
+  }
+  const int neq = d.m.neq[m], nd = d.m.ndof[m];
+  nv[16] = v[7];
+  nv[17] = (nd > 1 && neq > 0) ? v[6] / (double)neq : v[6];
+  const int it = d.m.iter[m] + 1;
+  d.m.iter[m] = it;
+  d.m.nIter[m] += 1;
+  if (fl & FL_TANGENT) d.m.nSeqNoUpd[m] = 0;
+  else d.m.nSeqNoUpd[m] += 1;
+  bool conv = false;
+  if (d.errFlag && *d.errFlag) d.m.status[m] |= SS_TIMEOUT;
+  if (v[20] > 0.0 || (d.m.status[m] & (SS_SINGULAR | SS_COROT | SS_TIMEOUT))) {
+    d.m.status[m] |= v[20] > 0.0 ? SS_NAN : 0;
+    d.m.state[m] = ST_ERROR;
+  } else if (d.m.fixedIt[m] > 0) {
+    conv = it == d.m.fixedIt[m];
+  } else if (it > d.m.maxIt[m]) {
+    d.m.status[m] |= SS_MAXIT;
+    d.m.state[m] = ST_ERROR;
+  } else if (it >= max(2, d.m.minIt[m])) {
+    bool exists1 = false, exists2 = false, oneOf = false, allOf = true;
+    const int* code = d.m.tolCode + 18 * m;
+    const double* tol = d.m.tolVal + 18 * m;
+    for (int k = 0; k < 18; ++k) {
+      if (code[k] == 2) { exists2 = true; if (nv[k] < tol[k]) oneOf = true; }
+      else if (code[k] == 1) { exists1 = true; if (nv[k] >= tol[k]) allOf = false; }
+    }
+    conv = true;
+    if (exists2) conv = conv && oneOf;
+    if (exists1) conv = conv && allOf;
+  }
+  if (conv) {
+    d.m.nStep[m] += 1;
+    d.m.state[m] = ST_NEED_STEP;
+    d.m.flags[m] = fl | FL_STEPDONE;
+  }
+}
+
+// terminateStep (solverRoutinesModule.f90:728-827): orthonormalise the triad
+// rotations of models that finished a step; keep their deformation for the next one
+__global__ void kStepEnd(DevData d) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.ntriTot) {
+    if ((d.m.flags[d.triModel[i]] & FL_STEPDONE) && d.triNdof[i] == 6) orthonormRot(d.ur + 12 * (size_t)i);
+  }
+  if (i < d.nelTot) {
+    if (d.m.flags[d.elModel[i]] & FL_STEPDONE)
+#pragma unroll
       for (int c = 0; c < 12; ++c) {
-        size_t ix = (size_t)c * d.nelTot + e0 + k;
+        size_t ix = (size_t)c * d.nelTot + i;
         d.finitPrev[ix] = d.finit[ix];
       }
   }
@@ -782,7 +835,10 @@ void launchIncrement(const DevData& d, cudaStream_t s) {
   kIncrement<<<blocksFor(n), TPB, 0, s>>>(d);
 }
 void launchNormsControl(const DevData& d, cudaStream_t s) {
-  kNormsControl<<<d.m.n, NTPB, 0, s>>>(d);
+  if (d.nchunkTot > 0) kNormsPartial<<<d.nchunkTot, CHUNK_TPB, 0, s>>>(d);
+  kControl<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d);
+  long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
+  kStepEnd<<<blocksFor(n), TPB, 0, s>>>(d);
 }
 void launchStaticBegin(const DevData& d, int* activeCount, cudaStream_t s) {
   kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount);

@@ -36,6 +36,7 @@ Engine::~Engine() {
     if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : evRun_)
     if (ev) cudaEventDestroy(ev);
+  if (evChunk_) cudaEventDestroy(evChunk_);
   for (void* p : allocs_) cudaFree(p);
   if (hActive_) cudaFreeHost(hActive_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -51,6 +52,7 @@ T* Engine::alloc(size_t n) {
   }
   cudaMemsetAsync(p, 0, n * sizeof(T), stream_);
   allocs_.push_back(p);
+  deviceBytes_ += n * sizeof(T);
   return static_cast<T*>(p);
 }
 
@@ -178,6 +180,25 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   d_.FSk = alloc<double>(neq); d_.FDk = alloc<double>(neq); d_.FIk = alloc<double>(neq); d_.Qk = alloc<double>(neq);
   d_.FIact = alloc<double>(neq); d_.res = alloc<double>(neq); d_.del = alloc<double>(neq);
   d_.x64 = alloc<double>(neq); d_.xref = alloc<double>(neq); d_.rref = alloc<double>(neq); d_.x32 = alloc<float>(neq);
+  {
+    // DOF chunks of at most 2048 DOFs, each inside one model
+    const int CH = 2048;
+    std::vector<int> cm, cs, ce, mco(nm), mnc(nm);
+    for (int k = 0; k < nm; ++k) {
+      mco[k] = (int)cm.size();
+      const int d0 = modelDofOff_[k], nd = models[k]->ndof;
+      for (int s = 0; s < nd; s += CH) {
+        cm.push_back(k);
+        cs.push_back(d0 + s);
+        ce.push_back(d0 + std::min(nd, s + CH));
+      }
+      mnc[k] = (int)cm.size() - mco[k];
+    }
+    d_.nchunkTot = (int)cm.size();
+    UPV(d_.chunkModel, int, cm); UPV(d_.chunkStart, int, cs); UPV(d_.chunkEnd, int, ce);
+    UPV(d_.modelChunkOff, int, mco); UPV(d_.modelNchunk, int, mnc);
+    d_.partial = alloc<double>(21 * (size_t)std::max(1, d_.nchunkTot));
+  }
   d_.rhs32 = nullptr;
 
   // ---- elements (SoA) -------------------------------------------------------------
@@ -338,6 +359,15 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       if (perWarpBytes > 200 * 1024) { err = "front too large for the shared-memory front kernels"; return -905; }
       levels_.push_back(lp);
     }
+    pplan_.order = dFlat;
+    pplan_.n = (int)flat.size();
+    pplan_.maxRow = 1;
+    for (const LevelPlan& lp : levels_) pplan_.maxRow = std::max(pplan_.maxRow, lp.maxRow);
+    pplan_.cntFactor = alloc<int>(nfr);
+    pplan_.cntForward = alloc<int>(nfr);
+    pplan_.readyBackward = alloc<int>(nfr);
+    pplan_.errFlag = alloc<int>(1);
+    d_.errFlag = pplan_.errFlag;
   }
 #undef UPV
   if (allocFailed_) { err = "out of device memory"; return -906; }
@@ -408,6 +438,10 @@ void Engine::resetPhaseTimings() {
 }
 
 void Engine::enqueueFactor(cudaStream_t s) {
+  if (opt_.persistent) {
+    launchFactorPersistent(d_, pplan_, opt_.fp32Factor, s);
+    return;
+  }
   for (const LevelPlan& lv : levels_) launchFactorLevel(d_, lv, opt_.fp32Factor, s);
 }
 
@@ -416,8 +450,13 @@ void Engine::enqueueSolve(cudaStream_t s) {
   for (int sweep = 0; sweep < opt_.refineSweeps; ++sweep) {
     if (sweep > 0) launchRefineResidual(d_, s);
     launchSolveSetup(d_, f32, sweep, s);
-    for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
-    for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);
+    if (opt_.persistent) {
+      launchForwardPersistent(d_, pplan_, f32, s);
+      launchBackwardPersistent(d_, pplan_, f32, s);
+    } else {
+      for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
+      for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);
+    }
     launchSolveAccumulate(d_, f32, s);
   }
   if (f32) launchSolveFinalize(d_, s);
@@ -443,7 +482,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   launchElements(d_, EM_INC, s);
   cudaEventRecordWithFlags(ev_[4], s, cudaEventRecordExternal);
   launchNormsControl(d_, s);
-  const int nl = (int)levels_.size(), sw = opt_.refineSweeps;
+  const int nl = opt_.persistent ? 1 : (int)levels_.size(), sw = opt_.refineSweeps;
   // kernels per batched iteration: 10 fixed + factor levels + per sweep (setup, accumulate,
   // forward and backward levels) + refinement residuals + mixed-precision finalise
   launchesPerIter_ = 10 + nl + sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
@@ -550,6 +589,49 @@ int Engine::run(long long maxBatched, RunStats* stats) {
     stats->batchedIterations += done;
   }
   return 0;
+}
+
+int Engine::launchChunk(int n) {
+  if (opt_.useGraph && !graphExec_) {
+    cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+    enqueueIteration(stream_);
+    if (cudaStreamEndCapture(stream_, &graph_) != cudaSuccess) return -920;
+    if (cudaGraphInstantiate(&graphExec_, graph_, 0) != cudaSuccess) return -921;
+  }
+  if (!evChunk_ && cudaEventCreateWithFlags(&evChunk_, cudaEventDisableTiming) != cudaSuccess) return -924;
+  for (int k = 0; k < n; ++k) {
+    if (opt_.useGraph) cudaGraphLaunch(graphExec_, stream_);
+    else enqueueIteration(stream_);
+  }
+  cudaMemcpyAsync(hActive_, dActive_, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaEventRecord(evChunk_, stream_);
+  chunkPending_ = true;
+  return 0;
+}
+
+int Engine::pollChunk(bool* ready, int* active) {
+  *ready = false;
+  if (!chunkPending_) {
+    *ready = true;
+    *active = 1;
+    return 0;
+  }
+  cudaError_t q = cudaEventQuery(evChunk_);
+  if (q == cudaErrorNotReady) return 0;
+  if (q != cudaSuccess) return -925;
+  chunkPending_ = false;
+  *ready = true;
+  *active = *hActive_;
+  return 0;
+}
+
+long long Engine::totalIterations() {
+  std::vector<long long> it(d_.m.n);
+  cudaMemcpyAsync(it.data(), d_.m.nIter, sizeof(long long) * it.size(), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  long long s = 0;
+  for (long long v : it) s += v;
+  return s;
 }
 
 void Engine::setStepLimit(long long lim) {

@@ -17,6 +17,7 @@ struct EngineOptions {
   bool fp32Factor = false;  // mixed precision: FP32 fronts + FP64 iterative refinement
   int refineSweeps = 3;     // solves per Newton iteration in mixed precision (1 + refinements)
   bool useGraph = true;     // capture the batched iteration in a CUDA graph
+  bool persistent = true;   // dependency-driven front kernels (one launch per phase)
 };
 
 struct RunStats {
@@ -39,6 +40,15 @@ class Engine {
   int initialState(std::string& err);
   // Runs batched iterations until no model is active or maxBatched is reached.
   int run(long long maxBatched, RunStats* stats);
+  // Non-blocking driving (serving): enqueue n batched iterations followed by an
+  // asynchronous read of the active-model count; poll reports whether that
+  // chunk finished (*ready) and whether any model is still active.
+  int launchChunk(int n);
+  int pollChunk(bool* ready, int* active);
+  // Device bytes this engine allocated.
+  size_t deviceBytes() const { return deviceBytes_; }
+  // Sum of Newton iterations over all models (blocking read).
+  long long totalIterations();
   // Advances model `m` by exactly one time step (other models may advance too).
   int advanceOneStep(int m, int* state);
 
@@ -84,6 +94,7 @@ class Engine {
   DevData d_{};
   std::vector<void*> allocs_;
   std::vector<LevelPlan> levels_;
+  PersistentPlan pplan_{};
   int* dActive_ = nullptr;
   int* hActive_ = nullptr;  // pinned
   cudaStream_t stream_ = nullptr;
@@ -104,6 +115,9 @@ class Engine {
   cudaEvent_t evRun_[2] = {nullptr, nullptr};
   double lastRunDevSec_ = 0.0;
   long long uploadedBytes_ = 0;
+  cudaEvent_t evChunk_ = nullptr;
+  bool chunkPending_ = false;
+  size_t deviceBytes_ = 0;
   double phaseMs_[3] = {0, 0, 0};
   long long phaseSamples_ = 0, phaseElems_ = 0;
 };

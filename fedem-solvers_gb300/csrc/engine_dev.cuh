@@ -14,9 +14,9 @@ namespace fgpu {
 // per-model state machine
 enum ModelState : int { ST_NEED_STEP = 0, ST_ITER = 1, ST_DONE = 2, ST_ERROR = 3 };
 // per-model flags for the current batched iteration
-enum ModelFlag : int { FL_ACTIVE = 1, FL_PRED = 2, FL_TANGENT = 4, FL_STATIC = 8, FL_REBUILD = 16 };
+enum ModelFlag : int { FL_ACTIVE = 1, FL_PRED = 2, FL_TANGENT = 4, FL_STATIC = 8, FL_REBUILD = 16, FL_STEPDONE = 32 };
 // per-model status bits
-enum ModelStatus : int { SS_SINGULAR = 1, SS_MAXIT = 2, SS_NAN = 4, SS_COROT = 8 };
+enum ModelStatus : int { SS_SINGULAR = 1, SS_MAXIT = 2, SS_NAN = 4, SS_COROT = 8, SS_TIMEOUT = 16 };
 
 struct DevModels {
   int n = 0;
@@ -79,6 +79,11 @@ struct DevData {
   float* w32;
   double* x64;  // solve vector, global equations
   float* x32;
+  int* errFlag;  // set by a kernel whose bounded wait ran out
+  // DOF chunks for the two-stage norm reduction (each chunk within one model)
+  int nchunkTot = 0;
+  int *chunkModel, *chunkStart, *chunkEnd, *modelChunkOff, *modelNchunk;
+  double* partial;  // 21 per chunk
 };
 
 }  // namespace fgpu

@@ -1,0 +1,117 @@
+// server.cpp -- continuous batching of simulation requests (see server.h).
+//
+// The reference solver has no serving mode; per request the semantics are
+// solverInit + solveNext until the end time (src/vpmSolver/solverInterface.h:65, :247).
+
+#include "server.h"
+
+#include <string>
+
+namespace fgpu {
+
+Server::Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBatch, int chunk)
+    : budget_(budgetBytes), opt_(opt), maxModels_(maxModelsPerBatch > 0 ? maxModelsPerBatch : 1 << 30),
+      chunk_(chunk > 0 ? chunk : 4), t0_(std::chrono::steady_clock::now()) {}
+
+double Server::now() const {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+}
+
+// device footprint of one model in an engine (element SoA, vectors, CSR, fronts)
+size_t Server::estimateBytes(const HostModel& m, const EngineOptions& opt) {
+  size_t el = (size_t)m.nel * (144 * 8 * 4 + 36 * 8 + 12 * 8 * 7 + 48 * 8 + 24 * 8 + 9 * 8 + 64);
+  size_t dof = (size_t)m.ndof * (8 * 8 + 12);
+  size_t eq = (size_t)m.neq * (8 * 12 + 24);
+  size_t csr = m.colInd.size() * (8 + 4 + 4 + 8) + m.slotSrc.size() * 8;
+  size_t fr = (size_t)(m.lSize + m.uSize + m.wSize) * (opt.fp32Factor ? 4 : 8) + m.fronts.size() * 96 +
+              m.asmSlot.size() * 12 + m.frontRows.size() * 4;
+  return el + dof + eq + csr + fr + (1 << 16);
+}
+
+int Server::submit(const HostModel* m) {
+  Request r;
+  r.model = m;
+  r.arrival = now();
+  reqs_.push_back(r);
+  pending_.push_back((int)reqs_.size() - 1);
+  return (int)reqs_.size() - 1;
+}
+
+int Server::admit() {
+  if (pending_.empty()) return 0;
+  // batching window: wait for a few requests unless the device is idle
+  bool idle = jobs_.empty();
+  double waited = now() - reqs_[pending_.front()].arrival;
+  if (!idle && (int)pending_.size() < minBatch_ && waited < maxWait_) return 0;
+  std::vector<int> take;
+  size_t bytes = 0;
+  while (!pending_.empty() && (int)take.size() < maxModels_) {
+    int id = pending_.front();
+    size_t b = estimateBytes(*reqs_[id].model, opt_);
+    if (inUse_ + bytes + b > budget_ && !(take.empty() && jobs_.empty())) break;
+    take.push_back(id);
+    bytes += b;
+    pending_.pop_front();
+  }
+  if (take.empty()) return 0;
+  Job j;
+  j.engine = std::make_unique<Engine>();
+  std::vector<const HostModel*> ms;
+  for (int id : take) ms.push_back(reqs_[id].model);
+  std::string err;
+  int rc = j.engine->upload(ms, opt_, err);
+  if (!rc) rc = j.engine->initialState(err);
+  double t = now();
+  if (rc) {
+    for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
+    return rc;
+  }
+  for (int id : take) { reqs_[id].state = 1; reqs_[id].admitted = t; }
+  j.ids = take;
+  j.bytes = j.engine->deviceBytes();
+  inUse_ += j.bytes;
+  if (j.engine->launchChunk(chunk_)) return -950;
+  jobs_.push_back(std::move(j));
+  return 1;
+}
+
+int Server::collect(Job& j) {
+  double t = now();
+  for (size_t k = 0; k < j.ids.size(); ++k) {
+    Request& r = reqs_[j.ids[k]];
+    r.ur.resize(12 * (size_t)r.model->ntri);
+    j.engine->getTriadUr((int)k, r.ur.data());
+    r.iterations = j.engine->modelIterations((int)k);
+    r.steps = j.engine->modelSteps((int)k);
+    r.state = j.engine->modelState((int)k) == ST_DONE ? 2 : 3;
+    r.finished = t;
+  }
+  return (int)j.ids.size();
+}
+
+int Server::pump() {
+  int finished = 0;
+  // collect finished engines, keep the others fed
+  for (size_t k = 0; k < jobs_.size();) {
+    bool ready = false;
+    int active = 1;
+    if (jobs_[k].engine->pollChunk(&ready, &active)) return -951;
+    if (ready && active == 0) {
+      finished += collect(jobs_[k]);
+      inUse_ -= jobs_[k].bytes;
+      jobs_.erase(jobs_.begin() + (long)k);
+      continue;
+    }
+    if (ready && jobs_[k].engine->launchChunk(chunk_)) return -952;
+    ++k;
+  }
+  // admit what fits (several admission rounds if memory allows)
+  for (int r = 0; r < 4 && !pending_.empty(); ++r) {
+    int a = admit();
+    if (a < 0) return a;
+    if (a == 0) break;
+  }
+  return finished;
+}
+
+}  // namespace fgpu

@@ -71,6 +71,14 @@ def load_library(path=None):
         "fgpu_batch_snapshot": (c_int, [vp]),
         "fgpu_batch_restore": (c_int, [vp]),
         "fgpu_batch_phase_timings": (c_ll, [vp, P(c_dbl), P(c_ll), c_int]),
+        "fgpu_server_create": (c_int, [c_dbl, c_int, c_int, c_int, c_int, c_dbl, P(vp)]),
+        "fgpu_server_destroy": (None, [vp]),
+        "fgpu_server_submit": (c_int, [vp, vp, P(c_int)]),
+        "fgpu_server_pump": (c_int, [vp]),
+        "fgpu_server_status": (c_int, [vp, P(c_ll)]),
+        "fgpu_server_now": (c_dbl, [vp]),
+        "fgpu_server_request": (c_int, [vp, c_int, P(c_int), P(c_dbl), P(c_ll), P(c_ll)]),
+        "fgpu_server_result": (c_int, [vp, c_int, P(c_dbl)]),
         "fgpu_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -88,4 +96,4 @@ def _argv(options):
 
 
 from .solver import FedemSolver  # noqa: E402,F401
-from .batch import Batch, Model  # noqa: E402,F401
+from .batch import Batch, Model, Server  # noqa: E402,F401

@@ -153,3 +153,63 @@ class Batch:
         v = np.zeros(18)
         self._lib.fgpu_batch_get_norms(self._h, model, _ptr(v, ctypes.c_double))
         return v
+
+
+class Server:
+    """Continuous batching of simulation requests (fgpu_server_* C ABI)."""
+
+    def __init__(self, budget_bytes=64e9, mixed=True, sweeps=0, max_models_per_batch=0, min_batch=8,
+                 max_wait=0.02, lib=None):
+        self._lib = lib or load_library()
+        h = ctypes.c_void_p()
+        rc = self._lib.fgpu_server_create(float(budget_bytes), 1 if mixed else 0, int(sweeps),
+                                          int(max_models_per_batch), int(min_batch), float(max_wait),
+                                          ctypes.byref(h))
+        if rc != 0:
+            raise FedemException("server create failed: " + self._lib.fgpu_last_error().decode())
+        self._h = h
+        self._models = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fgpu_server_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def submit(self, model):
+        rid = ctypes.c_int()
+        if self._lib.fgpu_server_submit(self._h, model._h, ctypes.byref(rid)) != 0:
+            raise FedemException("submit failed: " + self._lib.fgpu_last_error().decode())
+        self._models[rid.value] = model  # keep the host model alive until done
+        return rid.value
+
+    def pump(self):
+        n = self._lib.fgpu_server_pump(self._h)
+        if n < 0:
+            raise FedemException("pump failed: " + self._lib.fgpu_last_error().decode())
+        return n
+
+    def now(self):
+        return self._lib.fgpu_server_now(self._h)
+
+    def status(self):
+        s = np.zeros(4, dtype=np.int64)
+        self._lib.fgpu_server_status(self._h, _ptr(s, ctypes.c_longlong))
+        return {"requests": int(s[0]), "pending": int(s[1]), "live_batches": int(s[2]), "bytes": int(s[3])}
+
+    def request(self, rid):
+        st = ctypes.c_int()
+        t = np.zeros(3)
+        it, steps = ctypes.c_longlong(), ctypes.c_longlong()
+        self._lib.fgpu_server_request(self._h, rid, ctypes.byref(st), _ptr(t, ctypes.c_double), ctypes.byref(it),
+                                      ctypes.byref(steps))
+        return {"state": st.value, "arrival": t[0], "admitted": t[1], "finished": t[2], "iterations": it.value,
+                "steps": steps.value}
+
+    def result(self, rid):
+        m = self._models[rid]
+        ur = np.zeros(12 * m.ntri)
+        if self._lib.fgpu_server_result(self._h, rid, _ptr(ur, ctypes.c_double)) != 0:
+            raise FedemException("result: " + self._lib.fgpu_last_error().decode())
+        return ur.reshape((-1, 4, 3)).transpose(0, 2, 1)

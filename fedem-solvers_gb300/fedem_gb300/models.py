@@ -109,6 +109,22 @@ def cantilever_c1():
     return fsi, opts
 
 
+def served_pool_c5(n_models=64, seed=5, dof_min=1000, dof_max=200000, steps_min=100, steps_max=2000,
+                   steps_scale=1.0):
+    """Request pool of the served workload: the batch generator's beam chains with
+    sizes log-uniform in [dof_min, dof_max] DOF and time steps log-uniform in
+    [steps_min, steps_max] (times steps_scale).  Returns (fsi, options, elements, steps)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_models):
+        dof = math.exp(rng.uniform(math.log(dof_min), math.log(dof_max)))
+        n_el = max(2, int(round(dof / 6.0)))
+        steps = max(1, int(round(steps_scale * math.exp(rng.uniform(math.log(steps_min), math.log(steps_max))))))
+        sub = batch_c4(1, seed=int(rng.integers(1 << 30)), n_min=n_el, n_max=n_el, steps=steps)[0]
+        out.append((sub[0], sub[1], n_el, steps))
+    return out
+
+
 def batch_c4(n_models=256, seed=4, n_min=10, n_max=4000, steps=500):
     """Batched workload: chains with log-uniform element counts, +/-20% properties,
     random clamp and load triads, step loads uniform in [0.1, 10] kN.

@@ -81,6 +81,29 @@ int fgpu_batch_restore(fgpu_batch* b);
  * number of samples; reset != 0 clears the accumulators afterwards. */
 long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems, int reset);
 
+/* ---- serving: continuous batching of simulation requests ------------------
+ * Requests are admitted into new GPU batches (own stream each) as soon as the
+ * HBM budget allows, after a short batching window (min_batch requests or
+ * max_wait seconds, immediately when the GPU is idle); their work overlaps on
+ * the device with the batches already running.  Times are seconds on the
+ * server's steady clock (arrival stamped at submit). */
+typedef struct fgpu_server fgpu_server;
+int fgpu_server_create(double budget_bytes, int mixed, int sweeps, int max_models_per_batch, int min_batch,
+                       double max_wait, fgpu_server** out);
+void fgpu_server_destroy(fgpu_server* s);
+/* the model handle must stay alive until the request finished */
+int fgpu_server_submit(fgpu_server* s, fgpu_model* m, int* request_id);
+/* one admission/launch/collection pass; returns requests finished in it (< 0 error) */
+int fgpu_server_pump(fgpu_server* s);
+/* counts: requests, pending, live batches; bytes in use */
+int fgpu_server_status(fgpu_server* s, long long* status4);
+double fgpu_server_now(fgpu_server* s);
+/* per request: state (0 pending, 1 running, 2 done, 3 failed), arrival, admitted,
+ * finished times, Newton iterations, time steps */
+int fgpu_server_request(fgpu_server* s, int id, int* state, double* times3, long long* iters, long long* steps);
+/* final triad positions of a finished request (12 doubles per triad) */
+int fgpu_server_result(fgpu_server* s, int id, double* ur);
+
 /* Text of the last error of this thread. */
 const char* fgpu_last_error(void);
 
