@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=40)
     ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu/served legs (profiling runs)")
     ap.add_argument("--timed-only", action="store_true", help="one timed run, no warm-up, e2e or extras (ncu)")
+    ap.add_argument("--fp64", action="store_true", help="time the batched plain FP64 path instead of mixed")
+    ap.add_argument("--error-only", action="store_true", help="of the extras, run only the mixed-vs-FP64 check")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
@@ -268,7 +270,8 @@ def main():
     n_el = sum(m.nel for m in mods)
 
     # ---- device-resident timed runs (mixed precision, batched) ----------------------
-    b = Batch(mods, mixed=True, sweeps=args.sweeps)
+    mixed = not args.fp64
+    b = Batch(mods, mixed=mixed, sweeps=args.sweeps)
     b.snapshot()
     if args.timed_only:
         args.warmup, args.steps, args.no_extras = 0, 1, True
@@ -312,7 +315,7 @@ def main():
     out = np.zeros(12 * sum(m.ntri for m in mods))
     for k in range(0 if args.timed_only else args.steps):
         t0 = time.perf_counter()
-        be = Batch(mods, mixed=True, sweeps=args.sweeps)
+        be = Batch(mods, mixed=mixed, sweeps=args.sweeps)
         st = be.run()
         be.all_triads(out)
         e2e_s += time.perf_counter() - t0
@@ -323,7 +326,7 @@ def main():
     e2e_value = e2e_iters / e2e_s if e2e_s > 0 else None
 
     extras = {}
-    if not args.no_extras and rank == 0:
+    if (not args.no_extras or args.error_only) and rank == 0 and mixed:
         # ---- accuracy of the mixed path against the plain FP64 path ------------------
         bf = Batch(mods, mixed=False)
         bf.run()
@@ -339,6 +342,7 @@ def main():
             worst = max(worst, float(np.abs(a - c).max() / denom))
             off += 12 * nt
         extras["max_rel_disp_err_mixed_vs_fp64"] = worst
+    if not args.no_extras and rank == 0:
         # ---- plain per-model FP64 GPU path on a sample --------------------------------
         idx = np.linspace(0, len(mods) - 1, min(args.plain_sample, len(mods))).astype(int)
         p_it, p_s = 0, 0.0
@@ -375,11 +379,12 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if mixed else "f64",
                 "data": "synthetic (seeded generator of the 256-model beam batch)",
                 "config": {"workload": f"{args.models} beam models (10-4000 elements, log-uniform) x "
-                                       f"{args.sim_steps} HHT-alpha steps, batched mixed precision "
-                                       f"(FP32 fronts + FP64 refinement, {args.sweeps} solves/iteration)",
+                                       f"{args.sim_steps} HHT-alpha steps, batched " +
+                                       (f"mixed precision (FP32 fronts + FP64 refinement, {args.sweeps} "
+                                        f"solves/iteration)" if mixed else "plain FP64"),
                            "elements": n_el, "models_on_rank0": len(mods), "l2": "inputs larger than L2 "
                            "(element matrices and state of all models ~%.2f GB)" % (n_el * 5200 / 1e9),
                            "host_setup_s": setup_s},

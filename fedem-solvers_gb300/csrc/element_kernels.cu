@@ -199,6 +199,44 @@ __device__ inline void matvecSoA(const double* __restrict__ A, int nel, int e, c
   for (int r = 0; r < 12; ++r) y[r] *= s;
 }
 
+// Beam elements whose superelement axes are the beam's principal axes (the
+// usual FEDEM set-up) have exactly 40 structural nonzeros in K, M and C
+// (axial, torsion and the two bending planes).  They are stored as the 26
+// upper-triangle values of kBeamPattern; the product visits each row's
+// nonzeros in ascending column order, so it rounds exactly like the dense one.
+__device__ inline void matvecBeam(const double* __restrict__ A26, int nel, int e, const double* x, double s,
+                                  double* y) {
+  double a[26];
+#pragma unroll
+  for (int k = 0; k < 26; ++k) a[k] = A26[(size_t)k * nel + e];
+  // row -> (value index, column) pairs, ascending column
+  y[0] = a[0] * x[0];   y[0] += a[1] * x[6];
+  y[1] = a[2] * x[1];   y[1] += a[3] * x[5];   y[1] += a[4] * x[7];   y[1] += a[5] * x[11];
+  y[2] = a[6] * x[2];   y[2] += a[7] * x[4];   y[2] += a[8] * x[8];   y[2] += a[9] * x[10];
+  y[3] = a[10] * x[3];  y[3] += a[11] * x[9];
+  y[4] = a[7] * x[2];   y[4] += a[12] * x[4];  y[4] += a[13] * x[8];  y[4] += a[14] * x[10];
+  y[5] = a[3] * x[1];   y[5] += a[15] * x[5];  y[5] += a[16] * x[7];  y[5] += a[17] * x[11];
+  y[6] = a[1] * x[0];   y[6] += a[18] * x[6];
+  y[7] = a[4] * x[1];   y[7] += a[16] * x[5];  y[7] += a[19] * x[7];  y[7] += a[20] * x[11];
+  y[8] = a[8] * x[2];   y[8] += a[13] * x[4];  y[8] += a[21] * x[8];  y[8] += a[22] * x[10];
+  y[9] = a[11] * x[3];  y[9] += a[23] * x[9];
+  y[10] = a[9] * x[2];  y[10] += a[14] * x[4]; y[10] += a[22] * x[8]; y[10] += a[24] * x[10];
+  y[11] = a[5] * x[1];  y[11] += a[17] * x[5]; y[11] += a[20] * x[7]; y[11] += a[25] * x[11];
+#pragma unroll
+  for (int r = 0; r < 12; ++r) y[r] *= s;
+}
+
+// y = s * A x for element matrix 0 = K, 1 = M, 2 = C (compressed when the batch allows)
+__device__ inline void elemMatvec(const DevData& d, int which, int e, const double* x, double s, double* y) {
+  if (d.beamSparse) {
+    const double* A = which == 0 ? d.K26 : which == 1 ? d.M26 : d.C26;
+    matvecBeam(A, d.nelTot, e, x, s, y);
+  } else {
+    const double* A = which == 0 ? d.K : which == 1 ? d.M : d.C;
+    matvecSoA(A, d.nelTot, e, x, s, y);
+  }
+}
+
 __device__ inline void rotateStore(const double* S, const double* f, double* out, int nel, int e) {
 #pragma unroll
   for (int g = 0; g < 4; ++g)
@@ -325,7 +363,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   // last pass are already the values UpdateSupEls would recompute.
   const bool keepFsQ = mode == EM_PRED;
   if (!keepFsQ) {
-    matvecSoA(d.K, nel, e, fin, ss, y);
+    elemMatvec(d, 0, e, fin, ss, y);
     rotateStore(S, y, FSo, nel, e);
   }
   if (isStatic) {
@@ -333,14 +371,14 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
     for (int k = 0; k < 12; ++k) { FDo[(size_t)k * nel + e] = 0.0; FIo[(size_t)k * nel + e] = 0.0; }
   } else {
     // Fi = M * uldd
-    matvecSoA(d.M, nel, e, uldd, 1.0, y);
+    elemMatvec(d, 1, e, uldd, 1.0, y);
     rotateStore(S, y, FIo, nel, e);
     // Fd = stifScl * C * uld  (- kDmp * stifScl * K * (uld - vld)); exactly zero without damping
     const double dt = d.m.dt[m];
     const bool vldActive = mode == EM_INC && d.hasVld[e] && dt > 0.0;
     if (d.hasC[e] || vldActive) {
       if (d.hasC[e]) {
-        matvecSoA(d.C, nel, e, uld, ss, y);
+        elemMatvec(d, 2, e, uld, ss, y);
       } else {
 #pragma unroll
         for (int k = 0; k < 12; ++k) y[k] = 0.0;
@@ -349,7 +387,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
         double tmp[12], yk[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) tmp[k] = uld[k] - (fin[k] - d.finitPrev[(size_t)k * nel + e]) / dt;
-        matvecSoA(d.K, nel, e, tmp, ss, yk);
+        elemMatvec(d, 0, e, tmp, ss, yk);
         double kd = d.kDmp[e];
 #pragma unroll
         for (int k = 0; k < 12; ++k) y[k] -= kd * yk[k];

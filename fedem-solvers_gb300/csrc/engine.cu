@@ -237,6 +237,50 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     auto O = soa(9, [](const HostModel& h, int e, int c) { return h.elOffset[9 * (size_t)e + c]; });
     UPV(d_.offset, double, O);
   }
+  {
+    // principal-axes beam pattern: 26 upper-triangle pairs (row, col), 0-based
+    static const int pat[26][2] = {{0, 0}, {0, 6},  {1, 1},  {1, 5},  {1, 7},   {1, 11},  {2, 2},
+                                   {2, 4}, {2, 8},  {2, 10}, {3, 3},  {3, 9},   {4, 4},   {4, 8},
+                                   {4, 10}, {5, 5}, {5, 7},  {5, 11}, {6, 6},   {7, 7},   {7, 11},
+                                   {8, 8}, {8, 10}, {9, 9},  {10, 10}, {11, 11}};
+    bool inPat[144] = {false};
+    for (auto& p : pat) inPat[p[0] + 12 * p[1]] = inPat[p[1] + 12 * p[0]] = true;
+    bool sparse = opt_.compressBeams;
+    for (int k = 0; k < nm && sparse; ++k) {
+      const HostModel& h = *models[k];
+      for (int e = 0; e < h.nel && sparse; ++e)
+        for (int q = 0; q < 144 && sparse; ++q) {
+          if (inPat[q]) continue;
+          if (h.K[144 * (size_t)e + q] != 0.0 || h.M[144 * (size_t)e + q] != 0.0 ||
+              (h.hasC[e] && h.C[144 * (size_t)e + q] != 0.0))
+            sparse = false;
+        }
+    }
+    d_.beamSparse = sparse ? 1 : 0;
+    if (sparse) {
+      auto pack = [&](const std::vector<double> HostModel::*mat) {
+        std::vector<double> v((size_t)26 * nel);
+        for (int k = 0; k < nm; ++k) {
+          const HostModel& h = *models[k];
+          const std::vector<double>& src = h.*mat;
+          for (int e = 0; e < h.nel; ++e)
+            for (int q = 0; q < 26; ++q)
+              v[(size_t)q * nel + modelElOff_[k] + e] = src[144 * (size_t)e + pat[q][0] + 12 * pat[q][1]];
+        }
+        return v;
+      };
+      auto K26 = pack(&HostModel::K);
+      UPV(d_.K26, double, K26);
+      auto M26 = pack(&HostModel::M);
+      UPV(d_.M26, double, M26);
+      if (anyC) {
+        auto C26 = pack(&HostModel::C);
+        UPV(d_.C26, double, C26);
+      } else {
+        d_.C26 = alloc<double>(1);
+      }
+    }
+  }
   d_.N = alloc<double>(144 * (size_t)nel);
   d_.elMat = alloc<double>(144 * (size_t)nel);
   d_.finit = alloc<double>(12 * (size_t)nel);
@@ -361,6 +405,14 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     }
     pplan_.order = dFlat;
     pplan_.n = (int)flat.size();
+    std::vector<int> leaves;
+    for (int f = 0; f < nfr; ++f)
+      if (nchild[f] == 0) leaves.push_back(f);
+    int* dLeaves = nullptr;
+    UPV(dLeaves, int, leaves);
+    pplan_.leaves = dLeaves;
+    pplan_.nLeaves = (int)leaves.size();
+    pplan_.workCounter = alloc<int>(1);
     pplan_.maxRow = 1;
     for (const LevelPlan& lp : levels_) pplan_.maxRow = std::max(pplan_.maxRow, lp.maxRow);
     pplan_.cntFactor = alloc<int>(nfr);
@@ -439,7 +491,7 @@ void Engine::resetPhaseTimings() {
 
 void Engine::enqueueFactor(cudaStream_t s) {
   if (opt_.persistent) {
-    launchFactorPersistent(d_, pplan_, opt_.fp32Factor, s);
+    launchFactorCascade(d_, pplan_, opt_.fp32Factor, s);
     return;
   }
   for (const LevelPlan& lv : levels_) launchFactorLevel(d_, lv, opt_.fp32Factor, s);
@@ -451,8 +503,8 @@ void Engine::enqueueSolve(cudaStream_t s) {
     if (sweep > 0) launchRefineResidual(d_, s);
     launchSolveSetup(d_, f32, sweep, s);
     if (opt_.persistent) {
-      launchForwardPersistent(d_, pplan_, f32, s);
-      launchBackwardPersistent(d_, pplan_, f32, s);
+      launchForwardCascade(d_, pplan_, f32, s);
+      launchBackwardDynamic(d_, pplan_, f32, s);
     } else {
       for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
       for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);

@@ -18,6 +18,7 @@ struct EngineOptions {
   int refineSweeps = 3;     // solves per Newton iteration in mixed precision (1 + refinements)
   bool useGraph = true;     // capture the batched iteration in a CUDA graph
   bool persistent = true;   // dependency-driven front kernels (one launch per phase)
+  bool compressBeams = true;  // 26-value beam matrices when every element has the principal-axes pattern
 };
 
 struct RunStats {

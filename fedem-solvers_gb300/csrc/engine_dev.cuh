@@ -58,6 +58,10 @@ struct DevData {
   int *elTri, *elRef, *elModel;
   uint8_t *hasC, *hasVld;
   double* elMat;  // rotated element Newton matrices, SoA 144
+  // compressed beam matrices (26 upper values of the principal-axes pattern),
+  // used by the element pass when every element of the batch has that pattern
+  int beamSparse = 0;
+  double *K26, *M26, *C26;
   // CSR (full symmetric), global slots; column indices are global equations
   int64_t* rowPtr;  // neqTot + 1
   int* colInd;

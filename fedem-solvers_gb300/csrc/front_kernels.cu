@@ -161,199 +161,6 @@ __global__ void kBackwardLevel(DevData d, const int* __restrict__ fronts, int co
   for (int r = lane; r < np; r += 32) X[rows[r]] = xs[r];
 }
 
-// ---------------------------------------------------------------------------
-// Persistent, dependency-driven variants: one launch walks all heights.
-// Fronts are listed by increasing height in `order`; global warp w takes
-// order[w], order[w + W], ... (W = all resident warps).  A front waits until
-// its children (factor, forward) or its parent (backward) are done.  Every
-// front a warp waits on sits earlier in `order` and is owned by a running
-// warp whose current position is earlier still, so the warp at the smallest
-// position can always proceed: no deadlock while all warps are resident (the
-// grid is sized by occupancy).  Waits are bounded; on timeout the kernel sets
-// errFlag, skips the front and the models are reported failed.
-// ---------------------------------------------------------------------------
-constexpr long long kSpinLimit = 1LL << 22;
-
-__device__ inline bool waitCount(const int* cnt, int target, int* errFlag) {
-  long long spins = 0;
-  while (*(volatile const int*)cnt < target) {
-    __nanosleep(64);
-    if (++spins > kSpinLimit) {
-      atomicOr(errFlag, 1);
-      return false;
-    }
-  }
-  __threadfence();
-  return true;
-}
-
-template <typename T>
-__global__ void kFactorPersistent(DevData d, const int* __restrict__ order, int n, int maxRow, T* Lbase, T* Ubase,
-                                  double tolFact, int* cnt, int* errFlag) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int W = gridDim.x * wpb;
-  T* F = reinterpret_cast<T*>(smraw) + (size_t)w * ((size_t)maxRow * maxRow + 2 * maxRow);
-  T* lcol = F + (size_t)maxRow * maxRow;
-  T* diag0 = lcol + maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < n; idx += W) {
-    const int f = order[idx];
-    const int m = d.fModel[f];
-    if (!(d.m.flags[m] & FL_TANGENT)) continue;
-    const int nc = d.fNchild[f];
-    int ok = 1;
-    if (lane == 0 && nc > 0) ok = waitCount(cnt + f, nc, errFlag) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) continue;
-    const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
-    for (int k = lane; k < nr * nr; k += 32) F[k] = T(0);
-    __syncwarp();
-    const int64_t ao = d.fAsmOff[f];
-    const int na = d.fNasm[f];
-    for (int k = lane; k < na; k += 32) F[d.asmPos[ao + k]] = (T)d.csrVal[d.asmSlot[ao + k]];
-    __syncwarp();
-    for (int k = lane; k < np; k += 32) diag0[k] = F[k + nr * k];
-    __syncwarp();
-    const int64_t co = d.fChildOff[f];
-    for (int c = 0; c < nc; ++c) {
-      const int ch = d.childList[co + c];
-      const int cu = d.fNrow[ch] - d.fNpiv[ch];
-      const T* Uc = Ubase + d.fUOff[ch];
-      const int* rel = d.relIndex + d.fRelOff[ch];
-      for (int k = lane; k < cu * cu; k += 32) {
-        int a = k % cu, b = k / cu;
-        if (a >= b) F[rel[a] + nr * rel[b]] += __ldcg(Uc + k);
-      }
-      __syncwarp();
-    }
-    int neg = 0;
-    bool sing = false;
-    for (int k = 0; k < np; ++k) {
-      const T dk = F[k + nr * k];
-      const bool bad = !(fabs((double)dk) > tolFact * fabs((double)diag0[k]));
-      sing |= bad;
-      if (dk < T(0)) ++neg;
-      const T inv = bad ? T(0) : T(1) / dk;
-      for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
-      __syncwarp();
-      const int mrem = nr - k - 1;
-      for (int t = lane; t < mrem * mrem; t += 32) {
-        int ii = t % mrem, jj = t / mrem;
-        if (ii >= jj) {
-          int i = k + 1 + ii, j = k + 1 + jj;
-          F[i + nr * j] -= F[i + nr * k] * lcol[j];
-        }
-      }
-      __syncwarp();
-      for (int i = k + 1 + lane; i < nr; i += 32) F[i + nr * k] = lcol[i];
-      __syncwarp();
-    }
-    T* Lout = Lbase + d.fLOff[f];
-    for (int k = lane; k < nr * np; k += 32) Lout[k] = F[k];
-    T* Uout = Ubase + d.fUOff[f];
-    for (int k = lane; k < nu * nu; k += 32) {
-      int a = k % nu, b = k / nu;
-      Uout[k] = F[(np + a) + nr * (np + b)];
-    }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) {
-      if (neg) atomicAdd(&d.m.negPiv[m], neg);
-      if (sing) atomicOr(&d.m.status[m], SS_SINGULAR);
-      const int p = d.fParent[f];
-      if (p >= 0) atomicAdd(cnt + p, 1);
-    }
-    __syncwarp();
-  }
-}
-
-template <typename T>
-__global__ void kForwardPersistent(DevData d, const int* __restrict__ order, int n, int maxRow, const T* Lbase,
-                                   T* X, T* W, int* cnt, int* errFlag) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int Wt = gridDim.x * wpb;
-  T* v = reinterpret_cast<T*>(smraw) + (size_t)w * maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < n; idx += Wt) {
-    const int f = order[idx];
-    const int m = d.fModel[f];
-    if (!(d.m.flags[m] & FL_ACTIVE)) continue;
-    const int nc = d.fNchild[f];
-    int ok = 1;
-    if (lane == 0 && nc > 0) ok = waitCount(cnt + f, nc, errFlag) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) continue;
-    const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
-    const int* rows = d.frontRows + d.fRowOff[f];
-    for (int r = lane; r < nr; r += 32) v[r] = r < np ? X[rows[r]] : T(0);
-    __syncwarp();
-    const int64_t co = d.fChildOff[f];
-    for (int c = 0; c < nc; ++c) {
-      const int ch = d.childList[co + c];
-      const int cu = d.fNrow[ch] - d.fNpiv[ch];
-      const T* wc = W + d.fWOff[ch];
-      const int* rel = d.relIndex + d.fRelOff[ch];
-      for (int a = lane; a < cu; a += 32) v[rel[a]] += __ldcg(wc + a);
-      __syncwarp();
-    }
-    const T* L = Lbase + d.fLOff[f];
-    for (int k = 0; k < np; ++k) {
-      const T yk = v[k];
-      __syncwarp();
-      for (int i = k + 1 + lane; i < nr; i += 32) v[i] -= L[i + (size_t)nr * k] * yk;
-      __syncwarp();
-    }
-    for (int r = lane; r < np; r += 32) X[rows[r]] = v[r] / L[r + (size_t)nr * r];
-    T* wo = W + d.fWOff[f];
-    for (int a = lane; a < nu; a += 32) wo[a] = v[np + a];
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) {
-      const int p = d.fParent[f];
-      if (p >= 0) atomicAdd(cnt + p, 1);
-    }
-    __syncwarp();
-  }
-}
-
-template <typename T>
-__global__ void kBackwardPersistent(DevData d, const int* __restrict__ order, int n, int maxRow, const T* Lbase,
-                                    T* X, int* ready, int* errFlag) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int Wt = gridDim.x * wpb;
-  T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < n; idx += Wt) {
-    const int f = order[n - 1 - idx];  // decreasing height: parents first
-    const int m = d.fModel[f];
-    if (!(d.m.flags[m] & FL_ACTIVE)) continue;
-    int ok = 1;
-    if (lane == 0 && d.fParent[f] >= 0) ok = waitCount(ready + f, 1, errFlag) ? 1 : 0;
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) continue;
-    const int nr = d.fNrow[f], np = d.fNpiv[f];
-    const int* rows = d.frontRows + d.fRowOff[f];
-    for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + rows[r]);
-    __syncwarp();
-    const T* L = Lbase + d.fLOff[f];
-    for (int k = np - 1; k >= 0; --k) {
-      T s = T(0);
-      for (int i = k + 1 + lane; i < nr; i += 32) s += L[i + (size_t)nr * k] * xs[i];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) xs[k] -= s;
-      __syncwarp();
-    }
-    for (int r = lane; r < np; r += 32) X[rows[r]] = xs[r];
-    __threadfence();
-    __syncwarp();
-    const int nc = d.fNchild[f];
-    const int64_t co = d.fChildOff[f];
-    for (int c = lane; c < nc; c += 32) atomicExch(ready + d.childList[co + c], 1);
-    __syncwarp();
-  }
-}
-
 __global__ void kSolveSetup(DevData d, int fp32, int sweep) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
@@ -453,85 +260,6 @@ void launchBackwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaS
     size_t sm = (size_t)wpb * lv.maxRow * sizeof(double);
     kBackwardLevel<double><<<(lv.count + wpb - 1) / wpb, 32 * wpb, sm, s>>>(d, lv.fronts, lv.count, lv.maxRow,
                                                                             d.L64, d.x64);
-  }
-}
-
-namespace {
-int smCount() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
-
-// blocks that keep every warp resident (the persistent kernels rely on it)
-template <typename K>
-int residentBlocks(K kernel, int threads, size_t smem, int needed) {
-  int perSm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, threads, smem) != cudaSuccess || perSm < 1)
-    perSm = 1;
-  int cap = perSm * smCount();
-  return needed < cap ? (needed > 0 ? needed : 1) : cap;
-}
-}  // namespace
-
-void launchFactorPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
-  if (p.n <= 0) return;
-  const double tol = 1.0e-12;
-  size_t perWarp = (size_t)p.maxRow * p.maxRow + 2 * p.maxRow;
-  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * (size_t)d.nfrontTot, s);
-  if (fp32) {
-    int wpb = warpsPerBlock<float>(p.maxRow, perWarp);
-    size_t sm = (size_t)wpb * perWarp * sizeof(float);
-    allowSmem(kFactorPersistent<float>, sm);
-    int blocks = residentBlocks(kFactorPersistent<float>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kFactorPersistent<float><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L32, d.U32, tol,
-                                                         p.cntFactor, p.errFlag);
-  } else {
-    int wpb = warpsPerBlock<double>(p.maxRow, perWarp);
-    size_t sm = (size_t)wpb * perWarp * sizeof(double);
-    allowSmem(kFactorPersistent<double>, sm);
-    int blocks = residentBlocks(kFactorPersistent<double>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kFactorPersistent<double><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L64, d.U64, tol,
-                                                           p.cntFactor, p.errFlag);
-  }
-}
-
-void launchForwardPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
-  if (p.n <= 0) return;
-  const int wpb = 8;
-  cudaMemsetAsync(p.cntForward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
-  if (fp32) {
-    size_t sm = (size_t)wpb * p.maxRow * sizeof(float);
-    int blocks = residentBlocks(kForwardPersistent<float>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kForwardPersistent<float><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L32, d.x32, d.w32,
-                                                          p.cntForward, p.errFlag);
-  } else {
-    size_t sm = (size_t)wpb * p.maxRow * sizeof(double);
-    int blocks = residentBlocks(kForwardPersistent<double>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kForwardPersistent<double><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L64, d.x64, d.w64,
-                                                            p.cntForward, p.errFlag);
-  }
-}
-
-void launchBackwardPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
-  if (p.n <= 0) return;
-  const int wpb = 8;
-  cudaMemsetAsync(p.readyBackward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
-  if (fp32) {
-    size_t sm = (size_t)wpb * p.maxRow * sizeof(float);
-    int blocks = residentBlocks(kBackwardPersistent<float>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kBackwardPersistent<float><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L32, d.x32,
-                                                           p.readyBackward, p.errFlag);
-  } else {
-    size_t sm = (size_t)wpb * p.maxRow * sizeof(double);
-    int blocks = residentBlocks(kBackwardPersistent<double>, 32 * wpb, sm, (p.n + wpb - 1) / wpb);
-    kBackwardPersistent<double><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L64, d.x64,
-                                                             p.readyBackward, p.errFlag);
   }
 }
 

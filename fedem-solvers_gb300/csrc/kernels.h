@@ -39,16 +39,18 @@ struct LevelPlan {
   int count;
   int maxRow;         // largest front at this height
 };
-// persistent, dependency-driven front kernels over all heights (one launch each)
+// one-launch front kernels over all heights (front_cascade.cu)
 struct PersistentPlan {
-  const int* order;  // all fronts of the batch by increasing height
+  const int* order;   // all fronts of the batch by increasing height
   int n;
-  int maxRow;        // largest front of the batch
-  int *cntFactor, *cntForward, *readyBackward, *errFlag;
+  const int* leaves;  // fronts without children
+  int nLeaves;
+  int maxRow;         // largest front of the batch
+  int *cntFactor, *cntForward, *readyBackward, *workCounter, *errFlag;
 };
-void launchFactorPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
-void launchForwardPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
-void launchBackwardPersistent(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
+void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
+void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
+void launchBackwardDynamic(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
 // one launch per height
 void launchFactorLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
 void launchForwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
