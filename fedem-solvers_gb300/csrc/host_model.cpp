@@ -489,7 +489,9 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     int k = (int)w;
     c.wForce[k] = c.wDisp[k] > 0.0 ? 1.0 / c.wDisp[k] : 0.0;
   }
-  // SAM: DOFs per triad in input order; status code BC: 0 fixed, 1 free
+  // SAM: DOFs per triad in input order; status code BC: 0 fixed, 1 free,
+  // 2 free except in the initial equilibrium iterations
+  // (initiateTriadTypeModule.f90:57-123)
   std::vector<int> bcs = m.dofType;  // temporarily holds the BC codes, 6 per triad
   m.dofType.clear();
   m.triFirstDof.resize(m.ntri);
@@ -497,7 +499,8 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.triFirstDof[t] = m.ndof;
     for (int k = 0; k < m.triNdof[t]; ++k) {
       int bc = bcs[6 * t + k];
-      if (bc != 0 && bc != 1) { err = "prescribed triad DOFs are not supported"; return -30; }
+      if (bc == 2 && !c.initEquilibrium) bc = 1;
+      if (bc != 0 && bc != 1) { err = "BC code other than 0, 1 or 2 (2 only without initEquilibrium)"; return -30; }
       m.meqn.push_back(bc == 1 ? m.neq++ : -1);
       m.dofType.push_back(k < 3 ? 1 : 2);
     }
@@ -580,8 +583,12 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (it == triIndex.end()) { err = "load on unknown triad"; return -17; }
       int dof = r.inum("ldof", 0);
       if (dof < 1 || dof > m.triNdof[it->second]) { err = "load DOF must be 1..6"; return -18; }
+      if (r.inum("loadengineid", 0) > 0) { err = "time-dependent loads (loadEngineId) are not supported"; return -19; }
       int eq = m.meqn[m.triFirstDof[it->second] + dof - 1];
       if (eq >= 0) m.qext[eq] += r.num("f0", 0.0);
+    } else if (nr.name == "motion") {
+      err = "prescribed motions are not supported";
+      return -20;
     }
   }
   // element matrices, damping, scaling, corotation initialisation

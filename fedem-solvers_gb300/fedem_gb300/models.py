@@ -26,25 +26,57 @@ def _f(x):
     return repr(float(x))
 
 
+def _bc_line(k, clamp, motion):
+    if k == clamp:
+        return "  BC = 0 0 0 0 0 0\n"
+    if motion is not None and k == motion[0]:
+        # BC 2 on the prescribed DOF: free, except in initial equilibrium iterations
+        return "  BC = " + " ".join("2" if d + 1 == motion[1] else "1" for d in range(6)) + "\n"
+    return ""
+
+
+def _loads(n_el, load_node, load_dof, load, motion):
+    """&LOAD record, or with `motion` = (triad index, DOF, d1) a prescribed
+    deflection d1 * time driven by a SCALE function of the TIME sensor
+    (&MOTION, &ENGINE, &FUNCTION, &SENSOR as in the reference's
+    cantilever-prescribed.fsi)."""
+    out = []
+    if motion is None or load != 0.0:
+        out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
+                   f"  f0 = {_f(load)}\n/\n")
+    if motion is not None:
+        node, dof, d1 = motion
+        base = 2 * n_el + 20
+        out.append(f"&MOTION\n  id = {base}\n  triadId = {node + 1}\n  lDof = {int(dof)}\n  type = 'deflection'\n"
+                   f"  motionEngineId = {base + 1}\n  d0 = 0.0\n  d1 = {_f(d1)}\n/\n"
+                   f"&ENGINE\n  id = {base + 1}\n  functionId = {base + 2}\n  nArg = 1\n  argSensorId = {base + 3}\n/\n"
+                   f"&FUNCTION\n  id = {base + 2}\n  type = 'SCALE'\n  realDataSize = 1\n  realData = 1.0\n/\n"
+                   f"&SENSOR\n  id = {base + 3}\n  type = 'TIME'\n/\n")
+    return out
+
+
 def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof, load,
-                   shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x"):
+                   shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x",
+                   motion=None):
     """Solver-input text for a straight chain of `n_el` beams along X (or Z).
 
     Triad k sits at k*el_len on the axis; triad `clamp` has all six DOFs
     fixed; a constant (step) load `load` acts on DOF `load_dof` (1..6) of
     triad `load_node`.  shear_factor = 0 gives Euler-Bernoulli beams.
     `section` = (A, Iy, Iz, It) overrides the pipe section from od/wall.
+    `motion` = (triad index, DOF, d1) prescribes that DOF to d1 * time
+    (the load record is then left out when `load` is 0).
     """
     if axis == "z":
         return _chain_along_z(n_el, el_len, section or pipe_section(od, wall), E, G, rho, clamp, load_node,
-                              load_dof, load, shear_factor, weights, title)
+                              load_dof, load, shear_factor, weights, title, motion)
     area, iy, iz, it = section or pipe_section(od, wall)
     out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
            f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
            f"  weightRotation = {_f(weights[1])}\n  weightGeneralized = {_f(weights[2])}\n/\n"]
     for k in range(n_el + 1):
         x = _f(k * el_len)
-        bc = "  BC = 0 0 0 0 0 0\n" if k == clamp else ""
+        bc = _bc_line(k, clamp, motion)
         out.append(f"&TRIAD\n  id = {k + 1}\n  nDOFs = 6\n  ur = 1.0 0.0 0.0 {x} 0.0 1.0 0.0 0.0 "
                    f"0.0 0.0 1.0 0.0\n{bc}/\n")
     L = _f(el_len)
@@ -63,13 +95,12 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
             f"  undPosInSupElSystem = 1.0 0.0 0.0 {L} 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n")
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
-    out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
-               f"  f0 = {_f(load)}\n/\n")
+    out += _loads(n_el, load_node, load_dof, load, motion)
     return "".join(out)
 
 
 def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof, load, shear_factor, weights,
-                   title):
+                   title, motion):
     """Chain along global Z; the superelement X axis is the beam axis, so the
     superelement frame rotates global Z onto local X."""
     area, iy, iz, it = section
@@ -78,7 +109,7 @@ def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof,
            f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
            f"  weightRotation = {_f(weights[1])}\n  weightGeneralized = {_f(weights[2])}\n/\n"]
     for k in range(n_el + 1):
-        bc = "  BC = 0 0 0 0 0 0\n" if k == clamp else ""
+        bc = _bc_line(k, clamp, motion)
         out.append(f"&TRIAD\n  id = {k + 1}\n  nDOFs = 6\n  ur = 1.0 0.0 0.0 0.0 0.0 1.0 0.0 0.0 "
                    f"0.0 0.0 1.0 {_f(k * el_len)}\n{bc}/\n")
     L = _f(el_len)
@@ -96,8 +127,7 @@ def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof,
             f"  undPosInSupElSystem = {rot.format(p0=L, p1='0.0', p2='0.0')}\n/\n")
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
-    out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
-               f"  f0 = {_f(load)}\n/\n")
+    out += _loads(n_el, load_node, load_dof, load, motion)
     return "".join(out)
 
 

@@ -571,7 +571,24 @@ struct Load {
   int triad = -1;
   int dof = 0;  // 1..6 system DOF
   double f0 = 0.0, f1 = 0.0;
+  int engine = -1;
   double F = 0.0;
+};
+
+// General functions (functionTypeModule / engineRoutinesModule subset):
+// engine value = f(sensor value); sensor TIME gives the physical time;
+// function SCALE gives realData(1) * x; no function gives x.
+struct Func { int id = 0; std::string type; std::vector<double> real; };
+struct Sensor { int id = 0; std::string type; };
+struct EngineF { int id = 0; int func = -1; int sensor = -1; };
+
+// Prescribed motion (motionTypeModule.f90; motionRoutinesModule.f90:58-193)
+struct Motion {
+  int triad = -1, dof = 0;
+  double d0 = 0.0, d1 = 0.0;
+  int engine = -1;
+  double D = 0.0;  // current prescribed value
+  int iceq = 0;    // constraint equation (1-based)
 };
 
 struct TestItem {
@@ -587,6 +604,14 @@ struct OracleModel {
   std::vector<Prop> props;
   std::vector<Elem> elems;
   std::vector<Load> loads;
+  std::vector<Func> funcs;
+  std::vector<Sensor> sensors;
+  std::vector<EngineF> engines;
+  std::vector<Motion> motions;
+  std::vector<double> ccv;  // constant term of each constraint equation (TTCC(MPMCEQ(iceq)))
+  double tQStatic = -1.0e99;  // end of the quasi-static load steps
+  int quasiSteps = 0;         // quasi-static steps since the last dynamic one
+  std::vector<double> urdp, urddp;
   double gravity[3] = {0, 0, 0};
   double wDisp[3] = {1, 1, 1}, wForce[3] = {1, 1, 1};
 
@@ -775,9 +800,32 @@ static void getForceVectors(OracleModel& m) {
   }
 }
 
-// External load values F = f0 (+ f1 * engine) (forceRoutinesModule.f90:52-131).
+// Engine value at the current time (engineRoutinesModule.f90:163-240 subset).
+static double engineValue(const OracleModel& m, int e) {
+  const EngineF& en = m.engines[e];
+  double x = m.time;  // TIME sensor (or no sensor)
+  if (en.sensor >= 0 && lower(m.sensors[en.sensor].type) != "time") x = 0.0;
+  if (en.func < 0) return x;
+  const Func& f = m.funcs[en.func];
+  std::string t = lower(f.type);
+  if (t == "scale") return (f.real.empty() ? 1.0 : f.real[0]) * x;
+  if (t == "constant") return f.real.empty() ? 0.0 : f.real[0];
+  return x;
+}
+
+// External load values F = f0 + f1 * engine (forceRoutinesModule.f90:52-131, Evaluate).
 static void updateLoads(OracleModel& m) {
-  for (Load& l : m.loads) l.F = l.f0;
+  for (Load& l : m.loads) l.F = l.engine >= 0 ? l.f0 + l.f1 * engineValue(m, l.engine) : l.f0;
+}
+
+// Prescribed motions (motionRoutinesModule.f90:58-193): D = d0 + d1 * engine;
+// the constraint constant is the total value in linear statics, else the increment.
+static void updatePrescribedMotions(OracleModel& m, bool linearStatic) {
+  for (Motion& mo : m.motions) {
+    double Dprev = mo.D;
+    mo.D = mo.engine >= 0 ? mo.d0 + mo.d1 * engineValue(m, mo.engine) : mo.d0;
+    m.ccv[mo.iceq - 1] = linearStatic ? mo.D : mo.D - Dprev;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -820,7 +868,11 @@ static void buildElementNewton(Elem& e, double sM, double sC, double sK) {
   }
 }
 
-static void assembleSkyline(OracleModel& m, double sM, double sC, double sK) {
+// Element equation codes: >= 0 equation, -1 fixed, <= -2 prescribed DOF of
+// constraint equation iceq = -1 - code (asmSparse, sysMatrixTypeModule.f90:2099-2259:
+// rows/columns of constrained DOFs leave the matrix; with a right-hand side the
+// constant term c moves as B(jeq) -= c * EM(i,j)).
+static void assembleSkyline(OracleModel& m, double sM, double sC, double sK, std::vector<double>* rhs = nullptr) {
   skylineClear(m);
   bool rebuild = std::fabs(sM - m.oldScale[0]) + std::fabs(sK - m.oldScale[1]) + std::fabs(sC - m.oldScale[2]) > 1.0e-16;
   if (rebuild) {
@@ -837,6 +889,14 @@ static void assembleSkyline(OracleModel& m, double sM, double sC, double sK) {
         if (eq[j] < eq[i]) continue;
         skyAt(m, eq[i], eq[j]) += Ns[i + 12 * j];
       }
+    }
+    if (!rhs) continue;
+    for (int i = 0; i < 12; ++i) {
+      if (eq[i] > -2) continue;
+      double c = m.ccv[-2 - eq[i]];
+      if (!(std::fabs(c) > 1.0e-15)) continue;
+      for (int j = 0; j < 12; ++j)
+        if (eq[j] >= 0) (*rhs)[eq[j]] -= c * Ns[i + 12 * j];
     }
   }
 }
@@ -892,10 +952,15 @@ static void skylineSolve(const OracleModel& m, std::vector<double>& b) {
 // Norms (normRoutinesModule.f90:83-340, solverRoutinesModule.f90:285-380)
 // ---------------------------------------------------------------------------
 
-static void expandEq(const OracleModel& m, const std::vector<double>& eqv, std::vector<double>& dofv) {
+// Equation order -> DOF order (csExpand, solExtensionModule.f90:1352-1387):
+// free DOFs take the solution, prescribed DOFs F2 times their constant term.
+static void expandEq(const OracleModel& m, const std::vector<double>& eqv, std::vector<double>& dofv,
+                     double F2 = 1.0) {
   dofv.assign(m.ndof, 0.0);
-  for (int d = 0; d < m.ndof; ++d)
+  for (int d = 0; d < m.ndof; ++d) {
     if (m.meqn[d] > 0) dofv[d] = eqv[m.meqn[d] - 1];
+    else if (m.meqn[d] < 0) dofv[d] = F2 * m.ccv[-m.meqn[d] - 1];
+  }
 }
 
 static double scaledNorm(const OracleModel& m, const std::vector<double>& v, const double* w) {
@@ -1074,6 +1139,7 @@ static int newmarkInt(OracleModel& m) {
   m.FIactual = m.FIk;
   m.time += m.timeStep;
   updateLoads(m);
+  updatePrescribedMotions(m, false);
   // PredictVelAcc (:85-144)
   double DD = m.gamma / m.beta - 1.0, AA = 0.5 / m.beta - 1.0;
   double DA = (0.5 * m.gamma / m.beta - 1.0) * m.timeStep, AD = 1.0 / (m.beta * m.timeStep);
@@ -1105,15 +1171,18 @@ static int newmarkInt(OracleModel& m) {
     else if (nSeqNoUpdates >= m.maxSeqNoUpdate) doTangent = true;
     else doTangent = false;  // tolUpdateFactor <= 1 (default)
     if (doTangent) {
-      int ierr = factorNewton(m, SMASS, SDAMP, SSTIF);
+      // the predictor also moves the prescribed-motion terms to the right-hand side
+      bool rhsMotion = m.nIterThisStep == 0 && !m.motions.empty();
+      assembleSkyline(m, SMASS, SDAMP, SSTIF, rhsMotion ? &m.del : nullptr);
+      int ierr = skylineFactor(m, 1.0e-12);
       if (ierr < 0) return ierr;
       nSeqNoUpdates = 0;
     } else {
       ++nSeqNoUpdates;
     }
     skylineSolve(m, m.del);
-    // IncAndUpdate
-    expandEq(m, m.del, m.sinc[0]);
+    // IncAndUpdate: corrector steps replace the prescribed values by zero
+    expandEq(m, m.del, m.sinc[0], m.nIterThisStep == 0 ? 1.0 : 0.0);
     for (int d = 0; d < m.ndof; ++d) {
       m.sinc[1][d] = m.sinc[0][d] * m.svel;
       m.sinc[2][d] = m.sinc[0][d] * m.sacc;
@@ -1131,6 +1200,71 @@ static int newmarkInt(OracleModel& m) {
       if (m.nIterThisStep == m.fixedIt) break;
     } else if (m.nIterThisStep > m.maxIt) {
       return 1;  // max iterations without convergence: abort
+    } else if (m.nIterThisStep >= std::max(2, m.minIt)) {
+      if (hasConverged(m)) break;
+    }
+  }
+  getForceVectors(m);
+  return 0;
+}
+
+// restoreLastStep (solverRoutinesModule.f90:920-970)
+static void restoreLastStep(OracleModel& m) {
+  m.urd = m.urdp;
+  m.urdd = m.urddp;
+  for (Triad& t : m.triads)
+    if (t.nDOFs > 0) std::memcpy(t.ur, t.urPrev, sizeof(M34));
+  for (Elem& e : m.elems) {
+    std::memcpy(e.supTr, e.supTrPrev, sizeof(M34));
+    std::memcpy(e.finit, e.finitPrev, sizeof(e.finit));
+  }
+}
+
+// One quasi-static load step (staticEquilibriumModule.f90:470-892, staticInt, iop = 0).
+static int staticInt(OracleModel& m) {
+  const bool pureLinear = m.fixedIt == -1;
+  m.time += m.timeStep;
+  if (m.fixedIt < 0) {
+    restoreLastStep(m);
+    m.nIterThisStep = 0;
+  }
+  updateLoads(m);
+  updatePrescribedMotions(m, m.fixedIt < 0);
+  // staticIncAndUpdate without increment (linInc = 1): no corotation update
+  std::fill(m.rinc.begin(), m.rinc.end(), 0.0);
+  if (updateElems(m, false, true, false) != 0) return -1;
+  m.nIterThisStep = 0;
+  int nSeqNoUpdates = 0;
+  for (;;) {
+    getForceVectors(m);
+    for (int k = 0; k < m.neq; ++k)
+      m.residual[k] = (m.fixedIt >= 0 || m.nIterThisStep > 0) ? m.Qk[k] - m.FSk[k] : m.Qk[k];
+    m.del = m.residual;
+    bool doTangent = m.nIterThisStep < std::max(1, m.nUpdat) || nSeqNoUpdates >= m.maxSeqNoUpdate;
+    if (doTangent) {
+      bool rhsMotion = m.nIterThisStep == 0 && !m.motions.empty();
+      assembleSkyline(m, 0.0, 0.0, 1.0, rhsMotion ? &m.del : nullptr);
+      int ierr = skylineFactor(m, 1.0e-12);
+      if (ierr < 0) return ierr;
+      nSeqNoUpdates = 0;
+    } else {
+      ++nSeqNoUpdates;
+    }
+    skylineSolve(m, m.del);
+    // staticIncAndUpdate with the increment (linInc = 1 when purely linear)
+    expandEq(m, m.del, m.sinc[0], m.nIterThisStep == 0 ? 1.0 : 0.0);
+    for (int d = 0; d < m.ndof; ++d) m.rinc[d] += m.sinc[0][d];
+    incTriadsPos(m, m.sinc[0]);
+    if (updateElems(m, false, true, !pureLinear) != 0) return -1;
+    std::fill(m.sinc[1].begin(), m.sinc[1].end(), 0.0);
+    std::fill(m.sinc[2].begin(), m.sinc[2].end(), 0.0);
+    calculateNorms(m);
+    m.nIterThisStep++;
+    m.nIter++;
+    if (pureLinear || m.fixedIt > 0) {
+      if (m.nIterThisStep == std::abs(m.fixedIt)) break;
+    } else if (m.nIterThisStep > m.maxIt) {
+      return 1;
     } else if (m.nIterThisStep >= std::max(2, m.minIt)) {
       if (hasConverged(m)) break;
     }
@@ -1171,8 +1305,41 @@ static int setup(OracleModel& m, const char* fsi) {
       auto o = r.dv("orientation");
       for (size_t k = 0; k < 3 && k < o.size(); ++k) p.orient[k] = o[k];
       m.props.push_back(p);
+    } else if (r.name == "function") {
+      Func f;
+      f.id = r.i("id");
+      f.type = r.s("type");
+      f.real = r.dv("realdata");
+      m.funcs.push_back(f);
+    } else if (r.name == "sensor") {
+      Sensor sn;
+      sn.id = r.i("id");
+      sn.type = r.s("type");
+      m.sensors.push_back(sn);
     }
   }
+  // engines: functionId / argSensorId resolved to indices (engineRoutinesModule.f90)
+  for (const Record& r : recs) {
+    if (r.name != "engine") continue;
+    EngineF en;
+    en.id = r.i("id");
+    int fid = r.i("functionid", 0), sid = r.i("argsensorid", 0);
+    for (size_t k = 0; k < m.funcs.size(); ++k)
+      if (m.funcs[k].id == fid) en.func = (int)k;
+    for (size_t k = 0; k < m.sensors.size(); ++k)
+      if (m.sensors[k].id == sid) en.sensor = (int)k;
+    if (fid > 0 && en.func < 0) return -18;
+    if (en.func >= 0) {
+      std::string t = lower(m.funcs[en.func].type);
+      if (t != "scale" && t != "constant") return -19;  // other function types are not in this subset
+    }
+    m.engines.push_back(en);
+  }
+  auto findEngine = [&m](int id) {
+    for (size_t k = 0; k < m.engines.size(); ++k)
+      if (m.engines[k].id == id) return (int)k;
+    return -1;
+  };
   // superelements and their undeformed triad positions
   int pendingUnd = -1;
   for (const Record& r : recs) {
@@ -1236,7 +1403,22 @@ static int setup(OracleModel& m, const char* fsi) {
       if (l.dof < 1 || l.dof > 6) return -17;
       l.f0 = r.d("f0");
       l.f1 = r.d("f1");
+      int eid = r.i("loadengineid", 0);
+      if (eid > 0 && (l.engine = findEngine(eid)) < 0) return -18;
       m.loads.push_back(l);
+    } else if (r.name == "motion") {
+      Motion mo;
+      mo.triad = findTriad(m, r.i("triadid"));
+      if (mo.triad < 0) return -16;
+      mo.dof = r.i("ldof");
+      if (mo.dof < 1 || mo.dof > 6) return -17;
+      std::string t = lower(r.s("type"));
+      if (!t.empty() && t != "deflection") return -19;  // velocity/acceleration motions are not in this subset
+      mo.d0 = r.d("d0");
+      mo.d1 = r.d("d1");
+      int eid = r.i("motionengineid", 0);
+      if (eid > 0 && (mo.engine = findEngine(eid)) < 0) return -18;
+      m.motions.push_back(mo);
     }
   }
   (void)pendingUnd;
@@ -1308,12 +1490,26 @@ static int setup(OracleModel& m, const char* fsi) {
   m.meqn.assign(m.ndof, 0);
   m.dofType.assign(m.ndof, 1);
   m.neq = 0;
+  // BC 2 (fixed during initial equilibrium only) counts as free unless the
+  // initial equilibrium iterations are on (initiateTriadTypeModule.f90:57-123)
+  const bool addBC = m.opt.b("initEquilibrium", false);
+  std::vector<int> prescribed(m.ndof, 0);
+  for (size_t k = 0; k < m.motions.size(); ++k) {
+    Motion& mo = m.motions[k];
+    int d = m.triads[mo.triad].firstDof + mo.dof - 1;
+    if (mo.dof > m.triads[mo.triad].nDOFs || prescribed[d]) return -32;
+    mo.iceq = (int)k + 1;
+    prescribed[d] = mo.iceq;
+  }
   for (Triad& t : m.triads)
     for (int k = 0; k < t.nDOFs; ++k) {
-      m.dofType[t.firstDof + k] = k < 3 ? 1 : 2;
-      if (t.BC[k] == 1) m.meqn[t.firstDof + k] = ++m.neq;
-      else if (t.BC[k] != 0) return -30;  // prescribed DOFs are not in this subset
+      int d = t.firstDof + k;
+      m.dofType[d] = k < 3 ? 1 : 2;
+      if (prescribed[d]) m.meqn[d] = -prescribed[d];  // MEQN = -ICEQ (samSolverModule.f90)
+      else if (t.BC[k] == 1 || (t.BC[k] == 2 && !addBC)) m.meqn[d] = ++m.neq;
+      else if (t.BC[k] != 0) return -30;  // additional initial-equilibrium BCs are not in this subset
     }
+  m.ccv.assign(m.motions.size(), 0.0);
   for (const Elem& e : m.elems)
     for (int k = 0; k < 2; ++k)
       if (m.triads[e.tri[k]].nDOFs != 6) return -31;
@@ -1353,6 +1549,8 @@ static int setup(OracleModel& m, const char* fsi) {
   // system vectors
   m.urd.assign(m.ndof, 0.0);
   m.urdd.assign(m.ndof, 0.0);
+  m.urdp.assign(m.ndof, 0.0);
+  m.urddp.assign(m.ndof, 0.0);
   m.dk.assign(m.ndof, 0.0);
   m.ak.assign(m.ndof, 0.0);
   m.rinc.assign(m.ndof, 0.0);
@@ -1388,6 +1586,8 @@ static void readControl(OracleModel& m) {
   m.maxSeqNoUpdate = o.i("maxSeqNoUpdate", 100);
   m.tolUpdateFactor = o.d("tolUpdateFactor", 0.0);
   m.stiffDampFiltering = o.i("stiffDampFiltering", 1);
+  m.tQStatic = o.d("quasiStatic", 0.0);
+  if (m.tQStatic <= m.tStart) m.tQStatic = -1.0e99;  // no quasi-static increments
   for (int k = 0; k < 3; ++k) m.wForce[k] = m.wDisp[k] > 0.0 ? 1.0 / m.wDisp[k] : 0.0;
   initTol(o, "tolDispNorm", m.dis[0]);
   initTol(o, "tolDispTra", m.dis[1]);
@@ -1410,6 +1610,9 @@ static void readControl(OracleModel& m) {
 }
 
 static bool hasReached(const OracleModel& m, double t) { return m.time + 0.1 * m.minInc > t; }
+
+// systemTypeModule.f90:334-347
+static bool isQuasiStatic(const OracleModel& m, double t) { return t < m.tQStatic + 0.1 * m.minInc; }
 
 }  // namespace
 
@@ -1449,7 +1652,22 @@ extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
   if (!m || m->error) { if (ierr) *ierr = m ? m->error : -1; return 0; }
   if (m->tStart <= m->tEnd && hasReached(*m, m->tEnd)) return 0;
   m->timeStep = m->tInc;
-  int err = newmarkInt(*m);
+  // quasi-static load steps up to the quasiStatic time, Newmark after it
+  // (solverModule.f90:826-860)
+  bool linearStatic = false;
+  int err = 0;
+  if (isQuasiStatic(*m, m->time + m->timeStep)) {
+    m->quasiSteps++;
+    err = staticInt(*m);
+    linearStatic = m->fixedIt < 0;
+  } else {
+    if (m->quasiSteps > 0) {
+      // continuing with dynamics: estimate the starting velocity
+      for (int d = 0; d < m->ndof; ++d) m->urd[d] = m->rinc[d] / m->timeStep;
+      m->quasiSteps = 0;
+    }
+    err = newmarkInt(*m);
+  }
   if (err != 0) { m->error = err; if (ierr) *ierr = err; return 0; }
   m->nStep++;
   bool finished = m->tStart <= m->tEnd && hasReached(*m, m->tEnd);
@@ -1464,7 +1682,9 @@ extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
         for (int c = 0; c < 3; ++c) t.ur[r][c] = R[r][c];
     }
   }
-  if (!finished) {
+  if (!finished && !linearStatic) {
+    m->urdp = m->urd;
+    m->urddp = m->urdd;
     for (Triad& t : m->triads) std::memcpy(t.urPrev, t.ur, sizeof(M34));
     for (Elem& e : m->elems) {
       std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));

@@ -135,3 +135,25 @@ def test_invalid_model_fails_loudly(gpu_lib):
 
     with pytest.raises(FedemException):
         Model("&TRIAD\n id = 1\n/\n&SUP_EL\n id = 2\n numTriads = 2\n triadIds = 1 9\n/\n", [])
+
+
+def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
+    """Prescribed motions and engine-driven loads are refused with a message
+    instead of being dropped; BC code 2 counts as a free DOF when the initial
+    equilibrium iterations are off (initiateTriadTypeModule.f90:57-123)."""
+    from fedem_gb300 import FedemException, models
+    from fedem_gb300.batch import Model
+
+    with open(os.path.join(GOLDEN_DIR, "cantilever_prescribed.fsi")) as f:
+        fsi = f.read()
+    with pytest.raises(FedemException, match="prescribed motions"):
+        Model(fsi, [])
+    base = models.beam_chain_fsi(4, 1.0, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0, **models.STEEL)
+    with pytest.raises(FedemException, match="loadEngineId"):
+        Model(base.replace("  f0 =", "  loadEngineId = 7\n  f0 ="), [])
+    free = Model(base, [])
+    bc2 = Model(base.replace("&TRIAD\n  id = 5\n  nDOFs = 6\n", "&TRIAD\n  id = 5\n  nDOFs = 6\n  BC = 2 2 2 2 2 2\n"), [])
+    assert bc2.neq == free.neq
+    with pytest.raises(FedemException):
+        Model(base.replace("&TRIAD\n  id = 5\n  nDOFs = 6\n", "&TRIAD\n  id = 5\n  nDOFs = 6\n  BC = 2 2 2 2 2 2\n"),
+              ["-initEquilibrium"])
