@@ -418,6 +418,14 @@ int fgpu_batch_get_norms(fgpu_batch* b, int k, double* n18) {
   return 0;
 }
 
+int fgpu_batch_norms_noalloc(fgpu_batch* b, int k, double* n18) {
+  if (!b || !n18 || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  std::string err;
+  int rc = normsNoAlloc(b->engine.devData(), k, b->engine.normChunkOffset(k), b->engine.normChunkCount(k),
+                        b->engine.stream(), n18, err);
+  return rc ? fail(rc, err) : 0;
+}
+
 int fgpu_batch_step(fgpu_batch* b, int k, int* state) {
   if (!b || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad model index");
   int rc = b->engine.advanceOneStep(k, state);

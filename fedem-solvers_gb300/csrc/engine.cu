@@ -197,6 +197,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     d_.nchunkTot = (int)cm.size();
     UPV(d_.chunkModel, int, cm); UPV(d_.chunkStart, int, cs); UPV(d_.chunkEnd, int, ce);
     UPV(d_.modelChunkOff, int, mco); UPV(d_.modelNchunk, int, mnc);
+    normChunkOff_ = mco;
+    normChunkCnt_ = mnc;
     d_.partial = alloc<double>(21 * (size_t)std::max(1, d_.nchunkTot));
   }
   d_.rhs32 = nullptr;

@@ -66,6 +66,10 @@ class Engine {
   int getEqVector(int m, int which, double* v);  // 0 FS, 1 FD, 2 FI, 3 Q, 4 residual, 5 del
   const HostModel& host(int m) const { return *hm_[m]; }
   cudaStream_t stream() const { return stream_; }
+  const DevData& devData() const { return d_; }
+  // first norm chunk and chunk count (2048 DOFs each) of model m
+  int normChunkOffset(int m) const { return normChunkOff_[m]; }
+  int normChunkCount(int m) const { return normChunkCnt_[m]; }
   // Device counters for the launch count claim: kernels enqueued per batched iteration.
   int launchesPerIteration() const { return launchesPerIter_; }
   double lastRunSeconds() const { return lastRunSec_; }
@@ -103,6 +107,7 @@ class Engine {
   cudaGraphExec_t graphExec_ = nullptr;
   std::vector<int> modelTriOff_, modelDofOff_, modelEqOff_, modelElOff_;
   std::vector<int64_t> modelSlotOff_;
+  std::vector<int> normChunkOff_, normChunkCnt_;
   int launchesPerIter_ = 0;
   double lastRunSec_ = 0.0;
   bool allocFailed_ = false;

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "engine_dev.cuh"
 
 namespace fgpu {
@@ -60,5 +62,10 @@ void launchSolveSetup(const DevData& d, bool fp32, int sweep, cudaStream_t s);
 void launchSolveAccumulate(const DevData& d, bool fp32, cudaStream_t s);
 void launchSolveFinalize(const DevData& d, cudaStream_t s);
 void launchRefineResidual(const DevData& d, cudaStream_t s);
+
+// Convergence norms of model m recomputed into a fixed scratch array compiled
+// into the library (no device allocation); blocks until the 18 values are in
+// out18 (host).  c0/nc: the model's first norm chunk and chunk count.
+int normsNoAlloc(const DevData& d, int m, int c0, int nc, cudaStream_t s, double* out18, std::string& err);
 
 }  // namespace fgpu

@@ -67,6 +67,7 @@ def load_library(path=None):
         "fgpu_batch_get_newton_values": (c_int, [vp, c_int, P(c_dbl)]),
         "fgpu_batch_get_vector": (c_int, [vp, c_int, c_int, P(c_dbl)]),
         "fgpu_batch_get_norms": (c_int, [vp, c_int, P(c_dbl)]),
+        "fgpu_batch_norms_noalloc": (c_int, [vp, c_int, P(c_dbl)]),
         "fgpu_batch_step": (c_int, [vp, c_int, P(c_int)]),
         "fgpu_batch_snapshot": (c_int, [vp]),
         "fgpu_batch_restore": (c_int, [vp]),

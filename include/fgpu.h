@@ -68,6 +68,20 @@ int fgpu_batch_get_vector(fgpu_batch* b, int model, int which, double* v);
 /* last iteration norms (18: displacement, velocity, acceleration, residual
  * L2 + inf per DOF type, energy max/sum) */
 int fgpu_batch_get_norms(fgpu_batch* b, int model, double* norms18);
+/* The same 18 norms recomputed on the device from the model's current
+ * increment and residual vectors WITHOUT ALLOCATING anything: for callers that
+ * may not allocate device memory when they check convergence (a control or
+ * co-simulation loop between its own stream-ordered kernels, where cudaMalloc
+ * and cudaFree would synchronise the device; a process whose device memory is
+ * committed to resident batches).  It reduces into a fixed scratch array of
+ * about 41 KB per device compiled into the library, so models above 524,288
+ * DOFs are refused (error code, message in fgpu_last_error).  The first call on
+ * a device looks up that scratch's address: make it before any stream capture
+ * begins on the device.  Calls that overlap in time on one device race on the
+ * shared scratch: serialise them.  Blocks until the values are in norms18.
+ * No reference counterpart (the reference computes norms inside its own
+ * iteration loop only). */
+int fgpu_batch_norms_noalloc(fgpu_batch* b, int model, double* norms18);
 /* Advances only `model` by one time step (step-at-a-time driving). */
 int fgpu_batch_step(fgpu_batch* b, int model, int* state);
 /* Saves / restores the batch's mutable device state with device-to-device
