@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--models", type=int, default=256)
     ap.add_argument("--sim-steps", type=int, default=500)
-    ap.add_argument("--sweeps", type=int, default=3)
+    ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=24, help="models timed on the plain FP64 per-model path")
     ap.add_argument("--cpu-sample-steps", type=int, default=40)
     ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu/served legs (profiling runs)")
@@ -283,12 +283,13 @@ def main():
     if dist:
         dist.barrier()
     clocks.start()
-    iters, dev_s, wall_s, kernels, batched = 0, 0.0, 0.0, 0, 0
+    iters, dev_s, wall_s, kernels, batched, tsteps = 0, 0.0, 0.0, 0, 0, 0
     failed = 0
     for _ in range(args.steps):
         b.restore()
         st = b.run(max_batched=200000)
         iters += st["newton_iterations"]
+        tsteps += st["time_steps"]
         dev_s += st["device_us"] * 1e-6
         wall_s += st["wall_us"] * 1e-6
         kernels = st["kernels_per_iteration"]
@@ -298,13 +299,13 @@ def main():
     if dist:
         import torch
 
-        t = torch.tensor([dev_s, float(iters)], dtype=torch.float64, device="cuda")
+        t = torch.tensor([dev_s, float(iters), float(tsteps)], dtype=torch.float64, device="cuda")
         tmax = t.clone()
         dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
         dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        dev_s_max, iters_tot = float(tmax[0]), float(t[1])
+        dev_s_max, iters_tot, tsteps_tot = float(tmax[0]), float(t[1]), float(t[2])
     else:
-        dev_s_max, iters_tot = dev_s, float(iters)
+        dev_s_max, iters_tot, tsteps_tot = dev_s, float(iters), float(tsteps)
     value = iters_tot / dev_s_max
     nsamp, ms3, el_s = b.phase_timings()
     final_mixed = b.all_triads().copy()
@@ -345,17 +346,19 @@ def main():
     if not args.no_extras and rank == 0:
         # ---- plain per-model FP64 GPU path on a sample --------------------------------
         idx = np.linspace(0, len(mods) - 1, min(args.plain_sample, len(mods))).astype(int)
-        p_it, p_s = 0, 0.0
+        p_it, p_s, p_ts = 0, 0.0, 0
         for k in idx:
             bp = Batch([mods[k]], mixed=False)
             st = bp.run()
             p_it += st["newton_iterations"]
+            p_ts += st["time_steps"]
             p_s += st["device_us"] * 1e-6
             bp.close()
         plain_rate = p_it / p_s
-        extras["plain_fp64_per_model"] = {"value": plain_rate, "unit": UNIT,
+        extras["plain_fp64_per_model"] = {"value": plain_rate, "unit": UNIT, "time_steps_per_s": p_ts / p_s,
                                           "sample": f"{len(idx)} of {len(mods)} models run one at a time"}
         extras["speedup_vs_plain"] = value / plain_rate
+        extras["speedup_vs_plain_time_steps"] = (tsteps_tot / dev_s_max) / (p_ts / p_s)
         # ---- CPU oracle on a bounded sample ---------------------------------------------
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
         threads = os.cpu_count() or 1
@@ -389,6 +392,8 @@ def main():
                            "(element matrices and state of all models ~%.2f GB)" % (n_el * 5200 / 1e9),
                            "host_setup_s": setup_s},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "time_steps_per_s": tsteps_tot / dev_s_max,
+                "newton_iterations_per_time_step": iters_tot / max(tsteps_tot, 1.0),
                 "gpu_launches": kernels * batched, "kernels_per_batched_iteration": kernels,
                 "batched_iterations": batched, "models_failed": failed,
                 "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof}

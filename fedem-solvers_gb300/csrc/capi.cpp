@@ -348,7 +348,7 @@ int fgpu_batch_create(int n, fgpu_model* const* models, int mixed, int sweeps, f
   }
   EngineOptions opt;
   opt.fp32Factor = mixed != 0;
-  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 3 : 1);
+  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 2 : 1);
   std::string err;
   int rc = b->engine.upload(b->models, opt, err);
   if (!rc) rc = b->engine.initialState(err);
@@ -456,7 +456,7 @@ int fgpu_server_create(double budget, int mixed, int sweeps, int maxModels, int 
   if (!out) return fail(-1, "null output handle");
   EngineOptions opt;
   opt.fp32Factor = mixed != 0;
-  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 3 : 1);
+  opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 2 : 1);
   auto* s = new fgpu_server{Server((size_t)(budget > 0 ? budget : 64.0e9), opt, maxModels, 4)};
   s->srv.setBatchingWindow(minBatch, maxWait);
   *out = s;

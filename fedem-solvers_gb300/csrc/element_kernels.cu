@@ -127,16 +127,25 @@ __global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl) {
     m.iter[i] = 0;
     m.nSeqNoUpd[i] = 0;
     m.negPiv[i] = 0;
-    m.pc[4 * i + 0] = ga / be - 1.0;
-    m.pc[4 * i + 1] = (0.5 * ga / be - 1.0) * dt;
-    m.pc[4 * i + 2] = 1.0 / (be * dt);
-    m.pc[4 * i + 3] = 0.5 / be - 1.0;
-    m.sacc[i] = 1.0 / (be * dt * dt);
-    m.svel[i] = ga / (be * dt);
-    m.state[i] = ST_ITER;
     fl = FL_ACTIVE | FL_PRED;
+    if (t + dt < m.tQs[i] + 0.1 * m.minInc[i]) {
+      // quasi-static load step (solverModule.f90:826-841, isQuasiStatic)
+      fl |= FL_QSTATIC;
+      if (m.fixedIt[i] == -1) fl |= FL_LINEAR;
+      m.qsCount[i] += 1;
+    } else {
+      if (m.qsCount[i] > 0) fl |= FL_QS2DYN;
+      m.qsCount[i] = 0;
+      m.pc[4 * i + 0] = ga / be - 1.0;
+      m.pc[4 * i + 1] = (0.5 * ga / be - 1.0) * dt;
+      m.pc[4 * i + 2] = 1.0 / (be * dt);
+      m.pc[4 * i + 3] = 0.5 / be - 1.0;
+      m.sacc[i] = 1.0 / (be * dt * dt);
+      m.svel[i] = ga / (be * dt);
+    }
+    m.state[i] = ST_ITER;
   } else if (st == ST_ITER) {
-    fl = FL_ACTIVE;
+    fl = FL_ACTIVE | (m.flags[i] & (FL_QSTATIC | FL_LINEAR));
   } else {
     m.flags[i] = 0;
     return;
@@ -146,6 +155,7 @@ __global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl) {
   if (tangent) {
     fl |= FL_TANGENT;
     double sK = m.alpha[i] + 1.0, sC = m.svel[i] * sK, sM = m.sacc[i];
+    if (fl & FL_QSTATIC) { sM = 0.0; sK = 1.0; sC = 0.0; }  // stiffness only
     double* sn = m.scaleN + 3 * i;
     if (fabs(sM - sn[0]) + fabs(sK - sn[1]) + fabs(sC - sn[2]) > 1.0e-16) {
       sn[0] = sM; sn[1] = sK; sn[2] = sC;
@@ -162,11 +172,19 @@ __global__ void kPredictDofs(DevData d) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ndofTot) {
     int m = d.dofModel[i];
-    if (d.m.flags[m] & FL_PRED) {
+    const int fl = d.m.flags[m];
+    if ((fl & FL_PRED) && !(fl & FL_QSTATIC)) {
       const double* pc = d.m.pc + 4 * m;
       double v = d.urd[i], a = d.urdd[i];
+      if (fl & FL_QS2DYN) {
+        // starting velocity after quasi-static steps (solverModule.f90:850)
+        v = d.rinc[i] / d.m.dt[m];
+        d.urd[i] = v;
+      }
       d.dk[i] = pc[0] * v + pc[1] * a;
       d.ak[i] = pc[2] * v + pc[3] * a;
+      d.rinc[i] = 0.0;
+    } else if (fl & FL_PRED) {
       d.rinc[i] = 0.0;
     }
   }
@@ -176,7 +194,9 @@ __global__ void kPredictDofs(DevData d) {
       // FIactual = FIk of the converged previous step (NewmarkFlag = 0)
       double s = 0.0;
       const double* FI = d.Fel + (size_t)24 * d.nelTot;
-      for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) s += FI[d.eqSrc[k]];
+      const int beamLim = 12 * d.nelTot;  // axial elements have no inertia forces
+      for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k)
+        if (d.eqSrc[k] < beamLim) s += FI[d.eqSrc[k]];
       d.FIact[i] = s;
     }
   }
@@ -258,7 +278,9 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   } else if (mode == EM_STATIC || mode == EM_STATIC_INIT) {
     if (!(fl & FL_STATIC)) return;
   }  // EM_FINAL: every model
-  const bool isStatic = mode == EM_STATIC || mode == EM_STATIC_INIT;
+  // quasi-static steps: no velocity terms; pure linear ones keep the frame
+  const bool qs = (mode == EM_PRED || mode == EM_INC) && (fl & FL_QSTATIC);
+  const bool isStatic = mode == EM_STATIC || mode == EM_STATIC_INIT || qs;
   double S[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) S[k] = d.supTr[(size_t)k * nel + e];
@@ -282,7 +304,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
       }
     }
   }
-  const bool newPositions = mode == EM_INC || mode == EM_STATIC || mode == EM_FINAL;
+  const bool newPositions = (mode == EM_INC || mode == EM_STATIC || mode == EM_FINAL) && !(qs && (fl & FL_LINEAR));
   double fin[12];
   if (newPositions) {
     // corotated frame through the three reference points (shadowPosAlg = 1)
@@ -319,7 +341,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) d.supTr[(size_t)k * nel + e] = S[k];
   }
-  if (newPositions || mode == EM_STATIC_INIT) {
+  if (newPositions || mode == EM_STATIC_INIT || qs) {
     // deformation vector in the corotated axes
     double inv[12];
 #pragma unroll
@@ -361,7 +383,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   // Fs = stifScl * K * finit.  The predictor pass keeps the frame and the
   // deformation of the converged previous step, so FS and Q stored by the
   // last pass are already the values UpdateSupEls would recompute.
-  const bool keepFsQ = mode == EM_PRED;
+  const bool keepFsQ = mode == EM_PRED && !qs;
   if (!keepFsQ) {
     elemMatvec(d, 0, e, fin, ss, y);
     rotateStore(S, y, FSo, nel, e);
@@ -416,6 +438,130 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   rotateStore(S, y, Qo, nel, e);
 }
 
+// axial springs and dampers: direction, length, forces (UpdateSprings/UpdateDampers,
+// calcSpringForces, addInDampingForces, calcDamperForces); same pass gating as kElements
+__global__ void kAxial(DevData d, int mode) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nax = d.naxTot;
+  if (a >= nax) return;
+  const int m = d.axModel[a], fl = d.m.flags[m];
+  if (mode == EM_PRED) {
+    if (!(fl & FL_PRED)) return;
+  } else if (mode == EM_INC) {
+    if (!(fl & FL_ACTIVE)) return;
+  } else if (mode == EM_STATIC || mode == EM_STATIC_INIT) {
+    if (!(fl & FL_STATIC)) return;
+  }
+  const bool qs = (mode == EM_PRED || mode == EM_INC) && (fl & FL_QSTATIC);
+  const bool isStatic = mode == EM_STATIC || mode == EM_STATIC_INIT || qs;
+  const int t1 = d.axTri[a], t2 = d.axTri[nax + a];
+  const double* U1 = d.ur + 12 * (size_t)t1;
+  const double* U2 = d.ur + 12 * (size_t)t2;
+  double dv[3] = {U2[9] - U1[9], U2[10] - U1[10], U2[11] - U1[11]}, n[3];
+  const double l2 = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+  const double L = sqrt(l2);
+  const bool spring = d.axKind[a] == 0;
+  if (l2 < 1.0e-16) {
+    if (spring) {
+      atomicOr(&d.m.status[m], SS_COROT);  // the two points defining the spring coincide
+      return;
+    }
+    n[0] = n[1] = n[2] = 0.0;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) n[k] = dv[k] / L;
+  }
+  double v1[3] = {0, 0, 0}, v2[3] = {0, 0, 0};
+  if (!isStatic) {
+    const double* vs = mode == EM_PRED ? d.dk : d.urd;  // predicted velocities in the predictor
+    const int f1 = d.triFirstDof[t1], f2 = d.triFirstDof[t2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { v1[k] = vs[f1 + k]; v2[k] = vs[f2 + k]; }
+  }
+  double fs[6] = {0, 0, 0, 0, 0, 0}, fd[6] = {0, 0, 0, 0, 0, 0};
+  if (spring) {
+    const double F = d.axS0[a] * (L - d.axL0[a]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      fs[k] = 0.0 - F * n[k];
+      fs[3 + k] = 0.0 + F * n[k];
+    }
+    const double al = d.axAlpha2[a];
+    if (!isStatic && fabs(al) > 1.0e-16) {
+      const double km = d.axS0[a] * al * L / L;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        double f1 = 0.0, f2 = 0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f1 += n[i] * n[j] * km * v1[j];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f1 += -(n[i] * n[j] * km) * v2[j];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f2 += -(n[i] * n[j] * km) * v1[j];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) f2 += n[i] * n[j] * km * v2[j];
+        fd[i] = f1;
+        fd[3 + i] = f2;
+      }
+    }
+  } else {
+    const double vr[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
+    const double F = d.axD0[a] * (n[0] * vr[0] + n[1] * vr[1] + n[2] * vr[2]);
+    if (!isStatic)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        fd[k] = -F * n[k];
+        fd[3 + k] = -fd[k];
+      }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d.axN[(size_t)k * nax + a] = n[k];
+  d.axLen[a] = L;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    d.FelA[(size_t)k * nax + a] = fs[k];
+    d.FelA[(size_t)(6 + k) * nax + a] = fd[k];
+  }
+}
+
+// axial element Newton matrices [A -A; -A A], A = n n^T (s0 (sK + sC alpha2)) for a
+// spring (calcSpringStiffness, no geometric stiffness) or n n^T d0 sC for a damper
+// (addInDamperMat)
+__global__ void kAxialNewton(DevData d) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nax = d.naxTot;
+  if (a >= nax) return;
+  const int m = d.axModel[a];
+  if (!(d.m.flags[m] & FL_TANGENT)) return;
+  const double* sn = d.m.scaleN + 3 * m;  // sM, sK, sC
+  const double sK = sn[1], sC = sn[2];
+  double n[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) n[k] = d.axN[(size_t)k * nax + a];
+  const double L = d.axLen[a];
+  double A[9];
+  if (d.axKind[a] == 0) {
+    const double km = (d.axS0[a] * (sK + sC * d.axAlpha2[a])) * L / L;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) A[i + 3 * j] = n[i] * n[j] * km;
+  } else {
+    const double c = d.axD0[a];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) A[i + 3 * j] = n[i] * n[j] * c * sC;
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double v = A[(i % 3) + 3 * (j % 3)];
+      d.elMatA[(size_t)(i + 6 * j) * nax + a] = (i / 3 == j / 3) ? v : -v;
+    }
+}
+
 // residual: force predictor (7.53) or corrector (7.55); RHS del = residual
 __global__ void kResidual(DevData d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,14 +569,19 @@ __global__ void kResidual(DevData d) {
   int m = d.eqModel[i];
   int fl = d.m.flags[m];
   if (!(fl & FL_ACTIVE)) return;
-  const size_t blk = (size_t)12 * d.nelTot;
+  const size_t blk = (size_t)12 * d.nelTot, ablk = (size_t)6 * d.naxTot;
   double fs = 0.0, fd = 0.0, fi = 0.0, q = 0.0;
   for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) {
     size_t s = d.eqSrc[k];
-    fs += d.Fel[s];
-    fd += d.Fel[s + blk];
-    fi += d.Fel[s + 2 * blk];
-    q += d.Fel[s + 3 * blk];
+    if (s < blk) {
+      fs += d.Fel[s];
+      fd += d.Fel[s + blk];
+      fi += d.Fel[s + 2 * blk];
+      q += d.Fel[s + 3 * blk];
+    } else {  // axial spring/damper
+      fs += d.FelA[s - blk];
+      fd += d.FelA[s - blk + ablk];
+    }
   }
   q += d.qext[i];
   d.FSk[i] = fs;
@@ -438,7 +589,9 @@ __global__ void kResidual(DevData d) {
   d.FIk[i] = fi;
   d.Qk[i] = q;
   double a = d.m.alpha[m], sstif = a + 1.0, r;
-  if (fl & FL_PRED)
+  if (fl & FL_QSTATIC)  // staticEquilibriumModule.f90 (staticInt): Q alone in a pure linear step
+    r = ((fl & FL_LINEAR) && (fl & FL_PRED)) ? q : q - fs;
+  else if (fl & FL_PRED)
     r = sstif * (q - fs + fd) + fi - a * d.FIact[i];
   else
     r = sstif * (q - fs - fd) - fi - a * d.FIact[i];
@@ -496,13 +649,94 @@ __global__ void __launch_bounds__(128) kRotateElementNewton(DevData d) {
     }
 }
 
+// Beam batches in principal axes (26-value pattern): N = sM*M + sC*stifScl*C +
+// sK*stifScl*K built on the fly and rotated block by block.  Each 3x3 block of
+// N is diagonal (translations/rotations of one direction) or holds one
+// off-diagonal pair (bending coupling), so R B R^T costs 2-3 products per
+// entry instead of 6 for a dense block; only the 10 upper blocks are computed
+// and the lower ones written as their transposes (an exactly symmetric Ns).
+__device__ inline void storeBlock(double* out, int nel, int e, int bi, int bj, const double* S) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      out[(size_t)((3 * bi + r) + 12 * (3 * bj + c)) * nel + e] = S[r + 3 * c];
+      if (bi != bj) out[(size_t)((3 * bj + c) + 12 * (3 * bi + r)) * nel + e] = S[r + 3 * c];
+    }
+}
+
+// R diag(b) R^T (symmetric)
+__device__ inline void rotDiag(const double* R, double b0, double b1, double b2, double* S) {
+  double W[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) { W[r] = R[r] * b0; W[r + 3] = R[r + 3] * b1; W[r + 6] = R[r + 6] * b2; }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r <= c; ++r) {
+      double v = W[r] * R[c] + W[r + 3] * R[c + 3] + W[r + 6] * R[c + 6];
+      S[r + 3 * c] = v;
+      S[c + 3 * r] = v;
+    }
+}
+
+// R B R^T with B_12 = p, B_21 = q (0-based rows/cols 1 and 2), all else zero
+__device__ inline void rotPair(const double* R, double p, double q, double* S) {
+  double W1[3], W2[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) { W1[r] = R[r + 6] * q; W2[r] = R[r + 3] * p; }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) S[r + 3 * c] = W1[r] * R[c + 3] + W2[r] * R[c + 6];
+}
+
+__global__ void __launch_bounds__(128) kNewtonBeam(DevData d) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nel = d.nelTot;
+  if (e >= nel) return;
+  const int m = d.elModel[e];
+  if (!(d.m.flags[m] & FL_TANGENT)) return;
+  const double* sn = d.m.scaleN + 3 * m;
+  const double ss = d.stifScl[e];
+  const double sM = sn[0], sK = sn[1] * ss, sC = sn[2] * ss;
+  const bool hc = d.hasC[e];
+  double a[26];
+#pragma unroll
+  for (int k = 0; k < 26; ++k) {
+    const size_t ix = (size_t)k * nel + e;
+    double v = sM * d.M26[ix];
+    if (hc) v += sC * d.C26[ix];
+    v += sK * d.K26[ix];
+    a[k] = v;
+  }
+  double R[9], S[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = d.supTr[(size_t)k * nel + e];
+  double* out = d.elMat;
+  rotDiag(R, a[0], a[2], a[6], S);    storeBlock(out, nel, e, 0, 0, S);
+  rotPair(R, a[3], a[7], S);          storeBlock(out, nel, e, 0, 1, S);
+  rotDiag(R, a[1], a[4], a[8], S);    storeBlock(out, nel, e, 0, 2, S);
+  rotPair(R, a[5], a[9], S);          storeBlock(out, nel, e, 0, 3, S);
+  rotDiag(R, a[10], a[12], a[15], S); storeBlock(out, nel, e, 1, 1, S);
+  rotPair(R, a[13], a[16], S);        storeBlock(out, nel, e, 1, 2, S);
+  rotDiag(R, a[11], a[14], a[17], S); storeBlock(out, nel, e, 1, 3, S);
+  rotDiag(R, a[18], a[19], a[21], S); storeBlock(out, nel, e, 2, 2, S);
+  rotPair(R, a[20], a[22], S);        storeBlock(out, nel, e, 2, 3, S);
+  rotDiag(R, a[23], a[24], a[25], S); storeBlock(out, nel, e, 3, 3, S);
+}
+
 // CSR slot gather (deterministic segmented reduction over element contributions)
 __global__ void kCsrGather(DevData d) {
   long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.nslotTot) return;
   if (!(d.m.flags[d.slotModel[s]] & FL_TANGENT)) return;
   double v = 0.0;
-  for (long long k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) v += d.elMat[d.slotSrc[k]];
+  const int64_t lim = (int64_t)144 * d.nelTot;
+  for (long long k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) {
+    const int64_t src = d.slotSrc[k];
+    v += src < lim ? d.elMat[src] : d.elMatA[src - lim];
+  }
   d.csrVal[s] = v;
 }
 
@@ -511,18 +745,26 @@ __global__ void kIncrement(DevData d) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ndofTot) {
     int m = d.dofModel[i];
-    if (d.m.flags[m] & FL_ACTIVE) {
+    const int fl = d.m.flags[m];
+    if (fl & FL_ACTIVE) {
       int eq = d.meqn[i];
-      // corrector steps replace prescribed values by zero; fixed DOFs are zero
-      double s0 = eq >= 0 ? d.del[eq] : 0.0;
-      double sv = d.m.svel[m], sa = d.m.sacc[m];
+      // prescribed DOFs take their constraint value in the predictor and zero in
+      // corrector steps (solExtensionModule.f90:1352-1387); fixed DOFs are zero
+      double s0 = eq >= 0 ? d.del[eq]
+                          : (eq <= -2 && (fl & FL_PRED)) ? d.motCc[d.modelMotOff[m] - 2 - eq] : 0.0;
       d.sinc0[i] = s0;
-      d.sinc1[i] = s0 * sv;
-      d.sinc2[i] = s0 * sa;
       double ri = d.rinc[i] + s0;
       d.rinc[i] = ri;
-      d.urd[i] = sv * ri - d.dk[i];
-      d.urdd[i] = sa * ri - d.ak[i];
+      if (fl & FL_QSTATIC) {
+        d.sinc1[i] = 0.0;
+        d.sinc2[i] = 0.0;
+      } else {
+        double sv = d.m.svel[m], sa = d.m.sacc[m];
+        d.sinc1[i] = s0 * sv;
+        d.sinc2[i] = s0 * sa;
+        d.urd[i] = sv * ri - d.dk[i];
+        d.urdd[i] = sa * ri - d.ak[i];
+      }
     }
   }
   if (i < d.ntriTot) {
@@ -530,9 +772,10 @@ __global__ void kIncrement(DevData d) {
     if ((d.m.flags[m] & FL_ACTIVE) && d.triNdof[i] > 0) {
       double inc[6] = {0, 0, 0, 0, 0, 0};
       int d0 = d.triFirstDof[i], nd = d.triNdof[i];
+      const bool pred = d.m.flags[m] & FL_PRED;
       for (int k = 0; k < nd && k < 6; ++k) {
         int eq = d.meqn[d0 + k];
-        inc[k] = eq >= 0 ? d.del[eq] : 0.0;
+        inc[k] = eq >= 0 ? d.del[eq] : (eq <= -2 && pred) ? d.motCc[d.modelMotOff[m] - 2 - eq] : 0.0;
       }
       double* U = d.ur + 12 * (size_t)i;
       for (int r = 0; r < 3; ++r) U[9 + r] += inc[r];
@@ -544,6 +787,54 @@ __global__ void kIncrement(DevData d) {
         for (int k = 0; k < 9; ++k) U[k] = O[k];
       }
     }
+  }
+}
+
+// prescribed deflections at the start of a step (motionRoutinesModule.f90:58-193):
+// cc = D - Dprev, or the total D in a linear quasi-static step
+__global__ void kMotions(DevData d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.nmotTot) return;
+  const int m = d.motModel[k], fl = d.m.flags[m];
+  if (!(fl & FL_PRED)) return;
+  const double D = d.motD0[k] + d.motD1[k] * (d.motEA[k] * d.m.time[m] + d.motEB[k]);
+  d.motCc[k] = (fl & FL_LINEAR) ? D : D - d.motD[k];
+  d.motD[k] = D;
+}
+
+// predictor right-hand side: the prescribed values times the Newton matrix
+// columns of the prescribed DOFs, moved to the right-hand side (terms with
+// |cc| <= 1e-15 skipped, sysMatrixTypeModule.f90:2099-2259)
+__global__ void kMotionRhs(DevData d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.nmrTot) return;
+  const int eq = d.mrEq[k];
+  if (!(d.m.flags[d.eqModel[eq]] & FL_PRED)) return;
+  double b = d.del[eq];
+  for (int64_t q = d.mrPtr[k]; q < d.mrPtr[k + 1]; ++q) {
+    const double c = d.motCc[d.mrMot[q]];
+    const int64_t src = d.mrSrc[q], lim = (int64_t)144 * d.nelTot;
+    if (fabs(c) > 1.0e-15) b -= c * (src < lim ? d.elMat[src] : d.elMatA[src - lim]);
+  }
+  d.del[eq] = b;
+}
+
+// a pure linear quasi-static step restarts from the state after the initial
+// configuration (restoreLastStep, solverRoutinesModule.f90:920-970)
+__global__ void kQsRestore(DevData d) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int want = FL_PRED | FL_QSTATIC | FL_LINEAR;
+  if (i < d.ntriTot && (d.m.flags[d.triModel[i]] & want) == want)
+    for (int k = 0; k < 12; ++k) d.ur[12 * i + k] = d.urQs[12 * i + k];
+  if (i < d.nelTot && (d.m.flags[d.elModel[i]] & want) == want)
+    for (int k = 0; k < 12; ++k) {
+      size_t ix = (size_t)k * d.nelTot + i;
+      d.supTr[ix] = d.supTrQs[ix];
+      d.finit[ix] = d.finitPrev[ix];
+    }
+  if (i < d.ndofTot && (d.m.flags[d.dofModel[i]] & want) == want) {
+    d.urd[i] = d.urdQs[i];
+    d.urdd[i] = d.urddQs[i];
   }
 }
 
@@ -649,19 +940,27 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
 }
 
 // norms, convergence test (normTypeModule.f90:196-249) and iteration counters
+// one warp per model: lane k combines partial value k over the model's chunks
+// in chunk order, lane 0 evaluates the norms and the test
 __global__ void kControl(DevData d) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (m >= d.m.n) return;
   const int fl = d.m.flags[m];
   if (!(fl & FL_ACTIVE)) return;
-  double v[NPART];
   const int c0 = d.modelChunkOff[m], nc = d.modelNchunk[m];
-  for (int k = 0; k < NPART; ++k) v[k] = nc > 0 ? d.partial[(size_t)c0 * NPART + k] : 0.0;
-  for (int c = 1; c < nc; ++c)
-    for (int k = 0; k < NPART; ++k) {
-      double x = d.partial[(size_t)(c0 + c) * NPART + k];
-      v[k] = (k <= 6) ? v[k] + x : fmax(v[k], x);
+  double acc = 0.0;
+  if (lane < NPART) {
+    acc = nc > 0 ? d.partial[(size_t)c0 * NPART + lane] : 0.0;
+    for (int c = 1; c < nc; ++c) {
+      double x = d.partial[(size_t)(c0 + c) * NPART + lane];
+      acc = (lane <= 6) ? acc + x : fmax(acc, x);
     }
+  }
+  double v[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) v[k] = __shfl_sync(0xffffffffu, acc, k);
+  if (lane != 0) return;
   double* nv = d.m.normVal + 18 * m;
   nv[0] = v[0] > 0 ? sqrt(v[2] / v[0]) : 0.0;
   nv[4] = v[0] > 0 ? sqrt(v[3] / v[0]) : 0.0;
@@ -686,6 +985,8 @@ __global__ void kControl(DevData d) {
   if (v[20] > 0.0 || (d.m.status[m] & (SS_SINGULAR | SS_COROT | SS_TIMEOUT))) {
     d.m.status[m] |= v[20] > 0.0 ? SS_NAN : 0;
     d.m.state[m] = ST_ERROR;
+  } else if (fl & FL_LINEAR) {
+    conv = it == d.linearIters;  // pure linear quasi-static step: one solve (+ refinement)
   } else if (d.m.fixedIt[m] > 0) {
     conv = it == d.m.fixedIt[m];
   } else if (it > d.m.maxIt[m]) {
@@ -718,7 +1019,8 @@ __global__ void kStepEnd(DevData d) {
     if ((d.m.flags[d.triModel[i]] & FL_STEPDONE) && d.triNdof[i] == 6) orthonormRot(d.ur + 12 * (size_t)i);
   }
   if (i < d.nelTot) {
-    if (d.m.flags[d.elModel[i]] & FL_STEPDONE)
+    const int fl = d.m.flags[d.elModel[i]];
+    if ((fl & FL_STEPDONE) && !(fl & FL_LINEAR))
 #pragma unroll
       for (int c = 0; c < 12; ++c) {
         size_t ix = (size_t)c * d.nelTot + i;
@@ -753,8 +1055,12 @@ __global__ void kStaticResidual(DevData d) {
   const size_t blk = (size_t)12 * d.nelTot;
   for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) {
     size_t s = d.eqSrc[k];
-    fs += d.Fel[s];
-    q += d.Fel[s + 3 * blk];
+    if (s < blk) {
+      fs += d.Fel[s];
+      q += d.Fel[s + 3 * blk];
+    } else {
+      fs += d.FelA[s - blk];
+    }
   }
   q += d.qext[i];
   d.FSk[i] = fs;
@@ -855,15 +1161,19 @@ void launchPredictDofs(const DevData& d, cudaStream_t s) {
 }
 void launchElements(const DevData& d, int mode, cudaStream_t s) {
   if (d.nelTot > 0) kElements<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d, mode);
+  if (d.naxTot > 0) kAxial<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d, mode);
 }
 void launchResidual(const DevData& d, cudaStream_t s) {
   if (d.neqTot > 0) kResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);
 }
 void launchBuildElementNewton(const DevData& d, cudaStream_t s) {
-  if (d.nelTot > 0) kBuildElementNewton<<<blocksFor(d.nelTot), TPB, 0, s>>>(d);
+  // compressed beam batches build N inside kNewtonBeam
+  if (d.nelTot > 0 && !d.beamSparse) kBuildElementNewton<<<blocksFor(d.nelTot), TPB, 0, s>>>(d);
 }
 void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
-  if (d.nelTot > 0) kRotateElementNewton<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
+  if (d.nelTot > 0 && d.beamSparse) kNewtonBeam<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
+  else if (d.nelTot > 0) kRotateElementNewton<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
+  if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
   if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot), TPB, 0, s>>>(d);
@@ -874,9 +1184,20 @@ void launchIncrement(const DevData& d, cudaStream_t s) {
 }
 void launchNormsControl(const DevData& d, cudaStream_t s) {
   if (d.nchunkTot > 0) kNormsPartial<<<d.nchunkTot, CHUNK_TPB, 0, s>>>(d);
-  kControl<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d);
+  kControl<<<blocksFor(32LL * d.m.n, 128), 128, 0, s>>>(d);
   long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
   kStepEnd<<<blocksFor(n), TPB, 0, s>>>(d);
+}
+void launchMotions(const DevData& d, cudaStream_t s) {
+  if (d.nmotTot > 0) kMotions<<<blocksFor(d.nmotTot, 128), 128, 0, s>>>(d);
+}
+void launchMotionRhs(const DevData& d, cudaStream_t s) {
+  if (d.nmrTot > 0) kMotionRhs<<<blocksFor(d.nmrTot, 128), 128, 0, s>>>(d);
+}
+void launchQsRestore(const DevData& d, cudaStream_t s) {
+  if (!d.urQs) return;
+  long long n = std::max<long long>(std::max<long long>(d.ntriTot, d.nelTot), d.ndofTot);
+  kQsRestore<<<blocksFor(n), TPB, 0, s>>>(d);
 }
 void launchStaticBegin(const DevData& d, int* activeCount, cudaStream_t s) {
   kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount);

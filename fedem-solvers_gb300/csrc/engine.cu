@@ -84,12 +84,15 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   std::vector<int> frontOff(nm, 0);
   std::vector<int64_t> contribOff(nm, 0), eqContribOff(nm, 0), rowsOff(nm, 0), lOff(nm, 0), uOff(nm, 0),
       wOff(nm, 0), childOff(nm, 0), relOff(nm, 0), asmOff(nm, 0);
-  int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, maxH = 0;
+  int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, maxH = 0, nax = 0;
+  std::vector<int> modelAxOff(nm, 0);
   int64_t nslot = 0, ncontrib = 0, neqc = 0, nrows = 0, nl = 0, nu = 0, nw = 0, nch = 0, nrel = 0, nasm = 0;
   bool anyC = false;
   for (int k = 0; k < nm; ++k) {
     const HostModel& h = *models[k];
     modelTriOff_[k] = ntri; modelDofOff_[k] = ndof; modelEqOff_[k] = neq; modelElOff_[k] = nel;
+    modelAxOff[k] = nax;
+    nax += h.nax;
     modelSlotOff_[k] = nslot; frontOff[k] = nfr; contribOff[k] = ncontrib; eqContribOff[k] = neqc;
     rowsOff[k] = nrows; lOff[k] = nl; uOff[k] = nu; wOff[k] = nw; childOff[k] = nch; relOff[k] = nrel;
     asmOff[k] = nasm;
@@ -100,7 +103,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     maxH = std::max(maxH, h.maxHeight);
     for (uint8_t c : h.hasC) anyC |= c != 0;
   }
-  if (12LL * nel > INT_MAX || neqc > INT_MAX) { err = "batch too large for 32-bit gather indices"; return -901; }
+  if (12LL * nel + 6LL * nax > INT_MAX || neqc > INT_MAX) { err = "batch too large for 32-bit gather indices"; return -901; }
+  d_.naxTot = nax;
   d_.ntriTot = ntri; d_.ndofTot = ndof; d_.neqTot = neq; d_.nelTot = nel; d_.nslotTot = nslot;
   d_.nfrontTot = nfr;
   // ---- per-model control -------------------------------------------------------
@@ -109,7 +113,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   auto iv = [&](std::vector<int>& v) { v.assign(nm, 0); };
   std::vector<int> triOff(nm), ntriV(nm), dofOff(nm), ndofV(nm), eqOff(nm), neqV(nm), elOff(nm), nelV(nm);
   std::vector<double> tStart(nm), tEnd(nm), dt(nm), minInc(nm), alpha(nm), beta(nm), gamma(nm), wD(3 * nm),
-      wF(3 * nm), grav(3 * nm), tolV(18 * nm), scaleN(3 * nm, -1.0), equTol(nm), equLim(nm);
+      wF(3 * nm), grav(3 * nm), tolV(18 * nm), scaleN(3 * nm, -1.0), equTol(nm), equLim(nm), tQs(nm);
   std::vector<int> tolC(18 * nm), maxIt(nm), minIt(nm), fixedIt(nm), nUpdat(nm), maxSeq(nm), staticMode(nm),
       staticDone(nm);
   std::vector<long long> stepLimit(nm, LLONG_MAX);
@@ -128,6 +132,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     equTol[k] = eqTol; equLim[k] = eqLim;
     staticMode[k] = (eqLim > 0.0 && h.neq > 0) ? (eqTol > 0.0 ? 2 : 1) : 0;
     staticDone[k] = staticMode[k] == 0 ? 1 : 0;
+    tQs[k] = c.tQStatic;
   }
 #define UP_I(field, vec) if (!(M.field = alloc<int>(nm)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
 #define UP_D(field, vec, n) if (!(M.field = alloc<double>(n)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
@@ -136,7 +141,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   UP_D(time, tStart, nm); UP_D(dt, dt, nm); UP_D(tStart, tStart, nm); UP_D(tEnd, tEnd, nm);
   UP_D(minInc, minInc, nm); UP_D(alpha, alpha, nm); UP_D(beta, beta, nm); UP_D(gamma, gamma, nm);
   UP_D(scaleN, scaleN, 3 * nm); UP_D(wDisp, wD, 3 * nm); UP_D(wForce, wF, 3 * nm); UP_D(gravity, grav, 3 * nm);
-  UP_D(tolVal, tolV, 18 * nm); UP_D(equTol, equTol, nm); UP_D(equLim, equLim, nm);
+  UP_D(tolVal, tolV, 18 * nm); UP_D(equTol, equTol, nm); UP_D(equLim, equLim, nm); UP_D(tQs, tQs, nm);
   if (!(M.tolCode = alloc<int>(18 * nm)) || put(M.tolCode, tolC, stream_) != cudaSuccess) { err = "alloc tolCode"; return -902; }
   UP_I(maxIt, maxIt); UP_I(minIt, minIt); UP_I(fixedIt, fixedIt); UP_I(nUpdat, nUpdat); UP_I(maxSeq, maxSeq);
   UP_I(staticMode, staticMode); UP_I(staticDone, staticDone);
@@ -147,6 +152,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   M.state = alloc<int>(nm); M.flags = alloc<int>(nm); M.status = alloc<int>(nm); M.iter = alloc<int>(nm);
   M.nSeqNoUpd = alloc<int>(nm); M.negPiv = alloc<int>(nm); M.staticIter = alloc<int>(nm); M.staticNinc = alloc<int>(nm);
   M.nStep = alloc<long long>(nm); M.nIter = alloc<long long>(nm); M.stepLimit = alloc<long long>(nm);
+  M.qsCount = alloc<int>(nm);
   if (put(M.stepLimit, stepLimit, stream_) != cudaSuccess) { err = "upload stepLimit"; return -902; }
 
   // ---- triads, DOFs, equations ---------------------------------------------------
@@ -163,7 +169,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       triModel.push_back(k);
     }
     for (int i = 0; i < h.ndof; ++i) {
-      meqn.push_back(h.meqn[i] >= 0 ? h.meqn[i] + modelEqOff_[k] : -1);
+      meqn.push_back(h.meqn[i] >= 0 ? h.meqn[i] + modelEqOff_[k] : h.meqn[i]);
       dofType.push_back(h.dofType[i]);
       dofModel.push_back(k);
     }
@@ -175,6 +181,51 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   UPV(d_.triFirstDof, int, triFirst); UPV(d_.triNdof, int, triNd); UPV(d_.triModel, int, triModel);
   UPV(d_.meqn, int, meqn); UPV(d_.dofType, int, dofType); UPV(d_.dofModel, int, dofModel);
   UPV(d_.eqModel, int, eqModel); UPV(d_.qext, double, qext);
+  {
+    // prescribed deflections and their predictor right-hand-side terms
+    std::vector<int> motModel, motOff(nm), mrEq, mrMot;
+    std::vector<double> d0, d1, eA, eB, D0;
+    std::vector<int64_t> mrPtr(1, 0), mrSrc;
+    bool anyLinearQs = false;
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      motOff[k] = (int)motModel.size();
+      for (size_t j = 0; j < h.motD0.size(); ++j) {
+        motModel.push_back(k);
+        d0.push_back(h.motD0[j]); d1.push_back(h.motD1[j]); eA.push_back(h.motEA[j]); eB.push_back(h.motEB[j]);
+        // start-time value (updatePrescribedMotionsB, motionRoutinesModule.f90:213-245)
+        D0.push_back(h.motD0[j] + h.motD1[j] * (h.motEA[j] * h.ctl.tStart + h.motEB[j]));
+      }
+      for (size_t q = 0; q < h.mrEq.size(); ++q) {
+        mrEq.push_back(h.mrEq[q] + modelEqOff_[k]);
+        for (int t = h.mrPtr[q]; t < h.mrPtr[q + 1]; ++t) {
+          const int src = h.mrSrc[t];
+          if (src < 144 * h.nel) {
+            const int e = src / 144, entry = src % 144;
+            mrSrc.push_back((int64_t)entry * nel + e + modelElOff_[k]);
+          } else {
+            const int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
+            mrSrc.push_back((int64_t)144 * nel + (int64_t)entry * nax + modelAxOff[k] + a);
+          }
+          mrMot.push_back(h.mrMot[t] + motOff[k]);
+        }
+        mrPtr.push_back((int64_t)mrSrc.size());
+      }
+      anyLinearQs |= h.ctl.tQStatic > h.ctl.tStart && h.ctl.fixedIt == -1;
+    }
+    d_.nmotTot = (int)motModel.size();
+    d_.nmrTot = (int)mrEq.size();
+    UPV(d_.motModel, int, motModel); UPV(d_.modelMotOff, int, motOff);
+    UPV(d_.motD0, double, d0); UPV(d_.motD1, double, d1); UPV(d_.motEA, double, eA); UPV(d_.motEB, double, eB);
+    UPV(d_.motD, double, D0);
+    d_.motCc = alloc<double>(motModel.size());
+    UPV(d_.mrEq, int, mrEq); UPV(d_.mrMot, int, mrMot); UPV(d_.mrPtr, int64_t, mrPtr); UPV(d_.mrSrc, int64_t, mrSrc);
+    d_.linearIters = opt_.fp32Factor ? 3 : 1;
+    if (anyLinearQs) {
+      d_.urQs = alloc<double>(12 * (size_t)ntri); d_.supTrQs = alloc<double>(12 * (size_t)nel);
+      d_.urdQs = alloc<double>(ndof); d_.urddQs = alloc<double>(ndof);
+    }
+  }
   d_.urd = alloc<double>(ndof); d_.urdd = alloc<double>(ndof); d_.dk = alloc<double>(ndof); d_.ak = alloc<double>(ndof);
   d_.rinc = alloc<double>(ndof); d_.sinc0 = alloc<double>(ndof); d_.sinc1 = alloc<double>(ndof); d_.sinc2 = alloc<double>(ndof);
   d_.FSk = alloc<double>(neq); d_.FDk = alloc<double>(neq); d_.FIk = alloc<double>(neq); d_.Qk = alloc<double>(neq);
@@ -308,6 +359,28 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(d_.elTri, int, elTri); UPV(d_.elRef, int, elRef); UPV(d_.elModel, int, elModel);
     UPV(d_.stifScl, double, ss); UPV(d_.kDmp, double, kd); UPV(d_.hasC, uint8_t, hc); UPV(d_.hasVld, uint8_t, hv);
   }
+  // ---- axial springs and dampers ------------------------------------------------------
+  {
+    std::vector<uint8_t> kind(nax);
+    std::vector<int> tri(2 * (size_t)nax), axModel(nax);
+    std::vector<double> s0(nax), l0(nax), al(nax), d0(nax);
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      for (int a = 0; a < h.nax; ++a) {
+        const int g = modelAxOff[k] + a;
+        kind[g] = h.axKind[a];
+        for (int n = 0; n < 2; ++n) tri[(size_t)n * nax + g] = h.axTri[2 * a + n] + modelTriOff_[k];
+        axModel[g] = k;
+        s0[g] = h.axS0[a]; l0[g] = h.axL0[a]; al[g] = h.axAlpha2[a]; d0[g] = h.axD0[a];
+      }
+    }
+    UPV(d_.axKind, uint8_t, kind); UPV(d_.axTri, int, tri); UPV(d_.axModel, int, axModel);
+    UPV(d_.axS0, double, s0); UPV(d_.axL0, double, l0); UPV(d_.axAlpha2, double, al); UPV(d_.axD0, double, d0);
+    d_.axN = alloc<double>(3 * (size_t)nax);
+    d_.axLen = alloc<double>(nax);
+    d_.FelA = alloc<double>(12 * (size_t)nax);
+    d_.elMatA = alloc<double>(36 * (size_t)nax);
+  }
   // ---- CSR and gather maps -----------------------------------------------------------
   {
     std::vector<int64_t> rowPtr(neq + 1, 0), slotPtr(nslot + 1, 0), slotSrc;
@@ -328,12 +401,22 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         slotPtr[modelSlotOff_[k] + s + 1] = contribOff[k] + h.slotPtr[s + 1];
       }
       for (int src : h.slotSrc) {
-        int e = src / 144, entry = src % 144;
-        slotSrc.push_back((int64_t)entry * nel + modelElOff_[k] + e);
+        if (src < 144 * h.nel) {
+          int e = src / 144, entry = src % 144;
+          slotSrc.push_back((int64_t)entry * nel + modelElOff_[k] + e);
+        } else {  // axial element entry
+          int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
+          slotSrc.push_back((int64_t)144 * nel + (int64_t)entry * nax + modelAxOff[k] + a);
+        }
       }
       for (int src : h.eqSrc) {
-        int e = src / 12, loc = src % 12;
-        eqSrc.push_back(loc * nel + modelElOff_[k] + e);
+        if (src < 12 * h.nel) {
+          int e = src / 12, loc = src % 12;
+          eqSrc.push_back(loc * nel + modelElOff_[k] + e);
+        } else {
+          int a = (src - 12 * h.nel) / 6, loc = (src - 12 * h.nel) % 6;
+          eqSrc.push_back(12 * nel + loc * nax + modelAxOff[k] + a);
+        }
       }
     }
     UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int64_t, slotPtr);
@@ -405,8 +488,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       if (perWarpBytes > 200 * 1024) { err = "front too large for the shared-memory front kernels"; return -905; }
       levels_.push_back(lp);
     }
-    pplan_.order = dFlat;
-    pplan_.n = (int)flat.size();
     std::vector<int> leaves;
     for (int f = 0; f < nfr; ++f)
       if (nchild[f] == 0) leaves.push_back(f);
@@ -414,12 +495,21 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
     pplan_.nLeaves = (int)leaves.size();
-    pplan_.workCounter = alloc<int>(1);
     pplan_.maxRow = 1;
     for (const LevelPlan& lp : levels_) pplan_.maxRow = std::max(pplan_.maxRow, lp.maxRow);
+    pplan_.maxNpiv = 1;
+    for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
+    // longest leaf-to-root path: parents follow their children in each model's order
+    std::vector<int> pathLen(nfr, 1);
+    pplan_.maxPath = 1;
+    for (int f = nfr - 1; f >= 0; --f) {
+      if (parent[f] > f) pathLen[f] = pathLen[parent[f]] + 1;
+      else if (parent[f] >= 0) { err = "assembly tree not in post-order"; return -907; }
+      pplan_.maxPath = std::max(pplan_.maxPath, pathLen[f]);
+    }
     pplan_.cntFactor = alloc<int>(nfr);
     pplan_.cntForward = alloc<int>(nfr);
-    pplan_.readyBackward = alloc<int>(nfr);
+    pplan_.stateBackward = alloc<int>(nfr);
     pplan_.errFlag = alloc<int>(1);
     d_.errFlag = pplan_.errFlag;
   }
@@ -449,6 +539,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
                  M.staticDone})
     reg(p, sizeof(int) * nm);
   for (long long* p : {M.nStep, M.nIter, M.stepLimit}) reg(p, sizeof(long long) * nm);
+  reg(M.qsCount, sizeof(int) * nm);
+  if (d_.nmotTot > 0) {
+    reg(d_.motD, D * (size_t)d_.nmotTot);
+    reg(d_.motCc, D * (size_t)d_.nmotTot);
+  }
   uploadedBytes_ = t_putBytes;
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
@@ -501,31 +596,36 @@ void Engine::enqueueFactor(cudaStream_t s) {
 
 void Engine::enqueueSolve(cudaStream_t s) {
   const bool f32 = opt_.fp32Factor;
-  for (int sweep = 0; sweep < opt_.refineSweeps; ++sweep) {
+  const int sw = opt_.refineSweeps;
+  for (int sweep = 0; sweep < sw; ++sweep) {
     if (sweep > 0) launchRefineResidual(d_, s);
-    launchSolveSetup(d_, f32, sweep, s);
     if (opt_.persistent) {
-      launchForwardCascade(d_, pplan_, f32, s);
-      launchBackwardDynamic(d_, pplan_, f32, s);
+      // the right-hand side is read and the solution stored inside the two launches
+      launchForwardCascade(d_, pplan_, f32, (f32 && sweep > 0) ? d_.rref : d_.del, s);
+      launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
     } else {
+      launchSolveSetup(d_, f32, sweep, s);
       for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
       for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);
+      launchSolveAccumulate(d_, f32, s);
     }
-    launchSolveAccumulate(d_, f32, s);
   }
-  if (f32) launchSolveFinalize(d_, s);
+  if (f32 && !opt_.persistent) launchSolveFinalize(d_, s);
 }
 
 void Engine::enqueueIteration(cudaStream_t s) {
   cudaMemsetAsync(dActive_, 0, sizeof(int), s);
   cudaMemsetAsync(dActiveEl_, 0, sizeof(long long), s);
   launchBeginStep(d_, dActive_, dActiveEl_, s);
+  launchQsRestore(d_, s);
+  launchMotions(d_, s);
   launchPredictDofs(d_, s);
   launchElements(d_, EM_PRED, s);
   launchResidual(d_, s);
   launchBuildElementNewton(d_, s);
   launchRotateElementNewton(d_, s);
   launchCsrGather(d_, s);
+  launchMotionRhs(d_, s);
   cudaEventRecordWithFlags(ev_[0], s, cudaEventRecordExternal);
   enqueueFactor(s);
   cudaEventRecordWithFlags(ev_[1], s, cudaEventRecordExternal);
@@ -537,9 +637,15 @@ void Engine::enqueueIteration(cudaStream_t s) {
   cudaEventRecordWithFlags(ev_[4], s, cudaEventRecordExternal);
   launchNormsControl(d_, s);
   const int nl = opt_.persistent ? 1 : (int)levels_.size(), sw = opt_.refineSweeps;
-  // kernels per batched iteration: 10 fixed + factor levels + per sweep (setup, accumulate,
-  // forward and backward levels) + refinement residuals + mixed-precision finalise
-  launchesPerIter_ = 10 + nl + sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
+  // kernels per batched iteration: 12 fixed (begin step, predict, elements x2, residual,
+  // element Newton build + rotate (one fused kernel for compressed beams), CSR gather,
+  // increment, norms partial + control, step end)
+  // + factor launches + per sweep the forward and backward launches (per-height launches
+  // with separate set-up/accumulate kernels when not persistent) + refinement residuals
+  const int solveLaunches = opt_.persistent ? 2 * sw + (sw - 1)
+                                           : sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
+  launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
+                     (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0);
 }
 
 int Engine::readActive() {
@@ -574,6 +680,14 @@ int Engine::initialState(std::string& err) {
   FG_CHECK(cudaMemcpyAsync(d_.finitPrev, d_.finit, sizeof(double) * 12 * (size_t)d_.nelTot,
                            cudaMemcpyDeviceToDevice, stream_));
   FG_CHECK(cudaMemsetAsync(d_.rinc, 0, sizeof(double) * (size_t)d_.ndofTot, stream_));
+  if (d_.urQs) {
+    // the state pure linear quasi-static steps restart from
+    const size_t D = sizeof(double);
+    FG_CHECK(cudaMemcpyAsync(d_.urQs, d_.ur, D * 12 * (size_t)d_.ntriTot, cudaMemcpyDeviceToDevice, stream_));
+    FG_CHECK(cudaMemcpyAsync(d_.supTrQs, d_.supTr, D * 12 * (size_t)d_.nelTot, cudaMemcpyDeviceToDevice, stream_));
+    FG_CHECK(cudaMemcpyAsync(d_.urdQs, d_.urd, D * (size_t)d_.ndofTot, cudaMemcpyDeviceToDevice, stream_));
+    FG_CHECK(cudaMemcpyAsync(d_.urddQs, d_.urdd, D * (size_t)d_.ndofTot, cudaMemcpyDeviceToDevice, stream_));
+  }
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
   for (int k = 0; k < d_.m.n; ++k)

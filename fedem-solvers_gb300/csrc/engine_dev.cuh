@@ -14,7 +14,13 @@ namespace fgpu {
 // per-model state machine
 enum ModelState : int { ST_NEED_STEP = 0, ST_ITER = 1, ST_DONE = 2, ST_ERROR = 3 };
 // per-model flags for the current batched iteration
-enum ModelFlag : int { FL_ACTIVE = 1, FL_PRED = 2, FL_TANGENT = 4, FL_STATIC = 8, FL_REBUILD = 16, FL_STEPDONE = 32 };
+// FL_QSTATIC: a quasi-static load step (staticInt), FL_LINEAR: pure linear one
+// (numit = -1, restarted from the initial state), FL_QS2DYN: first dynamic step
+// after quasi-static ones (starting velocity rinc / dt)
+enum ModelFlag : int {
+  FL_ACTIVE = 1, FL_PRED = 2, FL_TANGENT = 4, FL_STATIC = 8, FL_REBUILD = 16, FL_STEPDONE = 32,
+  FL_QSTATIC = 64, FL_LINEAR = 128, FL_QS2DYN = 256
+};
 // per-model status bits
 enum ModelStatus : int { SS_SINGULAR = 1, SS_MAXIT = 2, SS_NAN = 4, SS_COROT = 8, SS_TIMEOUT = 16 };
 
@@ -33,6 +39,9 @@ struct DevModels {
   int *maxIt, *minIt, *fixedIt, *nUpdat, *maxSeq;
   int *state, *flags, *status, *iter, *nSeqNoUpd, *negPiv;
   long long *nStep, *stepLimit, *nIter;
+  // quasi-static load steps while time + dt < tQs; qsCount: such steps since the last dynamic one
+  double* tQs;
+  int* qsCount;
   // static equilibrium
   double *deln, *equTol, *equLim, *staticScale;
   int *staticIter, *staticNinc, *staticDone, *staticMode;  // staticMode: 0 none, 1 linear, 2 iterate
@@ -47,7 +56,7 @@ struct DevData {
   int *triFirstDof, *triNdof, *triModel;
   // DOF vectors
   double *urd, *urdd, *dk, *ak, *rinc, *sinc0, *sinc1, *sinc2;
-  int *meqn, *dofType, *dofModel;  // meqn: global equation or -1
+  int *meqn, *dofType, *dofModel;  // meqn: global equation, -1 fixed, -2 - k prescribed by model motion k
   // equation vectors
   double *FSk, *FDk, *FIk, *Qk, *qext, *FIact, *res, *del, *xref, *rref;
   float* rhs32;
@@ -84,6 +93,30 @@ struct DevData {
   double* x64;  // solve vector, global equations
   float* x32;
   int* errFlag;  // set by a kernel whose bounded wait ran out
+  // axial springs and dampers (SoA): kind (0 spring, 1 damper), triads [k * naxTot + a],
+  // model, constants; current direction axN (3) and length; element forces FelA
+  // (FS 6, FD 6) and Newton matrices elMatA (6x6, translational DOFs of both triads).
+  // Gather sources: eqSrc >= 12 * nelTot and slotSrc/mrSrc >= 144 * nelTot address
+  // FelA / elMatA with that offset removed.
+  int naxTot = 0;
+  uint8_t* axKind;
+  int *axTri, *axModel;
+  double *axS0, *axL0, *axAlpha2, *axD0, *axN, *axLen, *FelA, *elMatA;
+  // prescribed deflections: D(t) = d0 + d1 * (eA * t + eB); cc = constraint value of the
+  // current step (increment, or total in linear quasi-static steps)
+  int nmotTot = 0;
+  int *motModel, *modelMotOff;
+  double *motD0, *motD1, *motEA, *motEB, *motD, *motCc;
+  // predictor right-hand-side terms: del[mrEq[k]] -= cc[mrMot[q]] * elMat[mrSrc[q]]
+  int nmrTot = 0;
+  int *mrEq, *mrMot;
+  int64_t *mrPtr, *mrSrc;
+  // state linear quasi-static steps restart from (null when no model has such steps)
+  double *urQs, *supTrQs, *urdQs, *urddQs;
+  // iterations of a pure linear step: 1 with FP64 solves; with FP32 solves the
+  // single reference solve is followed by corrections against the FP64 residual
+  // Q - FS (iterative refinement of the same linear system)
+  int linearIters = 1;
   // DOF chunks for the two-stage norm reduction (each chunk within one model)
   int nchunkTot = 0;
   int *chunkModel, *chunkStart, *chunkEnd, *modelChunkOff, *modelNchunk;

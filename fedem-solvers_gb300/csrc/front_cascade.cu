@@ -6,10 +6,14 @@
 // is done, and the warp whose increment completes the count goes on with the
 // parent itself.  Nothing ever waits, so the launch is correct whatever the
 // residency (several engines may run concurrently on their own streams).
-// The backward solve runs top-down: blocks grab consecutive ranges of the
-// fronts sorted by decreasing height from a global counter, so every awaited
-// parent was grabbed earlier by a running block; each wait is bounded and
-// sets errFlag when it runs out.
+// The backward solve runs top-down along the leaf-to-root paths: the warp of
+// a leaf walks its path from the highest front not yet done down to the leaf,
+// claiming each front with a compare-and-swap before solving it.  A warp that
+// finds a front claimed by another warp waits for it; that warp is running and
+// solves the front without waiting on anything, so the wait ends whatever the
+// residency.  Each wait is still bounded and sets errFlag when it runs out.
+// The forward and backward solves stage each front's L block in shared memory
+// first (one burst of loads instead of one load latency per pivot).
 //
 // Front arithmetic is that of front_kernels.cu (SPRFC1/SPRFS1/SPRBS1
 // semantics, src/vpmCommon/vpmLinAlg/solExtensionModule.f90:153-505).
@@ -21,7 +25,9 @@ namespace {
 
 constexpr long long kSpinLimit = 1LL << 22;
 
-// partial LDL^T of front f in shared memory (F: maxRow^2, lcol/diag0: maxRow)
+// partial LDL^T of front f in shared memory (F: maxRow^2, lcol/diag0: maxRow).
+// Global loads are issued several per lane before they are used (the fronts
+// are small and latency-bound); the rank-1 updates run one row per lane.
 template <typename T>
 __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* Ubase, T* Lbase,
                                T* Uout0, double tolFact, int lane) {
@@ -31,7 +37,22 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
   __syncwarp();
   const int64_t ao = d.fAsmOff[f];
   const int na = d.fNasm[f];
-  for (int k = lane; k < na; k += 32) F[d.asmPos[ao + k]] = (T)d.csrVal[d.asmSlot[ao + k]];
+  for (int k0 = 0; k0 < na; k0 += 128) {
+    int64_t sl[4];
+    int ps[4];
+    double val[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = k0 + 32 * u + lane;
+      sl[u] = k < na ? d.asmSlot[ao + k] : -1;
+      ps[u] = k < na ? d.asmPos[ao + k] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) val[u] = sl[u] >= 0 ? __ldg(d.csrVal + sl[u]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (sl[u] >= 0) F[ps[u]] = (T)val[u];
+  }
   __syncwarp();
   for (int k = lane; k < np; k += 32) diag0[k] = F[k + nr * k];
   __syncwarp();
@@ -42,9 +63,16 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
     const int cu = d.fNrow[ch] - d.fNpiv[ch];
     const T* Uc = Ubase + d.fUOff[ch];
     const int* rel = d.relIndex + d.fRelOff[ch];
-    for (int k = lane; k < cu * cu; k += 32) {
-      int a = k % cu, b = k / cu;
-      if (a >= b) F[rel[a] + nr * rel[b]] += __ldcg(Uc + k);
+    // lane a adds rows a, a + 32, ... of the child's lower update matrix, column by column
+    for (int a0 = 0; a0 < cu; a0 += 32) {
+      const int a = a0 + lane;
+      const int ra = a < cu ? __ldg(rel + a) : 0;
+#pragma unroll 4
+      for (int b = 0; b < cu && b <= a0 + 31; ++b) {
+        const int rb = __ldg(rel + b);
+        const T u = (a < cu && a >= b) ? __ldcg(Uc + a + (size_t)cu * b) : T(0);
+        if (a < cu && a >= b) F[ra + nr * rb] += u;
+      }
     }
     __syncwarp();
   }
@@ -58,13 +86,10 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
     const T inv = bad ? T(0) : T(1) / dk;
     for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
     __syncwarp();
-    const int mrem = nr - k - 1;
-    for (int t = lane; t < mrem * mrem; t += 32) {
-      int ii = t % mrem, jj = t / mrem;
-      if (ii >= jj) {
-        int i = k + 1 + ii, j = k + 1 + jj;
-        F[i + nr * j] -= F[i + nr * k] * lcol[j];
-      }
+    // lower triangle of the trailing block, one row per lane
+    for (int i = k + 1 + lane; i < nr; i += 32) {
+      const T fik = F[i + nr * k];
+      for (int j = k + 1; j <= i; ++j) F[i + nr * j] -= fik * lcol[j];
     }
     __syncwarp();
     for (int i = k + 1 + lane; i < nr; i += 32) F[i + nr * k] = lcol[i];
@@ -85,11 +110,37 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
 
 // forward elimination of front f: v = [b_p; 0] + children's updates, y = L11^-1 v_p,
 // w = v_u - L21 y; X(pivots) = D^-1 y
+// copies the nr x np block L of a front into the warp's staging area Ls when
+// it fits (capL values), else returns the global block
+// (callers __syncwarp before reading Ls)
 template <typename T>
-__device__ void forwardOneFront(const DevData& d, int f, T* v, const T* Lbase, T* X, T* W, int lane) {
+__device__ inline const T* stageL(const T* Lg, int cnt, T* Ls, int capL, int lane) {
+  if (cnt > capL) return Lg;
+  for (int k0 = 0; k0 < cnt; k0 += 128) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = k0 + 32 * u + lane;
+      v[u] = k < cnt ? __ldg(Lg + k) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = k0 + 32 * u + lane;
+      if (k < cnt) Ls[k] = v[u];
+    }
+  }
+  return Ls;
+}
+
+template <typename T>
+__device__ void forwardOneFront(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase, const double* rhs,
+                                T* X, T* W, int lane) {
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
   const int* rows = d.frontRows + d.fRowOff[f];
-  for (int r = lane; r < nr; r += 32) v[r] = r < np ? X[rows[r]] : T(0);
+  // the factor block first (independent loads), then the right-hand side of
+  // the pivot rows rounded to the solve precision
+  const T* L = stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
+  for (int r = lane; r < nr; r += 32) v[r] = r < np ? (T)rhs[__ldg(rows + r)] : T(0);
   __syncwarp();
   const int nc = d.fNchild[f];
   const int64_t co = d.fChildOff[f];
@@ -98,10 +149,9 @@ __device__ void forwardOneFront(const DevData& d, int f, T* v, const T* Lbase, T
     const int cu = d.fNrow[ch] - d.fNpiv[ch];
     const T* wc = W + d.fWOff[ch];
     const int* rel = d.relIndex + d.fRelOff[ch];
-    for (int a = lane; a < cu; a += 32) v[rel[a]] += __ldcg(wc + a);
+    for (int a = lane; a < cu; a += 32) v[__ldg(rel + a)] += __ldcg(wc + a);
     __syncwarp();
   }
-  const T* L = Lbase + d.fLOff[f];
   for (int k = 0; k < np; ++k) {
     const T yk = v[k];
     __syncwarp();
@@ -151,76 +201,117 @@ __global__ void kFactorCascade(DevData d, const int* __restrict__ leaves, int nL
 }
 
 template <typename T>
-__global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, const T* Lbase,
-                                T* X, T* W, int* cnt) {
+__global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
+                                const T* Lbase, const double* rhs, T* X, T* W, int* cnt) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int Wt = gridDim.x * wpb;
-  T* v = reinterpret_cast<T*>(smraw) + (size_t)w * maxRow;
+  T* v = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
+  T* Ls = v + maxRow;
   for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
     int f = leaves[idx];
     if (!(d.m.flags[d.fModel[f]] & FL_ACTIVE)) continue;
     while (f >= 0) {
-      forwardOneFront<T>(d, f, v, Lbase, X, W, lane);
+      forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
       f = climb(d, f, cnt, lane);
     }
   }
 }
 
-// top-down: blocks grab ranges of the fronts sorted by decreasing height
+// backward substitution of front f (parent values already in X): the update
+// rows' contribution for every pivot at once (one lane per pivot), then the
+// unit triangle column by column; writes the pivot values to X
+// accumulation of the solved pivot values: ACC_SET del = x (FP64 solve), ACC_FIRST
+// xref = x, ACC_ADD xref += x (FP32 refinement sweeps); finalize: del = xref
+enum { ACC_SET = 0, ACC_FIRST = 1, ACC_ADD = 2 };
+
 template <typename T>
-__global__ void kBackwardDynamic(DevData d, const int* __restrict__ order, int n, int maxRow, const T* Lbase, T* X,
-                                 int* ready, int* work, int perWarp, int* errFlag) {
+__device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL, const T* Lbase, T* X, int acc,
+                                 bool finalize, int lane) {
+  const int nr = d.fNrow[f], np = d.fNpiv[f];
+  const int* rows = d.frontRows + d.fRowOff[f];
+  const T* L = stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
+  for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + __ldg(rows + r));
+  __syncwarp();
+  for (int k = lane; k < np; k += 32) {
+    T acc = xs[k];
+    for (int i = np; i < nr; ++i) acc -= L[i + (size_t)nr * k] * xs[i];
+    xs[k] = acc;
+  }
+  __syncwarp();
+  for (int j = np - 1; j > 0; --j) {
+    const T xj = xs[j];
+    for (int k = lane; k < j; k += 32) xs[k] -= L[j + (size_t)nr * k] * xj;
+    __syncwarp();
+  }
+  for (int r = lane; r < np; r += 32) {
+    const int row = rows[r];
+    const T x = xs[r];
+    X[row] = x;
+    if (acc == ACC_SET) {
+      d.del[row] = (double)x;
+    } else {
+      const double xr = acc == ACC_FIRST ? (double)x : d.xref[row] + (double)x;
+      d.xref[row] = xr;
+      if (finalize) d.del[row] = xr;
+    }
+  }
+}
+
+// top-down along the leaf-to-root paths; state[f]: 0 open, 1 claimed, 2 done
+template <typename T>
+__global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
+                               int maxPath, const T* Lbase, T* X, int* state, int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int base;
   const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * maxRow;
-  for (;;) {
-    if (threadIdx.x == 0) base = atomicAdd(work, wpb * perWarp);
-    __syncthreads();
-    const int b = base;
-    __syncthreads();
-    if (b >= n) break;
-    for (int j = 0; j < perWarp; ++j) {
-      const int idx = b + w * perWarp + j;
-      if (idx >= n) break;
-      const int f = order[n - 1 - idx];  // decreasing height: parents first
-      if (!(d.m.flags[d.fModel[f]] & FL_ACTIVE)) continue;
-      int ok = 1;
-      if (lane == 0 && d.fParent[f] >= 0) {
-        long long spins = 0;
-        while (*(volatile const int*)(ready + f) == 0) {
-          __nanosleep(32);
-          if (++spins > kSpinLimit) {
-            atomicOr(errFlag, 1);
-            ok = 0;
-            break;
+  const int Wt = gridDim.x * wpb;
+  const size_t perWarp = (size_t)(maxRow + capL) * sizeof(T) + (size_t)maxPath * sizeof(int);
+  unsigned char* mine = smraw + (size_t)w * ((perWarp + 15) & ~(size_t)15);
+  T* xs = reinterpret_cast<T*>(mine);
+  T* Ls = xs + maxRow;
+  int* path = reinterpret_cast<int*>(Ls + capL);
+  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
+    const int leaf = leaves[idx];
+    if (!(d.m.flags[d.fModel[leaf]] & FL_ACTIVE)) continue;
+    // the path from the leaf up to (not including) the first front already done
+    int n = 0;
+    if (lane == 0) {
+      int f = leaf;
+      while (f >= 0 && n < maxPath && *(volatile const int*)(state + f) != 2) {
+        path[n++] = f;
+        f = d.fParent[f];
+      }
+      __threadfence();
+    }
+    n = __shfl_sync(0xffffffffu, n, 0);
+    __syncwarp();
+    for (int j = n - 1; j >= 0; --j) {
+      const int f = path[j];
+      int own = 0, ok = 1;
+      if (lane == 0) {
+        int st = *(volatile const int*)(state + f);
+        if (st == 0) own = atomicCAS(state + f, 0, 1) == 0;
+        if (!own) {
+          long long spins = 0;
+          while (*(volatile const int*)(state + f) != 2) {
+            __nanosleep(20);
+            if (++spins > kSpinLimit) {
+              atomicOr(errFlag, 1);
+              ok = 0;
+              break;
+            }
           }
+          __threadfence();
         }
-        __threadfence();
       }
+      own = __shfl_sync(0xffffffffu, own, 0);
       ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) continue;
-      const int nr = d.fNrow[f], np = d.fNpiv[f];
-      const int* rows = d.frontRows + d.fRowOff[f];
-      for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + rows[r]);
-      __syncwarp();
-      const T* L = Lbase + d.fLOff[f];
-      for (int k = np - 1; k >= 0; --k) {
-        T s = T(0);
-        for (int i = k + 1 + lane; i < nr; i += 32) s += L[i + (size_t)nr * k] * xs[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) xs[k] -= s;
-        __syncwarp();
-      }
-      for (int r = lane; r < np; r += 32) X[rows[r]] = xs[r];
+      if (!ok) break;
+      if (!own) continue;
+      backwardOneFront<T>(d, f, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
       __threadfence();
       __syncwarp();
-      const int nc = d.fNchild[f];
-      const int64_t co = d.fChildOff[f];
-      for (int c = lane; c < nc; c += 32) atomicExch(ready + d.childList[co + c], 1);
-      __syncwarp();
+      if (lane == 0) atomicExch(state + f, 2);
     }
   }
 }
@@ -279,39 +370,57 @@ void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, c
   }
 }
 
-void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
+// staging capacity (values) of one front's L block per warp
+int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
+  long long want = (long long)p.maxRow * p.maxNpiv;
+  long long cap = (long long)(12 * 1024 / elemBytes);
+  return (int)(want < cap ? want : cap);
+}
+
+void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s) {
   if (p.nLeaves <= 0) return;
   const int wpb = 8;
   cudaMemsetAsync(p.cntForward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
   if (fp32) {
-    const size_t sm = (size_t)wpb * p.maxRow * sizeof(float);
+    const int capL = stagingCapacity(p, sizeof(float));
+    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
+    allowBigSmem(kForwardCascade<float>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L32, d.x32, d.w32,
-                                                       p.cntForward);
+    kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, d.L32, rhs,
+                                                       d.x32, d.w32, p.cntForward);
   } else {
-    const size_t sm = (size_t)wpb * p.maxRow * sizeof(double);
+    const int capL = stagingCapacity(p, sizeof(double));
+    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
+    allowBigSmem(kForwardCascade<double>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L64, d.x64, d.w64,
-                                                         p.cntForward);
+    kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, d.L64, rhs,
+                                                         d.x64, d.w64, p.cntForward);
   }
 }
 
-void launchBackwardDynamic(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
-  if (p.n <= 0) return;
-  const int wpb = 8, perWarp = 4;
-  cudaMemsetAsync(p.readyBackward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
-  cudaMemsetAsync(p.workCounter, 0, sizeof(int), s);
-  const int needed = (p.n + wpb * perWarp - 1) / (wpb * perWarp);
+void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s) {
+  const int acc = !fp32 ? ACC_SET : (sweep == 0 ? ACC_FIRST : ACC_ADD);
+  const int fin = (fp32 && last) ? 1 : 0;
+  if (p.nLeaves <= 0) return;
+  const int wpb = 8;
+  cudaMemsetAsync(p.stateBackward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
+  const int needed = (p.nLeaves + wpb - 1) / wpb;
   if (fp32) {
-    const size_t sm = (size_t)wpb * p.maxRow * sizeof(float);
-    const int blocks = occupancyBlocks(kBackwardDynamic<float>, 32 * wpb, sm, needed);
-    kBackwardDynamic<float><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L32, d.x32, p.readyBackward,
-                                                        p.workCounter, perWarp, p.errFlag);
+    const int capL = stagingCapacity(p, sizeof(float));
+    const size_t per = ((size_t)(p.maxRow + capL) * sizeof(float) + (size_t)p.maxPath * sizeof(int) + 15) & ~(size_t)15;
+    const size_t sm = (size_t)wpb * per;
+    allowBigSmem(kBackwardClaim<float>, sm);
+    const int blocks = occupancyBlocks(kBackwardClaim<float>, 32 * wpb, sm, needed);
+    kBackwardClaim<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, p.maxPath, d.L32,
+                                                      d.x32, p.stateBackward, p.errFlag, acc, fin);
   } else {
-    const size_t sm = (size_t)wpb * p.maxRow * sizeof(double);
-    const int blocks = occupancyBlocks(kBackwardDynamic<double>, 32 * wpb, sm, needed);
-    kBackwardDynamic<double><<<blocks, 32 * wpb, sm, s>>>(d, p.order, p.n, p.maxRow, d.L64, d.x64,
-                                                          p.readyBackward, p.workCounter, perWarp, p.errFlag);
+    const int capL = stagingCapacity(p, sizeof(double));
+    const size_t per = ((size_t)(p.maxRow + capL) * sizeof(double) + (size_t)p.maxPath * sizeof(int) + 15) & ~(size_t)15;
+    const size_t sm = (size_t)wpb * per;
+    allowBigSmem(kBackwardClaim<double>, sm);
+    const int blocks = occupancyBlocks(kBackwardClaim<double>, 32 * wpb, sm, needed);
+    kBackwardClaim<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, p.maxPath, d.L64,
+                                                        d.x64, p.stateBackward, p.errFlag, acc, fin);
   }
 }
 

@@ -114,6 +114,10 @@ struct Rec {
     return v.empty() ? def : v[0];
   }
   int inum(const char* k, int def) const { return (int)std::lround(num(k, (double)def)); }
+  std::string str(const char* k) const {
+    auto it = r.vals.find(k);
+    return (it == r.vals.end() || it->second.empty()) ? std::string() : lowerCase(it->second[0]);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -442,6 +446,8 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   c.tolInitEquil = o.d("tolInitEquil", 1.0e-3);
   c.limInitEquilStep = o.d("limInitEquilStep", 1.0);
   c.tolFactorize = o.d("tolFactorize", 1.0e-12);
+  c.tQStatic = o.d("quasiStatic", 0.0);
+  if (c.tQStatic <= c.tStart) c.tQStatic = -1.0e99;  // initiateSystemTypeModule.f90:129-132
   const char* tolKeys[18] = {"tolDispNorm", "tolDispTra", "tolDispRot", "tolDispGen", "tolVelNorm", "tolVelTra",
                              "tolVelRot",   "tolVelGen",  "tolAccNorm", "tolAccTra",  "tolAccRot",  "tolAccGen",
                              "tolResNorm",  "tolResTra",  "tolResRot",  "tolResGen",  "tolEnerMax", "tolEnerSum"};
@@ -485,6 +491,78 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       props.push_back(p);
     }
   }
+  // engines (engineRoutinesModule.f90 subset): value = f(x), x = time for a TIME
+  // sensor (or no sensor), else 0; f = SCALE (realData(1) * x), CONSTANT
+  // (realData(1)) or none (x).  Stored as x-coefficient eA and constant eB.
+  std::map<int, std::pair<std::string, double>> funcs;  // id -> (type, realData(1) or its default)
+  std::map<int, bool> timeSensor;                        // id -> TIME sensor
+  for (const NmlRecord& nr : recs) {
+    Rec r{nr};
+    if (nr.name == "function") {
+      auto rd = r.nums("realdata");
+      std::string type = r.str("type");
+      funcs[r.inum("id", 0)] = {type, rd.empty() ? (type == "scale" ? 1.0 : 0.0) : rd[0]};
+    } else if (nr.name == "sensor") {
+      timeSensor[r.inum("id", 0)] = r.str("type") == "time";
+    }
+  }
+  std::map<int, std::pair<double, double>> engines;  // id -> (eA, eB)
+  for (const NmlRecord& nr : recs) {
+    if (nr.name != "engine") continue;
+    Rec r{nr};
+    int fid = r.inum("functionid", 0), sid = r.inum("argsensorid", 0);
+    double xs = 1.0;
+    if (sid > 0) {
+      auto it = timeSensor.find(sid);
+      xs = (it != timeSensor.end() && it->second) ? 1.0 : 0.0;
+    }
+    double eA = xs, eB = 0.0;
+    if (fid > 0) {
+      auto it = funcs.find(fid);
+      if (it == funcs.end()) { err = "engine refers to unknown function"; return -21; }
+      if (it->second.first == "scale") eA = it->second.second * xs;
+      else if (it->second.first == "constant") { eA = 0.0; eB = it->second.second; }
+      else { err = "function type '" + it->second.first + "' is not supported (SCALE, CONSTANT)"; return -22; }
+    }
+    engines[r.inum("id", 0)] = {eA, eB};
+  }
+  // prescribed deflections: MEQN = -ICEQ of the constraint equation (samSolverModule.f90)
+  std::vector<int> motionOfDof(6 * (size_t)m.ntri, -1);
+  for (const NmlRecord& nr : recs) {
+    if (nr.name != "motion") continue;
+    Rec r{nr};
+    auto it = triIndex.find(r.inum("triadid", 0));
+    if (it == triIndex.end()) { err = "motion on unknown triad"; return -23; }
+    int dof = r.inum("ldof", 0);
+    if (dof < 1 || dof > m.triNdof[it->second]) { err = "motion DOF must be 1..nDOFs of its triad"; return -24; }
+    std::string type = r.str("type");
+    if (!type.empty() && type != "deflection") { err = "only prescribed deflections are supported"; return -25; }
+    int& slot = motionOfDof[6 * (size_t)it->second + dof - 1];
+    if (slot >= 0) { err = "two motions on one DOF"; return -26; }
+    slot = (int)m.motD0.size();
+    double eA = 0.0, eB = 0.0, d1 = r.num("d1", 0.0);
+    int eid = r.inum("motionengineid", 0);
+    if (eid > 0) {
+      auto e = engines.find(eid);
+      if (e == engines.end()) { err = "motion refers to unknown engine"; return -27; }
+      eA = e->second.first;
+      eB = e->second.second;
+    } else {
+      d1 = 0.0;
+    }
+    m.motD0.push_back(r.num("d0", 0.0));
+    m.motD1.push_back(d1);
+    m.motEA.push_back(eA);
+    m.motEB.push_back(eB);
+    if (c.initEquilibrium && m.motD0.back() + d1 * (eA * c.tStart + eB) != 0.0) {
+      err = "prescribed start values other than zero with initEquilibrium are not supported";
+      return -28;
+    }
+  }
+  if (!m.motD0.empty() && c.tQStatic > c.tStart && c.fixedIt < -1) {
+    err = "quasi-static steps need numit = -1 (linear) or numit >= 0";
+    return -29;
+  }
   for (double w = 0; w < 3; ++w) {
     int k = (int)w;
     c.wForce[k] = c.wDisp[k] > 0.0 ? 1.0 / c.wDisp[k] : 0.0;
@@ -501,7 +579,13 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       int bc = bcs[6 * t + k];
       if (bc == 2 && !c.initEquilibrium) bc = 1;
       if (bc != 0 && bc != 1) { err = "BC code other than 0, 1 or 2 (2 only without initEquilibrium)"; return -30; }
-      m.meqn.push_back(bc == 1 ? m.neq++ : -1);
+      const int mot = motionOfDof[6 * (size_t)t + k];
+      if (mot >= 0) {
+        m.meqn.push_back(-2 - mot);
+        m.motDof.push_back(m.ndof + k);
+      } else {
+        m.meqn.push_back(bc == 1 ? m.neq++ : -1);
+      }
       m.dofType.push_back(k < 3 ? 1 : 2);
     }
     m.ndof += m.triNdof[t];
@@ -586,11 +670,68 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (r.inum("loadengineid", 0) > 0) { err = "time-dependent loads (loadEngineId) are not supported"; return -19; }
       int eq = m.meqn[m.triFirstDof[it->second] + dof - 1];
       if (eq >= 0) m.qext[eq] += r.num("f0", 0.0);
-    } else if (nr.name == "motion") {
-      err = "prescribed motions are not supported";
-      return -20;
     }
   }
+  // axial springs (SPRING_ELEMENT + SPRING_BASE) first, then axial dampers (DAMPER)
+  std::map<int, const NmlRecord*> springBase;
+  for (const NmlRecord& nr : recs)
+    if (nr.name == "spring_base") springBase[Rec{nr}.inum("id", 0)] = &nr;
+  for (int pass = 0; pass < 2; ++pass)
+    for (const NmlRecord& nr : recs) {
+      Rec r{nr};
+      int t[2];
+      if (pass == 0 && nr.name == "spring_element") {
+        auto tids = r.nums("triadids");
+        auto sb = r.nums("springbaseid");
+        int nb = 0;
+        for (double v : sb) nb += v > 0.0;
+        if (tids.size() < 2 || tids[1] <= 0.0 || (tids.size() > 2 && tids[2] > 0.0) || nb != 1 || sb[0] <= 0.0) {
+          err = "only axial springs between two triads with one base spring are supported";
+          return -40;
+        }
+        auto b = springBase.find((int)std::lround(sb[0]));
+        if (b == springBase.end()) { err = "spring refers to unknown SPRING_BASE"; return -43; }
+        Rec br{*b->second};
+        for (const char* key : {"stifffuncid", "forcefuncid", "lengthengineid", "stiffscaleengineposid",
+                                "stiffscaleenginenegid", "springfailureid", "springyieldid"})
+          if (br.inum(key, 0) > 0) { err = "only constant linear springs are supported"; return -42; }
+        for (int k = 0; k < 2; ++k) {
+          auto it = triIndex.find((int)std::lround(tids[k]));
+          if (it == triIndex.end()) { err = "spring refers to unknown triad"; return -41; }
+          t[k] = it->second;
+        }
+        m.axKind.push_back(0);
+        m.axS0.push_back(br.num("s0", 0.0));
+        m.axL0.push_back(br.num("l0", 0.0));
+        m.axAlpha2.push_back(r.num("alpha2", 0.0));
+        m.axD0.push_back(0.0);
+      } else if (pass == 1 && nr.name == "damper") {
+        int id1 = r.inum("triad1id", 0), id2 = r.inum("triad2id", 0);
+        if (id1 <= 0 || id2 <= 0) { err = "only axial dampers between two triads are supported"; return -44; }
+        if (r.inum("coeffscaleengineid", 0) > 0 || r.inum("coefffuncid", 0) > 0 || r.inum("forcefuncid", 0) > 0) {
+          err = "only constant linear dampers are supported";
+          return -45;
+        }
+        auto i1 = triIndex.find(id1), i2 = triIndex.find(id2);
+        if (i1 == triIndex.end() || i2 == triIndex.end()) { err = "damper refers to unknown triad"; return -46; }
+        t[0] = i1->second;
+        t[1] = i2->second;
+        // the triad with most DOFs is triad 1 (initiateDamperTypeModule.f90:160-165)
+        if (m.triNdof[t[0]] < m.triNdof[t[1]]) std::swap(t[0], t[1]);
+        m.axKind.push_back(1);
+        m.axS0.push_back(0.0);
+        m.axL0.push_back(0.0);
+        m.axAlpha2.push_back(0.0);
+        m.axD0.push_back(r.num("d0", 0.0));
+      } else {
+        continue;
+      }
+      for (int k = 0; k < 2; ++k) {
+        if (m.triNdof[t[k]] < 3) { err = "axial element triads need translational DOFs"; return -47; }
+        m.axTri.push_back(t[k]);
+      }
+      m.nax++;
+    }
   // element matrices, damping, scaling, corotation initialisation
   std::vector<double> tmpC = m.C;
   m.K.assign(144 * (size_t)m.nel, 0.0);
@@ -640,17 +781,22 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   for (int e = 0; e < m.nel; ++e)
     for (int n = 0; n < 2; ++n)
       for (int d = 0; d < 6; ++d) m.elEq[12 * e + 6 * n + d] = m.meqn[m.triFirstDof[m.elTri[2 * e + n]] + d];
+  m.axEq.resize(6 * (size_t)m.nax);
+  for (int a = 0; a < m.nax; ++a)
+    for (int n = 0; n < 2; ++n)
+      for (int d = 0; d < 3; ++d) m.axEq[6 * a + 3 * n + d] = m.meqn[m.triFirstDof[m.axTri[2 * a + n]] + d];
   // full symmetric CSR pattern (union of element cliques, diagonal always present)
   std::vector<std::vector<int>> rows(m.neq);
   for (int i = 0; i < m.neq; ++i) rows[i].push_back(i);
-  for (int e = 0; e < m.nel; ++e) {
-    const int* q = &m.elEq[12 * e];
-    for (int i = 0; i < 12; ++i) {
+  auto clique = [&](const int* q, int n) {
+    for (int i = 0; i < n; ++i) {
       if (q[i] < 0) continue;
-      for (int j = 0; j < 12; ++j)
+      for (int j = 0; j < n; ++j)
         if (q[j] >= 0) rows[q[i]].push_back(q[j]);
     }
-  }
+  };
+  for (int e = 0; e < m.nel; ++e) clique(&m.elEq[12 * e], 12);
+  for (int a = 0; a < m.nax; ++a) clique(&m.axEq[6 * a], 6);
   m.rowPtr.assign(m.neq + 1, 0);
   for (int i = 0; i < m.neq; ++i) {
     std::sort(rows[i].begin(), rows[i].end());
@@ -674,6 +820,19 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       }
     }
   }
+  for (int a = 0; a < m.nax; ++a) {  // springs, then dampers (BuildNewtonMat order)
+    const int* q = &m.axEq[6 * a];
+    for (int i = 0; i < 6; ++i) {
+      if (q[i] < 0) continue;
+      const int* b = &m.colInd[m.rowPtr[q[i]]];
+      const int* en = &m.colInd[0] + m.rowPtr[q[i] + 1];
+      for (int j = 0; j < 6; ++j) {
+        if (q[j] < 0) continue;
+        int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
+        slotList[slot].push_back(144 * m.nel + 36 * a + i + 6 * j);
+      }
+    }
+  }
   m.slotPtr.assign(m.colInd.size() + 1, 0);
   for (size_t s = 0; s < slotList.size(); ++s) m.slotPtr[s + 1] = m.slotPtr[s] + (int)slotList[s].size();
   for (auto& l : slotList) m.slotSrc.insert(m.slotSrc.end(), l.begin(), l.end());
@@ -682,9 +841,41 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   for (int e = 0; e < m.nel; ++e)
     for (int i = 0; i < 12; ++i)
       if (m.elEq[12 * e + i] >= 0) eqList[m.elEq[12 * e + i]].push_back(12 * e + i);
+  for (int a = 0; a < m.nax; ++a)
+    for (int i = 0; i < 6; ++i)
+      if (m.axEq[6 * a + i] >= 0) eqList[m.axEq[6 * a + i]].push_back(12 * m.nel + 6 * a + i);
   m.eqPtr.assign(m.neq + 1, 0);
   for (int i = 0; i < m.neq; ++i) m.eqPtr[i + 1] = m.eqPtr[i] + (int)eqList[i].size();
   for (auto& l : eqList) m.eqSrc.insert(m.eqSrc.end(), l.begin(), l.end());
+  // prescribed-DOF terms moved to the right-hand side (asmSparse with a constant
+  // term, sysMatrixTypeModule.f90:2099-2259): element order, then prescribed row
+  std::vector<std::vector<std::pair<int, int>>> mrList(m.neq);
+  for (int e = 0; e < m.nel; ++e) {
+    const int* q = &m.elEq[12 * e];
+    for (int i = 0; i < 12; ++i) {
+      if (q[i] > -2) continue;
+      for (int j = 0; j < 12; ++j)
+        if (q[j] >= 0) mrList[q[j]].push_back({144 * e + i + 12 * j, -2 - q[i]});
+    }
+  }
+  for (int a = 0; a < m.nax; ++a) {
+    const int* q = &m.axEq[6 * a];
+    for (int i = 0; i < 6; ++i) {
+      if (q[i] > -2) continue;
+      for (int j = 0; j < 6; ++j)
+        if (q[j] >= 0) mrList[q[j]].push_back({144 * m.nel + 36 * a + i + 6 * j, -2 - q[i]});
+    }
+  }
+  m.mrPtr.assign(1, 0);
+  for (int i = 0; i < m.neq; ++i) {
+    if (mrList[i].empty()) continue;
+    m.mrEq.push_back(i);
+    for (auto& pr : mrList[i]) {
+      m.mrSrc.push_back(pr.first);
+      m.mrMot.push_back(pr.second);
+    }
+    m.mrPtr.push_back((int)m.mrSrc.size());
+  }
   return symbolicAnalysis(m, err);
 }
 

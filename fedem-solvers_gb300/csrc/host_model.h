@@ -27,6 +27,8 @@ struct Control {
   double tolVal[18] = {0.0};
   double wDisp[3] = {1, 1, 1}, wForce[3] = {1, 1, 1};
   double gravity[3] = {0, 0, 0};
+  // quasi-static load steps while time + dt < tQStatic (-quasiStatic; none when <= tStart)
+  double tQStatic = -1.0e99;
 };
 
 struct Front {            // one supernode of the assembly tree
@@ -50,7 +52,8 @@ struct HostModel {
   int ntri = 0;
   std::vector<int> triId, triNdof, triFirstDof;
   std::vector<double> ur;
-  // DOFs and equations (samSolverModule.f90:95-250): meqn 0-based, -1 fixed
+  // DOFs and equations (samSolverModule.f90:95-250): meqn 0-based, -1 fixed,
+  // -2 - k prescribed by motion k
   int ndof = 0, neq = 0;
   std::vector<int> meqn, dofType;
   // beam superelements: matrices column-major 12x12 in superelement axes
@@ -60,11 +63,27 @@ struct HostModel {
   std::vector<double> K, M, C, fg;                        // 144, 144, 144, 36 per element
   std::vector<double> stifScl, kDmp;
   std::vector<uint8_t> hasC, hasVld;
+  // axial springs (constant stiffness s0, stress-free length l0, stiffness-proportional
+  // damping alpha2) and axial dampers (coefficient d0) between two triads, springs first;
+  // they act on the translational DOFs (springRoutinesModule.f90, damperRoutinesModule.f90)
+  int nax = 0;
+  std::vector<uint8_t> axKind;  // 0 spring, 1 damper
+  std::vector<int> axTri, axEq; // 2 and 6 per axial element
+  std::vector<double> axS0, axL0, axAlpha2, axD0;
   // external point loads in equation order (constant f0; forceRoutinesModule.f90)
   std::vector<double> qext;
+  // prescribed deflections (motionRoutinesModule.f90:58-193): D(t) = d0 + d1 * (eA * t + eB)
+  // (engine = function of the TIME sensor); a prescribed DOF has meqn = -2 - motion index
+  std::vector<int> motDof;
+  std::vector<double> motD0, motD1, motEA, motEB;
+  // predictor right-hand-side terms of the prescribed DOFs: equation mrEq[k] gets
+  // -cc(motion mrMot[q]) * elMat[mrSrc[q]] for q in mrPtr[k]..mrPtr[k+1] (mrSrc = 144*e + entry)
+  std::vector<int> mrEq, mrPtr, mrSrc, mrMot;
   // full symmetric CSR pattern of the Newton matrix, equation order
   std::vector<int> rowPtr, colInd;
   // deterministic gather maps: CSR slot <- (element, entry); equation <- (element, local dof)
+  // (axial elements follow the beams: slotSrc = 144*nel + 36*axial + entry,
+  // eqSrc = 12*nel + 6*axial + local, mrSrc like slotSrc)
   std::vector<int> slotPtr, slotSrc;   // slotSrc = 144*element + entry
   std::vector<int> eqPtr, eqSrc;       // eqSrc = 12*element + local dof
   // multifrontal symbolic factorisation

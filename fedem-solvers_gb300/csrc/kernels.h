@@ -43,20 +43,28 @@ struct LevelPlan {
 };
 // one-launch front kernels over all heights (front_cascade.cu)
 struct PersistentPlan {
-  const int* order;   // all fronts of the batch by increasing height
-  int n;
   const int* leaves;  // fronts without children
   int nLeaves;
-  int maxRow;         // largest front of the batch
-  int *cntFactor, *cntForward, *readyBackward, *workCounter, *errFlag;
+  int maxRow;         // largest front of the batch (rows)
+  int maxNpiv;        // largest pivot block of the batch
+  int maxPath;        // longest leaf-to-root path (fronts)
+  int *cntFactor, *cntForward, *stateBackward, *errFlag;
 };
 void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
-void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
-void launchBackwardDynamic(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
+// forward elimination of the right-hand side rhs (FP64, rounded to the solve precision)
+void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s);
+// back substitution; stores the solution in del (FP64 solve) or accumulates it in xref
+// (FP32 refinement sweep `sweep`; the last sweep also copies xref to del)
+void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
 // one launch per height
 void launchFactorLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
 void launchForwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
 void launchBackwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
+// prescribed deflections (step start), their predictor right-hand side (after the
+// element Newton matrices), and the restart state of pure linear quasi-static steps
+void launchMotions(const DevData& d, cudaStream_t s);
+void launchMotionRhs(const DevData& d, cudaStream_t s);
+void launchQsRestore(const DevData& d, cudaStream_t s);
 // vector glue for the solves
 void launchSolveSetup(const DevData& d, bool fp32, int sweep, cudaStream_t s);
 void launchSolveAccumulate(const DevData& d, bool fp32, cudaStream_t s);

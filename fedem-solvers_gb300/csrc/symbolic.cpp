@@ -80,6 +80,10 @@ int symbolicAnalysis(HostModel& m, std::string& err) {
     int a = nodeOfTriad[m.elTri[2 * e]], b = nodeOfTriad[m.elTri[2 * e + 1]];
     if (a >= 0 && b >= 0 && a != b) { nb[a].push_back(b); nb[b].push_back(a); }
   }
+  for (int k = 0; k < m.nax; ++k) {  // axial springs and dampers couple their two triads
+    int a = nodeOfTriad[m.axTri[2 * k]], b = nodeOfTriad[m.axTri[2 * k + 1]];
+    if (a >= 0 && b >= 0 && a != b) { nb[a].push_back(b); nb[b].push_back(a); }
+  }
   g.adjPtr.assign(g.n + 1, 0);
   for (int v = 0; v < g.n; ++v) {
     std::sort(nb[v].begin(), nb[v].end());

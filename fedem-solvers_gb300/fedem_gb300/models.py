@@ -55,9 +55,35 @@ def _loads(n_el, load_node, load_dof, load, motion):
     return out
 
 
+def _axials(n_el, anchors, springs, dampers):
+    """Fixed anchor triads and axial spring/damper records.  `anchors` are
+    (x, y, z) points (triad ids 10*n_el + 100 + k, all DOFs fixed); springs are
+    (triad a, triad b, stiffness, stress-free length[, alpha2]) and dampers
+    (triad a, triad b, coefficient), with triads given as chain indices
+    0..n_el or ("anchor", k)."""
+    def tid(t):
+        return 10 * n_el + 100 + t[1] if isinstance(t, tuple) else t + 1
+
+    out = []
+    for k, (x, y, z) in enumerate(anchors or ()):
+        out.append(f"&TRIAD\n  id = {10 * n_el + 100 + k}\n  nDOFs = 6\n  ur = 1.0 0.0 0.0 {_f(x)} 0.0 1.0 0.0 "
+                   f"{_f(y)} 0.0 0.0 1.0 {_f(z)}\n  BC = 0 0 0 0 0 0\n/\n")
+    base = 20 * n_el + 200
+    for k, sp in enumerate(springs or ()):
+        a, b, stiff, l0 = sp[:4]
+        alpha2 = sp[4] if len(sp) > 4 else 0.0
+        out.append(f"&SPRING_BASE\n  id = {base + k}\n  l0 = {_f(l0)}\n  s0 = {_f(stiff)}\n/\n"
+                   f"&SPRING_ELEMENT\n  id = {base + k}\n  triadIDs = {tid(a)} {tid(b)}\n"
+                   f"  springBaseId = {base + k}\n  alpha2 = {_f(alpha2)}\n/\n")
+    for k, (a, b, coeff) in enumerate(dampers or ()):
+        out.append(f"&DAMPER\n  id = {base + 1000 + k}\n  triad1Id = {tid(a)}\n  triad2Id = {tid(b)}\n"
+                   f"  d0 = {_f(coeff)}\n/\n")
+    return out
+
+
 def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof, load,
                    shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x",
-                   motion=None):
+                   motion=None, anchors=None, springs=None, dampers=None):
     """Solver-input text for a straight chain of `n_el` beams along X (or Z).
 
     Triad k sits at k*el_len on the axis; triad `clamp` has all six DOFs
@@ -65,11 +91,14 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
     triad `load_node`.  shear_factor = 0 gives Euler-Bernoulli beams.
     `section` = (A, Iy, Iz, It) overrides the pipe section from od/wall.
     `motion` = (triad index, DOF, d1) prescribes that DOF to d1 * time
-    (the load record is then left out when `load` is 0).
+    (the load record is then left out when `load` is 0).  `anchors`,
+    `springs` and `dampers` add fixed triads and axial springs/dampers
+    (see _axials).
     """
+    extra = _axials(n_el, anchors, springs, dampers)
     if axis == "z":
         return _chain_along_z(n_el, el_len, section or pipe_section(od, wall), E, G, rho, clamp, load_node,
-                              load_dof, load, shear_factor, weights, title, motion)
+                              load_dof, load, shear_factor, weights, title, motion) + "".join(extra)
     area, iy, iz, it = section or pipe_section(od, wall)
     out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
            f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
@@ -96,7 +125,7 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
     out += _loads(n_el, load_node, load_dof, load, motion)
-    return "".join(out)
+    return "".join(out + extra)
 
 
 def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof, load, shear_factor, weights,

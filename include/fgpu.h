@@ -43,7 +43,7 @@ int fgpu_model_element_matrix(const fgpu_model* m, int iel, int which, double* m
 /* Uploads the models to the GPU (host -> HBM copies), solves each model's
  * initial static equilibrium if requested and prepares the batched iteration.
  * mixed != 0: FP32 frontal factorisation + FP64 iterative refinement with
- * `sweeps` solves per Newton iteration; mixed == 0: plain FP64. */
+ * `sweeps` solves per Newton iteration (0: default 2); mixed == 0: plain FP64. */
 int fgpu_batch_create(int nmodels, fgpu_model* const* models, int mixed, int sweeps, fgpu_batch** out);
 void fgpu_batch_destroy(fgpu_batch* b);
 /* Runs batched Newton iterations until every model reached its end time (or

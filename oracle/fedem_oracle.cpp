@@ -591,6 +591,19 @@ struct Motion {
   int iceq = 0;    // constraint equation (1-based)
 };
 
+// Axial spring (SPRING_ELEMENT with two triads and one SPRING_BASE of
+// constant stiffness s0 and stress-free length l0) or axial damper (DAMPER
+// between two triads, coefficient d0): springRoutinesModule.f90:200-239,
+// 551-742, 872-1124; damperRoutinesModule.f90:54-376.  Forces act along the
+// current direction n from triad 1 to triad 2 on the translational DOFs.
+struct Axial {
+  int kind = 0;  // 0 spring, 1 damper
+  int tri[2] = {-1, -1};
+  double s0 = 0.0, l0 = 0.0, alpha2 = 0.0, d0 = 0.0;
+  double n[3] = {0, 0, 0}, L = 0.0, F = 0.0;
+  double FS[6] = {0, 0, 0, 0, 0, 0}, FD[6] = {0, 0, 0, 0, 0, 0};
+};
+
 struct TestItem {
   int code = -1;  // 1 allOf, 2 oneOf, -1 inactive
   double absTol = 0.0, value = 0.0;
@@ -608,6 +621,9 @@ struct OracleModel {
   std::vector<Sensor> sensors;
   std::vector<EngineF> engines;
   std::vector<Motion> motions;
+  std::vector<Axial> axials;    // springs first, then dampers (assembly order)
+  std::vector<int> axEq;        // 6 per axial element: 0-based equation, -1 fixed, <= -2 prescribed
+  const std::vector<double>* axVel = nullptr;  // triad velocities the dampers see
   std::vector<double> ccv;  // constant term of each constraint equation (TTCC(MPMCEQ(iceq)))
   double tQStatic = -1.0e99;  // end of the quasi-static load steps
   int quasiSteps = 0;         // quasi-static steps since the last dynamic one
@@ -772,7 +788,73 @@ static int updateElems(OracleModel& m, bool newPositions, bool isStatic, bool co
       rotateOut(e, e.FI);
     }
   }
+  // axial springs and dampers (UpdateSprings / UpdateDampers, then
+  // calcSpringForces / addInDampingForces / calcDamperForces)
+  for (Axial& a : m.axials) {
+    const Triad& t1 = m.triads[a.tri[0]];
+    const Triad& t2 = m.triads[a.tri[1]];
+    double d[3] = {t2.ur[0][3] - t1.ur[0][3], t2.ur[1][3] - t1.ur[1][3], t2.ur[2][3] - t1.ur[2][3]};
+    double l2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (l2 < epsDiv0) {
+      if (a.kind == 0) return -1;  // the two points defining the spring coincide
+      a.L = std::sqrt(l2);
+      a.n[0] = a.n[1] = a.n[2] = 0.0;
+    } else {
+      a.L = std::sqrt(l2);
+      for (int k = 0; k < 3; ++k) a.n[k] = d[k] / a.L;
+    }
+    double v1[3] = {0, 0, 0}, v2[3] = {0, 0, 0};
+    if (!isStatic && m.axVel) {
+      for (int k = 0; k < 3; ++k) {
+        v1[k] = (*m.axVel)[t1.firstDof + k];
+        v2[k] = (*m.axVel)[t2.firstDof + k];
+      }
+    }
+    for (int k = 0; k < 6; ++k) a.FS[k] = a.FD[k] = 0.0;
+    if (a.kind == 0) {
+      a.F = a.s0 * (a.L - a.l0);
+      for (int k = 0; k < 3; ++k) {
+        a.FS[k] = 0.0 - a.F * a.n[k];
+        a.FS[3 + k] = 0.0 + a.F * a.n[k];
+      }
+      if (!isStatic && std::fabs(a.alpha2) > 1.0e-16) {
+        // stiffness-proportional damping forces C v with C = alpha2 * s0 * n n^T blocks
+        double km = a.s0 * a.alpha2 * a.L / a.L;
+        for (int i = 0; i < 3; ++i) {
+          double f1 = 0.0, f2 = 0.0;
+          for (int j = 0; j < 3; ++j) f1 += a.n[i] * a.n[j] * km * v1[j];
+          for (int j = 0; j < 3; ++j) f1 += -(a.n[i] * a.n[j] * km) * v2[j];
+          for (int j = 0; j < 3; ++j) f2 += -(a.n[i] * a.n[j] * km) * v1[j];
+          for (int j = 0; j < 3; ++j) f2 += a.n[i] * a.n[j] * km * v2[j];
+          a.FD[i] = f1;
+          a.FD[3 + i] = f2;
+        }
+      }
+    } else {
+      double vr[3] = {v2[0] - v1[0], v2[1] - v1[1], v2[2] - v1[2]};
+      double vel = a.n[0] * vr[0] + a.n[1] * vr[1] + a.n[2] * vr[2];
+      a.F = a.d0 * vel;
+      if (!isStatic)
+        for (int k = 0; k < 3; ++k) {
+          a.FD[k] = -a.F * a.n[k];
+          a.FD[3 + k] = -a.FD[k];
+        }
+    }
+  }
   return 0;
+}
+
+// 3x3 translational block of an axial element's Newton matrix
+// (calcSpringStiffness without geometric stiffness; addInDamperMat)
+static void axialBlock(const Axial& a, double sC, double sK, double* A) {
+  if (a.kind == 0) {
+    const double km = (a.s0 * (sK + sC * a.alpha2)) * a.L / a.L;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) A[i + 3 * j] = a.n[i] * a.n[j] * km;
+  } else {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) A[i + 3 * j] = a.n[i] * a.n[j] * a.d0 * sC;
+  }
 }
 
 // System force vectors (addInSysModule.f90:626-840, GetForceVectors).
@@ -790,6 +872,15 @@ static void getForceVectors(OracleModel& m) {
       m.FDk[eq[i]] += e.FD[i];
       m.FIk[eq[i]] += e.FI[i];
       m.Qk[eq[i]] += e.Q[i];
+    }
+  }
+  for (size_t k = 0; k < m.axials.size(); ++k) {
+    const Axial& a = m.axials[k];
+    const int* eq = &m.axEq[6 * k];
+    for (int i = 0; i < 6; ++i) {
+      if (eq[i] < 0) continue;
+      m.FSk[eq[i]] += a.FS[i];
+      m.FDk[eq[i]] += a.FD[i];
     }
   }
   for (Load& l : m.loads) {
@@ -897,6 +988,30 @@ static void assembleSkyline(OracleModel& m, double sM, double sC, double sK, std
       if (!(std::fabs(c) > 1.0e-15)) continue;
       for (int j = 0; j < 12; ++j)
         if (eq[j] >= 0) (*rhs)[eq[j]] -= c * Ns[i + 12 * j];
+    }
+  }
+  for (size_t k = 0; k < m.axials.size(); ++k) {
+    double A[9], E[36];
+    axialBlock(m.axials[k], sC, sK, A);
+    for (int bj = 0; bj < 2; ++bj)
+      for (int bi = 0; bi < 2; ++bi)
+        for (int c = 0; c < 3; ++c)
+          for (int r = 0; r < 3; ++r) E[(3 * bi + r) + 6 * (3 * bj + c)] = bi == bj ? A[r + 3 * c] : -A[r + 3 * c];
+    const int* eq = &m.axEq[6 * k];
+    for (int i = 0; i < 6; ++i) {
+      if (eq[i] < 0) continue;
+      for (int j = 0; j < 6; ++j) {
+        if (eq[j] < eq[i]) continue;
+        skyAt(m, eq[i], eq[j]) += E[i + 6 * j];
+      }
+    }
+    if (!rhs) continue;
+    for (int i = 0; i < 6; ++i) {
+      if (eq[i] > -2) continue;
+      double c = m.ccv[-2 - eq[i]];
+      if (!(std::fabs(c) > 1.0e-15)) continue;
+      for (int j = 0; j < 6; ++j)
+        if (eq[j] >= 0) (*rhs)[eq[j]] -= c * E[i + 6 * j];
     }
   }
 }
@@ -1118,6 +1233,7 @@ static int staticEquilibrium(OracleModel& m) {
   std::fill(m.urd.begin(), m.urd.end(), 0.0);
   std::fill(m.urdd.begin(), m.urdd.end(), 0.0);
   for (Elem& e : m.elems) setElemVelAcc(m, e, m.urd, m.urdd);
+  m.axVel = &m.urd;
   double ts = m.timeStep;
   m.timeStep = 0.0;
   updateElems(m, true, false, false);
@@ -1156,6 +1272,7 @@ static int newmarkInt(OracleModel& m) {
   for (;;) {
     if (m.nIterThisStep == 0) {
       for (Elem& e : m.elems) setElemVelAcc(m, e, m.dk, m.ak);
+      m.axVel = &m.dk;  // SetTriadsVelAcc(triads, dk, ak) in PredictAndUpdate
       if (updateElems(m, false, false, false) != 0) return -1;
       getForceVectors(m);
       for (int k = 0; k < m.neq; ++k)
@@ -1192,6 +1309,7 @@ static int newmarkInt(OracleModel& m) {
     }
     incTriadsPos(m, m.sinc[0]);
     for (Elem& e : m.elems) setElemVelAcc(m, e, m.urd, m.urdd);
+    m.axVel = &m.urd;
     if (updateElems(m, true, false, false) != 0) return -1;
     calculateNorms(m);
     m.nIterThisStep++;
@@ -1342,6 +1460,7 @@ static int setup(OracleModel& m, const char* fsi) {
   };
   // superelements and their undeformed triad positions
   int pendingUnd = -1;
+  std::vector<Axial> springs, dampers;
   for (const Record& r : recs) {
     if (r.name == "sup_el") {
       Elem e;
@@ -1406,6 +1525,43 @@ static int setup(OracleModel& m, const char* fsi) {
       int eid = r.i("loadengineid", 0);
       if (eid > 0 && (l.engine = findEngine(eid)) < 0) return -18;
       m.loads.push_back(l);
+    } else if (r.name == "spring_element") {
+      auto tids = r.dv("triadids");
+      auto sb = r.dv("springbaseid");
+      int nb = 0;
+      for (double v : sb) nb += v > 0.0;
+      if (tids.size() < 2 || tids[1] <= 0.0 || (tids.size() > 2 && tids[2] > 0.0) || nb != 1 || sb[0] <= 0.0)
+        return -40;  // axial springs between two triads only
+      Axial a;
+      a.kind = 0;
+      for (int k = 0; k < 2; ++k)
+        if ((a.tri[k] = findTriad(m, (int)std::lround(tids[k]))) < 0) return -41;
+      a.alpha2 = r.d("alpha2");
+      int bid = (int)std::lround(sb[0]);
+      bool found = false;
+      for (const Record& q : recs) {
+        if (q.name != "spring_base" || q.i("id") != bid) continue;
+        if (q.i("stifffuncid") > 0 || q.i("forcefuncid") > 0 || q.i("lengthengineid") > 0 ||
+            q.i("stiffscaleengineposid") > 0 || q.i("stiffscaleenginenegid") > 0 || q.i("springfailureid") > 0 ||
+            q.i("springyieldid") > 0)
+          return -42;  // constant linear springs only
+        a.s0 = q.d("s0");
+        a.l0 = q.d("l0");
+        found = true;
+      }
+      if (!found) return -43;
+      springs.push_back(a);
+    } else if (r.name == "damper") {
+      Axial a;
+      a.kind = 1;
+      int t1 = r.i("triad1id"), t2 = r.i("triad2id");
+      if (t1 <= 0 || t2 <= 0) return -44;  // axial dampers only
+      if (r.i("coeffscaleengineid") > 0 || r.i("coefffuncid") > 0 || r.i("forcefuncid") > 0) return -45;
+      if ((a.tri[0] = findTriad(m, t1)) < 0 || (a.tri[1] = findTriad(m, t2)) < 0) return -46;
+      // the triad with most DOFs is triad 1 (initiateDamperTypeModule.f90:160-165)
+      if (m.triads[a.tri[0]].nDOFs < m.triads[a.tri[1]].nDOFs) std::swap(a.tri[0], a.tri[1]);
+      a.d0 = r.d("d0");
+      dampers.push_back(a);
     } else if (r.name == "motion") {
       Motion mo;
       mo.triad = findTriad(m, r.i("triadid"));
@@ -1422,6 +1578,11 @@ static int setup(OracleModel& m, const char* fsi) {
     }
   }
   (void)pendingUnd;
+  m.axials = springs;
+  m.axials.insert(m.axials.end(), dampers.begin(), dampers.end());
+  for (const Axial& a : m.axials)
+    for (int k = 0; k < 2; ++k)
+      if (m.triads[a.tri[k]].nDOFs < 3) return -47;
   // element matrices (finiteElementModule.f90:283-541, CalcBeamElementMatrices)
   for (Elem& e : m.elems) {
     const Prop& p = m.props[(int)e.kDmp];
@@ -1517,21 +1678,26 @@ static int setup(OracleModel& m, const char* fsi) {
   for (size_t k = 0; k < m.elems.size(); ++k)
     for (int n = 0; n < 2; ++n)
       for (int d = 0; d < 6; ++d) m.elEq[12 * k + 6 * n + d] = m.meqn[m.triads[m.elems[k].tri[n]].firstDof + d] - 1;
+  m.axEq.assign(6 * m.axials.size(), -1);
+  for (size_t k = 0; k < m.axials.size(); ++k)
+    for (int n = 0; n < 2; ++n)
+      for (int d = 0; d < 3; ++d) m.axEq[6 * k + 3 * n + d] = m.meqn[m.triads[m.axials[k].tri[n]].firstDof + d] - 1;
   // skyline profile and CSR upper pattern
   m.first.resize(m.neq);
   for (int j = 0; j < m.neq; ++j) m.first[j] = j;
   std::vector<std::vector<int>> rows(m.neq);
-  for (size_t k = 0; k < m.elems.size(); ++k) {
-    const int* eq = &m.elEq[12 * k];
-    for (int i = 0; i < 12; ++i) {
+  auto clique = [&](const int* eq, int n) {
+    for (int i = 0; i < n; ++i) {
       if (eq[i] < 0) continue;
-      for (int j = 0; j < 12; ++j) {
+      for (int j = 0; j < n; ++j) {
         if (eq[j] < eq[i]) continue;
         m.first[eq[j]] = std::min(m.first[eq[j]], eq[i]);
         rows[eq[i]].push_back(eq[j]);
       }
     }
-  }
+  };
+  for (size_t k = 0; k < m.elems.size(); ++k) clique(&m.elEq[12 * k], 12);
+  for (size_t k = 0; k < m.axials.size(); ++k) clique(&m.axEq[6 * k], 6);
   m.colptr.resize(m.neq + 1);
   m.colptr[0] = 0;
   for (int j = 0; j < m.neq; ++j) m.colptr[j + 1] = m.colptr[j] + (j - m.first[j] + 1);
@@ -1634,6 +1800,12 @@ extern "C" OracleModel* oracle_create(const char* fsi, int argc, const char* con
     updateLoads(*m);
     err = staticEquilibrium(*m);
     if (!err) getForceVectors(*m);
+    // motions take their start-time values without moving the triads
+    // (updatePrescribedMotionsB, motionRoutinesModule.f90:213-245)
+    for (Motion& mo : m->motions) {
+      mo.D = mo.engine >= 0 ? mo.d0 + mo.d1 * engineValue(*m, mo.engine) : mo.d0;
+      if (!err && m->opt.b("initEquilibrium", false) && mo.D != 0.0) err = -33;  // not in this subset
+    }
   }
   if (err) {
     delete m;
@@ -1760,6 +1932,22 @@ extern "C" int oracle_assemble_newton(OracleModel* m, double sM, double sC, doub
         const int* en = &m->cols[0] + m->rowptr[eq[i] + 1];
         const int* f = std::lower_bound(b, en, eq[j]);
         values[f - &m->cols[0]] += Ns[i + 12 * j];
+      }
+    }
+  }
+  for (size_t k = 0; k < m->axials.size(); ++k) {
+    double A[9];
+    axialBlock(m->axials[k], sC, sK, A);
+    const int* eq = &m->axEq[6 * k];
+    for (int i = 0; i < 6; ++i) {
+      if (eq[i] < 0) continue;
+      for (int j = 0; j < 6; ++j) {
+        if (eq[j] < eq[i]) continue;
+        const double a = A[(i % 3) + 3 * (j % 3)];
+        const int* b = &m->cols[m->rowptr[eq[i]]];
+        const int* en = &m->cols[0] + m->rowptr[eq[i] + 1];
+        const int* f = std::lower_bound(b, en, eq[j]);
+        values[f - &m->cols[0]] += (i / 3 == j / 3) ? a : -a;
       }
     }
   }

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1.0e-10   # relative displacement error of the plain FP64 path
 MIXED_TOL = 1.0e-8   # relative displacement error of FP32 factor + FP64 refinement
-GPU_FEATURES = set()  # golden-case features ("requires") the GPU path implements
+GPU_FEATURES = {"prescribed_motion", "quasi_static"}  # golden-case features the GPU path implements
 
 
 def _golden_cases():
@@ -158,3 +158,129 @@ def test_runs_are_bitwise_reproducible(gpu):
         res.append([b.triads(k) for k in range(3)])
     for a, c in zip(res[0], res[1]):
         assert np.array_equal(a, c)
+
+
+def _prescribed_chain(n_el, tip_d1):
+    from fedem_gb300 import models
+
+    return models.beam_chain_fsi(n_el, 0.25, 0.1, 0.01, clamp=0, load_node=n_el // 2, load_dof=3, load=500.0,
+                                 motion=(n_el, 2, tip_d1), **models.STEEL)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_prescribed_motion_dynamics_matches_oracle(gpu, oracle_lib, mixed):
+    """Newmark steps with a prescribed tip deflection (ramp 0.05 * t) and a
+    mid-span load: constraint values in the predictor, zero in correctors, and
+    the prescribed columns moved to the right-hand side."""
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi = _prescribed_chain(24, 0.05)
+    opts = ["-timeInc=0.002", "-timeEnd=0.3", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-9"]
+    o = OracleModel(fsi, opts)
+    ur0 = o.triads()
+    o.run_all()
+    b = Batch([Model(fsi, opts)], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0
+    err = rel_disp_error(b.triads(0), o.triads(), ur0)
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    # the prescribed DOF follows the motion exactly
+    assert abs(b.triads(0)[24, 1, 3] - 0.05 * 0.3) < 1e-12
+    if not mixed:
+        assert b.info(0)["iterations"] == o.iterations()
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_quasi_static_then_dynamic_matches_oracle(gpu, oracle_lib, mixed):
+    """Pure linear quasi-static steps (numit = -1) up to t = 0.1, then Newmark
+    steps starting from the velocity rinc / dt, against the oracle."""
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi = _prescribed_chain(16, 0.2)
+    opts = ["-numit=-1", "-timeInc=0.01", "-timeEnd=0.2", "-quasiStatic=0.1", "-tolDispNorm=1.0e-9"]
+    o = OracleModel(fsi, opts)
+    ur0 = o.triads()
+    o.run_all()
+    b = Batch([Model(fsi, opts)], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0
+    err = rel_disp_error(b.triads(0), o.triads(), ur0)
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    if not mixed:
+        assert b.info(0)["iterations"] == o.iterations()
+
+
+def _frame_with_axials():
+    from fedem_gb300 import models
+
+    return models.beam_chain_fsi(30, 0.25, 0.1, 0.01, clamp=0, load_node=30, load_dof=2, load=800.0,
+                                 **models.STEEL, anchors=[(7.5, 1.0, 0.0), (3.0, -1.0, 0.5)],
+                                 springs=[(30, ("anchor", 0), 2.0e5, 1.0), (12, 27, 5.0e4, 3.75, 0.002),
+                                          (20, ("anchor", 1), 1.0e5, 2.2)],
+                                 dampers=[(30, ("anchor", 0), 300.0), (5, 18, 120.0)])
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_axial_springs_and_dampers_dynamics_match_oracle(gpu, oracle_lib, mixed):
+    """Beam chain with axial springs (one with stiffness-proportional damping)
+    and axial dampers, to ground and across the chain, under a tip step load."""
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi = _frame_with_axials()
+    opts = ["-timeInc=0.001", "-timeEnd=0.2", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-9"]
+    o = OracleModel(fsi, opts)
+    ur0 = o.triads()
+    o.run_all()
+    b = Batch([Model(fsi, opts)], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0
+    err = rel_disp_error(b.triads(0), o.triads(), ur0)
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    if not mixed:
+        assert b.info(0)["iterations"] == o.iterations()
+
+
+def test_axial_newton_matrix_matches_oracle(gpu, oracle_lib):
+    """FP64 Newton matrix with spring and damper blocks vs the oracle's assembly."""
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi = _frame_with_axials()
+    opts = ["-timeInc=0.001", "-timeEnd=0.001"]
+    o = OracleModel(fsi, opts)
+    beta, gamma, dt, alpha = 0.3025, 0.6, 1.0e-3, -0.1
+    sM, sK = 1.0 / (beta * dt * dt), 1.0 + alpha
+    rp_u, ci_u, v_u = o.newton_upper(sM, gamma / (beta * dt) * sK, sK)
+    m = Model(fsi, opts)
+    b = Batch([m])
+    b.step(0)
+    vals = b.newton_values(0)
+    rp, ci = m.csr_pattern()
+    dense_gpu = np.zeros((m.neq, m.neq))
+    for i in range(m.neq):
+        dense_gpu[i, ci[rp[i]:rp[i + 1]]] = vals[rp[i]:rp[i + 1]]
+    dense_ref = np.zeros((m.neq, m.neq))
+    for i in range(m.neq):
+        dense_ref[i, ci_u[rp_u[i]:rp_u[i + 1]]] = v_u[rp_u[i]:rp_u[i + 1]]
+    dense_ref = np.triu(dense_ref) + np.triu(dense_ref, 1).T
+    assert np.abs(dense_gpu - dense_ref).max() <= 1e-13 * np.abs(dense_ref).max()
+
+
+def test_axial_spring_linear_static_through_solver_abi(gpu):
+    """Cantilever tip tied to ground by an axial spring along the load:
+    u = P / (k + 3EI/L^3), through solverInit (linear initial equilibrium)."""
+    from fedem_gb300 import models
+    from fedem_gb300.solver import FedemSolver
+
+    n, L = 10, 0.25
+    _, inertia, _, _ = models.pipe_section(0.1, 0.01)
+    kb = 3 * models.STEEL["E"] * inertia / (n * L) ** 3
+    fsi = models.beam_chain_fsi(n, L, 0.1, 0.01, clamp=0, load_node=n, load_dof=2, load=1000.0, **models.STEEL,
+                                anchors=[(n * L, 1.0, 0.0)], springs=[(n, ("anchor", 0), 2.0 * kb, 1.0)])
+    s = FedemSolver(solver_options=["-initEquilibrium", "-tolInitEquil=0.0"], fsi=fsi)
+    u = s.get_state_var(n + 1)[1]
+    assert abs(u - 1000.0 / (3.0 * kb)) < 1e-10 * u
+    assert s.solver_done() == 0

@@ -18,10 +18,28 @@ def _models():
         out.append((fsi, opts))
     with open(os.path.join(GOLDEN_DIR, "cantilever_pipe.fsi")) as f:
         out.append((f.read(), ["-initEquilibrium"]))
+    out.append((_frame_with_axials(), ["-timeInc=0.001", "-timeEnd=0.05"]))
+    with open(os.path.join(GOLDEN_DIR, "cantilever_prescribed.fsi")) as f:
+        out.append((f.read(), ["-numit=-1", "-timeInc=0.2", "-timeEnd=1.0", "-quasiStatic=1.0"]))
     return out
 
 
-@pytest.mark.parametrize("idx", range(8))
+def _frame_with_axials():
+    """Chain of 30 beams with anchors, axial springs (one with stiffness-
+    proportional damping) and axial dampers across the chain and to ground."""
+    from fedem_gb300 import models
+
+    return models.beam_chain_fsi(30, 0.25, 0.1, 0.01, clamp=0, load_node=30, load_dof=2, load=800.0,
+                                 **models.STEEL, anchors=[(7.5, 1.0, 0.0), (3.0, -1.0, 0.5)],
+                                 springs=[(30, ("anchor", 0), 2.0e5, 1.0), (12, 27, 5.0e4, 3.75, 0.002),
+                                          (20, ("anchor", 1), 1.0e5, 2.2)],
+                                 dampers=[(30, ("anchor", 0), 300.0), (5, 18, 120.0)])
+
+
+N_MODELS = 10
+
+
+@pytest.mark.parametrize("idx", range(N_MODELS))
 def test_setup_matches_oracle_bitwise(gpu_lib, oracle_lib, idx):
     from fedem_gb300.batch import Model
     from oracle.oracle import OracleModel
@@ -51,7 +69,7 @@ def test_setup_matches_oracle_bitwise(gpu_lib, oracle_lib, idx):
     assert all((j, i) in a for (i, j) in a)
 
 
-@pytest.mark.parametrize("idx", range(8))
+@pytest.mark.parametrize("idx", range(N_MODELS))
 def test_symbolic_factorisation_is_consistent(gpu_lib, idx):
     from fedem_gb300.batch import Model
 
@@ -137,17 +155,27 @@ def test_invalid_model_fails_loudly(gpu_lib):
         Model("&TRIAD\n id = 1\n/\n&SUP_EL\n id = 2\n numTriads = 2\n triadIds = 1 9\n/\n", [])
 
 
-def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
-    """Prescribed motions and engine-driven loads are refused with a message
-    instead of being dropped; BC code 2 counts as a free DOF when the initial
-    equilibrium iterations are off (initiateTriadTypeModule.f90:57-123)."""
-    from fedem_gb300 import FedemException, models
+def test_prescribed_dofs_numbered_as_the_oracle(gpu_lib, oracle_lib):
+    """A prescribed DOF gets MEQN = -ICEQ (samSolverModule.f90), the free DOFs
+    are numbered around it, exactly as in the oracle."""
     from fedem_gb300.batch import Model
+    from oracle.oracle import OracleModel
 
     with open(os.path.join(GOLDEN_DIR, "cantilever_prescribed.fsi")) as f:
         fsi = f.read()
-    with pytest.raises(FedemException, match="prescribed motions"):
-        Model(fsi, [])
+    opts = ["-numit=-1", "-timeInc=0.2", "-timeEnd=1.0", "-quasiStatic=1.0"]
+    g, o = Model(fsi, opts), OracleModel(fsi, opts)
+    assert np.array_equal(g.meqn(), o.meqn())
+    assert (g.meqn() < 0).sum() == 1 and g.neq == o.neq
+
+
+def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
+    """Engine-driven loads are refused with a message instead of being
+    dropped; BC code 2 counts as a free DOF when the initial equilibrium
+    iterations are off (initiateTriadTypeModule.f90:57-123)."""
+    from fedem_gb300 import FedemException, models
+    from fedem_gb300.batch import Model
+
     base = models.beam_chain_fsi(4, 1.0, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0, **models.STEEL)
     with pytest.raises(FedemException, match="loadEngineId"):
         Model(base.replace("  f0 =", "  loadEngineId = 7\n  f0 ="), [])

@@ -82,3 +82,53 @@ def test_oracle_dynamic_run_is_deterministic(oracle_lib):
     assert np.array_equal(runs[0], runs[1])
     # the tip moves in +Y under the +Y step load
     assert runs[0][20, 1, 3] > 0.0
+
+
+def _spring_cantilever(k_factor=2.0, damper=None, alpha2=0.0):
+    from fedem_gb300 import models
+
+    n, L = 10, 0.25
+    E = models.STEEL["E"]
+    _, inertia, _, _ = models.pipe_section(0.1, 0.01)
+    kb = 3 * E * inertia / (n * L) ** 3
+    k = k_factor * kb
+    fsi = models.beam_chain_fsi(n, L, 0.1, 0.01, clamp=0, load_node=n, load_dof=2, load=1000.0, **models.STEEL,
+                                anchors=[(n * L, 1.0, 0.0)], springs=[(n, ("anchor", 0), k, 1.0, alpha2)],
+                                dampers=[(n, ("anchor", 0), damper)] if damper else None)
+    return fsi, k, kb
+
+
+def test_oracle_axial_spring_linear_static_matches_theory(oracle_lib):
+    """Tip of an Euler-Bernoulli cantilever tied to ground by an axial spring
+    along the load: u = P / (k + 3EI/L^3)."""
+    from oracle.oracle import OracleModel
+
+    fsi, k, kb = _spring_cantilever()
+    o = OracleModel(fsi, ["-initEquilibrium", "-tolInitEquil=0.0"])
+    u = o.state_var(11)[1]
+    assert abs(u - 1000.0 / (k + kb)) < 1e-10 * u
+
+
+def test_oracle_axial_damper_and_spring_newton_blocks(oracle_lib):
+    """Damper coefficient c and spring stiffness k enter the Newton matrix as
+    n n^T blocks on the translational DOFs (addInDamperMat, calcSpringStiffness):
+    with n = +y, the tip's y-y entry of N(sM=0, sC, sK) grows by sK*k + sC*c."""
+    import numpy as np
+
+    from oracle.oracle import OracleModel
+
+    c = 250.0
+    fsi0, k, _ = _spring_cantilever(k_factor=0.0)
+    fsi1, k1, _ = _spring_cantilever(damper=c)
+
+    def yy(fsi, sC, sK):
+        o = OracleModel(fsi, [])
+        meqn = o.meqn()
+        rp, ci, v = o.newton_upper(0.0, sC, sK)
+        eq = meqn[6 * 10 + 1] - 1  # tip y DOF
+        row = v[rp[eq]:rp[eq + 1]]
+        return row[list(ci[rp[eq]:rp[eq + 1]]).index(eq)]
+
+    for sC, sK in ((0.0, 1.0), (1.0, 0.0), (0.7, 1.3)):
+        d = yy(fsi1, sC, sK) - yy(fsi0, sC, sK)
+        assert abs(d - (sK * k1 + sC * c)) < 1e-9 * (sK * k1 + sC * c)
