@@ -802,6 +802,18 @@ __global__ void kMotions(DevData d) {
   d.motD[k] = D;
 }
 
+// engine-driven point loads at the new time (forceRoutinesModule.f90:52-131)
+__global__ void kLoads(DevData d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.nldTot) return;
+  const int eq = d.ldEq[k], m = d.eqModel[eq];
+  if (!(d.m.flags[m] & FL_PRED)) return;
+  const double t = d.m.time[m];
+  double q = d.qextBase[eq];
+  for (int j = d.ldPtr[k]; j < d.ldPtr[k + 1]; ++j) q += d.ldF0[j] + d.ldF1[j] * (d.ldEA[j] * t + d.ldEB[j]);
+  d.qext[eq] = q;
+}
+
 // predictor right-hand side: the prescribed values times the Newton matrix
 // columns of the prescribed DOFs, moved to the right-hand side (terms with
 // |cc| <= 1e-15 skipped, sysMatrixTypeModule.f90:2099-2259)
@@ -1187,6 +1199,9 @@ void launchNormsControl(const DevData& d, cudaStream_t s) {
   kControl<<<blocksFor(32LL * d.m.n, 128), 128, 0, s>>>(d);
   long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
   kStepEnd<<<blocksFor(n), TPB, 0, s>>>(d);
+}
+void launchLoads(const DevData& d, cudaStream_t s) {
+  if (d.nldTot > 0) kLoads<<<blocksFor(d.nldTot, 128), 128, 0, s>>>(d);
 }
 void launchMotions(const DevData& d, cudaStream_t s) {
   if (d.nmotTot > 0) kMotions<<<blocksFor(d.nmotTot, 128), 128, 0, s>>>(d);

@@ -176,11 +176,31 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     for (int i = 0; i < h.neq; ++i) eqModel.push_back(k);
     qext.insert(qext.end(), h.qext.begin(), h.qext.end());
   }
+  // engine-driven loads: constant part kept, start-time value in qext
+  std::vector<double> qextBase = qext, ldF0, ldF1, ldEA, ldEB;
+  std::vector<int> ldEq, ldPtr(1, 0);
+  for (int k = 0; k < nm; ++k) {
+    const HostModel& h = *models[k];
+    for (size_t q = 0; q < h.ldEq.size(); ++q) {
+      const int eq = h.ldEq[q] + modelEqOff_[k];
+      ldEq.push_back(eq);
+      double v = qextBase[eq];
+      for (int j = h.ldPtr[q]; j < h.ldPtr[q + 1]; ++j) {
+        ldF0.push_back(h.ldF0[j]); ldF1.push_back(h.ldF1[j]); ldEA.push_back(h.ldEA[j]); ldEB.push_back(h.ldEB[j]);
+        v += h.ldF0[j] + h.ldF1[j] * (h.ldEA[j] * h.ctl.tStart + h.ldEB[j]);
+      }
+      qext[eq] = v;
+      ldPtr.push_back((int)ldF0.size());
+    }
+  }
 #define UPV(ptr, T, vec) if (!(ptr = alloc<T>(vec.size())) || put(ptr, vec, stream_) != cudaSuccess) { err = "upload " #ptr; return -903; }
   UPV(d_.ur, double, ur);
   UPV(d_.triFirstDof, int, triFirst); UPV(d_.triNdof, int, triNd); UPV(d_.triModel, int, triModel);
   UPV(d_.meqn, int, meqn); UPV(d_.dofType, int, dofType); UPV(d_.dofModel, int, dofModel);
   UPV(d_.eqModel, int, eqModel); UPV(d_.qext, double, qext);
+  d_.nldTot = (int)ldEq.size();
+  UPV(d_.qextBase, double, qextBase); UPV(d_.ldEq, int, ldEq); UPV(d_.ldPtr, int, ldPtr);
+  UPV(d_.ldF0, double, ldF0); UPV(d_.ldF1, double, ldF1); UPV(d_.ldEA, double, ldEA); UPV(d_.ldEB, double, ldEB);
   {
     // prescribed deflections and their predictor right-hand-side terms
     std::vector<int> motModel, motOff(nm), mrEq, mrMot;
@@ -540,6 +560,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     reg(p, sizeof(int) * nm);
   for (long long* p : {M.nStep, M.nIter, M.stepLimit}) reg(p, sizeof(long long) * nm);
   reg(M.qsCount, sizeof(int) * nm);
+  if (d_.nldTot > 0) reg(d_.qext, D * (size_t)neq);
   if (d_.nmotTot > 0) {
     reg(d_.motD, D * (size_t)d_.nmotTot);
     reg(d_.motCc, D * (size_t)d_.nmotTot);
@@ -619,6 +640,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   launchBeginStep(d_, dActive_, dActiveEl_, s);
   launchQsRestore(d_, s);
   launchMotions(d_, s);
+  launchLoads(d_, s);
   launchPredictDofs(d_, s);
   launchElements(d_, EM_PRED, s);
   launchResidual(d_, s);
@@ -645,7 +667,8 @@ void Engine::enqueueIteration(cudaStream_t s) {
   const int solveLaunches = opt_.persistent ? 2 * sw + (sw - 1)
                                            : sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
-                     (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0);
+                     (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
+                     (d_.nldTot > 0 ? 1 : 0);
 }
 
 int Engine::readActive() {

@@ -93,6 +93,11 @@ struct DevData {
   double* x64;  // solve vector, global equations
   float* x32;
   int* errFlag;  // set by a kernel whose bounded wait ran out
+  // engine-driven point loads: equation ldEq[k] holds qextBase (its constant loads)
+  // + sum over ldPtr[k]..ldPtr[k+1] of f0 + f1 * (eA * t + eB), refreshed in qext at step start
+  int nldTot = 0;
+  int *ldEq, *ldPtr;
+  double *ldF0, *ldF1, *ldEA, *ldEB, *qextBase;
   // axial springs and dampers (SoA): kind (0 spring, 1 damper), triads [k * naxTot + a],
   // model, constants; current direction axN (3) and length; element forces FelA
   // (FS 6, FD 6) and Newton matrices elMatA (6x6, translational DOFs of both triads).

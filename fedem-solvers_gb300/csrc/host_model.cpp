@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <array>
 #include <map>
 
 namespace fgpu {
@@ -454,6 +455,17 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   for (int k = 0; k < 18; ++k) setTol(o, tolKeys[k], c, k);
 
   std::vector<NmlRecord> recs = readNamelists(fsi);
+  // record types this path does not implement are refused, never dropped
+  for (const NmlRecord& nr : recs)
+    for (const char* bad : {"masterslavejoint", "higher_pair", "mass", "user_el", "tire", "road", "supel_load",
+                            "spring_yield", "spring_failure", "master_curve", "friction_set", "bushing_element",
+                            "contact_element", "damper_base", "external_control_system", "control_variable",
+                            "control_line", "control_input", "control_element", "wind_point", "turbine_config",
+                            "master_pos", "generic_part"})
+      if (nr.name == bad) {
+        err = "&" + nr.name + " records are not supported by the GPU solver";
+        return -50;
+      }
   std::vector<Prop> props;
   std::map<int, int> triIndex;
   // pass 1: mechanism, environment, triads, properties
@@ -591,6 +603,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.ndof += m.triNdof[t];
   }
   // pass 2: superelements, undeformed positions, loads
+  std::map<int, std::vector<std::array<double, 4>>> engineLoads;  // equation -> (f0, f1, eA, eB)
   std::vector<int> elProp;
   std::map<int, int> elIndex;
   m.qext.assign(m.neq, 0.0);
@@ -667,10 +680,24 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (it == triIndex.end()) { err = "load on unknown triad"; return -17; }
       int dof = r.inum("ldof", 0);
       if (dof < 1 || dof > m.triNdof[it->second]) { err = "load DOF must be 1..6"; return -18; }
-      if (r.inum("loadengineid", 0) > 0) { err = "time-dependent loads (loadEngineId) are not supported"; return -19; }
       int eq = m.meqn[m.triFirstDof[it->second] + dof - 1];
-      if (eq >= 0) m.qext[eq] += r.num("f0", 0.0);
+      const int eid = r.inum("loadengineid", 0);
+      if (eid > 0) {
+        auto en = engines.find(eid);
+        if (en == engines.end()) { err = "load refers to unknown engine"; return -19; }
+        if (eq >= 0) engineLoads[eq].push_back({r.num("f0", 0.0), r.num("f1", 0.0), en->second.first, en->second.second});
+      } else if (eq >= 0) {
+        m.qext[eq] += r.num("f0", 0.0);
+      }
     }
+  }
+  m.ldPtr.assign(1, 0);
+  for (auto& kv : engineLoads) {
+    m.ldEq.push_back(kv.first);
+    for (auto& l : kv.second) {
+      m.ldF0.push_back(l[0]); m.ldF1.push_back(l[1]); m.ldEA.push_back(l[2]); m.ldEB.push_back(l[3]);
+    }
+    m.ldPtr.push_back((int)m.ldF0.size());
   }
   // axial springs (SPRING_ELEMENT + SPRING_BASE) first, then axial dampers (DAMPER)
   std::map<int, const NmlRecord*> springBase;

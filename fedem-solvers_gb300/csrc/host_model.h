@@ -70,8 +70,12 @@ struct HostModel {
   std::vector<uint8_t> axKind;  // 0 spring, 1 damper
   std::vector<int> axTri, axEq; // 2 and 6 per axial element
   std::vector<double> axS0, axL0, axAlpha2, axD0;
-  // external point loads in equation order (constant f0; forceRoutinesModule.f90)
+  // external point loads in equation order: constant ones summed in qext; loads
+  // driven by an engine, F = f0 + f1 * (eA * t + eB), listed per equation in input
+  // order (forceRoutinesModule.f90:52-131): equation ldEq[k] gets ldPtr[k]..ldPtr[k+1]
   std::vector<double> qext;
+  std::vector<int> ldEq, ldPtr;
+  std::vector<double> ldF0, ldF1, ldEA, ldEB;
   // prescribed deflections (motionRoutinesModule.f90:58-193): D(t) = d0 + d1 * (eA * t + eB)
   // (engine = function of the TIME sensor); a prescribed DOF has meqn = -2 - motion index
   std::vector<int> motDof;

@@ -63,6 +63,7 @@ void launchBackwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaS
 // prescribed deflections (step start), their predictor right-hand side (after the
 // element Newton matrices), and the restart state of pure linear quasi-static steps
 void launchMotions(const DevData& d, cudaStream_t s);
+void launchLoads(const DevData& d, cudaStream_t s);
 void launchMotionRhs(const DevData& d, cudaStream_t s);
 void launchQsRestore(const DevData& d, cudaStream_t s);
 // vector glue for the solves

@@ -35,13 +35,21 @@ def _bc_line(k, clamp, motion):
     return ""
 
 
-def _loads(n_el, load_node, load_dof, load, motion):
+def _loads(n_el, load_node, load_dof, load, motion, load_ramp=None):
     """&LOAD record, or with `motion` = (triad index, DOF, d1) a prescribed
     deflection d1 * time driven by a SCALE function of the TIME sensor
     (&MOTION, &ENGINE, &FUNCTION, &SENSOR as in the reference's
-    cantilever-prescribed.fsi)."""
+    cantilever-prescribed.fsi).  `load_ramp` = r makes the load
+    load * r * time (F = f0 + f1 * engine with f0 = 0, f1 = load)."""
     out = []
-    if motion is None or load != 0.0:
+    if load_ramp is not None:
+        base = 2 * n_el + 40
+        out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
+                   f"  f0 = 0.0\n  f1 = {_f(load)}\n  loadEngineId = {base}\n/\n"
+                   f"&ENGINE\n  id = {base}\n  functionId = {base + 1}\n  nArg = 1\n  argSensorId = {base + 2}\n/\n"
+                   f"&FUNCTION\n  id = {base + 1}\n  type = 'SCALE'\n  realDataSize = 1\n  realData = {_f(load_ramp)}\n/\n"
+                   f"&SENSOR\n  id = {base + 2}\n  type = 'TIME'\n/\n")
+    elif motion is None or load != 0.0:
         out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
                    f"  f0 = {_f(load)}\n/\n")
     if motion is not None:
@@ -83,7 +91,7 @@ def _axials(n_el, anchors, springs, dampers):
 
 def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof, load,
                    shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x",
-                   motion=None, anchors=None, springs=None, dampers=None):
+                   motion=None, anchors=None, springs=None, dampers=None, load_ramp=None):
     """Solver-input text for a straight chain of `n_el` beams along X (or Z).
 
     Triad k sits at k*el_len on the axis; triad `clamp` has all six DOFs
@@ -91,14 +99,15 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
     triad `load_node`.  shear_factor = 0 gives Euler-Bernoulli beams.
     `section` = (A, Iy, Iz, It) overrides the pipe section from od/wall.
     `motion` = (triad index, DOF, d1) prescribes that DOF to d1 * time
-    (the load record is then left out when `load` is 0).  `anchors`,
+    (the load record is then left out when `load` is 0); `load_ramp` = r
+    makes the load grow as load * r * time.  `anchors`,
     `springs` and `dampers` add fixed triads and axial springs/dampers
     (see _axials).
     """
     extra = _axials(n_el, anchors, springs, dampers)
     if axis == "z":
         return _chain_along_z(n_el, el_len, section or pipe_section(od, wall), E, G, rho, clamp, load_node,
-                              load_dof, load, shear_factor, weights, title, motion) + "".join(extra)
+                              load_dof, load, shear_factor, weights, title, motion, load_ramp) + "".join(extra)
     area, iy, iz, it = section or pipe_section(od, wall)
     out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
            f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
@@ -124,12 +133,12 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
             f"  undPosInSupElSystem = 1.0 0.0 0.0 {L} 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n")
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
-    out += _loads(n_el, load_node, load_dof, load, motion)
+    out += _loads(n_el, load_node, load_dof, load, motion, load_ramp)
     return "".join(out + extra)
 
 
 def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof, load, shear_factor, weights,
-                   title, motion):
+                   title, motion, load_ramp=None):
     """Chain along global Z; the superelement X axis is the beam axis, so the
     superelement frame rotates global Z onto local X."""
     area, iy, iz, it = section
@@ -156,7 +165,7 @@ def _chain_along_z(n_el, el_len, section, E, G, rho, clamp, load_node, load_dof,
             f"  undPosInSupElSystem = {rot.format(p0=L, p1='0.0', p2='0.0')}\n/\n")
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
-    out += _loads(n_el, load_node, load_dof, load, motion)
+    out += _loads(n_el, load_node, load_dof, load, motion, load_ramp)
     return "".join(out)
 
 

@@ -1397,6 +1397,13 @@ static int staticInt(OracleModel& m) {
 
 static int setup(OracleModel& m, const char* fsi) {
   std::vector<Record> recs = parseNamelists(fsi);
+  for (const Record& r : recs)
+    for (const char* bad : {"masterslavejoint", "higher_pair", "mass", "user_el", "tire", "road", "supel_load",
+                            "spring_yield", "spring_failure", "master_curve", "friction_set", "bushing_element",
+                            "contact_element", "damper_base", "external_control_system", "control_variable",
+                            "control_line", "control_input", "control_element", "wind_point", "turbine_config",
+                            "master_pos", "generic_part"})
+      if (r.name == bad) return -50;  // not in this restatement
   for (const Record& r : recs) {
     if (r.name == "mechanism") {
       m.wDisp[0] = r.d("weighttranslation", 1.0);

@@ -284,3 +284,27 @@ def test_axial_spring_linear_static_through_solver_abi(gpu):
     u = s.get_state_var(n + 1)[1]
     assert abs(u - 1000.0 / (3.0 * kb)) < 1e-10 * u
     assert s.solver_done() == 0
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_engine_driven_load_matches_oracle(gpu, oracle_lib, mixed):
+    """Tip load growing as 2 kN * 5 t (F = f0 + f1 * engine, SCALE function of
+    the TIME sensor) with axial springs, against the oracle."""
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi = models.beam_chain_fsi(20, 0.25, 0.1, 0.01, clamp=0, load_node=20, load_dof=2, load=2000.0,
+                                **models.STEEL, load_ramp=5.0, anchors=[(5.0, 1.0, 0.0)],
+                                springs=[(20, ("anchor", 0), 3.0e4, 1.0)])
+    opts = ["-timeInc=0.002", "-timeEnd=0.2", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-9"]
+    o = OracleModel(fsi, opts)
+    ur0 = o.triads()
+    o.run_all()
+    b = Batch([Model(fsi, opts)], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0
+    err = rel_disp_error(b.triads(0), o.triads(), ur0)
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    if not mixed:
+        assert b.info(0)["iterations"] == o.iterations()

@@ -177,8 +177,10 @@ def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
     from fedem_gb300.batch import Model
 
     base = models.beam_chain_fsi(4, 1.0, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0, **models.STEEL)
-    with pytest.raises(FedemException, match="loadEngineId"):
+    with pytest.raises(FedemException, match="unknown engine"):
         Model(base.replace("  f0 =", "  loadEngineId = 7\n  f0 ="), [])
+    with pytest.raises(FedemException, match="MASTERSLAVEJOINT|masterslavejoint"):
+        Model(base + "&MASTERSLAVEJOINT\n  id = 99\n  type = 'REVOLUTE'\n/\n", [])
     free = Model(base, [])
     bc2 = Model(base.replace("&TRIAD\n  id = 5\n  nDOFs = 6\n", "&TRIAD\n  id = 5\n  nDOFs = 6\n  BC = 2 2 2 2 2 2\n"), [])
     assert bc2.neq == free.neq
