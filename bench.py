@@ -35,9 +35,30 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Newton steps/s batched+served vs plain GPU at 1e-8 rel err; p50/p99 latency"
 UNIT = "Newton steps/s"
-# algorithmic work of the element pass per beam element and launch
-ELEM_BYTES = 4040          # K, M, frames, triads, velocities in; frame, deformation, forces out
-ELEM_FP64_FLOPS = 1400     # corotation, deformation, 2 matvecs 12x12, rotations
+# algorithmic bytes of the element pass per beam element and launch: K and M
+# (2 x 1152), frames 384, triads 192, velocities 192, fg 288 in; writes 576 out
+ELEM_BYTES = 4040
+# DRAM bytes of one forward-elimination launch on this workload (256 models),
+# read + write, from the ncu capture of kForwardCascade<float>
+FORWARD_TRAFFIC_256 = 150.8e6
+
+
+def forward_bytes(models, elem_bytes):
+    """Algorithmic bytes of one forward elimination over all fronts: the L
+    blocks (nrow x npiv), the front row lists, the right-hand side (FP64) of
+    the pivot rows, the solution (pivots) and update vector (non-pivot rows)
+    written, and each update vector read back with its relative index by the
+    parent front."""
+    import numpy as np
+
+    total = 0
+    for m in models:
+        _, info = m.symbolic()
+        npiv, nrow, parent = info[:, 0].astype(np.int64), info[:, 1].astype(np.int64), info[:, 2]
+        nu = nrow - npiv
+        total += int((elem_bytes * nrow * npiv + 4 * nrow + 8 * npiv + elem_bytes * npiv + elem_bytes * nu).sum())
+        total += int(((4 + elem_bytes) * nu[parent >= 0]).sum())
+    return total
 
 
 def parse():
@@ -370,15 +391,31 @@ def main():
         extras["served"] = served_leg(args)
 
     hbm_peak, peak_kind = measured_peaks()
-    roof = None
+    roof, roof_el = None, None
     if nsamp > 0 and ms3[0] > 0:
         achieved = el_s * ELEM_BYTES / (ms3[0] * 1e-3) / 1e9
-        fp64 = el_s * ELEM_FP64_FLOPS / (ms3[0] * 1e-3) / 1e12
+        roof_el = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                   "frac": achieved / hbm_peak, "traffic": None,
+                   "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
+                   "bytes_per_element": ELEM_BYTES, "samples": nsamp}
+    if nsamp > 0 and ms3[3] > 0:
+        # the dominant kernel: one forward elimination of the refinement solve
+        fb = forward_bytes(mods, 4)
+        t_fwd = ms3[3] * 1e-3 / nsamp
+        achieved = fb / t_fwd / 1e9
+        traffic = FORWARD_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "kernel": "kElements (element pass after the increment)",
-                "peak_source": peak_kind, "fp64_tflops": fp64, "samples": nsamp,
-                "phase_ms_per_iteration": {"elements": ms3[0] / nsamp, "factor": ms3[1] / nsamp,
-                                           "solve": ms3[2] / nsamp}}
+                "traffic": traffic, "kernel": "kForwardCascade<float> (forward elimination, all fronts)",
+                "algorithmic_bytes_per_launch": fb, "launch_ms": t_fwd * 1e3, "peak_source": peak_kind,
+                "note": "latency-bound: the launch time is set by the dependency chains of the deepest "
+                        "assembly trees, not by bytes",
+                "samples": nsamp}
+    elif roof_el is not None:
+        roof = roof_el
+    phases = None
+    if nsamp > 0:
+        phases = {"elements": ms3[0] / nsamp, "factor_and_first_forward": ms3[1] / nsamp,
+                  "other_solve": ms3[2] / nsamp, "second_forward": ms3[3] / nsamp}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
@@ -396,7 +433,8 @@ def main():
                 "newton_iterations_per_time_step": iters_tot / max(tsteps_tot, 1.0),
                 "gpu_launches": kernels * batched, "kernels_per_batched_iteration": kernels,
                 "batched_iterations": batched, "models_failed": failed,
-                "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof}
+                "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof,
+                "roofline_elements": roof_el, "phase_ms_per_iteration": phases}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

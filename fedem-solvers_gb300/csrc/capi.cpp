@@ -444,9 +444,9 @@ int fgpu_batch_restore(fgpu_batch* b) {
   return rc ? fail(rc, "restore failed (no snapshot?)") : 0;
 }
 
-long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems, int reset) {
-  if (!b || !ms3) return fail(-1, "bad argument");
-  long long n = b->engine.phaseTimings(ms3, elems);
+long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset) {
+  if (!b || !ms4) return fail(-1, "bad argument");
+  long long n = b->engine.phaseTimings(ms4, elems);
   if (reset) b->engine.resetPhaseTimings();
   return n;
 }

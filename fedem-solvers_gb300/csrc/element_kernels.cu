@@ -46,23 +46,30 @@ __device__ inline void crossd(const double* a, const double* b, double* c) {
 }
 
 // rotation tensor from a rotation vector through a unit quaternion
-__device__ inline void rotvecToMat(const double* rv, double* R /* col-major 3x3 */) {
+// (rotationModule.f90:355-370,393-436).  For half angles below epsTh2 = 5e-4
+// the reference interpolates sin(h)/h linearly (sinEpsOverEps = sin(epsTh2)/epsTh2,
+// evaluated on the host); cos(h) is then its Taylor series to h^6 (the next
+// term is below 1e-30), which spares the FP64 sine/cosine on the usual small
+// increments.  The quaternion is normalised twice, by one reciprocal each.
+__device__ inline void rotvecToMat(const double* rv, double sinEpsOverEps, double* R /* col-major 3x3 */) {
   const double epsTh2 = 0.0005;
   double thh = 0.5 * sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
-  double sthh, cthh;
-  sincos(thh, &sthh, &cthh);
-  double fac;
+  double cthh, fac;
   if (thh < epsTh2) {
+    const double h2 = thh * thh;
+    cthh = 1.0 - h2 * (0.5 - h2 * (1.0 / 24.0 - h2 * (1.0 / 720.0)));
     double f1 = thh / epsTh2;
-    fac = f1 * sin(epsTh2) / epsTh2 + 1.0 - f1;
+    fac = f1 * sinEpsOverEps + 1.0 - f1;
   } else {
+    double sthh;
+    sincos(thh, &sthh, &cthh);
     fac = sthh / thh;
   }
   double q0 = cthh, q1 = rv[0] * fac * 0.5, q2 = rv[1] * fac * 0.5, q3 = rv[2] * fac * 0.5;
-  double n = sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-  q0 /= n; q1 /= n; q2 /= n; q3 /= n;
-  n = sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-  q0 /= n; q1 /= n; q2 /= n; q3 /= n;
+  double inv = 1.0 / sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+  q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
+  inv = 1.0 / sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+  q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
   R[0] = 2.0 * (q1 * q1 + q0 * q0) - 1.0;
   R[4] = 2.0 * (q2 * q2 + q0 * q0) - 1.0;
   R[8] = 2.0 * (q3 * q3 + q0 * q0) - 1.0;
@@ -733,7 +740,7 @@ __global__ void kCsrGather(DevData d) {
   if (!(d.m.flags[d.slotModel[s]] & FL_TANGENT)) return;
   double v = 0.0;
   const int64_t lim = (int64_t)144 * d.nelTot;
-  for (long long k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) {
+  for (int k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) {
     const int64_t src = d.slotSrc[k];
     v += src < lim ? d.elMat[src] : d.elMatA[src - lim];
   }
@@ -781,7 +788,7 @@ __global__ void kIncrement(DevData d) {
       for (int r = 0; r < 3; ++r) U[9 + r] += inc[r];
       if (nd == 6) {
         double R[9], O[9];
-        rotvecToMat(inc + 3, R);
+        rotvecToMat(inc + 3, d.sinEpsOverEps, R);
         for (int c = 0; c < 3; ++c)
           for (int r = 0; r < 3; ++r) O[r + 3 * c] = R[r] * U[3 * c] + R[r + 3] * U[3 * c + 1] + R[r + 6] * U[3 * c + 2];
         for (int k = 0; k < 9; ++k) U[k] = O[k];
@@ -902,12 +909,28 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
   double v[NPART];
 #pragma unroll
   for (int k = 0; k < NPART; ++k) v[k] = 0.0;
-  for (int i = d.chunkStart[c] + threadIdx.x; i < d.chunkEnd[c]; i += CHUNK_TPB) {
-    int eq = d.meqn[i];
-    if (eq < 0) continue;
-    int t = d.dofType[i] - 1;
+  const int cEnd = d.chunkEnd[c];
+  for (int i0 = d.chunkStart[c] + threadIdx.x; i0 < cEnd; i0 += 4 * CHUNK_TPB) {
+    // four DOFs per pass: all loads issued before the ordered accumulation
+    int eqs[4], ts[4];
+    double a0[4], a1[4], a2[4], rr[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * CHUNK_TPB;
+      eqs[u] = i < cEnd ? d.meqn[i] : -1;
+      ts[u] = i < cEnd ? d.dofType[i] - 1 : 0;
+      a0[u] = i < cEnd ? d.sinc0[i] : 0.0;
+      a1[u] = i < cEnd ? d.sinc1[i] : 0.0;
+      a2[u] = i < cEnd ? d.sinc2[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) rr[u] = eqs[u] >= 0 ? d.res[eqs[u]] : 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+    if (eqs[u] < 0) continue;
+    const int t = ts[u];
     double wd = wD[t], wf = wF[t];
-    double s0 = d.sinc0[i], s1 = d.sinc1[i], s2 = d.sinc2[i], r = d.res[eq];
+    double s0 = a0[u], s1 = a1[u], s2 = a2[u], r = rr[u];
     if (isBad(s0) || isBad(r)) v[20] = 1.0;
     v[0] += wd * wd;
     v[1] += wf * wf;
@@ -925,6 +948,7 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
       v[11 + q] = fmax(v[11 + q], fabs(s1));
       v[14 + q] = fmax(v[14 + q], fabs(s2));
       v[17 + q] = fmax(v[17 + q], fabs(r));
+    }
     }
   }
   // warp tree (fixed pattern), then warps in order
@@ -1131,7 +1155,7 @@ __global__ void kStaticIncrement(DevData d) {
       for (int r = 0; r < 3; ++r) U[9 + r] += inc[r];
       if (nd == 6) {
         double R[9], O[9];
-        rotvecToMat(inc + 3, R);
+        rotvecToMat(inc + 3, d.sinEpsOverEps, R);
         for (int c = 0; c < 3; ++c)
           for (int r = 0; r < 3; ++r) O[r + 3 * c] = R[r] * U[3 * c] + R[r + 3] * U[3 * c + 1] + R[r + 6] * U[3 * c + 2];
         for (int k = 0; k < 9; ++k) U[k] = O[k];

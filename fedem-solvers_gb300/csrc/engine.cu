@@ -12,7 +12,9 @@
 // per-model flags, so models of uneven size and iteration count share launches.
 
 #include <chrono>
+#include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstring>
 
 #include "engine.h"
@@ -241,6 +243,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     d_.motCc = alloc<double>(motModel.size());
     UPV(d_.mrEq, int, mrEq); UPV(d_.mrMot, int, mrMot); UPV(d_.mrPtr, int64_t, mrPtr); UPV(d_.mrSrc, int64_t, mrSrc);
     d_.linearIters = opt_.fp32Factor ? 3 : 1;
+    d_.sinEpsOverEps = std::sin(0.0005) / 0.0005;
     if (anyLinearQs) {
       d_.urQs = alloc<double>(12 * (size_t)ntri); d_.supTrQs = alloc<double>(12 * (size_t)nel);
       d_.urdQs = alloc<double>(ndof); d_.urddQs = alloc<double>(ndof);
@@ -403,7 +406,12 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   }
   // ---- CSR and gather maps -----------------------------------------------------------
   {
-    std::vector<int64_t> rowPtr(neq + 1, 0), slotPtr(nslot + 1, 0), slotSrc;
+    if (ncontrib >= INT_MAX || 144LL * nel + 36LL * nax >= INT_MAX) {
+      err = "batch too large for 32-bit CSR gather lists";
+      return -901;
+    }
+    std::vector<int64_t> rowPtr(neq + 1, 0);
+    std::vector<int> slotPtr(nslot + 1, 0), slotSrc;
     std::vector<int> colInd, slotModel, eqPtr(neq + 1, 0), eqSrc;
     colInd.reserve(nslot);
     slotModel.reserve(nslot);
@@ -423,10 +431,10 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       for (int src : h.slotSrc) {
         if (src < 144 * h.nel) {
           int e = src / 144, entry = src % 144;
-          slotSrc.push_back((int64_t)entry * nel + modelElOff_[k] + e);
+          slotSrc.push_back(entry * nel + modelElOff_[k] + e);
         } else {  // axial element entry
           int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
-          slotSrc.push_back((int64_t)144 * nel + (int64_t)entry * nax + modelAxOff[k] + a);
+          slotSrc.push_back(144 * nel + entry * nax + modelAxOff[k] + a);
         }
       }
       for (int src : h.eqSrc) {
@@ -439,8 +447,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         }
       }
     }
-    UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int64_t, slotPtr);
-    UPV(d_.slotSrc, int64_t, slotSrc); UPV(d_.slotModel, int, slotModel); UPV(d_.eqPtr, int, eqPtr);
+    UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int, slotPtr);
+    UPV(d_.slotSrc, int, slotSrc); UPV(d_.slotModel, int, slotModel); UPV(d_.eqPtr, int, eqPtr);
     UPV(d_.eqSrc, int, eqSrc);
     d_.csrVal = alloc<double>(nslot);
   }
@@ -483,6 +491,24 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(d_.fAsmOff, int64_t, asmOffV);
     UPV(d_.frontRows, int, frontRows); UPV(d_.childList, int, childList); UPV(d_.relIndex, int, relIndex);
     UPV(d_.asmSlot, int64_t, asmSlot); UPV(d_.asmPos, int, asmPos);
+    {
+      // per-front list of the children's update rows: W source index and (child
+      // ordinal << 16 | row in this front), children in order
+      std::vector<int> cgOff(nfr + 1, 0), cgSrc, cgDst;
+      for (int f = 0; f < nfr; ++f) {
+        for (int c = 0; c < nchild[f]; ++c) {
+          const int ch = childList[childOffV[f] + c];
+          const int cu = nrow[ch] - npiv[ch];
+          for (int a = 0; a < cu; ++a) {
+            cgSrc.push_back((int)(wOffV[ch] + a));
+            cgDst.push_back((c << 16) | relIndex[relOffV[ch] + a]);
+          }
+        }
+        cgOff[f + 1] = (int)cgSrc.size();
+      }
+      if (nw >= INT_MAX) { err = "batch too large for 32-bit update-vector indices"; return -908; }
+      UPV(d_.cgOff, int, cgOff); UPV(d_.cgSrc, int, cgSrc); UPV(d_.cgDst, int, cgDst);
+    }
     if (opt_.fp32Factor) {
       d_.L32 = alloc<float>(nl); d_.U32 = alloc<float>(nu); d_.w32 = alloc<float>(nw);
       if (!d_.L32 || !d_.U32 || !d_.w32) { err = "out of device memory (factor)"; return -904; }
@@ -508,9 +534,20 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       if (perWarpBytes > 200 * 1024) { err = "front too large for the shared-memory front kernels"; return -905; }
       levels_.push_back(lp);
     }
+    // leaf-to-root path lengths: parents follow their children in each model's order
+    std::vector<int> pathLen(nfr, 1);
+    pplan_.maxPath = 1;
+    for (int f = nfr - 1; f >= 0; --f) {
+      if (parent[f] > f) pathLen[f] = pathLen[parent[f]] + 1;
+      else if (parent[f] >= 0) { err = "assembly tree not in post-order"; return -907; }
+      pplan_.maxPath = std::max(pplan_.maxPath, pathLen[f]);
+    }
+    // leaves with the longest paths first: the cascades' critical paths (the
+    // deep trees of the large models) start in the first wave of warps
     std::vector<int> leaves;
     for (int f = 0; f < nfr; ++f)
       if (nchild[f] == 0) leaves.push_back(f);
+    std::stable_sort(leaves.begin(), leaves.end(), [&](int a, int b) { return pathLen[a] > pathLen[b]; });
     int* dLeaves = nullptr;
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
@@ -519,14 +556,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     for (const LevelPlan& lp : levels_) pplan_.maxRow = std::max(pplan_.maxRow, lp.maxRow);
     pplan_.maxNpiv = 1;
     for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
-    // longest leaf-to-root path: parents follow their children in each model's order
-    std::vector<int> pathLen(nfr, 1);
-    pplan_.maxPath = 1;
-    for (int f = nfr - 1; f >= 0; --f) {
-      if (parent[f] > f) pathLen[f] = pathLen[parent[f]] + 1;
-      else if (parent[f] >= 0) { err = "assembly tree not in post-order"; return -907; }
-      pplan_.maxPath = std::max(pplan_.maxPath, pathLen[f]);
-    }
     pplan_.cntFactor = alloc<int>(nfr);
     pplan_.cntForward = alloc<int>(nfr);
     pplan_.stateBackward = alloc<int>(nfr);
@@ -596,33 +625,37 @@ int Engine::restore() {
   return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -933;
 }
 
-long long Engine::phaseTimings(double* ms3, long long* elems) {
-  for (int k = 0; k < 3; ++k) ms3[k] = phaseMs_[k];
+long long Engine::phaseTimings(double* ms4, long long* elems) {
+  for (int k = 0; k < 4; ++k) ms4[k] = phaseMs_[k];
   if (elems) *elems = phaseElems_;
   return phaseSamples_;
 }
 
 void Engine::resetPhaseTimings() {
-  phaseMs_[0] = phaseMs_[1] = phaseMs_[2] = 0.0;
+  phaseMs_[0] = phaseMs_[1] = phaseMs_[2] = phaseMs_[3] = 0.0;
   phaseSamples_ = phaseElems_ = 0;
 }
 
 void Engine::enqueueFactor(cudaStream_t s) {
   if (opt_.persistent) {
-    launchFactorCascade(d_, pplan_, opt_.fp32Factor, s);
+    // factorisation and the first forward elimination in one cascade
+    launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
     return;
   }
   for (const LevelPlan& lv : levels_) launchFactorLevel(d_, lv, opt_.fp32Factor, s);
 }
 
-void Engine::enqueueSolve(cudaStream_t s) {
+void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
   const bool f32 = opt_.fp32Factor;
   const int sw = opt_.refineSweeps;
   for (int sweep = 0; sweep < sw; ++sweep) {
     if (sweep > 0) launchRefineResidual(d_, s);
     if (opt_.persistent) {
-      // the right-hand side is read and the solution stored inside the two launches
-      launchForwardCascade(d_, pplan_, f32, (f32 && sweep > 0) ? d_.rref : d_.del, s);
+      // the right-hand side is read and the solution stored inside the launches;
+      // the first forward elimination ran with the factorisation
+      if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[5], s, cudaEventRecordExternal);
+      if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
+      if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[6], s, cudaEventRecordExternal);
       launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
     } else {
       launchSolveSetup(d_, f32, sweep, s);
@@ -651,7 +684,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   cudaEventRecordWithFlags(ev_[0], s, cudaEventRecordExternal);
   enqueueFactor(s);
   cudaEventRecordWithFlags(ev_[1], s, cudaEventRecordExternal);
-  enqueueSolve(s);
+  enqueueSolve(s, true);
   cudaEventRecordWithFlags(ev_[2], s, cudaEventRecordExternal);
   launchIncrement(d_, s);
   cudaEventRecordWithFlags(ev_[3], s, cudaEventRecordExternal);
@@ -664,7 +697,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   // increment, norms partial + control, step end)
   // + factor launches + per sweep the forward and backward launches (per-height launches
   // with separate set-up/accumulate kernels when not persistent) + refinement residuals
-  const int solveLaunches = opt_.persistent ? 2 * sw + (sw - 1)
+  const int solveLaunches = opt_.persistent ? 2 * sw - 1 + (sw - 1)
                                            : sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
@@ -750,6 +783,9 @@ int Engine::run(long long maxBatched, RunStats* stats) {
       phaseMs_[0] += t0;
       phaseMs_[1] += t1;
       phaseMs_[2] += t2;
+      float t3 = 0.0f;
+      if (opt_.persistent && opt_.refineSweeps > 1 && cudaEventElapsedTime(&t3, ev_[5], ev_[6]) == cudaSuccess)
+        phaseMs_[3] += t3;
       phaseElems_ += *hActiveEl_;
       ++phaseSamples_;
     }

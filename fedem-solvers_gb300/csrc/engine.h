@@ -81,16 +81,18 @@ class Engine {
   int snapshot();
   int restore();
   // Phase timings sampled with CUDA events inside the captured iteration:
-  // phase 0 = element pass after the increment, 1 = factorisation, 2 = solve.
-  // Returns samples; ms[3] = summed milliseconds, elems = summed active elements.
-  long long phaseTimings(double* ms3, long long* activeElems);
+  // phase 0 = element pass after the increment, 1 = factorisation with the
+  // first forward elimination, 2 = the rest of the solves, 3 = the forward
+  // elimination of the second solve (persistent mixed-precision batches; else 0).
+  // Returns samples; ms[4] = summed milliseconds, elems = summed active elements.
+  long long phaseTimings(double* ms4, long long* activeElems);
   void resetPhaseTimings();
 
  private:
   template <typename T>
   T* alloc(size_t n);
   void enqueueIteration(cudaStream_t s);
-  void enqueueSolve(cudaStream_t s);
+  void enqueueSolve(cudaStream_t s, bool timedForward = false);
   void enqueueFactor(cudaStream_t s);
   int readActive();
 
@@ -115,7 +117,7 @@ class Engine {
   std::vector<std::pair<void*, size_t>> mutable_;
   char* backup_ = nullptr;
   // phase timing events (recorded as external event nodes inside the graph)
-  cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   long long* dActiveEl_ = nullptr;
   long long* hActiveEl_ = nullptr;
   cudaEvent_t evRun_[2] = {nullptr, nullptr};
@@ -124,7 +126,7 @@ class Engine {
   cudaEvent_t evChunk_ = nullptr;
   bool chunkPending_ = false;
   size_t deviceBytes_ = 0;
-  double phaseMs_[3] = {0, 0, 0};
+  double phaseMs_[4] = {0, 0, 0, 0};
   long long phaseSamples_ = 0, phaseElems_ = 0;
 };
 

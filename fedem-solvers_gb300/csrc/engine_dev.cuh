@@ -75,8 +75,8 @@ struct DevData {
   int64_t* rowPtr;  // neqTot + 1
   int* colInd;
   double* csrVal;
-  int64_t* slotPtr;
-  int64_t* slotSrc;  // SoA index into elMat
+  int* slotPtr;      // 32-bit: a batch keeps its slot contributions below 2^31
+  int* slotSrc;      // SoA index into elMat (elMatA above 144 * nelTot)
   int* slotModel;
   int *eqPtr, *eqSrc;  // eqSrc = local * nelTot + element
   // fronts (global indices)
@@ -84,6 +84,9 @@ struct DevData {
   int *fNpiv, *fNrow, *fParent, *fModel, *fNchild, *fNasm;
   int64_t *fRowOff, *fLOff, *fUOff, *fWOff, *fChildOff, *fRelOff, *fAsmOff;
   int *frontRows, *childList, *relIndex;
+  // children's update rows of each front, in child order: W index and
+  // (child ordinal << 16 | destination row), cgOff[f]..cgOff[f+1]
+  int *cgOff, *cgSrc, *cgDst;
   int64_t* asmSlot;
   int* asmPos;
   double *L64, *U64;
@@ -122,6 +125,8 @@ struct DevData {
   // single reference solve is followed by corrections against the FP64 residual
   // Q - FS (iterative refinement of the same linear system)
   int linearIters = 1;
+  // sin(5e-4) / 5e-4 for the small-angle branch of the rotation update
+  double sinEpsOverEps = 1.0;
   // DOF chunks for the two-stage norm reduction (each chunk within one model)
   int nchunkTot = 0;
   int *chunkModel, *chunkStart, *chunkEnd, *modelChunkOff, *modelNchunk;

@@ -112,35 +112,39 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
 // w = v_u - L21 y; X(pivots) = D^-1 y
 // copies the nr x np block L of a front into the warp's staging area Ls when
 // it fits (capL values), else returns the global block
-// (callers __syncwarp before reading Ls)
+// asynchronous global -> shared copies of single elements (cp.async): every
+// copy of a block is in flight at once and none occupies a register
+template <typename T>
+__device__ inline void copyAsync(T* dstShared, const T* srcGlobal) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(dstShared);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(srcGlobal), "n"(sizeof(T)));
+}
+__device__ inline void copyAsyncWait() {
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// copies the L block into Ls (callers wait with copyAsyncWait and __syncwarp
+// before reading Ls); returns the global block when it does not fit
 template <typename T>
 __device__ inline const T* stageL(const T* Lg, int cnt, T* Ls, int capL, int lane) {
   if (cnt > capL) return Lg;
-  for (int k0 = 0; k0 < cnt; k0 += 128) {
-    T v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = k0 + 32 * u + lane;
-      v[u] = k < cnt ? __ldg(Lg + k) : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = k0 + 32 * u + lane;
-      if (k < cnt) Ls[k] = v[u];
-    }
-  }
+  for (int k = lane; k < cnt; k += 32) copyAsync(Ls + k, Lg + k);
   return Ls;
 }
 
 template <typename T>
 __device__ void forwardOneFront(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase, const double* rhs,
-                                T* X, T* W, int lane) {
+                                T* X, T* W, int lane, const T* Lres = nullptr) {
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
   const int* rows = d.frontRows + d.fRowOff[f];
-  // the factor block first (independent loads), then the right-hand side of
-  // the pivot rows rounded to the solve precision
-  const T* L = stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
+  // the factor block first (independent loads; or the front just factored in
+  // shared memory), then the right-hand side of the pivot rows rounded to the
+  // solve precision
+  const T* L = Lres ? Lres : stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
   for (int r = lane; r < nr; r += 32) v[r] = r < np ? (T)rhs[__ldg(rows + r)] : T(0);
+  copyAsyncWait();
   __syncwarp();
   const int nc = d.fNchild[f];
   const int64_t co = d.fChildOff[f];
@@ -161,6 +165,70 @@ __device__ void forwardOneFront(const DevData& d, int f, T* v, T* Ls, int capL, 
   for (int r = lane; r < np; r += 32) X[rows[r]] = v[r] / L[r + (size_t)nr * r];
   T* wo = W + d.fWOff[f];
   for (int a = lane; a < nu; a += 32) wo[a] = v[np + a];
+}
+
+// Forward elimination with few dependent memory round trips (fronts of at most
+// 64 rows and 64 child update rows): the front's descriptors, then its L block
+// (asynchronous copies), row list and child gather list together, then the
+// right-hand side and the children's update values together.
+
+template <typename T>
+__device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase,
+                                    const double* rhs, T* X, T* W, int lane, const T* Lres) {
+  const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
+  const int cg0 = d.cgOff[f], ncg = d.cgOff[f + 1] - cg0, nch = d.fNchild[f];
+  const int cnt = nr * np;
+  if (nr > 64 || ncg > 64 || (!Lres && cnt > capL)) return false;
+  const int* rows = d.frontRows + d.fRowOff[f];
+  // round 2: independent loads (the L block asynchronously into shared memory)
+  if (!Lres) {
+    const T* Lg = Lbase + d.fLOff[f];
+    for (int k = lane; k < cnt; k += 32) copyAsync(Ls + k, Lg + k);
+  }
+  int row[2], src[2], dst[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = lane + 32 * u;
+    row[u] = r < np ? __ldg(rows + r) : -1;
+    src[u] = r < ncg ? __ldg(d.cgSrc + cg0 + r) : -1;
+    dst[u] = r < ncg ? __ldg(d.cgDst + cg0 + r) : 0;
+  }
+  // round 3: values through the indices
+  double b[2];
+  T wv[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    b[u] = row[u] >= 0 ? rhs[row[u]] : 0.0;
+    wv[u] = src[u] >= 0 ? __ldcg(W + src[u]) : T(0);
+  }
+  if (!Lres) copyAsyncWait();
+  const T* L = Lres ? Lres : Ls;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = lane + 32 * u;
+    if (r < nr) v[r] = r < np ? (T)b[u] : T(0);
+  }
+  __syncwarp();
+  for (int c = 0; c < nch; ++c) {
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (src[u] >= 0 && (dst[u] >> 16) == c) v[dst[u] & 0xffff] += wv[u];
+    __syncwarp();
+  }
+  for (int k = 0; k < np; ++k) {
+    const T yk = v[k];
+    __syncwarp();
+    for (int i = k + 1 + lane; i < nr; i += 32) v[i] -= L[i + (size_t)nr * k] * yk;
+    __syncwarp();
+  }
+  T* wo = W + d.fWOff[f];
+  for (int a = lane; a < nu; a += 32) wo[a] = v[np + a];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = lane + 32 * u;
+    if (r < np) X[row[u]] = v[r] / L[r + (size_t)nr * r];
+  }
+  return true;
 }
 
 // After a front is done: release its data and count it at the parent; returns
@@ -200,6 +268,39 @@ __global__ void kFactorCascade(DevData d, const int* __restrict__ leaves, int nL
   }
 }
 
+// factorisation (models with a tangent update) fused with the forward
+// elimination of the first solve (all active models): one climb per front, and
+// the forward elimination reads L from the front still in shared memory
+template <typename T>
+__global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, T* Lbase,
+                                      T* Ubase, double tolFact, const double* rhs, T* X, T* Wv, int* cnt) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int Wt = gridDim.x * wpb;
+  const int capL = maxRow * maxRow;  // F doubles as the staging area of L
+  T* F = reinterpret_cast<T*>(smraw) + (size_t)w * ((size_t)maxRow * maxRow + 3 * maxRow);
+  T* lcol = F + (size_t)maxRow * maxRow;
+  T* diag0 = lcol + maxRow;
+  T* v = diag0 + maxRow;
+  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
+    int f = leaves[idx];
+    const int fl = d.m.flags[d.fModel[f]];
+    if (!(fl & FL_ACTIVE)) continue;
+    const bool factor = fl & FL_TANGENT;
+    while (f >= 0) {
+      const T* Lres = nullptr;
+      if (factor) {
+        factorOneFront<T>(d, f, F, lcol, diag0, Ubase, Lbase, Ubase, tolFact, lane);
+        __syncwarp();
+        Lres = F;
+      }
+      if (!forwardOneFrontFast<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres))
+        forwardOneFront<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres);
+      f = climb(d, f, cnt, lane);
+    }
+  }
+}
+
 template <typename T>
 __global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
                                 const T* Lbase, const double* rhs, T* X, T* W, int* cnt) {
@@ -212,7 +313,8 @@ __global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int n
     int f = leaves[idx];
     if (!(d.m.flags[d.fModel[f]] & FL_ACTIVE)) continue;
     while (f >= 0) {
-      forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
+      if (!forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr))
+        forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
       f = climb(d, f, cnt, lane);
     }
   }
@@ -232,6 +334,7 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
   const int* rows = d.frontRows + d.fRowOff[f];
   const T* L = stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
   for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + __ldg(rows + r));
+  copyAsyncWait();
   __syncwarp();
   for (int k = lane; k < np; k += 32) {
     T acc = xs[k];
@@ -367,6 +470,29 @@ void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, c
     const int blocks = occupancyBlocks(kFactorCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
     kFactorCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L64, d.U64, tol,
                                                         p.cntFactor);
+  }
+}
+
+void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
+                                cudaStream_t s) {
+  if (p.nLeaves <= 0) return;
+  const double tol = 1.0e-12;
+  const size_t perWarp = (size_t)p.maxRow * p.maxRow + 3 * p.maxRow;
+  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * (size_t)d.nfrontTot, s);
+  if (fp32) {
+    const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
+    const size_t sm = (size_t)wpb * perWarp * sizeof(float);
+    allowBigSmem(kFactorForwardCascade<float>, sm);
+    const int blocks = occupancyBlocks(kFactorForwardCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
+    kFactorForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L32, d.U32, tol,
+                                                             rhs, d.x32, d.w32, p.cntFactor);
+  } else {
+    const int wpb = factorWarpsPerBlock(perWarp * sizeof(double));
+    const size_t sm = (size_t)wpb * perWarp * sizeof(double);
+    allowBigSmem(kFactorForwardCascade<double>, sm);
+    const int blocks = occupancyBlocks(kFactorForwardCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
+    kFactorForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L64, d.U64, tol,
+                                                               rhs, d.x64, d.w64, p.cntFactor);
   }
 }
 

@@ -51,6 +51,10 @@ struct PersistentPlan {
   int *cntFactor, *cntForward, *stateBackward, *errFlag;
 };
 void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
+// factorisation of the models with a tangent update fused with the forward
+// elimination of rhs for every active model (first solve of an iteration)
+void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
+                                cudaStream_t s);
 // forward elimination of the right-hand side rhs (FP64, rounded to the solve precision)
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s);
 // back substitution; stores the solution in del (FP64 solve) or accumulates it in xref

@@ -142,8 +142,9 @@ class Batch:
             raise FedemException("restore failed: " + self._lib.fgpu_last_error().decode())
 
     def phase_timings(self, reset=False):
-        """(samples, [element ms, factor ms, solve ms], active elements) sampled inside run()."""
-        ms = np.zeros(3)
+        """(samples, [element ms, factor + first forward ms, other solve ms, second forward ms],
+        active elements) sampled inside run()."""
+        ms = np.zeros(4)
         el = ctypes.c_longlong()
         n = self._lib.fgpu_batch_phase_timings(self._h, _ptr(ms, ctypes.c_double), ctypes.byref(el),
                                                1 if reset else 0)

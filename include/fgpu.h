@@ -88,12 +88,14 @@ int fgpu_batch_step(fgpu_batch* b, int model, int* state);
  * copies (a rerun from the initial state without host transfers). */
 int fgpu_batch_snapshot(fgpu_batch* b);
 int fgpu_batch_restore(fgpu_batch* b);
-/* CUDA-event samples of three phases of the batched iteration, taken inside
- * fgpu_batch_run: ms3 = summed milliseconds of {element pass after the
- * increment, multifrontal factorisation, triangular solves incl. refinement};
- * elems = summed active elements of the sampled iterations.  Returns the
- * number of samples; reset != 0 clears the accumulators afterwards. */
-long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms3, long long* elems, int reset);
+/* CUDA-event samples of phases of the batched iteration, taken inside
+ * fgpu_batch_run: ms4 = summed milliseconds of {element pass after the
+ * increment, multifrontal factorisation with the first forward elimination,
+ * the remaining solve launches incl. refinement, the forward elimination of
+ * the second solve (0 with one solve)}; elems = summed active elements of the
+ * sampled iterations.  Returns the number of samples; reset != 0 clears the
+ * accumulators afterwards. */
+long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset);
 
 /* ---- serving: continuous batching of simulation requests ------------------
  * Requests are admitted into new GPU batches (own stream each) as soon as the
