@@ -735,9 +735,15 @@ __global__ void __launch_bounds__(128) kNewtonBeam(DevData d) {
 
 // CSR slot gather (deterministic segmented reduction over element contributions)
 __global__ void kCsrGather(DevData d) {
+  // a block whose slots all belong to one model reads its flags once
+  __shared__ int blockFlags;
+  const int bm = d.slotBlockModel[blockIdx.x];
+  if (threadIdx.x == 0) blockFlags = bm >= 0 ? d.m.flags[bm] : FL_TANGENT;
+  __syncthreads();
+  if (!(blockFlags & FL_TANGENT)) return;
   long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.nslotTot) return;
-  if (!(d.m.flags[d.slotModel[s]] & FL_TANGENT)) return;
+  if (bm < 0 && !(d.m.flags[d.slotModel[s]] & FL_TANGENT)) return;
   double v = 0.0;
   const int64_t lim = (int64_t)144 * d.nelTot;
   for (int k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) {
@@ -745,6 +751,12 @@ __global__ void kCsrGather(DevData d) {
     v += src < lim ? d.elMat[src] : d.elMatA[src - lim];
   }
   d.csrVal[s] = v;
+  // front-ordered copy for the factorisation, in its precision
+  const int a = d.slotAsm[s];
+  if (a >= 0) {
+    if (d.asmVal32) d.asmVal32[a] = (float)v;
+    else d.asmVal64[a] = v;
+  }
 }
 
 // increment: expand the solution, update velocities/accelerations and triads
@@ -1212,7 +1224,7 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
   if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
-  if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot), TPB, 0, s>>>(d);
+  if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot, kSlotBlock), kSlotBlock, 0, s>>>(d);
 }
 void launchIncrement(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;

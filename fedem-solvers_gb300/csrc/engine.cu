@@ -86,7 +86,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   std::vector<int> frontOff(nm, 0);
   std::vector<int64_t> contribOff(nm, 0), eqContribOff(nm, 0), rowsOff(nm, 0), lOff(nm, 0), uOff(nm, 0),
       wOff(nm, 0), childOff(nm, 0), relOff(nm, 0), asmOff(nm, 0);
-  int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, maxH = 0, nax = 0;
+  int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, nax = 0;
   std::vector<int> modelAxOff(nm, 0);
   int64_t nslot = 0, ncontrib = 0, neqc = 0, nrows = 0, nl = 0, nu = 0, nw = 0, nch = 0, nrel = 0, nasm = 0;
   bool anyC = false;
@@ -102,7 +102,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     nslot += (int64_t)h.colInd.size(); ncontrib += (int64_t)h.slotSrc.size(); neqc += (int64_t)h.eqSrc.size();
     nrows += (int64_t)h.frontRows.size(); nl += h.lSize; nu += h.uSize; nw += h.wSize;
     nch += (int64_t)h.childList.size(); nrel += (int64_t)h.relIndex.size(); nasm += (int64_t)h.asmSlot.size();
-    maxH = std::max(maxH, h.maxHeight);
     for (uint8_t c : h.hasC) anyC |= c != 0;
   }
   if (12LL * nel + 6LL * nax > INT_MAX || neqc > INT_MAX) { err = "batch too large for 32-bit gather indices"; return -901; }
@@ -449,6 +448,14 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     }
     UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int, slotPtr);
     UPV(d_.slotSrc, int, slotSrc); UPV(d_.slotModel, int, slotModel); UPV(d_.eqPtr, int, eqPtr);
+    {
+      std::vector<int> blockModel((nslot + kSlotBlock - 1) / kSlotBlock, -1);
+      for (size_t b = 0; b < blockModel.size(); ++b) {
+        const int64_t s0 = (int64_t)b * kSlotBlock, s1 = std::min<int64_t>(nslot, s0 + kSlotBlock) - 1;
+        blockModel[b] = slotModel[s0] == slotModel[s1] ? slotModel[s0] : -1;
+      }
+      UPV(d_.slotBlockModel, int, blockModel);
+    }
     UPV(d_.eqSrc, int, eqSrc);
     d_.csrVal = alloc<double>(nslot);
   }
@@ -456,8 +463,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   {
     std::vector<int> npiv, nrow, parent, fmodel, nchild, nasmv, frontRows, childList, relIndex, asmPos;
     std::vector<int64_t> rowOffV, lOffV, uOffV, wOffV, childOffV, relOffV, asmOffV, asmSlot;
-    std::vector<std::vector<int>> byHeight(maxH + 1);
-    std::vector<int> maxRowH(maxH + 1, 0);
     for (int k = 0; k < nm; ++k) {
       const HostModel& h = *models[k];
       for (size_t f = 0; f < h.fronts.size(); ++f) {
@@ -475,14 +480,50 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         childOffV.push_back(fr.childOff + childOff[k]);
         relOffV.push_back(fr.relOff + relOff[k]);
         asmOffV.push_back(fr.asmOff + asmOff[k]);
-        byHeight[fr.height].push_back(frontOff[k] + (int)f);
-        maxRowH[fr.height] = std::max(maxRowH[fr.height], fr.nrow);
       }
       for (int r : h.frontRows) frontRows.push_back(r + modelEqOff_[k]);
       for (int c : h.childList) childList.push_back(c + frontOff[k]);
       relIndex.insert(relIndex.end(), h.relIndex.begin(), h.relIndex.end());
       for (int s : h.asmSlot) asmSlot.push_back((int64_t)s + modelSlotOff_[k]);
       asmPos.insert(asmPos.end(), h.asmPos.begin(), h.asmPos.end());
+    }
+    // children's update matrices: lower triangles packed column by column into one
+    // segment per parent, children in order, with their positions in the parent front
+    std::vector<int64_t> segOff(nfr, 0), uOffPacked(nfr, 0);
+    std::vector<int> segLen(nfr, 0), segPos;
+    int64_t nuPacked = 0;
+    for (int f = 0; f < nfr; ++f) {
+      segOff[f] = nuPacked;
+      if (nrow[f] > 1024 || nchild[f] >= 2048) { err = "front too large for the packed update layout"; return -909; }
+      for (int c = 0; c < nchild[f]; ++c) {
+        const int ch = childList[childOffV[f] + c];
+        const int cu = nrow[ch] - npiv[ch];
+        const int* rel = &relIndex[relOffV[ch]];
+        uOffPacked[ch] = nuPacked;
+        for (int b = 0; b < cu; ++b)
+          for (int a = b; a < cu; ++a) {
+            segPos.push_back((c << 20) | (rel[a] + nrow[f] * rel[b]));
+            ++nuPacked;
+          }
+      }
+      segLen[f] = (int)(nuPacked - segOff[f]);
+    }
+    nu = nuPacked;
+    uOffV = uOffPacked;
+    pplan_.maxSeg = 1;
+    pplan_.maxAsm = 1;
+    for (int f = 0; f < nfr; ++f) {
+      pplan_.maxSeg = std::max(pplan_.maxSeg, segLen[f]);
+      pplan_.maxAsm = std::max(pplan_.maxAsm, nasmv[f]);
+    }
+    UPV(d_.fSegOff, int64_t, segOff); UPV(d_.fSegLen, int, segLen); UPV(d_.segPos, int, segPos);
+    {
+      std::vector<int> slotAsm(nslot, -1);
+      for (size_t k = 0; k < asmSlot.size(); ++k) slotAsm[asmSlot[k]] = (int)k;
+      if ((int64_t)asmSlot.size() >= INT_MAX) { err = "batch too large for 32-bit assembly indices"; return -908; }
+      UPV(d_.slotAsm, int, slotAsm);
+      if (opt_.fp32Factor) d_.asmVal32 = alloc<float>(asmSlot.size());
+      else d_.asmVal64 = alloc<double>(asmSlot.size());
     }
     UPV(d_.fNpiv, int, npiv); UPV(d_.fNrow, int, nrow); UPV(d_.fParent, int, parent); UPV(d_.fModel, int, fmodel);
     UPV(d_.fNchild, int, nchild); UPV(d_.fNasm, int, nasmv);
@@ -516,23 +557,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       d_.L64 = alloc<double>(nl); d_.U64 = alloc<double>(nu); d_.w64 = alloc<double>(nw);
       if (!d_.L64 || !d_.U64 || !d_.w64) { err = "out of device memory (factor)"; return -904; }
     }
-    std::vector<int> flat;
-    std::vector<size_t> starts;
-    for (int hgt = 0; hgt <= maxH; ++hgt) {
-      starts.push_back(flat.size());
-      flat.insert(flat.end(), byHeight[hgt].begin(), byHeight[hgt].end());
-    }
-    int* dFlat = nullptr;
-    UPV(dFlat, int, flat);
-    levels_.clear();
-    for (int hgt = 0; hgt <= maxH; ++hgt) {
-      LevelPlan lp;
-      lp.fronts = dFlat + starts[hgt];
-      lp.count = (int)byHeight[hgt].size();
-      lp.maxRow = maxRowH[hgt];
-      size_t perWarpBytes = ((size_t)lp.maxRow * lp.maxRow + 2 * lp.maxRow) * (opt_.fp32Factor ? 4 : 8);
-      if (perWarpBytes > 200 * 1024) { err = "front too large for the shared-memory front kernels"; return -905; }
-      levels_.push_back(lp);
+    int maxRowAll = 1;
+    for (int f = 0; f < nfr; ++f) maxRowAll = std::max(maxRowAll, nrow[f]);
+    if (((size_t)maxRowAll * maxRowAll + 3 * maxRowAll) * (opt_.fp32Factor ? 4 : 8) > 200 * 1024) {
+      err = "front too large for the shared-memory front kernels";
+      return -905;
     }
     // leaf-to-root path lengths: parents follow their children in each model's order
     std::vector<int> pathLen(nfr, 1);
@@ -551,9 +580,18 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     int* dLeaves = nullptr;
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
+    std::vector<int> lpath, lpathOff(1, 0);
+    for (int l : leaves) {
+      for (int f = l; f >= 0; f = parent[f]) lpath.push_back(f);
+      lpathOff.push_back((int)lpath.size());
+    }
+    int *dPath = nullptr, *dPathOff = nullptr;
+    UPV(dPath, int, lpath);
+    UPV(dPathOff, int, lpathOff);
+    pplan_.leafPath = dPath;
+    pplan_.leafPathOff = dPathOff;
     pplan_.nLeaves = (int)leaves.size();
-    pplan_.maxRow = 1;
-    for (const LevelPlan& lp : levels_) pplan_.maxRow = std::max(pplan_.maxRow, lp.maxRow);
+    pplan_.maxRow = maxRowAll;
     pplan_.maxNpiv = 1;
     for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
     pplan_.cntFactor = alloc<int>(nfr);
@@ -637,34 +675,22 @@ void Engine::resetPhaseTimings() {
 }
 
 void Engine::enqueueFactor(cudaStream_t s) {
-  if (opt_.persistent) {
-    // factorisation and the first forward elimination in one cascade
-    launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
-    return;
-  }
-  for (const LevelPlan& lv : levels_) launchFactorLevel(d_, lv, opt_.fp32Factor, s);
+  // factorisation and the first forward elimination in one cascade
+  launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
 }
 
 void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
   const bool f32 = opt_.fp32Factor;
   const int sw = opt_.refineSweeps;
   for (int sweep = 0; sweep < sw; ++sweep) {
+    // the right-hand side is read and the solution stored inside the launches;
+    // the first forward elimination ran with the factorisation
     if (sweep > 0) launchRefineResidual(d_, s);
-    if (opt_.persistent) {
-      // the right-hand side is read and the solution stored inside the launches;
-      // the first forward elimination ran with the factorisation
-      if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[5], s, cudaEventRecordExternal);
-      if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
-      if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[6], s, cudaEventRecordExternal);
-      launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
-    } else {
-      launchSolveSetup(d_, f32, sweep, s);
-      for (size_t h = 0; h < levels_.size(); ++h) launchForwardLevel(d_, levels_[h], f32, s);
-      for (size_t h = levels_.size(); h-- > 0;) launchBackwardLevel(d_, levels_[h], f32, s);
-      launchSolveAccumulate(d_, f32, s);
-    }
+    if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[5], s, cudaEventRecordExternal);
+    if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
+    if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[6], s, cudaEventRecordExternal);
+    launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
   }
-  if (f32 && !opt_.persistent) launchSolveFinalize(d_, s);
 }
 
 void Engine::enqueueIteration(cudaStream_t s) {
@@ -691,14 +717,13 @@ void Engine::enqueueIteration(cudaStream_t s) {
   launchElements(d_, EM_INC, s);
   cudaEventRecordWithFlags(ev_[4], s, cudaEventRecordExternal);
   launchNormsControl(d_, s);
-  const int nl = opt_.persistent ? 1 : (int)levels_.size(), sw = opt_.refineSweeps;
+  const int nl = 1, sw = opt_.refineSweeps;
   // kernels per batched iteration: 12 fixed (begin step, predict, elements x2, residual,
   // element Newton build + rotate (one fused kernel for compressed beams), CSR gather,
-  // increment, norms partial + control, step end)
-  // + factor launches + per sweep the forward and backward launches (per-height launches
-  // with separate set-up/accumulate kernels when not persistent) + refinement residuals
-  const int solveLaunches = opt_.persistent ? 2 * sw - 1 + (sw - 1)
-                                           : sw * (2 + 2 * nl) + (sw - 1) + (opt_.fp32Factor ? 1 : 0);
+  // increment, norms partial + control, step end) + the factorisation with the first
+  // forward elimination + per further solve a refinement residual and a forward
+  // elimination + a back substitution per solve
+  const int solveLaunches = 2 * sw - 1 + (sw - 1);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
                      (d_.nldTot > 0 ? 1 : 0);
@@ -784,7 +809,7 @@ int Engine::run(long long maxBatched, RunStats* stats) {
       phaseMs_[1] += t1;
       phaseMs_[2] += t2;
       float t3 = 0.0f;
-      if (opt_.persistent && opt_.refineSweeps > 1 && cudaEventElapsedTime(&t3, ev_[5], ev_[6]) == cudaSuccess)
+      if (opt_.refineSweeps > 1 && cudaEventElapsedTime(&t3, ev_[5], ev_[6]) == cudaSuccess)
         phaseMs_[3] += t3;
       phaseElems_ += *hActiveEl_;
       ++phaseSamples_;

@@ -17,7 +17,6 @@ struct EngineOptions {
   bool fp32Factor = false;  // mixed precision: FP32 fronts + FP64 iterative refinement
   int refineSweeps = 3;     // solves per Newton iteration in mixed precision (1 + refinements)
   bool useGraph = true;     // capture the batched iteration in a CUDA graph
-  bool persistent = true;   // dependency-driven front kernels (one launch per phase)
   bool compressBeams = true;  // 26-value beam matrices when every element has the principal-axes pattern
 };
 
@@ -83,7 +82,7 @@ class Engine {
   // Phase timings sampled with CUDA events inside the captured iteration:
   // phase 0 = element pass after the increment, 1 = factorisation with the
   // first forward elimination, 2 = the rest of the solves, 3 = the forward
-  // elimination of the second solve (persistent mixed-precision batches; else 0).
+  // elimination of the second solve (mixed-precision batches; else 0).
   // Returns samples; ms[4] = summed milliseconds, elems = summed active elements.
   long long phaseTimings(double* ms4, long long* activeElems);
   void resetPhaseTimings();
@@ -100,7 +99,6 @@ class Engine {
   EngineOptions opt_;
   DevData d_{};
   std::vector<void*> allocs_;
-  std::vector<LevelPlan> levels_;
   PersistentPlan pplan_{};
   int* dActive_ = nullptr;
   int* hActive_ = nullptr;  // pinned

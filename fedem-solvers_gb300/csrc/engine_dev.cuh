@@ -11,6 +11,8 @@
 
 namespace fgpu {
 
+constexpr int kSlotBlock = 256;  // CSR slots per block of the slot gather
+
 // per-model state machine
 enum ModelState : int { ST_NEED_STEP = 0, ST_ITER = 1, ST_DONE = 2, ST_ERROR = 3 };
 // per-model flags for the current batched iteration
@@ -66,7 +68,7 @@ struct DevData {
   double *stifScl, *kDmp;
   int *elTri, *elRef, *elModel;
   uint8_t *hasC, *hasVld;
-  double* elMat;  // rotated element Newton matrices, SoA 144
+  double* elMat;  // rotated element Newton matrices, SoA 144 (entry i + 12 j of element e at (i + 12 j) * nelTot + e)
   // compressed beam matrices (26 upper values of the principal-axes pattern),
   // used by the element pass when every element of the batch has that pattern
   int beamSparse = 0;
@@ -76,19 +78,32 @@ struct DevData {
   int* colInd;
   double* csrVal;
   int* slotPtr;      // 32-bit: a batch keeps its slot contributions below 2^31
-  int* slotSrc;      // SoA index into elMat (elMatA above 144 * nelTot)
+  int* slotSrc;      // index into elMat (elMatA above 144 * nelTot)
   int* slotModel;
+  int* slotBlockModel;  // per block of kSlotBlock slots: their model, or -1 when they span several
   int *eqPtr, *eqSrc;  // eqSrc = local * nelTot + element
   // fronts (global indices)
   int nfrontTot = 0;
   int *fNpiv, *fNrow, *fParent, *fModel, *fNchild, *fNasm;
-  int64_t *fRowOff, *fLOff, *fUOff, *fWOff, *fChildOff, *fRelOff, *fAsmOff;
+  int64_t *fRowOff, *fLOff, *fUOff, *fWOff, *fChildOff, *fRelOff, *fAsmOff;  // fUOff: the front's packed
+                                                                            // update matrix in its parent's segment
   int *frontRows, *childList, *relIndex;
   // children's update rows of each front, in child order: W index and
   // (child ordinal << 16 | destination row), cgOff[f]..cgOff[f+1]
   int *cgOff, *cgSrc, *cgDst;
   int64_t* asmSlot;
   int* asmPos;
+  // the original entries again in front-assembly order, written with the CSR
+  // values (slotAsm[s]: assembly index of CSR slot s, or -1), in the factor precision
+  int* slotAsm;
+  float* asmVal32;
+  double* asmVal64;
+  // children's update matrices, lower triangles packed column by column, one
+  // contiguous segment per parent front in child order: fSegOff/fSegLen, and
+  // for each segment entry (child ordinal << 20 | position in the parent front)
+  int64_t* fSegOff;
+  int* fSegLen;
+  int* segPos;
   double *L64, *U64;
   float *L32, *U32;
   double* w64;

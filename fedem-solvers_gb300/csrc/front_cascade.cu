@@ -15,66 +15,80 @@
 // The forward and backward solves stage each front's L block in shared memory
 // first (one burst of loads instead of one load latency per pivot).
 //
-// Front arithmetic is that of front_kernels.cu (SPRFC1/SPRFS1/SPRBS1
-// semantics, src/vpmCommon/vpmLinAlg/solExtensionModule.f90:153-505).
+// These kernels replace the factor and solve of the absent SAM/SPR solver that
+// the reference calls from csSolve (src/vpmCommon/vpmLinAlg/
+// solExtensionModule.f90:153-505: SPRFC1/SPRFC3, SPRFS1/SPRBS1).  Semantics
+// kept: LDL^T without pivoting, a pivot counts as singular when
+// |d_k| <= tolFactorize * |a_kk| (error -3), negative pivots are counted.
+// Fronts are dense column-major nrow x nrow tiles in shared memory (lower
+// triangle used), pivots first; children's contributions are added in child
+// order, so every sum has a fixed order (no atomics on floating-point data).
+// Mixed precision: FP32 factor and correction solves; the FP64 refinement
+// residual is in front_kernels.cu.
 
 #include "kernels.h"
 
 namespace fgpu {
 namespace {
 
-constexpr long long kSpinLimit = 1LL << 22;
+constexpr long long kSpinLimit = 1LL << 21;  // polls of a bounded wait (about 2 s with backoff)
+
+// GPU-scope acquire load / release store of a front state
+__device__ inline int loadAcquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void storeRelease(int* p, int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
 
 // partial LDL^T of front f in shared memory (F: maxRow^2, lcol/diag0: maxRow).
-// Global loads are issued several per lane before they are used (the fronts
-// are small and latency-bound); the rank-1 updates run one row per lane.
+// The original entries (front-ordered copy of the CSR values) and the
+// children's packed update matrices are contiguous per front and loaded
+// kFrontBatch per lane before use; the rank-1 updates run one row per lane.
+constexpr int kFrontBatch = 4;
 template <typename T>
-__device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* Ubase, T* Lbase,
-                               T* Uout0, double tolFact, int lane) {
+__device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* asmVal, T* Lbase,
+                               T* Ubase, double tolFact, int lane) {
   const int m = d.fModel[f];
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
+  const int64_t ao = d.fAsmOff[f], so = d.fSegOff[f];
+  const int na = d.fNasm[f], ns = d.fSegLen[f], nch = d.fNchild[f];
   for (int k = lane; k < nr * nr; k += 32) F[k] = T(0);
-  __syncwarp();
-  const int64_t ao = d.fAsmOff[f];
-  const int na = d.fNasm[f];
-  for (int k0 = 0; k0 < na; k0 += 128) {
-    int64_t sl[4];
-    int ps[4];
-    double val[4];
+  for (int k0 = 0; k0 < na; k0 += 32 * kFrontBatch) {
+    T val[kFrontBatch];
+    int pos[kFrontBatch];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kFrontBatch; ++u) {
       const int k = k0 + 32 * u + lane;
-      sl[u] = k < na ? d.asmSlot[ao + k] : -1;
-      ps[u] = k < na ? d.asmPos[ao + k] : 0;
+      pos[u] = k < na ? __ldg(d.asmPos + ao + k) : -1;
+      val[u] = k < na ? __ldg(asmVal + ao + k) : T(0);
     }
+    __syncwarp();
 #pragma unroll
-    for (int u = 0; u < 4; ++u) val[u] = sl[u] >= 0 ? __ldg(d.csrVal + sl[u]) : 0.0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (sl[u] >= 0) F[ps[u]] = (T)val[u];
+    for (int u = 0; u < kFrontBatch; ++u)
+      if (pos[u] >= 0) F[pos[u]] = val[u];
   }
   __syncwarp();
   for (int k = lane; k < np; k += 32) diag0[k] = F[k + nr * k];
   __syncwarp();
-  const int nc = d.fNchild[f];
-  const int64_t co = d.fChildOff[f];
-  for (int c = 0; c < nc; ++c) {
-    const int ch = d.childList[co + c];
-    const int cu = d.fNrow[ch] - d.fNpiv[ch];
-    const T* Uc = Ubase + d.fUOff[ch];
-    const int* rel = d.relIndex + d.fRelOff[ch];
-    // lane a adds rows a, a + 32, ... of the child's lower update matrix, column by column
-    for (int a0 = 0; a0 < cu; a0 += 32) {
-      const int a = a0 + lane;
-      const int ra = a < cu ? __ldg(rel + a) : 0;
-#pragma unroll 4
-      for (int b = 0; b < cu && b <= a0 + 31; ++b) {
-        const int rb = __ldg(rel + b);
-        const T u = (a < cu && a >= b) ? __ldcg(Uc + a + (size_t)cu * b) : T(0);
-        if (a < cu && a >= b) F[ra + nr * rb] += u;
-      }
+  // extend-add of the children's update matrices, child by child
+  for (int k0 = 0; k0 < ns; k0 += 32 * kFrontBatch) {
+    T val[kFrontBatch];
+    int pc[kFrontBatch];
+#pragma unroll
+    for (int u = 0; u < kFrontBatch; ++u) {
+      const int k = k0 + 32 * u + lane;
+      pc[u] = k < ns ? __ldg(d.segPos + so + k) : -1;
+      val[u] = k < ns ? __ldcg(Ubase + so + k) : T(0);
     }
-    __syncwarp();
+    for (int c = 0; c < nch; ++c) {
+#pragma unroll
+      for (int u = 0; u < kFrontBatch; ++u)
+        if (pc[u] >= 0 && (pc[u] >> 20) == c) F[pc[u] & 0xfffff] += val[u];
+      __syncwarp();
+    }
   }
   int neg = 0;
   bool sing = false;
@@ -97,11 +111,10 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
   }
   T* Lout = Lbase + d.fLOff[f];
   for (int k = lane; k < nr * np; k += 32) Lout[k] = F[k];
-  T* Uout = Uout0 + d.fUOff[f];
-  for (int k = lane; k < nu * nu; k += 32) {
-    int a = k % nu, b = k / nu;
-    Uout[k] = F[(np + a) + nr * (np + b)];
-  }
+  // update matrix: lower triangle packed column by column into the parent's segment
+  T* Uout = Ubase + d.fUOff[f];
+  for (int b = 0, base = 0; b < nu; base += nu - b, ++b)
+    for (int a = b + lane; a < nu; a += 32) Uout[base + a - b] = F[(np + a) + nr * (np + b)];
   if (lane == 0) {
     if (neg) atomicAdd(&d.m.negPiv[m], neg);
     if (sing) atomicOr(&d.m.status[m], SS_SINGULAR);
@@ -233,47 +246,33 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
 
 // After a front is done: release its data and count it at the parent; returns
 // the parent if this warp completed the parent's count (and must go on), else -1.
+// The warp barrier orders every lane's stores before lane 0's counter update,
+// a release-acquire RMW at GPU scope (no full fence): the warp that completes
+// the count acquires the children's stores, and its barrier passes them on to
+// its other lanes.
 __device__ inline int climb(const DevData& d, int f, int* cnt, int lane) {
-  __threadfence();
   __syncwarp();
   int next = -1;
   if (lane == 0) {
     const int p = d.fParent[f];
     if (p >= 0) {
-      int old = atomicAdd(cnt + p, 1);
+      int old;
+      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(cnt + p) : "memory");
       if (old == d.fNchild[p] - 1) next = p;
     }
   }
   next = __shfl_sync(0xffffffffu, next, 0);
-  if (next >= 0) __threadfence();
+  __syncwarp();
   return next;
-}
-
-template <typename T>
-__global__ void kFactorCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, T* Lbase,
-                               T* Ubase, double tolFact, int* cnt) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int W = gridDim.x * wpb;
-  T* F = reinterpret_cast<T*>(smraw) + (size_t)w * ((size_t)maxRow * maxRow + 2 * maxRow);
-  T* lcol = F + (size_t)maxRow * maxRow;
-  T* diag0 = lcol + maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += W) {
-    int f = leaves[idx];
-    if (!(d.m.flags[d.fModel[f]] & FL_TANGENT)) continue;
-    while (f >= 0) {
-      factorOneFront<T>(d, f, F, lcol, diag0, Ubase, Lbase, Ubase, tolFact, lane);
-      f = climb(d, f, cnt, lane);
-    }
-  }
 }
 
 // factorisation (models with a tangent update) fused with the forward
 // elimination of the first solve (all active models): one climb per front, and
 // the forward elimination reads L from the front still in shared memory
 template <typename T>
-__global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, T* Lbase,
-                                      T* Ubase, double tolFact, const double* rhs, T* X, T* Wv, int* cnt) {
+__global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow,
+                                      const T* asmVal, T* Lbase, T* Ubase, double tolFact, const double* rhs, T* X,
+                                      T* Wv, int* cnt) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int Wt = gridDim.x * wpb;
@@ -290,7 +289,7 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
     while (f >= 0) {
       const T* Lres = nullptr;
       if (factor) {
-        factorOneFront<T>(d, f, F, lcol, diag0, Ubase, Lbase, Ubase, tolFact, lane);
+        factorOneFront<T>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase, tolFact, lane);
         __syncwarp();
         Lres = F;
       }
@@ -363,7 +362,8 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
 
 // top-down along the leaf-to-root paths; state[f]: 0 open, 1 claimed, 2 done
 template <typename T>
-__global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
+__global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const int* __restrict__ leafPath,
+                               const int* __restrict__ leafPathOff, int nLeaves, int maxRow, int capL,
                                int maxPath, const T* Lbase, T* X, int* state, int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -376,45 +376,57 @@ __global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, int nL
   for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
     const int leaf = leaves[idx];
     if (!(d.m.flags[d.fModel[leaf]] & FL_ACTIVE)) continue;
-    // the path from the leaf up to (not including) the first front already done
-    int n = 0;
-    if (lane == 0) {
-      int f = leaf;
-      while (f >= 0 && n < maxPath && *(volatile const int*)(state + f) != 2) {
-        path[n++] = f;
-        f = d.fParent[f];
+    // the path from the leaf up to (not including) the first front already done:
+    // the precomputed path and its states are read by all lanes at once (a done
+    // front has only done ancestors)
+    const int p0 = leafPathOff[idx], len = leafPathOff[idx + 1] - p0;
+    int n = len;
+    for (int k0 = 0; k0 < len; k0 += 32) {
+      const int k = k0 + lane;
+      int st = 0;
+      if (k < len) {
+        const int f = __ldg(leafPath + p0 + k);
+        st = loadAcquire(state + f);
+        path[k] = f;
       }
-      __threadfence();
+      const unsigned done = __ballot_sync(0xffffffffu, k < len && st == 2);
+      if (done) {
+        n = k0 + __ffs(done) - 1;
+        break;
+      }
     }
-    n = __shfl_sync(0xffffffffu, n, 0);
+    // every lane's acquire before any lane's reads of the done fronts' values
     __syncwarp();
     for (int j = n - 1; j >= 0; --j) {
       const int f = path[j];
       int own = 0, ok = 1;
       if (lane == 0) {
-        int st = *(volatile const int*)(state + f);
+        int st = loadAcquire(state + f);
         if (st == 0) own = atomicCAS(state + f, 0, 1) == 0;
         if (!own) {
+          // exponential backoff (32 ns .. 1 us): thousands of warps may wait on
+          // the same few fronts near the roots, their polls must not crowd L2
           long long spins = 0;
-          while (*(volatile const int*)(state + f) != 2) {
-            __nanosleep(20);
+          unsigned pause = 32;
+          while (loadAcquire(state + f) != 2) {
+            __nanosleep(pause);
+            pause = pause < 1024 ? 2 * pause : 1024;
             if (++spins > kSpinLimit) {
               atomicOr(errFlag, 1);
               ok = 0;
               break;
             }
           }
-          __threadfence();
         }
       }
       own = __shfl_sync(0xffffffffu, own, 0);
       ok = __shfl_sync(0xffffffffu, ok, 0);
+      __syncwarp();  // lane 0's acquire before the other lanes' reads
       if (!ok) break;
       if (!own) continue;
       backwardOneFront<T>(d, f, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) atomicExch(state + f, 2);
+      __syncwarp();  // every lane's stores before lane 0's release
+      if (lane == 0) storeRelease(state + f, 2);
     }
   }
 }
@@ -451,28 +463,6 @@ int factorWarpsPerBlock(size_t perWarpBytes) {
 
 }  // namespace
 
-void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s) {
-  if (p.nLeaves <= 0) return;
-  const double tol = 1.0e-12;
-  const size_t perWarp = (size_t)p.maxRow * p.maxRow + 2 * p.maxRow;
-  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * (size_t)d.nfrontTot, s);
-  if (fp32) {
-    const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
-    const size_t sm = (size_t)wpb * perWarp * sizeof(float);
-    allowBigSmem(kFactorCascade<float>, sm);
-    const int blocks = occupancyBlocks(kFactorCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L32, d.U32, tol,
-                                                      p.cntFactor);
-  } else {
-    const int wpb = factorWarpsPerBlock(perWarp * sizeof(double));
-    const size_t sm = (size_t)wpb * perWarp * sizeof(double);
-    allowBigSmem(kFactorCascade<double>, sm);
-    const int blocks = occupancyBlocks(kFactorCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L64, d.U64, tol,
-                                                        p.cntFactor);
-  }
-}
-
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
                                 cudaStream_t s) {
   if (p.nLeaves <= 0) return;
@@ -484,15 +474,15 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
     const size_t sm = (size_t)wpb * perWarp * sizeof(float);
     allowBigSmem(kFactorForwardCascade<float>, sm);
     const int blocks = occupancyBlocks(kFactorForwardCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L32, d.U32, tol,
-                                                             rhs, d.x32, d.w32, p.cntFactor);
+    kFactorForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.asmVal32, d.L32,
+                                                             d.U32, tol, rhs, d.x32, d.w32, p.cntFactor);
   } else {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(double));
     const size_t sm = (size_t)wpb * perWarp * sizeof(double);
     allowBigSmem(kFactorForwardCascade<double>, sm);
     const int blocks = occupancyBlocks(kFactorForwardCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.L64, d.U64, tol,
-                                                               rhs, d.x64, d.w64, p.cntFactor);
+    kFactorForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.asmVal64,
+                                                               d.L64, d.U64, tol, rhs, d.x64, d.w64, p.cntFactor);
   }
 }
 
@@ -537,7 +527,8 @@ void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, i
     const size_t sm = (size_t)wpb * per;
     allowBigSmem(kBackwardClaim<float>, sm);
     const int blocks = occupancyBlocks(kBackwardClaim<float>, 32 * wpb, sm, needed);
-    kBackwardClaim<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, p.maxPath, d.L32,
+    kBackwardClaim<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.leafPath, p.leafPathOff, p.nLeaves, p.maxRow,
+                                                      capL, p.maxPath, d.L32,
                                                       d.x32, p.stateBackward, p.errFlag, acc, fin);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
@@ -545,7 +536,8 @@ void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, i
     const size_t sm = (size_t)wpb * per;
     allowBigSmem(kBackwardClaim<double>, sm);
     const int blocks = occupancyBlocks(kBackwardClaim<double>, 32 * wpb, sm, needed);
-    kBackwardClaim<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, p.maxPath, d.L64,
+    kBackwardClaim<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.leafPath, p.leafPathOff, p.nLeaves, p.maxRow,
+                                                        capL, p.maxPath, d.L64,
                                                         d.x64, p.stateBackward, p.errFlag, acc, fin);
   }
 }

@@ -35,22 +35,18 @@ void launchStaticNorm(const DevData& d, cudaStream_t s);
 void launchStaticIncrement(const DevData& d, cudaStream_t s);
 void launchStaticFinish(const DevData& d, cudaStream_t s);
 
-// --- front_kernels.cu --------------------------------------------------------
-struct LevelPlan {
-  const int* fronts;  // device list of global front indices at this height
-  int count;
-  int maxRow;         // largest front at this height
-};
-// one-launch front kernels over all heights (front_cascade.cu)
+// --- front_cascade.cu: one launch per phase over all fronts of all models ----
 struct PersistentPlan {
-  const int* leaves;  // fronts without children
+  const int* leaves;  // fronts without children, longest root path first
+  const int* leafPath, *leafPathOff;  // each leaf's fronts up to its root, leaf first
   int nLeaves;
   int maxRow;         // largest front of the batch (rows)
   int maxNpiv;        // largest pivot block of the batch
   int maxPath;        // longest leaf-to-root path (fronts)
+  int maxAsm;         // largest number of original entries of one front
+  int maxSeg;         // largest children update segment of one front (packed lower values)
   int *cntFactor, *cntForward, *stateBackward, *errFlag;
 };
-void launchFactorCascade(const DevData& d, const PersistentPlan& p, bool fp32, cudaStream_t s);
 // factorisation of the models with a tangent update fused with the forward
 // elimination of rhs for every active model (first solve of an iteration)
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
@@ -60,20 +56,13 @@ void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, 
 // back substitution; stores the solution in del (FP64 solve) or accumulates it in xref
 // (FP32 refinement sweep `sweep`; the last sweep also copies xref to del)
 void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
-// one launch per height
-void launchFactorLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
-void launchForwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
-void launchBackwardLevel(const DevData& d, const LevelPlan& lv, bool fp32, cudaStream_t s);
 // prescribed deflections (step start), their predictor right-hand side (after the
 // element Newton matrices), and the restart state of pure linear quasi-static steps
 void launchMotions(const DevData& d, cudaStream_t s);
 void launchLoads(const DevData& d, cudaStream_t s);
 void launchMotionRhs(const DevData& d, cudaStream_t s);
 void launchQsRestore(const DevData& d, cudaStream_t s);
-// vector glue for the solves
-void launchSolveSetup(const DevData& d, bool fp32, int sweep, cudaStream_t s);
-void launchSolveAccumulate(const DevData& d, bool fp32, cudaStream_t s);
-void launchSolveFinalize(const DevData& d, cudaStream_t s);
+// FP64 refinement residual r = b - A x (front_kernels.cu)
 void launchRefineResidual(const DevData& d, cudaStream_t s);
 
 // Convergence norms of model m recomputed into a fixed scratch array compiled
