@@ -223,9 +223,11 @@ def served_leg(args):
         if k == n_req and st["pending"] == 0 and st["live_batches"] == 0:
             break
     recs = [srv.request(i) for i in ids]
-    lat = np.array([r["finished"] - r["arrival"] for r in recs])
+    # latency from the scheduled arrival (a request submitted late, behind a
+    # blocking admission, still counts from when it arrived)
+    lat = np.array([r["finished"] - (t0 + a) for r, a in zip(recs, arrivals)])
     its = sum(r["iterations"] for r in recs)
-    span = max(r["finished"] for r in recs) - min(r["arrival"] for r in recs)
+    span = max(r["finished"] for r in recs) - t0
     failed = sum(1 for r in recs if r["state"] != 2)
     srv.close()
     return {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),

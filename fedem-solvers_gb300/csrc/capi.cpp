@@ -2,6 +2,7 @@
 // (src/vpmSolver/solverInterface.h, one model per process) and the batched
 // fgpu_* API.  Both drive the same GPU engine; there is no CPU solver path.
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -34,6 +35,7 @@ struct Singleton {
   std::unique_ptr<HostModel> model;
   std::unique_ptr<Engine> engine;
   bool finished = false;
+  bool inStep = false;  // startStep assembled an iteration that solveIteration has not solved
   int ierr = 0;
 };
 std::unique_ptr<Singleton> g_core;
@@ -105,7 +107,6 @@ extern "C" {
 int solverInit(int argc, char** argv, const char* cfsi, const double* stateData, int ndat,
                const double* /*gagesData*/, int /*ngda*/, const double* /*extInput*/, int* nxinp) {
   if (nxinp) *nxinp = 0;
-  if (stateData && ndat > 0) return fail(-1, "restart from state data is not supported");
   g_core.reset();
   std::string text;
   if (cfsi) {
@@ -129,23 +130,48 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
   rc = s->engine->upload(ms, opt, err);
   if (!rc) rc = s->engine->initialState(err);
   if (rc) return fail(rc, err);
+  if (stateData && ndat > 0) {  // restart from an in-core state array (saveState of the same model)
+    if ((size_t)ndat * sizeof(double) < s->engine->stateBytes()) return fail(-2, "state array too short");
+    if (s->engine->restoreStateFrom(stateData)) return fail(-3, "restoring the state failed");
+  }
   g_core = std::move(s);
   return 0;
 }
 
-int restartFromState(const double*, const int, const int) { return fail(-1, "restart is not supported"); }
+// solverInterface.h:87 -- the engine's mutable state from a saveState array
+// (results database options are not part of this path and are ignored)
+int restartFromState(const double* stateData, const int ndat, const int) {
+  if (!g_core || !stateData) return fail(-1, "no model or no state data");
+  const size_t bytes = g_core->engine->stateBytes();
+  if ((size_t)ndat * sizeof(double) < bytes) return fail(-2, "state array too short");
+  if (int rc = g_core->engine->restoreStateFrom(stateData)) return fail(rc, "restoring the state failed");
+  g_core->inStep = false;
+  g_core->ierr = 0;
+  g_core->finished = false;
+  return 0;
+}
 
 bool solveWindow(int, int, int, int, const int*, const double*, const double*, double*, int, double*, int* ierr) {
   if (ierr) *ierr = -1;
   return false;
 }
 
-int getStateSize(void) { return 0; }
+// solverInterface.h:118 -- doubles needed by saveState
+int getStateSize(void) {
+  if (!g_core) return 0;
+  return (int)((g_core->engine->stateBytes() + sizeof(double) - 1) / sizeof(double));
+}
 int getTransformationStateSize(void) { return 0; }
 int getPartDeformationStateSize(int) { return 0; }
 int getPartStressStateSize(int) { return 0; }
 int getGagesSize(void) { return 0; }
-bool saveState(double*, const int) { return false; }
+// solverInterface.h:156 -- the mutable state (positions, velocities, frames,
+// forces, step and iteration counters) into an in-core array
+bool saveState(double* stateData, const int ndat) {
+  if (!g_core || !stateData || g_core->inStep) return false;
+  if ((size_t)ndat * sizeof(double) < g_core->engine->stateBytes()) return false;
+  return g_core->engine->saveStateTo(stateData) == 0;
+}
 bool saveTransformationState(double*, const int) { return false; }
 bool saveGages(double*, const int) { return false; }
 bool savePartDeformationState(int, double*, const int) { return false; }
@@ -166,6 +192,7 @@ bool solveNext(int* ierr) {
     if (ierr) *ierr = s.ierr;
     return false;
   }
+  if (s.inStep) return solveIteration(ierr, true);  // finish the step startStep began
   if (hasReachedEnd(s)) return false;
   int state = 0;
   int rc = s.engine->advanceOneStep(0, &state);
@@ -179,13 +206,68 @@ bool solveNext(int* ierr) {
   return !s.finished;
 }
 
+// solverInterface.h:262 -- predictor and the first linearised system of the next step
 bool startStep(int* ierr) {
-  if (ierr) *ierr = -1;
-  return false;
+  int lerr = 0;
+  int& e = ierr ? *ierr : lerr;
+  e = 0;
+  if (!g_core || g_core->ierr) {
+    e = g_core ? g_core->ierr : -1;
+    return false;
+  }
+  Singleton& s = *g_core;
+  if (s.inStep) {
+    e = -999;  // a step is already started (the reference's state check)
+    return false;
+  }
+  if (hasReachedEnd(s)) return false;
+  s.engine->setStepLimitOf(0, s.engine->modelSteps(0) + 1);
+  if (int rc = s.engine->assembleIteration()) {
+    s.ierr = e = rc;
+    return false;
+  }
+  s.inStep = true;
+  return true;
 }
-bool solveIteration(int* ierr, bool) {
-  if (ierr) *ierr = -1;
-  return false;
+
+// solverInterface.h:278 -- solves the assembled system, updates the model and
+// assembles the next iteration unless converged; with `all`, until convergence
+bool solveIteration(int* ierr, bool all) {
+  int lerr = 0;
+  int& e = ierr ? *ierr : lerr;
+  e = 0;
+  if (!g_core || g_core->ierr) {
+    e = g_core ? g_core->ierr : -1;
+    return false;
+  }
+  Singleton& s = *g_core;
+  if (!s.inStep) {
+    e = -999;  // step not started
+    return false;
+  }
+  for (;;) {
+    if (int rc = s.engine->solveUpdateIteration()) {
+      s.ierr = e = rc;
+      return false;
+    }
+    const int state = s.engine->modelState(0);
+    if (state == ST_ERROR) {
+      const int st = s.engine->modelStatus(0);
+      s.ierr = e = (st & SS_SINGULAR) ? -3 : (st & SS_MAXIT) ? 1 : -1;
+      s.inStep = false;
+      return false;
+    }
+    if (state == ST_NEED_STEP) {  // converged: the step is complete
+      s.inStep = false;
+      s.finished = hasReachedEnd(s);
+      return all ? !s.finished : false;
+    }
+    if (int rc = s.engine->assembleIteration()) {
+      s.ierr = e = rc;
+      return false;
+    }
+    if (!all) return true;
+  }
 }
 bool solveEigenModes(const int, double*, double*, bool, int, int* ierr) {
   if (ierr) *ierr = -1;
@@ -214,7 +296,17 @@ double getTime(bool nextStep, int* ierr) {
   return nextStep ? t + g_core->model->ctl.tInc : t;
 }
 
-bool setTime(double) { return false; }
+// solverInterface.h:355 -- time increment of the next step: nextTime - time
+// (solverModule.f90:1558-1600: a negative increment or one above maxInc is an
+// error, one below minInc is raised to it)
+bool setTime(double nextTime) {
+  if (!g_core || g_core->inStep) return false;
+  const Control& c = g_core->model->ctl;
+  const double dt = nextTime - g_core->engine->modelTime(0);
+  if (dt < 0.0) return false;
+  if (dt >= c.minInc && dt > c.maxInc) return false;
+  return g_core->engine->setTimeStep(0, dt < c.minInc ? c.minInc : dt) == 0;
+}
 
 double evalFunc(int, const char*, double, int* ierr) {
   if (ierr) *ierr = -1;
@@ -247,9 +339,72 @@ int getSystemSize(bool dofs) {
   return dofs ? g_core->model->ndof : g_core->model->neq;
 }
 
-bool getSystemMatrix(double* Smat, int iMat) {
-  if (!g_core || iMat != 0) return false;
+// Dense system stiffness (1), mass (2) or damping (3) matrix at the current
+// configuration: the element matrices rotated to system axes with the current
+// frames (as AddInSupMat / MATTRA), the axial springs' and dampers' n n^T blocks
+// (calcSpringStiffness without geometric stiffness, addInDamperMat), assembled
+// over the free equations.
+static void assembleSystemMatrix(int iMat, double* Smat) {
   const HostModel& m = *g_core->model;
+  const int neq = m.neq;
+  std::memset(Smat, 0, sizeof(double) * (size_t)neq * neq);
+  std::vector<double> frames(12 * (size_t)m.nel), ur(12 * (size_t)m.ntri);
+  g_core->engine->getElementFrames(0, frames.data());
+  g_core->engine->getTriadUr(0, ur.data());
+  auto add = [&](int i, int j, double v) { Smat[(size_t)i + (size_t)neq * j] += v; };
+  for (int e = 0; e < m.nel; ++e) {
+    const double* X = iMat == 1 ? &m.K[144 * (size_t)e] : iMat == 2 ? &m.M[144 * (size_t)e] : &m.C[144 * (size_t)e];
+    if (iMat == 3 && !m.hasC[e]) continue;
+    const double scl = iMat == 2 ? 1.0 : m.stifScl[e];
+    const double* R = &frames[12 * (size_t)e];  // column-major 3x3 rotation first
+    const int* q = &m.elEq[12 * (size_t)e];
+    for (int bj = 0; bj < 4; ++bj)
+      for (int bi = 0; bi < 4; ++bi) {
+        double W[9];
+        for (int c = 0; c < 3; ++c)
+          for (int r = 0; r < 3; ++r) {
+            double v = 0.0;
+            for (int k = 0; k < 3; ++k) v += R[r + 3 * k] * (scl * X[(3 * bi + k) + 12 * (3 * bj + c)]);
+            W[r + 3 * c] = v;
+          }
+        for (int c = 0; c < 3; ++c)
+          for (int r = 0; r < 3; ++r) {
+            const int i = q[3 * bi + r], j = q[3 * bj + c];
+            if (i < 0 || j < 0) continue;
+            double v = 0.0;
+            for (int k = 0; k < 3; ++k) v += W[r + 3 * k] * R[c + 3 * k];
+            add(i, j, v);
+          }
+      }
+  }
+  for (int a = 0; a < m.nax; ++a) {
+    const double* x1 = &ur[12 * (size_t)m.axTri[2 * a] + 9];
+    const double* x2 = &ur[12 * (size_t)m.axTri[2 * a + 1] + 9];
+    double n[3] = {x2[0] - x1[0], x2[1] - x1[1], x2[2] - x1[2]};
+    const double L = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(L > 0.0)) continue;
+    for (double& c : n) c /= L;
+    double coeff = 0.0;
+    if (m.axKind[a] == 0) coeff = iMat == 1 ? m.axS0[a] : iMat == 3 ? m.axS0[a] * m.axAlpha2[a] : 0.0;
+    else coeff = iMat == 3 ? m.axD0[a] : 0.0;
+    if (coeff == 0.0) continue;
+    const int* q = &m.axEq[6 * (size_t)a];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) {
+        if (q[i] < 0 || q[j] < 0) continue;
+        const double v = n[i % 3] * n[j % 3] * coeff;
+        add(q[i], q[j], (i / 3 == j / 3) ? v : -v);
+      }
+  }
+}
+
+bool getSystemMatrix(double* Smat, int iMat) {
+  if (!g_core || !Smat || iMat < 0 || iMat > 3) return false;
+  const HostModel& m = *g_core->model;
+  if (iMat > 0) {
+    assembleSystemMatrix(iMat, Smat);
+    return true;
+  }
   std::vector<double> v(m.colInd.size());
   g_core->engine->getCsrValues(0, v.data());
   std::memset(Smat, 0, sizeof(double) * (size_t)m.neq * m.neq);
@@ -258,9 +413,9 @@ bool getSystemMatrix(double* Smat, int iMat) {
   return true;
 }
 bool getNewtonMatrix(double* Nmat) { return getSystemMatrix(Nmat, 0); }
-bool getStiffnessMatrix(double*) { return false; }
-bool getMassMatrix(double*) { return false; }
-bool getDampingMatrix(double*) { return false; }
+bool getStiffnessMatrix(double* Kmat) { return getSystemMatrix(Kmat, 1); }
+bool getMassMatrix(double* Mmat) { return getSystemMatrix(Mmat, 2); }
+bool getDampingMatrix(double* Cmat) { return getSystemMatrix(Cmat, 3); }
 
 bool getElementStiffnessMatrix(double* Kmat, int bid) {
   if (!g_core) return false;
@@ -273,13 +428,23 @@ bool getElementStiffnessMatrix(double* Kmat, int bid) {
   return false;
 }
 
+// solverInterface.h:472 -- iVec < 5: the current right-hand side of the
+// linearised system (solverModule.f90:1834-1849), 5: the external load vector
 bool getRhsVector(double* Rvec, int iVec) {
-  if (!g_core || iVec != 0) return false;
-  g_core->engine->getEqVector(0, 4, Rvec);
+  if (!g_core || !Rvec) return false;
+  g_core->engine->getEqVector(0, iVec == 5 ? 3 : 5, Rvec);
   return true;
 }
-bool setRhsVector(const double*) { return false; }
-bool addRhsVector(const double*) { return false; }
+// solverInterface.h:478-484 -- replace / add to the right-hand side of the
+// iteration assembled by startStep or solveIteration
+bool setRhsVector(const double* Rvec) {
+  if (!g_core || !Rvec || !g_core->inStep) return false;
+  return g_core->engine->setRhs(0, Rvec, false) == 0;
+}
+bool addRhsVector(const double* Rvec) {
+  if (!g_core || !Rvec || !g_core->inStep) return false;
+  return g_core->engine->setRhs(0, Rvec, true) == 0;
+}
 bool getJointSprCoeff(double*, int) { return false; }
 
 // ===========================================================================

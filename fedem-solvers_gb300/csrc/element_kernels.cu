@@ -591,6 +591,12 @@ __global__ void kResidual(DevData d) {
     }
   }
   q += d.qext[i];
+  // forces set by an external process (newmarkRoutinesModule.f90:747-749, 792-794);
+  // they apply to the iterations of one step (solverModule.f90:880-882)
+  if (fl & FL_PRED)
+    d.extRhs[i] = 0.0;
+  else
+    q += d.extRhs[i];
   d.FSk[i] = fs;
   d.FDk[i] = fd;
   d.FIk[i] = fi;

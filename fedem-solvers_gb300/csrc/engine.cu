@@ -41,6 +41,7 @@ Engine::~Engine() {
   if (evChunk_) cudaEventDestroy(evChunk_);
   for (void* p : allocs_) cudaFree(p);
   if (hActive_) cudaFreeHost(hActive_);
+  if (hStates_) cudaFreeHost(hStates_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -252,6 +253,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   d_.rinc = alloc<double>(ndof); d_.sinc0 = alloc<double>(ndof); d_.sinc1 = alloc<double>(ndof); d_.sinc2 = alloc<double>(ndof);
   d_.FSk = alloc<double>(neq); d_.FDk = alloc<double>(neq); d_.FIk = alloc<double>(neq); d_.Qk = alloc<double>(neq);
   d_.FIact = alloc<double>(neq); d_.res = alloc<double>(neq); d_.del = alloc<double>(neq);
+  d_.extRhs = alloc<double>(neq);
   d_.x64 = alloc<double>(neq); d_.xref = alloc<double>(neq); d_.rref = alloc<double>(neq); d_.x32 = alloc<float>(neq);
   {
     // DOF chunks of at most 2048 DOFs, each inside one model
@@ -605,6 +607,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   dActive_ = alloc<int>(1);
   dActiveEl_ = alloc<long long>(1);
   FG_CHECK(cudaMallocHost(&hActive_, sizeof(int)));
+  FG_CHECK(cudaMallocHost(&hStates_, sizeof(int) * (size_t)std::max(nm, 1)));
   FG_CHECK(cudaMallocHost(&hActiveEl_, sizeof(long long)));
   for (cudaEvent_t& ev : ev_) FG_CHECK(cudaEventCreate(&ev));
   // mutable state for snapshot/restore (everything a run changes that is read
@@ -613,7 +616,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   const size_t D = sizeof(double);
   reg(d_.ur, D * 12 * (size_t)ntri);
   for (double* p : {d_.urd, d_.urdd, d_.dk, d_.ak, d_.rinc, d_.sinc0, d_.sinc1, d_.sinc2}) reg(p, D * (size_t)ndof);
-  for (double* p : {d_.FSk, d_.FDk, d_.FIk, d_.Qk, d_.FIact, d_.res, d_.del}) reg(p, D * (size_t)neq);
+  for (double* p : {d_.FSk, d_.FDk, d_.FIk, d_.Qk, d_.FIact, d_.res, d_.del, d_.extRhs}) reg(p, D * (size_t)neq);
+  reg(M.dt, D * nm);
   reg(d_.supTr, D * 12 * (size_t)nel);
   reg(d_.finit, D * 12 * (size_t)nel);
   reg(d_.finitPrev, D * 12 * (size_t)nel);
@@ -631,6 +635,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   if (d_.nmotTot > 0) {
     reg(d_.motD, D * (size_t)d_.nmotTot);
     reg(d_.motCc, D * (size_t)d_.nmotTot);
+  }
+  if (d_.naxTot > 0) {
+    reg(d_.axN, D * 3 * (size_t)d_.naxTot);
+    reg(d_.axLen, D * (size_t)d_.naxTot);
+    reg(d_.FelA, D * 12 * (size_t)d_.naxTot);
   }
   uploadedBytes_ = t_putBytes;
   FG_CHECK(cudaStreamSynchronize(stream_));
@@ -660,7 +669,16 @@ int Engine::restore() {
     cudaMemcpyAsync(m.first, backup_ + off, m.second, cudaMemcpyDeviceToDevice, stream_);
     off += (m.second + 255) & ~size_t(255);
   }
+  invalidateNewtonScales();
   return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -933;
+}
+
+// the element Newton matrices are not part of the saved state: scale factors
+// no step can have make the next tangent iteration rebuild them
+void Engine::invalidateNewtonScales() {
+  scaleSentinel_.assign(3 * (size_t)d_.m.n, -1.0e300);
+  cudaMemcpyAsync(d_.m.scaleN, scaleSentinel_.data(), sizeof(double) * scaleSentinel_.size(),
+                  cudaMemcpyHostToDevice, stream_);
 }
 
 long long Engine::phaseTimings(double* ms4, long long* elems) {
@@ -679,6 +697,18 @@ void Engine::enqueueFactor(cudaStream_t s) {
   launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
 }
 
+// phase-timing events: external event nodes inside a captured graph, plain
+// records when the iteration is launched directly (the external flag is only
+// valid during stream capture)
+void Engine::recordPhase(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(ev, s);
+}
+
 void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
   const bool f32 = opt_.fp32Factor;
   const int sw = opt_.refineSweeps;
@@ -686,14 +716,16 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
     // the right-hand side is read and the solution stored inside the launches;
     // the first forward elimination ran with the factorisation
     if (sweep > 0) launchRefineResidual(d_, s);
-    if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[5], s, cudaEventRecordExternal);
+    if (sweep == 1 && timedForward) recordPhase(ev_[5], s);
     if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
-    if (sweep == 1 && timedForward) cudaEventRecordWithFlags(ev_[6], s, cudaEventRecordExternal);
+    if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
     launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
   }
 }
 
-void Engine::enqueueIteration(cudaStream_t s) {
+// first half of a Newton iteration: step start (predictor) or the corrector's
+// right-hand side, and the Newton matrix when the tangent is updated
+void Engine::enqueueAssembly(cudaStream_t s) {
   cudaMemsetAsync(dActive_, 0, sizeof(int), s);
   cudaMemsetAsync(dActiveEl_, 0, sizeof(long long), s);
   launchBeginStep(d_, dActive_, dActiveEl_, s);
@@ -707,16 +739,94 @@ void Engine::enqueueIteration(cudaStream_t s) {
   launchRotateElementNewton(d_, s);
   launchCsrGather(d_, s);
   launchMotionRhs(d_, s);
-  cudaEventRecordWithFlags(ev_[0], s, cudaEventRecordExternal);
+}
+
+// second half: factorisation and solves, the increment, the element pass and
+// the convergence test
+void Engine::enqueueSolveUpdate(cudaStream_t s) {
+  recordPhase(ev_[0], s);
   enqueueFactor(s);
-  cudaEventRecordWithFlags(ev_[1], s, cudaEventRecordExternal);
+  recordPhase(ev_[1], s);
   enqueueSolve(s, true);
-  cudaEventRecordWithFlags(ev_[2], s, cudaEventRecordExternal);
+  recordPhase(ev_[2], s);
   launchIncrement(d_, s);
-  cudaEventRecordWithFlags(ev_[3], s, cudaEventRecordExternal);
+  recordPhase(ev_[3], s);
   launchElements(d_, EM_INC, s);
-  cudaEventRecordWithFlags(ev_[4], s, cudaEventRecordExternal);
+  recordPhase(ev_[4], s);
   launchNormsControl(d_, s);
+}
+
+int Engine::assembleIteration() {
+  enqueueAssembly(stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -940;
+}
+
+int Engine::solveUpdateIteration() {
+  enqueueSolveUpdate(stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -941;
+}
+
+void Engine::setStepLimitOf(int m, long long lim) {
+  cudaMemcpyAsync(d_.m.stepLimit + m, &lim, sizeof(long long), cudaMemcpyHostToDevice, stream_);
+  cudaStreamSynchronize(stream_);
+}
+
+int Engine::setTimeStep(int m, double dt) {
+  cudaMemcpyAsync(d_.m.dt + m, &dt, sizeof(double), cudaMemcpyHostToDevice, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -942;
+}
+
+// solverModule.f90:1868-1901 (setRhsVector with keepDuringIterations): in the
+// predictor of a step the vector is also kept as external forces of the
+// step's later iterations; the right-hand side is replaced or added to
+int Engine::setRhs(int m, const double* v, bool add) {
+  const int n = hm_[m]->neq;
+  double* dst = d_.del + modelEqOff_[m];
+  int it = -1;
+  cudaMemcpyAsync(&it, d_.m.iter + m, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  if (it == 0)
+    cudaMemcpyAsync(d_.extRhs + modelEqOff_[m], v, sizeof(double) * n, cudaMemcpyHostToDevice, stream_);
+  if (!add) {
+    cudaMemcpyAsync(dst, v, sizeof(double) * n, cudaMemcpyHostToDevice, stream_);
+  } else {
+    std::vector<double> cur(n);
+    cudaMemcpyAsync(cur.data(), dst, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+    cudaStreamSynchronize(stream_);
+    for (int i = 0; i < n; ++i) cur[i] += v[i];
+    cudaMemcpyAsync(dst, cur.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_);
+  }
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -943;
+}
+
+size_t Engine::stateBytes() const {
+  size_t total = 0;
+  for (auto& m : mutable_) total += m.second;
+  return total;
+}
+
+int Engine::saveStateTo(void* host) {
+  size_t off = 0;
+  for (auto& m : mutable_) {
+    cudaMemcpyAsync(static_cast<char*>(host) + off, m.first, m.second, cudaMemcpyDeviceToHost, stream_);
+    off += m.second;
+  }
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -944;
+}
+
+int Engine::restoreStateFrom(const void* host) {
+  size_t off = 0;
+  for (auto& m : mutable_) {
+    cudaMemcpyAsync(m.first, static_cast<const char*>(host) + off, m.second, cudaMemcpyHostToDevice, stream_);
+    off += m.second;
+  }
+  invalidateNewtonScales();
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -945;
+}
+
+void Engine::enqueueIteration(cudaStream_t s) {
+  enqueueAssembly(s);
+  enqueueSolveUpdate(s);
   const int nl = 1, sw = opt_.refineSweeps;
   // kernels per batched iteration: 12 fixed (begin step, predict, elements x2, residual,
   // element Newton build + rotate (one fused kernel for compressed beams), CSR gather,
@@ -856,6 +966,7 @@ int Engine::launchChunk(int n) {
     else enqueueIteration(stream_);
   }
   cudaMemcpyAsync(hActive_, dActive_, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(hStates_, d_.m.state, sizeof(int) * (size_t)d_.m.n, cudaMemcpyDeviceToHost, stream_);
   cudaEventRecord(evChunk_, stream_);
   chunkPending_ = true;
   return 0;
@@ -922,6 +1033,18 @@ int Engine::getTriadUr(int m, double* ur) {
   int n = hm_[m]->ntri;
   cudaMemcpyAsync(ur, d_.ur + 12 * (size_t)modelTriOff_[m], sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, stream_);
   cudaStreamSynchronize(stream_);
+  return n;
+}
+
+int Engine::getElementFrames(int m, double* supTr12) {
+  const int n = hm_[m]->nel;
+  std::vector<double> soa(12 * (size_t)n);
+  for (int k = 0; k < 12; ++k)
+    cudaMemcpyAsync(soa.data() + (size_t)k * n, d_.supTr + (size_t)k * d_.nelTot + modelElOff_[m],
+                    sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  for (int e = 0; e < n; ++e)
+    for (int k = 0; k < 12; ++k) supTr12[12 * (size_t)e + k] = soa[(size_t)k * n + e];
   return n;
 }
 

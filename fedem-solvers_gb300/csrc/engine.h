@@ -41,10 +41,12 @@ class Engine {
   // Runs batched iterations until no model is active or maxBatched is reached.
   int run(long long maxBatched, RunStats* stats);
   // Non-blocking driving (serving): enqueue n batched iterations followed by an
-  // asynchronous read of the active-model count; poll reports whether that
-  // chunk finished (*ready) and whether any model is still active.
+  // asynchronous read of the active-model count and of every model's state;
+  // poll reports whether that chunk finished (*ready) and whether any model is
+  // still active; chunkStates() then holds the states (ModelState per model).
   int launchChunk(int n);
   int pollChunk(bool* ready, int* active);
+  const int* chunkStates() const { return hStates_; }
   // Device bytes this engine allocated.
   size_t deviceBytes() const { return deviceBytes_; }
   // Sum of Newton iterations over all models (blocking read).
@@ -61,6 +63,7 @@ class Engine {
   long long modelIterations(int m);
   int getTriadUr(int m, double* ur);  // 12 per triad of the model
   int getNorms(int m, double* norms18);
+  int getElementFrames(int m, double* supTr12);  // current 3x4 frames, 12 per element
   int getCsrValues(int m, double* vals);  // full symmetric CSR values of the last tangent
   int getEqVector(int m, int which, double* v);  // 0 FS, 1 FD, 2 FI, 3 Q, 4 residual, 5 del
   const HostModel& host(int m) const { return *hm_[m]; }
@@ -75,6 +78,18 @@ class Engine {
   double lastRunDeviceSeconds() const { return lastRunDevSec_; }  // CUDA events on the engine stream
   long long uploadedBytes() const { return uploadedBytes_; }
   void setStepLimit(long long lim);
+  // Externally driven stepping (solverInterface startStep / solveIteration):
+  // the two halves of a Newton iteration, launched directly and completed.
+  int assembleIteration();
+  int solveUpdateIteration();
+  void setStepLimitOf(int m, long long lim);
+  int setTimeStep(int m, double dt);
+  // replaces (add = false) or adds to the right-hand side of the assembled iteration
+  int setRhs(int m, const double* v, bool add);
+  // the mutable state as one host byte array (in-core restart)
+  size_t stateBytes() const;
+  int saveStateTo(void* host);
+  int restoreStateFrom(const void* host);
   // Saves / restores the mutable device state (device-to-device copies), so a
   // timed run can start again from the initial state already resident in HBM.
   int snapshot();
@@ -91,6 +106,8 @@ class Engine {
   template <typename T>
   T* alloc(size_t n);
   void enqueueIteration(cudaStream_t s);
+  void enqueueAssembly(cudaStream_t s);
+  void enqueueSolveUpdate(cudaStream_t s);
   void enqueueSolve(cudaStream_t s, bool timedForward = false);
   void enqueueFactor(cudaStream_t s);
   int readActive();
@@ -102,6 +119,7 @@ class Engine {
   PersistentPlan pplan_{};
   int* dActive_ = nullptr;
   int* hActive_ = nullptr;  // pinned
+  int* hStates_ = nullptr;  // pinned: every model's state after the last chunk
   cudaStream_t stream_ = nullptr;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graphExec_ = nullptr;
@@ -113,6 +131,9 @@ class Engine {
   bool allocFailed_ = false;
   // snapshot of mutable arrays: (device pointer, bytes) and the backup buffer
   std::vector<std::pair<void*, size_t>> mutable_;
+  std::vector<double> scaleSentinel_;
+  void invalidateNewtonScales();
+  void recordPhase(cudaEvent_t ev, cudaStream_t s);
   char* backup_ = nullptr;
   // phase timing events (recorded as external event nodes inside the graph)
   cudaEvent_t ev_[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

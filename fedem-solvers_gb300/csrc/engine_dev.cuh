@@ -61,6 +61,9 @@ struct DevData {
   int *meqn, *dofType, *dofModel;  // meqn: global equation, -1 fixed, -2 - k prescribed by model motion k
   // equation vectors
   double *FSk, *FDk, *FIk, *Qk, *qext, *FIact, *res, *del, *xref, *rref;
+  // forces set by an external process for the iterations of the current step
+  // (added to Q in the corrector residuals, cleared by the next predictor)
+  double* extRhs;
   float* rhs32;
   int* eqModel;
   // elements (SoA)

@@ -31,17 +31,7 @@
 namespace fgpu {
 namespace {
 
-constexpr long long kSpinLimit = 1LL << 21;  // polls of a bounded wait (about 2 s with backoff)
-
-// GPU-scope acquire load / release store of a front state
-__device__ inline int loadAcquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ inline void storeRelease(int* p, int v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
-}
+constexpr long long kSpinLimit = 1LL << 23;  // polls of a bounded wait (about 1-2 s)
 
 // partial LDL^T of front f in shared memory (F: maxRow^2, lcol/diag0: maxRow).
 // The original entries (front-ordered copy of the CSR values) and the
@@ -386,7 +376,7 @@ __global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const 
       int st = 0;
       if (k < len) {
         const int f = __ldg(leafPath + p0 + k);
-        st = loadAcquire(state + f);
+        st = *(volatile const int*)(state + f);
         path[k] = f;
       }
       const unsigned done = __ballot_sync(0xffffffffu, k < len && st == 2);
@@ -395,38 +385,36 @@ __global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const 
         break;
       }
     }
-    // every lane's acquire before any lane's reads of the done fronts' values
+    __threadfence();
     __syncwarp();
     for (int j = n - 1; j >= 0; --j) {
       const int f = path[j];
       int own = 0, ok = 1;
       if (lane == 0) {
-        int st = loadAcquire(state + f);
+        int st = *(volatile const int*)(state + f);
         if (st == 0) own = atomicCAS(state + f, 0, 1) == 0;
         if (!own) {
-          // exponential backoff (32 ns .. 1 us): thousands of warps may wait on
-          // the same few fronts near the roots, their polls must not crowd L2
           long long spins = 0;
-          unsigned pause = 32;
-          while (loadAcquire(state + f) != 2) {
-            __nanosleep(pause);
-            pause = pause < 1024 ? 2 * pause : 1024;
+          while (*(volatile const int*)(state + f) != 2) {
+            __nanosleep(20);
             if (++spins > kSpinLimit) {
               atomicOr(errFlag, 1);
               ok = 0;
               break;
             }
           }
+          __threadfence();
         }
       }
       own = __shfl_sync(0xffffffffu, own, 0);
       ok = __shfl_sync(0xffffffffu, ok, 0);
-      __syncwarp();  // lane 0's acquire before the other lanes' reads
+      __syncwarp();
       if (!ok) break;
       if (!own) continue;
       backwardOneFront<T>(d, f, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
-      __syncwarp();  // every lane's stores before lane 0's release
-      if (lane == 0) storeRelease(state + f, 2);
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) atomicExch(state + f, 2);
     }
   }
 }

@@ -437,6 +437,9 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   c.tEnd = o.d("timeEnd", 0.0);
   c.tInc = std::max(o.d("timeInc", 0.0), 1.0e-6);
   c.minInc = o.d("minInc", 0.001);
+  // initiateSystemTypeModule.f90:98, 125-126 (fixed step size)
+  c.maxInc = o.d("maxInc", 0.1);
+  if (c.tInc > 0.8 * c.maxInc) c.maxInc = 1.25 * c.tInc;
   c.maxIt = o.i("maxit", 15);
   c.minIt = o.i("minit", 1);
   c.fixedIt = o.i("numit", 0);

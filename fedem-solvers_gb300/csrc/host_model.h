@@ -16,7 +16,7 @@ namespace fgpu {
 // normTypeModule.f90:93-193).  Norm test codes: 1 = all-of, 2 = one-of, 0 = off.
 struct Control {
   double alpha = -0.1, beta = 0.3025, gamma = 0.6;
-  double tStart = 0.0, tEnd = 0.0, tInc = 0.0, minInc = 0.001;
+  double tStart = 0.0, tEnd = 0.0, tInc = 0.0, minInc = 0.001, maxInc = 0.1;
   int maxIt = 15, minIt = 1, fixedIt = 0, nUpdat = 0, maxSeqNoUpdate = 100;
   int stiffDampFiltering = 1;
   bool initEquilibrium = false;

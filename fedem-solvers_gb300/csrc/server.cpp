@@ -75,34 +75,46 @@ int Server::admit() {
   return 1;
 }
 
-int Server::collect(Job& j) {
+// Completes the requests of a job whose models reached their end time (or
+// failed) by the last chunk: results and finish time per request, while the
+// job's other models keep running.  all = true collects every request left.
+int Server::collect(Job& j, bool all) {
+  const int* states = j.engine->chunkStates();
   double t = now();
+  int n = 0;
   for (size_t k = 0; k < j.ids.size(); ++k) {
     Request& r = reqs_[j.ids[k]];
+    if (r.state != 1) continue;
+    const int st = states ? states[k] : ST_ITER;
+    if (!all && st != ST_DONE && st != ST_ERROR) continue;
     r.ur.resize(12 * (size_t)r.model->ntri);
     j.engine->getTriadUr((int)k, r.ur.data());
     r.iterations = j.engine->modelIterations((int)k);
     r.steps = j.engine->modelSteps((int)k);
     r.state = j.engine->modelState((int)k) == ST_DONE ? 2 : 3;
     r.finished = t;
+    ++n;
   }
-  return (int)j.ids.size();
+  return n;
 }
 
 int Server::pump() {
   int finished = 0;
-  // collect finished engines, keep the others fed
+  // collect finished requests and engines, keep the others fed
   for (size_t k = 0; k < jobs_.size();) {
     bool ready = false;
     int active = 1;
     if (jobs_[k].engine->pollChunk(&ready, &active)) return -951;
     if (ready && active == 0) {
-      finished += collect(jobs_[k]);
+      finished += collect(jobs_[k], true);
       inUse_ -= jobs_[k].bytes;
       jobs_.erase(jobs_.begin() + (long)k);
       continue;
     }
-    if (ready && jobs_[k].engine->launchChunk(chunk_)) return -952;
+    if (ready) {
+      finished += collect(jobs_[k], false);
+      if (jobs_[k].engine->launchChunk(chunk_)) return -952;
+    }
     ++k;
   }
   // admit what fits (several admission rounds if memory allows)

@@ -4,8 +4,10 @@
 // every admission round takes the pending requests that fit the remaining
 // HBM budget into a new engine with its own stream, so work of requests that
 // arrive while others run overlaps on the device.  Each request keeps its
-// state resident until it reaches its end time; finished engines release
-// their memory for the next admissions.
+// state resident until it reaches its end time, when it is completed (results
+// and finish time) at the next chunk boundary although the other models of
+// its engine go on; finished engines release their memory for the next
+// admissions.
 #pragma once
 
 #include <chrono>
@@ -48,7 +50,7 @@ class Server {
   };
   static size_t estimateBytes(const HostModel& m, const EngineOptions& opt);
   int admit();
-  int collect(Job& j);
+  int collect(Job& j, bool all);
 
   size_t budget_, inUse_ = 0;
   EngineOptions opt_;

@@ -51,6 +51,11 @@ def load_library(path=None):
         "getRhsVector": (c_bool, [P(c_dbl), c_int]),
         "getElementStiffnessMatrix": (c_bool, [P(c_dbl), c_int]),
         "getStateSize": (c_int, []),
+        "saveState": (c_bool, [P(c_dbl), c_int]),
+        "restartFromState": (c_int, [P(c_dbl), c_int, c_int]),
+        "setTime": (c_bool, [c_dbl]),
+        "setRhsVector": (c_bool, [P(c_dbl)]),
+        "addRhsVector": (c_bool, [P(c_dbl)]),
         "fgpu_model_create": (c_int, [ctypes.c_char_p, c_int, P(ctypes.c_char_p), P(vp)]),
         "fgpu_model_destroy": (None, [vp]),
         "fgpu_model_sizes": (c_int, [vp, P(c_ll)]),

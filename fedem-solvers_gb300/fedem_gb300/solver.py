@@ -3,7 +3,10 @@
 Mirrors PythonAPI/src/fedempy/solver.py (``FedemSolver``: constructor,
 ``solver_init`` :322, ``solve_next`` :631, ``solver_done`` :833,
 ``get_current_time``, ``get_state_var``, ``get_system_size``,
-``get_equations``, ``get_newton_matrix``, ``get_rhs_vector``) with the same
+``get_equations``, ``get_newton_matrix``, ``get_rhs_vector``, ``start_step``
+:677, ``solve_iteration`` :707, ``finish_step``, ``set_rhs_vector`` /
+``add_rhs_vector`` :1100-1110, ``get_state_size`` :495, ``save_state`` :546,
+``restart_from_state`` :398) with the same
 argument meaning and error behaviour (``FedemException`` on failure, the
 internal error flag blocks further calls after an error).
 """
@@ -30,11 +33,16 @@ class FedemSolver:
         if self.ierr.value != 0:
             raise FedemException(func + f"() cannot be called due to previous error ({self.ierr.value}).")
 
-    def solver_init(self, options, fsi=None):
-        """Reads the model (fsi text or -fsifile option) and initialises it."""
+    def solver_init(self, options, fsi=None, state_data=None):
+        """Reads the model (fsi text or -fsifile option) and initialises it,
+        continuing from state_data (a save_state array) when given."""
         argc, argv = _argv(["fedem_solver"] + list(options))
         cfsi = fsi.encode() if isinstance(fsi, str) else fsi
-        status = self._solver.solverInit(argc, argv, cfsi, None, 0, None, 0, None, None)
+        sd, nd = None, 0
+        if state_data is not None:
+            self._state_in = np.ascontiguousarray(state_data, dtype=np.float64)
+            sd, nd = self._state_in.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self._state_in.size
+        status = self._solver.solverInit(argc, argv, cfsi, sd, nd, None, 0, None, None)
         self.ierr.value = 0 if status >= 0 else status
         return status
 
@@ -77,13 +85,81 @@ class FedemSolver:
             raise FedemException("get_newton_matrix failed")
         return mat.reshape((n, n), order="F")
 
-    def get_rhs_vector(self):
+    def get_system_matrix(self, i_mat):
+        """Dense system matrix: 0 Newton, 1 stiffness, 2 mass, 3 damping (solverInterface.h:433)."""
+        n = self.get_system_size()
+        mat = np.zeros(n * n)
+        ok = self._solver.getSystemMatrix(mat.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(i_mat))
+        if not ok:
+            raise FedemException("get_system_matrix failed")
+        return mat.reshape((n, n), order="F")
+
+    def _rhs(self, i_vec):
         n = self.get_system_size()
         vec = np.zeros(n)
-        ok = self._solver.getRhsVector(vec.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0)
+        ok = self._solver.getRhsVector(vec.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(i_vec))
         if not ok:
             raise FedemException("get_rhs_vector failed")
         return vec
+
+    def get_rhs_vector(self):
+        """Right-hand side of the current linearised system."""
+        return self._rhs(0)
+
+    def get_external_force_vector(self):
+        """External force vector Q of the current iteration."""
+        return self._rhs(5)
+
+    def _vec(self, r_vec):
+        v = np.ascontiguousarray(r_vec, dtype=np.float64)
+        if v.size != self.get_system_size():
+            raise FedemException(f"Invalid vector length {v.size}")
+        return v
+
+    def set_rhs_vector(self, r_vec):
+        v = self._vec(r_vec)
+        return self._solver.setRhsVector(v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+    def add_rhs_vector(self, r_vec):
+        v = self._vec(r_vec)
+        return self._solver.addRhsVector(v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+    def start_step(self, time_next=None):
+        """Predictor and first linear system of the next step (optionally at time_next)."""
+        self.__check_error("start_step")
+        ok = True if time_next is None else self._solver.setTime(float(time_next))
+        return self._solver.startStep(ctypes.byref(self.ierr)) if ok else False
+
+    def solve_iteration(self):
+        """Solves the current system and assembles the next; False once converged."""
+        self.__check_error("solve_iteration")
+        return self._solver.solveIteration(ctypes.byref(self.ierr), False)
+
+    def finish_step(self):
+        """Iterates the started step to convergence; False at the end or on error."""
+        self.__check_error("finish_step")
+        return self._solver.solveIteration(ctypes.byref(self.ierr), True)
+
+    def get_state_size(self):
+        return self._solver.getStateSize()
+
+    def save_state(self):
+        """The solver state as a new float64 array (None if it cannot be saved now)."""
+        n = self.get_state_size()
+        data = np.zeros(n)
+        ok = self._solver.saveState(data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
+        return data if ok else None
+
+    def restart_from_state(self, state_data, write_to_rdb=2):
+        """Continues from a state saved by save_state; 0 on success."""
+        if write_to_rdb not in (0, 1, 2):
+            raise TypeError(f"Expected integer value in (0, 1, 2), got {write_to_rdb}.")
+        v = np.ascontiguousarray(state_data, dtype=np.float64)
+        rc = self._solver.restartFromState(v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), v.size,
+                                           int(write_to_rdb))
+        if rc == 0:
+            self.ierr.value = 0
+        return rc
 
     def run_all(self):
         """Runs the whole simulation (fedempy's usual solve_next loop)."""

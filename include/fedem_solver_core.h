@@ -12,13 +12,14 @@
  *
  * Hot path implemented on the GPU: initial static equilibrium and the
  * HHT-alpha Newton time steps of beam models (solverInit, solveNext,
- * getStateVar, getTime, getSystemSize, getEquations, getSystemMatrix with
- * iMat = 0, getNewtonMatrix, getRhsVector, getElementStiffnessMatrix,
- * solverDone, solverClose).  Entry points for features outside that path
- * (restart state, windowed stepping with external functions, eigenmodes,
- * inverse analysis, strain/beam-force recovery, externally driven iterations)
- * exist so the library loads as a drop-in, and return the reference's failure
- * value (false, 0 or a negative status, with *ierr = -1 where present).
+ * startStep, solveIteration, setTime, getStateVar, getTime, getSystemSize,
+ * getEquations, getSystemMatrix, getNewtonMatrix, getStiffness/Mass/
+ * DampingMatrix, get/set/addRhsVector, getElementStiffnessMatrix, in-core
+ * state save and restart, solverDone, solverClose).  Entry points for features
+ * outside that path (windowed stepping with external functions, eigenmodes,
+ * inverse analysis, strain/beam-force recovery, part and gauge states) exist
+ * so the library loads as a drop-in, and return the reference's failure value
+ * (false, 0 or a negative status, with *ierr = -1 where present).
  */
 #ifndef FEDEM_SOLVER_CORE_H
 #define FEDEM_SOLVER_CORE_H
@@ -32,26 +33,34 @@ extern "C" {
 
 /* solverInterface.h:65 -- reads the model (cfsi text, or -fsifile=<path> in
  * argv), sets it up on the GPU and solves the initial equilibrium when
- * -initEquilibrium is given.  Returns >= 0 on success, < 0 on error.
+ * -initEquilibrium is given; with stateData (ndat >= getStateSize()) the
+ * state saved by saveState for the same model is restored afterwards.
+ * Returns >= 0 on success, < 0 on error.
  * Extra option understood here: -gpuMixed (FP32 factor + FP64 refinement). */
 int solverInit(int argc, char** argv, const char* cfsi, const double* stateData, int ndat,
                const double* gagesData, int ngda, const double* extInput, int* nxinp);
 
-/* solverInterface.h:87 -- in-core restart: unsupported, returns -1. */
+/* solverInterface.h:87 -- in-core restart: restores a saveState array of the
+ * current model (positions, velocities, accelerations, element frames and
+ * forces, time, step counters); writeToRDB is ignored (no results database).
+ * Returns 0, or < 0 when there is no model or ndat < getStateSize(). */
 int restartFromState(const double* stateData, const int ndat, const int writeToRDB);
 
 /* solverInterface.h:110 -- windowed stepping with external inputs: unsupported. */
 bool solveWindow(int nStep, int nInc, int nIn, int nOut, const int* fOut, const double* times,
                  const double* inputs, double* outputs, int nDat, double* stateData, int* ierr);
 
-/* solverInterface.h:118-144 -- state vector sizes: no restart state, returns 0. */
+/* solverInterface.h:118 -- doubles saveState needs; :124-144 (transformation,
+ * part and gauge states, not kept by this solver) return 0. */
 int getStateSize(void);
 int getTransformationStateSize(void);
 int getPartDeformationStateSize(int bid);
 int getPartStressStateSize(int bid);
 int getGagesSize(void);
 
-/* solverInterface.h:156-170, :226-238 -- state saving: unsupported, returns false. */
+/* solverInterface.h:156 -- the solver state between steps into stateData;
+ * false within a started step or when ndat < getStateSize().
+ * :162-170, :226-238 (transformation, gauge and part states): false. */
 bool saveState(double* stateData, const int ndat);
 bool saveTransformationState(double* stateData, const int ndat);
 bool saveGages(double* stateData, const int ndat);
@@ -65,11 +74,19 @@ bool getBeamForcesFromDisp(const double* disp, const int* beamIDs, double* force
 bool getRelDisp(const double* disp, const int* Ids, double* relDis, const int ndof, const int nId);
 bool getRespVars(const double* disp, const int* Ids, double* resVar, const int ndof, const int nId);
 
-/* solverInterface.h:247 -- advances one time step on the GPU.  Returns false
- * at the end of the simulation or on error; *ierr != 0 tells them apart. */
+/* solverInterface.h:247 -- advances one time step on the GPU (or completes
+ * the step startStep began).  Returns false at the end of the simulation or
+ * on error; *ierr != 0 tells them apart. */
 bool solveNext(int* ierr);
 
-/* solverInterface.h:262, :278 -- externally driven Newton iterations: unsupported. */
+/* solverInterface.h:262 -- predictor of the next step and its first linear
+ * system (Newton matrix and right-hand side), which get/set/addRhsVector and
+ * getNewtonMatrix then see.  False at the end of the simulation or on error
+ * (*ierr = -999 when a step is already started).
+ * solverInterface.h:278 -- solves the assembled system, updates the state and
+ * assembles the next iteration; returns false when the step has converged
+ * (all = false) or, with all = true (iterate to convergence), at the end of
+ * the simulation; on error false with *ierr != 0 (-999: no step started). */
 bool startStep(int* ierr);
 bool solveIteration(int* ierr, bool all);
 
@@ -86,7 +103,9 @@ void solverClose(void);
 bool setExtFunc(int funcId, double value);
 /* solverInterface.h:349 -- current (or next) physical time. */
 double getTime(bool nextStep, int* ierr);
-/* solverInterface.h:355 -- unsupported, returns false. */
+/* solverInterface.h:355 -- time of the next step: increment nextTime - time,
+ * raised to the minimum increment; false for a negative increment or within
+ * a started step. */
 bool setTime(double nextTime);
 /* solverInterface.h:361, :369 */
 static inline double getCurrentTime(int* ierr) { return getTime(false, ierr); }
@@ -103,19 +122,26 @@ int getEquations(int bid, int* meqn);
 int getStateVar(int bid, double* var);
 /* solverInterface.h:426 -- number of equations (dofs = false) or DOFs. */
 int getSystemSize(bool dofs);
-/* solverInterface.h:433 -- dense column-major neq x neq matrix; iMat = 0
- * (Newton matrix of the last tangent update) is supported. */
+/* solverInterface.h:433 -- dense column-major neq x neq matrix: iMat = 0 the
+ * Newton matrix of the last tangent update, 1 stiffness, 2 mass, 3 damping at
+ * the current configuration (element matrices rotated with the current frames,
+ * axial spring/damper blocks included). */
 bool getSystemMatrix(double* Smat, int iMat);
-/* solverInterface.h:439-457 */
+/* solverInterface.h:439-457 -- getSystemMatrix with iMat = 0, 1, 2, 3 */
 bool getNewtonMatrix(double* Nmat);
 bool getStiffnessMatrix(double* Kmat);
 bool getMassMatrix(double* Mmat);
 bool getDampingMatrix(double* Cmat);
 /* solverInterface.h:465 -- 12x12 beam stiffness in element axes. */
 bool getElementStiffnessMatrix(double* Kmat, int bid);
-/* solverInterface.h:472 -- iVec = 0: the current right-hand side (residual). */
+/* solverInterface.h:472 -- iVec < 5: the right-hand side of the current
+ * linear system, 5: the external force vector Q. */
 bool getRhsVector(double* Rvec, int iVec);
-/* solverInterface.h:478, :484 -- unsupported (needs startStep), returns false. */
+/* solverInterface.h:478, :484 -- replaces / adds to the right-hand side of the
+ * system assembled by startStep or solveIteration.  Given in the first
+ * iteration of a step, the vector is also applied as external forces in the
+ * step's later iterations (the reference's keepDuringIterations).  False
+ * outside a started step. */
 bool setRhsVector(const double* Rvec);
 bool addRhsVector(const double* Rvec);
 /* solverInterface.h:491 -- unsupported, returns false. */

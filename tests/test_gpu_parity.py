@@ -308,3 +308,31 @@ def test_engine_driven_load_matches_oracle(gpu, oracle_lib, mixed):
     assert err <= (MIXED_TOL if mixed else FP64_TOL), err
     if not mixed:
         assert b.info(0)["iterations"] == o.iterations()
+
+
+def test_system_stiffness_mass_damping_through_solver_abi(gpu, oracle_lib):
+    """getSystemMatrix(1, 2, 3) (solverInterface.h:433) against the oracle's
+    assembly with unit scales after solverInit: beams with Rayleigh damping,
+    axial springs (one with stiffness-proportional damping) and dampers."""
+    from fedem_gb300 import models
+    from fedem_gb300.solver import FedemSolver
+    from oracle.oracle import OracleModel
+
+    fsi = models.beam_chain_fsi(12, 0.25, 0.1, 0.01, clamp=0, load_node=12, load_dof=2, load=100.0,
+                                **models.STEEL, anchors=[(3.0, 1.0, 0.0)],
+                                springs=[(12, ("anchor", 0), 2.0e5, 1.0, 0.002), (3, 9, 5.0e4, 1.5)],
+                                dampers=[(12, ("anchor", 0), 300.0)])
+    fsi = fsi.replace("  shadowPosAlg = 1\n", "  shadowPosAlg = 1\n  alpha1 = 0.5\n  alpha2 = 0.001\n")
+    opts = ["-timeInc=0.001", "-timeEnd=0.01"]
+    o = OracleModel(fsi, opts)
+    s = FedemSolver(solver_options=opts, fsi=fsi)
+    n = s.get_system_size()
+    for i_mat, scales in ((1, (0.0, 0.0, 1.0)), (2, (1.0, 0.0, 0.0)), (3, (0.0, 1.0, 0.0))):
+        rp, ci, v = o.newton_upper(*scales)
+        ref = np.zeros((n, n))
+        for i in range(n):
+            ref[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        ref = np.triu(ref) + np.triu(ref, 1).T
+        got = s.get_system_matrix(i_mat)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), i_mat
+    assert s.solver_done() == 0
