@@ -33,6 +33,50 @@ namespace {
 
 constexpr long long kSpinLimit = 1LL << 23;  // polls of a bounded wait (about 1-2 s)
 
+// Partial LDL^T of a front, blocked: the pivot panel (all rows, the np
+// pivot columns) is factored right-looking within the panel, one row per lane;
+// the update matrix (the Schur complement of the update block) is then formed
+// in one rank-np pass over its lower triangle, one entry per lane, and stored
+// packed column by column at Uout.  F afterwards holds D on the diagonal and
+// the unit L below it in the panel; the unscaled panel values of the update
+// rows (L d) are kept in the unused upper triangle (row k, column i) for the
+// rank-np pass.
+template <typename T>
+__device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int lane, double tolFact, int& neg,
+                              bool& sing, T* Uout) {
+  for (int k = 0; k < np; ++k) {
+    const T dk = F[k + nr * k];
+    const bool bad = !(fabs((double)dk) > tolFact * fabs((double)diag0[k]));
+    sing |= bad;
+    if (dk < T(0)) ++neg;
+    const T inv = bad ? T(0) : T(1) / dk;
+    for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
+    __syncwarp();
+    for (int i = k + 1 + lane; i < nr; i += 32) {
+      const T fik = F[i + nr * k];
+      const int je = i < np - 1 ? i : np - 1;
+      for (int j = k + 1; j <= je; ++j) F[i + nr * j] -= fik * lcol[j];
+      if (i >= np) F[k + nr * i] = fik;
+      F[i + nr * k] = lcol[i];
+    }
+    __syncwarp();
+  }
+  // update matrix, lower triangle packed column by column: entry e = lane + 32 q
+  // is (row np + b + t, column np + b)
+  const int nu = nr - np;
+  int b = 0, t = lane;
+  while (b < nu && t >= nu - b) { t -= nu - b; ++b; }
+  for (int e = lane; b < nu; e += 32) {
+    const int i = np + b + t, j = np + b;
+    T acc = T(0);
+    for (int k = 0; k < np; ++k) acc += F[k + nr * i] * F[j + nr * k];
+    Uout[e] = F[i + nr * j] - acc;
+    t += 32;
+    while (b < nu && t >= nu - b) { t -= nu - b; ++b; }
+  }
+  __syncwarp();
+}
+
 // partial LDL^T of front f in shared memory (F: maxRow^2, lcol/diag0: maxRow).
 // The original entries (front-ordered copy of the CSR values) and the
 // children's packed update matrices are contiguous per front and loaded
@@ -42,7 +86,7 @@ template <typename T>
 __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* asmVal, T* Lbase,
                                T* Ubase, double tolFact, int lane) {
   const int m = d.fModel[f];
-  const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
+  const int nr = d.fNrow[f], np = d.fNpiv[f];
   const int64_t ao = d.fAsmOff[f], so = d.fSegOff[f];
   const int na = d.fNasm[f], ns = d.fSegLen[f], nch = d.fNchild[f];
   for (int k = lane; k < nr * nr; k += 32) F[k] = T(0);
@@ -82,29 +126,10 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
   }
   int neg = 0;
   bool sing = false;
-  for (int k = 0; k < np; ++k) {
-    const T dk = F[k + nr * k];
-    const bool bad = !(fabs((double)dk) > tolFact * fabs((double)diag0[k]));
-    sing |= bad;
-    if (dk < T(0)) ++neg;
-    const T inv = bad ? T(0) : T(1) / dk;
-    for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
-    __syncwarp();
-    // lower triangle of the trailing block, one row per lane
-    for (int i = k + 1 + lane; i < nr; i += 32) {
-      const T fik = F[i + nr * k];
-      for (int j = k + 1; j <= i; ++j) F[i + nr * j] -= fik * lcol[j];
-    }
-    __syncwarp();
-    for (int i = k + 1 + lane; i < nr; i += 32) F[i + nr * k] = lcol[i];
-    __syncwarp();
-  }
+  // the update matrix goes packed into the parent's segment
+  factorBlocked<T>(F, lcol, diag0, nr, np, lane, tolFact, neg, sing, Ubase + d.fUOff[f]);
   T* Lout = Lbase + d.fLOff[f];
   for (int k = lane; k < nr * np; k += 32) Lout[k] = F[k];
-  // update matrix: lower triangle packed column by column into the parent's segment
-  T* Uout = Ubase + d.fUOff[f];
-  for (int b = 0, base = 0; b < nu; base += nu - b, ++b)
-    for (int a = b + lane; a < nu; a += 32) Uout[base + a - b] = F[(np + a) + nr * (np + b)];
   if (lane == 0) {
     if (neg) atomicAdd(&d.m.negPiv[m], neg);
     if (sing) atomicOr(&d.m.status[m], SS_SINGULAR);
