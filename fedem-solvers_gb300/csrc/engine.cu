@@ -596,9 +596,9 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     pplan_.maxRow = maxRowAll;
     pplan_.maxNpiv = 1;
     for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
-    pplan_.cntFactor = alloc<int>(nfr);
-    pplan_.cntForward = alloc<int>(nfr);
-    pplan_.stateBackward = alloc<int>(nfr);
+    pplan_.cntFactor = alloc<int>(nfr + 1);  // + the leaf counter
+    pplan_.cntForward = alloc<int>(nfr + 1);  // + the leaf counter
+    pplan_.stateBackward = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.errFlag = alloc<int>(1);
     d_.errFlag = pplan_.errFlag;
   }

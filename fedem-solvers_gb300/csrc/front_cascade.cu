@@ -281,6 +281,11 @@ __device__ inline int climb(const DevData& d, int f, int* cnt, int lane) {
   return next;
 }
 
+// Leaves are taken in their stored order (longest root paths first) from a
+// launch-wide counter, cnt[nfrontTot]; lane 0 asks for the next leaf before
+// the current one is processed, so the request's latency is hidden.
+__device__ inline int requestLeaf(int* next, int lane) { return lane == 0 ? atomicAdd(next, 1) : 0; }
+
 // factorisation (models with a tangent update) fused with the forward
 // elimination of the first solve (all active models): one climb per front, and
 // the forward elimination reads L from the front still in shared memory
@@ -289,19 +294,20 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
                                       const T* asmVal, T* Lbase, T* Ubase, double tolFact, const double* rhs, T* X,
                                       T* Wv, int* cnt) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int Wt = gridDim.x * wpb;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int capL = maxRow * maxRow;  // F doubles as the staging area of L
   T* F = reinterpret_cast<T*>(smraw) + (size_t)w * ((size_t)maxRow * maxRow + 3 * maxRow);
   T* lcol = F + (size_t)maxRow * maxRow;
   T* diag0 = lcol + maxRow;
   T* v = diag0 + maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
+  int* const next = cnt + d.nfrontTot;
+  int idx = __shfl_sync(0xffffffffu, requestLeaf(next, lane), 0);
+  while (idx < nLeaves) {
+    const int pending = requestLeaf(next, lane);
     int f = leaves[idx];
     const int fl = d.m.flags[d.fModel[f]];
-    if (!(fl & FL_ACTIVE)) continue;
     const bool factor = fl & FL_TANGENT;
-    while (f >= 0) {
+    while ((fl & FL_ACTIVE) && f >= 0) {
       const T* Lres = nullptr;
       if (factor) {
         factorOneFront<T>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase, tolFact, lane);
@@ -312,6 +318,7 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
         forwardOneFront<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres);
       f = climb(d, f, cnt, lane);
     }
+    idx = __shfl_sync(0xffffffffu, pending, 0);
   }
 }
 
@@ -319,18 +326,21 @@ template <typename T>
 __global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
                                 const T* Lbase, const double* rhs, T* X, T* W, int* cnt) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int Wt = gridDim.x * wpb;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* v = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
   T* Ls = v + maxRow;
-  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
+  int* const next = cnt + d.nfrontTot;
+  int idx = __shfl_sync(0xffffffffu, requestLeaf(next, lane), 0);
+  while (idx < nLeaves) {
+    const int pending = requestLeaf(next, lane);
     int f = leaves[idx];
-    if (!(d.m.flags[d.fModel[f]] & FL_ACTIVE)) continue;
-    while (f >= 0) {
+    const bool active = d.m.flags[d.fModel[f]] & FL_ACTIVE;
+    while (active && f >= 0) {
       if (!forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr))
         forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
       f = climb(d, f, cnt, lane);
     }
+    idx = __shfl_sync(0xffffffffu, pending, 0);
   }
 }
 
@@ -381,16 +391,21 @@ __global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const 
                                const int* __restrict__ leafPathOff, int nLeaves, int maxRow, int capL,
                                int maxPath, const T* Lbase, T* X, int* state, int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int Wt = gridDim.x * wpb;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t perWarp = (size_t)(maxRow + capL) * sizeof(T) + (size_t)maxPath * sizeof(int);
   unsigned char* mine = smraw + (size_t)w * ((perWarp + 15) & ~(size_t)15);
   T* xs = reinterpret_cast<T*>(mine);
   T* Ls = xs + maxRow;
   int* path = reinterpret_cast<int*>(Ls + capL);
-  for (int idx = blockIdx.x * wpb + w; idx < nLeaves; idx += Wt) {
+  int* const next = state + d.nfrontTot;
+  int idx = __shfl_sync(0xffffffffu, requestLeaf(next, lane), 0);
+  while (idx < nLeaves) {
+    const int pending = requestLeaf(next, lane);
     const int leaf = leaves[idx];
-    if (!(d.m.flags[d.fModel[leaf]] & FL_ACTIVE)) continue;
+    if (!(d.m.flags[d.fModel[leaf]] & FL_ACTIVE)) {
+      idx = __shfl_sync(0xffffffffu, pending, 0);
+      continue;
+    }
     // the path from the leaf up to (not including) the first front already done:
     // the precomputed path and its states are read by all lanes at once (a done
     // front has only done ancestors)
@@ -441,6 +456,7 @@ __global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const 
       __syncwarp();
       if (lane == 0) atomicExch(state + f, 2);
     }
+    idx = __shfl_sync(0xffffffffu, pending, 0);
   }
 }
 
@@ -481,7 +497,7 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
   if (p.nLeaves <= 0) return;
   const double tol = 1.0e-12;
   const size_t perWarp = (size_t)p.maxRow * p.maxRow + 3 * p.maxRow;
-  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * (size_t)d.nfrontTot, s);
+  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
   if (fp32) {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
     const size_t sm = (size_t)wpb * perWarp * sizeof(float);
@@ -509,7 +525,7 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s) {
   if (p.nLeaves <= 0) return;
   const int wpb = 8;
-  cudaMemsetAsync(p.cntForward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
+  cudaMemsetAsync(p.cntForward, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
@@ -532,7 +548,7 @@ void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, i
   const int fin = (fp32 && last) ? 1 : 0;
   if (p.nLeaves <= 0) return;
   const int wpb = 8;
-  cudaMemsetAsync(p.stateBackward, 0, sizeof(int) * (size_t)d.nfrontTot, s);
+  cudaMemsetAsync(p.stateBackward, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
   const int needed = (p.nLeaves + wpb - 1) / wpb;
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));

@@ -45,6 +45,7 @@ struct PersistentPlan {
   int maxPath;        // longest leaf-to-root path (fronts)
   int maxAsm;         // largest number of original entries of one front
   int maxSeg;         // largest children update segment of one front (packed lower values)
+  // per-front counters / states, each followed by the launch's leaf counter
   int *cntFactor, *cntForward, *stateBackward, *errFlag;
 };
 // factorisation of the models with a tangent update fused with the forward
