@@ -567,11 +567,9 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     }
     // leaf-to-root path lengths: parents follow their children in each model's order
     std::vector<int> pathLen(nfr, 1);
-    pplan_.maxPath = 1;
     for (int f = nfr - 1; f >= 0; --f) {
       if (parent[f] > f) pathLen[f] = pathLen[parent[f]] + 1;
       else if (parent[f] >= 0) { err = "assembly tree not in post-order"; return -907; }
-      pplan_.maxPath = std::max(pplan_.maxPath, pathLen[f]);
     }
     // leaves with the longest paths first: the cascades' critical paths (the
     // deep trees of the large models) start in the first wave of warps
@@ -582,23 +580,34 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     int* dLeaves = nullptr;
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
-    std::vector<int> lpath, lpathOff(1, 0);
-    for (int l : leaves) {
-      for (int f = l; f >= 0; f = parent[f]) lpath.push_back(f);
-      lpathOff.push_back((int)lpath.size());
+    // roots and leaf counts per model (the backward queue's initial slots and total)
+    std::vector<int> rootOff(nm + 1, 0), roots, leafCnt(nm, 0);
+    for (int f = 0; f < nfr; ++f) {
+      if (parent[f] < 0) ++rootOff[fmodel[f] + 1];
+      if (nchild[f] == 0) ++leafCnt[fmodel[f]];
     }
-    int *dPath = nullptr, *dPathOff = nullptr;
-    UPV(dPath, int, lpath);
-    UPV(dPathOff, int, lpathOff);
-    pplan_.leafPath = dPath;
-    pplan_.leafPathOff = dPathOff;
+    for (int m = 0; m < nm; ++m) rootOff[m + 1] += rootOff[m];
+    roots.resize(rootOff[nm]);
+    {
+      std::vector<int> fill(rootOff.begin(), rootOff.end() - 1);
+      for (int f = 0; f < nfr; ++f)
+        if (parent[f] < 0) roots[fill[fmodel[f]]++] = f;
+    }
+    int *dRootOff = nullptr, *dRoots = nullptr, *dLeafCnt = nullptr;
+    UPV(dRootOff, int, rootOff);
+    UPV(dRoots, int, roots);
+    UPV(dLeafCnt, int, leafCnt);
+    pplan_.modelRootOff = dRootOff;
+    pplan_.modelRoots = dRoots;
+    pplan_.modelLeafCnt = dLeafCnt;
     pplan_.nLeaves = (int)leaves.size();
     pplan_.maxRow = maxRowAll;
     pplan_.maxNpiv = 1;
     for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
     pplan_.cntFactor = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.cntForward = alloc<int>(nfr + 1);  // + the leaf counter
-    pplan_.stateBackward = alloc<int>(nfr + 1);  // + the leaf counter
+    pplan_.bwQueue = alloc<int>(std::max<size_t>(leaves.size(), 1));
+    pplan_.bwCtr = alloc<int>(3);
     pplan_.errFlag = alloc<int>(1);
     d_.errFlag = pplan_.errFlag;
   }
@@ -719,7 +728,7 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
     if (sweep == 1 && timedForward) recordPhase(ev_[5], s);
     if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
     if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
-    launchBackwardClaim(d_, pplan_, f32, sweep, sweep == sw - 1, s);
+    launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
   }
 }
 

@@ -6,12 +6,11 @@
 // is done, and the warp whose increment completes the count goes on with the
 // parent itself.  Nothing ever waits, so the launch is correct whatever the
 // residency (several engines may run concurrently on their own streams).
-// The backward solve runs top-down along the leaf-to-root paths: the warp of
-// a leaf walks its path from the highest front not yet done down to the leaf,
-// claiming each front with a compare-and-swap before solving it.  A warp that
-// finds a front claimed by another warp waits for it; that warp is running and
-// solves the front without waiting on anything, so the wait ends whatever the
-// residency.  Each wait is still bounded and sets errFlag when it runs out.
+// The backward solve runs top-down through a work queue of fronts whose
+// parents are solved (kBackwardQueue); a warp waits only for a queue slot to
+// be filled, by warps that are running and never wait themselves, so the wait
+// ends whatever the residency.  Each wait is still bounded and sets errFlag
+// when it runs out.
 // The forward and backward solves stage each front's L block in shared memory
 // first (one burst of loads instead of one load latency per pivot).
 //
@@ -385,78 +384,73 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
   }
 }
 
-// top-down along the leaf-to-root paths; state[f]: 0 open, 1 claimed, 2 done
+// Top-down work queue.  kBackwardPrep puts the roots of the active models in
+// the first queue slots and sets the slot total to their number of leaves;
+// a warp takes the next slot, waits until a front is stored there, solves it
+// and goes on with its first child, storing the other children in fresh
+// slots, until it reaches a leaf.  Every such chain ends at a distinct leaf,
+// so the slots are exactly the leaves of the active models: a warp whose slot
+// number reaches the total is done.  A front is stored only after its parent
+// is solved (fence, then the slot write; the taker fences after reading it).
+// A waiting warp holds no front, and every stored slot below the one it waits
+// for is held by a running warp that solves without waiting, so each wait
+// ends; it is still bounded and sets errFlag when it runs out.
+// ctr: [0] next slot to take, [1] next free slot, [2] slot total.
+__global__ void kBackwardPrep(DevData d, const int* __restrict__ rootOff, const int* __restrict__ roots,
+                              const int* __restrict__ leafCnt, int* queue, int* ctr) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= d.m.n || !(d.m.flags[m] & FL_ACTIVE)) return;
+  const int r0 = rootOff[m], nr = rootOff[m + 1] - r0;
+  const int base = atomicAdd(ctr + 1, nr);
+  for (int q = 0; q < nr; ++q) queue[base + q] = roots[r0 + q];
+  atomicAdd(ctr + 2, leafCnt[m]);
+}
+
 template <typename T>
-__global__ void kBackwardClaim(DevData d, const int* __restrict__ leaves, const int* __restrict__ leafPath,
-                               const int* __restrict__ leafPathOff, int nLeaves, int maxRow, int capL,
-                               int maxPath, const T* Lbase, T* X, int* state, int* errFlag, int acc, int finalize) {
+__global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
+                               int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t perWarp = (size_t)(maxRow + capL) * sizeof(T) + (size_t)maxPath * sizeof(int);
-  unsigned char* mine = smraw + (size_t)w * ((perWarp + 15) & ~(size_t)15);
-  T* xs = reinterpret_cast<T*>(mine);
+  T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
   T* Ls = xs + maxRow;
-  int* path = reinterpret_cast<int*>(Ls + capL);
-  int* const next = state + d.nfrontTot;
-  int idx = __shfl_sync(0xffffffffu, requestLeaf(next, lane), 0);
-  while (idx < nLeaves) {
-    const int pending = requestLeaf(next, lane);
-    const int leaf = leaves[idx];
-    if (!(d.m.flags[d.fModel[leaf]] & FL_ACTIVE)) {
-      idx = __shfl_sync(0xffffffffu, pending, 0);
-      continue;
-    }
-    // the path from the leaf up to (not including) the first front already done:
-    // the precomputed path and its states are read by all lanes at once (a done
-    // front has only done ancestors)
-    const int p0 = leafPathOff[idx], len = leafPathOff[idx + 1] - p0;
-    int n = len;
-    for (int k0 = 0; k0 < len; k0 += 32) {
-      const int k = k0 + lane;
-      int st = 0;
-      if (k < len) {
-        const int f = __ldg(leafPath + p0 + k);
-        st = *(volatile const int*)(state + f);
-        path[k] = f;
-      }
-      const unsigned done = __ballot_sync(0xffffffffu, k < len && st == 2);
-      if (done) {
-        n = k0 + __ffs(done) - 1;
-        break;
-      }
-    }
-    __threadfence();
-    __syncwarp();
-    for (int j = n - 1; j >= 0; --j) {
-      const int f = path[j];
-      int own = 0, ok = 1;
-      if (lane == 0) {
-        int st = *(volatile const int*)(state + f);
-        if (st == 0) own = atomicCAS(state + f, 0, 1) == 0;
-        if (!own) {
-          long long spins = 0;
-          while (*(volatile const int*)(state + f) != 2) {
-            __nanosleep(20);
-            if (++spins > kSpinLimit) {
-              atomicOr(errFlag, 1);
-              ok = 0;
-              break;
-            }
-          }
-          __threadfence();
+  const int total = *(volatile const int*)(ctr + 2);
+  for (;;) {
+    const int slot = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(ctr, 1) : 0, 0);
+    if (slot >= total) break;
+    int f = -1, ok = 1;
+    if (lane == 0) {
+      long long spins = 0;
+      while ((f = *(volatile const int*)(queue + slot)) < 0) {
+        __nanosleep(32);
+        if (++spins > kSpinLimit) {
+          atomicOr(errFlag, 1);
+          ok = 0;
+          break;
         }
       }
-      own = __shfl_sync(0xffffffffu, own, 0);
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      __syncwarp();
-      if (!ok) break;
-      if (!own) continue;
+      __threadfence();
+    }
+    f = __shfl_sync(0xffffffffu, f, 0);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    if (!ok) break;
+    while (f >= 0) {
       backwardOneFront<T>(d, f, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
       __threadfence();
       __syncwarp();
-      if (lane == 0) atomicExch(state + f, 2);
+      const int nch = d.fNchild[f];
+      int next = -1;
+      if (nch > 0) {
+        const int* ch = d.childList + d.fChildOff[f];
+        next = ch[0];
+        if (lane == 0 && nch > 1) {
+          const int base = atomicAdd(ctr + 1, nch - 1);
+          for (int q = 1; q < nch; ++q) atomicExch(queue + base + q - 1, ch[q]);
+        }
+      }
+      __syncwarp();
+      f = next;
     }
-    idx = __shfl_sync(0xffffffffu, pending, 0);
   }
 }
 
@@ -543,31 +537,30 @@ void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, 
   }
 }
 
-void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s) {
+void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s) {
   const int acc = !fp32 ? ACC_SET : (sweep == 0 ? ACC_FIRST : ACC_ADD);
   const int fin = (fp32 && last) ? 1 : 0;
   if (p.nLeaves <= 0) return;
   const int wpb = 8;
-  cudaMemsetAsync(p.stateBackward, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
+  cudaMemsetAsync(p.bwCtr, 0, sizeof(int) * 3, s);
+  cudaMemsetAsync(p.bwQueue, 0xff, sizeof(int) * (size_t)p.nLeaves, s);
+  kBackwardPrep<<<(d.m.n + 127) / 128, 128, 0, s>>>(d, p.modelRootOff, p.modelRoots, p.modelLeafCnt, p.bwQueue,
+                                                    p.bwCtr);
   const int needed = (p.nLeaves + wpb - 1) / wpb;
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
-    const size_t per = ((size_t)(p.maxRow + capL) * sizeof(float) + (size_t)p.maxPath * sizeof(int) + 15) & ~(size_t)15;
-    const size_t sm = (size_t)wpb * per;
-    allowBigSmem(kBackwardClaim<float>, sm);
-    const int blocks = occupancyBlocks(kBackwardClaim<float>, 32 * wpb, sm, needed);
-    kBackwardClaim<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.leafPath, p.leafPathOff, p.nLeaves, p.maxRow,
-                                                      capL, p.maxPath, d.L32,
-                                                      d.x32, p.stateBackward, p.errFlag, acc, fin);
+    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
+    allowBigSmem(kBackwardQueue<float>, sm);
+    const int blocks = occupancyBlocks(kBackwardQueue<float>, 32 * wpb, sm, needed);
+    kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, p.bwQueue, p.bwCtr,
+                                                      p.errFlag, acc, fin);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
-    const size_t per = ((size_t)(p.maxRow + capL) * sizeof(double) + (size_t)p.maxPath * sizeof(int) + 15) & ~(size_t)15;
-    const size_t sm = (size_t)wpb * per;
-    allowBigSmem(kBackwardClaim<double>, sm);
-    const int blocks = occupancyBlocks(kBackwardClaim<double>, 32 * wpb, sm, needed);
-    kBackwardClaim<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.leafPath, p.leafPathOff, p.nLeaves, p.maxRow,
-                                                        capL, p.maxPath, d.L64,
-                                                        d.x64, p.stateBackward, p.errFlag, acc, fin);
+    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
+    allowBigSmem(kBackwardQueue<double>, sm);
+    const int blocks = occupancyBlocks(kBackwardQueue<double>, 32 * wpb, sm, needed);
+    kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, p.bwQueue, p.bwCtr,
+                                                        p.errFlag, acc, fin);
   }
 }
 

@@ -38,15 +38,17 @@ void launchStaticFinish(const DevData& d, cudaStream_t s);
 // --- front_cascade.cu: one launch per phase over all fronts of all models ----
 struct PersistentPlan {
   const int* leaves;  // fronts without children, longest root path first
-  const int* leafPath, *leafPathOff;  // each leaf's fronts up to its root, leaf first
   int nLeaves;
   int maxRow;         // largest front of the batch (rows)
   int maxNpiv;        // largest pivot block of the batch
-  int maxPath;        // longest leaf-to-root path (fronts)
   int maxAsm;         // largest number of original entries of one front
   int maxSeg;         // largest children update segment of one front (packed lower values)
-  // per-front counters / states, each followed by the launch's leaf counter
-  int *cntFactor, *cntForward, *stateBackward, *errFlag;
+  // per-front counters, each followed by the launch's leaf counter
+  int *cntFactor, *cntForward, *errFlag;
+  // backward work queue: each model's roots (modelRootOff, modelRoots) and
+  // number of leaves, the queue (nLeaves slots) and its counters (3)
+  const int *modelRootOff, *modelRoots, *modelLeafCnt;
+  int *bwQueue, *bwCtr;
 };
 // factorisation of the models with a tangent update fused with the forward
 // elimination of rhs for every active model (first solve of an iteration)
@@ -56,7 +58,7 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s);
 // back substitution; stores the solution in del (FP64 solve) or accumulates it in xref
 // (FP32 refinement sweep `sweep`; the last sweep also copies xref to del)
-void launchBackwardClaim(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
+void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
 // prescribed deflections (step start), their predictor right-hand side (after the
 // element Newton matrices), and the restart state of pure linear quasi-static steps
 void launchMotions(const DevData& d, cudaStream_t s);
