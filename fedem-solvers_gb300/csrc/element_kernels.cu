@@ -50,7 +50,8 @@ __device__ inline void crossd(const double* a, const double* b, double* c) {
 // the reference interpolates sin(h)/h linearly (sinEpsOverEps = sin(epsTh2)/epsTh2,
 // evaluated on the host); cos(h) is then its Taylor series to h^6 (the next
 // term is below 1e-30), which spares the FP64 sine/cosine on the usual small
-// increments.  The quaternion is normalised twice, by one reciprocal each.
+// increments.  The quaternion is normalised twice, by one reciprocal square
+// root each.
 __device__ inline void rotvecToMat(const double* rv, double sinEpsOverEps, double* R /* col-major 3x3 */) {
   const double epsTh2 = 0.0005;
   double thh = 0.5 * sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
@@ -66,9 +67,9 @@ __device__ inline void rotvecToMat(const double* rv, double sinEpsOverEps, doubl
     fac = sthh / thh;
   }
   double q0 = cthh, q1 = rv[0] * fac * 0.5, q2 = rv[1] * fac * 0.5, q3 = rv[2] * fac * 0.5;
-  double inv = 1.0 / sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+  double inv = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
   q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
-  inv = 1.0 / sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+  inv = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
   q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
   R[0] = 2.0 * (q1 * q1 + q0 * q0) - 1.0;
   R[4] = 2.0 * (q2 * q2 + q0 * q0) - 1.0;
@@ -89,20 +90,24 @@ __device__ inline void orthonormRot(double* R /* col-major 3x3 */) {
   int imax = 0;
   if (r(1, 1) > r(imax, imax)) imax = 1;
   if (r(2, 2) > r(imax, imax)) imax = 2;
+  // one reciprocal for the three off-diagonal components and one reciprocal
+  // square root for the normalisation
   if (tr > r(imax, imax)) {
     q[0] = sqrt(1.0 + tr) * 0.5;
-    q[1] = (r(2, 1) - r(1, 2)) / (4.0 * q[0]);
-    q[2] = (r(0, 2) - r(2, 0)) / (4.0 * q[0]);
-    q[3] = (r(1, 0) - r(0, 1)) / (4.0 * q[0]);
+    const double f = 1.0 / (4.0 * q[0]);
+    q[1] = (r(2, 1) - r(1, 2)) * f;
+    q[2] = (r(0, 2) - r(2, 0)) * f;
+    q[3] = (r(1, 0) - r(0, 1)) * f;
   } else {
     int i = imax, j = (imax + 1) % 3, k = (imax + 2) % 3;
     q[i + 1] = sqrt(r(i, i) * 0.5 + (1.0 - tr) * 0.25);
-    q[0] = (r(k, j) - r(j, k)) / (4.0 * q[i + 1]);
-    q[j + 1] = (r(j, i) + r(i, j)) / (4.0 * q[i + 1]);
-    q[k + 1] = (r(k, i) + r(i, k)) / (4.0 * q[i + 1]);
+    const double f = 1.0 / (4.0 * q[i + 1]);
+    q[0] = (r(k, j) - r(j, k)) * f;
+    q[j + 1] = (r(j, i) + r(i, j)) * f;
+    q[k + 1] = (r(k, i) + r(i, k)) * f;
   }
-  double n = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  for (int a = 0; a < 4; ++a) q[a] /= n;
+  const double inv = rsqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int a = 0; a < 4; ++a) q[a] *= inv;
   R[0] = 2.0 * (q[1] * q[1] + q[0] * q[0]) - 1.0;
   R[4] = 2.0 * (q[2] * q[2] + q[0] * q[0]) - 1.0;
   R[8] = 2.0 * (q[3] * q[3] + q[0] * q[0]) - 1.0;
@@ -335,10 +340,10 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
       atomicOr(&d.m.status[m], SS_COROT);
       return;
     }
-    lx = sqrt(lx);
-    lz = sqrt(lz);
+    // unit vectors: one reciprocal square root per length, then products
+    const double ilx = rsqrt(lx), ilz = rsqrt(lz);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) { ex[k] /= lx; ez[k] /= lz; }
+    for (int k = 0; k < 3; ++k) { ex[k] *= ilx; ez[k] *= ilz; }
     crossd(ez, ex, ey);
     double T[12] = {ex[0], ex[1], ex[2], ey[0], ey[1], ey[2], ez[0], ez[1], ez[2], p[0][0], p[0][1], p[0][2]};
     double Rel[12];
@@ -917,6 +922,14 @@ __device__ inline bool isBad(double v) { return !(fabs(v) <= 1.0e300); }
 constexpr int NPART = 21;
 constexpr int CHUNK_TPB = 256;
 
+// |x| as a bit pattern: for non-negative doubles the order of the patterns is
+// the numeric order (NaN patterns are above infinity), so the maxima and the
+// finiteness test run on the integer pipe and leave the FP64 pipe to the sums
+__device__ inline unsigned long long absBits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+__device__ inline unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
 __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
   __shared__ double sh[CHUNK_TPB / 32][NPART];
   const int c = blockIdx.x;
@@ -924,9 +937,15 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
   if (!(d.m.flags[m] & FL_ACTIVE)) return;
   const double* wD = d.m.wDisp + 3 * m;
   const double* wF = d.m.wForce + 3 * m;
-  double v[NPART];
+  const unsigned long long badBits = absBits(1.0e300);
+  // sums: 2-4 disp/vel/acc, 5 residual, 6 energy; maxima as bit patterns:
+  // mx[0] energy, mx[1 + 3 q + t] vector q of DOF type t; (the weight sums
+  // 0 and 1 are per-model constants)
+  double v2 = 0.0, v3 = 0.0, v4 = 0.0, v5 = 0.0, v6 = 0.0;
+  unsigned long long mx[13];
 #pragma unroll
-  for (int k = 0; k < NPART; ++k) v[k] = 0.0;
+  for (int k = 0; k < 13; ++k) mx[k] = 0ull;
+  bool bad = false;
   const int cEnd = d.chunkEnd[c];
   for (int i0 = d.chunkStart[c] + threadIdx.x; i0 < cEnd; i0 += 4 * CHUNK_TPB) {
     // four DOFs per pass: all loads issued before the ordered accumulation
@@ -945,45 +964,54 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
     for (int u = 0; u < 4; ++u) rr[u] = eqs[u] >= 0 ? d.res[eqs[u]] : 0.0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-    if (eqs[u] < 0) continue;
-    const int t = ts[u];
-    double wd = wD[t], wf = wF[t];
-    double s0 = a0[u], s1 = a1[u], s2 = a2[u], r = rr[u];
-    if (isBad(s0) || isBad(r)) v[20] = 1.0;
-    v[0] += wd * wd;
-    v[1] += wf * wf;
-    v[2] += (wd * s0) * (wd * s0);
-    v[3] += (wd * s1) * (wd * s1);
-    v[4] += (wd * s2) * (wd * s2);
-    v[5] += (wf * r) * (wf * r);
-    double en = fabs(s0 * r);
-    v[6] += en;
-    v[7] = fmax(v[7], en);
+      if (eqs[u] < 0) continue;
+      const int t = ts[u];
+      const double wd = wD[t], wf = wF[t];
+      const double s0 = a0[u], s1 = a1[u], s2 = a2[u], r = rr[u];
+      const unsigned long long b0 = absBits(s0), b1 = absBits(s1), b2 = absBits(s2), br = absBits(r);
+      bad |= b0 > badBits || br > badBits;
+      v2 += (wd * s0) * (wd * s0);
+      v3 += (wd * s1) * (wd * s1);
+      v4 += (wd * s2) * (wd * s2);
+      v5 += (wf * r) * (wf * r);
+      const double en = fabs(s0 * r);
+      v6 += en;
+      mx[0] = umax64(mx[0], absBits(en));
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      if (q != t) continue;
-      v[8 + q] = fmax(v[8 + q], fabs(s0));
-      v[11 + q] = fmax(v[11 + q], fabs(s1));
-      v[14 + q] = fmax(v[14 + q], fabs(s2));
-      v[17 + q] = fmax(v[17 + q], fabs(r));
-    }
+      for (int q = 0; q < 3; ++q) {
+        if (q != t) continue;
+        mx[1 + q] = umax64(mx[1 + q], b0);
+        mx[4 + q] = umax64(mx[4 + q], b1);
+        mx[7 + q] = umax64(mx[7 + q], b2);
+        mx[10 + q] = umax64(mx[10 + q], br);
+      }
     }
   }
   // warp tree (fixed pattern), then warps in order
 #pragma unroll
-  for (int k = 0; k < NPART; ++k) {
-    double x = v[k];
+  for (int o = 16; o > 0; o >>= 1) {
+    v2 += __shfl_down_sync(0xffffffffu, v2, o);
+    v3 += __shfl_down_sync(0xffffffffu, v3, o);
+    v4 += __shfl_down_sync(0xffffffffu, v4, o);
+    v5 += __shfl_down_sync(0xffffffffu, v5, o);
+    v6 += __shfl_down_sync(0xffffffffu, v6, o);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double y = __shfl_down_sync(0xffffffffu, x, o);
-      x = (k <= 6) ? x + y : fmax(x, y);
-    }
-    v[k] = x;
+    for (int k = 0; k < 13; ++k) mx[k] = umax64(mx[k], __shfl_down_sync(0xffffffffu, mx[k], o));
   }
+  bad = __any_sync(0xffffffffu, bad);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0)
+  if (lane == 0) {
+    sh[w][0] = 0.0;
+    sh[w][1] = 0.0;
+    sh[w][2] = v2;
+    sh[w][3] = v3;
+    sh[w][4] = v4;
+    sh[w][5] = v5;
+    sh[w][6] = v6;
 #pragma unroll
-    for (int k = 0; k < NPART; ++k) sh[w][k] = v[k];
+    for (int k = 0; k < 13; ++k) sh[w][7 + k] = __longlong_as_double((long long)mx[k]);
+    sh[w][20] = bad ? 1.0 : 0.0;
+  }
   __syncthreads();
   if (threadIdx.x < NPART) {
     const int k = threadIdx.x;
@@ -1016,6 +1044,8 @@ __global__ void kControl(DevData d) {
   for (int k = 0; k < NPART; ++k) v[k] = __shfl_sync(0xffffffffu, acc, k);
   if (lane != 0) return;
   double* nv = d.m.normVal + 18 * m;
+  v[0] = d.m.sumWd2[m];
+  v[1] = d.m.sumWf2[m];
   nv[0] = v[0] > 0 ? sqrt(v[2] / v[0]) : 0.0;
   nv[4] = v[0] > 0 ? sqrt(v[3] / v[0]) : 0.0;
   nv[8] = v[0] > 0 ? sqrt(v[4] / v[0]) : 0.0;

@@ -115,7 +115,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   auto iv = [&](std::vector<int>& v) { v.assign(nm, 0); };
   std::vector<int> triOff(nm), ntriV(nm), dofOff(nm), ndofV(nm), eqOff(nm), neqV(nm), elOff(nm), nelV(nm);
   std::vector<double> tStart(nm), tEnd(nm), dt(nm), minInc(nm), alpha(nm), beta(nm), gamma(nm), wD(3 * nm),
-      wF(3 * nm), grav(3 * nm), tolV(18 * nm), scaleN(3 * nm, -1.0), equTol(nm), equLim(nm), tQs(nm);
+      wF(3 * nm), grav(3 * nm), tolV(18 * nm), scaleN(3 * nm, -1.0), equTol(nm), equLim(nm), tQs(nm),
+      sumWd2(nm, 0.0), sumWf2(nm, 0.0);
   std::vector<int> tolC(18 * nm), maxIt(nm), minIt(nm), fixedIt(nm), nUpdat(nm), maxSeq(nm), staticMode(nm),
       staticDone(nm);
   std::vector<long long> stepLimit(nm, LLONG_MAX);
@@ -135,6 +136,13 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     staticMode[k] = (eqLim > 0.0 && h.neq > 0) ? (eqTol > 0.0 ? 2 : 1) : 0;
     staticDone[k] = staticMode[k] == 0 ? 1 : 0;
     tQs[k] = c.tQStatic;
+    // the norms' weight sums over the free DOFs (constant), in DOF order
+    for (int i = 0; i < h.ndof; ++i)
+      if (h.meqn[i] >= 0) {
+        const int t = h.dofType[i] - 1;
+        sumWd2[k] += c.wDisp[t] * c.wDisp[t];
+        sumWf2[k] += c.wForce[t] * c.wForce[t];
+      }
   }
 #define UP_I(field, vec) if (!(M.field = alloc<int>(nm)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
 #define UP_D(field, vec, n) if (!(M.field = alloc<double>(n)) || put(M.field, vec, stream_) != cudaSuccess) { err = "alloc " #field; return -902; }
@@ -144,6 +152,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   UP_D(minInc, minInc, nm); UP_D(alpha, alpha, nm); UP_D(beta, beta, nm); UP_D(gamma, gamma, nm);
   UP_D(scaleN, scaleN, 3 * nm); UP_D(wDisp, wD, 3 * nm); UP_D(wForce, wF, 3 * nm); UP_D(gravity, grav, 3 * nm);
   UP_D(tolVal, tolV, 18 * nm); UP_D(equTol, equTol, nm); UP_D(equLim, equLim, nm); UP_D(tQs, tQs, nm);
+  UP_D(sumWd2, sumWd2, nm); UP_D(sumWf2, sumWf2, nm);
   if (!(M.tolCode = alloc<int>(18 * nm)) || put(M.tolCode, tolC, stream_) != cudaSuccess) { err = "alloc tolCode"; return -902; }
   UP_I(maxIt, maxIt); UP_I(minIt, minIt); UP_I(fixedIt, fixedIt); UP_I(nUpdat, nUpdat); UP_I(maxSeq, maxSeq);
   UP_I(staticMode, staticMode); UP_I(staticDone, staticDone);

@@ -37,6 +37,7 @@ struct DevModels {
   double *gravity;  // 3 per model
   double *wDisp, *wForce;  // 3 per model
   double *tolVal, *normVal;  // 18 per model
+  double *sumWd2, *sumWf2;   // sums of the squared displacement / force weights over the free DOFs
   int *tolCode;             // 18 per model
   int *maxIt, *minIt, *fixedIt, *nUpdat, *maxSeq;
   int *state, *flags, *status, *iter, *nSeqNoUpd, *negPiv;
