@@ -580,7 +580,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       if (parent[f] > f) pathLen[f] = pathLen[parent[f]] + 1;
       else if (parent[f] >= 0) { err = "assembly tree not in post-order"; return -907; }
     }
-    // leaves with the longest paths first: the cascades' critical paths (the
+    // tasks with the longest paths first: the cascades' critical paths (the
     // deep trees of the large models) start in the first wave of warps
     std::vector<int> leaves;
     for (int f = 0; f < nfr; ++f)
@@ -589,6 +589,46 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     int* dLeaves = nullptr;
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
+    pplan_.nLeaves = (int)leaves.size();
+    // forward-elimination tasks: fronts whose children are all leaves become
+    // groups (one warp eliminates the children and the front, passing the
+    // update vectors in shared memory) when every front of the group takes the fast
+    // forward elimination (at most 64 rows and 64 gathered child rows, its L
+    // block within the staging capacity); other leaves are tasks of their own
+    pplan_.maxRow = maxRowAll;
+    pplan_.maxNpiv = 1;
+    for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
+    const long long capL = stagingCapacity(pplan_, opt_.fp32Factor ? sizeof(float) : sizeof(double));
+    auto fastFront = [&](int f) { return nrow[f] <= 64 && (long long)nrow[f] * npiv[f] <= capL; };
+    std::vector<char> inGroup(nfr, 0), isHead(nfr, 0);
+    for (int f = 0; f < nfr; ++f) {
+      if (nchild[f] == 0 || nchild[f] > 8 || !fastFront(f)) continue;
+      bool ok = true;
+      int ncg = 0;
+      for (int c = 0; c < nchild[f] && ok; ++c) {
+        const int ch = childList[childOffV[f] + c];
+        ok = nchild[ch] == 0 && fastFront(ch);
+        ncg += nrow[ch] - npiv[ch];
+      }
+      if (!ok || ncg > 64) continue;
+      isHead[f] = 1;
+      for (int c = 0; c < nchild[f]; ++c) inGroup[childList[childOffV[f] + c]] = 1;
+    }
+    std::vector<int> tasks, taskLen;
+    for (int f = 0; f < nfr; ++f) {
+      if (isHead[f]) { tasks.push_back(f | (1 << 30)); taskLen.push_back(pathLen[f] + 1); }
+      else if (nchild[f] == 0 && !inGroup[f]) { tasks.push_back(f); taskLen.push_back(pathLen[f]); }
+    }
+    if (nfr >= (1 << 30)) { err = "too many fronts for the task encoding"; return -910; }
+    std::vector<int> order(tasks.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return taskLen[a] > taskLen[b]; });
+    std::vector<int> sortedTasks(tasks.size());
+    for (size_t k = 0; k < order.size(); ++k) sortedTasks[k] = tasks[order[k]];
+    int* dTasks = nullptr;
+    UPV(dTasks, int, sortedTasks);
+    pplan_.tasks = dTasks;
+    pplan_.nTasks = (int)sortedTasks.size();
     // roots and leaf counts per model (the backward queue's initial slots and total)
     std::vector<int> rootOff(nm + 1, 0), roots, leafCnt(nm, 0);
     for (int f = 0; f < nfr; ++f) {
@@ -609,10 +649,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     pplan_.modelRootOff = dRootOff;
     pplan_.modelRoots = dRoots;
     pplan_.modelLeafCnt = dLeafCnt;
-    pplan_.nLeaves = (int)leaves.size();
-    pplan_.maxRow = maxRowAll;
-    pplan_.maxNpiv = 1;
-    for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
     pplan_.cntFactor = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.cntForward = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.bwQueue = alloc<int>(std::max<size_t>(leaves.size(), 1));

@@ -81,9 +81,11 @@ __device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int
 // children's packed update matrices are contiguous per front and loaded
 // kFrontBatch per lane before use; the rank-1 updates run one row per lane.
 constexpr int kFrontBatch = 4;
+// Uout: the front's packed update matrix (its place in the parent's
+// segment); segIn: the front's own children segment
 template <typename T>
 __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* asmVal, T* Lbase,
-                               T* Ubase, double tolFact, int lane) {
+                               T* Uout, const T* segIn, double tolFact, int lane) {
   const int m = d.fModel[f];
   const int nr = d.fNrow[f], np = d.fNpiv[f];
   const int64_t ao = d.fAsmOff[f], so = d.fSegOff[f];
@@ -114,7 +116,7 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
     for (int u = 0; u < kFrontBatch; ++u) {
       const int k = k0 + 32 * u + lane;
       pc[u] = k < ns ? __ldg(d.segPos + so + k) : -1;
-      val[u] = k < ns ? __ldcg(Ubase + so + k) : T(0);
+      val[u] = k < ns ? __ldcg(segIn + k) : T(0);
     }
     for (int c = 0; c < nch; ++c) {
 #pragma unroll
@@ -125,8 +127,7 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
   }
   int neg = 0;
   bool sing = false;
-  // the update matrix goes packed into the parent's segment
-  factorBlocked<T>(F, lcol, diag0, nr, np, lane, tolFact, neg, sing, Ubase + d.fUOff[f]);
+  factorBlocked<T>(F, lcol, diag0, nr, np, lane, tolFact, neg, sing, Uout);
   T* Lout = Lbase + d.fLOff[f];
   for (int k = lane; k < nr * np; k += 32) Lout[k] = F[k];
   if (lane == 0) {
@@ -199,9 +200,13 @@ __device__ void forwardOneFront(const DevData& d, int f, T* v, T* Ls, int capL, 
 // (asynchronous copies), row list and child gather list together, then the
 // right-hand side and the children's update values together.
 
+// Wout: where the front's update vector goes; Win: the children's update
+// vectors concatenated in child order in shared memory (their gather list
+// order), or null to read them from W
 template <typename T>
 __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase,
-                                    const double* rhs, T* X, T* W, int lane, const T* Lres) {
+                                    const double* rhs, T* X, const T* W, int lane, const T* Lres, T* Wout,
+                                    const T* Win = nullptr) {
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
   const int cg0 = d.cgOff[f], ncg = d.cgOff[f + 1] - cg0, nch = d.fNchild[f];
   const int cnt = nr * np;
@@ -226,7 +231,7 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     b[u] = row[u] >= 0 ? rhs[row[u]] : 0.0;
-    wv[u] = src[u] >= 0 ? __ldcg(W + src[u]) : T(0);
+    wv[u] = src[u] < 0 ? T(0) : Win ? Win[lane + 32 * u] : __ldcg(W + src[u]);
   }
   if (!Lres) copyAsyncWait();
   const T* L = Lres ? Lres : Ls;
@@ -248,8 +253,7 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
     for (int i = k + 1 + lane; i < nr; i += 32) v[i] -= L[i + (size_t)nr * k] * yk;
     __syncwarp();
   }
-  T* wo = W + d.fWOff[f];
-  for (int a = lane; a < nu; a += 32) wo[a] = v[np + a];
+  for (int a = lane; a < nu; a += 32) Wout[a] = v[np + a];
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     const int r = lane + 32 * u;
@@ -285,6 +289,16 @@ __device__ inline int climb(const DevData& d, int f, int* cnt, int lane) {
 // the current one is processed, so the request's latency is hidden.
 __device__ inline int requestLeaf(int* next, int lane) { return lane == 0 ? atomicAdd(next, 1) : 0; }
 
+// Forward-elimination tasks are single leaves or groups: a group is a front
+// whose children are all leaves (kGroupBit set in the task), eliminated by one
+// warp -- the children first, their update vectors kept in shared memory, then
+// the front itself -- so that inside a group nothing goes through global
+// memory or a counter.  After a task the warp climbs as from a leaf.  (The
+// factorisation keeps one task per leaf: there the leaves are the most
+// expensive fronts, and factoring siblings one after the other lengthens the
+// critical path more than the saved climbs shorten it.)
+constexpr int kGroupBit = 1 << 30;
+
 // factorisation (models with a tangent update) fused with the forward
 // elimination of the first solve (all active models): one climb per front, and
 // the forward elimination reads L from the front still in shared memory
@@ -309,11 +323,12 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
     while ((fl & FL_ACTIVE) && f >= 0) {
       const T* Lres = nullptr;
       if (factor) {
-        factorOneFront<T>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase, tolFact, lane);
+        factorOneFront<T>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase + d.fUOff[f], Ubase + d.fSegOff[f], tolFact,
+                          lane);
         __syncwarp();
         Lres = F;
       }
-      if (!forwardOneFrontFast<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres))
+      if (!forwardOneFrontFast<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres, Wv + d.fWOff[f]))
         forwardOneFront<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres);
       f = climb(d, f, cnt, lane);
     }
@@ -322,20 +337,35 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
 }
 
 template <typename T>
-__global__ void kForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow, int capL,
+__global__ void kForwardCascade(DevData d, const int* __restrict__ tasks, int nTasks, int maxRow, int capL,
                                 const T* Lbase, const double* rhs, T* X, T* W, int* cnt) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* v = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
+  T* v = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL + 64);
   T* Ls = v + maxRow;
+  T* wsm = Ls + capL;
   int* const next = cnt + d.nfrontTot;
   int idx = __shfl_sync(0xffffffffu, requestLeaf(next, lane), 0);
-  while (idx < nLeaves) {
+  while (idx < nTasks) {
     const int pending = requestLeaf(next, lane);
-    int f = leaves[idx];
+    const int task = tasks[idx];
+    int f = task & ~kGroupBit;
     const bool active = d.m.flags[d.fModel[f]] & FL_ACTIVE;
+    if (active && (task & kGroupBit)) {
+      const int nch = d.fNchild[f];
+      const int* ch = d.childList + d.fChildOff[f];
+      int wo = 0;
+      for (int c = 0; c < nch; ++c) {
+        const int cf = ch[c];
+        forwardOneFrontFast<T>(d, cf, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, wsm + wo);
+        wo += d.fNrow[cf] - d.fNpiv[cf];
+        __syncwarp();
+      }
+      forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + d.fWOff[f], wsm);
+      f = climb(d, f, cnt, lane);
+    }
     while (active && f >= 0) {
-      if (!forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr))
+      if (!forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + d.fWOff[f]))
         forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
       f = climb(d, f, cnt, lane);
     }
@@ -517,23 +547,23 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
 }
 
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s) {
-  if (p.nLeaves <= 0) return;
+  if (p.nTasks <= 0) return;
   const int wpb = 8;
   cudaMemsetAsync(p.cntForward, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
-    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
+    const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(float);
     allowBigSmem(kForwardCascade<float>, sm);
-    const int blocks = occupancyBlocks(kForwardCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, d.L32, rhs,
-                                                       d.x32, d.w32, p.cntForward);
+    const int blocks = occupancyBlocks(kForwardCascade<float>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
+    kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L32, rhs, d.x32,
+                                                       d.w32, p.cntForward);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
-    const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
+    const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(double);
     allowBigSmem(kForwardCascade<double>, sm);
-    const int blocks = occupancyBlocks(kForwardCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, capL, d.L64, rhs,
-                                                         d.x64, d.w64, p.cntForward);
+    const int blocks = occupancyBlocks(kForwardCascade<double>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
+    kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L64, rhs, d.x64,
+                                                         d.w64, p.cntForward);
   }
 }
 

@@ -37,8 +37,13 @@ void launchStaticFinish(const DevData& d, cudaStream_t s);
 
 // --- front_cascade.cu: one launch per phase over all fronts of all models ----
 struct PersistentPlan {
-  const int* leaves;  // fronts without children, longest root path first
+  const int* leaves;  // fronts without children, longest root path first (factorisation)
   int nLeaves;
+  // forward-elimination tasks, longest root path first: a leaf, or a front
+  // whose children are all leaves with bit 30 set (a group, eliminated by one
+  // warp)
+  const int* tasks;
+  int nTasks;
   int maxRow;         // largest front of the batch (rows)
   int maxNpiv;        // largest pivot block of the batch
   int maxAsm;         // largest number of original entries of one front
@@ -50,6 +55,8 @@ struct PersistentPlan {
   const int *modelRootOff, *modelRoots, *modelLeafCnt;
   int *bwQueue, *bwCtr;
 };
+// values of one front's L block the solve kernels stage in shared memory
+int stagingCapacity(const PersistentPlan& p, size_t elemBytes);
 // factorisation of the models with a tangent update fused with the forward
 // elimination of rhs for every active model (first solve of an iteration)
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
