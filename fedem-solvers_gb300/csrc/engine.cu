@@ -629,11 +629,24 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(dTasks, int, sortedTasks);
     pplan_.tasks = dTasks;
     pplan_.nTasks = (int)sortedTasks.size();
-    // roots and leaf counts per model (the backward queue's initial slots and total)
+    // backward queue: fronts whose children are all leaves solve them inline;
+    // roots and chain counts per model (the queue's initial slots and total):
+    // a chain ends at a leaf not solved inline or at an inline front
+    std::vector<unsigned char> bwInline(nfr, 0);
+    for (int f = 0; f < nfr; ++f) {
+      bool all = nchild[f] > 0;
+      for (int c = 0; c < nchild[f] && all; ++c) all = nchild[childList[childOffV[f] + c]] == 0;
+      bwInline[f] = all ? 1 : 0;
+    }
     std::vector<int> rootOff(nm + 1, 0), roots, leafCnt(nm, 0);
     for (int f = 0; f < nfr; ++f) {
       if (parent[f] < 0) ++rootOff[fmodel[f] + 1];
-      if (nchild[f] == 0) ++leafCnt[fmodel[f]];
+      if (bwInline[f] || (nchild[f] == 0 && !(parent[f] >= 0 && bwInline[parent[f]]))) ++leafCnt[fmodel[f]];
+    }
+    {
+      unsigned char* dInline = nullptr;
+      UPV(dInline, unsigned char, bwInline);
+      pplan_.bwInline = dInline;
     }
     for (int m = 0; m < nm; ++m) rootOff[m + 1] += rootOff[m];
     roots.resize(rootOff[nm]);
@@ -648,7 +661,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(dLeafCnt, int, leafCnt);
     pplan_.modelRootOff = dRootOff;
     pplan_.modelRoots = dRoots;
-    pplan_.modelLeafCnt = dLeafCnt;
+    pplan_.modelSlotCnt = dLeafCnt;
     pplan_.cntFactor = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.cntForward = alloc<int>(nfr + 1);  // + the leaf counter
     pplan_.bwQueue = alloc<int>(std::max<size_t>(leaves.size(), 1));

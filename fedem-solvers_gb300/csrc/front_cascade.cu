@@ -418,27 +418,29 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
 // the first queue slots and sets the slot total to their number of leaves;
 // a warp takes the next slot, waits until a front is stored there, solves it
 // and goes on with its first child, storing the other children in fresh
-// slots, until it reaches a leaf.  Every such chain ends at a distinct leaf,
-// so the slots are exactly the leaves of the active models: a warp whose slot
-// number reaches the total is done.  A front is stored only after its parent
+// slots, until it reaches a leaf; a front whose children are all leaves
+// (bwInline) has them solved by the same warp, one after the other, which ends
+// the chain.  Every chain ends at a distinct leaf or such front, so the slots
+// are exactly the chains of the active models (their number per model is
+// slotCnt): a warp whose slot number reaches the total is done.  A front is stored only after its parent
 // is solved (fence, then the slot write; the taker fences after reading it).
 // A waiting warp holds no front, and every stored slot below the one it waits
 // for is held by a running warp that solves without waiting, so each wait
 // ends; it is still bounded and sets errFlag when it runs out.
 // ctr: [0] next slot to take, [1] next free slot, [2] slot total.
 __global__ void kBackwardPrep(DevData d, const int* __restrict__ rootOff, const int* __restrict__ roots,
-                              const int* __restrict__ leafCnt, int* queue, int* ctr) {
+                              const int* __restrict__ slotCnt, int* queue, int* ctr) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= d.m.n || !(d.m.flags[m] & FL_ACTIVE)) return;
   const int r0 = rootOff[m], nr = rootOff[m + 1] - r0;
   const int base = atomicAdd(ctr + 1, nr);
   for (int q = 0; q < nr; ++q) queue[base + q] = roots[r0 + q];
-  atomicAdd(ctr + 2, leafCnt[m]);
+  atomicAdd(ctr + 2, slotCnt[m]);
 }
 
 template <typename T>
 __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
-                               int* errFlag, int acc, int finalize) {
+                               const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
@@ -472,10 +474,18 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
       int next = -1;
       if (nch > 0) {
         const int* ch = d.childList + d.fChildOff[f];
-        next = ch[0];
-        if (lane == 0 && nch > 1) {
-          const int base = atomicAdd(ctr + 1, nch - 1);
-          for (int q = 1; q < nch; ++q) atomicExch(queue + base + q - 1, ch[q]);
+        if (bwInline[f]) {
+          // children that are all leaves: solved here, one after the other
+          for (int c = 0; c < nch; ++c) {
+            backwardOneFront<T>(d, ch[c], xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
+            __syncwarp();
+          }
+        } else {
+          next = ch[0];
+          if (lane == 0 && nch > 1) {
+            const int base = atomicAdd(ctr + 1, nch - 1);
+            for (int q = 1; q < nch; ++q) atomicExch(queue + base + q - 1, ch[q]);
+          }
         }
       }
       __syncwarp();
@@ -574,7 +584,7 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
   const int wpb = 8;
   cudaMemsetAsync(p.bwCtr, 0, sizeof(int) * 3, s);
   cudaMemsetAsync(p.bwQueue, 0xff, sizeof(int) * (size_t)p.nLeaves, s);
-  kBackwardPrep<<<(d.m.n + 127) / 128, 128, 0, s>>>(d, p.modelRootOff, p.modelRoots, p.modelLeafCnt, p.bwQueue,
+  kBackwardPrep<<<(d.m.n + 127) / 128, 128, 0, s>>>(d, p.modelRootOff, p.modelRoots, p.modelSlotCnt, p.bwQueue,
                                                     p.bwCtr);
   const int needed = (p.nLeaves + wpb - 1) / wpb;
   if (fp32) {
@@ -583,14 +593,14 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
     allowBigSmem(kBackwardQueue<float>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<float>, 32 * wpb, sm, needed);
     kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, p.bwQueue, p.bwCtr,
-                                                      p.errFlag, acc, fin);
+                                                      p.bwInline, p.errFlag, acc, fin);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
     allowBigSmem(kBackwardQueue<double>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<double>, 32 * wpb, sm, needed);
     kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, p.bwQueue, p.bwCtr,
-                                                        p.errFlag, acc, fin);
+                                                        p.bwInline, p.errFlag, acc, fin);
   }
 }
 

@@ -51,8 +51,10 @@ struct PersistentPlan {
   // per-front counters, each followed by the launch's leaf counter
   int *cntFactor, *cntForward, *errFlag;
   // backward work queue: each model's roots (modelRootOff, modelRoots) and
-  // number of leaves, the queue (nLeaves slots) and its counters (3)
-  const int *modelRootOff, *modelRoots, *modelLeafCnt;
+  // number of chains (slots), the fronts whose leaf children are solved inline,
+  // the queue (at most nLeaves slots) and its counters (3)
+  const int *modelRootOff, *modelRoots, *modelSlotCnt;
+  const unsigned char* bwInline;
   int *bwQueue, *bwCtr;
 };
 // values of one front's L block the solve kernels stage in shared memory
