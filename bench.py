@@ -38,9 +38,11 @@ UNIT = "Newton steps/s"
 # algorithmic bytes of the element pass per beam element and launch: K and M
 # (2 x 1152), frames 384, triads 192, velocities 192, fg 288 in; writes 576 out
 ELEM_BYTES = 4040
-# DRAM bytes of one forward-elimination launch on this workload (256 models),
-# read + write, from the ncu capture of kForwardCascade<float>
-FORWARD_TRAFFIC_256 = 150.8e6
+# DRAM bytes (read + write) of one launch on this workload (256 models), from
+# ncu captures of kForwardCascade<float> and of kFactorForwardCascade<float>
+# in an iteration where every model factors (profiles/)
+FORWARD_TRAFFIC_256 = 153.5e6
+FACTOR_TRAFFIC_256 = 294.7e6
 
 
 def forward_bytes(models, elem_bytes):
@@ -332,6 +334,8 @@ def main():
     value = iters_tot / dev_s_max
     nsamp, ms3, el_s = b.phase_timings()
     final_mixed = b.all_triads().copy()
+    # the dominant kernel timed alone (every model factoring), after the timed runs
+    fac_ms, fac_bytes = b.time_factor(reps=10) if mixed and not args.timed_only else (0.0, 0.0)
     b.close()
 
     # ---- e2e through the C ABI from host buffers ------------------------------------
@@ -400,18 +404,32 @@ def main():
                    "frac": achieved / hbm_peak, "traffic": None,
                    "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
                    "bytes_per_element": ELEM_BYTES, "samples": nsamp}
+    roof_fwd = None
     if nsamp > 0 and ms3[3] > 0:
-        # the dominant kernel: one forward elimination of the refinement solve
+        # one forward elimination of the refinement solve (sampled inside the run)
         fb = forward_bytes(mods, 4)
         t_fwd = ms3[3] * 1e-3 / nsamp
         achieved = fb / t_fwd / 1e9
         traffic = FORWARD_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
-        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic, "kernel": "kForwardCascade<float> (forward elimination, all fronts)",
-                "algorithmic_bytes_per_launch": fb, "launch_ms": t_fwd * 1e3, "peak_source": peak_kind,
-                "note": "latency-bound: the launch time is set by the dependency chains of the deepest "
-                        "assembly trees, not by bytes",
-                "samples": nsamp}
+        roof_fwd = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "traffic": traffic,
+                    "kernel": "kForwardCascade<float> (forward elimination, all fronts)",
+                    "algorithmic_bytes_per_launch": fb, "launch_ms": t_fwd * 1e3, "peak_source": peak_kind,
+                    "samples": nsamp}
+    if fac_ms > 0:
+        # the dominant kernel: the factorisation fused with the first forward
+        # elimination, every model factoring, timed alone on the engine stream
+        achieved = fac_bytes / (fac_ms * 1e-3) / 1e9
+        traffic = FACTOR_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel": "kFactorForwardCascade<float> (LDL^T of every front + first forward elimination)",
+                "algorithmic_bytes_per_launch": fac_bytes, "launch_ms": fac_ms, "peak_source": peak_kind,
+                "note": "latency-bound: the launch time is set by the dependency chains of the assembly "
+                        "trees and each front's dependent memory round trips, not by bytes",
+                "timing": "10 launches after the timed runs, CUDA events on the engine stream"}
+    elif roof_fwd is not None:
+        roof = roof_fwd
     elif roof_el is not None:
         roof = roof_el
     phases = None
@@ -436,7 +454,7 @@ def main():
                 "gpu_launches": kernels * batched, "kernels_per_batched_iteration": kernels,
                 "batched_iterations": batched, "models_failed": failed,
                 "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof,
-                "roofline_elements": roof_el, "phase_ms_per_iteration": phases}
+                "roofline_elements": roof_el, "roofline_forward": roof_fwd, "phase_ms_per_iteration": phases}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

@@ -616,6 +616,11 @@ long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems,
   return n;
 }
 
+int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2) {
+  if (!b || !out2 || reps < 1) return fail(-1, "bad argument");
+  return b->engine.timeFactor(reps, out2, out2 + 1);
+}
+
 int fgpu_server_create(double budget, int mixed, int sweeps, int maxModels, int minBatch, double maxWait,
                        fgpu_server** out) {
   if (!out) return fail(-1, "null output handle");

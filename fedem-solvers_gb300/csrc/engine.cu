@@ -527,6 +527,26 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       pplan_.maxSeg = std::max(pplan_.maxSeg, segLen[f]);
       pplan_.maxAsm = std::max(pplan_.maxAsm, nasmv[f]);
     }
+    // algorithmic bytes of the factorisation fused with the first forward
+    // elimination, per front (E: factor precision): original entries and their
+    // positions, children's update matrices and positions in, L and the packed
+    // update matrix out; pivot rows' indices and right-hand side (FP64) in,
+    // children's update vectors with their gather entries in, pivot solution
+    // and update vector out
+    {
+      const double E = opt_.fp32Factor ? 4.0 : 8.0;
+      factorBytes_ = 0.0;
+      for (int f = 0; f < nfr; ++f) {
+        const double nr = nrow[f], np = npiv[f], nuf = nr - np;
+        double ncg = 0.0;
+        for (int c = 0; c < nchild[f]; ++c) {
+          const int ch = childList[childOffV[f] + c];
+          ncg += nrow[ch] - npiv[ch];
+        }
+        factorBytes_ += nasmv[f] * (4.0 + E) + segLen[f] * (4.0 + E) + E * nr * np + E * nuf * (nuf + 1.0) / 2.0 +
+                        np * (4.0 + 8.0 + E) + ncg * (8.0 + E) + E * nuf;
+      }
+    }
     UPV(d_.fSegOff, int64_t, segOff); UPV(d_.fSegLen, int, segLen); UPV(d_.segPos, int, segPos);
     {
       std::vector<int> slotAsm(nslot, -1);
@@ -746,6 +766,35 @@ void Engine::invalidateNewtonScales() {
   scaleSentinel_.assign(3 * (size_t)d_.m.n, -1.0e300);
   cudaMemcpyAsync(d_.m.scaleN, scaleSentinel_.data(), sizeof(double) * scaleSentinel_.size(),
                   cudaMemcpyHostToDevice, stream_);
+}
+
+int Engine::timeFactor(int reps, double* msPerLaunch, double* bytes) {
+  const int nm = d_.m.n;
+  std::vector<int> flags(nm), status(nm), neg(nm), all(nm, FL_ACTIVE | FL_TANGENT);
+  cudaMemcpyAsync(flags.data(), d_.m.flags, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(status.data(), d_.m.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(neg.data(), d_.m.negPiv, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  cudaMemcpyAsync(d_.m.flags, all.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  enqueueFactor(stream_);  // warm-up
+  cudaEventRecord(e0, stream_);
+  for (int k = 0; k < reps; ++k) enqueueFactor(stream_);
+  cudaEventRecord(e1, stream_);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemcpyAsync(d_.m.flags, flags.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.status, status.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.negPiv, neg.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -946;
+  if (msPerLaunch) *msPerLaunch = reps > 0 ? ms / reps : 0.0;
+  if (bytes) *bytes = factorBytes_;
+  return 0;
 }
 
 long long Engine::phaseTimings(double* ms4, long long* elems) {

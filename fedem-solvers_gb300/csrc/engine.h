@@ -100,6 +100,11 @@ class Engine {
   // elimination of the second solve (mixed-precision batches; else 0).
   // Returns samples; ms[4] = summed milliseconds, elems = summed active elements.
   long long phaseTimings(double* ms4, long long* activeElems);
+  // Times `reps` launches of the factorisation fused with the first forward
+  // elimination with every model factoring (CUDA events on the engine stream);
+  // the flags, status and pivot counters are restored afterwards, the factors
+  // and solve vectors are scratch.  *bytes: algorithmic bytes of one launch.
+  int timeFactor(int reps, double* msPerLaunch, double* bytes);
   void resetPhaseTimings();
 
  private:
@@ -132,6 +137,7 @@ class Engine {
   // snapshot of mutable arrays: (device pointer, bytes) and the backup buffer
   std::vector<std::pair<void*, size_t>> mutable_;
   std::vector<double> scaleSentinel_;
+  double factorBytes_ = 0.0;  // algorithmic bytes of one factor + first forward launch, all models
   void invalidateNewtonScales();
   void recordPhase(cudaEvent_t ev, cudaStream_t s);
   char* backup_ = nullptr;

@@ -77,6 +77,7 @@ def load_library(path=None):
         "fgpu_batch_snapshot": (c_int, [vp]),
         "fgpu_batch_restore": (c_int, [vp]),
         "fgpu_batch_phase_timings": (c_ll, [vp, P(c_dbl), P(c_ll), c_int]),
+        "fgpu_batch_time_factor": (c_int, [vp, c_int, P(c_dbl)]),
         "fgpu_server_create": (c_int, [c_dbl, c_int, c_int, c_int, c_int, c_dbl, P(vp)]),
         "fgpu_server_destroy": (None, [vp]),
         "fgpu_server_submit": (c_int, [vp, vp, P(c_int)]),

@@ -150,6 +150,14 @@ class Batch:
                                                1 if reset else 0)
         return int(n), ms, int(el.value)
 
+    def time_factor(self, reps=10):
+        """(ms per launch, algorithmic bytes per launch) of the factorisation fused
+        with the first forward elimination, every model factoring."""
+        out = np.zeros(2)
+        if self._lib.fgpu_batch_time_factor(self._h, int(reps), _ptr(out, ctypes.c_double)) != 0:
+            raise FedemException("time_factor failed: " + self._lib.fgpu_last_error().decode())
+        return float(out[0]), float(out[1])
+
     def norms(self, model):
         v = np.zeros(18)
         self._lib.fgpu_batch_get_norms(self._h, model, _ptr(v, ctypes.c_double))

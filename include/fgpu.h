@@ -96,6 +96,13 @@ int fgpu_batch_restore(fgpu_batch* b);
  * sampled iterations.  Returns the number of samples; reset != 0 clears the
  * accumulators afterwards. */
 long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset);
+/* Times reps launches of the factorisation fused with the first forward
+ * elimination with every model factoring (CUDA events on the batch's stream).
+ * out2[0]: milliseconds per launch, out2[1]: algorithmic bytes of one launch.
+ * The factors and solve vectors are scratch afterwards (the models' flags,
+ * status and pivot counts are kept); time it after a run or restore a
+ * snapshot before the next one.  Returns 0, or < 0 on error. */
+int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
 
 /* ---- serving: continuous batching of simulation requests ------------------
  * Requests are admitted into new GPU batches (own stream each) as soon as the
