@@ -122,7 +122,19 @@ __device__ inline void orthonormRot(double* R /* col-major 3x3 */) {
 // ---------------------------------------------------------------------------
 // per-model control at the start of a batched iteration
 // ---------------------------------------------------------------------------
-__global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl) {
+// the roots of model i into every backward queue, and its chain count
+__device__ inline void seedBackward(const BackwardSeed& b, int i) {
+  for (int q = 0; q < b.nq; ++q) {
+    const int r0 = b.rootOff[i], nr = b.rootOff[i + 1] - r0;
+    int* ctr = b.ctr + 4 * q;
+    int* queue = b.queue + (size_t)q * b.stride;
+    const int base = atomicAdd(ctr + 1, nr);
+    for (int k = 0; k < nr; ++k) queue[base + k] = b.roots[r0 + k];
+    atomicAdd(ctr + 2, b.slotCnt[i]);
+  }
+}
+
+__global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl, BackwardSeed bs) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
   int st = m.state[i], fl = 0;
@@ -177,6 +189,7 @@ __global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl) {
   m.flags[i] = fl;
   atomicAdd(activeCount, 1);
   atomicAdd(reinterpret_cast<unsigned long long*>(activeEl), (unsigned long long)m.nel[i]);
+  seedBackward(bs, i);
 }
 
 // predicted velocity/acceleration increments and the actual inertia force
@@ -1116,7 +1129,7 @@ __global__ void kStepEnd(DevData d) {
 // ---------------------------------------------------------------------------
 // static equilibrium iterations
 // ---------------------------------------------------------------------------
-__global__ void kStaticBegin(DevModels m, int* activeCount) {
+__global__ void kStaticBegin(DevModels m, int* activeCount, BackwardSeed bs) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
   if (m.staticDone[i] || m.state[i] == ST_ERROR) { m.flags[i] = 0; return; }
@@ -1128,6 +1141,7 @@ __global__ void kStaticBegin(DevModels m, int* activeCount) {
   }
   m.flags[i] = fl;
   atomicAdd(activeCount, 1);
+  seedBackward(bs, i);
 }
 
 __global__ void kStaticResidual(DevData d) {
@@ -1236,8 +1250,9 @@ __global__ void kStaticFinish(DevModels m) {
 
 }  // namespace
 
-void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, cudaStream_t s) {
-  kBeginStep<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, activeEl);
+void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, const BackwardSeed& seed,
+                     cudaStream_t s) {
+  kBeginStep<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, activeEl, seed);
 }
 void launchPredictDofs(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.neqTot ? d.ndofTot : d.neqTot;
@@ -1286,8 +1301,8 @@ void launchQsRestore(const DevData& d, cudaStream_t s) {
   long long n = std::max<long long>(std::max<long long>(d.ntriTot, d.nelTot), d.ndofTot);
   kQsRestore<<<blocksFor(n), TPB, 0, s>>>(d);
 }
-void launchStaticBegin(const DevData& d, int* activeCount, cudaStream_t s) {
-  kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount);
+void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s) {
+  kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, seed);
 }
 void launchStaticResidual(const DevData& d, cudaStream_t s) {
   if (d.neqTot > 0) kStaticResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);

@@ -679,20 +679,33 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(dRootOff, int, rootOff);
     UPV(dRoots, int, roots);
     UPV(dLeafCnt, int, leafCnt);
-    pplan_.modelRootOff = dRootOff;
-    pplan_.modelRoots = dRoots;
-    pplan_.modelSlotCnt = dLeafCnt;
-    pplan_.cntFactor = alloc<int>(nfr + 1);  // + the leaf counter
-    pplan_.cntForward = alloc<int>(nfr + 1);  // + the leaf counter
-    pplan_.bwQueue = alloc<int>(std::max<size_t>(leaves.size(), 1));
-    pplan_.bwCtr = alloc<int>(3);
+    // iteration counters in one block, zeroed by one memset per iteration:
+    // active models (int) and elements (long long), the backward queues'
+    // counters (4 per solve), the factorisation's per-front counters and one set
+    // per refinement forward elimination (each + its leaf counter)
+    const int nq = std::max(1, opt_.fp32Factor ? opt_.refineSweeps : 1);
+    ctrInts_ = 4 + 4 * (size_t)nq + (size_t)nq * (nfr + 1);
+    ctrBlock_ = alloc<int>(ctrInts_);
+    if (!ctrBlock_) { err = "out of device memory (counters)"; return -906; }
+    dActive_ = ctrBlock_;
+    dActiveEl_ = reinterpret_cast<long long*>(ctrBlock_ + 2);
+    pplan_.bwCtr = ctrBlock_ + 4;
+    pplan_.cntFactor = ctrBlock_ + 4 + 4 * nq;
+    pplan_.cntForward = pplan_.cntFactor + (nfr + 1);
+    pplan_.bwQueue = alloc<int>((size_t)nq * std::max<size_t>(leaves.size(), 1));
+    queueInts_ = (size_t)nq * std::max<size_t>(leaves.size(), 1);
+    seed_.nq = nq;
+    seed_.stride = (int)std::max<size_t>(leaves.size(), 1);
+    seed_.rootOff = dRootOff;
+    seed_.roots = dRoots;
+    seed_.slotCnt = dLeafCnt;
+    seed_.queue = pplan_.bwQueue;
+    seed_.ctr = pplan_.bwCtr;
     pplan_.errFlag = alloc<int>(1);
     d_.errFlag = pplan_.errFlag;
   }
 #undef UPV
   if (allocFailed_) { err = "out of device memory"; return -906; }
-  dActive_ = alloc<int>(1);
-  dActiveEl_ = alloc<long long>(1);
   FG_CHECK(cudaMallocHost(&hActive_, sizeof(int)));
   FG_CHECK(cudaMallocHost(&hStates_, sizeof(int) * (size_t)std::max(nm, 1)));
   FG_CHECK(cudaMallocHost(&hActiveEl_, sizeof(long long)));
@@ -779,9 +792,14 @@ int Engine::timeFactor(int reps, double* msPerLaunch, double* bytes) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  const size_t cntBytes = sizeof(int) * ((size_t)d_.nfrontTot + 1);
+  cudaMemsetAsync(pplan_.cntFactor, 0, cntBytes, stream_);
   enqueueFactor(stream_);  // warm-up
   cudaEventRecord(e0, stream_);
-  for (int k = 0; k < reps; ++k) enqueueFactor(stream_);
+  for (int k = 0; k < reps; ++k) {
+    cudaMemsetAsync(pplan_.cntFactor, 0, cntBytes, stream_);
+    enqueueFactor(stream_);
+  }
   cudaEventRecord(e1, stream_);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -833,18 +851,24 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
     // the first forward elimination ran with the factorisation
     if (sweep > 0) launchRefineResidual(d_, s);
     if (sweep == 1 && timedForward) recordPhase(ev_[5], s);
-    if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, s);
+    if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
     if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
     launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
   }
 }
 
+// the iteration's counters to zero and its backward queue slots to empty (-1):
+// two memsets, before the step-start kernel seeds the queues
+void Engine::resetIterationCounters(cudaStream_t s) {
+  cudaMemsetAsync(ctrBlock_, 0, sizeof(int) * ctrInts_, s);
+  if (queueInts_) cudaMemsetAsync(pplan_.bwQueue, 0xff, sizeof(int) * queueInts_, s);
+}
+
 // first half of a Newton iteration: step start (predictor) or the corrector's
 // right-hand side, and the Newton matrix when the tangent is updated
 void Engine::enqueueAssembly(cudaStream_t s) {
-  cudaMemsetAsync(dActive_, 0, sizeof(int), s);
-  cudaMemsetAsync(dActiveEl_, 0, sizeof(long long), s);
-  launchBeginStep(d_, dActive_, dActiveEl_, s);
+  resetIterationCounters(s);
+  launchBeginStep(d_, dActive_, dActiveEl_, seed_, s);
   launchQsRestore(d_, s);
   launchMotions(d_, s);
   launchLoads(d_, s);
@@ -963,12 +987,12 @@ int Engine::readActive() {
 
 int Engine::initialState(std::string& err) {
   // staticEquilibriumModule.f90:50-437: iterate the models that asked for it
-  launchStaticBegin(d_, dActive_, stream_);
+  launchStaticBegin(d_, dActive_, BackwardSeed{}, stream_);
   launchElements(d_, EM_STATIC_INIT, stream_);
   launchBuildElementNewton(d_, stream_);
   for (int guard = 0; guard < 100000; ++guard) {
-    cudaMemsetAsync(dActive_, 0, sizeof(int), stream_);
-    launchStaticBegin(d_, dActive_, stream_);
+    resetIterationCounters(stream_);
+    launchStaticBegin(d_, dActive_, seed_, stream_);
     if (readActive() == 0) break;
     launchStaticResidual(d_, stream_);
     launchBuildElementNewton(d_, stream_);

@@ -138,6 +138,10 @@ class Engine {
   std::vector<std::pair<void*, size_t>> mutable_;
   std::vector<double> scaleSentinel_;
   double factorBytes_ = 0.0;  // algorithmic bytes of one factor + first forward launch, all models
+  int* ctrBlock_ = nullptr;   // the iteration counters (see upload)
+  size_t ctrInts_ = 0, queueInts_ = 0;
+  BackwardSeed seed_;
+  void resetIterationCounters(cudaStream_t s);
   void invalidateNewtonScales();
   void recordPhase(cudaEvent_t ev, cudaStream_t s);
   char* backup_ = nullptr;

@@ -414,30 +414,20 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
   }
 }
 
-// Top-down work queue.  kBackwardPrep puts the roots of the active models in
-// the first queue slots and sets the slot total to their number of leaves;
-// a warp takes the next slot, waits until a front is stored there, solves it
-// and goes on with its first child, storing the other children in fresh
-// slots, until it reaches a leaf; a front whose children are all leaves
+// Top-down work queue.  The step-start kernel puts the roots of the active
+// models in the first queue slots and sets the slot total to their number of
+// chains; a warp takes the next slot, waits until a front is stored there,
+// solves it and goes on with its first child, storing the other children in
+// fresh slots, until it reaches a leaf; a front whose children are all leaves
 // (bwInline) has them solved by the same warp, one after the other, which ends
 // the chain.  Every chain ends at a distinct leaf or such front, so the slots
-// are exactly the chains of the active models (their number per model is
-// slotCnt): a warp whose slot number reaches the total is done.  A front is stored only after its parent
-// is solved (fence, then the slot write; the taker fences after reading it).
-// A waiting warp holds no front, and every stored slot below the one it waits
+// are exactly the chains of the active models: a warp whose slot number
+// reaches the total is done.  A front is stored only after its parent is
+// solved (fence, then the slot write; the taker fences after reading it).  A
+// waiting warp holds no front, and every stored slot below the one it waits
 // for is held by a running warp that solves without waiting, so each wait
 // ends; it is still bounded and sets errFlag when it runs out.
 // ctr: [0] next slot to take, [1] next free slot, [2] slot total.
-__global__ void kBackwardPrep(DevData d, const int* __restrict__ rootOff, const int* __restrict__ roots,
-                              const int* __restrict__ slotCnt, int* queue, int* ctr) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= d.m.n || !(d.m.flags[m] & FL_ACTIVE)) return;
-  const int r0 = rootOff[m], nr = rootOff[m + 1] - r0;
-  const int base = atomicAdd(ctr + 1, nr);
-  for (int q = 0; q < nr; ++q) queue[base + q] = roots[r0 + q];
-  atomicAdd(ctr + 2, slotCnt[m]);
-}
-
 template <typename T>
 __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
                                const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize) {
@@ -531,7 +521,6 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
   if (p.nLeaves <= 0) return;
   const double tol = 1.0e-12;
   const size_t perWarp = (size_t)p.maxRow * p.maxRow + 3 * p.maxRow;
-  cudaMemsetAsync(p.cntFactor, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
   if (fp32) {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
     const size_t sm = (size_t)wpb * perWarp * sizeof(float);
@@ -556,24 +545,25 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
   return (int)(want < cap ? want : cap);
 }
 
-void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s) {
+void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
+                          cudaStream_t s) {
   if (p.nTasks <= 0) return;
   const int wpb = 8;
-  cudaMemsetAsync(p.cntForward, 0, sizeof(int) * ((size_t)d.nfrontTot + 1), s);
+  int* cnt = p.cntForward + (size_t)(sweep - 1) * ((size_t)d.nfrontTot + 1);
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
     const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(float);
     allowBigSmem(kForwardCascade<float>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<float>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
     kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L32, rhs, d.x32,
-                                                       d.w32, p.cntForward);
+                                                       d.w32, cnt);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(double);
     allowBigSmem(kForwardCascade<double>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<double>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
     kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L64, rhs, d.x64,
-                                                         d.w64, p.cntForward);
+                                                         d.w64, cnt);
   }
 }
 
@@ -582,25 +572,23 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
   const int fin = (fp32 && last) ? 1 : 0;
   if (p.nLeaves <= 0) return;
   const int wpb = 8;
-  cudaMemsetAsync(p.bwCtr, 0, sizeof(int) * 3, s);
-  cudaMemsetAsync(p.bwQueue, 0xff, sizeof(int) * (size_t)p.nLeaves, s);
-  kBackwardPrep<<<(d.m.n + 127) / 128, 128, 0, s>>>(d, p.modelRootOff, p.modelRoots, p.modelSlotCnt, p.bwQueue,
-                                                    p.bwCtr);
+  int* queue = p.bwQueue + (size_t)sweep * p.nLeaves;
+  int* ctr = p.bwCtr + 4 * sweep;
   const int needed = (p.nLeaves + wpb - 1) / wpb;
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
     allowBigSmem(kBackwardQueue<float>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<float>, 32 * wpb, sm, needed);
-    kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, p.bwQueue, p.bwCtr,
-                                                      p.bwInline, p.errFlag, acc, fin);
+    kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, queue, ctr, p.bwInline,
+                                                      p.errFlag, acc, fin);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
     allowBigSmem(kBackwardQueue<double>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<double>, 32 * wpb, sm, needed);
-    kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, p.bwQueue, p.bwCtr,
-                                                        p.bwInline, p.errFlag, acc, fin);
+    kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline,
+                                                        p.errFlag, acc, fin);
   }
 }
 

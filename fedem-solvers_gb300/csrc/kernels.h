@@ -19,7 +19,21 @@ enum ElemMode : int {
 };
 
 // --- element_kernels.cu ----------------------------------------------------
-void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, cudaStream_t s);
+// Seeding of the backward work queues by the step-start kernels: for each
+// solve q of the iteration, queue q receives the roots of the active models
+// and ctr[4 q + 2] their number of chains (ctr[4 q] and ctr[4 q + 1] are the
+// take and fill positions); nq = 0 seeds nothing.
+struct BackwardSeed {
+  int nq = 0;      // queues (solves per iteration)
+  int stride = 0;  // slots per queue
+  const int* rootOff = nullptr;  // per model: its roots in roots[rootOff[m]..rootOff[m+1])
+  const int* roots = nullptr;
+  const int* slotCnt = nullptr;  // per model: its number of chains
+  int* queue = nullptr;
+  int* ctr = nullptr;
+};
+void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, const BackwardSeed& seed,
+                     cudaStream_t s);
 void launchPredictDofs(const DevData& d, cudaStream_t s);
 void launchElements(const DevData& d, int mode, cudaStream_t s);
 void launchResidual(const DevData& d, cudaStream_t s);
@@ -29,7 +43,7 @@ void launchCsrGather(const DevData& d, cudaStream_t s);
 void launchIncrement(const DevData& d, cudaStream_t s);
 void launchNormsControl(const DevData& d, cudaStream_t s);
 // static equilibrium helpers
-void launchStaticBegin(const DevData& d, int* activeCount, cudaStream_t s);
+void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s);
 void launchStaticResidual(const DevData& d, cudaStream_t s);
 void launchStaticNorm(const DevData& d, cudaStream_t s);
 void launchStaticIncrement(const DevData& d, cudaStream_t s);
@@ -48,12 +62,13 @@ struct PersistentPlan {
   int maxNpiv;        // largest pivot block of the batch
   int maxAsm;         // largest number of original entries of one front
   int maxSeg;         // largest children update segment of one front (packed lower values)
-  // per-front counters, each followed by the launch's leaf counter
+  // per-front counters, each followed by the launch's leaf counter: one set for
+  // the factorisation, one per refinement forward elimination (nfrontTot + 1
+  // apart); zeroed with the other iteration counters at the iteration start
   int *cntFactor, *cntForward, *errFlag;
-  // backward work queue: each model's roots (modelRootOff, modelRoots) and
-  // number of chains (slots), the fronts whose leaf children are solved inline,
-  // the queue (at most nLeaves slots) and its counters (3)
-  const int *modelRootOff, *modelRoots, *modelSlotCnt;
+  // backward work queues, one per solve of the iteration (nLeaves slots apart),
+  // and their counters (4 per queue), seeded by the step-start kernels; the
+  // fronts whose leaf children are solved inline
   const unsigned char* bwInline;
   int *bwQueue, *bwCtr;
 };
@@ -64,7 +79,8 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes);
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
                                 cudaStream_t s);
 // forward elimination of the right-hand side rhs (FP64, rounded to the solve precision)
-void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, cudaStream_t s);
+void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
+                          cudaStream_t s);
 // back substitution; stores the solution in del (FP64 solve) or accumulates it in xref
 // (FP32 refinement sweep `sweep`; the last sweep also copies xref to del)
 void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
