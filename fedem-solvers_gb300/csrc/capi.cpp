@@ -105,8 +105,7 @@ extern "C" {
 // ===========================================================================
 
 int solverInit(int argc, char** argv, const char* cfsi, const double* stateData, int ndat,
-               const double* /*gagesData*/, int /*ngda*/, const double* /*extInput*/, int* nxinp) {
-  if (nxinp) *nxinp = 0;
+               const double* /*gagesData*/, int /*ngda*/, const double* extInput, int* nxinp) {
   g_core.reset();
   std::string text;
   if (cfsi) {
@@ -122,6 +121,11 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
   const char* const* cargv = const_cast<const char* const*>(argv);
   int rc = buildModel(text.c_str(), argc, cargv, *s->model, err);
   if (rc) return fail(rc < 0 ? rc : -100 - rc, err);
+  // initial external function values (solverInterface.C:575-576): extInput[0..*nxinp)
+  if (extInput && nxinp && *nxinp > 0) {
+    s->model->extInit.assign(extInput, extInput + std::min(*nxinp, s->model->nExt));
+    s->model->extInit.resize(s->model->nExt, 0.0);
+  }
   EngineOptions opt;
   opt.fp32Factor = hasFlag(argc, argv, "gpuMixed");
   opt.refineSweeps = opt.fp32Factor ? 4 : 1;
@@ -151,9 +155,39 @@ int restartFromState(const double* stateData, const int ndat, const int) {
   return 0;
 }
 
-bool solveWindow(int, int, int, int, const int*, const double*, const double*, double*, int, double*, int* ierr) {
-  if (ierr) *ierr = -1;
-  return false;
+// solverInterface.h:110 (solverInterface.C:858-910) -- nStep steps; before
+// each, the step's time (times, nInc >= nStep) and the external function values
+// 1..nIn (inputs, nIn per step) are applied; after each, the nOut functions
+// fOut are evaluated into outputs (nOut per step); the state is saved into
+// stateData at the end when nDat > 0.  False at the end of the simulation or
+// on error (*ierr != 0).
+bool solveWindow(int nStep, int nInc, int nIn, int nOut, const int* fOut, const double* times,
+                 const double* inputs, double* outputs, int nDat, double* stateData, int* ierr) {
+  int lerr = 0;
+  int& e = ierr ? *ierr : lerr;
+  e = 0;
+  if (!g_core || g_core->ierr) {
+    e = g_core ? g_core->ierr : -1;
+    return false;
+  }
+  if (!times) nInc = 0;
+  if (!inputs) nIn = 0;
+  if (!outputs || !fOut) nOut = 0;
+  if (!stateData) nDat = 0;
+  if (nInc > 0 && nInc < nStep) {
+    e = nInc - nStep;  // too short times array
+    return false;
+  }
+  bool more = true;
+  for (int i = 0; i < nStep && more && e == 0; ++i) {
+    if (nInc > 0 && !setTime(times[i])) e = -1;
+    for (int j = 0; j < nIn; ++j)
+      if (!setExtFunc(1 + j, inputs[(size_t)i * nIn + j])) --e;
+    if (e == 0) more = solveNext(&e);
+    for (int j = 0; j < nOut && e == 0; ++j) outputs[(size_t)i * nOut + j] = evalFunc(fOut[j], nullptr, -1.0, &e);
+  }
+  if (e == 0 && nDat > 0 && !saveState(stateData, nDat)) e = -2;
+  return e == 0 && more;
 }
 
 // solverInterface.h:118 -- doubles needed by saveState
@@ -284,7 +318,12 @@ int solverDone(bool) {
 }
 void solverClose(void) { g_core.reset(); }
 
-bool setExtFunc(int, double) { return false; }
+// solverInterface.h:342 -- value of external function channel funcId (1-based)
+// for the next step; false when the model has no such channel
+bool setExtFunc(int funcId, double value) {
+  if (!g_core) return false;
+  return g_core->engine->setExtValue(0, funcId - 1, value) == 0;
+}
 
 double getTime(bool nextStep, int* ierr) {
   if (!g_core) {
@@ -293,7 +332,7 @@ double getTime(bool nextStep, int* ierr) {
   }
   if (ierr) *ierr = 0;
   double t = g_core->engine->modelTime(0);
-  return nextStep ? t + g_core->model->ctl.tInc : t;
+  return nextStep ? t + g_core->engine->modelDt(0) : t;
 }
 
 // solverInterface.h:355 -- time increment of the next step: nextTime - time
@@ -308,11 +347,47 @@ bool setTime(double nextTime) {
   return g_core->engine->setTimeStep(0, dt < c.minInc ? c.minInc : dt) == 0;
 }
 
-double evalFunc(int, const char*, double, int* ierr) {
-  if (ierr) *ierr = -1;
-  return 0.0;
+// solverInterface.h:383 -- value of the engine with user id uid, or (with a
+// tag) of the first engine with that tag (solverModule.f90:1602-1640:
+// a user id match wins; no match gives zero); x >= 0 without a tag
+// evaluates the engine's function at x instead of its current argument
+double evalFunc(int uid, const char* tag, double x, int* ierr) {
+  int lerr = 0;
+  int& e = ierr ? *ierr : lerr;
+  if (!g_core) {
+    e = -999;  // outside model scope
+    return 0.0;
+  }
+  Singleton& s = *g_core;
+  const HostModel& m = *s.model;
+  const bool hasX = !tag && x >= 0.0;
+  auto value = [&](size_t k) {
+    if (m.engFType[k] == 3) return s.engine->extValue(0, m.engCh[k]);
+    if (m.engFType[k] == 2) return m.engFc[k];
+    const double arg = hasX ? x : (m.engTimeArg[k] ? s.engine->modelTime(0) : 0.0);
+    return m.engFType[k] == 1 ? m.engFc[k] * arg : arg;
+  };
+  bool found = false;
+  double tagValue = 0.0;
+  for (size_t k = 0; k < m.engId.size(); ++k) {
+    if (m.engUserId[k] == uid) return value(k);
+    if (tag && !found && m.engTag[k] == tag) {
+      found = true;
+      tagValue = value(k);
+      if (uid <= 0) return tagValue;
+    }
+  }
+  return 0.0;  // no such engine: zero
 }
-int getFuncId(const char*) { return -1; }
+// solverInterface.h:398 -- user id of the first engine with the tag, -1 if none
+int getFuncId(const char* tag) {
+  if (!g_core) return -999;
+  if (!tag) return -1;
+  const HostModel& m = *g_core->model;
+  for (size_t k = 0; k < m.engId.size(); ++k)
+    if (m.engTag[k] == tag) return m.engUserId[k];
+  return -1;
+}
 
 int getEquations(int bid, int* meqn) {
   if (!g_core) return 0;

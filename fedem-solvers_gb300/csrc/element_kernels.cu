@@ -840,7 +840,8 @@ __global__ void kMotions(DevData d) {
   if (k >= d.nmotTot) return;
   const int m = d.motModel[k], fl = d.m.flags[m];
   if (!(fl & FL_PRED)) return;
-  const double D = d.motD0[k] + d.motD1[k] * (d.motEA[k] * d.m.time[m] + d.motEB[k]);
+  const int ch = d.motCh[k];
+  const double D = d.motD0[k] + d.motD1[k] * (ch >= 0 ? d.extVal[ch] : d.motEA[k] * d.m.time[m] + d.motEB[k]);
   d.motCc[k] = (fl & FL_LINEAR) ? D : D - d.motD[k];
   d.motD[k] = D;
 }
@@ -853,7 +854,10 @@ __global__ void kLoads(DevData d) {
   if (!(d.m.flags[m] & FL_PRED)) return;
   const double t = d.m.time[m];
   double q = d.qextBase[eq];
-  for (int j = d.ldPtr[k]; j < d.ldPtr[k + 1]; ++j) q += d.ldF0[j] + d.ldF1[j] * (d.ldEA[j] * t + d.ldEB[j]);
+  for (int j = d.ldPtr[k]; j < d.ldPtr[k + 1]; ++j) {
+    const int ch = d.ldCh[j];
+    q += d.ldF0[j] + d.ldF1[j] * (ch >= 0 ? d.extVal[ch] : d.ldEA[j] * t + d.ldEB[j]);
+  }
   d.qext[eq] = q;
 }
 

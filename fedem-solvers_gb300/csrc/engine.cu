@@ -187,9 +187,24 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     for (int i = 0; i < h.neq; ++i) eqModel.push_back(k);
     qext.insert(qext.end(), h.qext.begin(), h.qext.end());
   }
+  // external function channels of every model (values set by the caller, zero at start)
+  modelExtOff_.assign(nm, 0);
+  int nextTot = 0;
+  for (int k = 0; k < nm; ++k) {
+    modelExtOff_[k] = nextTot;
+    nextTot += models[k]->nExt;
+  }
+  modelExtCnt_.resize(nm);
+  std::vector<double> extInit(std::max(nextTot, 1), 0.0);
+  for (int k = 0; k < nm; ++k) {
+    modelExtCnt_[k] = models[k]->nExt;
+    for (int c = 0; c < (int)models[k]->extInit.size() && c < models[k]->nExt; ++c)
+      extInit[modelExtOff_[k] + c] = models[k]->extInit[c];
+  }
+  auto extAt = [&](int k, int ch) { return ch < (int)models[k]->extInit.size() ? models[k]->extInit[ch] : 0.0; };
   // engine-driven loads: constant part kept, start-time value in qext
   std::vector<double> qextBase = qext, ldF0, ldF1, ldEA, ldEB;
-  std::vector<int> ldEq, ldPtr(1, 0);
+  std::vector<int> ldEq, ldPtr(1, 0), ldCh;
   for (int k = 0; k < nm; ++k) {
     const HostModel& h = *models[k];
     for (size_t q = 0; q < h.ldEq.size(); ++q) {
@@ -198,7 +213,9 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       double v = qextBase[eq];
       for (int j = h.ldPtr[q]; j < h.ldPtr[q + 1]; ++j) {
         ldF0.push_back(h.ldF0[j]); ldF1.push_back(h.ldF1[j]); ldEA.push_back(h.ldEA[j]); ldEB.push_back(h.ldEB[j]);
-        v += h.ldF0[j] + h.ldF1[j] * (h.ldEA[j] * h.ctl.tStart + h.ldEB[j]);
+        const int ch = h.ldCh[j];
+        ldCh.push_back(ch >= 0 ? ch + modelExtOff_[k] : -1);
+        v += h.ldF0[j] + h.ldF1[j] * (ch >= 0 ? extAt(k, ch) : h.ldEA[j] * h.ctl.tStart + h.ldEB[j]);
       }
       qext[eq] = v;
       ldPtr.push_back((int)ldF0.size());
@@ -212,9 +229,12 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   d_.nldTot = (int)ldEq.size();
   UPV(d_.qextBase, double, qextBase); UPV(d_.ldEq, int, ldEq); UPV(d_.ldPtr, int, ldPtr);
   UPV(d_.ldF0, double, ldF0); UPV(d_.ldF1, double, ldF1); UPV(d_.ldEA, double, ldEA); UPV(d_.ldEB, double, ldEB);
+  UPV(d_.ldCh, int, ldCh);
+  d_.nextTot = nextTot;
+  UPV(d_.extVal, double, extInit);
   {
     // prescribed deflections and their predictor right-hand-side terms
-    std::vector<int> motModel, motOff(nm), mrEq, mrMot;
+    std::vector<int> motModel, motOff(nm), mrEq, mrMot, motCh;
     std::vector<double> d0, d1, eA, eB, D0;
     std::vector<int64_t> mrPtr(1, 0), mrSrc;
     bool anyLinearQs = false;
@@ -224,8 +244,10 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       for (size_t j = 0; j < h.motD0.size(); ++j) {
         motModel.push_back(k);
         d0.push_back(h.motD0[j]); d1.push_back(h.motD1[j]); eA.push_back(h.motEA[j]); eB.push_back(h.motEB[j]);
+        const int ch = h.motCh[j];
+        motCh.push_back(ch >= 0 ? ch + modelExtOff_[k] : -1);
         // start-time value (updatePrescribedMotionsB, motionRoutinesModule.f90:213-245)
-        D0.push_back(h.motD0[j] + h.motD1[j] * (h.motEA[j] * h.ctl.tStart + h.motEB[j]));
+        D0.push_back(h.motD0[j] + h.motD1[j] * (ch >= 0 ? extAt(k, ch) : h.motEA[j] * h.ctl.tStart + h.motEB[j]));
       }
       for (size_t q = 0; q < h.mrEq.size(); ++q) {
         mrEq.push_back(h.mrEq[q] + modelEqOff_[k]);
@@ -249,6 +271,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(d_.motModel, int, motModel); UPV(d_.modelMotOff, int, motOff);
     UPV(d_.motD0, double, d0); UPV(d_.motD1, double, d1); UPV(d_.motEA, double, eA); UPV(d_.motEB, double, eB);
     UPV(d_.motD, double, D0);
+    UPV(d_.motCh, int, motCh);
     d_.motCc = alloc<double>(motModel.size());
     UPV(d_.mrEq, int, mrEq); UPV(d_.mrMot, int, mrMot); UPV(d_.mrPtr, int64_t, mrPtr); UPV(d_.mrSrc, int64_t, mrSrc);
     d_.linearIters = opt_.fp32Factor ? 3 : 1;
@@ -732,6 +755,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   for (long long* p : {M.nStep, M.nIter, M.stepLimit}) reg(p, sizeof(long long) * nm);
   reg(M.qsCount, sizeof(int) * nm);
   if (d_.nldTot > 0) reg(d_.qext, D * (size_t)neq);
+  if (d_.nextTot > 0) reg(d_.extVal, D * (size_t)d_.nextTot);
   if (d_.nmotTot > 0) {
     reg(d_.motD, D * (size_t)d_.nmotTot);
     reg(d_.motCc, D * (size_t)d_.nmotTot);
@@ -909,6 +933,20 @@ int Engine::solveUpdateIteration() {
 void Engine::setStepLimitOf(int m, long long lim) {
   cudaMemcpyAsync(d_.m.stepLimit + m, &lim, sizeof(long long), cudaMemcpyHostToDevice, stream_);
   cudaStreamSynchronize(stream_);
+}
+
+int Engine::setExtValue(int m, int ch, double v) {
+  if (m < 0 || m >= (int)modelExtOff_.size() || ch < 0 || ch >= modelExtCnt_[m]) return -1;
+  cudaMemcpyAsync(d_.extVal + modelExtOff_[m] + ch, &v, sizeof(double), cudaMemcpyHostToDevice, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -947;
+}
+
+double Engine::extValue(int m, int ch) {
+  if (m < 0 || m >= (int)modelExtOff_.size() || ch < 0 || ch >= modelExtCnt_[m]) return 0.0;
+  double v = 0.0;
+  cudaMemcpyAsync(&v, d_.extVal + modelExtOff_[m] + ch, sizeof(double), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return v;
 }
 
 int Engine::setTimeStep(int m, double dt) {
@@ -1166,6 +1204,7 @@ T readOne(const T* p, cudaStream_t s) {
 int Engine::modelState(int m) { return readOne(d_.m.state + m, stream_); }
 int Engine::modelStatus(int m) { return readOne(d_.m.status + m, stream_); }
 double Engine::modelTime(int m) { return readOne(d_.m.time + m, stream_); }
+double Engine::modelDt(int m) { return readOne(d_.m.dt + m, stream_); }
 long long Engine::modelSteps(int m) { return readOne(d_.m.nStep + m, stream_); }
 long long Engine::modelIterations(int m) { return readOne(d_.m.nIter + m, stream_); }
 

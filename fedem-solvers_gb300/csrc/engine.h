@@ -59,6 +59,7 @@ class Engine {
   int modelState(int m);
   int modelStatus(int m);
   double modelTime(int m);
+  double modelDt(int m);
   long long modelSteps(int m);
   long long modelIterations(int m);
   int getTriadUr(int m, double* ur);  // 12 per triad of the model
@@ -84,6 +85,9 @@ class Engine {
   int solveUpdateIteration();
   void setStepLimitOf(int m, long long lim);
   int setTimeStep(int m, double dt);
+  // external function channel ch (0-based) of model m: its value for the next step
+  int setExtValue(int m, int ch, double v);
+  double extValue(int m, int ch);
   // replaces (add = false) or adds to the right-hand side of the assembled iteration
   int setRhs(int m, const double* v, bool add);
   // the mutable state as one host byte array (in-core restart)
@@ -137,6 +141,7 @@ class Engine {
   // snapshot of mutable arrays: (device pointer, bytes) and the backup buffer
   std::vector<std::pair<void*, size_t>> mutable_;
   std::vector<double> scaleSentinel_;
+  std::vector<int> modelExtOff_, modelExtCnt_;
   double factorBytes_ = 0.0;  // algorithmic bytes of one factor + first forward launch, all models
   int* ctrBlock_ = nullptr;   // the iteration counters (see upload)
   size_t ctrInts_ = 0, queueInts_ = 0;

@@ -120,6 +120,11 @@ struct DevData {
   int nldTot = 0;
   int *ldEq, *ldPtr;
   double *ldF0, *ldF1, *ldEA, *ldEB, *qextBase;
+  // external functions: a load term or motion whose engine is one (ldCh / motCh
+  // >= 0, a global channel) takes extVal[ch] instead of eA * t + eB
+  int* ldCh;
+  int nextTot = 0;
+  double* extVal;
   // axial springs and dampers (SoA): kind (0 spring, 1 damper), triads [k * naxTot + a],
   // model, constants; current direction axN (3) and length; element forces FelA
   // (FS 6, FD 6) and Newton matrices elMatA (6x6, translational DOFs of both triads).
@@ -134,6 +139,7 @@ struct DevData {
   int nmotTot = 0;
   int *motModel, *modelMotOff;
   double *motD0, *motD1, *motEA, *motEB, *motD, *motCc;
+  int* motCh;
   // predictor right-hand-side terms: del[mrEq[k]] -= cc[mrMot[q]] * elMat[mrSrc[q]]
   int nmrTot = 0;
   int *mrEq, *mrMot;

@@ -119,6 +119,14 @@ struct Rec {
     auto it = r.vals.find(k);
     return (it == r.vals.end() || it->second.empty()) ? std::string() : lowerCase(it->second[0]);
   }
+  // the value as written (quotes removed), for names compared case-sensitively
+  std::string raw(const char* k) const {
+    auto it = r.vals.find(k);
+    if (it == r.vals.end() || it->second.empty()) return std::string();
+    std::string v = it->second[0];
+    if (v.size() >= 2 && (v.front() == '\'' || v.front() == '"') && v.back() == v.front()) v = v.substr(1, v.size() - 2);
+    return v;
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -508,20 +516,38 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   }
   // engines (engineRoutinesModule.f90 subset): value = f(x), x = time for a TIME
   // sensor (or no sensor), else 0; f = SCALE (realData(1) * x), CONSTANT
-  // (realData(1)) or none (x).  Stored as x-coefficient eA and constant eB.
-  std::map<int, std::pair<std::string, double>> funcs;  // id -> (type, realData(1) or its default)
-  std::map<int, bool> timeSensor;                        // id -> TIME sensor
+  // (realData(1)), none (x), or an external function: DEVICE_FUNCTION without
+  // a file, whose value on channel `channel` the caller sets (setExtFunc).
+  // Stored as x-coefficient eA, constant eB and external channel (0-based, -1 none).
+  struct FuncDef {
+    std::string type;
+    double c = 0.0;
+    int channel = 0;
+  };
+  std::map<int, FuncDef> funcs;  // id -> definition
+  std::map<int, bool> timeSensor;  // id -> TIME sensor
   for (const NmlRecord& nr : recs) {
     Rec r{nr};
     if (nr.name == "function") {
       auto rd = r.nums("realdata");
-      std::string type = r.str("type");
-      funcs[r.inum("id", 0)] = {type, rd.empty() ? (type == "scale" ? 1.0 : 0.0) : rd[0]};
+      FuncDef fd;
+      fd.type = r.str("type");
+      fd.c = rd.empty() ? (fd.type == "scale" ? 1.0 : 0.0) : rd[0];
+      if (fd.type == "device_function") {
+        if (!r.raw("filename").empty()) { err = "device functions reading a file are not supported"; return -22; }
+        fd.channel = r.inum("channel", 0);
+        if (fd.channel < 1) { err = "external function without a channel (>= 1)"; return -22; }
+      }
+      funcs[r.inum("id", 0)] = fd;
     } else if (nr.name == "sensor") {
       timeSensor[r.inum("id", 0)] = r.str("type") == "time";
     }
   }
-  std::map<int, std::pair<double, double>> engines;  // id -> (eA, eB)
+  struct EngineVal {
+    double eA, eB;
+    int ch;
+  };
+  std::map<int, EngineVal> engines;  // id -> value coefficients
   for (const NmlRecord& nr : recs) {
     if (nr.name != "engine") continue;
     Rec r{nr};
@@ -532,14 +558,31 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       xs = (it != timeSensor.end() && it->second) ? 1.0 : 0.0;
     }
     double eA = xs, eB = 0.0;
+    int ch = -1, ftype = 0;
+    double fc = 0.0;
     if (fid > 0) {
       auto it = funcs.find(fid);
       if (it == funcs.end()) { err = "engine refers to unknown function"; return -21; }
-      if (it->second.first == "scale") eA = it->second.second * xs;
-      else if (it->second.first == "constant") { eA = 0.0; eB = it->second.second; }
-      else { err = "function type '" + it->second.first + "' is not supported (SCALE, CONSTANT)"; return -22; }
+      fc = it->second.c;
+      if (it->second.type == "scale") { eA = it->second.c * xs; ftype = 1; }
+      else if (it->second.type == "constant") { eA = 0.0; eB = it->second.c; ftype = 2; }
+      else if (it->second.type == "device_function") { eA = 0.0; ch = it->second.channel - 1; ftype = 3; }
+      else { err = "function type '" + it->second.type + "' is not supported (SCALE, CONSTANT, DEVICE_FUNCTION)"; return -22; }
     }
-    engines[r.inum("id", 0)] = {eA, eB};
+    const int id = r.inum("id", 0);
+    engines[id] = {eA, eB, ch};
+    // the engine table for evalFunc / getFuncId (solverModule.f90:1602-1680)
+    auto ext = r.nums("extid");
+    m.engId.push_back(id);
+    m.engUserId.push_back(ext.empty() ? id : (int)std::lround(ext[0]));
+    m.engTag.push_back(r.raw("tag"));
+    m.engEA.push_back(eA);
+    m.engEB.push_back(eB);
+    m.engCh.push_back(ch);
+    m.engFType.push_back(ftype);
+    m.engFc.push_back(fc);
+    m.engTimeArg.push_back(xs != 0.0 ? 1 : 0);
+    if (ch + 1 > m.nExt) m.nExt = ch + 1;
   }
   // prescribed deflections: MEQN = -ICEQ of the constraint equation (samSolverModule.f90)
   std::vector<int> motionOfDof(6 * (size_t)m.ntri, -1);
@@ -556,12 +599,14 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     if (slot >= 0) { err = "two motions on one DOF"; return -26; }
     slot = (int)m.motD0.size();
     double eA = 0.0, eB = 0.0, d1 = r.num("d1", 0.0);
+    int ch = -1;
     int eid = r.inum("motionengineid", 0);
     if (eid > 0) {
       auto e = engines.find(eid);
       if (e == engines.end()) { err = "motion refers to unknown engine"; return -27; }
-      eA = e->second.first;
-      eB = e->second.second;
+      eA = e->second.eA;
+      eB = e->second.eB;
+      ch = e->second.ch;
     } else {
       d1 = 0.0;
     }
@@ -569,6 +614,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.motD1.push_back(d1);
     m.motEA.push_back(eA);
     m.motEB.push_back(eB);
+    m.motCh.push_back(ch);
     if (c.initEquilibrium && m.motD0.back() + d1 * (eA * c.tStart + eB) != 0.0) {
       err = "prescribed start values other than zero with initEquilibrium are not supported";
       return -28;
@@ -606,7 +652,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.ndof += m.triNdof[t];
   }
   // pass 2: superelements, undeformed positions, loads
-  std::map<int, std::vector<std::array<double, 4>>> engineLoads;  // equation -> (f0, f1, eA, eB)
+  std::map<int, std::vector<std::array<double, 5>>> engineLoads;  // equation -> (f0, f1, eA, eB, channel)
   std::vector<int> elProp;
   std::map<int, int> elIndex;
   m.qext.assign(m.neq, 0.0);
@@ -688,7 +734,9 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (eid > 0) {
         auto en = engines.find(eid);
         if (en == engines.end()) { err = "load refers to unknown engine"; return -19; }
-        if (eq >= 0) engineLoads[eq].push_back({r.num("f0", 0.0), r.num("f1", 0.0), en->second.first, en->second.second});
+        if (eq >= 0)
+          engineLoads[eq].push_back({r.num("f0", 0.0), r.num("f1", 0.0), en->second.eA, en->second.eB,
+                                     (double)en->second.ch});
       } else if (eq >= 0) {
         m.qext[eq] += r.num("f0", 0.0);
       }
@@ -699,6 +747,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.ldEq.push_back(kv.first);
     for (auto& l : kv.second) {
       m.ldF0.push_back(l[0]); m.ldF1.push_back(l[1]); m.ldEA.push_back(l[2]); m.ldEB.push_back(l[3]);
+      m.ldCh.push_back((int)l[4]);
     }
     m.ldPtr.push_back((int)m.ldF0.size());
   }

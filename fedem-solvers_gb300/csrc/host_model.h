@@ -76,10 +76,20 @@ struct HostModel {
   std::vector<double> qext;
   std::vector<int> ldEq, ldPtr;
   std::vector<double> ldF0, ldF1, ldEA, ldEB;
+  std::vector<int> ldCh;  // external channel of the load's engine (value ext[ch] instead of eA t + eB), -1 none
+  // engines: base id, user id, tag, value eA t + eB (+ ext[ch] when ch >= 0), the
+  // function (0 none, 1 SCALE fc x, 2 CONSTANT fc, 3 external) and whether its
+  // argument is the time; nExt: external channels used
+  std::vector<int> engId, engUserId, engCh, engFType, engTimeArg;
+  std::vector<std::string> engTag;
+  std::vector<double> engEA, engEB, engFc;
+  int nExt = 0;
+  std::vector<double> extInit;  // initial external function values (empty: zero)
   // prescribed deflections (motionRoutinesModule.f90:58-193): D(t) = d0 + d1 * (eA * t + eB)
   // (engine = function of the TIME sensor); a prescribed DOF has meqn = -2 - motion index
   std::vector<int> motDof;
   std::vector<double> motD0, motD1, motEA, motEB;
+  std::vector<int> motCh;  // external channel of the motion's engine, -1 none
   // predictor right-hand-side terms of the prescribed DOFs: equation mrEq[k] gets
   // -cc(motion mrMot[q]) * elMat[mrSrc[q]] for q in mrPtr[k]..mrPtr[k+1] (mrSrc = 144*e + entry)
   std::vector<int> mrEq, mrPtr, mrSrc, mrMot;

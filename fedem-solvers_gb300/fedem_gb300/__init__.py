@@ -54,6 +54,11 @@ def load_library(path=None):
         "saveState": (c_bool, [P(c_dbl), c_int]),
         "restartFromState": (c_int, [P(c_dbl), c_int, c_int]),
         "setTime": (c_bool, [c_dbl]),
+        "setExtFunc": (c_bool, [c_int, c_dbl]),
+        "evalFunc": (c_dbl, [c_int, ctypes.c_char_p, c_dbl, P(c_int)]),
+        "getFuncId": (c_int, [ctypes.c_char_p]),
+        "solveWindow": (c_bool, [c_int, c_int, c_int, c_int, P(c_int), P(c_dbl), P(c_dbl), P(c_dbl), c_int,
+                                 P(c_dbl), P(c_int)]),
         "setRhsVector": (c_bool, [P(c_dbl)]),
         "addRhsVector": (c_bool, [P(c_dbl)]),
         "fgpu_model_create": (c_int, [ctypes.c_char_p, c_int, P(ctypes.c_char_p), P(vp)]),

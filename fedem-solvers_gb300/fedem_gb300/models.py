@@ -35,14 +35,25 @@ def _bc_line(k, clamp, motion):
     return ""
 
 
-def _loads(n_el, load_node, load_dof, load, motion, load_ramp=None):
+def _loads(n_el, load_node, load_dof, load, motion, load_ramp=None, load_ext=None):
     """&LOAD record, or with `motion` = (triad index, DOF, d1) a prescribed
     deflection d1 * time driven by a SCALE function of the TIME sensor
     (&MOTION, &ENGINE, &FUNCTION, &SENSOR as in the reference's
     cantilever-prescribed.fsi).  `load_ramp` = r makes the load
-    load * r * time (F = f0 + f1 * engine with f0 = 0, f1 = load)."""
+    load * r * time (F = f0 + f1 * engine with f0 = 0, f1 = load).
+    `load_ext` = (channel, user id, tag) drives the load by an external
+    function instead (DEVICE_FUNCTION without a file): F = load * value."""
     out = []
-    if load_ramp is not None:
+    if load_ext is not None:
+        channel, uid, tag = load_ext
+        base = 2 * n_el + 60
+        out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
+                   f"  f0 = 0.0\n  f1 = {_f(load)}\n  loadEngineId = {base}\n/\n"
+                   f"&ENGINE\n  id = {base}\n  extId = {int(uid)}\n  tag = '{tag}'\n  functionId = {base + 1}\n"
+                   f"  nArg = 0\n/\n"
+                   f"&FUNCTION\n  id = {base + 1}\n  type = 'DEVICE_FUNCTION'\n  channel = {int(channel)}\n"
+                   f"  fileName = ''\n/\n")
+    elif load_ramp is not None:
         base = 2 * n_el + 40
         out.append(f"&LOAD\n  id = {2 * n_el + 10}\n  triadId = {load_node + 1}\n  lDof = {int(load_dof)}\n"
                    f"  f0 = 0.0\n  f1 = {_f(load)}\n  loadEngineId = {base}\n/\n"
@@ -91,7 +102,7 @@ def _axials(n_el, anchors, springs, dampers):
 
 def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof, load,
                    shear_factor=0.0, weights=(0.1, 1.0, 1.0), title="beam chain", section=None, axis="x",
-                   motion=None, anchors=None, springs=None, dampers=None, load_ramp=None):
+                   motion=None, anchors=None, springs=None, dampers=None, load_ramp=None, load_ext=None):
     """Solver-input text for a straight chain of `n_el` beams along X (or Z).
 
     Triad k sits at k*el_len on the axis; triad `clamp` has all six DOFs
@@ -100,7 +111,8 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
     `section` = (A, Iy, Iz, It) overrides the pipe section from od/wall.
     `motion` = (triad index, DOF, d1) prescribes that DOF to d1 * time
     (the load record is then left out when `load` is 0); `load_ramp` = r
-    makes the load grow as load * r * time.  `anchors`,
+    makes the load grow as load * r * time; `load_ext` = (channel, user id,
+    tag) makes it load * (external function value).  `anchors`,
     `springs` and `dampers` add fixed triads and axial springs/dampers
     (see _axials).
     """
@@ -133,7 +145,7 @@ def beam_chain_fsi(n_el, el_len, od, wall, E, G, rho, clamp, load_node, load_dof
             f"  undPosInSupElSystem = 1.0 0.0 0.0 {L} 0.0 1.0 0.0 0.0 0.0 0.0 1.0 0.0\n/\n")
     out.append(f"&ELEMENT_PROPERTY\n  id = 1\n  geometry = {_f(area)} {_f(iy)} {_f(iz)} {_f(it)} "
                f"{_f(shear_factor)} {_f(shear_factor)} 0.0 0.0\n  material = {_f(rho)} {_f(E)} {_f(G)}\n/\n")
-    out += _loads(n_el, load_node, load_dof, load, motion, load_ramp)
+    out += _loads(n_el, load_node, load_dof, load, motion, load_ramp, load_ext)
     return "".join(out + extra)
 
 

@@ -6,7 +6,8 @@ Mirrors PythonAPI/src/fedempy/solver.py (``FedemSolver``: constructor,
 ``get_equations``, ``get_newton_matrix``, ``get_rhs_vector``, ``start_step``
 :677, ``solve_iteration`` :707, ``finish_step``, ``set_rhs_vector`` /
 ``add_rhs_vector`` :1100-1110, ``get_state_size`` :495, ``save_state`` :546,
-``restart_from_state`` :398) with the same
+``restart_from_state`` :398, ``set_ext_func`` :888, ``get_function`` :941,
+``get_function_ids`` :973, ``solve_window`` :429) with the same
 argument meaning and error behaviour (``FedemException`` on failure, the
 internal error flag blocks further calls after an error).
 """
@@ -139,6 +140,44 @@ class FedemSolver:
         """Iterates the started step to convergence; False at the end or on error."""
         self.__check_error("finish_step")
         return self._solver.solveIteration(ctypes.byref(self.ierr), True)
+
+    def set_ext_func(self, func_id, value=None):
+        """Value of external function channel func_id (1-based) for the next step."""
+        return self._solver.setExtFunc(int(func_id), float(0.0 if value is None else value))
+
+    def get_function(self, uid=0, tag=None, arg=None):
+        """Value of the engine with user id uid (or the tagged one), at arg when given."""
+        t = tag.encode() if isinstance(tag, str) else tag
+        return self._solver.evalFunc(int(uid), t, float(-1.0 if arg is None else arg), ctypes.byref(self.ierr))
+
+    def get_function_ids(self, tags):
+        if isinstance(tags, str):
+            return self._solver.getFuncId(tags.encode())
+        return [self._solver.getFuncId(t.encode()) if isinstance(t, str) else int(t) for t in tags]
+
+    def solve_window(self, n_step, inputs=None, f_out=None, xtimes=None):
+        """n_step steps with the external function values of each step (inputs,
+        len(inputs) // n_step per step) and step times (xtimes); returns the
+        values of the functions f_out after each step and whether the
+        simulation goes on."""
+        P = ctypes.POINTER
+        n_inc, times = 0, None
+        if xtimes is not None:
+            xt = np.ascontiguousarray(xtimes, dtype=np.float64)
+            n_inc, times = xt.size, xt.ctypes.data_as(P(ctypes.c_double))
+        n_in, inp = 0, None
+        if inputs is not None:
+            iv = np.ascontiguousarray(inputs, dtype=np.float64)
+            n_in, inp = iv.size // max(int(n_step), 1), iv.ctypes.data_as(P(ctypes.c_double))
+        n_out, fo, out = 0, None, None
+        if f_out is not None:
+            fv = np.ascontiguousarray(f_out, dtype=np.int32)
+            n_out, fo = fv.size, fv.ctypes.data_as(P(ctypes.c_int))
+            outv = np.zeros(int(n_step) * fv.size)
+            out = outv.ctypes.data_as(P(ctypes.c_double))
+        more = self._solver.solveWindow(int(n_step), n_inc, n_in, n_out, fo, times, inp, out, 0, None,
+                                        ctypes.byref(self.ierr))
+        return (list(outv) if f_out is not None else None), more
 
     def get_state_size(self):
         return self._solver.getStateSize()

@@ -15,9 +15,10 @@
  * startStep, solveIteration, setTime, getStateVar, getTime, getSystemSize,
  * getEquations, getSystemMatrix, getNewtonMatrix, getStiffness/Mass/
  * DampingMatrix, get/set/addRhsVector, getElementStiffnessMatrix, in-core
- * state save and restart, solverDone, solverClose).  Entry points for features
- * outside that path (windowed stepping with external functions, eigenmodes,
- * inverse analysis, strain/beam-force recovery, part and gauge states) exist
+ * state save and restart, external functions (setExtFunc, evalFunc,
+ * getFuncId, solveWindow), solverDone, solverClose).  Entry points for features
+ * outside that path (eigenmodes, inverse analysis, strain/beam-force
+ * recovery, part and gauge states) exist
  * so the library loads as a drop-in, and return the reference's failure value
  * (false, 0 or a negative status, with *ierr = -1 where present).
  */
@@ -46,7 +47,12 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
  * Returns 0, or < 0 when there is no model or ndat < getStateSize(). */
 int restartFromState(const double* stateData, const int ndat, const int writeToRDB);
 
-/* solverInterface.h:110 -- windowed stepping with external inputs: unsupported. */
+/* solverInterface.h:110 -- nStep steps; before each, the step time (times,
+ * when nInc >= nStep) and the values of external function channels 1..nIn
+ * (inputs, nIn per step) are applied; after each, the engines with user ids
+ * fOut are evaluated into outputs (nOut per step); with nDat > 0 the state is
+ * saved into stateData at the end.  False at the end of the simulation or on
+ * error (*ierr != 0; nInc - nStep for a too short times array). */
 bool solveWindow(int nStep, int nInc, int nIn, int nOut, const int* fOut, const double* times,
                  const double* inputs, double* outputs, int nDat, double* stateData, int* ierr);
 
@@ -99,7 +105,9 @@ int solverDone(bool removeSingletons);
 /* solverInterface.h:330 */
 void solverClose(void);
 
-/* solverInterface.h:342 -- external function values: unsupported, returns false. */
+/* solverInterface.h:342 -- value of external function channel funcId
+ * (1-based: a DEVICE_FUNCTION without a file and with that channel) for the
+ * next step; false when the model has no such channel. */
 bool setExtFunc(int funcId, double value);
 /* solverInterface.h:349 -- current (or next) physical time. */
 double getTime(bool nextStep, int* ierr);
@@ -110,9 +118,12 @@ bool setTime(double nextTime);
 /* solverInterface.h:361, :369 */
 static inline double getCurrentTime(int* ierr) { return getTime(false, ierr); }
 static inline double getNextTime(int* ierr) { return getTime(true, ierr); }
-/* solverInterface.h:383 -- general functions: unsupported, *ierr = -1. */
+/* solverInterface.h:383 -- value of the engine with user id uid, or with a tag
+ * of the first engine with that tag (a user id match wins, no match gives 0);
+ * x >= 0 (without a tag) evaluates the engine's function at x.  Engines of
+ * SCALE, CONSTANT and external functions of the TIME sensor (or none). */
 double evalFunc(int uid, const char* tag, double x, int* ierr);
-/* solverInterface.h:398 -- unsupported, returns -1. */
+/* solverInterface.h:398 -- user id of the first engine with the tag, -1 if none. */
 int getFuncId(const char* tag);
 
 /* solverInterface.h:407 -- 1-based equation numbers of the DOFs of the triad

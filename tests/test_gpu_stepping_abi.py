@@ -211,3 +211,65 @@ def test_save_state_and_restart_reproduce_the_run(gpu, mixed):
     np.testing.assert_array_equal(np.array(third), np.array(cont))
     assert s3.restart_from_state(state[:-1]) < 0  # too short
     s3.solver_done()
+
+
+def _ext_models():
+    from fedem_gb300 import models
+
+    common = dict(clamp=0, load_node=N_EL, load_dof=2, load=1500.0, **models.STEEL)
+    fsi_time = models.beam_chain_fsi(N_EL, 0.25, 0.1, 0.01, load_ramp=40.0, **common)
+    fsi_ext = models.beam_chain_fsi(N_EL, 0.25, 0.1, 0.01, load_ext=(1, 7, "tipload"), **common)
+    return fsi_time, fsi_ext
+
+
+def test_external_function_load_equals_the_time_engine(gpu):
+    """A load driven by an external function (setExtFunc before every step,
+    solverInterface.h:342) set to 40 t gives the results of the same load
+    driven by a SCALE(40) function of the TIME sensor; evalFunc and getFuncId
+    see the engines (solverInterface.h:383, :398)."""
+    fsi_time, fsi_ext = _ext_models()
+    ref = _solve_next_history(OPTS, fsi_time)
+    s = _solver(OPTS, fsi_ext)
+    assert s.get_function_ids("tipload") == 7 and s.get_function_ids("nothing") == -1
+    assert not s.set_ext_func(2, 1.0)  # the model has one channel
+    hist = []
+    while True:
+        t = s.get_next_time()
+        assert s.set_ext_func(1, 40.0 * t)
+        ok = s.solve_next()
+        assert s.ierr.value == 0
+        hist.append(_positions(s))
+        assert s.get_function(7) == 40.0 * t
+        assert s.get_function(tag="tipload") == 40.0 * t
+        if not ok:
+            break
+    np.testing.assert_allclose(np.array(hist), ref, rtol=0.0, atol=1e-13)
+    s.solver_done()
+    s = _solver(OPTS, fsi_time)
+    s.solve_next()
+    uid = 2 * N_EL + 40  # the time engine's id (no extId): its user id
+    assert abs(s.get_function(uid) - 40.0 * s.get_current_time()) < 1e-15
+    assert s.get_function(uid, arg=0.5) == 20.0
+    s.solver_done()
+
+
+def test_solve_window_equals_step_by_step(gpu):
+    """solveWindow (solverInterface.h:110) over 10 steps with the external
+    values as inputs and the engine as output equals setExtFunc + solveNext."""
+    _, fsi_ext = _ext_models()
+    a = _solver(OPTS, fsi_ext)
+    times = [a.get_current_time() + 0.001 * (k + 1) for k in range(10)]
+    for t in times:
+        a.set_ext_func(1, 40.0 * t)
+        assert a.start_step(time_next=t)
+        a.finish_step()
+    ref = _positions(a)
+    a.solver_done()
+    b = _solver(OPTS, fsi_ext)
+    outputs, more = b.solve_window(10, inputs=[40.0 * t for t in times], f_out=[7], xtimes=times)
+    assert more and b.ierr.value == 0
+    np.testing.assert_array_equal(np.array(outputs), 40.0 * np.array(times))
+    np.testing.assert_array_equal(_positions(b), ref)
+    outputs, more = b.solve_window(2, inputs=[1.0, 2.0], f_out=[7], xtimes=[0.5])  # too short times array
+    assert not more and b.ierr.value == 1 - 2
+    b.solver_done()

@@ -187,3 +187,18 @@ def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
     with pytest.raises(FedemException):
         Model(base.replace("&TRIAD\n  id = 5\n  nDOFs = 6\n", "&TRIAD\n  id = 5\n  nDOFs = 6\n  BC = 2 2 2 2 2 2\n"),
               ["-initEquilibrium"])
+
+
+def test_external_function_records():
+    """DEVICE_FUNCTION without a file is an external function (setExtFunc
+    channel); with a file, or without a channel, the model is refused."""
+    from fedem_gb300 import FedemException, models
+    from fedem_gb300.batch import Model
+
+    fsi = models.beam_chain_fsi(4, 0.25, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0,
+                                load_ext=(2, 5, "tip"), **models.STEEL)
+    Model(fsi, ["-timeInc=0.01", "-timeEnd=0.1"]).close()
+    with pytest.raises(FedemException, match="file"):
+        Model(fsi.replace("fileName = ''", "fileName = 'inputs.asc'"), ["-timeInc=0.01", "-timeEnd=0.1"])
+    with pytest.raises(FedemException, match="channel"):
+        Model(fsi.replace("channel = 2", "channel = 0"), ["-timeInc=0.01", "-timeEnd=0.1"])
