@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "eigen.h"
 #include "../../include/fedem_solver_core.h"
 #include "../../include/fgpu.h"
 #include "engine.h"
@@ -303,9 +304,49 @@ bool solveIteration(int* ierr, bool all) {
     if (!all) return true;
   }
 }
-bool solveEigenModes(const int, double*, double*, bool, int, int* ierr) {
-  if (ierr) *ierr = -1;
-  return false;
+// solverInterface.h:293 (solverModule.f90:1004-1092) -- the nmod lowest
+// eigenmodes of K phi = lambda M phi at the current state: eval = sqrt|lambda|
+// / 2 pi (Hz), evec = M-orthonormal eigenvectors, nmod columns in equation
+// order (neq each) or DOF order (ndof each, zero at fixed and prescribed DOFs).
+// *ierr = number of negative eigenvalues, or a positive count when the Lanczos
+// iteration did not converge every mode; < 0 on error.  useLaPack is ignored
+// (one Lanczos solver).  Between steps only.
+bool solveEigenModes(const int nmod, double* eval, double* evec, bool dofOrder, int, int* ierr) {
+  int lerr = 0;
+  int& e = ierr ? *ierr : lerr;
+  e = 0;
+  if (!g_core || g_core->ierr || !eval) {
+    e = g_core ? (g_core->ierr ? g_core->ierr : -1) : -1;
+    return false;
+  }
+  Singleton& s = *g_core;
+  if (s.inStep) {
+    e = -999;
+    return false;
+  }
+  const HostModel& m = *s.model;
+  std::vector<double> lambda, vecs;
+  int nNeg = 0;
+  const int rc = lowestModes(*s.engine, m, nmod, lambda, vecs, nNeg);
+  if (rc < 0) {
+    e = rc;
+    return false;
+  }
+  const double twoPi = 8.0 * std::atan(1.0);
+  for (int k = 0; k < nmod; ++k) eval[k] = std::sqrt(std::fabs(lambda[k])) / twoPi;
+  if (evec) {
+    for (int k = 0; k < nmod; ++k) {
+      const double* v = &vecs[(size_t)m.neq * k];
+      if (dofOrder) {
+        double* o = evec + (size_t)m.ndof * k;
+        for (int i = 0; i < m.ndof; ++i) o[i] = m.meqn[i] >= 0 ? v[m.meqn[i]] : 0.0;
+      } else {
+        std::memcpy(evec + (size_t)m.neq * k, v, sizeof(double) * m.neq);
+      }
+    }
+  }
+  e = nNeg + rc;
+  return true;
 }
 bool solveInverse(const double*, const int*, const int*, int, int, int* ierr) {
   if (ierr) *ierr = -1;

@@ -1133,6 +1133,12 @@ __global__ void kStepEnd(DevData d) {
 // ---------------------------------------------------------------------------
 // static equilibrium iterations
 // ---------------------------------------------------------------------------
+// backward queues of the active models, for solves outside a step start
+__global__ void kSeedBackward(DevModels m, BackwardSeed bs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m.n && (m.flags[i] & FL_ACTIVE)) seedBackward(bs, i);
+}
+
 __global__ void kStaticBegin(DevModels m, int* activeCount, BackwardSeed bs) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
@@ -1304,6 +1310,9 @@ void launchQsRestore(const DevData& d, cudaStream_t s) {
   if (!d.urQs) return;
   long long n = std::max<long long>(std::max<long long>(d.ntriTot, d.nelTot), d.ndofTot);
   kQsRestore<<<blocksFor(n), TPB, 0, s>>>(d);
+}
+void launchSeedBackward(const DevData& d, const BackwardSeed& seed, cudaStream_t s) {
+  kSeedBackward<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, seed);
 }
 void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s) {
   kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, seed);

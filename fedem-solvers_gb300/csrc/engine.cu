@@ -935,6 +935,51 @@ void Engine::setStepLimitOf(int m, long long lim) {
   cudaStreamSynchronize(stream_);
 }
 
+int Engine::prepareStiffnessSolves() {
+  const int nm = d_.m.n;
+  savedFlags_.assign(nm, 0);
+  cudaMemcpyAsync(savedFlags_.data(), d_.m.flags, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  std::vector<int> fl(nm, FL_ACTIVE | FL_TANGENT | FL_REBUILD);
+  std::vector<double> sc(3 * (size_t)nm);
+  for (int k = 0; k < nm; ++k) { sc[3 * k] = 0.0; sc[3 * k + 1] = 1.0; sc[3 * k + 2] = 0.0; }
+  cudaMemcpyAsync(d_.m.flags, fl.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.scaleN, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, stream_);
+  launchBuildElementNewton(d_, stream_);
+  launchRotateElementNewton(d_, stream_);
+  launchCsrGather(d_, stream_);
+  resetIterationCounters(stream_);
+  enqueueFactor(stream_);
+  // solves from here on: active, no tangent update
+  std::fill(fl.begin(), fl.end(), FL_ACTIVE);
+  cudaMemcpyAsync(d_.m.flags, fl.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -948;
+  std::vector<int> st(nm);
+  cudaMemcpy(st.data(), d_.m.status, sizeof(int) * nm, cudaMemcpyDeviceToHost);
+  for (int k = 0; k < nm; ++k)
+    if (st[k] & SS_SINGULAR) return -3;
+  return 0;
+}
+
+int Engine::solveStiffness(int m, const double* b, double* x) {
+  const int n = hm_[m]->neq;
+  cudaMemcpyAsync(d_.del + modelEqOff_[m], b, sizeof(double) * n, cudaMemcpyHostToDevice, stream_);
+  resetIterationCounters(stream_);
+  launchSeedBackward(d_, seed_, stream_);
+  enqueueFactor(stream_);  // forward elimination only (no tangent flag)
+  enqueueSolve(stream_);
+  cudaMemcpyAsync(x, d_.del + modelEqOff_[m], sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -949;
+}
+
+int Engine::endStiffnessSolves() {
+  if (!savedFlags_.empty())
+    cudaMemcpyAsync(d_.m.flags, savedFlags_.data(), sizeof(int) * savedFlags_.size(), cudaMemcpyHostToDevice,
+                    stream_);
+  invalidateNewtonScales();
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -950;
+}
+
 int Engine::setExtValue(int m, int ch, double v) {
   if (m < 0 || m >= (int)modelExtOff_.size() || ch < 0 || ch >= modelExtCnt_[m]) return -1;
   cudaMemcpyAsync(d_.extVal + modelExtOff_[m] + ch, &v, sizeof(double), cudaMemcpyHostToDevice, stream_);

@@ -85,6 +85,15 @@ class Engine {
   int solveUpdateIteration();
   void setStepLimitOf(int m, long long lim);
   int setTimeStep(int m, double dt);
+  // Solves with the stiffness matrix at the current configuration (eigenmodes):
+  // prepareStiffnessSolves assembles and factors K of every model (Newton matrix
+  // scales 0, 1, 0), solveStiffness solves K x = b for model m (b, x: its
+  // equations; the other models' vectors are scratch), endStiffnessSolves puts the
+  // flags back and makes the next tangent iteration rebuild the Newton matrices.
+  // Only between steps: the factors of the step in progress are overwritten.
+  int prepareStiffnessSolves();
+  int solveStiffness(int m, const double* b, double* x);
+  int endStiffnessSolves();
   // external function channel ch (0-based) of model m: its value for the next step
   int setExtValue(int m, int ch, double v);
   double extValue(int m, int ch);
@@ -142,6 +151,7 @@ class Engine {
   std::vector<std::pair<void*, size_t>> mutable_;
   std::vector<double> scaleSentinel_;
   std::vector<int> modelExtOff_, modelExtCnt_;
+  std::vector<int> savedFlags_;
   double factorBytes_ = 0.0;  // algorithmic bytes of one factor + first forward launch, all models
   int* ctrBlock_ = nullptr;   // the iteration counters (see upload)
   size_t ctrInts_ = 0, queueInts_ = 0;

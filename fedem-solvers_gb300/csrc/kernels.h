@@ -44,6 +44,7 @@ void launchIncrement(const DevData& d, cudaStream_t s);
 void launchNormsControl(const DevData& d, cudaStream_t s);
 // static equilibrium helpers
 void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s);
+void launchSeedBackward(const DevData& d, const BackwardSeed& seed, cudaStream_t s);
 void launchStaticResidual(const DevData& d, cudaStream_t s);
 void launchStaticNorm(const DevData& d, cudaStream_t s);
 void launchStaticIncrement(const DevData& d, cudaStream_t s);

@@ -55,6 +55,7 @@ def load_library(path=None):
         "restartFromState": (c_int, [P(c_dbl), c_int, c_int]),
         "setTime": (c_bool, [c_dbl]),
         "setExtFunc": (c_bool, [c_int, c_dbl]),
+        "solveEigenModes": (c_bool, [c_int, P(c_dbl), P(c_dbl), c_bool, c_int, P(c_int)]),
         "evalFunc": (c_dbl, [c_int, ctypes.c_char_p, c_dbl, P(c_int)]),
         "getFuncId": (c_int, [ctypes.c_char_p]),
         "solveWindow": (c_bool, [c_int, c_int, c_int, c_int, P(c_int), P(c_dbl), P(c_dbl), P(c_dbl), c_int,

@@ -7,7 +7,7 @@ Mirrors PythonAPI/src/fedempy/solver.py (``FedemSolver``: constructor,
 :677, ``solve_iteration`` :707, ``finish_step``, ``set_rhs_vector`` /
 ``add_rhs_vector`` :1100-1110, ``get_state_size`` :495, ``save_state`` :546,
 ``restart_from_state`` :398, ``set_ext_func`` :888, ``get_function`` :941,
-``get_function_ids`` :973, ``solve_window`` :429) with the same
+``get_function_ids`` :973, ``solve_window`` :429, ``solve_modes`` :742) with the same
 argument meaning and error behaviour (``FedemException`` on failure, the
 internal error flag blocks further calls after an error).
 """
@@ -178,6 +178,22 @@ class FedemSolver:
         more = self._solver.solveWindow(int(n_step), n_inc, n_in, n_out, fo, times, inp, out, 0, None,
                                         ctypes.byref(self.ierr))
         return (list(outv) if f_out is not None else None), more
+
+    def solve_modes(self, n_modes, dof_order=False, use_lapack=0):
+        """The n_modes lowest eigenmodes at the current state: (eigenvalues in
+        Hz, eigenvectors, success); (None, None, success) when *ierr != 0."""
+        self.__check_error("solve_modes")
+        dim = self.get_system_size(dofs=True) if dof_order else self.get_system_size()
+        e_val = np.zeros(int(n_modes))
+        e_vec = np.zeros(dim * int(n_modes))
+        P = ctypes.POINTER(ctypes.c_double)
+        ok = self._solver.solveEigenModes(int(n_modes), e_val.ctypes.data_as(P), e_vec.ctypes.data_as(P),
+                                          bool(dof_order), int(use_lapack), ctypes.byref(self.ierr))
+        if self.ierr.value != 0:
+            if self.ierr.value > 0:
+                self.ierr.value = 0
+            return None, None, ok
+        return list(e_val), [e_vec[dim * i:dim * (i + 1)] for i in range(int(n_modes))], ok
 
     def get_state_size(self):
         return self._solver.getStateSize()

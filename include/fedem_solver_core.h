@@ -16,9 +16,10 @@
  * getEquations, getSystemMatrix, getNewtonMatrix, getStiffness/Mass/
  * DampingMatrix, get/set/addRhsVector, getElementStiffnessMatrix, in-core
  * state save and restart, external functions (setExtFunc, evalFunc,
- * getFuncId, solveWindow), solverDone, solverClose).  Entry points for features
- * outside that path (eigenmodes, inverse analysis, strain/beam-force
- * recovery, part and gauge states) exist
+ * getFuncId, solveWindow), eigenmodes (solveEigenModes), solverDone,
+ * solverClose).  Entry points for features
+ * outside that path (inverse analysis, strain/beam-force recovery, part and
+ * gauge states) exist
  * so the library loads as a drop-in, and return the reference's failure value
  * (false, 0 or a negative status, with *ierr = -1 where present).
  */
@@ -96,7 +97,13 @@ bool solveNext(int* ierr);
 bool startStep(int* ierr);
 bool solveIteration(int* ierr, bool all);
 
-/* solverInterface.h:293, :309 -- eigenmodes and inverse analysis: unsupported. */
+/* solverInterface.h:293 -- the nmod lowest eigenmodes of K phi = lambda M phi at
+ * the current state (Lanczos on the GPU-factored stiffness matrix): eval in Hz
+ * (sqrt|lambda| / 2 pi), evec M-orthonormal, nmod columns in equation order or
+ * (dofOrder) DOF order.  *ierr = number of negative eigenvalues (+1 when the
+ * iteration did not converge every mode), < 0 on error; useLaPack is ignored.
+ * Between steps only.
+ * solverInterface.h:309 -- inverse analysis: unsupported. */
 bool solveEigenModes(const int nmod, double* eval, double* evec, bool dofOrder, int useLaPack, int* ierr);
 bool solveInverse(const double* x, const int* xeqs, const int* feqs, int ndis, int nfrs, int* ierr);
 

@@ -273,3 +273,51 @@ def test_solve_window_equals_step_by_step(gpu):
     outputs, more = b.solve_window(2, inputs=[1.0, 2.0], f_out=[7], xtimes=[0.5])  # too short times array
     assert not more and b.ierr.value == 1 - 2
     b.solver_done()
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_eigenmodes_match_a_dense_generalized_eigensolve(gpu, mixed):
+    """solveEigenModes (solverInterface.h:293): the 6 lowest modes of K phi =
+    lambda M phi at the initial state against scipy's dense generalized
+    eigensolver on the same K and M (getSystemMatrix 1 and 2); frequencies in
+    Hz, M-orthonormal vectors, DOF order with zeros at the clamp; the first
+    bending frequency near the Euler-Bernoulli value; stepping afterwards is
+    unchanged."""
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    from fedem_gb300 import models
+
+    fsi = _fsi(0.0)
+    s = _solver(OPTS, fsi, mixed)
+    n = s.get_system_size()
+    K, M = s.get_system_matrix(1), s.get_system_matrix(2)
+    lam, phi = scipy_linalg.eigh(K, M, subset_by_index=[0, 5])
+    ref = np.sqrt(lam) / (2.0 * np.pi)
+    f, vecs, ok = s.solve_modes(6)
+    assert ok and s.ierr.value == 0
+    f = np.array(f)
+    np.testing.assert_allclose(f, ref, rtol=1e-9)
+    V = np.array(vecs).T  # n x 6
+    np.testing.assert_allclose(V.T @ M @ V, np.eye(6), atol=1e-9)
+    # K phi - lambda M phi relative to K phi (the Ritz residual bound is 1e-9 in
+    # the M norm of K^-1 M, which K amplifies up to its condition number)
+    resid = np.abs(K @ V - (M @ V) * lam).max() / np.abs(K @ V).max()
+    assert resid < 1e-6, resid
+    # Euler-Bernoulli cantilever, first bending frequency (20 consistent-mass elements: within 1 %)
+    area, inertia, _, _ = models.pipe_section(0.1, 0.01)
+    L = N_EL * 0.25
+    f1 = 1.875104 ** 2 / (2 * np.pi) * np.sqrt(models.STEEL["E"] * inertia / (models.STEEL["rho"] * area * L ** 4))
+    assert abs(f[0] - f1) < 0.01 * f1, (f[0], f1)
+    fd, vd, ok = s.solve_modes(6, dof_order=True)
+    assert ok and len(vd[0]) == s.get_system_size(dofs=True)
+    np.testing.assert_allclose(np.array(fd), f, rtol=1e-12)
+    assert np.all(np.array(vd)[:, :6] == 0.0)  # the clamped triad
+    # the time steps after the eigenvalue analysis are those of a run without it
+    for _ in range(10):
+        assert s.solve_next()
+    after = _positions(s)
+    s.solver_done()
+    s2 = _solver(OPTS, fsi, mixed)
+    for _ in range(10):
+        s2.solve_next()
+    np.testing.assert_array_equal(after, _positions(s2))
+    s2.solver_done()
