@@ -207,7 +207,7 @@ template <typename T>
 __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase,
                                     const double* rhs, T* X, const T* W, int lane, const T* Lres, T* Wout,
                                     const T* Win = nullptr) {
-  const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
+  const int nr = d.fNrow[f], np = d.fNpiv[f];
   const int cg0 = d.cgOff[f], ncg = d.cgOff[f + 1] - cg0, nch = d.fNchild[f];
   const int cnt = nr * np;
   if (nr > 64 || ncg > 64 || (!Lres && cnt > capL)) return false;
@@ -247,18 +247,19 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
       if (src[u] >= 0 && (dst[u] >> 16) == c) v[dst[u] & 0xffff] += wv[u];
     __syncwarp();
   }
+  // the elimination with the rows in registers (lane r: rows r and r + 32), the
+  // pivot value of each step passed by a shuffle: no barrier between steps
+  T v0 = lane < nr ? v[lane] : T(0), v1 = lane + 32 < nr ? v[lane + 32] : T(0);
   for (int k = 0; k < np; ++k) {
-    const T yk = v[k];
-    __syncwarp();
-    for (int i = k + 1 + lane; i < nr; i += 32) v[i] -= L[i + (size_t)nr * k] * yk;
-    __syncwarp();
+    const T yk = __shfl_sync(0xffffffffu, k < 32 ? v0 : v1, k & 31);
+    const T* Lk = L + (size_t)nr * k;
+    if (lane > k && lane < nr) v0 -= Lk[lane] * yk;
+    if (lane + 32 > k && lane + 32 < nr) v1 -= Lk[lane + 32] * yk;
   }
-  for (int a = lane; a < nu; a += 32) Wout[a] = v[np + a];
-#pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int r = lane + 32 * u;
-    if (r < np) X[row[u]] = v[r] / L[r + (size_t)nr * r];
-  }
+  if (lane >= np && lane < nr) Wout[lane - np] = v0;
+  if (lane + 32 >= np && lane + 32 < nr) Wout[lane + 32 - np] = v1;
+  if (lane < np) X[row[0]] = v0 / L[lane + (size_t)nr * lane];
+  if (lane + 32 < np) X[row[1]] = v1 / L[(lane + 32) + (size_t)nr * (lane + 32)];
   return true;
 }
 
@@ -389,16 +390,32 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
   for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + __ldg(rows + r));
   copyAsyncWait();
   __syncwarp();
-  for (int k = lane; k < np; k += 32) {
-    T acc = xs[k];
-    for (int i = np; i < nr; ++i) acc -= L[i + (size_t)nr * k] * xs[i];
-    xs[k] = acc;
-  }
-  __syncwarp();
-  for (int j = np - 1; j > 0; --j) {
-    const T xj = xs[j];
-    for (int k = lane; k < j; k += 32) xs[k] -= L[j + (size_t)nr * k] * xj;
+  if (np <= 32) {
+    // one pivot per lane in a register; the back substitution passes each
+    // solved value by a shuffle (no barrier between steps)
+    T a = T(0);
+    if (lane < np) {
+      a = xs[lane];
+      for (int i = np; i < nr; ++i) a -= L[i + (size_t)nr * lane] * xs[i];
+    }
+    for (int j = np - 1; j > 0; --j) {
+      const T xj = __shfl_sync(0xffffffffu, a, j);
+      if (lane < j) a -= L[j + (size_t)nr * lane] * xj;
+    }
+    if (lane < np) xs[lane] = a;
     __syncwarp();
+  } else {
+    for (int k = lane; k < np; k += 32) {
+      T a = xs[k];
+      for (int i = np; i < nr; ++i) a -= L[i + (size_t)nr * k] * xs[i];
+      xs[k] = a;
+    }
+    __syncwarp();
+    for (int j = np - 1; j > 0; --j) {
+      const T xj = xs[j];
+      for (int k = lane; k < j; k += 32) xs[k] -= L[j + (size_t)nr * k] * xj;
+      __syncwarp();
+    }
   }
   for (int r = lane; r < np; r += 32) {
     const int row = rows[r];
