@@ -40,25 +40,60 @@ constexpr long long kSpinLimit = 1LL << 23;  // polls of a bounded wait (about 1
 // the unit L below it in the panel; the unscaled panel values of the update
 // rows (L d) are kept in the unused upper triangle (row k, column i) for the
 // rank-np pass.
+// a pivot counts as singular when |d_k| <= tolFactorize * |a_kk| (the FP32
+// factor tests in FP32, keeping the FP64 pipe free)
+__device__ inline bool singularPivot(float dk, float d0, double tol) { return !(fabsf(dk) > (float)tol * fabsf(d0)); }
+__device__ inline bool singularPivot(double dk, double d0, double tol) { return !(fabs(dk) > tol * fabs(d0)); }
+
 template <typename T>
 __device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int lane, double tolFact, int& neg,
                               bool& sing, T* Uout) {
-  for (int k = 0; k < np; ++k) {
-    const T dk = F[k + nr * k];
-    const bool bad = !(fabs((double)dk) > tolFact * fabs((double)diag0[k]));
-    sing |= bad;
-    if (dk < T(0)) ++neg;
-    const T inv = bad ? T(0) : T(1) / dk;
-    for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
-    __syncwarp();
-    for (int i = k + 1 + lane; i < nr; i += 32) {
-      const T fik = F[i + nr * k];
-      const int je = i < np - 1 ? i : np - 1;
-      for (int j = k + 1; j <= je; ++j) F[i + nr * j] -= fik * lcol[j];
-      if (i >= np) F[k + nr * i] = fik;
-      F[i + nr * k] = lcol[i];
+  if (np <= 32 && nr <= 64) {
+    // rows lane and lane + 32; the multipliers of the pivot rows (lanes below
+    // np) are passed by shuffles, one barrier per pivot
+    const int i0 = lane, i1 = lane + 32;
+    for (int k = 0; k < np; ++k) {
+      const T dk = F[k + nr * k];
+      const bool bad = singularPivot(dk, diag0[k], tolFact);
+      sing |= bad;
+      if (dk < T(0)) ++neg;
+      const T inv = bad ? T(0) : T(1) / dk;
+      const bool r0 = i0 > k && i0 < nr, r1 = i1 > k && i1 < nr;
+      const T f0 = r0 ? F[i0 + nr * k] : T(0), f1 = r1 ? F[i1 + nr * k] : T(0);
+      const T l0 = f0 * inv, l1 = f1 * inv;
+      for (int j = k + 1; j < np; ++j) {
+        const T lj = __shfl_sync(0xffffffffu, l0, j);
+        if (r0 && j <= i0) F[i0 + nr * j] -= f0 * lj;
+        if (r1) F[i1 + nr * j] -= f1 * lj;
+      }
+      if (r0) {
+        if (i0 >= np) F[k + nr * i0] = f0;
+        F[i0 + nr * k] = l0;
+      }
+      if (r1) {
+        if (i1 >= np) F[k + nr * i1] = f1;
+        F[i1 + nr * k] = l1;
+      }
+      __syncwarp();
     }
-    __syncwarp();
+  } else {
+    for (int k = 0; k < np; ++k) {
+      const T dk = F[k + nr * k];
+      const bool bad = singularPivot(dk, diag0[k], tolFact);
+      sing |= bad;
+      if (dk < T(0)) ++neg;
+      const T inv = bad ? T(0) : T(1) / dk;
+      for (int i = k + 1 + lane; i < nr; i += 32) lcol[i] = F[i + nr * k] * inv;
+      __syncwarp();
+      for (int i = k + 1 + lane; i < nr; i += 32) {
+        const T fik = F[i + nr * k];
+        const int je = i < np - 1 ? i : np - 1;
+        for (int j = k + 1; j <= je; ++j) F[i + nr * j] -= fik * lcol[j];
+        if (i >= np) F[k + nr * i] = fik;
+        F[i + nr * k] = lcol[i];
+      }
+      __syncwarp();
+    }
   }
   // update matrix, lower triangle packed column by column: entry e = lane + 32 q
   // is (row np + b + t, column np + b)
