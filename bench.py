@@ -41,8 +41,8 @@ ELEM_BYTES = 4040
 # DRAM bytes (read + write) of one launch on this workload (256 models), from
 # ncu captures of kForwardCascade<float> and of kFactorForwardCascade<float>
 # in an iteration where every model factors (profiles/)
-FORWARD_TRAFFIC_256 = 153.5e6
-FACTOR_TRAFFIC_256 = 294.7e6
+FORWARD_TRAFFIC_256 = 153.6e6
+FACTOR_TRAFFIC_256 = 307.4e6
 
 
 def forward_bytes(models, elem_bytes):
