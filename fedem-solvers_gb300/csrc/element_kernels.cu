@@ -591,22 +591,46 @@ __global__ void kAxialNewton(DevData d) {
 __global__ void kResidual(DevData d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
-  int m = d.eqModel[i];
-  int fl = d.m.flags[m];
+  // the list of the equation's first two contributions is read with the model's
+  // flags, before the activity test, to save a dependent round trip
+  const int m = d.eqModel[i];
+  const int k0 = d.eqPtr[i], k1 = d.eqPtr[i + 1];
+  const size_t s0 = k0 < k1 ? (size_t)d.eqSrc[k0] : 0, s1 = k0 + 1 < k1 ? (size_t)d.eqSrc[k0 + 1] : 0;
+  const int fl = d.m.flags[m];
   if (!(fl & FL_ACTIVE)) return;
   const size_t blk = (size_t)12 * d.nelTot, ablk = (size_t)6 * d.naxTot;
   double fs = 0.0, fd = 0.0, fi = 0.0, q = 0.0;
-  for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) {
-    size_t s = d.eqSrc[k];
-    if (s < blk) {
-      fs += d.Fel[s];
-      fd += d.Fel[s + blk];
-      fi += d.Fel[s + 2 * blk];
-      q += d.Fel[s + 3 * blk];
-    } else {  // axial spring/damper
-      fs += d.FelA[s - blk];
-      fd += d.FelA[s - blk + ablk];
+  // one contribution: element forces FS, FD, FI, Q, or FS, FD of an axial spring/damper
+  auto add = [&](double v0, double v1, double v2, double v3, bool el) {
+    fs += v0;
+    fd += v1;
+    if (el) {
+      fi += v2;
+      q += v3;
     }
+  };
+  auto load = [&](size_t s, double& v0, double& v1, double& v2, double& v3) {
+    const bool el = s < blk;
+    const double* b = el ? d.Fel + s : d.FelA + (s - blk);
+    const size_t st = el ? blk : ablk;
+    v0 = b[0];
+    v1 = b[st];
+    v2 = el ? b[2 * st] : 0.0;
+    v3 = el ? b[3 * st] : 0.0;
+    return el;
+  };
+  // equations of beam chains have one or two contributions: the loads of the first
+  // two are issued together; the sums keep the order of the list
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+  bool ea = false, eb = false;
+  if (k0 < k1) ea = load(s0, a0, a1, a2, a3);
+  if (k0 + 1 < k1) eb = load(s1, b0, b1, b2, b3);
+  if (k0 < k1) add(a0, a1, a2, a3, ea);
+  if (k0 + 1 < k1) add(b0, b1, b2, b3, eb);
+  for (int k = k0 + 2; k < k1; ++k) {
+    double c0, c1, c2, c3;
+    const bool ec = load((size_t)d.eqSrc[k], c0, c1, c2, c3);
+    add(c0, c1, c2, c3, ec);
   }
   q += d.qext[i];
   // forces set by an external process (newmarkRoutinesModule.f90:747-749, 792-794);
@@ -758,28 +782,65 @@ __global__ void __launch_bounds__(128) kNewtonBeam(DevData d) {
 }
 
 // CSR slot gather (deterministic segmented reduction over element contributions)
-__global__ void kCsrGather(DevData d) {
+// The block of kSlotBlock slots runs on kSlotBlock / 4 threads, four slots a thread.
+// Each CSR slot of a beam chain has one or two contributions, so the slot pointers,
+// the first two source indices and their values are loaded in three rounds with
+// every load of a round independent; longer lists continue one by one. The sum keeps
+// the order of the list (v = 0, then += each contribution).
+constexpr int kGatherSlotsPerThread = 4;
+
+__device__ __forceinline__ double gatherEntry(const DevData& d, int src, int64_t lim) {
+  return src < lim ? d.elMat[src] : d.elMatA[src - lim];
+}
+
+__global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather(DevData d) {
   // a block whose slots all belong to one model reads its flags once
   __shared__ int blockFlags;
   const int bm = d.slotBlockModel[blockIdx.x];
   if (threadIdx.x == 0) blockFlags = bm >= 0 ? d.m.flags[bm] : FL_TANGENT;
   __syncthreads();
   if (!(blockFlags & FL_TANGENT)) return;
-  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.nslotTot) return;
-  if (bm < 0 && !(d.m.flags[d.slotModel[s]] & FL_TANGENT)) return;
-  double v = 0.0;
+  constexpr int R = kGatherSlotsPerThread;
   const int64_t lim = (int64_t)144 * d.nelTot;
-  for (int k = d.slotPtr[s]; k < d.slotPtr[s + 1]; ++k) {
-    const int64_t src = d.slotSrc[k];
-    v += src < lim ? d.elMat[src] : d.elMatA[src - lim];
+  int64_t sl[R];
+  int p0[R], p1[R], at[R], i0[R], i1[R];
+  double c0[R], c1[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    sl[r] = (int64_t)blockIdx.x * kSlotBlock + r * (kSlotBlock / R) + threadIdx.x;
+    p0[r] = p1[r] = 0;
+    at[r] = -1;
+    if (sl[r] < d.nslotTot && (bm >= 0 || (d.m.flags[d.slotModel[sl[r]]] & FL_TANGENT))) {
+      p0[r] = d.slotPtr[sl[r]];
+      p1[r] = d.slotPtr[sl[r] + 1];
+      at[r] = d.slotAsm[sl[r]];
+    } else {
+      sl[r] = -1;
+    }
   }
-  d.csrVal[s] = v;
-  // front-ordered copy for the factorisation, in its precision
-  const int a = d.slotAsm[s];
-  if (a >= 0) {
-    if (d.asmVal32) d.asmVal32[a] = (float)v;
-    else d.asmVal64[a] = v;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    i0[r] = p0[r] < p1[r] ? d.slotSrc[p0[r]] : 0;
+    i1[r] = p0[r] + 1 < p1[r] ? d.slotSrc[p0[r] + 1] : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    c0[r] = p0[r] < p1[r] ? gatherEntry(d, i0[r], lim) : 0.0;
+    c1[r] = p0[r] + 1 < p1[r] ? gatherEntry(d, i1[r], lim) : 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (sl[r] < 0) continue;
+    double v = 0.0;
+    if (p0[r] < p1[r]) v += c0[r];
+    if (p0[r] + 1 < p1[r]) v += c1[r];
+    for (int k = p0[r] + 2; k < p1[r]; ++k) v += gatherEntry(d, d.slotSrc[k], lim);
+    d.csrVal[sl[r]] = v;
+    // front-ordered copy for the factorisation, in its precision
+    if (at[r] >= 0) {
+      if (d.asmVal32) d.asmVal32[at[r]] = (float)v;
+      else d.asmVal64[at[r]] = v;
+    }
   }
 }
 
@@ -1285,7 +1346,7 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
   if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
-  if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot, kSlotBlock), kSlotBlock, 0, s>>>(d);
+  if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot, kSlotBlock), kSlotBlock / kGatherSlotsPerThread, 0, s>>>(d);
 }
 void launchIncrement(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;

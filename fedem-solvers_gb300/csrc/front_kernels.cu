@@ -19,9 +19,11 @@ inline int blocksFor(long long n, int tpb = TPB) { return (int)((n + tpb - 1) / 
 __global__ void kRefineResidual(DevData d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
+  // the row's extent is read with the model index, before the activity test
+  const int64_t kb = d.rowPtr[i], ke = d.rowPtr[i + 1];
   if (!(d.m.flags[d.eqModel[i]] & FL_ACTIVE)) return;
   double s = 0.0;
-  for (int64_t k = d.rowPtr[i]; k < d.rowPtr[i + 1]; ++k) s += d.csrVal[k] * d.xref[d.colInd[k]];
+  for (int64_t k = kb; k < ke; ++k) s += d.csrVal[k] * d.xref[d.colInd[k]];
   d.rref[i] = d.del[i] - s;
 }
 
