@@ -35,9 +35,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Newton steps/s batched+served vs plain GPU at 1e-8 rel err; p50/p99 latency"
 UNIT = "Newton steps/s"
-# algorithmic bytes of the element pass per beam element and launch: K and M
-# (2 x 1152), frames 384, triads 192, velocities 192, fg 288 in; writes 576 out
-ELEM_BYTES = 4040
+# algorithmic bytes of the element pass after the increment, per beam element, on
+# this workload (compressed 26-value K and M, no damping, no gravity), triad data
+# counted once per triad (a chain has one triad per element):
+#   in:  model 4, triads 8, frame 96, reference points 12, offsets 72, relative
+#        frame 96, undeformed triad frames 192, stiffness scale 8, flags 2,
+#        K 208, M 208, triad position 96 + accelerations 48 + first DOF 4
+#   out: frame 96, deformation 96, FS, FI, FD, Q 4 x 96
+ELEM_BYTES = 1630
 # DRAM bytes (read + write) of one launch on this workload (256 models), from
 # ncu captures of kForwardCascade<float> and of kFactorForwardCascade<float>
 # in an iteration where every model factors (profiles/)
@@ -403,6 +408,7 @@ def main():
         roof_el = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                    "frac": achieved / hbm_peak, "traffic": None,
                    "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
+                   "note": "bound by the FP64 rate (FP64 pipe 84-88 % busy), not by HBM",
                    "bytes_per_element": ELEM_BYTES, "samples": nsamp}
     roof_fwd = None
     if nsamp > 0 and ms3[3] > 0:

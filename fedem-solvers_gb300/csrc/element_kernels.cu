@@ -19,6 +19,9 @@
 
 #include <cmath>
 
+#include <algorithm>
+#include <mutex>
+
 #include "kernels.h"
 
 namespace fgpu {
@@ -311,6 +314,10 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   for (int k = 0; k < 12; ++k) S[k] = d.supTr[(size_t)k * nel + e];
   int tri[2] = {d.elTri[e], d.elTri[nel + e]};
   double uld[12], uldd[12];
+  // the damping force is the only user of the local velocities (stiffness-proportional
+  // damping C, or the kDmp term of the pass after the increment)
+  const bool needUld =
+      !isStatic && (d.hasC[e] || (mode == EM_INC && d.hasVld[e] && d.m.dt[m] > 0.0));
   if (!isStatic) {
     const double* vs = mode == EM_PRED ? d.dk : d.urd;
     const double* as = mode == EM_PRED ? d.ak : d.urdd;
@@ -319,12 +326,15 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
       int d0 = d.triFirstDof[tri[n]];
 #pragma unroll
       for (int g = 0; g < 2; ++g) {
-        double v0 = vs[d0 + 3 * g], v1 = vs[d0 + 3 * g + 1], v2 = vs[d0 + 3 * g + 2];
         double a0 = as[d0 + 3 * g], a1 = as[d0 + 3 * g + 1], a2 = as[d0 + 3 * g + 2];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          uld[6 * n + 3 * g + r] = S[3 * r] * v0 + S[3 * r + 1] * v1 + S[3 * r + 2] * v2;
+        for (int r = 0; r < 3; ++r)
           uldd[6 * n + 3 * g + r] = S[3 * r] * a0 + S[3 * r + 1] * a1 + S[3 * r + 2] * a2;
+        if (needUld) {
+          double v0 = vs[d0 + 3 * g], v1 = vs[d0 + 3 * g + 1], v2 = vs[d0 + 3 * g + 2];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            uld[6 * n + 3 * g + r] = S[3 * r] * v0 + S[3 * r + 1] * v1 + S[3 * r + 2] * v2;
         }
       }
     }
@@ -793,53 +803,71 @@ __device__ __forceinline__ double gatherEntry(const DevData& d, int src, int64_t
   return src < lim ? d.elMat[src] : d.elMatA[src - lim];
 }
 
-__global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather(DevData d) {
-  // a block whose slots all belong to one model reads its flags once
-  __shared__ int blockFlags;
-  const int bm = d.slotBlockModel[blockIdx.x];
-  if (threadIdx.x == 0) blockFlags = bm >= 0 ? d.m.flags[bm] : FL_TANGENT;
-  __syncthreads();
-  if (!(blockFlags & FL_TANGENT)) return;
+// Grid-stride over the blocks of kSlotBlock slots with a grid of resident blocks only:
+// in iterations where few or no models update the tangent, the slot blocks of the
+// other models are skipped by a flag test (32 slot blocks per round of loads)
+// instead of a block launch each.
+__global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather(DevData d, int nSlotBlocks) {
   constexpr int R = kGatherSlotsPerThread;
   const int64_t lim = (int64_t)144 * d.nelTot;
-  int64_t sl[R];
-  int p0[R], p1[R], at[R], i0[R], i1[R];
-  double c0[R], c1[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    sl[r] = (int64_t)blockIdx.x * kSlotBlock + r * (kSlotBlock / R) + threadIdx.x;
-    p0[r] = p1[r] = 0;
-    at[r] = -1;
-    if (sl[r] < d.nslotTot && (bm >= 0 || (d.m.flags[d.slotModel[sl[r]]] & FL_TANGENT))) {
-      p0[r] = d.slotPtr[sl[r]];
-      p1[r] = d.slotPtr[sl[r] + 1];
-      at[r] = d.slotAsm[sl[r]];
-    } else {
-      sl[r] = -1;
+  const int lane = threadIdx.x & 31;
+  for (int b0 = blockIdx.x; b0 < nSlotBlocks; b0 += 32 * gridDim.x) {
+    // lane j of each warp tests slot block b0 + j * gridDim.x (its model's flags, or
+    // every slot's when the block spans several models); the ballot is the same in
+    // every warp of the block, which then works through the selected slot blocks
+    const int bj = b0 + lane * gridDim.x;
+    int bmj = -1;
+    bool sel = false;
+    if (bj < nSlotBlocks) {
+      bmj = d.slotBlockModel[bj];
+      sel = bmj < 0 || (d.m.flags[bmj] & FL_TANGENT);
     }
-  }
+    unsigned pending = __ballot_sync(0xffffffffu, sel);
+    while (pending) {
+      const int j = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const int b = b0 + j * (int)gridDim.x;
+      const int bm = __shfl_sync(0xffffffffu, bmj, j);
+      int64_t sl[R];
+      int p0[R], p1[R], at[R], i0[R], i1[R];
+      double c0[R], c1[R];
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    i0[r] = p0[r] < p1[r] ? d.slotSrc[p0[r]] : 0;
-    i1[r] = p0[r] + 1 < p1[r] ? d.slotSrc[p0[r] + 1] : 0;
-  }
+      for (int r = 0; r < R; ++r) {
+        sl[r] = (int64_t)b * kSlotBlock + r * (kSlotBlock / R) + threadIdx.x;
+        p0[r] = p1[r] = 0;
+        at[r] = -1;
+        if (sl[r] < d.nslotTot && (bm >= 0 || (d.m.flags[d.slotModel[sl[r]]] & FL_TANGENT))) {
+          p0[r] = d.slotPtr[sl[r]];
+          p1[r] = d.slotPtr[sl[r] + 1];
+          at[r] = d.slotAsm[sl[r]];
+        } else {
+          sl[r] = -1;
+        }
+      }
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    c0[r] = p0[r] < p1[r] ? gatherEntry(d, i0[r], lim) : 0.0;
-    c1[r] = p0[r] + 1 < p1[r] ? gatherEntry(d, i1[r], lim) : 0.0;
-  }
+      for (int r = 0; r < R; ++r) {
+        i0[r] = p0[r] < p1[r] ? d.slotSrc[p0[r]] : 0;
+        i1[r] = p0[r] + 1 < p1[r] ? d.slotSrc[p0[r] + 1] : 0;
+      }
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    if (sl[r] < 0) continue;
-    double v = 0.0;
-    if (p0[r] < p1[r]) v += c0[r];
-    if (p0[r] + 1 < p1[r]) v += c1[r];
-    for (int k = p0[r] + 2; k < p1[r]; ++k) v += gatherEntry(d, d.slotSrc[k], lim);
-    d.csrVal[sl[r]] = v;
-    // front-ordered copy for the factorisation, in its precision
-    if (at[r] >= 0) {
-      if (d.asmVal32) d.asmVal32[at[r]] = (float)v;
-      else d.asmVal64[at[r]] = v;
+      for (int r = 0; r < R; ++r) {
+        c0[r] = p0[r] < p1[r] ? gatherEntry(d, i0[r], lim) : 0.0;
+        c1[r] = p0[r] + 1 < p1[r] ? gatherEntry(d, i1[r], lim) : 0.0;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (sl[r] < 0) continue;
+        double v = 0.0;
+        if (p0[r] < p1[r]) v += c0[r];
+        if (p0[r] + 1 < p1[r]) v += c1[r];
+        for (int k = p0[r] + 2; k < p1[r]; ++k) v += gatherEntry(d, d.slotSrc[k], lim);
+        d.csrVal[sl[r]] = v;
+        // front-ordered copy for the factorisation, in its precision
+        if (at[r] >= 0) {
+          if (d.asmVal32) d.asmVal32[at[r]] = (float)v;
+          else d.asmVal64[at[r]] = v;
+        }
+      }
     }
   }
 }
@@ -1346,7 +1374,24 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
   if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
-  if (d.nslotTot > 0) kCsrGather<<<blocksFor(d.nslotTot, kSlotBlock), kSlotBlock / kGatherSlotsPerThread, 0, s>>>(d);
+  if (d.nslotTot <= 0) return;
+  // resident blocks of the device this launch runs on (queried once per device)
+  static int perSm[64] = {0}, sms[64] = {0};
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int bps = 0, nsm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && perSm[dev] == 0) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm[dev], kCsrGather, kSlotBlock / kGatherSlotsPerThread, 0);
+      cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (dev < 64) { bps = perSm[dev]; nsm = sms[dev]; }
+  }
+  const int nb = blocksFor(d.nslotTot, kSlotBlock);
+  const int grid = bps > 0 && nsm > 0 ? std::min(nb, bps * nsm) : nb;
+  kCsrGather<<<grid, kSlotBlock / kGatherSlotsPerThread, 0, s>>>(d, nb);
 }
 void launchIncrement(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;

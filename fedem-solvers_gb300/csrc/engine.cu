@@ -288,7 +288,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   d_.extRhs = alloc<double>(neq);
   d_.x64 = alloc<double>(neq); d_.xref = alloc<double>(neq); d_.rref = alloc<double>(neq); d_.x32 = alloc<float>(neq);
   {
-    // DOF chunks of at most 2048 DOFs, each inside one model
+    // DOF chunks of at most 2048 DOFs (eight per thread of a 256-thread block;
+    // 1024 and 4096 were measured slower), each inside one model
     const int CH = 2048;
     std::vector<int> cm, cs, ce, mco(nm), mnc(nm);
     for (int k = 0; k < nm; ++k) {
