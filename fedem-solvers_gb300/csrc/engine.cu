@@ -11,10 +11,14 @@
 // and replayed; models that are idle or in another phase early-exit on their
 // per-model flags, so models of uneven size and iteration count share launches.
 
+#include <atomic>
 #include <chrono>
+#include <thread>
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "engine.h"
@@ -68,6 +72,40 @@ cudaError_t put(T* dst, const std::vector<T>& src, cudaStream_t s) {
   t_putBytes += (long long)(src.size() * sizeof(T));
   return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s);
 }
+// fn(k) for every model k on the host's threads; each model writes its own
+// ranges of the batch arrays (offsets fixed beforehand), so the result does not
+// depend on the schedule
+template <typename F>
+void forEachModel(int nm, F fn) {
+  const int hw = (int)std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min(nm, hw > 0 ? hw : 1));
+  if (nt <= 1) {
+    for (int k = 0; k < nm; ++k) fn(k);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> pool;
+  pool.reserve(nt);
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (int k = next.fetch_add(1); k < nm; k = next.fetch_add(1)) fn(k);
+    });
+  for (auto& th : pool) th.join();
+}
+
+// setup trace: with FGPU_SETUP_TRACE set, each phase of the upload waits for the
+// stream and prints its host + device time to stderr
+struct SetupTrace {
+  bool on = std::getenv("FGPU_SETUP_TRACE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* phase, cudaStream_t s) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "fgpu setup %-24s %8.1f ms\n", phase, std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
 }  // namespace
 
 int Engine::upload(const std::vector<const HostModel*>& models, const EngineOptions& opt, std::string& err) {
@@ -77,6 +115,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   if (!opt_.fp32Factor) opt_.refineSweeps = 1;
   if (opt_.refineSweeps < 1) opt_.refineSweeps = 1;
   FG_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SetupTrace trace;
   const int nm = (int)models.size();
   // ---- global offsets --------------------------------------------------------
   modelTriOff_.assign(nm, 0);
@@ -109,6 +148,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   d_.naxTot = nax;
   d_.ntriTot = ntri; d_.ndofTot = ndof; d_.neqTot = neq; d_.nelTot = nel; d_.nslotTot = nslot;
   d_.nfrontTot = nfr;
+  trace.mark("offsets", stream_);
   // ---- per-model control -------------------------------------------------------
   DevModels& M = d_.m;
   M.n = nm;
@@ -166,6 +206,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   M.qsCount = alloc<int>(nm);
   if (put(M.stepLimit, stepLimit, stream_) != cudaSuccess) { err = "upload stepLimit"; return -902; }
 
+  trace.mark("control", stream_);
   // ---- triads, DOFs, equations ---------------------------------------------------
   std::vector<double> ur;
   ur.reserve(12 * (size_t)ntri);
@@ -311,30 +352,17 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   }
   d_.rhs32 = nullptr;
 
+  trace.mark("triads, DOFs, norms", stream_);
   // ---- elements (SoA) -------------------------------------------------------------
   auto soa = [&](int width, auto getter) {
     std::vector<double> v((size_t)width * nel);
-    for (int k = 0; k < nm; ++k) {
+    forEachModel(nm, [&](int k) {
       const HostModel& h = *models[k];
-      for (int e = 0; e < h.nel; ++e)
-        for (int c = 0; c < width; ++c) v[(size_t)c * nel + modelElOff_[k] + e] = getter(h, e, c);
-    }
+      for (int c = 0; c < width; ++c)
+        for (int e = 0; e < h.nel; ++e) v[(size_t)c * nel + modelElOff_[k] + e] = getter(h, e, c);
+    });
     return v;
   };
-  {
-    auto K = soa(144, [](const HostModel& h, int e, int c) { return h.K[144 * (size_t)e + c]; });
-    UPV(d_.K, double, K);
-  }
-  {
-    auto Mm = soa(144, [](const HostModel& h, int e, int c) { return h.M[144 * (size_t)e + c]; });
-    UPV(d_.M, double, Mm);
-  }
-  if (anyC) {
-    auto C = soa(144, [](const HostModel& h, int e, int c) { return h.C[144 * (size_t)e + c]; });
-    UPV(d_.C, double, C);
-  } else {
-    d_.C = alloc<double>(1);
-  }
   {
     auto fg = soa(36, [](const HostModel& h, int e, int c) { return h.fg[36 * (size_t)e + c]; });
     UPV(d_.fg, double, fg);
@@ -355,28 +383,33 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
                                    {8, 8}, {8, 10}, {9, 9},  {10, 10}, {11, 11}};
     bool inPat[144] = {false};
     for (auto& p : pat) inPat[p[0] + 12 * p[1]] = inPat[p[1] + 12 * p[0]] = true;
+    std::vector<uint8_t> modelSparse(nm, 1);
+    if (opt_.compressBeams)
+      forEachModel(nm, [&](int k) {
+        const HostModel& h = *models[k];
+        for (int e = 0; e < h.nel && modelSparse[k]; ++e)
+          for (int q = 0; q < 144; ++q) {
+            if (inPat[q]) continue;
+            if (h.K[144 * (size_t)e + q] != 0.0 || h.M[144 * (size_t)e + q] != 0.0 ||
+                (h.hasC[e] && h.C[144 * (size_t)e + q] != 0.0)) {
+              modelSparse[k] = 0;
+              break;
+            }
+          }
+      });
     bool sparse = opt_.compressBeams;
-    for (int k = 0; k < nm && sparse; ++k) {
-      const HostModel& h = *models[k];
-      for (int e = 0; e < h.nel && sparse; ++e)
-        for (int q = 0; q < 144 && sparse; ++q) {
-          if (inPat[q]) continue;
-          if (h.K[144 * (size_t)e + q] != 0.0 || h.M[144 * (size_t)e + q] != 0.0 ||
-              (h.hasC[e] && h.C[144 * (size_t)e + q] != 0.0))
-            sparse = false;
-        }
-    }
+    for (int k = 0; k < nm; ++k) sparse = sparse && modelSparse[k];
     d_.beamSparse = sparse ? 1 : 0;
     if (sparse) {
       auto pack = [&](const std::vector<double> HostModel::*mat) {
         std::vector<double> v((size_t)26 * nel);
-        for (int k = 0; k < nm; ++k) {
+        forEachModel(nm, [&](int k) {
           const HostModel& h = *models[k];
           const std::vector<double>& src = h.*mat;
-          for (int e = 0; e < h.nel; ++e)
-            for (int q = 0; q < 26; ++q)
+          for (int q = 0; q < 26; ++q)
+            for (int e = 0; e < h.nel; ++e)
               v[(size_t)q * nel + modelElOff_[k] + e] = src[144 * (size_t)e + pat[q][0] + 12 * pat[q][1]];
-        }
+        });
         return v;
       };
       auto K26 = pack(&HostModel::K);
@@ -391,7 +424,29 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       }
     }
   }
-  d_.N = alloc<double>(144 * (size_t)nel);
+  // full 12x12 matrices: read on the device only by batches that are not compressed
+  if (!d_.beamSparse) {
+    {
+      auto K = soa(144, [](const HostModel& h, int e, int c) { return h.K[144 * (size_t)e + c]; });
+      UPV(d_.K, double, K);
+    }
+    {
+      auto Mm = soa(144, [](const HostModel& h, int e, int c) { return h.M[144 * (size_t)e + c]; });
+      UPV(d_.M, double, Mm);
+    }
+    if (anyC) {
+      auto C = soa(144, [](const HostModel& h, int e, int c) { return h.C[144 * (size_t)e + c]; });
+      UPV(d_.C, double, C);
+    } else {
+      d_.C = alloc<double>(1);
+    }
+    d_.N = alloc<double>(144 * (size_t)nel);
+  } else {
+    d_.K = alloc<double>(1);
+    d_.M = alloc<double>(1);
+    d_.C = alloc<double>(1);
+    d_.N = alloc<double>(1);
+  }
   d_.elMat = alloc<double>(144 * (size_t)nel);
   d_.finit = alloc<double>(12 * (size_t)nel);
   d_.finitPrev = alloc<double>(12 * (size_t)nel);
@@ -400,7 +455,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     std::vector<int> elTri(2 * (size_t)nel), elRef(3 * (size_t)nel), elModel(nel);
     std::vector<double> ss(nel), kd(nel);
     std::vector<uint8_t> hc(nel), hv(nel);
-    for (int k = 0; k < nm; ++k) {
+    forEachModel(nm, [&](int k) {
       const HostModel& h = *models[k];
       for (int e = 0; e < h.nel; ++e) {
         int g = modelElOff_[k] + e;
@@ -412,10 +467,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         hc[g] = h.hasC[e];
         hv[g] = h.hasVld[e];
       }
-    }
+    });
     UPV(d_.elTri, int, elTri); UPV(d_.elRef, int, elRef); UPV(d_.elModel, int, elModel);
     UPV(d_.stifScl, double, ss); UPV(d_.kDmp, double, kd); UPV(d_.hasC, uint8_t, hc); UPV(d_.hasVld, uint8_t, hv);
   }
+  trace.mark("elements", stream_);
   // ---- axial springs and dampers ------------------------------------------------------
   {
     std::vector<uint8_t> kind(nax);
@@ -438,6 +494,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     d_.FelA = alloc<double>(12 * (size_t)nax);
     d_.elMatA = alloc<double>(36 * (size_t)nax);
   }
+  trace.mark("axial elements", stream_);
   // ---- CSR and gather maps -----------------------------------------------------------
   {
     if (ncontrib >= INT_MAX || 144LL * nel + 36LL * nax >= INT_MAX) {
@@ -445,42 +502,41 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       return -901;
     }
     std::vector<int64_t> rowPtr(neq + 1, 0);
-    std::vector<int> slotPtr(nslot + 1, 0), slotSrc;
-    std::vector<int> colInd, slotModel, eqPtr(neq + 1, 0), eqSrc;
-    colInd.reserve(nslot);
-    slotModel.reserve(nslot);
-    slotSrc.reserve(ncontrib);
-    eqSrc.reserve(neqc);
-    for (int k = 0; k < nm; ++k) {
+    std::vector<int> slotPtr(nslot + 1, 0), slotSrc(ncontrib);
+    std::vector<int> colInd(nslot), slotModel(nslot), eqPtr(neq + 1, 0), eqSrc(neqc);
+    forEachModel(nm, [&](int k) {
       const HostModel& h = *models[k];
       for (int i = 0; i < h.neq; ++i) {
         rowPtr[modelEqOff_[k] + i + 1] = modelSlotOff_[k] + h.rowPtr[i + 1];
         eqPtr[modelEqOff_[k] + i + 1] = (int)(eqContribOff[k] + h.eqPtr[i + 1]);
       }
+      const int64_t s0 = modelSlotOff_[k];
       for (size_t s = 0; s < h.colInd.size(); ++s) {
-        colInd.push_back(h.colInd[s] + modelEqOff_[k]);
-        slotModel.push_back(k);
-        slotPtr[modelSlotOff_[k] + s + 1] = contribOff[k] + h.slotPtr[s + 1];
+        colInd[s0 + s] = h.colInd[s] + modelEqOff_[k];
+        slotModel[s0 + s] = k;
+        slotPtr[s0 + s + 1] = (int)(contribOff[k] + h.slotPtr[s + 1]);
       }
+      int64_t o = contribOff[k];
       for (int src : h.slotSrc) {
         if (src < 144 * h.nel) {
           int e = src / 144, entry = src % 144;
-          slotSrc.push_back(entry * nel + modelElOff_[k] + e);
+          slotSrc[o++] = entry * nel + modelElOff_[k] + e;
         } else {  // axial element entry
           int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
-          slotSrc.push_back(144 * nel + entry * nax + modelAxOff[k] + a);
+          slotSrc[o++] = 144 * nel + entry * nax + modelAxOff[k] + a;
         }
       }
+      o = eqContribOff[k];
       for (int src : h.eqSrc) {
         if (src < 12 * h.nel) {
           int e = src / 12, loc = src % 12;
-          eqSrc.push_back(loc * nel + modelElOff_[k] + e);
+          eqSrc[o++] = loc * nel + modelElOff_[k] + e;
         } else {
           int a = (src - 12 * h.nel) / 6, loc = (src - 12 * h.nel) % 6;
-          eqSrc.push_back(12 * nel + loc * nax + modelAxOff[k] + a);
+          eqSrc[o++] = 12 * nel + loc * nax + modelAxOff[k] + a;
         }
       }
-    }
+    });
     UPV(d_.rowPtr, int64_t, rowPtr); UPV(d_.colInd, int, colInd); UPV(d_.slotPtr, int, slotPtr);
     UPV(d_.slotSrc, int, slotSrc); UPV(d_.slotModel, int, slotModel); UPV(d_.eqPtr, int, eqPtr);
     {
@@ -494,6 +550,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(d_.eqSrc, int, eqSrc);
     d_.csrVal = alloc<double>(nslot);
   }
+  trace.mark("CSR and gather maps", stream_);
   // ---- fronts ------------------------------------------------------------------------------
   {
     std::vector<int> npiv, nrow, parent, fmodel, nchild, nasmv, frontRows, childList, relIndex, asmPos;
@@ -525,24 +582,34 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     // children's update matrices: lower triangles packed column by column into one
     // segment per parent, children in order, with their positions in the parent front
     std::vector<int64_t> segOff(nfr, 0), uOffPacked(nfr, 0);
-    std::vector<int> segLen(nfr, 0), segPos;
+    std::vector<int> segLen(nfr, 0);
     int64_t nuPacked = 0;
     for (int f = 0; f < nfr; ++f) {
       segOff[f] = nuPacked;
       if (nrow[f] > 1024 || nchild[f] >= 2048) { err = "front too large for the packed update layout"; return -909; }
       for (int c = 0; c < nchild[f]; ++c) {
         const int ch = childList[childOffV[f] + c];
-        const int cu = nrow[ch] - npiv[ch];
-        const int* rel = &relIndex[relOffV[ch]];
+        const int64_t cu = nrow[ch] - npiv[ch];
         uOffPacked[ch] = nuPacked;
-        for (int b = 0; b < cu; ++b)
-          for (int a = b; a < cu; ++a) {
-            segPos.push_back((c << 20) | (rel[a] + nrow[f] * rel[b]));
-            ++nuPacked;
-          }
+        nuPacked += cu * (cu + 1) / 2;
       }
       segLen[f] = (int)(nuPacked - segOff[f]);
     }
+    // positions of the packed entries in their parent front, filled per model
+    std::vector<int> segPos(nuPacked);
+    forEachModel(nm, [&](int k) {
+      const int fEnd = k + 1 < nm ? frontOff[k + 1] : nfr;
+      for (int f = frontOff[k]; f < fEnd; ++f) {
+        int64_t o = segOff[f];
+        for (int c = 0; c < nchild[f]; ++c) {
+          const int ch = childList[childOffV[f] + c];
+          const int cu = nrow[ch] - npiv[ch];
+          const int* rel = &relIndex[relOffV[ch]];
+          for (int b = 0; b < cu; ++b)
+            for (int a = b; a < cu; ++a) segPos[o++] = (c << 20) | (rel[a] + nrow[f] * rel[b]);
+        }
+      }
+    });
     nu = nuPacked;
     uOffV = uOffPacked;
     pplan_.maxSeg = 1;
@@ -587,6 +654,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     UPV(d_.fAsmOff, int64_t, asmOffV);
     UPV(d_.frontRows, int, frontRows); UPV(d_.childList, int, childList); UPV(d_.relIndex, int, relIndex);
     UPV(d_.asmSlot, int64_t, asmSlot); UPV(d_.asmPos, int, asmPos);
+    trace.mark("front structure", stream_);
     {
       // per-front list of the children's update rows: W source index and (child
       // ordinal << 16 | row in this front), children in order
@@ -671,6 +739,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     for (size_t k = 0; k < order.size(); ++k) sortedTasks[k] = tasks[order[k]];
     int* dTasks = nullptr;
     UPV(dTasks, int, sortedTasks);
+    trace.mark("child gathers, leaves, tasks", stream_);
     pplan_.tasks = dTasks;
     pplan_.nTasks = (int)sortedTasks.size();
     // backward queue: fronts whose children are all leaves solve them inline;
@@ -729,6 +798,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     d_.errFlag = pplan_.errFlag;
   }
 #undef UPV
+  trace.mark("queues and counters", stream_);
   if (allocFailed_) { err = "out of device memory"; return -906; }
   FG_CHECK(cudaMallocHost(&hActive_, sizeof(int)));
   FG_CHECK(cudaMallocHost(&hStates_, sizeof(int) * (size_t)std::max(nm, 1)));
@@ -769,6 +839,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   uploadedBytes_ = t_putBytes;
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
+  trace.mark("state registry", stream_);
   return 0;
 }
 
@@ -1070,6 +1141,7 @@ int Engine::readActive() {
 }
 
 int Engine::initialState(std::string& err) {
+  SetupTrace trace;
   // staticEquilibriumModule.f90:50-437: iterate the models that asked for it
   launchStaticBegin(d_, dActive_, BackwardSeed{}, stream_);
   launchElements(d_, EM_STATIC_INIT, stream_);
@@ -1107,6 +1179,7 @@ int Engine::initialState(std::string& err) {
   FG_CHECK(cudaGetLastError());
   for (int k = 0; k < d_.m.n; ++k)
     if (modelState(k) == ST_ERROR) { err = "initial static equilibrium failed"; return -910; }
+  trace.mark("initial state", stream_);
   return 0;
 }
 

@@ -66,7 +66,7 @@ def build(verbose=False, force=False, ptxas_info=False):
                 print(o)
     objs = [os.path.join(obj_dir, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
     if force or jobs or not os.path.exists(LIB_PATH):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB_PATH] + objs)
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB_PATH] + objs + ["-lpthread"])
     return LIB_PATH
 
 
