@@ -553,32 +553,35 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   trace.mark("CSR and gather maps", stream_);
   // ---- fronts ------------------------------------------------------------------------------
   {
-    std::vector<int> npiv, nrow, parent, fmodel, nchild, nasmv, frontRows, childList, relIndex, asmPos;
-    std::vector<int64_t> rowOffV, lOffV, uOffV, wOffV, childOffV, relOffV, asmOffV, asmSlot;
-    for (int k = 0; k < nm; ++k) {
+    std::vector<int> npiv(nfr), nrow(nfr), parent(nfr), fmodel(nfr), nchild(nfr), nasmv(nfr), frontRows(nrows),
+        childList(nch), relIndex(nrel), asmPos(nasm);
+    std::vector<int64_t> rowOffV(nfr), lOffV(nfr), uOffV(nfr), wOffV(nfr), childOffV(nfr), relOffV(nfr),
+        asmOffV(nfr), asmSlot(nasm);
+    forEachModel(nm, [&](int k) {
       const HostModel& h = *models[k];
       for (size_t f = 0; f < h.fronts.size(); ++f) {
         const Front& fr = h.fronts[f];
-        npiv.push_back(fr.npiv);
-        nrow.push_back(fr.nrow);
-        parent.push_back(fr.parent >= 0 ? fr.parent + frontOff[k] : -1);
-        fmodel.push_back(k);
-        nchild.push_back(fr.nchild);
-        nasmv.push_back(fr.nasm);
-        rowOffV.push_back(fr.rowOff + rowsOff[k]);
-        lOffV.push_back(fr.lOff + lOff[k]);
-        uOffV.push_back(fr.uOff + uOff[k]);
-        wOffV.push_back(fr.wOff + wOff[k]);
-        childOffV.push_back(fr.childOff + childOff[k]);
-        relOffV.push_back(fr.relOff + relOff[k]);
-        asmOffV.push_back(fr.asmOff + asmOff[k]);
+        const size_t g = frontOff[k] + f;
+        npiv[g] = fr.npiv;
+        nrow[g] = fr.nrow;
+        parent[g] = fr.parent >= 0 ? fr.parent + frontOff[k] : -1;
+        fmodel[g] = k;
+        nchild[g] = fr.nchild;
+        nasmv[g] = fr.nasm;
+        rowOffV[g] = fr.rowOff + rowsOff[k];
+        lOffV[g] = fr.lOff + lOff[k];
+        uOffV[g] = fr.uOff + uOff[k];
+        wOffV[g] = fr.wOff + wOff[k];
+        childOffV[g] = fr.childOff + childOff[k];
+        relOffV[g] = fr.relOff + relOff[k];
+        asmOffV[g] = fr.asmOff + asmOff[k];
       }
-      for (int r : h.frontRows) frontRows.push_back(r + modelEqOff_[k]);
-      for (int c : h.childList) childList.push_back(c + frontOff[k]);
-      relIndex.insert(relIndex.end(), h.relIndex.begin(), h.relIndex.end());
-      for (int s : h.asmSlot) asmSlot.push_back((int64_t)s + modelSlotOff_[k]);
-      asmPos.insert(asmPos.end(), h.asmPos.begin(), h.asmPos.end());
-    }
+      for (size_t i = 0; i < h.frontRows.size(); ++i) frontRows[rowsOff[k] + i] = h.frontRows[i] + modelEqOff_[k];
+      for (size_t i = 0; i < h.childList.size(); ++i) childList[childOff[k] + i] = h.childList[i] + frontOff[k];
+      std::copy(h.relIndex.begin(), h.relIndex.end(), relIndex.begin() + relOff[k]);
+      for (size_t i = 0; i < h.asmSlot.size(); ++i) asmSlot[asmOff[k] + i] = (int64_t)h.asmSlot[i] + modelSlotOff_[k];
+      std::copy(h.asmPos.begin(), h.asmPos.end(), asmPos.begin() + asmOff[k]);
+    });
     // children's update matrices: lower triangles packed column by column into one
     // segment per parent, children in order, with their positions in the parent front
     std::vector<int64_t> segOff(nfr, 0), uOffPacked(nfr, 0);
