@@ -208,26 +208,32 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
 
   trace.mark("control", stream_);
   // ---- triads, DOFs, equations ---------------------------------------------------
-  std::vector<double> ur;
-  ur.reserve(12 * (size_t)ntri);
-  std::vector<int> triFirst, triNd, triModel, meqn, dofType, dofModel, eqModel;
-  std::vector<double> qext;
-  for (int k = 0; k < nm; ++k) {
+  std::vector<double> ur(12 * (size_t)ntri), qext(neq);
+  std::vector<int> triFirst(ntri), triNd(ntri), triModel(ntri), meqn(ndof), dofType(ndof), dofModel(ndof),
+      eqModel(neq);
+  for (int k = 0; k < nm; ++k)
+    if (models[k]->ur.size() != 12 * (size_t)models[k]->ntri || models[k]->qext.size() != (size_t)models[k]->neq) {
+      err = "inconsistent host model arrays";
+      return -902;
+    }
+  forEachModel(nm, [&](int k) {
     const HostModel& h = *models[k];
-    ur.insert(ur.end(), h.ur.begin(), h.ur.end());
+    std::copy(h.ur.begin(), h.ur.end(), ur.begin() + 12 * (size_t)modelTriOff_[k]);
     for (int t = 0; t < h.ntri; ++t) {
-      triFirst.push_back(h.triFirstDof[t] + modelDofOff_[k]);
-      triNd.push_back(h.triNdof[t]);
-      triModel.push_back(k);
+      const int g = modelTriOff_[k] + t;
+      triFirst[g] = h.triFirstDof[t] + modelDofOff_[k];
+      triNd[g] = h.triNdof[t];
+      triModel[g] = k;
     }
     for (int i = 0; i < h.ndof; ++i) {
-      meqn.push_back(h.meqn[i] >= 0 ? h.meqn[i] + modelEqOff_[k] : h.meqn[i]);
-      dofType.push_back(h.dofType[i]);
-      dofModel.push_back(k);
+      const int g = modelDofOff_[k] + i;
+      meqn[g] = h.meqn[i] >= 0 ? h.meqn[i] + modelEqOff_[k] : h.meqn[i];
+      dofType[g] = h.dofType[i];
+      dofModel[g] = k;
     }
-    for (int i = 0; i < h.neq; ++i) eqModel.push_back(k);
-    qext.insert(qext.end(), h.qext.begin(), h.qext.end());
-  }
+    for (int i = 0; i < h.neq; ++i) eqModel[modelEqOff_[k] + i] = k;
+    std::copy(h.qext.begin(), h.qext.end(), qext.begin() + modelEqOff_[k]);
+  });
   // external function channels of every model (values set by the caller, zero at start)
   modelExtOff_.assign(nm, 0);
   int nextTot = 0;
