@@ -247,7 +247,7 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
   const int cnt = nr * np;
   if (nr > 64 || ncg > 64 || (!Lres && cnt > capL)) return false;
   const int* rows = d.frontRows + d.fRowOff[f];
-  // round 2: independent loads (the L block asynchronously into shared memory)
+  // second round of loads: independent loads (the L block asynchronously into shared memory)
   if (!Lres) {
     const T* Lg = Lbase + d.fLOff[f];
     for (int k = lane; k < cnt; k += 32) copyAsync(Ls + k, Lg + k);
@@ -260,7 +260,7 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
     src[u] = r < ncg ? __ldg(d.cgSrc + cg0 + r) : -1;
     dst[u] = r < ncg ? __ldg(d.cgDst + cg0 + r) : 0;
   }
-  // round 3: values through the indices
+  // third round of loads: values through the indices
   double b[2];
   T wv[2];
 #pragma unroll
