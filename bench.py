@@ -10,14 +10,18 @@ tangent assembly and factorisation when updated, solve, update, norms).
 
 value: Newton iterations of all models / device time of the batched run,
        state already resident in HBM (restored device-to-device between steps).
-e2e:   the same through the C ABI from host buffers: upload (fgpu_batch_create),
-       run, download of every triad position, per step.
-Also reported: the plain per-model FP64 GPU path on a sample of models, the
-max relative displacement error of the mixed path against the FP64 path, the
-CPU oracle on a bounded sample (cpu_baseline), sampled phase roofline, clocks.
+e2e:   the same through the C ABI from host buffers, per step: model set-up
+       from the text (host threads), upload (fgpu_batch_create), run, download
+       of every triad position.
+Also reported: the batched plain FP64 path, the plain per-model FP64 GPU path
+on a sample of models, the mixed path's error against the FP64 path, the CPU
+oracle over the whole workload (cpu_baseline, and every model's final state
+compared with both GPU paths), phase rooflines, clocks, the served leg.
 
 --impl reference: the CPU oracle (restatement of the reference algorithm; the
-reference itself does not build here) on a bounded sample with all host cores.
+reference itself does not build here) on the same workload and boundary: the
+timed steps together are one full run of every model, set-up included, on all
+host threads.
 """
 import argparse
 import json
@@ -78,11 +82,11 @@ def parse():
     ap.add_argument("--sim-steps", type=int, default=500)
     ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=24, help="models timed on the plain FP64 per-model path")
-    ap.add_argument("--cpu-sample-steps", type=int, default=40)
     ap.add_argument("--no-extras", action="store_true", help="skip plain/error/cpu/served legs (profiling runs)")
     ap.add_argument("--timed-only", action="store_true", help="one timed run, no warm-up, e2e or extras (ncu)")
     ap.add_argument("--fp64", action="store_true", help="time the batched plain FP64 path instead of mixed")
     ap.add_argument("--error-only", action="store_true", help="of the extras, run only the mixed-vs-FP64 check")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the full CPU oracle run (parity + cpu_baseline)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
@@ -90,19 +94,32 @@ def parse():
     return ap.parse_args()
 
 
+def rank_env():
+    """(rank, world size, local rank) from the launcher's environment."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
+    """One process per GPU: the rank's device is LOCAL_RANK, selected in the
+    solver library's own CUDA runtime (fgpu_set_device) before anything is
+    created; the process group (for the timing max and the sums) is NCCL."""
+    rank, world, local = rank_env()
     if world <= 1:
-        return None, 0, 1
+        return None, 0, 1, local
     import torch
     import torch.distributed as dist
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     dist.init_process_group("nccl")
-    return dist, rank, world
+    return dist, rank, world, local
+
+
+def rank_device(local, lib=None):
+    """Selects this rank's GPU in the solver library; returns (ordinal, PCI bus id)."""
+    from fedem_gb300.batch import set_device
+
+    return set_device(local, lib)
 
 
 def shard(cases, rank, world):
@@ -116,6 +133,18 @@ def shard(cases, rank, world):
         if r == rank:
             mine.append(k)
     return sorted(mine)
+
+
+def workload_config(args, cases):
+    """The `config` of both arms: the same workload and the same timing boundary."""
+    n_el = sum(c[2] for c in cases)
+    return {"workload": f"{args.models} beam models (10-4000 elements, log-uniform, +/-20 % properties) x "
+                        f"{args.sim_steps} HHT-alpha steps (alpha -0.1, dt 1 ms, Newton tolerance 1e-8)",
+            "models": args.models, "time_steps_per_model": args.sim_steps, "elements": n_el,
+            "e2e_boundary": "model text and options in, final triad positions out: model set-up (parse, "
+                            "element matrices, equation numbering, symbolic analysis) and the whole run inside "
+                            "the timed region",
+            "l2": "inputs larger than L2 (element matrices and state of all models ~%.2f GB)" % (n_el * 5200 / 1e9)}
 
 
 class ClockSampler:
@@ -143,7 +172,7 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, index=None):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -151,7 +180,9 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+        if not vis.isdigit():
+            vis = str(index if index is not None else 0)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -182,25 +213,38 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_oracle_rate(cases, sample_steps, threads):
-    """Oracle Newton iterations/s over the first `sample_steps` steps of every model."""
+def oracle_full_run(cases, threads):
+    """The CPU oracle over the whole workload: every model from its text to its
+    end time (set-up inside the timed region, as in the e2e legs), one model per
+    host thread at a time, largest first.  Returns (seconds, Newton iterations,
+    final triad positions per model, iterations per model)."""
     from oracle.oracle import OracleModel
 
-    def one(case):
-        fsi, opts, _ = case
-        o = OracleModel(fsi, opts)
-        for _ in range(sample_steps):
-            if not o.solve_next():
-                break
-        it = o.iterations()
+    order = sorted(range(len(cases)), key=lambda k: -cases[k][2])
+    urs, its, scale = [None] * len(cases), [0] * len(cases), [0.0] * len(cases)
+
+    def one(k):
+        o = OracleModel(cases[k][0], cases[k][1])
+        o.run_all()
+        urs[k] = o.triads().copy()
+        its[k] = o.iterations()
+        scale[k] = o.max_displacement()
         o.close()
-        return it
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        iters = sum(ex.map(one, cases))
+        list(ex.map(one, order))
     dt = time.perf_counter() - t0
-    return iters / dt, iters, dt
+    return dt, sum(its), urs, its, scale
+
+
+def rel_disp_error(a, c, x0, scale=None):
+    """max |a - c| over the triad positions / the displacement scale: the
+    given one (the largest displacement over the run), else max |c - x0|."""
+    import numpy as np
+
+    denom = max(float(scale if scale is not None else np.abs(c - x0).max()), 1e-300)
+    return float(np.abs(a - c).max()) / denom
 
 
 def served_leg(args):
@@ -246,39 +290,92 @@ def served_leg(args):
 
 
 def run_reference(args, dist, rank, world):
-    """The CPU oracle on a bounded sample of the same workload, all host threads."""
+    """The reference arm: the CPU oracle (the FP64 restatement of the reference
+    algorithm; the reference itself does not build here) on the same workload
+    and config as the GPU arm, all host threads.  Bench step k advances every
+    model through time steps [k w, (k + 1) w), w = ceil(steps / K), so the K
+    timed steps together are exactly one full run of the workload; each model's
+    set-up (parse, element matrices, skyline structure) is inside the first
+    step, as model set-up is inside the GPU arm's e2e region."""
+    import numpy as np
+
     from fedem_gb300 import models
+    from oracle.oracle import OracleModel
 
     if rank != 0:
         return
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     cases = models.batch_c4(args.models, seed=4, steps=args.sim_steps)
     threads = os.cpu_count() or 1
-    steps = max(1, args.cpu_sample_steps // 4)
+    # untimed warm-up: a few steps of the smallest models
+    small = sorted(range(len(cases)), key=lambda k: cases[k][2])[:min(8, len(cases))]
     for _ in range(args.warmup):
-        cpu_oracle_rate(cases[:8], 2, threads)
-    rates, tot_it, tot_t = [], 0, 0.0
-    for _ in range(args.steps):
-        r, it, dt = cpu_oracle_rate(cases, steps, threads)
-        rates.append(r)
-        tot_it += it
-        tot_t += dt
+        def warm(k):
+            o = OracleModel(cases[k][0], cases[k][1])
+            for _ in range(3):
+                o.solve_next()
+            o.close()
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(warm, small))
+    K = max(1, args.steps)
+    window = int(math.ceil(args.sim_steps / K))
+    order = sorted(range(len(cases)), key=lambda k: -cases[k][2])
+    objs = [None] * len(cases)
+    live = [True] * len(cases)
+
+    def advance(k):
+        if not live[k]:
+            return 0
+        if objs[k] is None:
+            objs[k] = OracleModel(cases[k][0], cases[k][1])
+        o = objs[k]
+        it0 = o.iterations()
+        for _ in range(window):
+            if not o.solve_next():
+                live[k] = False
+                break
+        return o.iterations() - it0
+
+    tot_it, tot_t = 0, 0.0
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for _ in range(K):
+            t0 = time.perf_counter()
+            tot_it += sum(ex.map(advance, order))
+            tot_t += time.perf_counter() - t0
+    for o in objs:
+        if o is not None:
+            o.close()
     value = tot_it / tot_t
-    sample = f"all {args.models} models, first {steps} time steps each, per bench step"
+    sample = (f"all {args.models} models, {window} time steps of each per bench step: the {K} timed steps are "
+              f"one full {args.sim_steps}-step run of the workload ({tot_it} Newton iterations, {tot_t:.1f} s), "
+              f"model set-up inside the first step; {threads} host threads, one model per thread at a time")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator of the 256-model beam batch)",
-            "config": {"workload": f"{args.models} beam models x {args.sim_steps} HHT steps (bounded sample)",
-                       "sample": sample},
+            "config": workload_config(args, cases),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+def backward_bytes(models, elem_bytes):
+    """Algorithmic bytes of one back substitution over all fronts: the L block
+    (nrow x npiv), the row list, the solution values of all rows gathered, the
+    pivots' solution written in the solve precision and in FP64."""
+    import numpy as np
+
+    total = 0
+    for m in models:
+        _, info = m.symbolic()
+        npiv, nrow = info[:, 0].astype(np.int64), info[:, 1].astype(np.int64)
+        total += int((elem_bytes * nrow * npiv + 4 * nrow + elem_bytes * nrow + (elem_bytes + 8) * npiv).sum())
+    return total
+
+
 def main():
     args = parse()
-    dist, rank, world = dist_setup()
+    dist, rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, dist, rank, world)
         if dist:
@@ -288,20 +385,25 @@ def main():
 
     import fedem_gb300
     from fedem_gb300 import models
-    from fedem_gb300.batch import Batch, Model
+    from fedem_gb300.batch import Batch, create_models
 
-    fedem_gb300.load_library()
+    lib = fedem_gb300.load_library()
+    dev, bus = rank_device(local, lib)
+    print(f"rank {rank}: solver device {dev} ({bus})", file=sys.stderr, flush=True)
     cases_all = models.batch_c4(args.models, seed=4, steps=args.sim_steps)
     mine = shard(cases_all, rank, world)
     cases = [cases_all[k] for k in mine]
+    threads = os.cpu_count() or 1
     t_setup = time.perf_counter()
-    mods = [Model(f, o) for f, o, _ in cases]
+    mods = create_models(cases, threads)
     setup_s = time.perf_counter() - t_setup
     n_el = sum(m.nel for m in mods)
 
     # ---- device-resident timed runs (mixed precision, batched) ----------------------
     mixed = not args.fp64
     b = Batch(mods, mixed=mixed, sweeps=args.sweeps)
+    if b.device() != dev:
+        raise RuntimeError(f"batch on device {b.device()}, rank {rank} selected {dev}")
     b.snapshot()
     if args.timed_only:
         args.warmup, args.steps, args.no_extras = 0, 1, True
@@ -325,7 +427,7 @@ def main():
         kernels = st["kernels_per_iteration"]
         batched += st["batched_iterations"]
         failed += st["models_failed"]
-    clocks_info = clocks.stop()
+    clocks_info = clocks.stop(dev)
     if dist:
         import torch
 
@@ -337,18 +439,20 @@ def main():
     else:
         dev_s_max, iters_tot, tsteps_tot = dev_s, float(iters), float(tsteps)
     value = iters_tot / dev_s_max
-    nsamp, ms3, el_s = b.phase_timings()
+    nsamp, ms5, el_s = b.phase_timings()
     final_mixed = b.all_triads().copy()
+    iters_mixed = [b.info(k)["iterations"] for k in range(len(mods))]
     # the dominant kernel timed alone (every model factoring), after the timed runs
     fac_ms, fac_bytes = b.time_factor(reps=10) if mixed and not args.timed_only else (0.0, 0.0)
     b.close()
 
-    # ---- e2e through the C ABI from host buffers ------------------------------------
+    # ---- e2e through the C ABI from host buffers: set-up, upload, run, download --------
     e2e_iters, e2e_s, h2d, d2h = 0, 0.0, 0, 0
     out = np.zeros(12 * sum(m.ntri for m in mods))
     for k in range(0 if args.timed_only else args.steps):
         t0 = time.perf_counter()
-        be = Batch(mods, mixed=mixed, sweeps=args.sweeps)
+        me = create_models(cases, threads)
+        be = Batch(me, mixed=mixed, sweeps=args.sweeps)
         st = be.run()
         be.all_triads(out)
         e2e_s += time.perf_counter() - t0
@@ -356,25 +460,69 @@ def main():
         h2d = st["h2d_bytes"]
         d2h = out.nbytes
         be.close()
+        for m in me:
+            m.close()
     e2e_value = e2e_iters / e2e_s if e2e_s > 0 else None
 
     extras = {}
+    x0s = []
+    for m in mods:
+        nt = m.ntri
+        x0s.append(np.stack([np.arange(nt) * 0.25, np.zeros(nt), np.zeros(nt)], 1))
+
+    def split(flat):
+        out_, off = [], 0
+        for m in mods:
+            out_.append(flat[off:off + 12 * m.ntri].reshape(m.ntri, 4, 3)[:, 3, :])
+            off += 12 * m.ntri
+        return out_
+
     if (not args.no_extras or args.error_only) and rank == 0 and mixed:
-        # ---- accuracy of the mixed path against the plain FP64 path ------------------
+        # ---- the batched plain FP64 path: its throughput and the mixed path's error --------
         bf = Batch(mods, mixed=False)
+        bf.snapshot()
         bf.run()
         final_fp64 = bf.all_triads().copy()
+        iters_fp64 = [bf.info(k)["iterations"] for k in range(len(mods))]
+        bf.restore()
+        stf = bf.run()
         bf.close()
-        off, worst = 0, 0.0
-        for m, (fsi, opts, n) in zip(mods, cases):
-            nt = m.ntri
-            a = final_mixed[off:off + 12 * nt].reshape(nt, 4, 3)[:, 3, :]
-            c = final_fp64[off:off + 12 * nt].reshape(nt, 4, 3)[:, 3, :]
-            x0 = np.stack([np.arange(nt) * 0.25, np.zeros(nt), np.zeros(nt)], 1)
-            denom = max(np.abs(c - x0).max(), 1e-300)
-            worst = max(worst, float(np.abs(a - c).max() / denom))
-            off += 12 * nt
-        extras["max_rel_disp_err_mixed_vs_fp64"] = worst
+        extras["batched_fp64"] = {"value": stf["newton_iterations"] / (stf["device_us"] * 1e-6), "unit": UNIT,
+                                  "note": "same batch, plain FP64 fronts and one solve per iteration, device time"}
+        extras["speedup_mixed_vs_batched_fp64"] = value / extras["batched_fp64"]["value"]
+        pm, pf = split(final_mixed), split(final_fp64)
+        errs = [rel_disp_error(a, c, x0) for a, c, x0 in zip(pm, pf, x0s)]
+        extras["max_rel_disp_err_mixed_vs_fp64"] = max(errs)
+        if not args.no_oracle and not args.error_only:
+            # ---- the CPU oracle over the whole workload: parity of every model + cpu_baseline
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+            c_dt, c_it, c_urs, c_its, c_scale = oracle_full_run(cases, threads)
+            e64 = [rel_disp_error(a, c[:, :, 3], x0, sc) for a, c, x0, sc in zip(pf, c_urs, x0s, c_scale)]
+            emx = [rel_disp_error(a, c[:, :, 3], x0, sc) for a, c, x0, sc in zip(pm, c_urs, x0s, c_scale)]
+            f64 = [rel_disp_error(a, c[:, :, 3], x0) for a, c, x0 in zip(pf, c_urs, x0s)]
+            fmx = [rel_disp_error(a, c[:, :, 3], x0) for a, c, x0 in zip(pm, c_urs, x0s)]
+            extras["parity_vs_oracle"] = {
+                "models": len(mods),
+                "max_rel_disp_err_fp64_vs_oracle": max(e64),
+                "worst_model_fp64": int(np.argmax(e64)),
+                "max_rel_disp_err_mixed_vs_oracle": max(emx),
+                "worst_model_mixed": int(np.argmax(emx)),
+                "models_fp64_over_1e-10": int(sum(e > 1e-10 for e in e64)),
+                "models_mixed_over_1e-8": int(sum(e > 1e-8 for e in emx)),
+                "models_fp64_iterations_differ": int(sum(a != c for a, c in zip(iters_fp64, c_its))),
+                "models_mixed_iterations_differ": int(sum(a != c for a, c in zip(iters_mixed, c_its))),
+                "definition": "final triad positions after all steps: max |gpu - oracle| / the model's largest "
+                              "triad displacement over the run (oracle)",
+                "final_state_normalised": {"max_fp64": max(f64), "max_mixed": max(fmx),
+                                           "definition": "the same over max |oracle - x0| of the final state, "
+                                                         "which is small for models that end near a zero of "
+                                                         "their oscillation"},
+                "per_model_rel_err_fp64": [float("%.3g" % e) for e in e64],
+                "per_model_rel_err_mixed": [float("%.3g" % e) for e in emx]}
+            extras["cpu_baseline"] = {"value": c_it / c_dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                      "sample": f"the full workload: all {len(cases)} models, all "
+                                                f"{args.sim_steps} time steps, set-up included ({c_it} Newton "
+                                                f"iterations, {c_dt:.1f} s), one model per thread"}
     if not args.no_extras and rank == 0:
         # ---- plain per-model FP64 GPU path on a sample --------------------------------
         idx = np.linspace(0, len(mods) - 1, min(args.plain_sample, len(mods))).astype(int)
@@ -391,36 +539,41 @@ def main():
                                           "sample": f"{len(idx)} of {len(mods)} models run one at a time"}
         extras["speedup_vs_plain"] = value / plain_rate
         extras["speedup_vs_plain_time_steps"] = (tsteps_tot / dev_s_max) / (p_ts / p_s)
-        # ---- CPU oracle on a bounded sample ---------------------------------------------
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-        threads = os.cpu_count() or 1
-        c_rate, c_it, c_dt = cpu_oracle_rate(cases, args.cpu_sample_steps, threads)
-        extras["cpu_baseline"] = {"value": c_rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                  "sample": f"all {len(cases)} models, first {args.cpu_sample_steps} "
-                                            f"time steps each ({c_it} Newton iterations, {c_dt:.1f} s)"}
         # ---- served: Poisson request stream with continuous batching ----------------------
         extras["served"] = served_leg(args)
 
     hbm_peak, peak_kind = measured_peaks()
     roof, roof_el = None, None
-    if nsamp > 0 and ms3[0] > 0:
-        achieved = el_s * ELEM_BYTES / (ms3[0] * 1e-3) / 1e9
+    if nsamp > 0 and ms5[0] > 0:
+        achieved = el_s * ELEM_BYTES / (ms5[0] * 1e-3) / 1e9
         roof_el = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                    "frac": achieved / hbm_peak, "traffic": None,
                    "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
                    "note": "bound by the FP64 rate (FP64 pipe 84-88 % busy), not by HBM",
                    "bytes_per_element": ELEM_BYTES, "samples": nsamp}
+    E = 4 if mixed else 8
     roof_fwd = None
-    if nsamp > 0 and ms3[3] > 0:
+    if nsamp > 0 and ms5[3] > 0:
         # one forward elimination of the refinement solve (sampled inside the run)
-        fb = forward_bytes(mods, 4)
-        t_fwd = ms3[3] * 1e-3 / nsamp
+        fb = forward_bytes(mods, E)
+        t_fwd = ms5[3] * 1e-3 / nsamp
         achieved = fb / t_fwd / 1e9
         traffic = FORWARD_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
         roof_fwd = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                     "frac": achieved / hbm_peak, "traffic": traffic,
                     "kernel": "kForwardCascade<float> (forward elimination, all fronts)",
                     "algorithmic_bytes_per_launch": fb, "launch_ms": t_fwd * 1e3, "peak_source": peak_kind,
+                    "samples": nsamp}
+    roof_bwd = None
+    if nsamp > 0 and ms5[4] > 0:
+        bb = backward_bytes(mods, E)
+        t_bwd = ms5[4] * 1e-3 / nsamp
+        achieved = bb / t_bwd / 1e9
+        roof_bwd = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "traffic": None,
+                    "kernel": "kBackwardQueue (back substitution of the first solve, all fronts)",
+                    "algorithmic_bytes_per_launch": bb, "launch_ms": t_bwd * 1e3, "peak_source": peak_kind,
+                    "note": "latency-bound like the factor: queue hand-offs along the assembly trees",
                     "samples": nsamp}
     if fac_ms > 0:
         # the dominant kernel: the factorisation fused with the first forward
@@ -440,27 +593,26 @@ def main():
         roof = roof_el
     phases = None
     if nsamp > 0:
-        phases = {"elements": ms3[0] / nsamp, "factor_and_first_forward": ms3[1] / nsamp,
-                  "other_solve": ms3[2] / nsamp, "second_forward": ms3[3] / nsamp}
+        phases = {"elements": ms5[0] / nsamp, "factor_and_first_forward": ms5[1] / nsamp,
+                  "other_solve": ms5[2] / nsamp, "second_forward": ms5[3] / nsamp,
+                  "first_backward": ms5[4] / nsamp}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if mixed else "f64",
                 "data": "synthetic (seeded generator of the 256-model beam batch)",
-                "config": {"workload": f"{args.models} beam models (10-4000 elements, log-uniform) x "
-                                       f"{args.sim_steps} HHT-alpha steps, batched " +
-                                       (f"mixed precision (FP32 fronts + FP64 refinement, {args.sweeps} "
-                                        f"solves/iteration)" if mixed else "plain FP64"),
-                           "elements": n_el, "models_on_rank0": len(mods), "l2": "inputs larger than L2 "
-                           "(element matrices and state of all models ~%.2f GB)" % (n_el * 5200 / 1e9),
-                           "host_setup_s": setup_s},
+                "config": workload_config(args, cases_all),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "time_steps_per_s": tsteps_tot / dev_s_max,
                 "newton_iterations_per_time_step": iters_tot / max(tsteps_tot, 1.0),
                 "gpu_launches": kernels * batched, "kernels_per_batched_iteration": kernels,
-                "batched_iterations": batched, "models_failed": failed,
+                "batched_iterations": batched, "models_failed": failed, "models_on_rank0": len(mods),
+                "host_setup_s": setup_s, "host_threads": threads, "device": {"ordinal": dev, "pci_bus_id": bus},
                 "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof,
-                "roofline_elements": roof_el, "roofline_forward": roof_fwd, "phase_ms_per_iteration": phases}
+                "roofline_elements": roof_el, "roofline_forward": roof_fwd, "roofline_backward": roof_bwd,
+                "phase_ms_per_iteration": phases,
+                "value_definition": "Newton iterations of all models / device time of the batched mixed run, "
+                                    "state resident in HBM (restored device-to-device between steps)"}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

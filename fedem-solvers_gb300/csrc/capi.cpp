@@ -2,6 +2,7 @@
 // (src/vpmSolver/solverInterface.h, one model per process) and the batched
 // fgpu_* API.  Both drive the same GPU engine; there is no CPU solver path.
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -28,6 +29,31 @@ int fail(int code, const std::string& msg) {
   g_lastError = msg;
   return code;
 }
+
+// The device fgpu_set_device chose for the engines created from now on (-1:
+// the calling thread's current device).  The library links its own CUDA
+// runtime, so a device selected through another runtime (a framework's) is not
+// seen here: callers on several GPUs must name theirs with fgpu_set_device.
+std::atomic<int> g_device{-1};
+
+int selectDevice(std::string& err) {
+  const int dev = g_device.load();
+  if (dev < 0) return 0;
+  cudaError_t e = cudaSetDevice(dev);
+  if (e != cudaSuccess) {
+    err = std::string("cudaSetDevice failed: ") + cudaGetErrorString(e);
+    return -960;
+  }
+  return 0;
+}
+
+// Makes an engine's device current for the rest of an entry point (each
+// thread has its own current device in the CUDA runtime).
+struct OnDevice {
+  explicit OnDevice(int dev) {
+    if (dev >= 0) cudaSetDevice(dev);
+  }
+};
 
 // ---------------------------------------------------------------------------
 // legacy singleton (solverInterface.C:49 keeps the same kind of global state)
@@ -130,11 +156,18 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
   EngineOptions opt;
   opt.fp32Factor = hasFlag(argc, argv, "gpuMixed");
   opt.refineSweeps = opt.fp32Factor ? 4 : 1;
+  if ((rc = selectDevice(err))) return fail(rc, err);
   s->engine = std::make_unique<Engine>();
   std::vector<const HostModel*> ms{s->model.get()};
   rc = s->engine->upload(ms, opt, err);
   if (!rc) rc = s->engine->initialState(err);
   if (rc) return fail(rc, err);
+  if (s->engine->modelState(0) == ST_ERROR) {  // the initial static equilibrium failed
+    const int st = s->engine->modelStatus(0);
+    return fail((st & SS_SINGULAR) ? -3 : -1,
+                (st & SS_SINGULAR) ? "singular system matrix in the initial static equilibrium"
+                                   : "the initial static equilibrium failed");
+  }
   if (stateData && ndat > 0) {  // restart from an in-core state array (saveState of the same model)
     if ((size_t)ndat * sizeof(double) < s->engine->stateBytes()) return fail(-2, "state array too short");
     if (s->engine->restoreStateFrom(stateData)) return fail(-3, "restoring the state failed");
@@ -146,6 +179,7 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
 // solverInterface.h:87 -- the engine's mutable state from a saveState array
 // (results database options are not part of this path and are ignored)
 int restartFromState(const double* stateData, const int ndat, const int) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !stateData) return fail(-1, "no model or no state data");
   const size_t bytes = g_core->engine->stateBytes();
   if ((size_t)ndat * sizeof(double) < bytes) return fail(-2, "state array too short");
@@ -167,6 +201,7 @@ bool solveWindow(int nStep, int nInc, int nIn, int nOut, const int* fOut, const 
   int lerr = 0;
   int& e = ierr ? *ierr : lerr;
   e = 0;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || g_core->ierr) {
     e = g_core ? g_core->ierr : -1;
     return false;
@@ -193,6 +228,7 @@ bool solveWindow(int nStep, int nInc, int nIn, int nOut, const int* fOut, const 
 
 // solverInterface.h:118 -- doubles needed by saveState
 int getStateSize(void) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return 0;
   return (int)((g_core->engine->stateBytes() + sizeof(double) - 1) / sizeof(double));
 }
@@ -203,6 +239,7 @@ int getGagesSize(void) { return 0; }
 // solverInterface.h:156 -- the mutable state (positions, velocities, frames,
 // forces, step and iteration counters) into an in-core array
 bool saveState(double* stateData, const int ndat) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !stateData || g_core->inStep) return false;
   if ((size_t)ndat * sizeof(double) < g_core->engine->stateBytes()) return false;
   return g_core->engine->saveStateTo(stateData) == 0;
@@ -218,6 +255,7 @@ bool getRespVars(const double*, const int*, double*, const int, const int) { ret
 
 bool solveNext(int* ierr) {
   if (ierr) *ierr = 0;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) {
     if (ierr) *ierr = -1;
     return false;
@@ -246,6 +284,7 @@ bool startStep(int* ierr) {
   int lerr = 0;
   int& e = ierr ? *ierr : lerr;
   e = 0;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || g_core->ierr) {
     e = g_core ? g_core->ierr : -1;
     return false;
@@ -271,6 +310,7 @@ bool solveIteration(int* ierr, bool all) {
   int lerr = 0;
   int& e = ierr ? *ierr : lerr;
   e = 0;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || g_core->ierr) {
     e = g_core ? g_core->ierr : -1;
     return false;
@@ -315,6 +355,7 @@ bool solveEigenModes(const int nmod, double* eval, double* evec, bool dofOrder, 
   int lerr = 0;
   int& e = ierr ? *ierr : lerr;
   e = 0;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || g_core->ierr || !eval) {
     e = g_core ? (g_core->ierr ? g_core->ierr : -1) : -1;
     return false;
@@ -362,11 +403,13 @@ void solverClose(void) { g_core.reset(); }
 // solverInterface.h:342 -- value of external function channel funcId (1-based)
 // for the next step; false when the model has no such channel
 bool setExtFunc(int funcId, double value) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return false;
   return g_core->engine->setExtValue(0, funcId - 1, value) == 0;
 }
 
 double getTime(bool nextStep, int* ierr) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) {
     if (ierr) *ierr = -1;
     return 0.0;
@@ -380,6 +423,7 @@ double getTime(bool nextStep, int* ierr) {
 // (solverModule.f90:1558-1600: a negative increment or one above maxInc is an
 // error, one below minInc is raised to it)
 bool setTime(double nextTime) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || g_core->inStep) return false;
   const Control& c = g_core->model->ctl;
   const double dt = nextTime - g_core->engine->modelTime(0);
@@ -395,6 +439,7 @@ bool setTime(double nextTime) {
 double evalFunc(int uid, const char* tag, double x, int* ierr) {
   int lerr = 0;
   int& e = ierr ? *ierr : lerr;
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) {
     e = -999;  // outside model scope
     return 0.0;
@@ -422,6 +467,7 @@ double evalFunc(int uid, const char* tag, double x, int* ierr) {
 }
 // solverInterface.h:398 -- user id of the first engine with the tag, -1 if none
 int getFuncId(const char* tag) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return -999;
   if (!tag) return -1;
   const HostModel& m = *g_core->model;
@@ -431,6 +477,7 @@ int getFuncId(const char* tag) {
 }
 
 int getEquations(int bid, int* meqn) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return 0;
   const HostModel& m = *g_core->model;
   int t = triadIndex(m, bid);
@@ -440,6 +487,7 @@ int getEquations(int bid, int* meqn) {
 }
 
 int getStateVar(int bid, double* var) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return 0;
   const HostModel& m = *g_core->model;
   int t = triadIndex(m, bid);
@@ -451,6 +499,7 @@ int getStateVar(int bid, double* var) {
 }
 
 int getSystemSize(bool dofs) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return 0;
   return dofs ? g_core->model->ndof : g_core->model->neq;
 }
@@ -515,6 +564,7 @@ static void assembleSystemMatrix(int iMat, double* Smat) {
 }
 
 bool getSystemMatrix(double* Smat, int iMat) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !Smat || iMat < 0 || iMat > 3) return false;
   const HostModel& m = *g_core->model;
   if (iMat > 0) {
@@ -534,6 +584,7 @@ bool getMassMatrix(double* Mmat) { return getSystemMatrix(Mmat, 2); }
 bool getDampingMatrix(double* Cmat) { return getSystemMatrix(Cmat, 3); }
 
 bool getElementStiffnessMatrix(double* Kmat, int bid) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core) return false;
   const HostModel& m = *g_core->model;
   for (int e = 0; e < m.nel; ++e)
@@ -547,6 +598,7 @@ bool getElementStiffnessMatrix(double* Kmat, int bid) {
 // solverInterface.h:472 -- iVec < 5: the current right-hand side of the
 // linearised system (solverModule.f90:1834-1849), 5: the external load vector
 bool getRhsVector(double* Rvec, int iVec) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !Rvec) return false;
   g_core->engine->getEqVector(0, iVec == 5 ? 3 : 5, Rvec);
   return true;
@@ -554,10 +606,12 @@ bool getRhsVector(double* Rvec, int iVec) {
 // solverInterface.h:478-484 -- replace / add to the right-hand side of the
 // iteration assembled by startStep or solveIteration
 bool setRhsVector(const double* Rvec) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !Rvec || !g_core->inStep) return false;
   return g_core->engine->setRhs(0, Rvec, false) == 0;
 }
 bool addRhsVector(const double* Rvec) {
+  OnDevice onDev(g_core ? g_core->engine->device() : -1);
   if (!g_core || !Rvec || !g_core->inStep) return false;
   return g_core->engine->setRhs(0, Rvec, true) == 0;
 }
@@ -631,7 +685,8 @@ int fgpu_batch_create(int n, fgpu_model* const* models, int mixed, int sweeps, f
   opt.fp32Factor = mixed != 0;
   opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 2 : 1);
   std::string err;
-  int rc = b->engine.upload(b->models, opt, err);
+  int rc = selectDevice(err);
+  if (!rc) rc = b->engine.upload(b->models, opt, err);
   if (!rc) rc = b->engine.initialState(err);
   if (rc) return fail(rc, err);
   *out = b.release();
@@ -642,6 +697,7 @@ void fgpu_batch_destroy(fgpu_batch* b) { delete b; }
 
 int fgpu_batch_run(fgpu_batch* b, long long maxBatched, long long* s8) {
   if (!b) return fail(-1, "null batch");
+  OnDevice onDev(b->engine.device());
   RunStats st;
   b->engine.setStepLimit(1LL << 62);
   int rc = b->engine.run(maxBatched > 0 ? maxBatched : (1LL << 40), &st);
@@ -660,6 +716,7 @@ int fgpu_batch_run(fgpu_batch* b, long long maxBatched, long long* s8) {
 int fgpu_batch_model_info(fgpu_batch* b, int k, int* state, int* status, double* time, long long* steps,
                           long long* iters) {
   if (!b || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad model index");
+  OnDevice onDev(b->engine.device());
   if (state) *state = b->engine.modelState(k);
   if (status) *status = b->engine.modelStatus(k);
   if (time) *time = b->engine.modelTime(k);
@@ -670,12 +727,14 @@ int fgpu_batch_model_info(fgpu_batch* b, int k, int* state, int* status, double*
 
 int fgpu_batch_get_triads(fgpu_batch* b, int k, double* ur) {
   if (!b || !ur || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   b->engine.getTriadUr(k, ur);
   return 0;
 }
 
 long long fgpu_batch_get_all_triads(fgpu_batch* b, double* ur) {
   if (!b || !ur) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   long long off = 0;
   for (int k = 0; k < b->engine.numModels(); ++k) off += 12LL * b->engine.getTriadUr(k, ur + off);
   return off;
@@ -683,57 +742,74 @@ long long fgpu_batch_get_all_triads(fgpu_batch* b, double* ur) {
 
 int fgpu_batch_get_newton_values(fgpu_batch* b, int k, double* vals) {
   if (!b || !vals || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   b->engine.getCsrValues(k, vals);
   return 0;
 }
 
 int fgpu_batch_get_vector(fgpu_batch* b, int k, int which, double* v) {
   if (!b || !v || k < 0 || k >= b->engine.numModels() || which < 0 || which > 5) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   b->engine.getEqVector(k, which, v);
   return 0;
 }
 
 int fgpu_batch_get_norms(fgpu_batch* b, int k, double* n18) {
   if (!b || !n18 || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   b->engine.getNorms(k, n18);
   return 0;
 }
 
 int fgpu_batch_norms_noalloc(fgpu_batch* b, int k, double* n18) {
   if (!b || !n18 || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   std::string err;
   int rc = normsNoAlloc(b->engine.devData(), k, b->engine.normChunkOffset(k), b->engine.normChunkCount(k),
-                        b->engine.stream(), n18, err);
+                        b->engine.device(), b->engine.stream(), n18, err);
   return rc ? fail(rc, err) : 0;
 }
 
 int fgpu_batch_step(fgpu_batch* b, int k, int* state) {
   if (!b || k < 0 || k >= b->engine.numModels()) return fail(-1, "bad model index");
+  OnDevice onDev(b->engine.device());
   int rc = b->engine.advanceOneStep(k, state);
   return rc ? fail(rc, "step failed") : 0;
 }
 
 int fgpu_batch_snapshot(fgpu_batch* b) {
   if (!b) return fail(-1, "null batch");
+  OnDevice onDev(b->engine.device());
   int rc = b->engine.snapshot();
   return rc ? fail(rc, "snapshot failed") : 0;
 }
 
 int fgpu_batch_restore(fgpu_batch* b) {
   if (!b) return fail(-1, "null batch");
+  OnDevice onDev(b->engine.device());
   int rc = b->engine.restore();
   return rc ? fail(rc, "restore failed (no snapshot?)") : 0;
 }
 
 long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset) {
   if (!b || !ms4) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   long long n = b->engine.phaseTimings(ms4, elems);
   if (reset) b->engine.resetPhaseTimings();
   return n;
 }
 
+long long fgpu_batch_phase_timings_n(fgpu_batch* b, double* ms, int n, long long* elems, int reset) {
+  if (!b || !ms || n < 1 || n > 5) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  long long k = b->engine.phaseTimings(ms, elems, n);
+  if (reset) b->engine.resetPhaseTimings();
+  return k;
+}
+
 int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2) {
   if (!b || !out2 || reps < 1) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
   return b->engine.timeFactor(reps, out2, out2 + 1);
 }
 
@@ -743,7 +819,11 @@ int fgpu_server_create(double budget, int mixed, int sweeps, int maxModels, int 
   EngineOptions opt;
   opt.fp32Factor = mixed != 0;
   opt.refineSweeps = sweeps > 0 ? sweeps : (mixed ? 2 : 1);
-  auto* s = new fgpu_server{Server((size_t)(budget > 0 ? budget : 64.0e9), opt, maxModels, 4)};
+  std::string err;
+  if (int rc = selectDevice(err)) return fail(rc, err);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto* s = new fgpu_server{Server((size_t)(budget > 0 ? budget : 64.0e9), opt, maxModels, 4, dev)};
   s->srv.setBatchingWindow(minBatch, maxWait);
   *out = s;
   return 0;
@@ -792,6 +872,38 @@ int fgpu_server_result(fgpu_server* s, int id, double* ur) {
   std::memcpy(ur, r.ur.data(), sizeof(double) * r.ur.size());
   return 0;
 }
+
+int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag) {
+  if (!b || spins < 1) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  int rc = b->engine.probeWaitTimeout(spins, flag);
+  return rc ? fail(rc, "wait probe failed") : 0;
+}
+
+int fgpu_set_device(int ordinal) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return fail(-960, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (ordinal < 0 || ordinal >= n)
+    return fail(-961, "device ordinal " + std::to_string(ordinal) + " outside 0.." + std::to_string(n - 1));
+  e = cudaSetDevice(ordinal);
+  if (e != cudaSuccess) return fail(-962, std::string("cudaSetDevice failed: ") + cudaGetErrorString(e));
+  g_device.store(ordinal);
+  return 0;
+}
+
+int fgpu_get_device(int* ordinal, char* pciBusId, int len) {
+  int dev = g_device.load();
+  if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) return fail(-960, "no CUDA device");
+  if (ordinal) *ordinal = dev;
+  if (pciBusId && len > 0) {
+    cudaError_t e = cudaDeviceGetPCIBusId(pciBusId, len, dev);
+    if (e != cudaSuccess) return fail(-963, std::string("cudaDeviceGetPCIBusId failed: ") + cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+int fgpu_batch_device(const fgpu_batch* b) { return b ? b->engine.device() : fail(-1, "null batch"); }
 
 const char* fgpu_last_error(void) { return g_lastError.c_str(); }
 

@@ -1122,7 +1122,8 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
   if (threadIdx.x < NPART) {
     const int k = threadIdx.x;
     double x = sh[0][k];
-    for (int ww = 1; ww < CHUNK_TPB / 32; ++ww) x = (k <= 6) ? x + sh[ww][k] : fmax(x, sh[ww][k]);
+    for (int ww = 1; ww < CHUNK_TPB / 32; ++ww)
+      x = (k <= 6) ? x + sh[ww][k] : __longlong_as_double((long long)umax64(absBits(x), absBits(sh[ww][k])));
     d.partial[(size_t)c * NPART + k] = x;
   }
 }
@@ -1142,7 +1143,8 @@ __global__ void kControl(DevData d) {
     acc = nc > 0 ? d.partial[(size_t)c0 * NPART + lane] : 0.0;
     for (int c = 1; c < nc; ++c) {
       double x = d.partial[(size_t)(c0 + c) * NPART + lane];
-      acc = (lane <= 6) ? acc + x : fmax(acc, x);
+      // maxima (and the NaN flag) as |x| bit patterns: a NaN stays in the norm
+      acc = (lane <= 6) ? acc + x : __longlong_as_double((long long)umax64(absBits(acc), absBits(x)));
     }
   }
   double v[NPART];

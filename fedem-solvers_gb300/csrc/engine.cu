@@ -35,6 +35,7 @@ namespace fgpu {
   } while (0)
 
 Engine::~Engine() {
+  cudaSetDevice(device_);
   if (graphExec_) cudaGraphExecDestroy(graphExec_);
   if (graph_) cudaGraphDestroy(graph_);
   if (stream_) cudaStreamSynchronize(stream_);
@@ -112,6 +113,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   hm_ = models;
   opt_ = opt;
   t_putBytes = 0;
+  FG_CHECK(cudaGetDevice(&device_));
   if (!opt_.fp32Factor) opt_.refineSweeps = 1;
   if (opt_.refineSweeps < 1) opt_.refineSweeps = 1;
   FG_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -920,14 +922,14 @@ int Engine::timeFactor(int reps, double* msPerLaunch, double* bytes) {
   return 0;
 }
 
-long long Engine::phaseTimings(double* ms4, long long* elems) {
-  for (int k = 0; k < 4; ++k) ms4[k] = phaseMs_[k];
+long long Engine::phaseTimings(double* ms, long long* elems, int n) {
+  for (int k = 0; k < n && k < 5; ++k) ms[k] = phaseMs_[k];
   if (elems) *elems = phaseElems_;
   return phaseSamples_;
 }
 
 void Engine::resetPhaseTimings() {
-  phaseMs_[0] = phaseMs_[1] = phaseMs_[2] = phaseMs_[3] = 0.0;
+  phaseMs_[0] = phaseMs_[1] = phaseMs_[2] = phaseMs_[3] = phaseMs_[4] = 0.0;
   phaseSamples_ = phaseElems_ = 0;
 }
 
@@ -958,7 +960,9 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
     if (sweep == 1 && timedForward) recordPhase(ev_[5], s);
     if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
     if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
+    if (sweep == 0 && timedForward) recordPhase(ev_[7], s);
     launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
+    if (sweep == 0 && timedForward) recordPhase(ev_[8], s);
   }
 }
 
@@ -1186,9 +1190,29 @@ int Engine::initialState(std::string& err) {
   }
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
-  for (int k = 0; k < d_.m.n; ++k)
-    if (modelState(k) == ST_ERROR) { err = "initial static equilibrium failed"; return -910; }
+  // a model whose initial equilibrium failed (singular, NaN, no convergence)
+  // stays in its error state with its status bits; the others go on
   trace.mark("initial state", stream_);
+  return 0;
+}
+
+// A bounded wait that nothing ends: one warp of the back-substitution queue
+// kernel waits for a queue slot that is never filled, with `spins` polls.
+// Returns the error flag the wait set (1 when it ran out).  Test hook for the
+// failure path: afterwards every active model of the engine fails with
+// SS_TIMEOUT at its next convergence test.
+int Engine::probeWaitTimeout(long long spins, int* flag) {
+  int* q = nullptr;
+  if (cudaMalloc(&q, sizeof(int) * 8) != cudaSuccess) return -955;
+  const int init[8] = {-1, 0, 0, 0, 0, 0, 1, 0};  // queue slot 0 empty; ctr = {take 0, fill 0, total 1}
+  cudaMemcpyAsync(q, init, sizeof(init), cudaMemcpyHostToDevice, stream_);
+  launchBackwardWaitProbe(d_, pplan_, q, q + 4, spins, stream_);
+  int f = 0;
+  cudaMemcpyAsync(&f, pplan_.errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  const cudaError_t e = cudaStreamSynchronize(stream_);
+  cudaFree(q);
+  if (e != cudaSuccess) return -956;
+  if (flag) *flag = f;
   return 0;
 }
 
@@ -1227,6 +1251,8 @@ int Engine::run(long long maxBatched, RunStats* stats) {
       float t3 = 0.0f;
       if (opt_.refineSweeps > 1 && cudaEventElapsedTime(&t3, ev_[5], ev_[6]) == cudaSuccess)
         phaseMs_[3] += t3;
+      float t4 = 0.0f;
+      if (cudaEventElapsedTime(&t4, ev_[7], ev_[8]) == cudaSuccess) phaseMs_[4] += t4;
       phaseElems_ += *hActiveEl_;
       ++phaseSamples_;
     }

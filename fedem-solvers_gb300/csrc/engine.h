@@ -49,6 +49,9 @@ class Engine {
   const int* chunkStates() const { return hStates_; }
   // Device bytes this engine allocated.
   size_t deviceBytes() const { return deviceBytes_; }
+  // The CUDA device the engine was uploaded to (the calling thread's current
+  // device at upload); every later call on the engine must run with it current.
+  int device() const { return device_; }
   // Sum of Newton iterations over all models (blocking read).
   long long totalIterations();
   // Advances model `m` by exactly one time step (other models may advance too).
@@ -110,15 +113,18 @@ class Engine {
   // Phase timings sampled with CUDA events inside the captured iteration:
   // phase 0 = element pass after the increment, 1 = factorisation with the
   // first forward elimination, 2 = the rest of the solves, 3 = the forward
-  // elimination of the second solve (mixed-precision batches; else 0).
-  // Returns samples; ms[4] = summed milliseconds, elems = summed active elements.
-  long long phaseTimings(double* ms4, long long* activeElems);
+  // elimination of the second solve (mixed-precision batches; else 0),
+  // 4 = the back substitution of the first solve.
+  // Returns samples; ms[n] (n <= 5) = summed milliseconds, elems = summed active elements.
+  long long phaseTimings(double* ms, long long* activeElems, int n = 4);
   // Times `reps` launches of the factorisation fused with the first forward
   // elimination with every model factoring (CUDA events on the engine stream);
   // the flags, status and pivot counters are restored afterwards, the factors
   // and solve vectors are scratch.  *bytes: algorithmic bytes of one launch.
   int timeFactor(int reps, double* msPerLaunch, double* bytes);
   void resetPhaseTimings();
+  // Test hook: a bounded wait of `spins` polls that nothing ends (see engine.cu).
+  int probeWaitTimeout(long long spins, int* flag);
 
  private:
   template <typename T>
@@ -161,7 +167,7 @@ class Engine {
   void recordPhase(cudaEvent_t ev, cudaStream_t s);
   char* backup_ = nullptr;
   // phase timing events (recorded as external event nodes inside the graph)
-  cudaEvent_t ev_[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_[9] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   long long* dActiveEl_ = nullptr;
   long long* hActiveEl_ = nullptr;
   cudaEvent_t evRun_[2] = {nullptr, nullptr};
@@ -170,7 +176,8 @@ class Engine {
   cudaEvent_t evChunk_ = nullptr;
   bool chunkPending_ = false;
   size_t deviceBytes_ = 0;
-  double phaseMs_[4] = {0, 0, 0, 0};
+  int device_ = 0;
+  double phaseMs_[5] = {0, 0, 0, 0, 0};
   long long phaseSamples_ = 0, phaseElems_ = 0;
 };
 

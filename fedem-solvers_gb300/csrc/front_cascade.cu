@@ -30,7 +30,6 @@
 namespace fgpu {
 namespace {
 
-constexpr long long kSpinLimit = 1LL << 23;  // polls of a bounded wait (about 1-2 s)
 
 // Partial LDL^T of a front, blocked: the pivot panel (all rows, the np
 // pivot columns) is factored right-looking within the panel, one row per lane;
@@ -482,7 +481,8 @@ __device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL
 // ctr: [0] next slot to take, [1] next free slot, [2] slot total.
 template <typename T>
 __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
-                               const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize) {
+                               const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize,
+                               long long spinLimit) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
@@ -496,7 +496,7 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
       long long spins = 0;
       while ((f = *(volatile const int*)(queue + slot)) < 0) {
         __nanosleep(32);
-        if (++spins > kSpinLimit) {
+        if (++spins > spinLimit) {
           atomicOr(errFlag, 1);
           ok = 0;
           break;
@@ -633,15 +633,25 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
     allowBigSmem(kBackwardQueue<float>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<float>, 32 * wpb, sm, needed);
     kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, queue, ctr, p.bwInline,
-                                                      p.errFlag, acc, fin);
+                                                      p.errFlag, acc, fin, p.spinLimit);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
     allowBigSmem(kBackwardQueue<double>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<double>, 32 * wpb, sm, needed);
     kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline,
-                                                        p.errFlag, acc, fin);
+                                                        p.errFlag, acc, fin, p.spinLimit);
   }
+}
+
+void launchBackwardWaitProbe(const DevData& d, const PersistentPlan& p, int* queue, int* ctr, long long spins,
+                             cudaStream_t s) {
+  // one warp; it waits on slot 0 and touches no front (the wait gives up first)
+  const int capL = stagingCapacity(p, sizeof(double));
+  const size_t sm = (size_t)(p.maxRow + capL) * sizeof(double);
+  allowBigSmem(kBackwardQueue<double>, sm);
+  kBackwardQueue<double><<<1, 32, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline, p.errFlag,
+                                           ACC_SET, 0, spins);
 }
 
 }  // namespace fgpu

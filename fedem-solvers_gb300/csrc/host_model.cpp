@@ -464,6 +464,17 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
                              "tolVelRot",   "tolVelGen",  "tolAccNorm", "tolAccTra",  "tolAccRot",  "tolAccGen",
                              "tolResNorm",  "tolResTra",  "tolResRot",  "tolResGen",  "tolEnerMax", "tolEnerSum"};
   for (int k = 0; k < 18; ++k) setTol(o, tolKeys[k], c, k);
+  // options that change the results and that this path does not implement are
+  // refused, never ignored: iteration cut-back (newmarkRoutinesModule.f90:879-896,
+  // 979-1009, 1106-1116, active when cutbackFactor < 1), line search (:915-918),
+  // geometric stiffness, centripetal force correction, the Newmark variants of
+  // NewmarkFlag and tangent updates by tolerance (:826-842, tolUpdateFactor > 1)
+  if (o.d("cutbackFactor", 1.0) < 1.0) { err = "iteration cut-back (-cutbackFactor < 1) is not supported"; return -60; }
+  if (o.b("cutbackSing", false)) { err = "cut-back on singularities (-cutbackSing) is not supported"; return -60; }
+  for (const char* key : {"lineSearch", "stressStiffDyn", "stressStiffEqu", "centripForceCorr"})
+    if (o.b(key, false)) { err = std::string("-") + key + " is not supported by the GPU solver"; return -61; }
+  if (o.i("NewmarkFlag", 0) != 0) { err = "-NewmarkFlag other than 0 is not supported"; return -62; }
+  if (o.d("tolUpdateFactor", 0.0) > 1.0) { err = "tangent updates by tolerance (-tolUpdateFactor > 1) are not supported"; return -63; }
 
   std::vector<NmlRecord> recs = readNamelists(fsi);
   // record types this path does not implement are refused, never dropped

@@ -72,6 +72,9 @@ struct PersistentPlan {
   // fronts whose leaf children are solved inline
   const unsigned char* bwInline;
   int *bwQueue, *bwCtr;
+  // polls of a bounded wait in the back substitution before it gives up and
+  // sets errFlag (about 1-2 s at the default)
+  long long spinLimit = 1LL << 23;
 };
 // values of one front's L block the solve kernels stage in shared memory
 int stagingCapacity(const PersistentPlan& p, size_t elemBytes);
@@ -85,6 +88,11 @@ void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, 
 // back substitution; stores the solution in del (FP64 solve) or accumulates it in xref
 // (FP32 refinement sweep `sweep`; the last sweep also copies xref to del)
 void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
+// One warp of the back-substitution queue kernel on a private queue (4 ints of
+// counters at ctr, the slots at queue), waiting at most `spins` polls: with an
+// empty slot 0 and a slot total of 1 the wait runs out and sets p.errFlag.
+void launchBackwardWaitProbe(const DevData& d, const PersistentPlan& p, int* queue, int* ctr, long long spins,
+                             cudaStream_t s);
 // prescribed deflections (step start), their predictor right-hand side (after the
 // element Newton matrices), and the restart state of pure linear quasi-static steps
 void launchMotions(const DevData& d, cudaStream_t s);
@@ -96,7 +104,8 @@ void launchRefineResidual(const DevData& d, cudaStream_t s);
 
 // Convergence norms of model m recomputed into a fixed scratch array compiled
 // into the library (no device allocation); blocks until the 18 values are in
-// out18 (host).  c0/nc: the model's first norm chunk and chunk count.
-int normsNoAlloc(const DevData& d, int m, int c0, int nc, cudaStream_t s, double* out18, std::string& err);
+// out18 (host).  c0/nc: the model's first norm chunk and chunk count; dev: the
+// batch's device (made current for the launch).
+int normsNoAlloc(const DevData& d, int m, int c0, int nc, int dev, cudaStream_t s, double* out18, std::string& err);
 
 }  // namespace fgpu

@@ -9,8 +9,8 @@
 
 namespace fgpu {
 
-Server::Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBatch, int chunk)
-    : budget_(budgetBytes), opt_(opt), maxModels_(maxModelsPerBatch > 0 ? maxModelsPerBatch : 1 << 30),
+Server::Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBatch, int chunk, int device)
+    : budget_(budgetBytes), device_(device), opt_(opt), maxModels_(maxModelsPerBatch > 0 ? maxModelsPerBatch : 1 << 30),
       chunk_(chunk > 0 ? chunk : 4), t0_(std::chrono::steady_clock::now()) {}
 
 double Server::now() const {
@@ -99,6 +99,7 @@ int Server::collect(Job& j, bool all) {
 }
 
 int Server::pump() {
+  if (cudaSetDevice(device_) != cudaSuccess) return -953;
   int finished = 0;
   // collect finished requests and engines, keep the others fed
   for (size_t k = 0; k < jobs_.size();) {

@@ -29,7 +29,8 @@ struct Request {
 
 class Server {
  public:
-  Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBatch, int chunk);
+  // device: the CUDA device every engine of this server runs on
+  Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBatch, int chunk, int device);
   int submit(const HostModel* m);  // returns the request id (arrival stamped now)
   // One pass: admit pending requests that fit, keep every live engine fed with
   // a chunk of batched iterations, collect finished engines.  Returns the
@@ -53,6 +54,7 @@ class Server {
   int collect(Job& j, bool all);
 
   size_t budget_, inUse_ = 0;
+  int device_ = 0;
   EngineOptions opt_;
   int maxModels_, chunk_;
   int minBatch_ = 8;        // admission waits for this many requests ...

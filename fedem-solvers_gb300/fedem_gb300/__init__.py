@@ -84,6 +84,7 @@ def load_library(path=None):
         "fgpu_batch_restore": (c_int, [vp]),
         "fgpu_batch_phase_timings": (c_ll, [vp, P(c_dbl), P(c_ll), c_int]),
         "fgpu_batch_time_factor": (c_int, [vp, c_int, P(c_dbl)]),
+        "fgpu_batch_phase_timings_n": (c_ll, [vp, P(c_dbl), c_int, P(c_ll), c_int]),
         "fgpu_server_create": (c_int, [c_dbl, c_int, c_int, c_int, c_int, c_dbl, P(vp)]),
         "fgpu_server_destroy": (None, [vp]),
         "fgpu_server_submit": (c_int, [vp, vp, P(c_int)]),
@@ -92,6 +93,10 @@ def load_library(path=None):
         "fgpu_server_now": (c_dbl, [vp]),
         "fgpu_server_request": (c_int, [vp, c_int, P(c_int), P(c_dbl), P(c_ll), P(c_ll)]),
         "fgpu_server_result": (c_int, [vp, c_int, P(c_dbl)]),
+        "fgpu_set_device": (c_int, [c_int]),
+        "fgpu_get_device": (c_int, [P(c_int), ctypes.c_char_p, c_int]),
+        "fgpu_batch_device": (c_int, [vp]),
+        "fgpu_batch_probe_wait_timeout": (c_int, [vp, c_ll, P(c_int)]),
         "fgpu_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

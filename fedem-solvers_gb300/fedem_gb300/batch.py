@@ -6,6 +6,7 @@ and advances all of them to their end time together, one Newton iteration
 per model per batched iteration.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -64,6 +65,45 @@ class Model:
         if rc != 0:
             raise FedemException("element_matrix: bad argument")
         return m.reshape((12, 12), order="F")
+
+
+def create_models(cases, threads=None, lib=None):
+    """Model set-up (fgpu_model_create) of many (fsi, options, ...) cases on the
+    host's threads; the C call releases the interpreter lock and keeps no
+    shared state, so the models are built in parallel.  Returns them in order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    lib = lib or load_library()
+    cases = list(cases)
+    n = threads or os.cpu_count() or 1
+    # largest models first for the balance, results back in input order
+    order = sorted(range(len(cases)), key=lambda k: -len(cases[k][0]))
+    out = [None] * len(cases)
+
+    def one(k):
+        out[k] = Model(cases[k][0], cases[k][1], lib=lib)
+
+    with ThreadPoolExecutor(max_workers=max(1, n)) as ex:
+        list(ex.map(one, order))
+    return out
+
+
+def set_device(ordinal, lib=None):
+    """Selects the CUDA device of every batch/server created afterwards
+    (fgpu_set_device); returns (ordinal, PCI bus id)."""
+    lib = lib or load_library()
+    if lib.fgpu_set_device(int(ordinal)) != 0:
+        raise FedemException("fgpu_set_device failed: " + lib.fgpu_last_error().decode())
+    return get_device(lib)
+
+
+def get_device(lib=None):
+    lib = lib or load_library()
+    dev = ctypes.c_int(-1)
+    bus = ctypes.create_string_buffer(64)
+    if lib.fgpu_get_device(ctypes.byref(dev), bus, 64) != 0:
+        raise FedemException("fgpu_get_device failed: " + lib.fgpu_last_error().decode())
+    return dev.value, bus.value.decode()
 
 
 class Batch:
@@ -142,13 +182,17 @@ class Batch:
             raise FedemException("restore failed: " + self._lib.fgpu_last_error().decode())
 
     def phase_timings(self, reset=False):
-        """(samples, [element ms, factor + first forward ms, other solve ms, second forward ms],
-        active elements) sampled inside run()."""
-        ms = np.zeros(4)
+        """(samples, [element ms, factor + first forward ms, other solve ms, second forward ms,
+        first back substitution ms], active elements) sampled inside run()."""
+        ms = np.zeros(5)
         el = ctypes.c_longlong()
-        n = self._lib.fgpu_batch_phase_timings(self._h, _ptr(ms, ctypes.c_double), ctypes.byref(el),
-                                               1 if reset else 0)
+        n = self._lib.fgpu_batch_phase_timings_n(self._h, _ptr(ms, ctypes.c_double), 5, ctypes.byref(el),
+                                                 1 if reset else 0)
         return int(n), ms, int(el.value)
+
+    def device(self):
+        """CUDA device ordinal the batch was uploaded to."""
+        return int(self._lib.fgpu_batch_device(self._h))
 
     def time_factor(self, reps=10):
         """(ms per launch, algorithmic bytes per launch) of the factorisation fused

@@ -22,6 +22,21 @@ extern "C" {
 typedef struct fgpu_model fgpu_model;  /* host-side set-up of one model */
 typedef struct fgpu_batch fgpu_batch;  /* models resident on the GPU    */
 
+/* Device selection.  The library carries its own CUDA runtime, so the device a
+ * caller selected through another runtime (e.g. a deep-learning framework) is
+ * not seen here.  fgpu_set_device makes `ordinal` current on the calling thread
+ * and the device of every batch, server and legacy solverInit created
+ * afterwards (from any thread); without it they use the creating thread's
+ * current device of this runtime (device 0 unless set).  Every later call on a
+ * handle runs on the handle's device, whichever thread makes it.  A process per
+ * GPU calls fgpu_set_device(local rank) once before creating anything. */
+int fgpu_set_device(int ordinal);
+/* The selected device (or the calling thread's current one) and its PCI bus id
+ * ("0000:1b:00.0" style, len bytes at most; pciBusId may be NULL). */
+int fgpu_get_device(int* ordinal, char* pciBusId, int len);
+/* The device a batch was uploaded to. */
+int fgpu_batch_device(const fgpu_batch* b);
+
 /* Host set-up of one model (the preprocessing part of solverInit,
  * solverInterface.h:65): parses the solver-input text and options, builds
  * the element matrices, equation numbering, sparsity pattern, gather maps and
@@ -53,8 +68,10 @@ void fgpu_batch_destroy(fgpu_batch* b);
  * fgpu_batch_create, 0. */
 int fgpu_batch_run(fgpu_batch* b, long long maxBatched, long long* stats10);
 /* per-model results: state (0 stepping, 1 iterating, 2 done, 3 error),
- * status bits (1 singular, 2 max iterations, 4 NaN, 8 corotation), time,
- * steps, Newton iterations */
+ * status bits (1 singular, 2 max iterations, 4 NaN, 8 corotation, 16 a bounded
+ * wait ran out), time, steps, Newton iterations.  A model that fails (in its
+ * initial static equilibrium or in a step) stops in state 3 with its bits set;
+ * the other models of the batch go on unaffected. */
 int fgpu_batch_model_info(fgpu_batch* b, int model, int* state, int* status, double* time, long long* steps,
                           long long* iters);
 /* triad position matrices of one model, 12 doubles (3x4 column-major) each */
@@ -96,6 +113,9 @@ int fgpu_batch_restore(fgpu_batch* b);
  * sampled iterations.  Returns the number of samples; reset != 0 clears the
  * accumulators afterwards. */
 long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset);
+/* The same with n (1..5) phases: the four above, then the back substitution of
+ * the first solve of the iteration. */
+long long fgpu_batch_phase_timings_n(fgpu_batch* b, double* ms, int n, long long* elems, int reset);
 /* Times reps launches of the factorisation fused with the first forward
  * elimination with every model factoring (CUDA events on the batch's stream).
  * out2[0]: milliseconds per launch, out2[1]: algorithmic bytes of one launch.
@@ -103,6 +123,15 @@ long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems,
  * status and pivot counts are kept); time it after a run or restore a
  * snapshot before the next one.  Returns 0, or < 0 on error. */
 int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
+
+/* Failure-path test hook: runs one warp of the back-substitution queue kernel
+ * on a private queue whose only slot is never filled, with a wait limit of
+ * `spins` polls (about 32 ns each), so the bounded wait runs out and sets the
+ * batch's wait-error flag, which *flag receives (1).  No fault, trap or hang:
+ * the kernel returns and the context stays usable.  Every model of the batch
+ * still running then fails with status 16 (wait timed out) at its next
+ * convergence test, as after a real wait that ran out. */
+int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag);
 
 /* ---- serving: continuous batching of simulation requests ------------------
  * Requests are admitted into new GPU batches (own stream each) as soon as the

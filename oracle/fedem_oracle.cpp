@@ -660,6 +660,10 @@ struct OracleModel {
   double oldScale[3] = {-1, -1, -1};
   bool finished = false;
   int error = 0;
+  // largest triad displacement from the start positions seen at the end of any
+  // step so far (the scale of the response over the run, for relative errors)
+  std::vector<double> x0;
+  double maxDisp = 0.0;
 };
 
 namespace {
@@ -1819,11 +1823,15 @@ extern "C" OracleModel* oracle_create(const char* fsi, int argc, const char* con
     if (ierr) *ierr = err;
     return nullptr;
   }
+  for (const Triad& t : m->triads)
+    for (int r = 0; r < 3; ++r) m->x0.push_back(t.ur[r][3]);
   if (ierr) *ierr = 0;
   return m;
 }
 
 extern "C" void oracle_destroy(OracleModel* m) { delete m; }
+
+extern "C" double oracle_get_max_displacement(OracleModel* m) { return m ? m->maxDisp : 0.0; }
 
 // solverModule.f90:658-1000, solveStep (fixed step size, no quasi-static range)
 extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
@@ -1870,6 +1878,8 @@ extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
       std::memcpy(e.finitPrev, e.finit, sizeof(e.finit));
     }
   }
+  for (size_t k = 0; k < m->triads.size(); ++k)
+    for (int r = 0; r < 3; ++r) m->maxDisp = std::max(m->maxDisp, std::fabs(m->triads[k].ur[r][3] - m->x0[3 * k + r]));
   m->finished = finished;
   return finished ? 0 : 1;
 }

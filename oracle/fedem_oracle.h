@@ -46,6 +46,9 @@ int oracle_get_nelements(OracleModel* m);
 int oracle_get_meqn(OracleModel* m, int* meqn);
 /* All triad position matrices, 12 doubles (3x4 column-major) per triad. */
 int oracle_get_triad_ur(OracleModel* m, double* ur);
+/* Largest triad displacement from the start positions at the end of any
+ * step so far: the response scale of the run, for relative errors. */
+double oracle_get_max_displacement(OracleModel* m);
 /* Total Newton iterations done so far in the time integration. */
 long long oracle_get_iterations(OracleModel* m);
 /* Newton iterations in the last step and the last iteration norms

@@ -43,6 +43,7 @@ def load():
         "oracle_get_meqn": (ci, [vp, _P(ci)]),
         "oracle_get_triad_ur": (ci, [vp, _P(cd)]),
         "oracle_get_iterations": (ctypes.c_longlong, [vp]),
+        "oracle_get_max_displacement": (cd, [vp]),
         "oracle_get_last_norms": (ci, [vp, _P(cd)]),
         "oracle_get_csr_pattern": (ci, [vp, _P(ci), _P(ci)]),
         "oracle_assemble_newton": (ci, [vp, cd, cd, cd, _P(cd)]),
@@ -113,6 +114,10 @@ class OracleModel:
 
     def iterations(self):
         return self.lib.oracle_get_iterations(self.h)
+
+    def max_displacement(self):
+        """Largest triad displacement from the start positions over the steps so far."""
+        return self.lib.oracle_get_max_displacement(self.h)
 
     def csr_upper_pattern(self):
         nnz = self.lib.oracle_get_csr_pattern(self.h, None, None)

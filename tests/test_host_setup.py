@@ -202,3 +202,21 @@ def test_external_function_records():
         Model(fsi.replace("fileName = ''", "fileName = 'inputs.asc'"), ["-timeInc=0.01", "-timeEnd=0.1"])
     with pytest.raises(FedemException, match="channel"):
         Model(fsi.replace("channel = 2", "channel = 0"), ["-timeInc=0.01", "-timeEnd=0.1"])
+
+
+@pytest.mark.parametrize("opt", ["-cutbackFactor=0.5", "-cutbackSing", "-lineSearch", "-stressStiffDyn",
+                                 "-stressStiffEqu+", "-centripForceCorr", "-NewmarkFlag=100",
+                                 "-tolUpdateFactor=10.0"])
+def test_result_changing_options_are_refused(gpu_lib, opt):
+    """Options that change the results and that this path does not implement
+    (iteration cut-back, line search, geometric stiffness, centripetal
+    correction, Newmark variants, tangent updates by tolerance) fail model
+    creation with a message instead of being ignored; their defaults pass."""
+    from fedem_gb300 import FedemException, models
+    from fedem_gb300.batch import Model
+
+    base = models.beam_chain_fsi(4, 1.0, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0, **models.STEEL)
+    with pytest.raises(FedemException, match="not supported"):
+        Model(base, ["-timeInc=0.01", opt])
+    Model(base, ["-timeInc=0.01", "-cutbackFactor=1.0", "-lineSearch-", "-NewmarkFlag=0",
+                 "-tolUpdateFactor=0.0"]).close()

@@ -62,3 +62,65 @@ def test_two_rank_sharding_covers_every_model_once():
     loads = [sum(sizes[k] for k in part) for part in parts]
     assert loadsum == sum(sizes)
     assert max(loads) <= 0.5 * sum(sizes) + max(sizes)  # balanced by element count
+
+
+class _FakeSolverLib:
+    """Stands in for libfedem_solver_core.so's device entry points on CPU:
+    records the ordinal each rank asks for."""
+
+    def __init__(self):
+        self.asked = []
+        self.cur = -1
+
+    def fgpu_set_device(self, ordinal):
+        self.asked.append(ordinal)
+        self.cur = ordinal
+        return 0
+
+    def fgpu_get_device(self, dev_ref, bus, n):
+        dev_ref._obj.value = self.cur
+        bus.value = b"fake:%d" % self.cur
+        return 0
+
+    def fgpu_last_error(self):
+        return b""
+
+
+def _device_worker(rank, world, port, out):
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "fedem-solvers_gb300")]
+    import torch.distributed as dist
+
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    r, w, local = bench.rank_env()
+    fake = _FakeSolverLib()
+    dev, bus = bench.rank_device(local, fake)
+    gathered = [None] * world
+    dist.all_gather_object(gathered, (r, w, local, fake.asked, dev, bus))
+    if rank == 0:
+        out.put(gathered)
+    dist.destroy_process_group()
+
+
+def test_each_rank_selects_its_own_device():
+    """bench.py gives the solver library each rank's LOCAL_RANK as its device
+    (fgpu_set_device) before anything is created, so two ranks on one node use
+    two GPUs."""
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_device_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for r, (rank, world, local, asked, dev, bus) in enumerate(res):
+        assert (rank, world, local) == (r, 2, r)
+        assert asked == [r] and dev == r and bus == f"fake:{r}"

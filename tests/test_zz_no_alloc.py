@@ -9,7 +9,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1.0e-13  # same chunks, mapping and reduction order: expected bit-equal
+# same chunks, thread mapping, expressions, reduction order and weight sums as
+# the batch's own norms pass: the values are compared bit for bit
 
 
 def _norms(lib, batch, model, noalloc):
@@ -21,7 +22,7 @@ def _norms(lib, batch, model, noalloc):
 
 
 def _close(a, b):
-    return np.all(np.abs(a - b) <= RTOL * np.maximum(np.abs(a), np.abs(b)))
+    return np.array_equal(a, b, equal_nan=True)
 
 
 def test_noalloc_norms_match_stored_norms_on_two_calls_in_a_row(gpu):
@@ -64,4 +65,24 @@ def test_noalloc_norms_refuse_models_above_the_scratch_limit(gpu):
     # the small model of the same batch still works after the refusal
     b.step(0)
     assert _close(_norms(lib, b, 0, noalloc=True), _norms(lib, b, 0, noalloc=False))
+    b.close()
+
+
+def test_noalloc_norms_keep_a_nan_like_the_stored_norms(gpu):
+    """A model whose residual turned NaN (NaN point load): the batch's stored
+    norms carry the NaN in its maxima, and the no-allocation norms are the
+    same values, NaN in the same places."""
+    from fedem_gb300 import load_library, models
+    from fedem_gb300.batch import Batch, Model
+
+    lib = load_library()
+    fsi, opts = models.cantilever_c1()
+    bad = models.beam_chain_fsi(3000, 0.25, 0.1, 0.01, clamp=0, load_node=3000, load_dof=2, load=1000.0,
+                                **models.STEEL).replace("f0 = ", "f0 = nan ! ", 1)
+    b = Batch([Model(fsi, opts), Model(bad, opts)])
+    b.step(1)
+    ref = _norms(lib, b, 1, noalloc=False)
+    assert np.isnan(ref).any()
+    assert _close(_norms(lib, b, 1, noalloc=True), ref)
+    assert _close(_norms(lib, b, 1, noalloc=True), ref)
     b.close()
