@@ -228,3 +228,147 @@ def batch_c4(n_models=256, seed=4, n_min=10, n_max=4000, steps=500):
         opts = ["-timeInc=0.001", f"-timeEnd={steps * 0.001!r}", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
         out.append((fsi, opts, n_el))
     return out
+
+
+# ---------------------------------------------------------------------------
+# General frames: beams in any direction, master-slave joints, springs, dampers
+# ---------------------------------------------------------------------------
+def _beam_frame(a, b):
+    """Superelement axes of a beam from point a to b: x along the beam, y and z
+    completing a right-handed frame (the beam element takes its local axes from
+    these).  Returns the 3x3 rotation (columns ex, ey, ez) and the length."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    ex = b - a
+    L = float(np.linalg.norm(ex))
+    ex = ex / L
+    # the global axis least aligned with the beam completes the frame
+    ref = np.eye(3)[int(np.argmin(np.abs(ex)))]
+    ez = np.cross(ex, ref)
+    ez /= np.linalg.norm(ez)
+    ey = np.cross(ez, ex)
+    return np.stack([ex, ey, ez], 1), L
+
+
+def _rows34(R, p):
+    """3x4 position matrix [R | p] as the file writes it: row by row."""
+    return " ".join(_f(R[r, c]) if c < 3 else _f(p[r]) for r in range(3) for c in range(4))
+
+
+def frame_fsi(triads, beams, props, joints=(), loads=(), springs=(), dampers=(), gravity=None,
+              weights=(0.1, 1.0, 1.0), title="frame"):
+    """Solver-input text of a general frame.
+
+    triads:  dicts {id, pos (3), bc (6 ints, default free)}; global axes.
+    beams:   (id, triad a, triad b, property id) 2-noded beam superelements.
+    props:   dicts {id, A, Iy, Iz, It, rho, E, G, shear (0 = Euler-Bernoulli)}.
+    joints:  dicts {id, type (1 revolute, 3 rigid, 4 free), slave, master,
+             pos (3), rot (3x3, columns = joint axes; default identity),
+             dofs [(lDof, iMat), ...], bc [..], init [..]}: &MASTERSLAVEJOINT.
+    loads:   (triad id, DOF 1..6, f0) constant point loads.
+    springs: (triad a, triad b, stiffness, stress-free length[, alpha2]).
+    dampers: (triad a, triad b, coefficient).
+    gravity: (gx, gy, gz) or None.
+    """
+    pos = {t["id"]: np.asarray(t["pos"], float) for t in triads}
+    out = [f"&HEADING\n  modelFile = '{title}'\n/\n",
+           f"&MECHANISM\n  id = 1\n  weightTranslation = {_f(weights[0])}\n"
+           f"  weightRotation = {_f(weights[1])}\n  weightGeneralized = {_f(weights[2])}\n/\n"]
+    if gravity is not None:
+        out.append("&ENVIRONMENT\n  gravity = " + " ".join(_f(g) for g in gravity) + "\n/\n")
+    for t in triads:
+        bc = t.get("bc")
+        bcl = ("  BC = " + " ".join(str(int(v)) for v in bc) + "\n") if bc is not None else ""
+        out.append(f"&TRIAD\n  id = {t['id']}\n  nDOFs = 6\n  ur = {_rows34(np.eye(3), pos[t['id']])}\n{bcl}/\n")
+    for (sid, ta, tb, pid) in beams:
+        R, L = _beam_frame(pos[ta], pos[tb])
+        out.append(
+            f"&SUP_EL\n  id = {sid}\n  numTriads = 2\n  triadIds = {ta} {tb}\n  elPropId = {pid}\n  shadowPosAlg = 1\n"
+            f"  refTriad1Id = {ta}, offset1 = 0.0 0.0 0.0\n  refTriad2Id = {tb}, offset2 = 0.0 0.0 0.0\n"
+            f"  refTriad3Id = {ta}, offset3 = 0.0 {_f(L)} 0.0\n"
+            f"  supPos = {_rows34(R, pos[ta])}\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {ta}\n"
+            f"  undPosInSupElSystem = {_rows34(R, (0.0, 0.0, 0.0))}\n/\n"
+            f"&TRIAD_UNDPOS\n  supElId = {sid}\n  triadId = {tb}\n"
+            f"  undPosInSupElSystem = {_rows34(R, (L, 0.0, 0.0))}\n/\n")
+    for p in props:
+        out.append(f"&ELEMENT_PROPERTY\n  id = {p['id']}\n  geometry = {_f(p['A'])} {_f(p['Iy'])} {_f(p['Iz'])} "
+                   f"{_f(p['It'])} {_f(p.get('shear', 0.0))} {_f(p.get('shear', 0.0))} 0.0 0.0\n"
+                   f"  material = {_f(p['rho'])} {_f(p['E'])} {_f(p['G'])}\n/\n")
+    for j in joints:
+        R = np.asarray(j.get("rot", np.eye(3)), float)
+        dofs = list(j.get("dofs", []))
+        bc = list(j.get("bc", [1] * len(dofs)))
+        init = list(j.get("init", [0.0] * len(dofs)))
+        lines = [f"&MASTERSLAVEJOINT\n  id = {j['id']}\n  type = {int(j.get('type', 1))}\n"
+                 f"  slaveId = {j['slave']}\n  masterId = {j['master']}\n"
+                 f"  initPosInGlobal = {_rows34(R, j['pos'])}\n  nJointVars = {len(dofs)}\n"]
+        if dofs:
+            lines.append("  JointVarDefs = " + " ".join(f"{int(a)} {int(b)}" for a, b in dofs) + "\n")
+            lines.append("  BC = " + " ".join(str(int(v)) for v in bc) + "\n")
+            lines.append("  JVarInitVal = " + " ".join(_f(v) for v in init) + "\n")
+        out.append("".join(lines) + "/\n")
+    for k, (tid, dof, f0) in enumerate(loads):
+        out.append(f"&LOAD\n  id = {900000 + k}\n  triadId = {tid}\n  lDof = {int(dof)}\n  f0 = {_f(f0)}\n/\n")
+    for k, sp in enumerate(springs):
+        a, b, stiff, l0 = sp[:4]
+        alpha2 = sp[4] if len(sp) > 4 else 0.0
+        out.append(f"&SPRING_BASE\n  id = {800000 + k}\n  l0 = {_f(l0)}\n  s0 = {_f(stiff)}\n/\n"
+                   f"&SPRING_ELEMENT\n  id = {800000 + k}\n  triadIDs = {a} {b}\n"
+                   f"  springBaseId = {800000 + k}\n  alpha2 = {_f(alpha2)}\n/\n")
+    for k, (a, b, coeff) in enumerate(dampers):
+        out.append(f"&DAMPER\n  id = {850000 + k}\n  triad1Id = {a}\n  triad2Id = {b}\n  d0 = {_f(coeff)}\n/\n")
+    return "".join(out)
+
+
+def pipe_props(pid, od, wall, E=STEEL["E"], G=STEEL["G"], rho=STEEL["rho"]):
+    area, iy, iz, it = pipe_section(od, wall)
+    return {"id": pid, "A": area, "Iy": iy, "Iz": iz, "It": it, "rho": rho, "E": E, "G": G}
+
+
+def hinged_beam(n_left=8, n_right=8, el_len=0.25, load=10.0, joint_type=1):
+    """Two beam segments along X joined at x = n_left * el_len: the left one
+    clamped at x = 0, the right one pinned (translations fixed) at its end.
+    The joint's master is the left segment's end triad, its slave the right
+    segment's first triad (same point).  joint_type 1: revolute about global Z
+    (bending about Z released: a Gerber beam, which carries a transverse Y load
+    at the hinge on the left cantilever alone); 3: rigid (a continuous beam).
+    The load acts on the master triad in Y."""
+    triads, beams = [], []
+    nid = 1
+    for k in range(n_left + 1):
+        triads.append({"id": nid, "pos": (k * el_len, 0.0, 0.0), "bc": [0] * 6 if k == 0 else None})
+        nid += 1
+    master = nid - 1
+    slave = nid
+    for k in range(n_right + 1):
+        bc = [0, 0, 0, 1, 1, 1] if k == n_right else None
+        triads.append({"id": nid, "pos": ((n_left + k) * el_len, 0.0, 0.0), "bc": bc})
+        nid += 1
+    sid = 1000
+    for k in range(n_left):
+        beams.append((sid, k + 1, k + 2, 1))
+        sid += 1
+    for k in range(n_right):
+        beams.append((sid, slave + k, slave + k + 1, 1))
+        sid += 1
+    j = {"id": 500, "type": joint_type, "slave": slave, "master": master, "pos": (n_left * el_len, 0.0, 0.0)}
+    if joint_type == 1:
+        j["dofs"] = [(6, 1)]
+    fsi = frame_fsi(triads, beams, [pipe_props(1, 0.1, 0.01)], joints=[j], loads=[(master, 2, load)],
+                    title="hinged beam")
+    return fsi, master, slave
+
+
+def pendulum(length=1.0, n_el=4, theta0=0.1, g=9.81):
+    """A pipe hanging from a revolute joint (axis global Z) at the origin,
+    released at rest theta0 from the vertical under gravity -Y.  The joint's
+    master is a clamped ground triad, its slave the pipe's top triad."""
+    d = np.array([np.sin(theta0), -np.cos(theta0), 0.0])
+    triads = [{"id": 1, "pos": (0.0, 0.0, 0.0), "bc": [0] * 6}]
+    for k in range(n_el + 1):
+        triads.append({"id": 2 + k, "pos": tuple(d * length * k / n_el)})
+    beams = [(100 + k, 2 + k, 3 + k, 1) for k in range(n_el)]
+    j = {"id": 50, "type": 1, "slave": 2, "master": 1, "pos": (0.0, 0.0, 0.0), "dofs": [(6, 1)]}
+    fsi = frame_fsi(triads, beams, [pipe_props(1, 0.05, 0.005)], joints=[j], gravity=(0.0, -g, 0.0),
+                    title="pendulum")
+    return fsi, 2 + n_el

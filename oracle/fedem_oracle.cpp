@@ -604,6 +604,26 @@ struct Axial {
   double FS[6] = {0, 0, 0, 0, 0, 0}, FD[6] = {0, 0, 0, 0, 0, 0};
 };
 
+// Master-slave joint with one master triad (MasterSlaveJointTypeModule): the
+// slave triad's DOFs are dependent, u_s = T [u_master; joint DOFs], with T
+// rebuilt from the current geometry (masterSlaveJointRoutinesModule.f90:
+// 374-577, updateDependencies) and the slave placed on its kinematic position
+// (:218-299, moveJointInPosition) before every element update.
+struct Joint {
+  int id = 0, type = 0;
+  int slave = -1, master = -1;  // triad indices
+  M34 JPosInG, JPosInT, STPos0InJ;
+  int nMats = 0;
+  std::vector<int> lDof, iMat, BC;  // per joint DOF (iMat 1-based)
+  std::vector<double> jVar, jVarPrev;
+  int firstDof = -1;  // first joint DOF in the DOF vectors
+  int nM = 0;         // master DOFs in the constraint (0 for a grounded master)
+  int ncol = 0;       // nM + joint DOFs
+  double TR[3][3];
+  std::vector<double> T;      // 6 x ncol, row-major
+  std::vector<int> colEq;     // 0-based equation of each column, -1 fixed/prescribed
+};
+
 struct TestItem {
   int code = -1;  // 1 allOf, 2 oneOf, -1 inactive
   double absTol = 0.0, value = 0.0;
@@ -622,6 +642,8 @@ struct OracleModel {
   std::vector<EngineF> engines;
   std::vector<Motion> motions;
   std::vector<Axial> axials;    // springs first, then dampers (assembly order)
+  std::vector<Joint> joints;
+  std::vector<int> dep;         // per DOF: 6 * joint + row of a dependent DOF, else -1
   std::vector<int> axEq;        // 6 per axial element: 0-based equation, -1 fixed, <= -2 prescribed
   const std::vector<double>* axVel = nullptr;  // triad velocities the dampers see
   std::vector<double> ccv;  // constant term of each constraint equation (TTCC(MPMCEQ(iceq)))
@@ -754,9 +776,127 @@ static void rotateOut(const Elem& e, double* f) {
   }
 }
 
+// spin(v) x = v x x (rotationModule)
+static void spinMat(const double* v, double S[3][3]) {
+  S[0][0] = 0.0;   S[0][1] = -v[2]; S[0][2] = v[1];
+  S[1][0] = v[2];  S[1][1] = 0.0;   S[1][2] = -v[0];
+  S[2][0] = -v[1]; S[2][1] = v[0];  S[2][2] = 0.0;
+}
+
+// position matrix of the joint variables of level iMat (1-based): translations
+// of its translational DOFs and the rotation of its (at most one) rotational DOF
+static void jointPosFromVars(const Joint& J, int im, M34 P) {
+  double th[3] = {0.0, 0.0, 0.0};
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 4; ++c) P[r][c] = 0.0;
+  for (size_t k = 0; k < J.lDof.size(); ++k) {
+    if (J.iMat[k] != im) continue;
+    if (J.lDof[k] <= 3) P[J.lDof[k] - 1][3] = J.jVar[k];
+    else th[J.lDof[k] - 4] = J.jVar[k];
+  }
+  double R[3][3];
+  vec_to_mat(th, R);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) P[r][c] = R[r][c];
+}
+
+// moveJointInPosition (masterSlaveJointRoutinesModule.f90:218-299, one master
+// triad) followed by updateDependencies (:374-577) for a joint whose dependent
+// triad has global system directions and no prescribed master or joint DOFs
+static void updateJoint(OracleModel& m, Joint& J) {
+  Triad& S = m.triads[J.slave];
+  const Triad& Mt = m.triads[J.master];
+  matmul34(Mt.ur, J.JPosInT, J.JPosInG);
+  double e[3];
+  for (int k = 0; k < 3; ++k) e[k] = -(S.ur[k][3] - Mt.ur[k][3]);
+  spinMat(e, J.TR);  // TR = -spin(e), e = dependent triad relative to the master
+  M34 P, Q;
+  std::memcpy(P, J.STPos0InJ, sizeof(M34));
+  for (int i = 1; i <= J.nMats; ++i) {
+    M34 F;
+    jointPosFromVars(J, i, F);
+    matmul34(F, P, Q);
+    std::memcpy(P, Q, sizeof(M34));
+  }
+  matmul34(J.JPosInG, P, S.ur);
+  // constraint coefficients
+  std::fill(J.T.begin(), J.T.end(), 0.0);
+  const int nc = J.ncol;
+  for (int lm = 0; lm < J.nM; ++lm)
+    for (int ls = 0; ls < 6; ++ls) {
+      double v = 0.0;
+      if (ls < 3 && lm < 3) v = ls == lm ? 1.0 : 0.0;
+      else if (ls < 3) v = J.TR[ls][lm - 3];
+      else if (lm >= 3) v = ls == lm ? 1.0 : 0.0;
+      J.T[ls * nc + lm] = v;
+    }
+  std::vector<M34> csys(J.nMats + 1), png(J.nMats + 1);
+  M34 Pacc;
+  std::memcpy(Pacc, J.JPosInG, sizeof(M34));
+  for (int i = J.nMats; i >= 1; --i) {
+    std::memcpy(csys[i], Pacc, sizeof(M34));
+    M34 F, N;
+    jointPosFromVars(J, i, F);
+    matmul34(Pacc, F, N);
+    std::memcpy(Pacc, N, sizeof(M34));
+    std::memcpy(png[i], Pacc, sizeof(M34));
+  }
+  for (size_t k = 0; k < J.lDof.size(); ++k) {
+    const int lm = J.lDof[k], im = J.iMat[k];
+    double dUS[6];
+    if (lm <= 3) {
+      for (int r = 0; r < 3; ++r) { dUS[r] = csys[im][r][lm - 1]; dUS[3 + r] = 0.0; }
+    } else {
+      double dOm[3], ecc[3], dUG[3];
+      for (int r = 0; r < 3; ++r) {
+        dOm[r] = csys[im][r][lm - 4];
+        ecc[r] = S.ur[r][3] - png[im][r][3];
+      }
+      cross(dOm, ecc, dUG);
+      for (int r = 0; r < 3; ++r) { dUS[r] = dUG[r]; dUS[3 + r] = dOm[r]; }
+    }
+    for (int ls = 0; ls < 6; ++ls) J.T[ls * nc + J.nM + (int)k] = dUS[ls];
+  }
+}
+
+static void updateJoints(OracleModel& m) {
+  for (Joint& J : m.joints) updateJoint(m, J);
+}
+
+// IncJointsVar (masterSlaveJointRoutinesModule.f90:40-99): joint variables += increments
+static void incJointsVar(OracleModel& m, const std::vector<double>& inc) {
+  for (Joint& J : m.joints)
+    for (size_t k = 0; k < J.jVar.size(); ++k) J.jVar[k] += inc[J.firstDof + k];
+}
+
+struct Term {
+  int eq;
+  double c;
+};
+
+// equations and coefficients a DOF's value contributes to (MEEN < 0 expands
+// through MPMCEQ/MMCEQ/TTCC, sysMatrixTypeModule.f90:2099-2259)
+static void dofTerms(const OracleModel& m, int d, std::vector<Term>& out) {
+  out.clear();
+  if (m.dep[d] >= 0) {
+    const Joint& J = m.joints[m.dep[d] / 6];
+    const int r = m.dep[d] % 6;
+    for (int c = 0; c < J.ncol; ++c)
+      if (J.colEq[c] >= 0) out.push_back({J.colEq[c], J.T[r * J.ncol + c]});
+  } else if (m.meqn[d] > 0) {
+    out.push_back({m.meqn[d] - 1, 1.0});
+  }
+}
+
+static bool elemConstrained(const OracleModel& m, const Elem& e) {
+  return m.dep[m.triads[e.tri[0]].firstDof] >= 0 || m.dep[m.triads[e.tri[1]].firstDof] >= 0;
+}
+
 // Element forces (supElRoutinesModule.f90:231-456, UpdateSupEls; and :460-630,
-// UpdateSupElsStatic when isStatic).
+// UpdateSupElsStatic when isStatic).  The joints are updated first, as
+// UpdateMechanism does (newmarkRoutinesModule.f90:206-323).
 static int updateElems(OracleModel& m, bool newPositions, bool isStatic, bool corotInStatic) {
+  updateJoints(m);
   for (Elem& e : m.elems) {
     if (newPositions || (isStatic && corotInStatic)) {
       if (updateCorot(m, e, false) != 0) return -1;
@@ -867,9 +1007,23 @@ static void getForceVectors(OracleModel& m) {
   std::fill(m.FDk.begin(), m.FDk.end(), 0.0);
   std::fill(m.FIk.begin(), m.FIk.end(), 0.0);
   std::fill(m.Qk.begin(), m.Qk.end(), 0.0);
+  std::vector<Term> terms;
   for (size_t k = 0; k < m.elems.size(); ++k) {
     const Elem& e = m.elems[k];
     const int* eq = &m.elEq[12 * k];
+    if (elemConstrained(m, e)) {
+      // csAddEV through the constraint equations of dependent DOFs
+      for (int i = 0; i < 12; ++i) {
+        dofTerms(m, m.triads[e.tri[i / 6]].firstDof + i % 6, terms);
+        for (const Term& t : terms) {
+          m.FSk[t.eq] += t.c * e.FS[i];
+          m.FDk[t.eq] += t.c * e.FD[i];
+          m.FIk[t.eq] += t.c * e.FI[i];
+          m.Qk[t.eq] += t.c * e.Q[i];
+        }
+      }
+      continue;
+    }
     for (int i = 0; i < 12; ++i) {
       if (eq[i] < 0) continue;
       m.FSk[eq[i]] += e.FS[i];
@@ -975,9 +1129,24 @@ static void assembleSkyline(OracleModel& m, double sM, double sC, double sK, std
     for (Elem& e : m.elems) buildElementNewton(e, sM, sC, sK);
   }
   double Ns[144];
+  std::vector<Term> ti, tj;
   for (size_t k = 0; k < m.elems.size(); ++k) {
     rotatedElementMatrix(m.elems[k], m.elems[k].N, Ns);
     const int* eq = &m.elEq[12 * k];
+    if (elemConstrained(m, m.elems[k])) {
+      // T^T N T: every pair of terms, upper triangle (asmSparse with MEEN < 0)
+      const Elem& e = m.elems[k];
+      for (int i = 0; i < 12; ++i) {
+        dofTerms(m, m.triads[e.tri[i / 6]].firstDof + i % 6, ti);
+        for (int j = 0; j < 12; ++j) {
+          dofTerms(m, m.triads[e.tri[j / 6]].firstDof + j % 6, tj);
+          for (const Term& a : ti)
+            for (const Term& b : tj)
+              if (b.eq >= a.eq) skyAt(m, a.eq, b.eq) += a.c * b.c * Ns[i + 12 * j];
+        }
+      }
+      continue;
+    }
     for (int i = 0; i < 12; ++i) {
       if (eq[i] < 0) continue;
       for (int j = 0; j < 12; ++j) {
@@ -1079,6 +1248,14 @@ static void expandEq(const OracleModel& m, const std::vector<double>& eqv, std::
   for (int d = 0; d < m.ndof; ++d) {
     if (m.meqn[d] > 0) dofv[d] = eqv[m.meqn[d] - 1];
     else if (m.meqn[d] < 0) dofv[d] = F2 * m.ccv[-m.meqn[d] - 1];
+    else if (m.dep[d] >= 0) {  // dependent DOF: its constraint equation (constant term 0)
+      const Joint& J = m.joints[m.dep[d] / 6];
+      const int r = m.dep[d] % 6;
+      double v = 0.0;
+      for (int c = 0; c < J.ncol; ++c)
+        if (J.colEq[c] >= 0) v += J.T[r * J.ncol + c] * eqv[J.colEq[c]];
+      dofv[d] = v;
+    }
   }
 }
 
@@ -1181,6 +1358,11 @@ static void incTriadsPos(OracleModel& m, const std::vector<double>& inc) {
   }
 }
 
+static void incAll(OracleModel& m, const std::vector<double>& inc) {
+  incTriadsPos(m, inc);
+  incJointsVar(m, inc);
+}
+
 static int factorNewton(OracleModel& m, double sM, double sC, double sK) {
   assembleSkyline(m, sM, sC, sK);
   int ierr = skylineFactor(m, 1.0e-12);
@@ -1222,7 +1404,7 @@ static int staticEquilibrium(OracleModel& m) {
         }
         expandEq(m, m.del, m.sinc[0]);
         for (int d = 0; d < m.ndof; ++d) m.rinc[d] += m.sinc[0][d];
-        incTriadsPos(m, m.sinc[0]);
+        incAll(m, m.sinc[0]);
         if (updateElems(m, false, true, true) != 0) return -1;
         m.nIterThisStep++;
         m.nIter++;
@@ -1247,6 +1429,7 @@ static int staticEquilibrium(OracleModel& m) {
     std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
     std::memcpy(e.finitPrev, e.finit, sizeof(e.finit));
   }
+  for (Joint& J : m.joints) J.jVarPrev = J.jVar;
   return 0;
 }
 
@@ -1311,7 +1494,7 @@ static int newmarkInt(OracleModel& m) {
       m.urd[d] = m.svel * m.rinc[d] - m.dk[d];
       m.urdd[d] = m.sacc * m.rinc[d] - m.ak[d];
     }
-    incTriadsPos(m, m.sinc[0]);
+    incAll(m, m.sinc[0]);
     for (Elem& e : m.elems) setElemVelAcc(m, e, m.urd, m.urdd);
     m.axVel = &m.urd;
     if (updateElems(m, true, false, false) != 0) return -1;
@@ -1334,6 +1517,7 @@ static int newmarkInt(OracleModel& m) {
 static void restoreLastStep(OracleModel& m) {
   m.urd = m.urdp;
   m.urdd = m.urddp;
+  for (Joint& J : m.joints) J.jVar = J.jVarPrev;
   for (Triad& t : m.triads)
     if (t.nDOFs > 0) std::memcpy(t.ur, t.urPrev, sizeof(M34));
   for (Elem& e : m.elems) {
@@ -1376,7 +1560,7 @@ static int staticInt(OracleModel& m) {
     // staticIncAndUpdate with the increment (linInc = 1 when purely linear)
     expandEq(m, m.del, m.sinc[0], m.nIterThisStep == 0 ? 1.0 : 0.0);
     for (int d = 0; d < m.ndof; ++d) m.rinc[d] += m.sinc[0][d];
-    incTriadsPos(m, m.sinc[0]);
+    incAll(m, m.sinc[0]);
     if (updateElems(m, false, true, !pureLinear) != 0) return -1;
     std::fill(m.sinc[1].begin(), m.sinc[1].end(), 0.0);
     std::fill(m.sinc[2].begin(), m.sinc[2].end(), 0.0);
@@ -1402,7 +1586,7 @@ static int staticInt(OracleModel& m) {
 static int setup(OracleModel& m, const char* fsi) {
   std::vector<Record> recs = parseNamelists(fsi);
   for (const Record& r : recs)
-    for (const char* bad : {"masterslavejoint", "higher_pair", "mass", "user_el", "tire", "road", "supel_load",
+    for (const char* bad : {"higher_pair", "mass", "user_el", "tire", "road", "supel_load",
                             "spring_yield", "spring_failure", "master_curve", "friction_set", "bushing_element",
                             "contact_element", "damper_base", "external_control_system", "control_variable",
                             "control_line", "control_input", "control_element", "wind_point", "turbine_config",
@@ -1589,6 +1773,74 @@ static int setup(OracleModel& m, const char* fsi) {
     }
   }
   (void)pendingUnd;
+  // master-slave joints (initiateJointTypeModule.f90:120-600): one master
+  // triad, joint variables JointVarDefs = (lDof, iMat) pairs with at most one
+  // rotation per position matrix, no joint springs, dampers or friction
+  for (const Record& r : recs) {
+    if (r.name != "masterslavejoint") continue;
+    Joint J;
+    J.id = r.i("id");
+    J.type = r.i("type");
+    if (J.type != 1 && J.type != 3 && J.type != 4) return -70;  // revolute, rigid, free (point-to-point)
+    if (r.i("version") < 0) return -70;
+    J.slave = findTriad(m, r.i("slaveid"));
+    J.master = findTriad(m, r.i("masterid"));
+    if (J.slave < 0 || J.master < 0 || J.slave == J.master) return -71;
+    if (m.triads[J.slave].nDOFs != 6) return -72;
+    const int nv = r.i("njointvars", 0);
+    auto defs = r.dv("jointvardefs"), bc = r.dv("bc"), v0 = r.dv("jvarinitval");
+    for (const char* key : {"springid", "damperid", "frictionsetid", "frictionspringid", "frictionengineid"})
+      for (double v : r.dv(key))
+        if (v > 0.0) return -73;
+    for (int k = 0; k < nv; ++k) {
+      const int ld = 2 * k < (int)defs.size() ? (int)std::lround(defs[2 * k]) : 0;
+      const int im = 2 * k + 1 < (int)defs.size() ? (int)std::lround(defs[2 * k + 1]) : 0;
+      if (ld < 1 || ld > 6 || im < 1) return -74;
+      J.lDof.push_back(ld);
+      J.iMat.push_back(im);
+      J.BC.push_back(k < (int)bc.size() ? (int)std::lround(bc[k]) : 1);
+      J.jVar.push_back(k < (int)v0.size() ? v0[k] : 0.0);
+      J.nMats = std::max(J.nMats, im);
+    }
+    for (int im = 1; im <= J.nMats; ++im) {
+      int nrot = 0;
+      for (int k = 0; k < nv; ++k) nrot += J.iMat[k] == im && J.lDof[k] > 3;
+      if (nrot > 1) return -75;  // several rotations in one level need dOmega/dTheta
+    }
+    J.jVarPrev = J.jVar;
+    // joint position: initPosInGlobal row by row, rotation re-orthonormalised
+    auto pg = r.dv("initposinglobal");
+    rowMajor34(pg, J.JPosInG);
+    {
+      double R[3][3];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) R[a][b] = J.JPosInG[a][b];
+      orthonorm3(R);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) J.JPosInG[a][b] = R[a][b];
+    }
+    M34 inv, tmp;
+    invert34(J.JPosInG, inv);
+    matmul34(inv, m.triads[J.slave].ur, J.STPos0InJ);
+    for (int im = J.nMats; im >= 1; --im) {
+      M34 F, Fi;
+      jointPosFromVars(J, im, F);
+      invert34(F, Fi);
+      matmul34(Fi, J.STPos0InJ, tmp);
+      std::memcpy(J.STPos0InJ, tmp, sizeof(M34));
+    }
+    invert34(m.triads[J.master].ur, inv);
+    matmul34(inv, J.JPosInG, J.JPosInT);
+    J.nM = std::min(6, m.triads[J.master].nDOFs);
+    J.ncol = J.nM + nv;
+    J.T.assign(6 * (size_t)J.ncol, 0.0);
+    m.joints.push_back(J);
+  }
+  for (size_t a = 0; a < m.joints.size(); ++a)
+    for (size_t b = 0; b < m.joints.size(); ++b)
+      if (a != b && (m.joints[a].slave == m.joints[b].slave || m.joints[a].master == m.joints[b].slave))
+        return -76;  // a triad dependent twice, or chained joints
+  if (!m.joints.empty() && !m.motions.empty()) return -77;  // joints with prescribed motions: not in this subset
   m.axials = springs;
   m.axials.insert(m.axials.end(), dampers.begin(), dampers.end());
   for (const Axial& a : m.axials)
@@ -1659,9 +1911,22 @@ static int setup(OracleModel& m, const char* fsi) {
     m.ndof += t.nDOFs;
     std::memcpy(t.urPrev, t.ur, sizeof(M34));
   }
+  const int ntriDof = m.ndof;
+  for (Joint& J : m.joints) {  // joint DOFs after the triads (initSAM_dofStatus)
+    J.firstDof = m.ndof;
+    m.ndof += (int)J.lDof.size();
+  }
   m.meqn.assign(m.ndof, 0);
   m.dofType.assign(m.ndof, 1);
+  m.dep.assign(m.ndof, -1);
   m.neq = 0;
+  for (size_t j = 0; j < m.joints.size(); ++j) {
+    const Triad& st = m.triads[m.joints[j].slave];
+    for (int k = 0; k < 6; ++k) {
+      if (st.BC[k] != 1) return -78;  // a dependent DOF must be free
+      m.dep[st.firstDof + k] = 6 * (int)j + k;
+    }
+  }
   // BC 2 (fixed during initial equilibrium only) counts as free unless the
   // initial equilibrium iterations are on (initiateTriadTypeModule.f90:57-123)
   const bool addBC = m.opt.b("initEquilibrium", false);
@@ -1677,10 +1942,31 @@ static int setup(OracleModel& m, const char* fsi) {
     for (int k = 0; k < t.nDOFs; ++k) {
       int d = t.firstDof + k;
       m.dofType[d] = k < 3 ? 1 : 2;
+      if (m.dep[d] >= 0) continue;  // dependent (joint slave) DOF: no equation
       if (prescribed[d]) m.meqn[d] = -prescribed[d];  // MEQN = -ICEQ (samSolverModule.f90)
       else if (t.BC[k] == 1 || (t.BC[k] == 2 && !addBC)) m.meqn[d] = ++m.neq;
       else if (t.BC[k] != 0) return -30;  // additional initial-equilibrium BCs are not in this subset
     }
+  for (Joint& J : m.joints)
+    for (size_t k = 0; k < J.lDof.size(); ++k) {
+      const int d = J.firstDof + (int)k;
+      m.dofType[d] = J.lDof[k] <= 3 ? 1 : 2;
+      if (J.BC[k] == 1 || (J.BC[k] == 2 && !addBC)) m.meqn[d] = ++m.neq;
+      else if (J.BC[k] != 0) return -30;
+    }
+  (void)ntriDof;
+  for (Joint& J : m.joints) {
+    J.colEq.assign(J.ncol, -1);
+    for (int c = 0; c < J.nM; ++c) J.colEq[c] = m.meqn[m.triads[J.master].firstDof + c] - 1;
+    for (size_t k = 0; k < J.lDof.size(); ++k) J.colEq[J.nM + k] = m.meqn[J.firstDof + k] - 1;
+    for (int c = 0; c < J.ncol; ++c)
+      if (J.colEq[c] < -1) return -77;  // prescribed master DOF
+  }
+  for (const Axial& a : m.axials)
+    for (int k = 0; k < 2; ++k)
+      if (m.dep[m.triads[a.tri[k]].firstDof] >= 0) return -79;  // axial element on a dependent triad
+  for (const Load& l : m.loads)
+    if (m.dep[m.triads[l.triad].firstDof] >= 0) return -79;  // load on a dependent triad
   m.ccv.assign(m.motions.size(), 0.0);
   for (const Elem& e : m.elems)
     for (int k = 0; k < 2; ++k)
@@ -1707,7 +1993,25 @@ static int setup(OracleModel& m, const char* fsi) {
       }
     }
   };
-  for (size_t k = 0; k < m.elems.size(); ++k) clique(&m.elEq[12 * k], 12);
+  for (size_t k = 0; k < m.elems.size(); ++k) {
+    if (!elemConstrained(m, m.elems[k])) {
+      clique(&m.elEq[12 * k], 12);
+      continue;
+    }
+    // every equation the element's DOFs expand to (the coefficients vary)
+    std::vector<int> ex;
+    for (int n = 0; n < 2; ++n) {
+      const Triad& t = m.triads[m.elems[k].tri[n]];
+      const int d0 = t.firstDof;
+      if (m.dep[d0] >= 0) {
+        const Joint& J = m.joints[m.dep[d0] / 6];
+        for (int c = 0; c < J.ncol; ++c) ex.push_back(J.colEq[c]);
+      } else {
+        for (int q = 0; q < 6; ++q) ex.push_back(m.meqn[d0 + q] - 1);
+      }
+    }
+    clique(ex.data(), (int)ex.size());
+  }
   for (size_t k = 0; k < m.axials.size(); ++k) clique(&m.axEq[6 * k], 6);
   m.colptr.resize(m.neq + 1);
   m.colptr[0] = 0;
@@ -1877,6 +2181,7 @@ extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
       std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
       std::memcpy(e.finitPrev, e.finit, sizeof(e.finit));
     }
+    for (Joint& J : m->joints) J.jVarPrev = J.jVar;
   }
   for (size_t k = 0; k < m->triads.size(); ++k)
     for (int r = 0; r < 3; ++r) m->maxDisp = std::max(m->maxDisp, std::fabs(m->triads[k].ur[r][3] - m->x0[3 * k + r]));
@@ -1941,14 +2246,29 @@ extern "C" int oracle_assemble_newton(OracleModel* m, double sM, double sC, doub
     }
     rotatedElementMatrix(e, Nl, Ns);
     const int* eq = &m->elEq[12 * k];
+    auto add = [&](int a, int b, double v) {
+      const int* lo = &m->cols[m->rowptr[a]];
+      const int* en = &m->cols[0] + m->rowptr[a + 1];
+      values[std::lower_bound(lo, en, b) - &m->cols[0]] += v;
+    };
+    if (elemConstrained(*m, e)) {
+      std::vector<Term> ti, tj;
+      for (int i = 0; i < 12; ++i) {
+        dofTerms(*m, m->triads[e.tri[i / 6]].firstDof + i % 6, ti);
+        for (int j = 0; j < 12; ++j) {
+          dofTerms(*m, m->triads[e.tri[j / 6]].firstDof + j % 6, tj);
+          for (const Term& a : ti)
+            for (const Term& b : tj)
+              if (b.eq >= a.eq) add(a.eq, b.eq, a.c * b.c * Ns[i + 12 * j]);
+        }
+      }
+      continue;
+    }
     for (int i = 0; i < 12; ++i) {
       if (eq[i] < 0) continue;
       for (int j = 0; j < 12; ++j) {
         if (eq[j] < eq[i]) continue;
-        const int* b = &m->cols[m->rowptr[eq[i]]];
-        const int* en = &m->cols[0] + m->rowptr[eq[i] + 1];
-        const int* f = std::lower_bound(b, en, eq[j]);
-        values[f - &m->cols[0]] += Ns[i + 12 * j];
+        add(eq[i], eq[j], Ns[i + 12 * j]);
       }
     }
   }
