@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "kernels.h"
+#include "rotation.cuh"
 
 namespace fgpu {
 namespace {
@@ -30,60 +31,6 @@ namespace {
 constexpr int TPB = 256;
 
 inline int blocksFor(long long n, int tpb = TPB) { return (int)((n + tpb - 1) / tpb); }
-
-// 3x4 position matrices, column-major: T[r + 3c]
-__device__ inline void compose34(const double* a, const double* b, double* o) {
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      double s = a[r] * b[3 * c] + a[r + 3] * b[3 * c + 1] + a[r + 6] * b[3 * c + 2];
-      if (c == 3) s += a[r + 9];
-      o[r + 3 * c] = s;
-    }
-}
-
-__device__ inline void crossd(const double* a, const double* b, double* c) {
-  double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
-  c[0] = x; c[1] = y; c[2] = z;
-}
-
-// rotation tensor from a rotation vector through a unit quaternion
-// (rotationModule.f90:355-370,393-436).  For half angles below epsTh2 = 5e-4
-// the reference interpolates sin(h)/h linearly (sinEpsOverEps = sin(epsTh2)/epsTh2,
-// evaluated on the host); cos(h) is then its Taylor series to h^6 (the next
-// term is below 1e-30), which spares the FP64 sine/cosine on the usual small
-// increments.  The quaternion is normalised twice, by one reciprocal square
-// root each.
-__device__ inline void rotvecToMat(const double* rv, double sinEpsOverEps, double* R /* col-major 3x3 */) {
-  const double epsTh2 = 0.0005;
-  double thh = 0.5 * sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
-  double cthh, fac;
-  if (thh < epsTh2) {
-    const double h2 = thh * thh;
-    cthh = 1.0 - h2 * (0.5 - h2 * (1.0 / 24.0 - h2 * (1.0 / 720.0)));
-    double f1 = thh / epsTh2;
-    fac = f1 * sinEpsOverEps + 1.0 - f1;
-  } else {
-    double sthh;
-    sincos(thh, &sthh, &cthh);
-    fac = sthh / thh;
-  }
-  double q0 = cthh, q1 = rv[0] * fac * 0.5, q2 = rv[1] * fac * 0.5, q3 = rv[2] * fac * 0.5;
-  double inv = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-  q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
-  inv = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-  q0 *= inv; q1 *= inv; q2 *= inv; q3 *= inv;
-  R[0] = 2.0 * (q1 * q1 + q0 * q0) - 1.0;
-  R[4] = 2.0 * (q2 * q2 + q0 * q0) - 1.0;
-  R[8] = 2.0 * (q3 * q3 + q0 * q0) - 1.0;
-  R[3] = 2.0 * (q1 * q2 - q3 * q0);
-  R[6] = 2.0 * (q1 * q3 + q2 * q0);
-  R[7] = 2.0 * (q2 * q3 - q1 * q0);
-  R[1] = 2.0 * (q2 * q1 + q3 * q0);
-  R[2] = 2.0 * (q3 * q1 - q2 * q0);
-  R[5] = 2.0 * (q3 * q2 + q1 * q0);
-}
 
 // re-orthonormalise a rotation tensor through its quaternion (Spurrier)
 __device__ inline void orthonormRot(double* R /* col-major 3x3 */) {
@@ -120,6 +67,22 @@ __device__ inline void orthonormRot(double* R /* col-major 3x3 */) {
   R[1] = 2.0 * (q[2] * q[1] + q[3] * q[0]);
   R[2] = 2.0 * (q[3] * q[1] - q[2] * q[0]);
   R[5] = 2.0 * (q[3] * q[2] + q[1] * q[0]);
+}
+
+// value of a dependent DOF (a joint's slave triad) from the equation vector eqv
+// scaled by f: its row of the joint's constraint coefficients (csExpand,
+// solExtensionModule.f90:1352-1387; the constant term of a joint is zero)
+__device__ inline double dependentValue(const DevData& d, int dd, const double* eqv, double f) {
+  const int j = dd / 6, r = dd % 6;
+  const double* T = d.jT + 72 * (size_t)j + 12 * r;
+  const int* ce = d.jColEq + 12 * j;
+  const int nc = d.jNcol[j];
+  double s = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    const int q = ce[c];
+    if (q >= 0) s += T[c] * (eqv[q] * f);
+  }
+  return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -223,8 +186,12 @@ __global__ void kPredictDofs(DevData d) {
       double s = 0.0;
       const double* FI = d.Fel + (size_t)24 * d.nelTot;
       const int beamLim = 12 * d.nelTot;  // axial elements have no inertia forces
-      for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k)
-        if (d.eqSrc[k] < beamLim) s += FI[d.eqSrc[k]];
+      const int xLim = beamLim + 6 * d.naxTot;  // expanded forces of elements with a dependent triad
+      for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) {
+        const int src = d.eqSrc[k];
+        if (src < beamLim) s += FI[src];
+        else if (src >= xLim) s += d.FelX[src - xLim + 2];
+      }
       d.FIact[i] = s;
     }
   }
@@ -620,6 +587,14 @@ __global__ void kResidual(DevData d) {
     }
   };
   auto load = [&](size_t s, double& v0, double& v1, double& v2, double& v3) {
+    if (s >= blk + ablk) {  // expanded forces (FS, FD, FI, Q interleaved)
+      const double* b = d.FelX + (s - blk - ablk);
+      v0 = b[0];
+      v1 = b[1];
+      v2 = b[2];
+      v3 = b[3];
+      return true;
+    }
     const bool el = s < blk;
     const double* b = el ? d.Fel + s : d.FelA + (s - blk);
     const size_t st = el ? blk : ablk;
@@ -800,7 +775,9 @@ __global__ void __launch_bounds__(128) kNewtonBeam(DevData d) {
 constexpr int kGatherSlotsPerThread = 4;
 
 __device__ __forceinline__ double gatherEntry(const DevData& d, int src, int64_t lim) {
-  return src < lim ? d.elMat[src] : d.elMatA[src - lim];
+  if (src < lim) return d.elMat[src];
+  const int64_t lim2 = lim + (int64_t)36 * d.naxTot;  // expanded matrices of elements with a dependent triad
+  return src < lim2 ? d.elMatA[src - lim] : d.elMatX[src - lim2];
 }
 
 // Grid-stride over the blocks of kSlotBlock slots with a grid of resident blocks only:
@@ -881,9 +858,11 @@ __global__ void kIncrement(DevData d) {
     if (fl & FL_ACTIVE) {
       int eq = d.meqn[i];
       // prescribed DOFs take their constraint value in the predictor and zero in
-      // corrector steps (solExtensionModule.f90:1352-1387); fixed DOFs are zero
+      // corrector steps (solExtensionModule.f90:1352-1387); fixed DOFs are zero;
+      // dependent DOFs their joint's constraint equation
       double s0 = eq >= 0 ? d.del[eq]
                           : (eq <= -2 && (fl & FL_PRED)) ? d.motCc[d.modelMotOff[m] - 2 - eq] : 0.0;
+      if (eq == -1 && d.dofDep && d.dofDep[i] >= 0) s0 = dependentValue(d, d.dofDep[i], d.del, 1.0);
       d.sinc0[i] = s0;
       double ri = d.rinc[i] + s0;
       d.rinc[i] = ri;
@@ -908,6 +887,7 @@ __global__ void kIncrement(DevData d) {
       for (int k = 0; k < nd && k < 6; ++k) {
         int eq = d.meqn[d0 + k];
         inc[k] = eq >= 0 ? d.del[eq] : (eq <= -2 && pred) ? d.motCc[d.modelMotOff[m] - 2 - eq] : 0.0;
+        if (eq == -1 && d.dofDep && d.dofDep[d0 + k] >= 0) inc[k] = dependentValue(d, d.dofDep[d0 + k], d.del, 1.0);
       }
       double* U = d.ur + 12 * (size_t)i;
       for (int r = 0; r < 3; ++r) U[9 + r] += inc[r];
@@ -1252,11 +1232,15 @@ __global__ void kStaticResidual(DevData d) {
   if (!(d.m.flags[m] & FL_STATIC)) return;
   double fs = 0.0, q = 0.0;
   const size_t blk = (size_t)12 * d.nelTot;
+  const size_t xlim = blk + (size_t)6 * d.naxTot;
   for (int k = d.eqPtr[i]; k < d.eqPtr[i + 1]; ++k) {
     size_t s = d.eqSrc[k];
     if (s < blk) {
       fs += d.Fel[s];
       q += d.Fel[s + 3 * blk];
+    } else if (s >= xlim) {
+      fs += d.FelX[s - xlim];
+      q += d.FelX[s - xlim + 3];
     } else {
       fs += d.FelA[s - blk];
     }
@@ -1300,6 +1284,7 @@ __global__ void kStaticIncrement(DevData d) {
     if (d.m.flags[m] & FL_STATIC) {
       int eq = d.meqn[i];
       double s0 = eq >= 0 ? d.del[eq] * d.m.staticScale[m] : 0.0;
+      if (eq == -1 && d.dofDep && d.dofDep[i] >= 0) s0 = dependentValue(d, d.dofDep[i], d.del, d.m.staticScale[m]);
       d.sinc0[i] = s0;
       d.rinc[i] += s0;
     }
@@ -1313,6 +1298,7 @@ __global__ void kStaticIncrement(DevData d) {
       for (int k = 0; k < nd && k < 6; ++k) {
         int eq = d.meqn[d0 + k];
         inc[k] = eq >= 0 ? d.del[eq] * f : 0.0;
+        if (eq == -1 && d.dofDep && d.dofDep[d0 + k] >= 0) inc[k] = dependentValue(d, d.dofDep[d0 + k], d.del, f);
       }
       double* U = d.ur + 12 * (size_t)i;
       for (int r = 0; r < 3; ++r) U[9 + r] += inc[r];
@@ -1360,8 +1346,10 @@ void launchPredictDofs(const DevData& d, cudaStream_t s) {
   kPredictDofs<<<blocksFor(n), TPB, 0, s>>>(d);
 }
 void launchElements(const DevData& d, int mode, cudaStream_t s) {
+  launchJoints(d, mode, s);  // dependent triads first, as UpdateMechanism updates the joints first
   if (d.nelTot > 0) kElements<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d, mode);
   if (d.naxTot > 0) kAxial<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d, mode);
+  launchExpandForces(d, mode, s);
 }
 void launchResidual(const DevData& d, cudaStream_t s) {
   if (d.neqTot > 0) kResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);
@@ -1374,6 +1362,7 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
   if (d.nelTot > 0 && d.beamSparse) kNewtonBeam<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
   else if (d.nelTot > 0) kRotateElementNewton<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
   if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
+  launchExpandElements(d, s);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
   if (d.nslotTot <= 0) return;

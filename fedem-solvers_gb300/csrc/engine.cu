@@ -503,6 +503,81 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     d_.elMatA = alloc<double>(36 * (size_t)nax);
   }
   trace.mark("axial elements", stream_);
+  // ---- master-slave joints and the elements holding a dependent triad ---------------------
+  std::vector<int> modelJointOff(nm, 0), modelCxOff(nm, 0);
+  std::vector<int64_t> cxMatBase(nm, 0), cxVecBase(nm, 0);
+  {
+    int nj = 0, ncx = 0;
+    int64_t xm = 0, xv = 0;
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      modelJointOff[k] = nj;
+      modelCxOff[k] = ncx;
+      cxMatBase[k] = xm;
+      cxVecBase[k] = xv;
+      nj += h.njoint;
+      ncx += (int)h.cxEl.size();
+      xm += h.cxMatSize;
+      xv += h.cxVecSize;
+    }
+    d_.njointTot = nj;
+    d_.ncxTot = ncx;
+    if (nj > 0) {
+      std::vector<int> jS, jM, jNM, jNc, jF, jNd, jNmat, jOff, jMod, jL, jI, jCE, dep(ndof, -1), cEl, cNx, cMO, cVO,
+          cNode;
+      std::vector<double> jV, jPT, jS0;
+      for (int k = 0; k < nm; ++k) {
+        const HostModel& h = *models[k];
+        for (int j = 0; j < h.njoint; ++j) {
+          jS.push_back(h.jSlave[j] + modelTriOff_[k]);
+          jM.push_back(h.jMaster[j] + modelTriOff_[k]);
+          jNM.push_back(h.jNM[j]);
+          jNc.push_back(h.jNM[j] + h.jNdof[j]);
+          jF.push_back(h.jFirstDof[j] + modelDofOff_[k]);
+          jNd.push_back(h.jNdof[j]);
+          jNmat.push_back(h.jNmats[j]);
+          jOff.push_back((int)jL.size());
+          jMod.push_back(k);
+          for (int q = h.jDofOff[j]; q < h.jDofOff[j + 1]; ++q) {
+            jL.push_back(h.jLdof[q]);
+            jI.push_back(h.jImat[q]);
+            jV.push_back(h.jVar0[q]);
+          }
+          for (int q = 0; q < 12; ++q) {
+            jPT.push_back(h.jPosInT[12 * j + q]);
+            jS0.push_back(h.jSTPos0[12 * j + q]);
+            const int e = h.jColEq[12 * j + q];
+            jCE.push_back(e >= 0 ? e + modelEqOff_[k] : -1);
+          }
+        }
+        for (int i = 0; i < h.ndof; ++i)
+          if (h.dofDep[i] >= 0) dep[modelDofOff_[k] + i] = h.dofDep[i] + 6 * modelJointOff[k];
+        for (size_t c = 0; c < h.cxEl.size(); ++c) {
+          const int e = h.cxEl[c];
+          cEl.push_back(e + modelElOff_[k]);
+          cNx.push_back(h.cxNx[c]);
+          cMO.push_back((int)(cxMatBase[k] + h.cxMatOff[c]));
+          cVO.push_back((int)(cxVecBase[k] + h.cxVecOff[c]));
+          for (int n = 0; n < 2; ++n) {
+            const int dd = h.dofDep[h.triFirstDof[h.elTri[2 * e + n]]];
+            cNode.push_back(dd >= 0 ? dd / 6 + modelJointOff[k] : -1);
+          }
+        }
+      }
+      if (xm >= INT_MAX / 2 || xv >= INT_MAX / 2) { err = "too many expanded element entries"; return -901; }
+      UPV(d_.jSlave, int, jS); UPV(d_.jMaster, int, jM); UPV(d_.jNM, int, jNM); UPV(d_.jNcol, int, jNc);
+      UPV(d_.jFirstDof, int, jF); UPV(d_.jNdof, int, jNd); UPV(d_.jNmats, int, jNmat); UPV(d_.jDofOff, int, jOff);
+      UPV(d_.jModel, int, jMod); UPV(d_.jLdof, int, jL); UPV(d_.jImat, int, jI); UPV(d_.jVar, double, jV);
+      UPV(d_.jPosInT, double, jPT); UPV(d_.jSTPos0, double, jS0); UPV(d_.jColEq, int, jCE);
+      UPV(d_.dofDep, int, dep);
+      d_.jT = alloc<double>(72 * (size_t)nj);
+      UPV(d_.cxEl, int, cEl); UPV(d_.cxNx, int, cNx); UPV(d_.cxMatOff, int, cMO); UPV(d_.cxVecOff, int, cVO);
+      UPV(d_.cxNode, int, cNode);
+      d_.elMatX = alloc<double>((size_t)std::max<int64_t>(xm, 1));
+      d_.FelX = alloc<double>((size_t)std::max<int64_t>(xv, 1));
+    }
+  }
+  trace.mark("joints", stream_);
   // ---- CSR and gather maps -----------------------------------------------------------
   {
     if (ncontrib >= INT_MAX || 144LL * nel + 36LL * nax >= INT_MAX) {
@@ -525,13 +600,16 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         slotPtr[s0 + s + 1] = (int)(contribOff[k] + h.slotPtr[s + 1]);
       }
       int64_t o = contribOff[k];
+      const int hx = 144 * h.nel + 36 * h.nax, hv = 12 * h.nel + 6 * h.nax;
       for (int src : h.slotSrc) {
         if (src < 144 * h.nel) {
           int e = src / 144, entry = src % 144;
           slotSrc[o++] = entry * nel + modelElOff_[k] + e;
-        } else {  // axial element entry
+        } else if (src < hx) {  // axial element entry
           int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
           slotSrc[o++] = 144 * nel + entry * nax + modelAxOff[k] + a;
+        } else {  // expanded matrix of an element with a dependent triad
+          slotSrc[o++] = (int)(144LL * nel + 36LL * nax + cxMatBase[k] + (src - hx));
         }
       }
       o = eqContribOff[k];
@@ -539,9 +617,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         if (src < 12 * h.nel) {
           int e = src / 12, loc = src % 12;
           eqSrc[o++] = loc * nel + modelElOff_[k] + e;
-        } else {
+        } else if (src < hv) {
           int a = (src - 12 * h.nel) / 6, loc = (src - 12 * h.nel) % 6;
           eqSrc[o++] = 12 * nel + loc * nax + modelAxOff[k] + a;
+        } else {  // expanded forces of an element with a dependent triad
+          eqSrc[o++] = (int)(12LL * nel + 6LL * nax + cxVecBase[k] + (src - hv));
         }
       }
     });
@@ -847,6 +927,16 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     reg(d_.axLen, D * (size_t)d_.naxTot);
     reg(d_.FelA, D * 12 * (size_t)d_.naxTot);
   }
+  if (d_.njointTot > 0) {
+    size_t nv = 0, xv = 0;
+    for (int k = 0; k < nm; ++k) {
+      nv += models[k]->jLdof.size();
+      xv += (size_t)models[k]->cxVecSize;
+    }
+    if (nv) reg(d_.jVar, D * nv);
+    reg(d_.jT, D * 72 * (size_t)d_.njointTot);
+    if (xv) reg(d_.FelX, D * xv);
+  }
   uploadedBytes_ = t_putBytes;
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
@@ -1144,7 +1234,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   const int solveLaunches = 2 * sw - 1 + (sw - 1);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
-                     (d_.nldTot > 0 ? 1 : 0);
+                     (d_.nldTot > 0 ? 1 : 0) + (d_.njointTot > 0 ? 2 : 0) + (d_.ncxTot > 0 ? 3 : 0);
 }
 
 int Engine::readActive() {

@@ -152,6 +152,28 @@ struct DevData {
   int linearIters = 1;
   // sin(5e-4) / 5e-4 for the small-angle branch of the rotation update
   double sinEpsOverEps = 1.0;
+  // master-slave joints (one master triad each; see host_model.h): slave and
+  // master triad, master DOFs in T, columns of T, first joint DOF, joint DOF
+  // count, position-matrix levels, first entry in the per-joint-DOF arrays,
+  // model; joint frame in the master's axes and the slave's start position in
+  // the joint frame (12 each); constraint coefficients T (6 rows x 12 columns
+  // per joint, row-major) and the global equation of each column (12, -1 fixed)
+  int njointTot = 0;
+  int *jSlave, *jMaster, *jNM, *jNcol, *jFirstDof, *jNdof, *jNmats, *jDofOff, *jModel;
+  int *jLdof, *jImat;  // per joint DOF: 1..6 and level (1-based)
+  double* jVar;        // per joint DOF: current value
+  double *jPosInT, *jSTPos0, *jT;
+  int* jColEq;
+  int* dofDep;  // per DOF: 6 * joint + row of a dependent DOF, else -1 (null without joints)
+  // elements with a dependent triad: their element, expanded DOF count, offsets
+  // of the expanded Newton matrix (elMatX, nx x nx column-major) and of the
+  // expanded forces (FelX: FS, FD, FI, Q interleaved per expanded DOF), and per
+  // node the joint whose dependent triad it is (-1 for a free triad).  Gather
+  // sources at or above 144 * nelTot + 36 * naxTot (matrix) and 12 * nelTot +
+  // 6 * naxTot (forces) address these with that offset removed.
+  int ncxTot = 0;
+  int *cxEl, *cxNx, *cxMatOff, *cxVecOff, *cxNode;
+  double *elMatX, *FelX;
   // DOF chunks for the two-stage norm reduction (each chunk within one model)
   int nchunkTot = 0;
   int *chunkModel, *chunkStart, *chunkEnd, *modelChunkOff, *modelNchunk;

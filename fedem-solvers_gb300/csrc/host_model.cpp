@@ -215,6 +215,68 @@ int frameFrom3Points(const double* p1, const double* p2, const double* p3, doubl
   return 0;
 }
 
+// Rotation tensor (column-major 3x3) from a rotation vector through a unit
+// quaternion (rotationModule.f90:355-370, 393-436, 478-500)
+void rotvecToMat(const double* rv, double* R) {
+  const double epsTh2 = 0.0005;
+  const double thh = 0.5 * std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+  double fac;
+  if (thh < epsTh2) {
+    const double f1 = thh / epsTh2;
+    fac = f1 * std::sin(epsTh2) / epsTh2 + 1.0 - f1;
+  } else {
+    fac = std::sin(thh) / thh;
+  }
+  double q[4] = {std::cos(thh), rv[0] * fac * 0.5, rv[1] * fac * 0.5, rv[2] * fac * 0.5};
+  for (int pass = 0; pass < 2; ++pass) {
+    const double n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    for (double& v : q) v /= n;
+  }
+  R[0] = 2.0 * (q[1] * q[1] + q[0] * q[0]) - 1.0;
+  R[4] = 2.0 * (q[2] * q[2] + q[0] * q[0]) - 1.0;
+  R[8] = 2.0 * (q[3] * q[3] + q[0] * q[0]) - 1.0;
+  R[3] = 2.0 * (q[1] * q[2] - q[3] * q[0]);
+  R[6] = 2.0 * (q[1] * q[3] + q[2] * q[0]);
+  R[7] = 2.0 * (q[2] * q[3] - q[1] * q[0]);
+  R[1] = 2.0 * (q[2] * q[1] + q[3] * q[0]);
+  R[2] = 2.0 * (q[3] * q[1] - q[2] * q[0]);
+  R[5] = 2.0 * (q[3] * q[2] + q[1] * q[0]);
+}
+
+// Re-orthonormalise the rotation part of a 3x4 matrix through its quaternion
+// (rotationModule.f90:447-476, 478-500)
+void orthonormRot34(double* T) {
+  auto r = [&](int i, int j) { return T[i + 3 * j]; };
+  double q[4];
+  const double tr = r(0, 0) + r(1, 1) + r(2, 2);
+  int imax = 0;
+  if (r(1, 1) > r(imax, imax)) imax = 1;
+  if (r(2, 2) > r(imax, imax)) imax = 2;
+  if (tr > r(imax, imax)) {
+    q[0] = std::sqrt(1.0 + tr) * 0.5;
+    q[1] = (r(2, 1) - r(1, 2)) / (4.0 * q[0]);
+    q[2] = (r(0, 2) - r(2, 0)) / (4.0 * q[0]);
+    q[3] = (r(1, 0) - r(0, 1)) / (4.0 * q[0]);
+  } else {
+    const int i = imax, j = (imax + 1) % 3, k = (imax + 2) % 3;
+    q[i + 1] = std::sqrt(r(i, i) * 0.5 + (1.0 - tr) * 0.25);
+    q[0] = (r(k, j) - r(j, k)) / (4.0 * q[i + 1]);
+    q[j + 1] = (r(j, i) + r(i, j)) / (4.0 * q[i + 1]);
+    q[k + 1] = (r(k, i) + r(i, k)) / (4.0 * q[i + 1]);
+  }
+  const double n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (double& v : q) v /= n;
+  T[0] = 2.0 * (q[1] * q[1] + q[0] * q[0]) - 1.0;
+  T[4] = 2.0 * (q[2] * q[2] + q[0] * q[0]) - 1.0;
+  T[8] = 2.0 * (q[3] * q[3] + q[0] * q[0]) - 1.0;
+  T[3] = 2.0 * (q[1] * q[2] - q[3] * q[0]);
+  T[6] = 2.0 * (q[1] * q[3] + q[2] * q[0]);
+  T[7] = 2.0 * (q[2] * q[3] - q[1] * q[0]);
+  T[1] = 2.0 * (q[2] * q[1] + q[3] * q[0]);
+  T[2] = 2.0 * (q[3] * q[1] - q[2] * q[0]);
+  T[5] = 2.0 * (q[3] * q[2] + q[1] * q[0]);
+}
+
 // ---------------------------------------------------------------------------
 // 12-DOF beam element matrices in superelement axes (Femlib BEAM31/BEAM35).
 // E is column-major; e(i,j) uses 1-based indices like the element library.
@@ -479,7 +541,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   std::vector<NmlRecord> recs = readNamelists(fsi);
   // record types this path does not implement are refused, never dropped
   for (const NmlRecord& nr : recs)
-    for (const char* bad : {"masterslavejoint", "higher_pair", "mass", "user_el", "tire", "road", "supel_load",
+    for (const char* bad : {"higher_pair", "mass", "user_el", "tire", "road", "supel_load",
                             "spring_yield", "spring_failure", "master_curve", "friction_set", "bushing_element",
                             "contact_element", "damper_base", "external_control_system", "control_variable",
                             "control_line", "control_input", "control_element", "wind_point", "turbine_config",
@@ -631,6 +693,74 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       return -28;
     }
   }
+  // master-slave joints (initiateJointTypeModule.f90:120-600): one master
+  // triad; joint variables JointVarDefs = (lDof, iMat) pairs with at most one
+  // rotation per position matrix; no joint springs, dampers or friction
+  struct JointIn {
+    int slave, master, nMats = 0;
+    std::vector<int> ldof, imat, bc;
+    std::vector<double> v0;
+    double PJG[12];
+  };
+  std::vector<JointIn> jin;
+  for (const NmlRecord& nr : recs) {
+    if (nr.name != "masterslavejoint") continue;
+    Rec r{nr};
+    const int type = r.inum("type", 0);
+    if (type != 1 && type != 3 && type != 4) {
+      err = "only point-to-point revolute, rigid and free joints (type 1, 3, 4) are supported";
+      return -70;
+    }
+    if (r.inum("version", 0) < 0) { err = "free joints without rotation coupling are not supported"; return -70; }
+    JointIn J;
+    auto si = triIndex.find(r.inum("slaveid", 0)), mi = triIndex.find(r.inum("masterid", 0));
+    if (si == triIndex.end() || mi == triIndex.end() || si->second == mi->second) {
+      err = "joint with an invalid dependent or independent triad";
+      return -71;
+    }
+    J.slave = si->second;
+    J.master = mi->second;
+    if (m.triNdof[J.slave] != 6) { err = "the dependent triad of a joint needs 6 DOFs"; return -72; }
+    for (const char* key : {"springid", "damperid", "frictionsetid", "frictionspringid", "frictionengineid"})
+      for (double v : r.nums(key))
+        if (v > 0.0) { err = "joint springs, dampers and friction are not supported"; return -73; }
+    const int nv = r.inum("njointvars", 0);
+    auto defs = r.nums("jointvardefs"), bc = r.nums("bc"), v0 = r.nums("jvarinitval");
+    for (int k = 0; k < nv; ++k) {
+      const int ld = 2 * k < (int)defs.size() ? (int)std::lround(defs[2 * k]) : 0;
+      const int im = 2 * k + 1 < (int)defs.size() ? (int)std::lround(defs[2 * k + 1]) : 0;
+      if (ld < 1 || ld > 6 || im < 1) { err = "invalid joint variable definition"; return -74; }
+      J.ldof.push_back(ld);
+      J.imat.push_back(im);
+      J.bc.push_back(k < (int)bc.size() ? (int)std::lround(bc[k]) : 1);
+      J.v0.push_back(k < (int)v0.size() ? v0[k] : 0.0);
+      J.nMats = std::max(J.nMats, im);
+    }
+    for (int im = 1; im <= J.nMats; ++im) {
+      int nrot = 0;
+      for (int k = 0; k < nv; ++k) nrot += J.imat[k] == im && J.ldof[k] > 3;
+      if (nrot > 1) { err = "joints with several rotations in one position matrix are not supported"; return -75; }
+    }
+    auto pg = r.nums("initposinglobal");  // 3x4 row by row
+    for (int col = 0; col < 4; ++col)
+      for (int row = 0; row < 3; ++row) {
+        const size_t k = (size_t)(4 * row + col);
+        J.PJG[row + 3 * col] = k < pg.size() ? pg[k] : 0.0;
+      }
+    orthonormRot34(J.PJG);
+    jin.push_back(J);
+  }
+  for (size_t a = 0; a < jin.size(); ++a)
+    for (size_t b = 0; b < jin.size(); ++b)
+      if (a != b && (jin[a].slave == jin[b].slave || jin[a].master == jin[b].slave)) {
+        err = "a triad dependent in two joints, or chained joints, are not supported";
+        return -76;
+      }
+  if (!jin.empty() && !m.motD0.empty()) { err = "joints together with prescribed motions are not supported"; return -77; }
+  if (!jin.empty() && c.tQStatic > c.tStart && c.fixedIt == -1) {
+    err = "joints together with pure linear quasi-static steps are not supported";
+    return -77;
+  }
   if (!m.motD0.empty() && c.tQStatic > c.tStart && c.fixedIt < -1) {
     err = "quasi-static steps need numit = -1 (linear) or numit >= 0";
     return -29;
@@ -645,10 +775,18 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   std::vector<int> bcs = m.dofType;  // temporarily holds the BC codes, 6 per triad
   m.dofType.clear();
   m.triFirstDof.resize(m.ntri);
+  std::vector<int> slaveOf(m.ntri, -1);
+  for (size_t j = 0; j < jin.size(); ++j) slaveOf[jin[j].slave] = (int)j;
   for (int t = 0; t < m.ntri; ++t) {
     m.triFirstDof[t] = m.ndof;
     for (int k = 0; k < m.triNdof[t]; ++k) {
       int bc = bcs[6 * t + k];
+      if (slaveOf[t] >= 0) {  // dependent DOF of a joint: no equation (samSolverModule.f90:613-633)
+        if (bc != 1 && !(bc == 2 && !c.initEquilibrium)) { err = "a joint's dependent triad must be free"; return -78; }
+        m.meqn.push_back(-1);
+        m.dofType.push_back(k < 3 ? 1 : 2);
+        continue;
+      }
       if (bc == 2 && !c.initEquilibrium) bc = 1;
       if (bc != 0 && bc != 1) { err = "BC code other than 0, 1 or 2 (2 only without initEquilibrium)"; return -30; }
       const int mot = motionOfDof[6 * (size_t)t + k];
@@ -661,6 +799,64 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       m.dofType.push_back(k < 3 ? 1 : 2);
     }
     m.ndof += m.triNdof[t];
+  }
+  m.dofDep.assign(m.ndof, -1);
+  for (size_t j = 0; j < jin.size(); ++j)
+    for (int k = 0; k < 6; ++k) m.dofDep[m.triFirstDof[jin[j].slave] + k] = 6 * (int)j + k;
+  // joint DOFs after all triad DOFs (initSAM_dofStatus, samSolverModule.f90:95-250)
+  m.njoint = (int)jin.size();
+  for (size_t j = 0; j < jin.size(); ++j) {
+    const JointIn& J = jin[j];
+    const int nv = (int)J.ldof.size();
+    m.jSlave.push_back(J.slave);
+    m.jMaster.push_back(J.master);
+    m.jNM.push_back(std::min(6, m.triNdof[J.master]));
+    m.jFirstDof.push_back(m.ndof);
+    m.jNdof.push_back(nv);
+    m.jNmats.push_back(J.nMats);
+    m.jDofOff.push_back((int)m.jLdof.size());
+    for (int k = 0; k < nv; ++k) {
+      const int bc = J.bc[k];
+      if (bc != 0 && bc != 1 && !(bc == 2 && !c.initEquilibrium)) { err = "joint DOF BC other than 0, 1"; return -30; }
+      m.meqn.push_back(bc != 0 ? m.neq++ : -1);
+      m.dofType.push_back(J.ldof[k] <= 3 ? 1 : 2);
+      m.dofDep.push_back(-1);
+      m.jLdof.push_back(J.ldof[k]);
+      m.jImat.push_back(J.imat[k]);
+      m.jVar0.push_back(J.v0[k]);
+    }
+    m.ndof += nv;
+    // joint frame in the master triad's axes and the slave's start position in
+    // the joint frame with every joint variable at zero (initiateJointTypeModule.f90:564-598)
+    double inv[12], S0[12], tmp[12];
+    inverse34(J.PJG, inv);
+    compose34(inv, &m.ur[12 * (size_t)J.slave], S0);
+    for (int im = J.nMats; im >= 1; --im) {
+      double F[12] = {0}, th[3] = {0, 0, 0}, Fi[12];
+      for (int k = 0; k < nv; ++k)
+        if (J.imat[k] == im) {
+          if (J.ldof[k] <= 3) F[9 + J.ldof[k] - 1] = J.v0[k];
+          else th[J.ldof[k] - 4] = J.v0[k];
+        }
+      rotvecToMat(th, F);
+      inverse34(F, Fi);
+      compose34(Fi, S0, tmp);
+      std::memcpy(S0, tmp, sizeof(S0));
+    }
+    for (double v : S0) m.jSTPos0.push_back(v);
+    inverse34(&m.ur[12 * (size_t)J.master], inv);
+    compose34(inv, J.PJG, tmp);
+    for (double v : tmp) m.jPosInT.push_back(v);
+  }
+  m.jDofOff.push_back((int)m.jLdof.size());
+  for (int j = 0; j < m.njoint; ++j) {
+    for (int col = 0; col < 12; ++col) {
+      int e = -1;
+      if (col < m.jNM[j]) e = m.meqn[m.triFirstDof[m.jMaster[j]] + col];
+      else if (col - m.jNM[j] < m.jNdof[j]) e = m.meqn[m.jFirstDof[j] + col - m.jNM[j]];
+      if (e < -1) { err = "a joint's independent triad has a prescribed DOF"; return -77; }
+      m.jColEq.push_back(e);
+    }
   }
   // pass 2: superelements, undeformed positions, loads
   std::map<int, std::vector<std::array<double, 5>>> engineLoads;  // equation -> (f0, f1, eA, eB, channel)
@@ -740,6 +936,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (it == triIndex.end()) { err = "load on unknown triad"; return -17; }
       int dof = r.inum("ldof", 0);
       if (dof < 1 || dof > m.triNdof[it->second]) { err = "load DOF must be 1..6"; return -18; }
+      if (m.dofDep[m.triFirstDof[it->second]] >= 0) { err = "loads on a joint's dependent triad are not supported"; return -79; }
       int eq = m.meqn[m.triFirstDof[it->second] + dof - 1];
       const int eid = r.inum("loadengineid", 0);
       if (eid > 0) {
@@ -818,6 +1015,10 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       }
       for (int k = 0; k < 2; ++k) {
         if (m.triNdof[t[k]] < 3) { err = "axial element triads need translational DOFs"; return -47; }
+        if (m.dofDep[m.triFirstDof[t[k]]] >= 0) {
+          err = "springs and dampers on a joint's dependent triad are not supported";
+          return -79;
+        }
         m.axTri.push_back(t[k]);
       }
       m.nax++;
@@ -875,6 +1076,34 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   for (int a = 0; a < m.nax; ++a)
     for (int n = 0; n < 2; ++n)
       for (int d = 0; d < 3; ++d) m.axEq[6 * a + 3 * n + d] = m.meqn[m.triFirstDof[m.axTri[2 * a + n]] + d];
+  // elements with a joint's dependent triad: expanded DOFs (the master's DOFs
+  // and the joint DOFs in place of the dependent triad's; asmSparse with
+  // MEEN < 0, sysMatrixTypeModule.f90:2099-2259)
+  m.elCx.assign(m.nel, -1);
+  for (int e = 0; e < m.nel; ++e) {
+    const int ta = m.elTri[2 * e], tb = m.elTri[2 * e + 1];
+    if (m.dofDep[m.triFirstDof[ta]] < 0 && m.dofDep[m.triFirstDof[tb]] < 0) continue;
+    m.elCx[e] = (int)m.cxEl.size();
+    m.cxEl.push_back(e);
+    m.cxEqOff.push_back((int)m.cxEq.size());
+    for (int n = 0; n < 2; ++n) {
+      const int t = m.elTri[2 * e + n], dd = m.dofDep[m.triFirstDof[t]];
+      if (dd >= 0) {
+        const int j = dd / 6;
+        for (int col = 0; col < m.jNM[j] + m.jNdof[j]; ++col) m.cxEq.push_back(m.jColEq[12 * j + col]);
+      } else {
+        for (int d = 0; d < 6; ++d) m.cxEq.push_back(m.meqn[m.triFirstDof[t] + d]);
+      }
+    }
+    const int nx = (int)m.cxEq.size() - m.cxEqOff.back();
+    m.cxNx.push_back(nx);
+    m.cxMatOff.push_back(m.cxMatSize);
+    m.cxVecOff.push_back(m.cxVecSize);
+    m.cxMatSize += nx * nx;
+    m.cxVecSize += 4 * nx;
+  }
+  m.cxEqOff.push_back((int)m.cxEq.size());
+  const int xMatBase = 144 * m.nel + 36 * m.nax, xVecBase = 12 * m.nel + 6 * m.nax;
   // full symmetric CSR pattern (union of element cliques, diagonal always present)
   std::vector<std::vector<int>> rows(m.neq);
   for (int i = 0; i < m.neq; ++i) rows[i].push_back(i);
@@ -885,7 +1114,11 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
         if (q[j] >= 0) rows[q[i]].push_back(q[j]);
     }
   };
-  for (int e = 0; e < m.nel; ++e) clique(&m.elEq[12 * e], 12);
+  for (int e = 0; e < m.nel; ++e) {
+    const int c = m.elCx[e];
+    if (c < 0) clique(&m.elEq[12 * e], 12);
+    else clique(&m.cxEq[m.cxEqOff[c]], m.cxNx[c]);
+  }
   for (int a = 0; a < m.nax; ++a) clique(&m.axEq[6 * a], 6);
   m.rowPtr.assign(m.neq + 1, 0);
   for (int i = 0; i < m.neq; ++i) {
@@ -898,15 +1131,17 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   // slot <- (element, entry) lists, in element order (deterministic summation order)
   std::vector<std::vector<int>> slotList(m.colInd.size());
   for (int e = 0; e < m.nel; ++e) {
-    const int* q = &m.elEq[12 * e];
-    for (int i = 0; i < 12; ++i) {
+    const int c = m.elCx[e];
+    const int n = c < 0 ? 12 : m.cxNx[c];
+    const int* q = c < 0 ? &m.elEq[12 * e] : &m.cxEq[m.cxEqOff[c]];
+    for (int i = 0; i < n; ++i) {
       if (q[i] < 0) continue;
       const int* b = &m.colInd[m.rowPtr[q[i]]];
       const int* en = &m.colInd[0] + m.rowPtr[q[i] + 1];
-      for (int j = 0; j < 12; ++j) {
+      for (int j = 0; j < n; ++j) {
         if (q[j] < 0) continue;
         int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
-        slotList[slot].push_back(144 * e + i + 12 * j);
+        slotList[slot].push_back(c < 0 ? 144 * e + i + 12 * j : xMatBase + m.cxMatOff[c] + i + n * j);
       }
     }
   }
@@ -928,9 +1163,18 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   for (auto& l : slotList) m.slotSrc.insert(m.slotSrc.end(), l.begin(), l.end());
   // equation <- (element, local DOF) lists
   std::vector<std::vector<int>> eqList(m.neq);
-  for (int e = 0; e < m.nel; ++e)
-    for (int i = 0; i < 12; ++i)
-      if (m.elEq[12 * e + i] >= 0) eqList[m.elEq[12 * e + i]].push_back(12 * e + i);
+  for (int e = 0; e < m.nel; ++e) {
+    const int c = m.elCx[e];
+    if (c < 0) {
+      for (int i = 0; i < 12; ++i)
+        if (m.elEq[12 * e + i] >= 0) eqList[m.elEq[12 * e + i]].push_back(12 * e + i);
+    } else {
+      for (int i = 0; i < m.cxNx[c]; ++i) {
+        const int q = m.cxEq[m.cxEqOff[c] + i];
+        if (q >= 0) eqList[q].push_back(xVecBase + m.cxVecOff[c] + 4 * i);
+      }
+    }
+  }
   for (int a = 0; a < m.nax; ++a)
     for (int i = 0; i < 6; ++i)
       if (m.axEq[6 * a + i] >= 0) eqList[m.axEq[6 * a + i]].push_back(12 * m.nel + 6 * a + i);

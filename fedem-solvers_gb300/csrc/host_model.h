@@ -93,11 +93,37 @@ struct HostModel {
   // predictor right-hand-side terms of the prescribed DOFs: equation mrEq[k] gets
   // -cc(motion mrMot[q]) * elMat[mrSrc[q]] for q in mrPtr[k]..mrPtr[k+1] (mrSrc = 144*e + entry)
   std::vector<int> mrEq, mrPtr, mrSrc, mrMot;
+  // master-slave joints with one master triad (masterSlaveJointTypeModule.f90):
+  // the slave triad's 6 DOFs are dependent, u_s = T [u_master; joint DOFs], T
+  // (6 x ncol, ncol = nM master DOFs + the joint DOFs) rebuilt from the current
+  // geometry after every increment.  Joint DOFs follow all triad DOFs (SAM
+  // order).  Per joint: slave and master triad, master DOFs in T (0 for a
+  // grounded master), first joint DOF, its DOF count and position-matrix levels,
+  // first entry in the per-joint-DOF arrays; joint frame in the master's axes and
+  // the slave's start position in the joint frame (3x4 column-major each); the
+  // 0-based equation of every column of T (-1 for a fixed DOF).
+  int njoint = 0;
+  std::vector<int> jSlave, jMaster, jNM, jFirstDof, jNdof, jNmats, jDofOff;
+  std::vector<int> jLdof, jImat;      // per joint DOF: 1..6 and level (1-based)
+  std::vector<double> jVar0;          // per joint DOF: start value
+  std::vector<double> jPosInT, jSTPos0;  // 12 per joint
+  std::vector<int> jColEq;            // 12 per joint
+  std::vector<int> dofDep;            // per DOF: 6 * joint + row of a dependent DOF, else -1
+  // elements with a dependent triad: their DOFs expand through T.  Per such
+  // element: the element, its expanded DOF count nx (6 per free triad, ncol per
+  // dependent one) and the offsets of its expanded equations (cxEq), of its
+  // expanded Newton matrix (nx x nx, column-major) and of its expanded force
+  // vectors (FS, FD, FI, Q interleaved, 4 per expanded DOF)
+  std::vector<int> cxEl, cxNx, cxEqOff, cxMatOff, cxVecOff, cxEq;
+  std::vector<int> elCx;  // per element: its index in cxEl, or -1
+  int cxMatSize = 0, cxVecSize = 0;
   // full symmetric CSR pattern of the Newton matrix, equation order
   std::vector<int> rowPtr, colInd;
   // deterministic gather maps: CSR slot <- (element, entry); equation <- (element, local dof)
   // (axial elements follow the beams: slotSrc = 144*nel + 36*axial + entry,
   // eqSrc = 12*nel + 6*axial + local, mrSrc like slotSrc)
+  // (expanded elements follow the axial ones: slotSrc = 144*nel + 36*nax +
+  // cxMatOff + p + nx*q, eqSrc = 12*nel + 6*nax + cxVecOff + 4*p)
   std::vector<int> slotPtr, slotSrc;   // slotSrc = 144*element + entry
   std::vector<int> eqPtr, eqSrc;       // eqSrc = 12*element + local dof
   // multifrontal symbolic factorisation

@@ -50,6 +50,15 @@ void launchStaticNorm(const DevData& d, cudaStream_t s);
 void launchStaticIncrement(const DevData& d, cudaStream_t s);
 void launchStaticFinish(const DevData& d, cudaStream_t s);
 
+// --- joint_kernels.cu: master-slave joints ----------------------------------
+// per joint: joint variables incremented (EM_INC, EM_STATIC), dependent triad
+// placed, constraint coefficients rebuilt; same model gating as the element pass
+void launchJoints(const DevData& d, int mode, cudaStream_t s);
+// expanded Newton matrices of the elements with a dependent triad (tangent models)
+void launchExpandElements(const DevData& d, cudaStream_t s);
+// expanded forces of those elements after an element pass of this mode
+void launchExpandForces(const DevData& d, int mode, cudaStream_t s);
+
 // --- front_cascade.cu: one launch per phase over all fronts of all models ----
 struct PersistentPlan {
   const int* leaves;  // fronts without children, longest root path first (factorisation)

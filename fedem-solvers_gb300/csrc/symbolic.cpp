@@ -6,7 +6,9 @@
 // (src/vpmCommon/vpmLinAlg/asmExtensionModule.f90:227-893: SPRPRP, SPRSAS,
 // SPRRNM, SPRTRS, SPRSMB).  SPR's source is not part of the reference tree,
 // so the ordering here is our own, deterministic and documented:
-//   * equations are grouped by triad (all free DOFs of a triad form one node);
+//   * equations are grouped by triad and by joint (all free DOFs of a triad, or
+//     all free DOFs of a joint, form one node); nodes are adjacent when the
+//     Newton matrix pattern couples them;
 //   * nested dissection on the node graph: breadth-first level structures
 //     from a pseudo-peripheral node, the separator is the smallest level set
 //     in the middle third; components of at most LEAF_NODES nodes are leaves;
@@ -60,30 +62,34 @@ void bfs(const NodeGraph& g, int start, const std::vector<int>& mark, int tag, s
 
 int symbolicAnalysis(HostModel& m, std::string& err) {
   // ---- node graph -------------------------------------------------------
+  // nodes: the free equations of each triad, then of each joint (DOF order);
+  // two nodes are adjacent when the Newton matrix couples their equations
   NodeGraph g;
-  std::vector<int> nodeOfTriad(m.ntri, -1);
-  for (int t = 0; t < m.ntri; ++t) {
-    bool anyFree = false;
-    for (int d = 0; d < m.triNdof[t]; ++d) anyFree |= m.meqn[m.triFirstDof[t] + d] >= 0;
-    if (anyFree) nodeOfTriad[t] = g.n++;
-  }
-  g.eqPtr.assign(g.n + 1, 0);
-  for (int t = 0; t < m.ntri; ++t) {
-    int v = nodeOfTriad[t];
-    if (v < 0) continue;
-    for (int d = 0; d < m.triNdof[t]; ++d)
-      if (m.meqn[m.triFirstDof[t] + d] >= 0) g.eqs.push_back(m.meqn[m.triFirstDof[t] + d]);
-    g.eqPtr[v + 1] = (int)g.eqs.size();
-  }
+  std::vector<int> eqNode(m.neq, -1);
+  g.eqPtr.assign(1, 0);
+  auto addNode = [&](int d0, int nd) {
+    bool any = false;
+    for (int d = d0; d < d0 + nd; ++d)
+      if (m.meqn[d] >= 0) {
+        eqNode[m.meqn[d]] = g.n;
+        g.eqs.push_back(m.meqn[d]);
+        any = true;
+      }
+    if (any) {
+      g.eqPtr.push_back((int)g.eqs.size());
+      ++g.n;
+    }
+  };
+  for (int t = 0; t < m.ntri; ++t) addNode(m.triFirstDof[t], m.triNdof[t]);
+  for (int j = 0; j < m.njoint; ++j) addNode(m.jFirstDof[j], m.jNdof[j]);
+  for (int e = 0; e < m.neq; ++e)
+    if (eqNode[e] < 0) { err = "equation without a node"; return -43; }
   std::vector<std::vector<int>> nb(g.n);
-  for (int e = 0; e < m.nel; ++e) {
-    int a = nodeOfTriad[m.elTri[2 * e]], b = nodeOfTriad[m.elTri[2 * e + 1]];
-    if (a >= 0 && b >= 0 && a != b) { nb[a].push_back(b); nb[b].push_back(a); }
-  }
-  for (int k = 0; k < m.nax; ++k) {  // axial springs and dampers couple their two triads
-    int a = nodeOfTriad[m.axTri[2 * k]], b = nodeOfTriad[m.axTri[2 * k + 1]];
-    if (a >= 0 && b >= 0 && a != b) { nb[a].push_back(b); nb[b].push_back(a); }
-  }
+  for (int i = 0; i < m.neq; ++i)
+    for (int k = m.rowPtr[i]; k < m.rowPtr[i + 1]; ++k) {
+      const int a = eqNode[i], b = eqNode[m.colInd[k]];
+      if (a != b) nb[a].push_back(b);
+    }
   g.adjPtr.assign(g.n + 1, 0);
   for (int v = 0; v < g.n; ++v) {
     std::sort(nb[v].begin(), nb[v].end());

@@ -21,6 +21,10 @@ def _models():
     out.append((_frame_with_axials(), ["-timeInc=0.001", "-timeEnd=0.05"]))
     with open(os.path.join(GOLDEN_DIR, "cantilever_prescribed.fsi")) as f:
         out.append((f.read(), ["-numit=-1", "-timeInc=0.2", "-timeEnd=1.0", "-quasiStatic=1.0"]))
+    # master-slave joints: a revolute hinge, a rigid joint, a pendulum on a grounded master
+    out.append((models.hinged_beam(joint_type=1)[0], ["-timeInc=0.001", "-timeEnd=0.05"]))
+    out.append((models.hinged_beam(joint_type=3)[0], ["-timeInc=0.001", "-timeEnd=0.05"]))
+    out.append((models.pendulum()[0], ["-timeInc=0.001", "-timeEnd=0.05"]))
     return out
 
 
@@ -36,7 +40,7 @@ def _frame_with_axials():
                                  dampers=[(30, ("anchor", 0), 300.0), (5, 18, 120.0)])
 
 
-N_MODELS = 10
+N_MODELS = 13
 
 
 @pytest.mark.parametrize("idx", range(N_MODELS))
@@ -170,17 +174,20 @@ def test_prescribed_dofs_numbered_as_the_oracle(gpu_lib, oracle_lib):
 
 
 def test_unsupported_records_fail_loudly_and_bc2_is_free(gpu_lib):
-    """Engine-driven loads are refused with a message instead of being
-    dropped; BC code 2 counts as a free DOF when the initial equilibrium
-    iterations are off (initiateTriadTypeModule.f90:57-123)."""
+    """Input the GPU path does not implement (here a reference to an unknown
+    engine, higher pairs, point-to-path joints) is refused with a message
+    instead of being dropped; BC code 2 counts as a free DOF when the initial
+    equilibrium iterations are off (initiateTriadTypeModule.f90:57-123)."""
     from fedem_gb300 import FedemException, models
     from fedem_gb300.batch import Model
 
     base = models.beam_chain_fsi(4, 1.0, 0.1, 0.01, clamp=0, load_node=4, load_dof=2, load=10.0, **models.STEEL)
     with pytest.raises(FedemException, match="unknown engine"):
         Model(base.replace("  f0 =", "  loadEngineId = 7\n  f0 ="), [])
-    with pytest.raises(FedemException, match="MASTERSLAVEJOINT|masterslavejoint"):
-        Model(base + "&MASTERSLAVEJOINT\n  id = 99\n  type = 'REVOLUTE'\n/\n", [])
+    with pytest.raises(FedemException, match="HIGHER_PAIR|higher_pair"):
+        Model(base + "&HIGHER_PAIR\n  id = 99\n/\n", [])
+    with pytest.raises(FedemException, match="joints"):  # point-to-path joint types
+        Model(base + "&MASTERSLAVEJOINT\n  id = 99\n  type = 6\n  slaveId = 5\n  masterId = 4\n/\n", [])
     free = Model(base, [])
     bc2 = Model(base.replace("&TRIAD\n  id = 5\n  nDOFs = 6\n", "&TRIAD\n  id = 5\n  nDOFs = 6\n  BC = 2 2 2 2 2 2\n"), [])
     assert bc2.neq == free.neq
