@@ -451,6 +451,10 @@ double evalFunc(int uid, const char* tag, double x, int* ierr) {
     if (m.engFType[k] == 3) return s.engine->extValue(0, m.engCh[k]);
     if (m.engFType[k] == 2) return m.engFc[k];
     const double arg = hasX ? x : (m.engTimeArg[k] ? s.engine->modelTime(0) : 0.0);
+    if (m.engFType[k] == 4) {  // SINUSOIDAL: frequency, delay, amplitude, mean
+      const double* sp = &m.engSin[4 * k];
+      return sp[3] + sp[2] * std::sin(2.0 * M_PI * (sp[0] * arg - sp[1]));
+    }
     return m.engFType[k] == 1 ? m.engFc[k] * arg : arg;
   };
   bool found = false;

@@ -97,6 +97,14 @@ __device__ inline void seedBackward(const BackwardSeed& b, int i) {
     const int base = atomicAdd(ctr + 1, nr);
     for (int k = 0; k < nr; ++k) queue[base + k] = b.roots[r0 + k];
     atomicAdd(ctr + 2, b.slotCnt[i]);
+    if (b.strideL > 0) {  // the large roots into the large-front queue
+      const int l0 = b.rootOffL[i], nl = b.rootOffL[i + 1] - l0;
+      int* ctrL = b.ctrL + 4 * q;
+      int* queueL = b.queueL + (size_t)q * b.strideL;
+      const int baseL = atomicAdd(ctrL + 1, nl);
+      for (int k = 0; k < nl; ++k) queueL[baseL + k] = b.rootsL[l0 + k];
+      atomicAdd(ctrL + 2, b.slotCntL[i]);
+    }
   }
 }
 
@@ -925,7 +933,10 @@ __global__ void kLoads(DevData d) {
   double q = d.qextBase[eq];
   for (int j = d.ldPtr[k]; j < d.ldPtr[k + 1]; ++j) {
     const int ch = d.ldCh[j];
-    q += d.ldF0[j] + d.ldF1[j] * (ch >= 0 ? d.extVal[ch] : d.ldEA[j] * t + d.ldEB[j]);
+    double ev = ch >= 0 ? d.extVal[ch] : d.ldEA[j] * t + d.ldEB[j];
+    const double* sp = d.ldSin + 4 * (size_t)j;
+    if (sp[2] != 0.0 || sp[3] != 0.0) ev += sp[3] + sp[2] * sin(2.0 * M_PI * (sp[0] * t - sp[1]));
+    q += d.ldF0[j] + d.ldF1[j] * ev;
   }
   d.qext[eq] = q;
 }

@@ -252,7 +252,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   }
   auto extAt = [&](int k, int ch) { return ch < (int)models[k]->extInit.size() ? models[k]->extInit[ch] : 0.0; };
   // engine-driven loads: constant part kept, start-time value in qext
-  std::vector<double> qextBase = qext, ldF0, ldF1, ldEA, ldEB;
+  std::vector<double> qextBase = qext, ldF0, ldF1, ldEA, ldEB, ldSin;
   std::vector<int> ldEq, ldPtr(1, 0), ldCh;
   for (int k = 0; k < nm; ++k) {
     const HostModel& h = *models[k];
@@ -264,7 +264,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
         ldF0.push_back(h.ldF0[j]); ldF1.push_back(h.ldF1[j]); ldEA.push_back(h.ldEA[j]); ldEB.push_back(h.ldEB[j]);
         const int ch = h.ldCh[j];
         ldCh.push_back(ch >= 0 ? ch + modelExtOff_[k] : -1);
-        v += h.ldF0[j] + h.ldF1[j] * (ch >= 0 ? extAt(k, ch) : h.ldEA[j] * h.ctl.tStart + h.ldEB[j]);
+        const double* sp = &h.ldSin[4 * (size_t)j];
+        for (int q = 0; q < 4; ++q) ldSin.push_back(sp[q]);
+        double ev = ch >= 0 ? extAt(k, ch) : h.ldEA[j] * h.ctl.tStart + h.ldEB[j];
+        if (sp[2] != 0.0 || sp[3] != 0.0) ev += sp[3] + sp[2] * std::sin(2.0 * M_PI * (sp[0] * h.ctl.tStart - sp[1]));
+        v += h.ldF0[j] + h.ldF1[j] * ev;
       }
       qext[eq] = v;
       ldPtr.push_back((int)ldF0.size());
@@ -279,6 +283,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   UPV(d_.qextBase, double, qextBase); UPV(d_.ldEq, int, ldEq); UPV(d_.ldPtr, int, ldPtr);
   UPV(d_.ldF0, double, ldF0); UPV(d_.ldF1, double, ldF1); UPV(d_.ldEA, double, ldEA); UPV(d_.ldEB, double, ldEB);
   UPV(d_.ldCh, int, ldCh);
+  UPV(d_.ldSin, double, ldSin);
   d_.nextTot = nextTot;
   UPV(d_.extVal, double, extInit);
   {
@@ -771,12 +776,35 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       d_.L64 = alloc<double>(nl); d_.U64 = alloc<double>(nu); d_.w64 = alloc<double>(nw);
       if (!d_.L64 || !d_.U64 || !d_.w64) { err = "out of device memory (factor)"; return -904; }
     }
-    int maxRowAll = 1;
-    for (int f = 0; f < nfr; ++f) maxRowAll = std::max(maxRowAll, nrow[f]);
+    // large fronts (more than kLargeFrontRows rows) and all their ancestors go to
+    // the block-per-front kernels; the warp kernels size their shared memory by
+    // the small fronts only
+    std::vector<unsigned char> large(nfr, 0);
+    std::vector<int> nLargeChild(nfr, 0);
+    for (int f = 0; f < nfr; ++f) {
+      if (nrow[f] > kLargeFrontRows) large[f] = 1;
+      if (large[f] && parent[f] >= 0) large[parent[f]] = 1;  // parents follow their children
+    }
+    int maxRowAll = 1, maxRowLarge = 0, nLargeFronts = 0;
+    for (int f = 0; f < nfr; ++f) {
+      if (large[f]) {
+        maxRowLarge = std::max(maxRowLarge, nrow[f]);
+        ++nLargeFronts;
+        if (parent[f] >= 0) ++nLargeChild[parent[f]];
+      } else {
+        maxRowAll = std::max(maxRowAll, nrow[f]);
+      }
+    }
     if (((size_t)maxRowAll * maxRowAll + 3 * maxRowAll) * (opt_.fp32Factor ? 4 : 8) > 200 * 1024) {
       err = "front too large for the shared-memory front kernels";
       return -905;
     }
+    if (maxRowLarge >= 1024) { err = "front of 1024 rows or more"; return -905; }
+    UPV(d_.fLarge, uint8_t, large);
+    UPV(d_.fNlarge, int, nLargeChild);
+    pplan_.fLarge = d_.fLarge;
+    pplan_.fNlarge = d_.fNlarge;
+    pplan_.maxRowLarge = maxRowLarge;
     // leaf-to-root path lengths: parents follow their children in each model's order
     std::vector<int> pathLen(nfr, 1);
     for (int f = nfr - 1; f >= 0; --f) {
@@ -785,10 +813,19 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     }
     // tasks with the longest paths first: the cascades' critical paths (the
     // deep trees of the large models) start in the first wave of warps
-    std::vector<int> leaves;
-    for (int f = 0; f < nfr; ++f)
-      if (nchild[f] == 0) leaves.push_back(f);
+    std::vector<int> leaves, largeTasks;
+    for (int f = 0; f < nfr; ++f) {
+      if (nchild[f] == 0 && !large[f]) leaves.push_back(f);
+      if (large[f] && nLargeChild[f] == 0) largeTasks.push_back(f);
+    }
     std::stable_sort(leaves.begin(), leaves.end(), [&](int a, int b) { return pathLen[a] > pathLen[b]; });
+    std::stable_sort(largeTasks.begin(), largeTasks.end(), [&](int a, int b) { return pathLen[a] > pathLen[b]; });
+    if (!largeTasks.empty()) {
+      int* dLT = nullptr;
+      UPV(dLT, int, largeTasks);
+      pplan_.largeTasks = dLT;
+    }
+    pplan_.nLargeTasks = (int)largeTasks.size();
     int* dLeaves = nullptr;
     UPV(dLeaves, int, leaves);
     pplan_.leaves = dLeaves;
@@ -800,7 +837,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     // block within the staging capacity); other leaves are tasks of their own
     pplan_.maxRow = maxRowAll;
     pplan_.maxNpiv = 1;
-    for (int f = 0; f < nfr; ++f) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
+    for (int f = 0; f < nfr; ++f)
+      if (!large[f]) pplan_.maxNpiv = std::max(pplan_.maxNpiv, npiv[f]);
     const long long capL = stagingCapacity(pplan_, opt_.fp32Factor ? sizeof(float) : sizeof(double));
     auto fastFront = [&](int f) { return nrow[f] <= 64 && (long long)nrow[f] * npiv[f] <= capL; };
     std::vector<char> inGroup(nfr, 0), isHead(nfr, 0);
@@ -838,14 +876,29 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     // a chain ends at a leaf not solved inline or at an inline front
     std::vector<unsigned char> bwInline(nfr, 0);
     for (int f = 0; f < nfr; ++f) {
-      bool all = nchild[f] > 0;
+      bool all = nchild[f] > 0 && !large[f];
       for (int c = 0; c < nchild[f] && all; ++c) all = nchild[childList[childOffV[f] + c]] == 0;
       bwInline[f] = all ? 1 : 0;
     }
+    // the warp queue starts at the tops of the small subtrees (roots, or fronts
+    // under a large parent); the large-front queue at the large roots, its
+    // chains ending at large fronts without large children
+    auto smallTop = [&](int f) { return !large[f] && (parent[f] < 0 || large[parent[f]]); };
     std::vector<int> rootOff(nm + 1, 0), roots, leafCnt(nm, 0);
+    std::vector<int> rootOffL(nm + 1, 0), rootsL, chainL(nm, 0);
     for (int f = 0; f < nfr; ++f) {
-      if (parent[f] < 0) ++rootOff[fmodel[f] + 1];
-      if (bwInline[f] || (nchild[f] == 0 && !(parent[f] >= 0 && bwInline[parent[f]]))) ++leafCnt[fmodel[f]];
+      if (smallTop(f)) ++rootOff[fmodel[f] + 1];
+      if (!large[f] && (bwInline[f] || (nchild[f] == 0 && !(parent[f] >= 0 && bwInline[parent[f]]))))
+        ++leafCnt[fmodel[f]];
+      if (large[f] && parent[f] < 0) ++rootOffL[fmodel[f] + 1];
+      if (large[f] && nLargeChild[f] == 0) ++chainL[fmodel[f]];
+    }
+    for (int m = 0; m < nm; ++m) rootOffL[m + 1] += rootOffL[m];
+    rootsL.resize(rootOffL[nm]);
+    {
+      std::vector<int> fill(rootOffL.begin(), rootOffL.end() - 1);
+      for (int f = 0; f < nfr; ++f)
+        if (large[f] && parent[f] < 0) rootsL[fill[fmodel[f]]++] = f;
     }
     {
       unsigned char* dInline = nullptr;
@@ -857,7 +910,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     {
       std::vector<int> fill(rootOff.begin(), rootOff.end() - 1);
       for (int f = 0; f < nfr; ++f)
-        if (parent[f] < 0) roots[fill[fmodel[f]]++] = f;
+        if (smallTop(f)) roots[fill[fmodel[f]]++] = f;
     }
     int *dRootOff = nullptr, *dRoots = nullptr, *dLeafCnt = nullptr;
     UPV(dRootOff, int, rootOff);
@@ -868,7 +921,10 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     // counters (4 per solve), the factorisation's per-front counters and one set
     // per refinement forward elimination (each + its leaf counter)
     const int nq = std::max(1, opt_.fp32Factor ? opt_.refineSweeps : 1);
-    ctrInts_ = 4 + 4 * (size_t)nq + (size_t)nq * (nfr + 1);
+    // with large fronts: their queue counters (4 per solve) and per-front counters
+    // (factor + one set per refinement forward elimination) follow
+    const size_t largeInts = nLargeFronts > 0 ? 4 * (size_t)nq + (size_t)nq * (nfr + 1) : 0;
+    ctrInts_ = 4 + 4 * (size_t)nq + (size_t)nq * (nfr + 1) + largeInts;
     ctrBlock_ = alloc<int>(ctrInts_);
     if (!ctrBlock_) { err = "out of device memory (counters)"; return -906; }
     dActive_ = ctrBlock_;
@@ -878,6 +934,24 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     pplan_.cntForward = pplan_.cntFactor + (nfr + 1);
     pplan_.bwQueue = alloc<int>((size_t)nq * std::max<size_t>(leaves.size(), 1));
     queueInts_ = (size_t)nq * std::max<size_t>(leaves.size(), 1);
+    if (nLargeFronts > 0) {
+      pplan_.bwLCtr = pplan_.cntFactor + (size_t)nq * (nfr + 1);
+      pplan_.cntLargeFactor = pplan_.bwLCtr + 4 * nq;
+      pplan_.cntLargeForward = pplan_.cntLargeFactor + (nfr + 1);
+      pplan_.largeStride = std::max<int>((int)largeTasks.size(), 1);
+      pplan_.bwLQueue = alloc<int>((size_t)nq * pplan_.largeStride);
+      largeQueueInts_ = (size_t)nq * pplan_.largeStride;
+      int *dRootOffL = nullptr, *dRootsL = nullptr, *dChainL = nullptr;
+      UPV(dRootOffL, int, rootOffL);
+      UPV(dRootsL, int, rootsL);
+      UPV(dChainL, int, chainL);
+      seed_.strideL = pplan_.largeStride;
+      seed_.rootOffL = dRootOffL;
+      seed_.rootsL = dRootsL;
+      seed_.slotCntL = dChainL;
+      seed_.queueL = pplan_.bwLQueue;
+      seed_.ctrL = pplan_.bwLCtr;
+    }
     seed_.nq = nq;
     seed_.stride = (int)std::max<size_t>(leaves.size(), 1);
     seed_.rootOff = dRootOff;
@@ -990,11 +1064,15 @@ int Engine::timeFactor(int reps, double* msPerLaunch, double* bytes) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const size_t cntBytes = sizeof(int) * ((size_t)d_.nfrontTot + 1);
-  cudaMemsetAsync(pplan_.cntFactor, 0, cntBytes, stream_);
+  auto clear = [&]() {
+    cudaMemsetAsync(pplan_.cntFactor, 0, cntBytes, stream_);
+    if (pplan_.cntLargeFactor) cudaMemsetAsync(pplan_.cntLargeFactor, 0, cntBytes, stream_);
+  };
+  clear();
   enqueueFactor(stream_);  // warm-up
   cudaEventRecord(e0, stream_);
   for (int k = 0; k < reps; ++k) {
-    cudaMemsetAsync(pplan_.cntFactor, 0, cntBytes, stream_);
+    clear();
     enqueueFactor(stream_);
   }
   cudaEventRecord(e1, stream_);
@@ -1024,8 +1102,10 @@ void Engine::resetPhaseTimings() {
 }
 
 void Engine::enqueueFactor(cudaStream_t s) {
-  // factorisation and the first forward elimination in one cascade
+  // factorisation and the first forward elimination in one cascade (small
+  // fronts by warps, then the large fronts above them by thread blocks)
   launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
+  launchLargeFactorForward(d_, pplan_, opt_.fp32Factor, d_.del, s);
 }
 
 // phase-timing events: external event nodes inside a captured graph, plain
@@ -1048,9 +1128,13 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
     // the first forward elimination ran with the factorisation
     if (sweep > 0) launchRefineResidual(d_, s);
     if (sweep == 1 && timedForward) recordPhase(ev_[5], s);
-    if (sweep > 0) launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
+    if (sweep > 0) {
+      launchForwardCascade(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
+      launchLargeForward(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
+    }
     if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
     if (sweep == 0 && timedForward) recordPhase(ev_[7], s);
+    launchLargeBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
     launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
     if (sweep == 0 && timedForward) recordPhase(ev_[8], s);
   }
@@ -1061,6 +1145,7 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
 void Engine::resetIterationCounters(cudaStream_t s) {
   cudaMemsetAsync(ctrBlock_, 0, sizeof(int) * ctrInts_, s);
   if (queueInts_) cudaMemsetAsync(pplan_.bwQueue, 0xff, sizeof(int) * queueInts_, s);
+  if (largeQueueInts_) cudaMemsetAsync(pplan_.bwLQueue, 0xff, sizeof(int) * largeQueueInts_, s);
 }
 
 // first half of a Newton iteration: step start (predictor) or the corrector's
@@ -1231,8 +1316,9 @@ void Engine::enqueueIteration(cudaStream_t s) {
   // increment, norms partial + control, step end) + the factorisation with the first
   // forward elimination + per further solve a refinement residual and a forward
   // elimination + a back substitution per solve
-  const int solveLaunches = 2 * sw - 1 + (sw - 1);
-  launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl + solveLaunches + (d_.urQs ? 1 : 0) +
+  const int solveLaunches = (2 * sw - 1 + (sw - 1)) * (pplan_.nLargeTasks > 0 ? 2 : 1);
+  launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl * (pplan_.nLargeTasks > 0 ? 2 : 1) + solveLaunches +
+                     (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
                      (d_.nldTot > 0 ? 1 : 0) + (d_.njointTot > 0 ? 2 : 0) + (d_.ncxTot > 0 ? 3 : 0);
 }

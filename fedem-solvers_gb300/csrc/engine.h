@@ -160,7 +160,7 @@ class Engine {
   std::vector<int> savedFlags_;
   double factorBytes_ = 0.0;  // algorithmic bytes of one factor + first forward launch, all models
   int* ctrBlock_ = nullptr;   // the iteration counters (see upload)
-  size_t ctrInts_ = 0, queueInts_ = 0;
+  size_t ctrInts_ = 0, queueInts_ = 0, largeQueueInts_ = 0;
   BackwardSeed seed_;
   void resetIterationCounters(cudaStream_t s);
   void invalidateNewtonScales();

@@ -92,6 +92,9 @@ struct DevData {
   int64_t *fRowOff, *fLOff, *fUOff, *fWOff, *fChildOff, *fRelOff, *fAsmOff;  // fUOff: the front's packed
                                                                             // update matrix in its parent's segment
   int *frontRows, *childList, *relIndex;
+  // large fronts (one thread block each) and every front's number of large children
+  uint8_t* fLarge;
+  int* fNlarge;
   // children's update rows of each front, in child order: W index and
   // (child ordinal << 16 | destination row), cgOff[f]..cgOff[f+1]
   int *cgOff, *cgSrc, *cgDst;
@@ -120,6 +123,7 @@ struct DevData {
   int nldTot = 0;
   int *ldEq, *ldPtr;
   double *ldF0, *ldF1, *ldEA, *ldEB, *qextBase;
+  double* ldSin;  // 4 per load term: SINUSOIDAL frequency, delay, amplitude, mean (zeros otherwise)
   // external functions: a load term or motion whose engine is one (ldCh / motCh
   // >= 0, a global channel) takes extVal[ch] instead of eA * t + eB
   int* ldCh;

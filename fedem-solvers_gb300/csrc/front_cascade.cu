@@ -298,7 +298,8 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
 }
 
 // After a front is done: release its data and count it at the parent; returns
-// the parent if this warp completed the parent's count (and must go on), else -1.
+// the parent if this warp completed the parent's count (and must go on), else -1
+// (also for a large parent: the large-front kernels take it up afterwards).
 // The warp barrier orders every lane's stores before lane 0's counter update,
 // a release-acquire RMW at GPU scope (no full fence): the warp that completes
 // the count acquires the children's stores, and its barrier passes them on to
@@ -308,7 +309,7 @@ __device__ inline int climb(const DevData& d, int f, int* cnt, int lane) {
   int next = -1;
   if (lane == 0) {
     const int p = d.fParent[f];
-    if (p >= 0) {
+    if (p >= 0 && !d.fLarge[p]) {  // a large parent is left to the large-front kernels
       int old;
       asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(cnt + p) : "memory");
       if (old == d.fNchild[p] - 1) next = p;

@@ -592,10 +592,15 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   // (realData(1)), none (x), or an external function: DEVICE_FUNCTION without
   // a file, whose value on channel `channel` the caller sets (setExtFunc).
   // Stored as x-coefficient eA, constant eB and external channel (0-based, -1 none).
+  // SINUSOIDAL: realData = frequency (Hz), delay (periods), amplitude, mean;
+  // value mean + amplitude * sin(2 pi (frequency x - delay)) (the first three
+  // as the reference's regular-wave use of the function reads them,
+  // hydroDynamicsModule.f90:345-349)
   struct FuncDef {
     std::string type;
     double c = 0.0;
     int channel = 0;
+    double sine[4] = {0, 0, 0, 0};
   };
   std::map<int, FuncDef> funcs;  // id -> definition
   std::map<int, bool> timeSensor;  // id -> TIME sensor
@@ -606,6 +611,8 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       FuncDef fd;
       fd.type = r.str("type");
       fd.c = rd.empty() ? (fd.type == "scale" ? 1.0 : 0.0) : rd[0];
+      if (fd.type == "sinusoidal")
+        for (size_t k = 0; k < 4 && k < rd.size(); ++k) fd.sine[k] = rd[k];
       if (fd.type == "device_function") {
         if (!r.raw("filename").empty()) { err = "device functions reading a file are not supported"; return -22; }
         fd.channel = r.inum("channel", 0);
@@ -619,6 +626,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   struct EngineVal {
     double eA, eB;
     int ch;
+    double sine[4];
   };
   std::map<int, EngineVal> engines;  // id -> value coefficients
   for (const NmlRecord& nr : recs) {
@@ -632,7 +640,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     }
     double eA = xs, eB = 0.0;
     int ch = -1, ftype = 0;
-    double fc = 0.0;
+    double fc = 0.0, sine[4] = {0, 0, 0, 0};
     if (fid > 0) {
       auto it = funcs.find(fid);
       if (it == funcs.end()) { err = "engine refers to unknown function"; return -21; }
@@ -640,10 +648,19 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (it->second.type == "scale") { eA = it->second.c * xs; ftype = 1; }
       else if (it->second.type == "constant") { eA = 0.0; eB = it->second.c; ftype = 2; }
       else if (it->second.type == "device_function") { eA = 0.0; ch = it->second.channel - 1; ftype = 3; }
-      else { err = "function type '" + it->second.type + "' is not supported (SCALE, CONSTANT, DEVICE_FUNCTION)"; return -22; }
+      else if (it->second.type == "sinusoidal") {
+        eA = 0.0;
+        ftype = 4;
+        for (int k = 0; k < 4; ++k) sine[k] = it->second.sine[k];
+        sine[0] *= xs;  // frequency 0 without a TIME sensor: a constant
+      } else {
+        err = "function type '" + it->second.type + "' is not supported (SCALE, CONSTANT, SINUSOIDAL, DEVICE_FUNCTION)";
+        return -22;
+      }
     }
     const int id = r.inum("id", 0);
-    engines[id] = {eA, eB, ch};
+    engines[id] = {eA, eB, ch, {sine[0], sine[1], sine[2], sine[3]}};
+    for (double v : sine) m.engSin.push_back(v);
     // the engine table for evalFunc / getFuncId (solverModule.f90:1602-1680)
     auto ext = r.nums("extid");
     m.engId.push_back(id);
@@ -680,6 +697,10 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       eA = e->second.eA;
       eB = e->second.eB;
       ch = e->second.ch;
+      if (e->second.sine[2] != 0.0 || e->second.sine[3] != 0.0) {
+        err = "prescribed motions driven by a SINUSOIDAL function are not supported";
+        return -27;
+      }
     } else {
       d1 = 0.0;
     }
@@ -859,7 +880,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     }
   }
   // pass 2: superelements, undeformed positions, loads
-  std::map<int, std::vector<std::array<double, 5>>> engineLoads;  // equation -> (f0, f1, eA, eB, channel)
+  std::map<int, std::vector<std::array<double, 9>>> engineLoads;  // equation -> (f0, f1, eA, eB, channel, sine x4)
   std::vector<int> elProp;
   std::map<int, int> elIndex;
   m.qext.assign(m.neq, 0.0);
@@ -944,7 +965,8 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
         if (en == engines.end()) { err = "load refers to unknown engine"; return -19; }
         if (eq >= 0)
           engineLoads[eq].push_back({r.num("f0", 0.0), r.num("f1", 0.0), en->second.eA, en->second.eB,
-                                     (double)en->second.ch});
+                                     (double)en->second.ch, en->second.sine[0], en->second.sine[1],
+                                     en->second.sine[2], en->second.sine[3]});
       } else if (eq >= 0) {
         m.qext[eq] += r.num("f0", 0.0);
       }
@@ -956,6 +978,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     for (auto& l : kv.second) {
       m.ldF0.push_back(l[0]); m.ldF1.push_back(l[1]); m.ldEA.push_back(l[2]); m.ldEB.push_back(l[3]);
       m.ldCh.push_back((int)l[4]);
+      for (int k = 5; k < 9; ++k) m.ldSin.push_back(l[k]);
     }
     m.ldPtr.push_back((int)m.ldF0.size());
   }

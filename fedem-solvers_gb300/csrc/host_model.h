@@ -77,12 +77,18 @@ struct HostModel {
   std::vector<int> ldEq, ldPtr;
   std::vector<double> ldF0, ldF1, ldEA, ldEB;
   std::vector<int> ldCh;  // external channel of the load's engine (value ext[ch] instead of eA t + eB), -1 none
+  // a load term whose engine is a SINUSOIDAL function adds mean + amplitude *
+  // sin(2 pi (frequency x - delay)), x the time for a TIME sensor, else 0: 4
+  // values per load term (frequency (0 without a TIME sensor), delay,
+  // amplitude, mean; all 0 for other engines)
+  std::vector<double> ldSin;
   // engines: base id, user id, tag, value eA t + eB (+ ext[ch] when ch >= 0), the
-  // function (0 none, 1 SCALE fc x, 2 CONSTANT fc, 3 external) and whether its
+  // function (0 none, 1 SCALE fc x, 2 CONSTANT fc, 3 external, 4 SINUSOIDAL) and whether its
   // argument is the time; nExt: external channels used
   std::vector<int> engId, engUserId, engCh, engFType, engTimeArg;
   std::vector<std::string> engTag;
   std::vector<double> engEA, engEB, engFc;
+  std::vector<double> engSin;  // 4 per engine: SINUSOIDAL parameters as for ldSin
   int nExt = 0;
   std::vector<double> extInit;  // initial external function values (empty: zero)
   // prescribed deflections (motionRoutinesModule.f90:58-193): D(t) = d0 + d1 * (eA * t + eB)

@@ -26,11 +26,22 @@ enum ElemMode : int {
 struct BackwardSeed {
   int nq = 0;      // queues (solves per iteration)
   int stride = 0;  // slots per queue
-  const int* rootOff = nullptr;  // per model: its roots in roots[rootOff[m]..rootOff[m+1])
+  // per model: the tops of its small-front subtrees (fronts whose parent is a
+  // large front, or roots) in roots[rootOff[m]..rootOff[m+1]), and its number
+  // of chains
+  const int* rootOff = nullptr;
   const int* roots = nullptr;
-  const int* slotCnt = nullptr;  // per model: its number of chains
+  const int* slotCnt = nullptr;
   int* queue = nullptr;
   int* ctr = nullptr;
+  // the same for the large-front queues (seeded with the large roots; chains
+  // end at large fronts without large children); strideL = 0: no large fronts
+  int strideL = 0;
+  const int* rootOffL = nullptr;
+  const int* rootsL = nullptr;
+  const int* slotCntL = nullptr;
+  int* queueL = nullptr;
+  int* ctrL = nullptr;
 };
 void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, const BackwardSeed& seed,
                      cudaStream_t s);
@@ -84,7 +95,33 @@ struct PersistentPlan {
   // polls of a bounded wait in the back substitution before it gives up and
   // sets errFlag (about 1-2 s at the default)
   long long spinLimit = 1LL << 23;
+  // large fronts (more than kLargeFrontRows rows, and all their ancestors),
+  // one thread block each (front_large.cu): the number of large children of
+  // every front (d.fNlarge, global), the cascade's start tasks (large fronts
+  // without large children, longest root path first), the largest large front,
+  // their counters (factor, then one set per refinement forward elimination,
+  // nfrontTot + 1 apart) and backward queues (largeStride slots per solve, 4
+  // counters per solve)
+  const unsigned char* fLarge = nullptr;
+  const int* fNlarge = nullptr;
+  const int* largeTasks = nullptr;
+  int nLargeTasks = 0;
+  int maxRowLarge = 0;
+  int *cntLargeFactor = nullptr, *cntLargeForward = nullptr;
+  int *bwLQueue = nullptr, *bwLCtr = nullptr;
+  int largeStride = 0;
 };
+// fronts with more rows than this are factored and solved by a thread block
+// each (front_large.cu); smaller ones by one warp each in shared memory
+constexpr int kLargeFrontRows = 96;
+// the large-front kernels: factorisation (tangent models) fused with the first
+// forward elimination, a further forward elimination (refinement sweep), and
+// the back substitution of the large fronts (before the warp queue's)
+void launchLargeFactorForward(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
+                              cudaStream_t s);
+void launchLargeForward(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
+                        cudaStream_t s);
+void launchLargeBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
 // values of one front's L block the solve kernels stage in shared memory
 int stagingCapacity(const PersistentPlan& p, size_t elemBytes);
 // factorisation of the models with a tangent update fused with the forward

@@ -372,3 +372,98 @@ def pendulum(length=1.0, n_el=4, theta0=0.1, g=9.81):
     fsi = frame_fsi(triads, beams, [pipe_props(1, 0.05, 0.005)], joints=[j], gravity=(0.0, -g, 0.0),
                     title="pendulum")
     return fsi, 2 + n_el
+
+
+def space_frame_c2(seed=2, storeys=12, bays=4, h=3.0, bay=3.0, n_joints=40, n_springs=40, load=10.0e3,
+                   freq=2.0, steps=2000, dt=1.0e-3):
+    """Space-frame tower: `storeys` x (`bays` x `bays`) lattice of steel pipes
+    (3 m storeys and bays), base clamped.  Members: columns, floor beams in X
+    and Y, one floor diagonal per bay and one diagonal brace per panel of the
+    four outer faces (1,164 beams at the default size).  Pipe OD uniform in
+    [0.05, 0.2] m per member, wall OD/10.  `n_joints` revolute joints at
+    random floor nodes release one X floor beam's end rotation about global Y
+    (a pinned beam end: the beam attaches to a dependent triad at the node).
+    `n_springs` axial spring + damper pairs between random node pairs
+    (k uniform in [1e5, 1e7] N/m, c = 1e-3 k, stress-free at the start).
+    Lateral top load: `load` N in X spread over the top floor's nodes,
+    sinusoidal at `freq` Hz.  Returns (fsi, options)."""
+    rng = np.random.default_rng(seed)
+    n = bays + 1
+
+    def nid(i, j, k):
+        return 1 + i + n * (j + n * k)
+
+    triads = []
+    for k in range(storeys + 1):
+        for j in range(n):
+            for i in range(n):
+                triads.append({"id": nid(i, j, k), "pos": (i * bay, j * bay, k * h),
+                               "bc": [0] * 6 if k == 0 else None})
+    members = []
+    for k in range(storeys):
+        for j in range(n):
+            for i in range(n):
+                members.append((nid(i, j, k), nid(i, j, k + 1)))
+    for k in range(1, storeys + 1):
+        for j in range(n):
+            for i in range(bays):
+                members.append((nid(i, j, k), nid(i + 1, j, k)))
+        for j in range(bays):
+            for i in range(n):
+                members.append((nid(i, j, k), nid(i, j + 1, k)))
+        for j in range(bays):
+            for i in range(bays):
+                members.append((nid(i, j, k), nid(i + 1, j + 1, k)))
+    for k in range(storeys):  # outer faces: one diagonal per panel
+        for i in range(bays):
+            members.append((nid(i, 0, k), nid(i + 1, 0, k + 1)))
+            members.append((nid(i, bays, k), nid(i + 1, bays, k + 1)))
+        for j in range(bays):
+            members.append((nid(0, j, k), nid(0, j + 1, k + 1)))
+            members.append((nid(bays, j, k), nid(bays, j + 1, k + 1)))
+    ods = rng.uniform(0.05, 0.2, size=len(members))
+    props = [pipe_props(1 + e, ods[e], ods[e] / 10.0) for e in range(len(members))]
+    # revolute joints: the far end of an X floor beam gets its own (dependent) triad
+    xbeams = [e for e, (a, b) in enumerate(members)
+              if triads[a - 1]["pos"][2] == triads[b - 1]["pos"][2] and triads[b - 1]["pos"][0] > triads[a - 1]["pos"][0]
+              and triads[b - 1]["pos"][1] == triads[a - 1]["pos"][1]]
+    picks = rng.permutation(xbeams)
+    joints, used = [], set()
+    next_id = nid(bays, bays, storeys) + 1
+    rot = np.array([[0.0, 1.0, 0.0], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0]])  # joint Z = global Y
+    for e in picks:
+        if len(joints) == n_joints:
+            break
+        a, b = members[e]
+        if b in used:
+            continue
+        used.add(b)
+        slave = next_id
+        next_id += 1
+        triads.append({"id": slave, "pos": triads[b - 1]["pos"]})
+        members[e] = (a, slave)
+        joints.append({"id": 700000 + len(joints), "type": 1, "slave": slave, "master": b,
+                       "pos": triads[b - 1]["pos"], "rot": rot, "dofs": [(6, 1)]})
+    free = [t["id"] for t in triads if t.get("bc") is None and t["id"] <= nid(bays, bays, storeys)]
+    springs, dampers = [], []
+    for _ in range(n_springs):
+        a, b = rng.choice(free, size=2, replace=False)
+        pa, pb = np.array(triads[a - 1]["pos"]), np.array(triads[b - 1]["pos"])
+        kk = rng.uniform(1.0e5, 1.0e7)
+        springs.append((int(a), int(b), kk, float(np.linalg.norm(pb - pa))))
+        dampers.append((int(a), int(b), 1.0e-3 * kk))
+    beams = [(100000 + e, a, b, 1 + e) for e, (a, b) in enumerate(members)]
+    top = [nid(i, j, storeys) for j in range(n) for i in range(n)]
+    fsi = frame_fsi(triads, beams, props, joints=joints, springs=springs, dampers=dampers,
+                    title=f"space frame {storeys}x{bays}x{bays}")
+    # sinusoidal lateral top load (engine of a SINUSOIDAL function of the TIME sensor)
+    eng = 990000
+    fsi += (f"&FUNCTION\n  id = {eng + 1}\n  type = 'SINUSOIDAL'\n  realDataSize = 4\n"
+            f"  realData = {_f(freq)} 0.0 1.0 0.0\n/\n"
+            f"&SENSOR\n  id = {eng + 2}\n  type = 'TIME'\n/\n"
+            f"&ENGINE\n  id = {eng}\n  functionId = {eng + 1}\n  nArg = 1\n  argSensorId = {eng + 2}\n/\n")
+    for k, t in enumerate(top):
+        fsi += (f"&LOAD\n  id = {980000 + k}\n  triadId = {t}\n  lDof = 1\n  f0 = 0.0\n"
+                f"  f1 = {_f(load / len(top))}\n  loadEngineId = {eng}\n/\n")
+    opts = ["-timeInc=%r" % dt, "-timeEnd=%r" % (steps * dt), "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
+    return fsi, opts

@@ -1059,6 +1059,11 @@ static double engineValue(const OracleModel& m, int e) {
   std::string t = lower(f.type);
   if (t == "scale") return (f.real.empty() ? 1.0 : f.real[0]) * x;
   if (t == "constant") return f.real.empty() ? 0.0 : f.real[0];
+  if (t == "sinusoidal") {  // realData: frequency, delay (periods), amplitude, mean
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    for (size_t k = 0; k < 4 && k < f.real.size(); ++k) p[k] = f.real[k];
+    return p[3] + p[2] * std::sin(2.0 * M_PI * (p[0] * x - p[1]));
+  }
   return x;
 }
 
@@ -1644,7 +1649,7 @@ static int setup(OracleModel& m, const char* fsi) {
     if (fid > 0 && en.func < 0) return -18;
     if (en.func >= 0) {
       std::string t = lower(m.funcs[en.func].type);
-      if (t != "scale" && t != "constant") return -19;  // other function types are not in this subset
+      if (t != "scale" && t != "constant" && t != "sinusoidal") return -19;  // other function types are not in this subset
     }
     m.engines.push_back(en);
   }

@@ -1,0 +1,57 @@
+"""The space-frame tower (12 storeys x 4 x 4 bays, 1,164 pipes, 40 revolute
+joints, 40 spring/damper pairs, sinusoidal top load): its assembly tree has
+fronts of several hundred rows, factored and solved one thread block per
+front (front_large.cu) above the warp-per-front subtrees.  Checked against the
+oracle over 100 steps (FP64 within 1e-10, mixed within 1e-8 of the largest
+displacement over the run, FP64 iteration counts equal) and in a batch with
+beam chains (bitwise the same as alone)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1.0e-10
+MIXED_TOL = 1.0e-8
+
+
+def _c2(steps=100):
+    from fedem_gb300 import models
+
+    return models.space_frame_c2(steps=steps)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_space_frame_matches_oracle(gpu, oracle_lib, mixed):
+    from fedem_gb300.batch import Batch, Model
+    from oracle.oracle import OracleModel
+
+    fsi, opts = _c2()
+    m = Model(fsi, opts)
+    assert m.max_front > 96  # large fronts present
+    o = OracleModel(fsi, opts)
+    o.run_all()
+    ref, scale = o.triads(), o.max_displacement()
+    b = Batch([m], mixed=mixed)
+    st = b.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0, b.info(0)
+    err = np.abs(b.triads(0)[:, :, 3] - ref[:, :, 3]).max() / scale
+    assert err <= (MIXED_TOL if mixed else FP64_TOL), err
+    if not mixed:
+        assert b.info(0)["iterations"] == o.iterations()
+    b.close()
+    o.close()
+
+
+def test_space_frame_same_alone_and_with_chains(gpu):
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model
+
+    cases = [_c2(40)] + [(f, o) for f, o, _ in models.batch_c4(4, seed=41, n_max=500, steps=40)]
+    mix = Batch([Model(f, o) for f, o in cases], mixed=True)
+    mix.run()
+    for k, (f, o) in enumerate(cases):
+        alone = Batch([Model(f, o)], mixed=True)
+        alone.run()
+        np.testing.assert_array_equal(mix.triads(k), alone.triads(0))
+        alone.close()
+    mix.close()
