@@ -1,38 +1,47 @@
 // front_large.cu -- multifrontal factorisation and solves of the large fronts
-// (more rows than one warp's shared-memory front holds), one thread block per
-// front.
+// (more rows than one warp's shared-memory front holds).
 //
 // Large fronts are marked upward-closed on the host (every ancestor of a large
 // front is large), so the warp kernels of front_cascade.cu finish every small
 // subtree first and these kernels take the tops of the assembly trees:
-//   factor + forward: a cascade over the large fronts (blocks start at large
-//     fronts whose children are all small, a parent's counter completes on its
-//     last large child, the completing block climbs to it; nothing waits);
-//   forward (refinement sweeps): the same cascade without the factorisation;
+//   factor + forward: a cascade over the large fronts (clusters of blocks start
+//     at large fronts whose children are all small, a parent's counter
+//     completes on its last large child, the completing cluster climbs to it;
+//     nothing waits on another cluster);
+//   forward (refinement sweeps): the same cascade without the factorisation,
+//     one block per front;
 //   backward: a top-down work queue of large fronts seeded with the large roots
 //     (a block waits only for a slot that a running block fills), before the
 //     warp queue takes the small fronts below them.
 // A large front is factored in place in its outputs: its pivot columns in its
 // L block (nrow x npiv, column-major) and its trailing lower triangle in its
 // packed update matrix (column by column, inside the parent's segment), so no
-// workspace is needed.  Blocked right-looking LDL^T, panels of kPanel pivots:
-// the panel is factored column by column (the unscaled column in shared
-// memory), then the trailing lower triangle is updated with the panel,
-// C -= L_p D_p L_p^T.  Semantics as the warp kernels and the reference's
+// workspace is needed.  Blocked right-looking LDL^T in panels of up to 32
+// pivots: each panel is factored in shared memory (its diagonal block by one
+// warp, the rows below it one per thread, no barrier inside), then the
+// trailing lower triangle is updated with it, C -= L_p D_p L_p^T, in 64 x 64
+// tiles with 4 x 4 register blocks, the tiles shared out over the blocks of a
+// thread-block cluster (GB300's FP64 units are thin: one front's update on one
+// SM would set the pace).  Semantics as the warp kernels and the reference's
 // SPRFC1/SPRFS1/SPRBS1 seam (solExtensionModule.f90:153-505): no pivoting, a
 // pivot is singular when |d_k| <= tolFactorize |a_kk|, negative pivots counted,
 // children's update matrices added in child order (fixed summation order).
-// Data other blocks wrote (children's updates, solution values) are read
-// through L2 (__ldcg), and a block's own front data too, since its threads
-// read back what others of the block wrote.
+// Front data written by other threads or blocks are read through L2 (__ldcg).
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
 
 #include "kernels.h"
 
 namespace fgpu {
 namespace {
 
-constexpr int kLT = 256;    // threads per large-front block
-constexpr int kPanel = 32;  // pivots per panel
+namespace cg = cooperative_groups;
+
+constexpr int kLT = 256;         // threads per large-front block
+constexpr int kClusterCtas = 8;  // blocks of a cluster that factor one large front together
+constexpr int kTile = 64;        // trailing-update tile (rows and columns)
 
 // lower-triangle entry (ii >= jj) of an nu x nu matrix packed column by column
 __device__ inline int64_t packedAt(int ii, int jj, int nu) {
@@ -61,26 +70,39 @@ __device__ inline void st(T* p, T v) {
   __stcg(p, v);
 }
 
-// assembly (original entries, then the children's update matrices in child
-// order) and the blocked partial LDL^T of large front f; shared: ucol (nr),
-// diag0 (np), dpan (kPanel)
+// a barrier of all threads of the cluster, their global writes visible to
+// every thread of the cluster afterwards (each thread fences first)
+__device__ inline void clusterBarrier() {
+  __threadfence();
+  cg::this_cluster().sync();
+}
+
+// Assembly (original entries, then the children's update matrices in child
+// order) and the blocked partial LDL^T of large front f by the blocks of a
+// cluster (crank of csize): the assembly is split over all their threads,
+// every block factors each panel itself (the same arithmetic, so the same
+// values) and takes its share of the trailing tiles; block 0 writes the panel
+// back and reports the pivots.  Shared memory: the panel P (kb <= 32 columns of
+// ldp rows, column-major: the panel's rows k0 .. nr-1), diag0 (np), dpan (kb).
 template <typename T>
-__device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, T* Ubase, double tolFact, T* ucol,
-                            T* diag0, T* dpan) {
+__device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, T* Ubase, double tolFact, T* P,
+                            int ldp, int kbMax, T* diag0, T* dpan, int crank, int csize) {
   const int tid = threadIdx.x;
+  const int gtid = crank * kLT + tid, gstride = csize * kLT;
   Front<T> F{Lbase + d.fLOff[f], Ubase + d.fUOff[f], d.fNrow[f], d.fNpiv[f], d.fNrow[f] - d.fNpiv[f]};
   const int nr = F.nr, np = F.np, nu = F.nu;
   const int64_t nL = (int64_t)nr * np, nU = (int64_t)nu * (nu + 1) / 2;
-  for (int64_t k = tid; k < nL; k += kLT) st(F.L + k, T(0));
-  for (int64_t k = tid; k < nU; k += kLT) st(F.U + k, T(0));
-  __syncthreads();
+  clusterBarrier();
+  for (int64_t k = gtid; k < nL; k += gstride) st(F.L + k, T(0));
+  for (int64_t k = gtid; k < nU; k += gstride) st(F.U + k, T(0));
+  clusterBarrier();
   const int64_t ao = d.fAsmOff[f];
   const int na = d.fNasm[f];
-  for (int k = tid; k < na; k += kLT) {  // original entries: pivot columns only, distinct positions
+  for (int k = gtid; k < na; k += gstride) {  // original entries: pivot columns only, distinct positions
     const int p = __ldg(d.asmPos + ao + k);
     st(F.L + p, __ldg(asmVal + ao + k));
   }
-  __syncthreads();
+  clusterBarrier();
   for (int k = tid; k < np; k += kLT) diag0[k] = ld(F.L + k + (int64_t)nr * k);
   // extend-add, child by child (positions are distinct within one child)
   const T* seg = Ubase + d.fSegOff[f];
@@ -92,73 +114,137 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
     const int ch = d.childList[co + c];
     const int cu = d.fNrow[ch] - d.fNpiv[ch];
     const int64_t len = (int64_t)cu * (cu + 1) / 2;
-    __syncthreads();
-    for (int64_t k = tid; k < len; k += kLT) {
+    if (c > 0) clusterBarrier();
+    for (int64_t k = gtid; k < len; k += gstride) {
       const int p = __ldg(spos + off + k) & 0xfffff;
       T* q = F.at(p % nr, p / nr);
       st(q, ld(q) + ld(seg + off + k));
     }
     off += len;
   }
-  __syncthreads();
   int neg = 0;
   bool sing = false;
-  for (int k0 = 0; k0 < np; k0 += kPanel) {
-    const int kb = min(kPanel, np - k0);
-    // panel: pivots k0 .. k0 + kb - 1, right-looking inside the panel
-    for (int k = k0; k < k0 + kb; ++k) {
-      const T dk = ld(F.L + k + (int64_t)nr * k);
-      for (int i = k + 1 + tid; i < nr; i += kLT) ucol[i] = ld(F.L + i + (int64_t)nr * k);
-      if (tid == 0) {
-        const bool bad = singularPivot(dk, diag0[k], tolFact);
-        sing |= bad;
-        if (dk < T(0)) ++neg;
-        dpan[k - k0] = dk;
-      }
-      __syncthreads();
-      const bool bad = singularPivot(dk, diag0[k], tolFact);
-      const T inv = bad ? T(0) : T(1) / dk;
-      const int je = k0 + kb - 1;
-      for (int i = k + 1 + tid; i < nr; i += kLT) {
-        const T l = ucol[i] * inv;
-        st(F.L + i + (int64_t)nr * k, l);
-        const int jm = i < je ? i : je;
-        for (int j = k + 1; j <= jm; ++j) {
-          T* q = F.L + i + (int64_t)nr * j;
-          st(q, ld(q) - l * ucol[j]);
-        }
-      }
-      __syncthreads();
-    }
-    // trailing lower triangle: columns j >= j0, C(i, j) -= sum_k L(i, k) d_k L(j, k)
-    const int j0 = k0 + kb, nt = nr - j0;
-    int b = 0, t = tid;
-    while (b < nt && t >= nt - b) { t -= nt - b; ++b; }
-    while (b < nt) {
-      const int j = j0 + b, i = j + t;
-      T acc = T(0);
+  for (int k0 = 0; k0 < np; k0 += kbMax) {
+    clusterBarrier();  // the panel's columns complete (assembly, earlier trailing updates)
+    const int kb = min(kbMax, np - k0), pr = nr - k0;  // panel columns and rows
+    for (int kk = 0; kk < kb; ++kk)
+      for (int r = tid; r < pr; r += kLT) P[kk * ldp + r] = ld(F.L + (k0 + r) + (int64_t)nr * (k0 + kk));
+    __syncthreads();
+    // the panel's kb x kb diagonal block, right-looking, by warp 0 alone: lane
+    // r owns row r; the unscaled value of each scaled entry (row r, column k) is
+    // kept in the unused upper triangle (row k, column r)
+    if (tid < 32) {
+      const int r = tid;
       for (int kk = 0; kk < kb; ++kk) {
-        const int k = k0 + kk;
-        acc += ld(F.L + i + (int64_t)nr * k) * (ld(F.L + j + (int64_t)nr * k) * dpan[kk]);
+        const T dk = P[kk * ldp + kk];
+        const bool bad = singularPivot(dk, diag0[k0 + kk], tolFact);
+        if (r == 0) {
+          sing |= bad;
+          if (dk < T(0)) ++neg;
+          dpan[kk] = dk;
+        }
+        const T inv = bad ? T(0) : T(1) / dk;
+        T l = T(0);
+        if (r > kk && r < kb) {
+          const T u = P[kk * ldp + r];
+          P[r * ldp + kk] = u;
+          l = u * inv;
+          P[kk * ldp + r] = l;
+        }
+        __syncwarp();
+        if (r > kk && r < kb)
+          for (int j = kk + 1; j <= r; ++j) P[j * ldp + r] -= l * P[j * ldp + kk];
+        __syncwarp();
       }
-      T* q = F.at(i, j);
-      st(q, ld(q) - acc);
-      t += kLT;
-      while (b < nt && t >= nt - b) { t -= nt - b; ++b; }
     }
     __syncthreads();
+    // the panel's rows below the block, each on its own: for k in order,
+    // a = P(r, k) - sum_{j < k} l_rj u_kj, l_rk = a / d_k (the right-looking
+    // updates of the row, in the same order)
+    for (int r = kb + tid; r < pr; r += kLT) {
+      T lr[32];
+#pragma unroll
+      for (int kk = 0; kk < 32; ++kk) {
+        if (kk >= kb) break;
+        T a = P[kk * ldp + r];
+#pragma unroll
+        for (int j = 0; j < kk; ++j) a -= lr[j] * P[kk * ldp + j];
+        const bool bad = singularPivot(dpan[kk], diag0[k0 + kk], tolFact);
+        lr[kk] = a * (bad ? T(0) : T(1) / dpan[kk]);
+      }
+#pragma unroll
+      for (int kk = 0; kk < 32; ++kk) {
+        if (kk >= kb) break;
+        P[kk * ldp + r] = lr[kk];
+      }
+    }
+    __syncthreads();
+    if (crank == 0)
+      for (int kk = 0; kk < kb; ++kk)
+        for (int r = kk + tid; r < pr; r += kLT) st(F.L + (k0 + r) + (int64_t)nr * (k0 + kk), P[kk * ldp + r]);
+    // trailing lower triangle, rows and columns k0 + kb .. nr-1 (panel-local
+    // kb .. pr-1): C(i, j) -= sum_k P(i, k) d_k P(j, k), tile by tile; a
+    // thread's 4 x 4 block is rows lr + 16 a and columns lc + 16 b of the tile
+    const int nt = pr - kb;
+    const int ntiles = (nt + kTile - 1) / kTile;
+    const int lr = tid & 15, lc = tid >> 4;
+    int tcount = 0;
+    for (int tj = 0; tj < ntiles; ++tj)
+      for (int ti = tj; ti < ntiles; ++ti) {
+        if (tcount++ % csize != crank) continue;  // this block's share of the tiles
+        const int r0 = kb + ti * kTile, c0 = kb + tj * kTile;
+        T acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+        for (int kk = 0; kk < kb; ++kk) {
+          const T* Pk = P + kk * ldp;
+          const T dk = dpan[kk];
+          T av[4], bv[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int r = r0 + lr + 16 * a;
+            av[a] = r < pr ? Pk[r] : T(0);
+          }
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int c = c0 + lc + 16 * b;
+            bv[b] = c < pr ? Pk[c] * dk : T(0);
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int c = c0 + lc + 16 * b;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int r = r0 + lr + 16 * a;
+            if (r < pr && c < pr && r >= c) {
+              T* q = F.at(k0 + r, k0 + c);
+              st(q, ld(q) - acc[a][b]);
+            }
+          }
+        }
+      }
   }
-  if (tid == 0) {
+  if (tid == 0 && crank == 0) {
     const int m = d.fModel[f];
     if (neg) atomicAdd(&d.m.negPiv[m], neg);
     if (sing) atomicOr(&d.m.status[m], SS_SINGULAR);
   }
+  clusterBarrier();  // L block and update matrix complete
 }
 
-// forward elimination of large front f (v: nr values in shared memory)
+// forward elimination of large front f (v: nr values in shared memory), in
+// blocks of 32 pivots: warp 0 eliminates the block's unit lower triangle with
+// shuffles, then every thread updates its rows below the block with it
 template <typename T>
 __device__ void forwardLarge(const DevData& d, int f, const T* Lbase, const double* rhs, T* X, T* W, T* v) {
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
   const T* L = Lbase + d.fLOff[f];
   const int* rows = d.frontRows + d.fRowOff[f];
@@ -175,10 +261,22 @@ __device__ void forwardLarge(const DevData& d, int f, const T* Lbase, const doub
     for (int a = tid; a < cu; a += kLT) v[__ldg(rel + a)] += ld(wc + a);
   }
   __syncthreads();
-  for (int k = 0; k < np; ++k) {
-    const T yk = v[k];
+  for (int b0 = 0; b0 < np; b0 += 32) {
+    const int bs = min(32, np - b0);
+    if (tid < 32) {  // the block's triangle: lane r holds v[b0 + r]
+      T x = lane < bs ? v[b0 + lane] : T(0);
+      for (int k = 0; k < bs - 1; ++k) {
+        const T yk = __shfl_sync(0xffffffffu, x, k);
+        if (lane > k && lane < bs) x -= ld(L + (b0 + lane) + (int64_t)nr * (b0 + k)) * yk;
+      }
+      if (lane < bs) v[b0 + lane] = x;
+    }
     __syncthreads();
-    for (int i = k + 1 + tid; i < nr; i += kLT) v[i] -= ld(L + i + (int64_t)nr * k) * yk;
+    for (int i = b0 + bs + tid; i < nr; i += kLT) {
+      T s = v[i];
+      for (int k = 0; k < bs; ++k) s -= ld(L + i + (int64_t)nr * (b0 + k)) * v[b0 + k];
+      v[i] = s;
+    }
     __syncthreads();
   }
   for (int r = tid; r < np; r += kLT) X[__ldg(rows + r)] = v[r] / ld(L + r + (int64_t)nr * r);
@@ -208,27 +306,36 @@ __device__ inline int climbLarge(const DevData& d, const PersistentPlan& p, int 
 template <typename T>
 __global__ void __launch_bounds__(kLT) kLargeFactorForward(DevData d, PersistentPlan p, const T* asmVal, T* Lbase,
                                                             T* Ubase, double tolFact, const double* rhs, T* X, T* W,
-                                                            int* cnt, int doFactor) {
+                                                            int* cnt, int doFactor, int panel) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  const int ldp = (p.maxRowLarge + 3) & ~3;
   T* v = reinterpret_cast<T*>(smraw);
-  T* ucol = v + p.maxRowLarge;
-  T* diag0 = ucol + p.maxRowLarge;
-  T* dpan = diag0 + p.maxRowLarge;
+  T* diag0 = v + ldp;
+  T* dpan = diag0 + ldp;
+  T* P = dpan + 32;
   __shared__ int shIdx, shNext;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank(), csize = (int)cluster.num_blocks();
   int* const next = cnt + d.nfrontTot;
   for (;;) {
-    if (threadIdx.x == 0) shIdx = atomicAdd(next, 1);
-    __syncthreads();
-    const int idx = shIdx;
-    __syncthreads();
+    // block 0 of the cluster takes the task; every block reads it from there
+    if (crank == 0 && threadIdx.x == 0) shIdx = atomicAdd(next, 1);
+    cluster.sync();
+    const int idx = *cluster.map_shared_rank(&shIdx, 0);
+    cluster.sync();
     if (idx >= p.nLargeTasks) break;
     int f = p.largeTasks[idx];
     const int fl = d.m.flags[d.fModel[f]];
     const bool factor = doFactor && (fl & FL_TANGENT);
     while ((fl & FL_ACTIVE) && f >= 0) {
-      if (factor) factorLarge<T>(d, f, asmVal, Lbase, Ubase, tolFact, ucol, diag0, dpan);
-      forwardLarge<T>(d, f, Lbase, rhs, X, W, v);
-      f = climbLarge(d, p, f, cnt, &shNext);
+      if (factor) factorLarge<T>(d, f, asmVal, Lbase, Ubase, tolFact, P, ldp, panel, diag0, dpan, crank, csize);
+      if (crank == 0) {
+        forwardLarge<T>(d, f, Lbase, rhs, X, W, v);
+        f = climbLarge(d, p, f, cnt, &shNext);
+      }
+      cluster.sync();
+      f = *cluster.map_shared_rank(&shNext, 0);
+      cluster.sync();
     }
   }
 }
@@ -245,6 +352,7 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
   T* xs = reinterpret_cast<T*>(smraw);
   __shared__ int shSlot, shF, shOk;
   const int tid = threadIdx.x;
+  const int w = tid >> 5, lane = tid & 31;
   const int total = *(volatile const int*)(ctr + 2);
   for (;;) {
     if (tid == 0) shSlot = atomicAdd(ctr, 1);
@@ -276,16 +384,36 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
       const int* rows = d.frontRows + d.fRowOff[f];
       for (int r = tid; r < nr; r += kLT) xs[r] = ld(X + __ldg(rows + r));
       __syncthreads();
-      // the update rows' contribution for every pivot, then the unit triangle
-      for (int k = tid; k < np; k += kLT) {
-        T a = xs[k];
-        for (int i = np; i < nr; ++i) a -= ld(L + i + (int64_t)nr * k) * xs[i];
-        xs[k] = a;
+      // the update rows' contribution for every pivot: one warp per pivot, the
+      // lanes over the rows in a fixed pattern, a fixed shuffle tree
+      for (int k = w; k < np; k += kLT / 32) {
+        T a = T(0);
+        for (int i = np + lane; i < nr; i += 32) a += ld(L + i + (int64_t)nr * k) * xs[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) xs[k] -= a;
       }
       __syncthreads();
-      for (int j = np - 1; j > 0; --j) {
-        const T xj = xs[j];
-        for (int k = tid; k < j; k += kLT) xs[k] -= ld(L + j + (int64_t)nr * k) * xj;
+      // the unit upper triangle L11^T, blocks of 32 pivots from the last: warp
+      // 0 solves the block with shuffles, then the pivots above it are updated
+      // with the block's values (one warp per pivot)
+      for (int bEnd = np; bEnd > 0; bEnd -= 32) {
+        const int b0 = bEnd > 32 ? bEnd - 32 : 0, bs = bEnd - b0;
+        if (tid < 32) {
+          T x = lane < bs ? xs[b0 + lane] : T(0);
+          for (int j = bs - 1; j > 0; --j) {
+            const T xj = __shfl_sync(0xffffffffu, x, j);
+            if (lane < j) x -= ld(L + (b0 + j) + (int64_t)nr * (b0 + lane)) * xj;
+          }
+          if (lane < bs) xs[b0 + lane] = x;
+        }
+        __syncthreads();
+        for (int k = w; k < b0; k += kLT / 32) {
+          T a = lane < bs ? ld(L + (b0 + lane) + (int64_t)nr * k) * xs[b0 + lane] : T(0);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+          if (lane == 0) xs[k] -= a;
+        }
         __syncthreads();
       }
       for (int r = tid; r < np; r += kLT) {
@@ -305,9 +433,8 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
       // large children: the first continues here, the others go to fresh slots
       const int nch = d.fNchild[f];
       const int* chl = d.childList + d.fChildOff[f];
-      int first = -1;
       if (tid == 0) {
-        int nl = 0;
+        int first = -1, nl = 0;
         for (int c = 0; c < nch; ++c)
           if (p.fLarge[chl[c]]) {
             if (first < 0) first = chl[c];
@@ -355,13 +482,49 @@ void bigSmem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// panel width: 32 pivots, fewer when the panel of the largest front would not
+// fit the shared memory (about 200 KB)
+template <typename T>
+int panelWidth(int maxRow) {
+  const size_t ldp = (size_t)((maxRow + 3) & ~3);
+  int kb = 32;
+  while (kb > 4 && (2 * ldp + 32 + (size_t)kb * ldp) * sizeof(T) > 200 * 1024) kb -= 4;
+  return kb;
+}
+
+// Factorisations run as clusters of kClusterCtas blocks per front (a grid of
+// as many clusters as fit at once, at most one per start task); forward
+// eliminations alone as single blocks.
 template <typename T>
 void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmVal, T* L, T* U, const double* rhs,
                         T* X, T* W, int* cnt, bool factor, cudaStream_t s) {
-  const size_t sm = (3 * (size_t)p.maxRowLarge + kPanel) * sizeof(T);
+  const size_t ldp = (size_t)((p.maxRowLarge + 3) & ~3);
+  const int kb = panelWidth<T>(p.maxRowLarge);
+  const size_t sm = (2 * ldp + 32 + (factor ? (size_t)kb * ldp : 0)) * sizeof(T);
   bigSmem(kLargeFactorForward<T>, sm);
-  const int grid = gridFor(kLargeFactorForward<T>, sm, p.nLargeTasks);
-  kLargeFactorForward<T><<<grid, kLT, sm, s>>>(d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, factor ? 1 : 0);
+  if (!factor) {
+    const int grid = gridFor(kLargeFactorForward<T>, sm, p.nLargeTasks);
+    kLargeFactorForward<T><<<grid, kLT, sm, s>>>(d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, 0, kb);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kLT);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(kClusterCtas * p.nLargeTasks);
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, kLargeFactorForward<T>, &cfg) != cudaSuccess || clusters < 1)
+    clusters = 1;
+  clusters = std::min(clusters, p.nLargeTasks);
+  cfg.gridDim = dim3(kClusterCtas * clusters);
+  cudaLaunchKernelEx(&cfg, kLargeFactorForward<T>, d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, 1, kb);
 }
 
 }  // namespace

@@ -383,8 +383,9 @@ def space_frame_c2(seed=2, storeys=12, bays=4, h=3.0, bay=3.0, n_joints=40, n_sp
     [0.05, 0.2] m per member, wall OD/10.  `n_joints` revolute joints at
     random floor nodes release one X floor beam's end rotation about global Y
     (a pinned beam end: the beam attaches to a dependent triad at the node).
-    `n_springs` axial spring + damper pairs between random node pairs
-    (k uniform in [1e5, 1e7] N/m, c = 1e-3 k, stress-free at the start).
+    `n_springs` axial spring + damper pairs, each between a random node and
+    another random node at most one storey away (k uniform in [1e5, 1e7] N/m,
+    c = 1e-3 k, stress-free at the start).
     Lateral top load: `load` N in X spread over the top floor's nodes,
     sinusoidal at `freq` Hz.  Returns (fsi, options)."""
     rng = np.random.default_rng(seed)
@@ -447,7 +448,11 @@ def space_frame_c2(seed=2, storeys=12, bays=4, h=3.0, bay=3.0, n_joints=40, n_sp
     free = [t["id"] for t in triads if t.get("bc") is None and t["id"] <= nid(bays, bays, storeys)]
     springs, dampers = [], []
     for _ in range(n_springs):
-        a, b = rng.choice(free, size=2, replace=False)
+        # a random node tied to another random node at most one storey away
+        a = int(rng.choice(free))
+        za = triads[a - 1]["pos"][2]
+        near = [t for t in free if t != a and abs(triads[t - 1]["pos"][2] - za) <= h + 1e-9]
+        b = int(rng.choice(near))
         pa, pb = np.array(triads[a - 1]["pos"]), np.array(triads[b - 1]["pos"])
         kk = rng.uniform(1.0e5, 1.0e7)
         springs.append((int(a), int(b), kk, float(np.linalg.norm(pb - pa))))
