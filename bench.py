@@ -87,6 +87,10 @@ def parse():
     ap.add_argument("--fp64", action="store_true", help="time the batched plain FP64 path instead of mixed")
     ap.add_argument("--error-only", action="store_true", help="of the extras, run only the mixed-vs-FP64 check")
     ap.add_argument("--no-oracle", action="store_true", help="skip the full CPU oracle run (parity + cpu_baseline)")
+    ap.add_argument("--space-frame-steps", type=int, default=2000, help="time steps of the space-frame tower leg")
+    ap.add_argument("--no-space-frame", action="store_true", help="skip the space-frame tower leg")
+    ap.add_argument("--space-frame-only", action="store_true",
+                    help="run only the space-frame tower leg (GPU) and print its JSON")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
@@ -289,6 +293,124 @@ def served_leg(args):
                     f"{args.serve_steps_scale}"}
 
 
+def factor_flops(model):
+    """Factorisation flops of one model's fronts, sum over the columns j of L
+    of c_j (c_j + 3), c_j the off-diagonal entries of column j (a front of nr
+    rows and np pivots has c = nr - 1 - k at its pivot k)."""
+    import numpy as np
+
+    _, info = model.symbolic()
+    tot = 0
+    for npiv, nrow in info[:, :2].astype(np.int64):
+        c = nrow - 1 - np.arange(npiv)
+        tot += int((c * (c + 3)).sum())
+    return tot
+
+
+def space_frame_oracle(steps):
+    """The oracle over the space-frame tower, single-threaded, set-up included.
+    Runs in a spawned process beside the GPU legs.  Returns (seconds, Newton
+    iterations, final triad matrices, largest displacement over the run)."""
+    from fedem_gb300 import models
+    from oracle.oracle import OracleModel
+
+    fsi, opts = models.space_frame_c2(steps=steps)
+    t0 = time.perf_counter()
+    o = OracleModel(fsi, opts)
+    o.run_all()
+    dt = time.perf_counter() - t0
+    out = dt, o.iterations(), o.triads().copy(), o.max_displacement()
+    o.close()
+    return out
+
+
+def start_frame_oracle(args):
+    """(pool, pending result) of the space-frame oracle run in a spawned
+    process (a fresh interpreter: safe beside this process's CUDA context), or
+    (None, None) with --no-oracle."""
+    if args.no_oracle:
+        return None, None
+    import multiprocessing
+
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    pool = multiprocessing.get_context("spawn").Pool(1)
+    return pool, pool.apply_async(space_frame_oracle, (args.space_frame_steps,))
+
+
+def space_frame_leg(args, pending=None):
+    """The space-frame tower (12 storeys x 4 x 4 bays, 1,164 pipes, 40 revolute
+    joints, 40 spring/damper pairs, 10 kN at 2 Hz on the top floor) through
+    args.space_frame_steps time steps, one model per batch: plain FP64 and
+    mixed precision, device time of a full run after a warm-up run, phase
+    timings, the factorisation against the measured FP64 FMA rate, and, when
+    `pending` (the oracle's run in a spawned process) is given, both final
+    states against the oracle's and the oracle's time as the CPU baseline."""
+    import numpy as np
+
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Batch, Model, measure_fp64_peak
+
+    fsi, opts = models.space_frame_c2(steps=args.space_frame_steps)
+    m = Model(fsi, opts)
+    flops = factor_flops(m)
+    peak_tf, _ = measure_fp64_peak()
+    out = {"workload": f"space-frame tower, 12 storeys x 4 x 4 bays, {m.nel} beams, 40 revolute joints, 40 "
+                       f"spring/damper pairs, sinusoidal 10 kN top load at 2 Hz, {args.space_frame_steps} "
+                       f"HHT-alpha steps of 1 ms", "equations": m.neq, "unit": UNIT,
+           "factor_flops_per_factorisation": flops, "fp64_fma_peak_tflops": peak_tf,
+           "fp64_peak_source": "measured (fgpu_measure_fp64_peak: 8 FMA chains per thread, 8 blocks per SM)"}
+    finals = {}
+    for mixed in (False, True):
+        b = Batch([m], mixed=mixed)
+        b.snapshot()
+        b.run(max_batched=64)  # warm-up: graph instantiation, first launches
+        b.restore()
+        b.phase_timings(reset=True)
+        st = b.run()
+        n, ms, _ = b.phase_timings()
+        key = "mixed" if mixed else "fp64"
+        finals[key] = b.triads(0).copy()
+        its = b.info(0)["iterations"]
+        if its != st["newton_iterations"]:
+            raise RuntimeError("space-frame run: iteration counts disagree")
+        ph = (ms / max(n, 1)).tolist()
+        leg = {"value": st["newton_iterations"] / (st["device_us"] * 1e-6),
+               "time_steps_per_s": st["time_steps"] / (st["device_us"] * 1e-6),
+               "newton_iterations": its, "batched_iterations": st["batched_iterations"],
+               "kernels_per_batched_iteration": st["kernels_per_iteration"], "failed": st["models_failed"],
+               "ms_per_iteration": st["device_us"] * 1e-3 / max(st["batched_iterations"], 1),
+               "phase_ms_per_iteration": {"elements": ph[0], "factor_and_first_forward": ph[1],
+                                          "other_solve": ph[2], "second_forward": ph[3],
+                                          "first_backward": ph[4]}}
+        # the factorisation fused with the first forward elimination, timed alone
+        # (10 launches, CUDA events on the engine stream) after the run
+        f_ms, _ = b.time_factor(reps=10)
+        leg["factor_ms"] = f_ms
+        if not mixed:
+            achieved = flops / (f_ms * 1e-3) / 1e12
+            leg["roofline_factor"] = {"bound": "fp64", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                                      "frac": achieved / peak_tf, "traffic": None,
+                                      "kernel": "kFactorForwardCascade<double> + kLargeFactorForward<double>",
+                                      "timing": "10 launches after the run, CUDA events on the engine stream"}
+        else:
+            leg["factor_gflops"] = flops / (f_ms * 1e-3) / 1e9
+        out[key] = leg
+        b.close()
+    if pending is not None:
+        c_dt, c_it, c_ur, c_scale = pending.get()
+        out["parity_vs_oracle"] = {
+            "max_rel_disp_err_fp64": float(np.abs(finals["fp64"][:, :, 3] - c_ur[:, :, 3]).max() / c_scale),
+            "max_rel_disp_err_mixed": float(np.abs(finals["mixed"][:, :, 3] - c_ur[:, :, 3]).max() / c_scale),
+            "oracle_iterations": c_it, "fp64_iterations": out["fp64"]["newton_iterations"],
+            "definition": "final triad positions: max |gpu - oracle| / the largest triad displacement over "
+                          "the run (oracle)"}
+        out["cpu_baseline"] = {"value": c_it / c_dt, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"the full run ({args.space_frame_steps} steps, {c_it} Newton iterations, "
+                                         f"{c_dt:.1f} s), set-up included, one thread"}
+    m.close()
+    return out
+
+
 def run_reference(args, dist, rank, world):
     """The reference arm: the CPU oracle (the FP64 restatement of the reference
     algorithm; the reference itself does not build here) on the same workload
@@ -387,8 +509,15 @@ def main():
     from fedem_gb300 import models
     from fedem_gb300.batch import Batch, create_models
 
+    want_frame = not args.no_space_frame and rank == 0 and not args.timed_only
     lib = fedem_gb300.load_library()
     dev, bus = rank_device(local, lib)
+    if args.space_frame_only:
+        pool, pending = start_frame_oracle(args)
+        print(json.dumps({"space_frame": space_frame_leg(args, pending)}), flush=True)
+        if pool is not None:
+            pool.close()
+        return
     print(f"rank {rank}: solver device {dev} ({bus})", file=sys.stderr, flush=True)
     cases_all = models.batch_c4(args.models, seed=4, steps=args.sim_steps)
     mine = shard(cases_all, rank, world)
@@ -539,8 +668,15 @@ def main():
                                           "sample": f"{len(idx)} of {len(mods)} models run one at a time"}
         extras["speedup_vs_plain"] = value / plain_rate
         extras["speedup_vs_plain_time_steps"] = (tsteps_tot / dev_s_max) / (p_ts / p_s)
+        # the space-frame oracle starts here, after the c4 oracle leg (whose
+        # timing it would otherwise share cores with), and runs beside the GPU legs
+        pool, pending = start_frame_oracle(args) if want_frame else (None, None)
         # ---- served: Poisson request stream with continuous batching ----------------------
         extras["served"] = served_leg(args)
+        if want_frame:
+            extras["space_frame"] = space_frame_leg(args, pending)
+            if pool is not None:
+                pool.close()
 
     hbm_peak, peak_kind = measured_peaks()
     roof, roof_el = None, None

@@ -1406,7 +1406,10 @@ int Engine::run(long long maxBatched, RunStats* stats) {
   auto t0 = std::chrono::steady_clock::now();
   cudaEventRecord(evRun_[0], stream_);
   long long done = 0;
-  const int chunk = 8;
+  // an odd chunk length: the phase durations are sampled from the last
+  // iteration of each chunk, and with two iterations per time step an even
+  // length would always sample the same kind (predictor or corrector)
+  const int chunk = 7;
   while (done < maxBatched) {
     int n = (int)std::min<long long>(chunk, maxBatched - done);
     for (int k = 0; k < n; ++k) {

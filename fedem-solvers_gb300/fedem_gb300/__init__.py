@@ -97,6 +97,7 @@ def load_library(path=None):
         "fgpu_get_device": (c_int, [P(c_int), ctypes.c_char_p, c_int]),
         "fgpu_batch_device": (c_int, [vp]),
         "fgpu_batch_probe_wait_timeout": (c_int, [vp, c_ll, P(c_int)]),
+        "fgpu_measure_fp64_peak": (c_int, [P(c_dbl), P(c_dbl)]),
         "fgpu_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -106,6 +106,16 @@ def get_device(lib=None):
     return dev.value, bus.value.decode()
 
 
+def measure_fp64_peak(lib=None):
+    """Measured FP64 FMA rate of the current device: (TFLOP/s, ms of the best
+    launch) from fgpu_measure_fp64_peak."""
+    lib = lib or load_library()
+    tf, ms = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    if lib.fgpu_measure_fp64_peak(ctypes.byref(tf), ctypes.byref(ms)) != 0:
+        raise FedemException("fgpu_measure_fp64_peak failed")
+    return tf.value, ms.value
+
+
 class Batch:
     """Models resident on the GPU, advanced together (mixed or FP64)."""
 

@@ -133,6 +133,14 @@ int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
  * convergence test, as after a real wait that ran out. */
 int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag);
 
+/* Measured FP64 fused multiply-add rate of the library's current device:
+ * eight independent FMA chains per thread, eight 256-thread blocks per SM,
+ * best of five timed launches after three warm-up launches (CUDA events).
+ * *tflops: FP64 TFLOP/s (2 flops per FMA); *ms: the best launch's time.
+ * Returns 0, or < 0 on error.  The peak that FP64-bound kernels are quoted
+ * against. */
+int fgpu_measure_fp64_peak(double* tflops, double* ms);
+
 /* ---- serving: continuous batching of simulation requests ------------------
  * Requests are admitted into new GPU batches (own stream each) as soon as the
  * HBM budget allows, after a short batching window (min_batch requests or
