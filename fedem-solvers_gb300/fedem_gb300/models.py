@@ -472,3 +472,75 @@ def space_frame_c2(seed=2, storeys=12, bays=4, h=3.0, bay=3.0, n_joints=40, n_sp
                 f"  f1 = {_f(load / len(top))}\n  loadEngineId = {eng}\n/\n")
     opts = ["-timeInc=%r" % dt, "-timeEnd=%r" % (steps * dt), "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
     return fsi, opts
+
+
+def part_records(pid, triad_ids, origin, files, n_gen, undpos, R=None, alpha1=0.0, alpha2=0.0, gen_bc=None,
+                 ref_offset=1.0):
+    """&SUP_EL and &TRIAD_UNDPOS records of a reduced part: triads
+    `triad_ids`, generalized DOFs `n_gen`, matrices from `files` (K, M, G
+    paths), part axes R (columns; default global) at `origin`, each triad's
+    position in part axes in `undpos`.  The corotated frame follows the first
+    two triads and a point `ref_offset` along part Y from the first one
+    (shadowPosAlg 1)."""
+    R = np.eye(3) if R is None else np.asarray(R, float)
+    ta, tb = triad_ids[0], triad_ids[1]
+    files_line = " ".join(f"'{files[k]}'" for k in ("K", "M", "G"))
+    bc = "" if gen_bc is None else "  BC = " + " ".join(str(int(v)) for v in gen_bc) + "\n"
+    out = [f"&SUP_EL\n  id = {pid}\n  numTriads = {len(triad_ids)}\n  triadIds = {' '.join(map(str, triad_ids))}\n"
+           f"  numGenDOFs = {n_gen}\n{bc}  inputFiles = {files_line}\n  shadowPosAlg = 1\n"
+           f"  refTriad1Id = {ta}, offset1 = 0.0 0.0 0.0\n  refTriad2Id = {tb}, offset2 = 0.0 0.0 0.0\n"
+           f"  refTriad3Id = {ta}, offset3 = 0.0 {_f(ref_offset)} 0.0\n"
+           f"  alpha1 = {_f(alpha1)}\n  alpha2 = {_f(alpha2)}\n"
+           f"  supPos = {_rows34(R, origin)}\n/\n"]
+    for t, p in zip(triad_ids, undpos):
+        out.append(f"&TRIAD_UNDPOS\n  supElId = {pid}\n  triadId = {t}\n"
+                   f"  undPosInSupElSystem = {_rows34(np.eye(3), p)}\n/\n")
+    return "".join(out)
+
+
+def superelement_chain_c3(directory, n_parts=16, n_modes=30, length=2.0, width=0.2, height=0.2, nx=40, ny=4,
+                          nz=4, torque=500.0, freq=2.0, damping=0.01, damping_hz=10.0, steps=4000, dt=5.0e-4,
+                          g=9.81):
+    """Superelement chain: `n_parts` steel blocks (length x width x height,
+    meshed with nx x ny x nz hexahedra) in series along global X, each reduced
+    by the Craig-Bampton reducer to its two end-face triads plus `n_modes`
+    component modes ((12 + n_modes)^2 K and M, written as binary matrix files
+    into `directory`).  Consecutive parts are joined by revolute joints whose
+    axis is the chain axis X (the master is the end triad of part k, the
+    slave the first triad of part k + 1): every part is free to turn about
+    the axis, bending and shear pass through.  The first triad is clamped,
+    the last one pinned (translations fixed).  Gravity -Z; a harmonic torque
+    `torque` sin(2 pi freq t) about X at the last triad; Rayleigh damping
+    `damping` at `damping_hz`, half mass- and half stiffness-proportional.
+    Returns (fsi, options, info)."""
+    from . import reducer
+
+    paths, (Kr, Mr, fg, w2) = reducer.block_part_files(directory, length, width, height, nx, ny, nz, n_modes)
+    w0 = 2.0 * np.pi * damping_hz
+    a1, a2 = damping * w0, damping / w0
+    triads, joints, parts = [], [], []
+    rot = np.array([[0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])  # joint Z = global X
+    for k in range(n_parts):
+        ta, tb = 1 + 2 * k, 2 + 2 * k
+        x0 = k * length
+        triads.append({"id": ta, "pos": (x0, 0.0, 0.0), "bc": [0] * 6 if k == 0 else None})
+        triads.append({"id": tb, "pos": (x0 + length, 0.0, 0.0),
+                       "bc": [0, 0, 0, 1, 1, 1] if k == n_parts - 1 else None})
+        parts.append(part_records(5000 + k, [ta, tb], (x0, 0.0, 0.0), paths, n_modes,
+                                  [(0.0, 0.0, 0.0), (length, 0.0, 0.0)], alpha1=a1, alpha2=a2,
+                                  ref_offset=length))
+        if k > 0:
+            joints.append({"id": 600 + k, "type": 1, "slave": ta, "master": ta - 1, "pos": (x0, 0.0, 0.0),
+                           "rot": rot, "dofs": [(6, 1)]})
+    fsi = frame_fsi(triads, [], [], joints=joints, gravity=(0.0, 0.0, -g), title="superelement chain")
+    fsi += "".join(parts)
+    eng = 990000
+    fsi += (f"&FUNCTION\n  id = {eng + 1}\n  type = 'SINUSOIDAL'\n  realDataSize = 4\n"
+            f"  realData = {_f(freq)} 0.0 1.0 0.0\n/\n"
+            f"&SENSOR\n  id = {eng + 2}\n  type = 'TIME'\n/\n"
+            f"&ENGINE\n  id = {eng}\n  functionId = {eng + 1}\n  nArg = 1\n  argSensorId = {eng + 2}\n/\n"
+            f"&LOAD\n  id = 980000\n  triadId = {2 * n_parts}\n  lDof = 4\n  f0 = 0.0\n  f1 = {_f(torque)}\n"
+            f"  loadEngineId = {eng}\n/\n")
+    opts = ["-timeInc=%r" % dt, "-timeEnd=%r" % (steps * dt), "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
+    info = {"Kr": Kr, "Mr": Mr, "fg": fg, "w2": w2, "files": paths, "tip": 2 * n_parts}
+    return fsi, opts, info

@@ -551,20 +551,44 @@ struct Prop {
   double orient[3] = {0};
 };
 
+// Superelement (SupElType, supElTypeModule.f90): nTri triads with six DOFs
+// each, then nGen generalized (component-mode) DOFs; n = 6 nTri + nGen.  A
+// beam is the case nTri = 2, nGen = 0 with matrices from its cross section;
+// a reduced part reads K, M and the gravity force vectors from files.
 struct Elem {
   int id = 0;
-  int tri[2] = {-1, -1};      // triad indices
+  int nTri = 2, nGen = 0, n = 12;
+  std::vector<int> tri;       // triad indices
   int ref[3] = {0, 0, 0};     // local node index of the three reference triads
   double offset[3][3];        // reference point offsets, in triad axes
   M34 supTr, supTrPrev, triRelSup;
-  M34 TrUnd[2];
-  double K[144], M[144], C[144], N[144];
-  double fg[36];              // 12x3 column-major gravity force vectors
+  std::vector<double> TrUnd;  // undeformed triad positions, 12 per triad (3x4 row-major)
+  std::vector<double> K, M, C, N;  // n x n column-major
+  std::vector<double> fg;          // n x 3 column-major gravity force vectors
   bool hasC = false, hasVld = false;
   double stiffScale = 1.0, massScale = 1.0, alpha1 = 0.0, alpha2 = 0.0;
+  std::vector<double> alpha3, alpha4;  // damping factors of the generalized DOFs
   double stifScl = 1.0, kDmp = 0.0;
-  double finit[12], finitPrev[12], uld[12], uldd[12], vld[12];
-  double FS[12], FD[12], FI[12], Q[12];
+  std::vector<double> finit, finitPrev, uld, uldd, vld;  // vld: the 6 nTri triad DOFs
+  std::vector<double> FS, FD, FI, Q;
+  std::vector<double> genUr, genUrPrev;  // generalized DOF values (genDOFs%ur)
+  std::vector<int> genBC;
+  int genFirstDof = -1;  // first generalized DOF in the DOF vectors
+  int prop = -1;         // beam property index (elPropId), -1 for a reduced part
+  std::string files[3];  // stiffness, mass, gravity force matrix files
+  double tu(int i, int r, int c) const { return TrUnd[12 * i + 4 * r + c]; }
+  void allocate() {
+    n = 6 * nTri + nGen;
+    K.assign((size_t)n * n, 0.0);
+    M.assign((size_t)n * n, 0.0);
+    C.assign((size_t)n * n, 0.0);
+    N.assign((size_t)n * n, 0.0);
+    fg.assign((size_t)n * 3, 0.0);
+    for (auto* v : {&finit, &finitPrev, &uld, &uldd, &FS, &FD, &FI, &Q}) v->assign(n, 0.0);
+    vld.assign(6 * nTri, 0.0);
+    genUr.assign(nGen, 0.0);
+    genUrPrev.assign(nGen, 0.0);
+  }
 };
 
 struct Load {
@@ -656,7 +680,8 @@ struct OracleModel {
   // SAM
   int ndof = 0, neq = 0;
   std::vector<int> meqn, dofType;
-  std::vector<int> elEq;  // 12 per element: 0-based equation or -1
+  std::vector<int> elEq;   // n per element: 0-based equation, -1 fixed, <= -2 prescribed
+  std::vector<int> elOff;  // start of each element's codes in elEq
 
   // skyline (upper profile, column oriented)
   std::vector<int> first;      // first row of each column
@@ -730,33 +755,44 @@ static int updateCorot(const OracleModel& m, Elem& e, bool init) {
 static void buildFinit(const OracleModel& m, Elem& e) {
   M34 inv;
   invert34(e.supTr, inv);
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < e.nTri; ++i) {
     M34 loc;
     matmul34(inv, m.triads[e.tri[i]].ur, loc);
-    double* f = e.finit + 6 * i;
-    for (int r = 0; r < 3; ++r) f[r] = loc[r][3] - e.TrUnd[i][r][3];
+    double* f = e.finit.data() + 6 * i;
+    for (int r = 0; r < 3; ++r) f[r] = loc[r][3] - e.tu(i, r, 3);
     double dR[3][3];
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c)
-        dR[r][c] = loc[r][0] * e.TrUnd[i][0][c] + loc[r][1] * e.TrUnd[i][1][c] + loc[r][2] * e.TrUnd[i][2][c];
+        dR[r][c] = loc[r][0] * e.tu(i, 0, c) + loc[r][1] * e.tu(i, 1, c) + loc[r][2] * e.tu(i, 2, c);
     f[3] = dR[2][1];
     f[4] = dR[0][2];
     f[5] = dR[1][0];
   }
+  // generalized DOFs (:1108-1112)
+  for (int g = 0; g < e.nGen; ++g) e.finit[6 * e.nTri + g] = e.genUr[g];
 }
 
-static void matvec12(const double* A, const double* x, double s, double* y) {
-  for (int i = 0; i < 12; ++i) {
+// y = s * A x, A n x n column-major (the leading nr rows and columns when nr < n)
+static void matvecN(const double* A, int n, const double* x, double s, double* y, int nr = -1) {
+  if (nr < 0) nr = n;
+  for (int i = 0; i < nr; ++i) {
     double t = 0.0;
-    for (int j = 0; j < 12; ++j) t += A[i + 12 * j] * x[j];
+    for (int j = 0; j < nr; ++j) t += A[i + (size_t)n * j] * x[j];
     y[i] = s * t;
   }
 }
 
-// Element velocity/acceleration in corotated axes (supElRoutinesModule.f90:47-85).
+// System DOF (0-based) of local DOF i of an element: triad DOFs, then the
+// generalized DOFs (csExtractElv / MADOF order of the element's SAM nodes).
+static int elemDof(const OracleModel& m, const Elem& e, int i) {
+  return i < 6 * e.nTri ? m.triads[e.tri[i / 6]].firstDof + i % 6 : e.genFirstDof + (i - 6 * e.nTri);
+}
+
+// Element velocity/acceleration in corotated axes (supElRoutinesModule.f90:47-85);
+// the generalized DOFs are copied.
 static void setElemVelAcc(const OracleModel& m, Elem& e, const std::vector<double>& v,
                           const std::vector<double>& a) {
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < e.nTri; ++i) {
     int d = m.triads[e.tri[i]].firstDof;
     for (int g = 0; g < 2; ++g) {
       double vv[3], aa[3];
@@ -767,10 +803,16 @@ static void setElemVelAcc(const OracleModel& m, Elem& e, const std::vector<doubl
       }
     }
   }
+  for (int g = 0; g < e.nGen; ++g) {
+    e.uld[6 * e.nTri + g] = v[e.genFirstDof + g];
+    e.uldd[6 * e.nTri + g] = a[e.genFirstDof + g];
+  }
 }
 
+// triad DOF groups to system directions (UpdateSupEls :410-450); the
+// generalized DOFs keep their values
 static void rotateOut(const Elem& e, double* f) {
-  for (int g = 0; g < 4; ++g) {
+  for (int g = 0; g < 2 * e.nTri; ++g) {
     double x[3] = {f[3 * g], f[3 * g + 1], f[3 * g + 2]};
     for (int r = 0; r < 3; ++r) f[3 * g + r] = e.supTr[r][0] * x[0] + e.supTr[r][1] * x[1] + e.supTr[r][2] * x[2];
   }
@@ -889,7 +931,9 @@ static void dofTerms(const OracleModel& m, int d, std::vector<Term>& out) {
 }
 
 static bool elemConstrained(const OracleModel& m, const Elem& e) {
-  return m.dep[m.triads[e.tri[0]].firstDof] >= 0 || m.dep[m.triads[e.tri[1]].firstDof] >= 0;
+  for (int i = 0; i < e.nTri; ++i)
+    if (m.dep[m.triads[e.tri[i]].firstDof] >= 0) return true;
+  return false;
 }
 
 // Element forces (supElRoutinesModule.f90:231-456, UpdateSupEls; and :460-630,
@@ -904,32 +948,37 @@ static int updateElems(OracleModel& m, bool newPositions, bool isStatic, bool co
     } else if (isStatic) {
       buildFinit(m, e);
     }
+    const int n = e.n;
     if (isStatic) {
-      for (int k = 0; k < 12; ++k) { e.FI[k] = 0.0; e.FD[k] = 0.0; }
+      for (int k = 0; k < n; ++k) { e.FI[k] = 0.0; e.FD[k] = 0.0; }
     } else {
-      matvec12(e.M, e.uldd, 1.0, e.FI);
+      matvecN(e.M.data(), n, e.uldd.data(), 1.0, e.FI.data());
       if (e.hasC)
-        matvec12(e.C, e.uld, e.stifScl, e.FD);
+        matvecN(e.C.data(), n, e.uld.data(), e.stifScl, e.FD.data());
       else
-        for (int k = 0; k < 12; ++k) e.FD[k] = 0.0;
+        for (int k = 0; k < n; ++k) e.FD[k] = 0.0;
       if (m.timeStep > 0.0 && e.hasVld) {
-        double tmp[12], fs[12];
-        for (int k = 0; k < 12; ++k) e.vld[k] = (e.finit[k] - e.finitPrev[k]) / m.timeStep;
-        for (int k = 0; k < 12; ++k) tmp[k] = e.uld[k] - e.vld[k];
-        matvec12(e.K, tmp, e.stifScl, fs);
-        for (int k = 0; k < 12; ++k) e.FD[k] -= e.kDmp * fs[k];
+        // rigid-body filtering of the stiffness-proportional damping on the
+        // triad DOFs: Fd -= alpha2 K (uld - vld), vld = (finit - finitPrev) / h
+        const int nv = 6 * e.nTri;
+        std::vector<double> tmp(nv), fs(nv);
+        for (int k = 0; k < nv; ++k) e.vld[k] = (e.finit[k] - e.finitPrev[k]) / m.timeStep;
+        for (int k = 0; k < nv; ++k) tmp[k] = e.uld[k] - e.vld[k];
+        matvecN(e.K.data(), n, tmp.data(), e.stifScl, fs.data(), nv);
+        for (int k = 0; k < nv; ++k) e.FD[k] -= e.kDmp * fs[k];
       }
     }
-    matvec12(e.K, e.finit, e.stifScl, e.FS);
+    matvecN(e.K.data(), n, e.finit.data(), e.stifScl, e.FS.data());
     double gl[3];
     for (int c = 0; c < 3; ++c)
       gl[c] = m.gravity[0] * e.supTr[0][c] + m.gravity[1] * e.supTr[1][c] + m.gravity[2] * e.supTr[2][c];
-    for (int i = 0; i < 12; ++i) e.Q[i] = e.stifScl * (e.fg[i] * gl[0] + e.fg[i + 12] * gl[1] + e.fg[i + 24] * gl[2]);
-    rotateOut(e, e.FS);
-    rotateOut(e, e.Q);
+    for (int i = 0; i < n; ++i)
+      e.Q[i] = e.stifScl * (e.fg[i] * gl[0] + e.fg[i + n] * gl[1] + e.fg[i + 2 * n] * gl[2]);
+    rotateOut(e, e.FS.data());
+    rotateOut(e, e.Q.data());
     if (!isStatic) {
-      rotateOut(e, e.FD);
-      rotateOut(e, e.FI);
+      rotateOut(e, e.FD.data());
+      rotateOut(e, e.FI.data());
     }
   }
   // axial springs and dampers (UpdateSprings / UpdateDampers, then
@@ -1010,11 +1059,11 @@ static void getForceVectors(OracleModel& m) {
   std::vector<Term> terms;
   for (size_t k = 0; k < m.elems.size(); ++k) {
     const Elem& e = m.elems[k];
-    const int* eq = &m.elEq[12 * k];
+    const int* eq = &m.elEq[m.elOff[k]];
     if (elemConstrained(m, e)) {
       // csAddEV through the constraint equations of dependent DOFs
-      for (int i = 0; i < 12; ++i) {
-        dofTerms(m, m.triads[e.tri[i / 6]].firstDof + i % 6, terms);
+      for (int i = 0; i < e.n; ++i) {
+        dofTerms(m, elemDof(m, e, i), terms);
         for (const Term& t : terms) {
           m.FSk[t.eq] += t.c * e.FS[i];
           m.FDk[t.eq] += t.c * e.FD[i];
@@ -1024,7 +1073,7 @@ static void getForceVectors(OracleModel& m) {
       }
       continue;
     }
-    for (int i = 0; i < 12; ++i) {
+    for (int i = 0; i < e.n; ++i) {
       if (eq[i] < 0) continue;
       m.FSk[eq[i]] += e.FS[i];
       m.FDk[eq[i]] += e.FD[i];
@@ -1096,25 +1145,41 @@ static inline double& skyAt(OracleModel& m, int i, int j) {  // i <= j
 // the upper triangle (supElRoutinesModule.f90:1127-1187 AddInSupMat + MATTRA;
 // sysMatrixTypeModule.f90:2099-2259 asmSparse semantics for free DOFs).
 static void rotatedElementMatrix(const Elem& e, const double* Nloc, double* Ns) {
-  // Ns = R * N * R^T blockwise, R = supTr(:,1:3)
-  double T[144];
-  for (int bi = 0; bi < 4; ++bi)
-    for (int bj = 0; bj < 4; ++bj) {
+  // Ns = R * N * R^T on the triad DOF groups, R = supTr(:,1:3); the rows and
+  // columns of generalized DOFs are not rotated (MATTRA on the triad groups only)
+  const int n = e.n, nb = 2 * e.nTri, nt = 6 * e.nTri;
+  for (int bi = 0; bi < nb; ++bi)
+    for (int bj = 0; bj < nb; ++bj) {
       double B[3][3], W[3][3];
       for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) B[r][c] = Nloc[(3 * bi + r) + 12 * (3 * bj + c)];
+        for (int c = 0; c < 3; ++c) B[r][c] = Nloc[(3 * bi + r) + (size_t)n * (3 * bj + c)];
       for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) W[r][c] = e.supTr[r][0] * B[0][c] + e.supTr[r][1] * B[1][c] + e.supTr[r][2] * B[2][c];
       for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c)
-          T[(3 * bi + r) + 12 * (3 * bj + c)] = W[r][0] * e.supTr[c][0] + W[r][1] * e.supTr[c][1] + W[r][2] * e.supTr[c][2];
+          Ns[(3 * bi + r) + (size_t)n * (3 * bj + c)] =
+              W[r][0] * e.supTr[c][0] + W[r][1] * e.supTr[c][1] + W[r][2] * e.supTr[c][2];
     }
-  std::memcpy(Ns, T, sizeof(T));
+  for (int bi = 0; bi < nb; ++bi)
+    for (int j = nt; j < n; ++j) {
+      const double* b = Nloc + 3 * bi + (size_t)n * j;
+      for (int r = 0; r < 3; ++r)
+        Ns[(3 * bi + r) + (size_t)n * j] = e.supTr[r][0] * b[0] + e.supTr[r][1] * b[1] + e.supTr[r][2] * b[2];
+    }
+  for (int i = nt; i < n; ++i)
+    for (int bj = 0; bj < nb; ++bj) {
+      double b[3];
+      for (int c = 0; c < 3; ++c) b[c] = Nloc[i + (size_t)n * (3 * bj + c)];
+      for (int c = 0; c < 3; ++c)
+        Ns[i + (size_t)n * (3 * bj + c)] = b[0] * e.supTr[c][0] + b[1] * e.supTr[c][1] + b[2] * e.supTr[c][2];
+    }
+  for (int i = nt; i < n; ++i)
+    for (int j = nt; j < n; ++j) Ns[i + (size_t)n * j] = Nloc[i + (size_t)n * j];
 }
 
 static void buildElementNewton(Elem& e, double sM, double sC, double sK) {
   // supElRoutinesModule.f90:1254-1320, BuildSupNewtonMat (material stiffness)
-  for (int k = 0; k < 144; ++k) {
+  for (int k = 0; k < e.n * e.n; ++k) {
     double v = sM * e.M[k];
     if (e.hasC) v += sC * e.stifScl * e.C[k];
     v += sK * e.stifScl * e.K[k];
@@ -1133,39 +1198,42 @@ static void assembleSkyline(OracleModel& m, double sM, double sC, double sK, std
     m.oldScale[0] = sM; m.oldScale[1] = sK; m.oldScale[2] = sC;
     for (Elem& e : m.elems) buildElementNewton(e, sM, sC, sK);
   }
-  double Ns[144];
+  std::vector<double> NsV;
   std::vector<Term> ti, tj;
   for (size_t k = 0; k < m.elems.size(); ++k) {
-    rotatedElementMatrix(m.elems[k], m.elems[k].N, Ns);
-    const int* eq = &m.elEq[12 * k];
-    if (elemConstrained(m, m.elems[k])) {
+    const Elem& e = m.elems[k];
+    const int n = e.n;
+    NsV.resize((size_t)n * n);
+    double* Ns = NsV.data();
+    rotatedElementMatrix(e, e.N.data(), Ns);
+    const int* eq = &m.elEq[m.elOff[k]];
+    if (elemConstrained(m, e)) {
       // T^T N T: every pair of terms, upper triangle (asmSparse with MEEN < 0)
-      const Elem& e = m.elems[k];
-      for (int i = 0; i < 12; ++i) {
-        dofTerms(m, m.triads[e.tri[i / 6]].firstDof + i % 6, ti);
-        for (int j = 0; j < 12; ++j) {
-          dofTerms(m, m.triads[e.tri[j / 6]].firstDof + j % 6, tj);
+      for (int i = 0; i < n; ++i) {
+        dofTerms(m, elemDof(m, e, i), ti);
+        for (int j = 0; j < n; ++j) {
+          dofTerms(m, elemDof(m, e, j), tj);
           for (const Term& a : ti)
             for (const Term& b : tj)
-              if (b.eq >= a.eq) skyAt(m, a.eq, b.eq) += a.c * b.c * Ns[i + 12 * j];
+              if (b.eq >= a.eq) skyAt(m, a.eq, b.eq) += a.c * b.c * Ns[i + (size_t)n * j];
         }
       }
       continue;
     }
-    for (int i = 0; i < 12; ++i) {
+    for (int i = 0; i < n; ++i) {
       if (eq[i] < 0) continue;
-      for (int j = 0; j < 12; ++j) {
+      for (int j = 0; j < n; ++j) {
         if (eq[j] < eq[i]) continue;
-        skyAt(m, eq[i], eq[j]) += Ns[i + 12 * j];
+        skyAt(m, eq[i], eq[j]) += Ns[i + (size_t)n * j];
       }
     }
     if (!rhs) continue;
-    for (int i = 0; i < 12; ++i) {
+    for (int i = 0; i < n; ++i) {
       if (eq[i] > -2) continue;
       double c = m.ccv[-2 - eq[i]];
       if (!(std::fabs(c) > 1.0e-15)) continue;
-      for (int j = 0; j < 12; ++j)
-        if (eq[j] >= 0) (*rhs)[eq[j]] -= c * Ns[i + 12 * j];
+      for (int j = 0; j < n; ++j)
+        if (eq[j] >= 0) (*rhs)[eq[j]] -= c * Ns[i + (size_t)n * j];
     }
   }
   for (size_t k = 0; k < m.axials.size(); ++k) {
@@ -1363,8 +1431,15 @@ static void incTriadsPos(OracleModel& m, const std::vector<double>& inc) {
   }
 }
 
+// IncSupElsGenDofs (supElRoutinesModule.f90:168-200): generalized DOFs += increments
+static void incGenDofs(OracleModel& m, const std::vector<double>& inc) {
+  for (Elem& e : m.elems)
+    for (int g = 0; g < e.nGen; ++g) e.genUr[g] += inc[e.genFirstDof + g];
+}
+
 static void incAll(OracleModel& m, const std::vector<double>& inc) {
   incTriadsPos(m, inc);
+  incGenDofs(m, inc);
   incJointsVar(m, inc);
 }
 
@@ -1432,7 +1507,8 @@ static int staticEquilibrium(OracleModel& m) {
   for (Triad& t : m.triads) std::memcpy(t.urPrev, t.ur, sizeof(M34));
   for (Elem& e : m.elems) {
     std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
-    std::memcpy(e.finitPrev, e.finit, sizeof(e.finit));
+    e.finitPrev = e.finit;
+    e.genUrPrev = e.genUr;
   }
   for (Joint& J : m.joints) J.jVarPrev = J.jVar;
   return 0;
@@ -1527,7 +1603,8 @@ static void restoreLastStep(OracleModel& m) {
     if (t.nDOFs > 0) std::memcpy(t.ur, t.urPrev, sizeof(M34));
   for (Elem& e : m.elems) {
     std::memcpy(e.supTr, e.supTrPrev, sizeof(M34));
-    std::memcpy(e.finit, e.finitPrev, sizeof(e.finit));
+    e.finit = e.finitPrev;
+    e.genUr = e.genUrPrev;
   }
 }
 
@@ -1587,6 +1664,42 @@ static int staticInt(OracleModel& m) {
 // ---------------------------------------------------------------------------
 // Set-up (initiateModule.f90:43-547 subset; samSolverModule.f90:95-250)
 // ---------------------------------------------------------------------------
+
+// Reads nval doubles from a FEDEM binary matrix file (readDoubleDBfile,
+// binaryDBInterface.f90:387-435; writeTagDB/readTagDB, binaryDB.c:643-731):
+// the file opens with the tag text '#FEDEM <dtype>', its header ends with the
+// version field ';1.0;\n', and the values follow as raw little-endian doubles
+// to the end of the file.  The bytes between the tag text and the version
+// field (the endian mark and checksum that FFa_writeTag of the fedem-foundation
+// submodule writes) are not interpreted.  A relative path is taken relative to
+// the directory of the -fsifile option, else the working directory.
+static int readFmx(const OracleModel& m, const std::string& name, const char* dtype, size_t nval,
+                   std::vector<double>& out) {
+  if (name.empty()) return -1;
+  std::string path = name;
+  const std::string fsiFile = m.opt.s("fsifile");
+  if (path[0] != '/' && !fsiFile.empty()) {
+    const size_t slash = fsiFile.find_last_of('/');
+    if (slash != std::string::npos) path = fsiFile.substr(0, slash + 1) + path;
+  }
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return -1;
+  std::vector<char> buf;
+  char chunk[65536];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  std::fclose(f);
+  const std::string tag = std::string("#FEDEM ") + dtype;
+  const size_t dataBytes = 8 * nval;
+  if (buf.size() < tag.size() + 6 + dataBytes) return -2;
+  const size_t head = buf.size() - dataBytes;
+  if (std::memcmp(buf.data(), tag.data(), tag.size()) != 0) return -3;
+  const std::string ver = ";1.0;\n";
+  if (std::memcmp(buf.data() + head - ver.size(), ver.data(), ver.size()) != 0) return -4;
+  out.assign(nval, 0.0);
+  std::memcpy(out.data(), buf.data() + head, dataBytes);
+  return 0;
+}
 
 static int setup(OracleModel& m, const char* fsi) {
   std::vector<Record> recs = parseNamelists(fsi);
@@ -1663,20 +1776,42 @@ static int setup(OracleModel& m, const char* fsi) {
   std::vector<Axial> springs, dampers;
   for (const Record& r : recs) {
     if (r.name == "sup_el") {
+      // SUP_EL namelist (supElTypeModule.f90:1299-1350) as ReadSupEls uses it
+      // (initiateSupElTypeModule.f90:140-700)
       Elem e;
       e.id = r.i("id");
       auto tids = r.dv("triadids");
-      if (r.i("numtriads", 2) != 2 || tids.size() < 2) return -10;
-      for (int k = 0; k < 2; ++k) {
+      e.nTri = r.i("numtriads", 2);
+      e.nGen = r.i("numgendofs", 0);
+      if (e.nTri < 2 || (int)tids.size() < e.nTri || e.nGen < 0) return -10;
+      // not in this restatement: nonlinear parts, part load cases, stress
+      // stiffening, mass-matrix correction, the shadowPosAlg 2 frame,
+      // time-dependent stiffness or damping scaling
+      if (r.i("numstates", 0) > 0 || r.i("numloadcase", 0) > 0) return -10;
+      for (double v : r.dv("stressstiffflag"))
+        if (v > 0.0) return -10;
+      if (r.i("masscorrflag", -1) > 0 || r.i("shadowposalg", 0) > 1) return -10;
+      if (r.i("stiffengineid", 0) > 0 || r.i("strdmpengineid", 0) > 0) return -10;
+      e.tri.assign(e.nTri, -1);
+      for (int k = 0; k < e.nTri; ++k) {
         e.tri[k] = findTriad(m, (int)std::lround(tids[k]));
         if (e.tri[k] < 0) return -11;
       }
       int refIds[3] = {r.i("reftriad1id"), r.i("reftriad2id"), r.i("reftriad3id")};
       for (int j = 0; j < 3; ++j) {
         e.ref[j] = -1;
-        for (int k = 0; k < 2; ++k)
+        for (int k = 0; k < e.nTri; ++k)
           if ((int)std::lround(tids[k]) == refIds[j]) e.ref[j] = k;
         if (e.ref[j] < 0) return -12;
+      }
+      e.TrUnd.assign(12 * (size_t)e.nTri, 0.0);
+      if (const auto* f = r.get("inputfiles"))
+        for (size_t k = 0; k < 3 && k < f->size(); ++k) e.files[k] = (*f)[k];
+      auto bcg = r.dv("bc"), a3 = r.dv("alpha3"), a4 = r.dv("alpha4");
+      for (int g = 0; g < e.nGen; ++g) {
+        e.genBC.push_back(g < (int)bcg.size() ? (int)std::lround(bcg[g]) : 1);
+        e.alpha3.push_back(g < (int)a3.size() ? a3[g] : 0.0);
+        e.alpha4.push_back(g < (int)a4.size() ? a4[g] : 0.0);
       }
       std::vector<double> off[3] = {r.dv("offset1"), r.dv("offset2"), r.dv("offset3")};
       rowMajor34(r.dv("suppos"), e.supTr);
@@ -1693,13 +1828,12 @@ static int setup(OracleModel& m, const char* fsi) {
         const Triad& t = m.triads[e.tri[e.ref[j]]];
         for (int c = 0; c < 3; ++c) e.offset[j][c] = so[0] * t.ur[0][c] + so[1] * t.ur[1][c] + so[2] * t.ur[2][c];
       }
-      int pid = r.i("elpropid");
-      int pidx = -1;
-      for (size_t k = 0; k < m.props.size(); ++k)
-        if (m.props[k].id == pid) pidx = (int)k;
-      if (pidx < 0) return -13;
-      // remember property index in K[0] slot temporarily via alpha; store separately
-      e.kDmp = (double)pidx;
+      if (e.files[0].empty()) {  // a beam: matrices from its element property
+        int pid = r.i("elpropid");
+        for (size_t k = 0; k < m.props.size(); ++k)
+          if (m.props[k].id == pid) e.prop = (int)k;
+        if (e.prop < 0 || e.nTri != 2 || e.nGen != 0) return -13;
+      }
       m.elems.push_back(e);
       pendingUnd = (int)m.elems.size() - 1;
     } else if (r.name == "triad_undpos") {
@@ -1710,10 +1844,16 @@ static int setup(OracleModel& m, const char* fsi) {
       if (ei < 0) return -14;
       Elem& e = m.elems[ei];
       int node = -1;
-      for (int k = 0; k < 2; ++k)
+      for (int k = 0; k < e.nTri; ++k)
         if (m.triads[e.tri[k]].id == tid) node = k;
       if (node < 0) return -15;
-      rowMajor34(r.dv("undposinsupelsystem"), e.TrUnd[node]);
+      for (const char* key : {"eccvec", "eccmass"})
+        for (double v : r.dv(key))
+          if (std::fabs(v) > 1.0e-16) return -15;  // eccentricity vectors are not in this restatement
+      M34 U;
+      rowMajor34(r.dv("undposinsupelsystem"), U);
+      for (int rr = 0; rr < 3; ++rr)
+        for (int c = 0; c < 4; ++c) e.TrUnd[12 * node + 4 * rr + c] = U[rr][c];
     } else if (r.name == "load") {
       Load l;
       l.triad = findTriad(m, r.i("triadid"));
@@ -1851,14 +1991,68 @@ static int setup(OracleModel& m, const char* fsi) {
   for (const Axial& a : m.axials)
     for (int k = 0; k < 2; ++k)
       if (m.triads[a.tri[k]].nDOFs < 3) return -47;
-  // element matrices (finiteElementModule.f90:283-541, CalcBeamElementMatrices)
+  // element matrices: reduced parts from their matrix files (ReadSupElMatrices,
+  // initiateSupElTypeModule.f90:962-1033), beams from their cross section
+  // (finiteElementModule.f90:283-541, CalcBeamElementMatrices)
   for (Elem& e : m.elems) {
-    const Prop& p = m.props[(int)e.kDmp];
+    e.allocate();
+    if (e.prop < 0) {
+      const size_t nn = (size_t)e.n * e.n;
+      if (readFmx(m, e.files[0], "stiffness matrix", nn, e.K) != 0) return -80;
+      if (readFmx(m, e.files[1], "mass matrix", nn, e.M) != 0) return -81;
+      if (!e.files[2].empty() && readFmx(m, e.files[2], "gravity force vectors", 3 * (size_t)e.n, e.fg) != 0)
+        return -82;
+      // structural damping (computeStructDamping, :740-780): Rayleigh on the
+      // unscaled matrices, individual factors on the generalized DOFs
+      bool haveM = e.alpha1 > 0.0, haveK = e.alpha2 > 0.0;
+      for (int g = 0; g < e.nGen; ++g) {
+        haveM = haveM || e.alpha3[g] > 0.0;
+        haveK = haveK || e.alpha4[g] > 0.0;
+      }
+      bool any3 = false, any4 = false;
+      for (int g = 0; g < e.nGen; ++g) {
+        any3 = any3 || e.alpha3[g] > 0.0;
+        any4 = any4 || e.alpha4[g] > 0.0;
+      }
+      for (int g = 0; g < e.nGen; ++g) {
+        if (!any3) e.alpha3[g] = e.alpha1;
+        if (!any4) e.alpha4[g] = e.alpha2;
+      }
+      const int n = e.n, nd = 6 * e.nTri;
+      if (haveM || haveK) {
+        for (size_t k = 0; k < nn; ++k) e.C[k] = e.alpha1 * e.M[k] + e.alpha2 * e.K[k];
+        for (int g = 0; g < e.nGen; ++g) {
+          const int j = nd + g;
+          const double d3 = e.alpha3[g] - e.alpha1, d4 = e.alpha4[g] - e.alpha2;
+          if (std::fabs(d3) > 1.0e-16) {
+            e.C[j + (size_t)n * j] += d3 * e.M[j + (size_t)n * j];
+            for (int i = 0; i < nd; ++i) e.C[i + (size_t)n * j] += d3 * e.M[i + (size_t)n * j];
+            for (int i = 0; i < nd; ++i) e.C[j + (size_t)n * i] += d3 * e.M[j + (size_t)n * i];
+          }
+          if (std::fabs(d4) > 1.0e-16) e.C[j + (size_t)n * j] += d4 * e.K[j + (size_t)n * j];
+        }
+        e.hasC = true;
+      }
+      if (std::fabs(e.stiffScale - 1.0) > 1.0e-16)
+        for (size_t k = 0; k < nn; ++k) e.K[k] *= e.stiffScale;
+      if (std::fabs(e.massScale - 1.0) > 1.0e-16) {
+        for (size_t k = 0; k < nn; ++k) e.M[k] *= e.massScale;
+        for (int k = 0; k < 3 * n; ++k) e.fg[k] *= e.massScale;
+      }
+      double a2 = e.alpha2;
+      if (e.hasC && std::fabs(e.stiffScale - 1.0) > 1.0e-16) a2 /= e.stiffScale;
+      e.kDmp = a2;
+      e.hasVld = a2 > 0.0 && m.stiffDampFiltering > 0;
+      if (updateCorot(m, e, true) != 0) return -22;
+      std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
+      continue;
+    }
+    const Prop& p = m.props[e.prop];
     e.kDmp = 0.0;
     double Xg[5][3];
     for (int k = 0; k < 3; ++k) {
-      Xg[3][k] = e.TrUnd[0][k][3];
-      Xg[4][k] = e.TrUnd[1][k][3];
+      Xg[3][k] = e.tu(0, k, 3);
+      Xg[4][k] = e.tu(1, k, 3);
       Xg[0][k] = Xg[3][k];
       Xg[1][k] = Xg[4][k];
     }
@@ -1874,13 +2068,13 @@ static int setup(OracleModel& m, const char* fsi) {
     for (int q = 0; q < 5; ++q) { X[q] = Xg[q][0]; Y[q] = Xg[q][1]; Z[q] = Xg[q][2]; }
     double EP[6] = {p.mat[1], p.mat[2], p.geo[0], p.geo[1], p.geo[2], p.geo[3]};
     double CA[2] = {p.geo[4], p.geo[5]}, XS[2] = {p.geo[6], p.geo[7]};
-    if (beam31(e.K, X, Y, Z, EP, CA, XS) != 0) return -21;
+    if (beam31(e.K.data(), X, Y, Z, EP, CA, XS) != 0) return -21;
     double rho = p.mat[0];
     double Ix = p.geo[1] + p.geo[2];
     if (Ix <= 0.0) Ix = p.geo[3];
     double Area = EP[2], z1 = Ix;
     if (EP[0] <= epsDiv0 && rho > epsDiv0) { Area = 1.0; z1 = Ix / rho; }
-    beam35(e.M, X, Y, Z, Area, rho, z1);
+    beam35(e.M.data(), X, Y, Z, Area, rho, z1);
     for (int i = 0; i < 12; ++i)
       for (int c = 0; c < 3; ++c) e.fg[i + 12 * c] = e.M[i + 12 * c] + e.M[i + 12 * (c + 6)];
     // structural damping (initiateSupElTypeModule.f90:549-599), unscaled matrices
@@ -1901,10 +2095,6 @@ static int setup(OracleModel& m, const char* fsi) {
     e.kDmp = a2;
     e.hasVld = a2 > 0.0 && m.stiffDampFiltering > 0;
     (void)a1;
-    for (int k = 0; k < 12; ++k) {
-      e.finit[k] = e.finitPrev[k] = e.uld[k] = e.uldd[k] = e.vld[k] = 0.0;
-      e.FS[k] = e.FD[k] = e.FI[k] = e.Q[k] = 0.0;
-    }
     if (updateCorot(m, e, true) != 0) return -22;
     std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
   }
@@ -1917,7 +2107,12 @@ static int setup(OracleModel& m, const char* fsi) {
     std::memcpy(t.urPrev, t.ur, sizeof(M34));
   }
   const int ntriDof = m.ndof;
-  for (Joint& J : m.joints) {  // joint DOFs after the triads (initSAM_dofStatus)
+  for (Elem& e : m.elems) {  // generalized DOFs of the parts after the triads (initSAM_dofStatus)
+    if (e.nGen == 0) continue;
+    e.genFirstDof = m.ndof;
+    m.ndof += e.nGen;
+  }
+  for (Joint& J : m.joints) {  // joint DOFs after those
     J.firstDof = m.ndof;
     m.ndof += (int)J.lDof.size();
   }
@@ -1952,6 +2147,13 @@ static int setup(OracleModel& m, const char* fsi) {
       else if (t.BC[k] == 1 || (t.BC[k] == 2 && !addBC)) m.meqn[d] = ++m.neq;
       else if (t.BC[k] != 0) return -30;  // additional initial-equilibrium BCs are not in this subset
     }
+  for (Elem& e : m.elems)
+    for (int g = 0; g < e.nGen; ++g) {
+      const int d = e.genFirstDof + g;
+      m.dofType[d] = 3;  // genDof_p
+      if (e.genBC[g] == 1 || (e.genBC[g] == 2 && !addBC)) m.meqn[d] = ++m.neq;
+      else if (e.genBC[g] != 0) return -30;
+    }
   for (Joint& J : m.joints)
     for (size_t k = 0; k < J.lDof.size(); ++k) {
       const int d = J.firstDof + (int)k;
@@ -1974,12 +2176,13 @@ static int setup(OracleModel& m, const char* fsi) {
     if (m.dep[m.triads[l.triad].firstDof] >= 0) return -79;  // load on a dependent triad
   m.ccv.assign(m.motions.size(), 0.0);
   for (const Elem& e : m.elems)
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < e.nTri; ++k)
       if (m.triads[e.tri[k]].nDOFs != 6) return -31;
-  m.elEq.assign(12 * m.elems.size(), -1);
+  m.elOff.assign(m.elems.size() + 1, 0);
+  for (size_t k = 0; k < m.elems.size(); ++k) m.elOff[k + 1] = m.elOff[k] + m.elems[k].n;
+  m.elEq.assign(m.elOff.back(), -1);
   for (size_t k = 0; k < m.elems.size(); ++k)
-    for (int n = 0; n < 2; ++n)
-      for (int d = 0; d < 6; ++d) m.elEq[12 * k + 6 * n + d] = m.meqn[m.triads[m.elems[k].tri[n]].firstDof + d] - 1;
+    for (int i = 0; i < m.elems[k].n; ++i) m.elEq[m.elOff[k] + i] = m.meqn[elemDof(m, m.elems[k], i)] - 1;
   m.axEq.assign(6 * m.axials.size(), -1);
   for (size_t k = 0; k < m.axials.size(); ++k)
     for (int n = 0; n < 2; ++n)
@@ -2000,12 +2203,12 @@ static int setup(OracleModel& m, const char* fsi) {
   };
   for (size_t k = 0; k < m.elems.size(); ++k) {
     if (!elemConstrained(m, m.elems[k])) {
-      clique(&m.elEq[12 * k], 12);
+      clique(&m.elEq[m.elOff[k]], m.elems[k].n);
       continue;
     }
     // every equation the element's DOFs expand to (the coefficients vary)
     std::vector<int> ex;
-    for (int n = 0; n < 2; ++n) {
+    for (int n = 0; n < m.elems[k].nTri; ++n) {
       const Triad& t = m.triads[m.elems[k].tri[n]];
       const int d0 = t.firstDof;
       if (m.dep[d0] >= 0) {
@@ -2015,6 +2218,7 @@ static int setup(OracleModel& m, const char* fsi) {
         for (int q = 0; q < 6; ++q) ex.push_back(m.meqn[d0 + q] - 1);
       }
     }
+    for (int g = 0; g < m.elems[k].nGen; ++g) ex.push_back(m.meqn[m.elems[k].genFirstDof + g] - 1);
     clique(ex.data(), (int)ex.size());
   }
   for (size_t k = 0; k < m.axials.size(); ++k) clique(&m.axEq[6 * k], 6);
@@ -2184,7 +2388,8 @@ extern "C" int oracle_solve_next(OracleModel* m, int* ierr) {
     for (Triad& t : m->triads) std::memcpy(t.urPrev, t.ur, sizeof(M34));
     for (Elem& e : m->elems) {
       std::memcpy(e.supTrPrev, e.supTr, sizeof(M34));
-      std::memcpy(e.finitPrev, e.finit, sizeof(e.finit));
+      e.finitPrev = e.finit;
+      e.genUrPrev = e.genUr;
     }
     for (Joint& J : m->joints) J.jVarPrev = J.jVar;
   }
@@ -2240,17 +2445,20 @@ extern "C" int oracle_get_csr_pattern(OracleModel* m, int* rowptr, int* cols) {
 extern "C" int oracle_assemble_newton(OracleModel* m, double sM, double sC, double sK, double* values) {
   if (!m) return 0;
   std::fill(values, values + m->cols.size(), 0.0);
-  double Ns[144], Nl[144];
+  std::vector<double> Ns, Nl;
   for (size_t k = 0; k < m->elems.size(); ++k) {
     const Elem& e = m->elems[k];
-    for (int q = 0; q < 144; ++q) {
+    const int n = e.n;
+    Ns.resize((size_t)n * n);
+    Nl.resize((size_t)n * n);
+    for (int q = 0; q < n * n; ++q) {
       double v = sM * e.M[q];
       if (e.hasC) v += sC * e.stifScl * e.C[q];
       v += sK * e.stifScl * e.K[q];
       Nl[q] = v;
     }
-    rotatedElementMatrix(e, Nl, Ns);
-    const int* eq = &m->elEq[12 * k];
+    rotatedElementMatrix(e, Nl.data(), Ns.data());
+    const int* eq = &m->elEq[m->elOff[k]];
     auto add = [&](int a, int b, double v) {
       const int* lo = &m->cols[m->rowptr[a]];
       const int* en = &m->cols[0] + m->rowptr[a + 1];
@@ -2258,22 +2466,22 @@ extern "C" int oracle_assemble_newton(OracleModel* m, double sM, double sC, doub
     };
     if (elemConstrained(*m, e)) {
       std::vector<Term> ti, tj;
-      for (int i = 0; i < 12; ++i) {
-        dofTerms(*m, m->triads[e.tri[i / 6]].firstDof + i % 6, ti);
-        for (int j = 0; j < 12; ++j) {
-          dofTerms(*m, m->triads[e.tri[j / 6]].firstDof + j % 6, tj);
+      for (int i = 0; i < n; ++i) {
+        dofTerms(*m, elemDof(*m, e, i), ti);
+        for (int j = 0; j < n; ++j) {
+          dofTerms(*m, elemDof(*m, e, j), tj);
           for (const Term& a : ti)
             for (const Term& b : tj)
-              if (b.eq >= a.eq) add(a.eq, b.eq, a.c * b.c * Ns[i + 12 * j]);
+              if (b.eq >= a.eq) add(a.eq, b.eq, a.c * b.c * Ns[i + (size_t)n * j]);
         }
       }
       continue;
     }
-    for (int i = 0; i < 12; ++i) {
+    for (int i = 0; i < n; ++i) {
       if (eq[i] < 0) continue;
-      for (int j = 0; j < 12; ++j) {
+      for (int j = 0; j < n; ++j) {
         if (eq[j] < eq[i]) continue;
-        add(eq[i], eq[j], Ns[i + 12 * j]);
+        add(eq[i], eq[j], Ns[i + (size_t)n * j]);
       }
     }
   }
@@ -2296,13 +2504,29 @@ extern "C" int oracle_assemble_newton(OracleModel* m, double sM, double sC, doub
   return (int)m->cols.size();
 }
 
+// K (which 0), M (1) or C (2) of element iel, n x n column-major; returns n * n
 extern "C" int oracle_get_element_matrix(OracleModel* m, int iel, int which, double* mat) {
   if (!m || iel < 0 || iel >= (int)m->elems.size()) return 0;
   const Elem& e = m->elems[iel];
-  const double* src = which == 0 ? e.K : which == 1 ? e.M : e.C;
-  if (which == 2 && !e.hasC) { std::fill(mat, mat + 144, 0.0); return 144; }
-  std::copy(src, src + 144, mat);
-  return 144;
+  const int nn = e.n * e.n;
+  const std::vector<double>& src = which == 0 ? e.K : which == 1 ? e.M : e.C;
+  if (which == 2 && !e.hasC) { std::fill(mat, mat + nn, 0.0); return nn; }
+  std::copy(src.begin(), src.begin() + nn, mat);
+  return nn;
+}
+
+// number of DOFs of element iel (6 per triad + generalized DOFs)
+extern "C" int oracle_get_element_size(OracleModel* m, int iel) {
+  if (!m || iel < 0 || iel >= (int)m->elems.size()) return 0;
+  return m->elems[iel].n;
+}
+
+// generalized DOF values of element iel (genDOFs%ur); returns their number
+extern "C" int oracle_get_gen_dofs(OracleModel* m, int iel, double* v) {
+  if (!m || iel < 0 || iel >= (int)m->elems.size()) return 0;
+  const Elem& e = m->elems[iel];
+  if (v) std::copy(e.genUr.begin(), e.genUr.end(), v);
+  return e.nGen;
 }
 
 extern "C" int oracle_get_force_vector(OracleModel* m, int which, double* vec) {

@@ -61,8 +61,13 @@ int oracle_get_csr_pattern(OracleModel* m, int* rowptr, int* cols);
 /* Assembles the Newton matrix sM*M + sC*C + sK*K at the current configuration
  * into the upper CSR pattern above.  Returns nnz. */
 int oracle_assemble_newton(OracleModel* m, double sM, double sC, double sK, double* values);
-/* Element 12x12 matrices (column-major, superelement axes): 0=K, 1=M, 2=C. */
+/* Element n x n matrices (column-major, superelement axes): 0=K, 1=M, 2=C.
+ * Returns n * n. */
 int oracle_get_element_matrix(OracleModel* m, int iel, int which, double* mat);
+/* DOFs of element iel: 6 per triad, then its generalized DOFs. */
+int oracle_get_element_size(OracleModel* m, int iel);
+/* Generalized DOF values of element iel; returns their number. */
+int oracle_get_gen_dofs(OracleModel* m, int iel, double* v);
 /* System force vectors in equation order: 0=FS, 1=FD, 2=FI, 3=Q. */
 int oracle_get_force_vector(OracleModel* m, int which, double* vec);
 

@@ -49,6 +49,8 @@ def load():
         "oracle_assemble_newton": (ci, [vp, cd, cd, cd, _P(cd)]),
         "oracle_get_element_matrix": (ci, [vp, ci, ci, _P(cd)]),
         "oracle_get_force_vector": (ci, [vp, ci, _P(cd)]),
+        "oracle_get_element_size": (ci, [vp, ci]),
+        "oracle_get_gen_dofs": (ci, [vp, ci, _P(cd)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -134,9 +136,16 @@ class OracleModel:
         return rp, ci, v
 
     def element_matrix(self, iel, which):
-        m = np.zeros(144)
+        n = self.lib.oracle_get_element_size(self.h, iel)
+        m = np.zeros(n * n)
         self.lib.oracle_get_element_matrix(self.h, iel, which, m.ctypes.data_as(_P(ctypes.c_double)))
-        return m.reshape((12, 12), order="F")
+        return m.reshape((n, n), order="F")
+
+    def gen_dofs(self, iel):
+        """Generalized DOF values of element iel (empty for a beam)."""
+        v = np.zeros(max(1, self.lib.oracle_get_gen_dofs(self.h, iel, None)))
+        n = self.lib.oracle_get_gen_dofs(self.h, iel, v.ctypes.data_as(_P(ctypes.c_double)))
+        return v[:n]
 
     def force_vector(self, which):
         v = np.zeros(self.neq)
