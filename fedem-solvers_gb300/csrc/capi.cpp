@@ -366,6 +366,12 @@ bool solveEigenModes(const int nmod, double* eval, double* evec, bool dofOrder, 
     return false;
   }
   const HostModel& m = *s.model;
+  if (m.njoint > 0 || m.npart > 0) {
+    // the mass matrix of the eigenproblem is assembled from the beam elements
+    // on the host; joints' constraint equations and parts are not in it
+    e = -998;
+    return false;
+  }
   std::vector<double> lambda, vecs;
   int nNeg = 0;
   const int rc = lowestModes(*s.engine, m, nmod, lambda, vecs, nNeg);
@@ -572,6 +578,9 @@ bool getSystemMatrix(double* Smat, int iMat) {
   if (!g_core || !Smat || iMat < 0 || iMat > 3) return false;
   const HostModel& m = *g_core->model;
   if (iMat > 0) {
+    // assembled on the host from the beam elements and axial springs/dampers;
+    // joints' constraint equations and parts are not in it
+    if (m.njoint > 0 || m.npart > 0) return false;
     assembleSystemMatrix(iMat, Smat);
     return true;
   }

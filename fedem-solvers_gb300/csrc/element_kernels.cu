@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
   // the damping force is the only user of the local velocities (stiffness-proportional
   // damping C, or the kDmp term of the pass after the increment)
   const bool needUld =
-      !isStatic && (d.hasC[e] || (mode == EM_INC && d.hasVld[e] && d.m.dt[m] > 0.0));
+      !isStatic && (d.hasC[e] || ((mode == EM_INC || mode == EM_PRED) && d.hasVld[e] && d.m.dt[m] > 0.0));
   if (!isStatic) {
     const double* vs = mode == EM_PRED ? d.dk : d.urd;
     const double* as = mode == EM_PRED ? d.ak : d.urdd;
@@ -405,9 +405,12 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
     // Fi = M * uldd
     elemMatvec(d, 1, e, uldd, 1.0, y);
     rotateStore(S, y, FIo, nel, e);
-    // Fd = stifScl * C * uld  (- kDmp * stifScl * K * (uld - vld)); exactly zero without damping
+    // Fd = stifScl * C * uld  (- kDmp * stifScl * K * (uld - vld)); exactly zero without damping.
+    // The rigid-body filtering applies in the predictor too (UpdateSupEls is
+    // called with the step size there), where the deformation is the previous
+    // step's and vld is zero.
     const double dt = d.m.dt[m];
-    const bool vldActive = mode == EM_INC && d.hasVld[e] && dt > 0.0;
+    const bool vldActive = (mode == EM_INC || mode == EM_PRED) && d.hasVld[e] && dt > 0.0;
     if (d.hasC[e] || vldActive) {
       if (d.hasC[e]) {
         elemMatvec(d, 2, e, uld, ss, y);
@@ -953,7 +956,7 @@ __global__ void kMotionRhs(DevData d) {
   for (int64_t q = d.mrPtr[k]; q < d.mrPtr[k + 1]; ++q) {
     const double c = d.motCc[d.mrMot[q]];
     const int64_t src = d.mrSrc[q], lim = (int64_t)144 * d.nelTot;
-    if (fabs(c) > 1.0e-15) b -= c * (src < lim ? d.elMat[src] : d.elMatA[src - lim]);
+    if (fabs(c) > 1.0e-15) b -= c * gatherEntry(d, (int)src, lim);
   }
   d.del[eq] = b;
 }
@@ -1359,6 +1362,7 @@ void launchPredictDofs(const DevData& d, cudaStream_t s) {
 void launchElements(const DevData& d, int mode, cudaStream_t s) {
   launchJoints(d, mode, s);  // dependent triads first, as UpdateMechanism updates the joints first
   if (d.nelTot > 0) kElements<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d, mode);
+  launchParts(d, mode, s);
   if (d.naxTot > 0) kAxial<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d, mode);
   launchExpandForces(d, mode, s);
 }
@@ -1374,6 +1378,7 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
   else if (d.nelTot > 0) kRotateElementNewton<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
   if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
   launchExpandElements(d, s);
+  launchPartsNewton(d, s);
 }
 void launchCsrGather(const DevData& d, cudaStream_t s) {
   if (d.nslotTot <= 0) return;
@@ -1404,6 +1409,7 @@ void launchNormsControl(const DevData& d, cudaStream_t s) {
   kControl<<<blocksFor(32LL * d.m.n, 128), 128, 0, s>>>(d);
   long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
   kStepEnd<<<blocksFor(n), TPB, 0, s>>>(d);
+  launchPartsStepEnd(d, s);
 }
 void launchLoads(const DevData& d, cudaStream_t s) {
   if (d.nldTot > 0) kLoads<<<blocksFor(d.nldTot, 128), 128, 0, s>>>(d);

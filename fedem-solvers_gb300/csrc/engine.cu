@@ -130,13 +130,17 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       wOff(nm, 0), childOff(nm, 0), relOff(nm, 0), asmOff(nm, 0);
   int ntri = 0, ndof = 0, neq = 0, nel = 0, nfr = 0, nax = 0;
   std::vector<int> modelAxOff(nm, 0);
-  int64_t nslot = 0, ncontrib = 0, neqc = 0, nrows = 0, nl = 0, nu = 0, nw = 0, nch = 0, nrel = 0, nasm = 0;
+  std::vector<int64_t> mrXBase(nm, 0);  // start of each model's expanded matrices (parts, dependent triads)
+  int64_t nslot = 0, ncontrib = 0, neqc = 0, nrows = 0, nl = 0, nu = 0, nw = 0, nch = 0, nrel = 0, nasm = 0,
+          nxm = 0;
   bool anyC = false;
   for (int k = 0; k < nm; ++k) {
     const HostModel& h = *models[k];
     modelTriOff_[k] = ntri; modelDofOff_[k] = ndof; modelEqOff_[k] = neq; modelElOff_[k] = nel;
     modelAxOff[k] = nax;
     nax += h.nax;
+    mrXBase[k] = nxm;
+    nxm += h.cxMatSize;
     modelSlotOff_[k] = nslot; frontOff[k] = nfr; contribOff[k] = ncontrib; eqContribOff[k] = neqc;
     rowsOff[k] = nrows; lOff[k] = nl; uOff[k] = nu; wOff[k] = nw; childOff[k] = nch; relOff[k] = nrel;
     asmOff[k] = nasm;
@@ -310,9 +314,11 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
           if (src < 144 * h.nel) {
             const int e = src / 144, entry = src % 144;
             mrSrc.push_back((int64_t)entry * nel + e + modelElOff_[k]);
-          } else {
+          } else if (src < 144 * h.nel + 36 * h.nax) {
             const int a = (src - 144 * h.nel) / 36, entry = (src - 144 * h.nel) % 36;
             mrSrc.push_back((int64_t)144 * nel + (int64_t)entry * nax + modelAxOff[k] + a);
+          } else {  // the expanded matrix of a part (or of an element with a dependent triad)
+            mrSrc.push_back((int64_t)144 * nel + 36LL * nax + mrXBase[k] + (src - 144 * h.nel - 36 * h.nax));
           }
           mrMot.push_back(h.mrMot[t] + motOff[k]);
         }
@@ -569,7 +575,6 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
           }
         }
       }
-      if (xm >= INT_MAX / 2 || xv >= INT_MAX / 2) { err = "too many expanded element entries"; return -901; }
       UPV(d_.jSlave, int, jS); UPV(d_.jMaster, int, jM); UPV(d_.jNM, int, jNM); UPV(d_.jNcol, int, jNc);
       UPV(d_.jFirstDof, int, jF); UPV(d_.jNdof, int, jNd); UPV(d_.jNmats, int, jNmat); UPV(d_.jDofOff, int, jOff);
       UPV(d_.jModel, int, jMod); UPV(d_.jLdof, int, jL); UPV(d_.jImat, int, jI); UPV(d_.jVar, double, jV);
@@ -578,11 +583,100 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
       d_.jT = alloc<double>(72 * (size_t)nj);
       UPV(d_.cxEl, int, cEl); UPV(d_.cxNx, int, cNx); UPV(d_.cxMatOff, int, cMO); UPV(d_.cxVecOff, int, cVO);
       UPV(d_.cxNode, int, cNode);
+    }
+    if (xm >= INT_MAX / 2 || xv >= INT_MAX / 2) { err = "too many expanded element entries"; return -901; }
+    if (xm > 0 || xv > 0) {
       d_.elMatX = alloc<double>((size_t)std::max<int64_t>(xm, 1));
       d_.FelX = alloc<double>((size_t)std::max<int64_t>(xv, 1));
     }
   }
   trace.mark("joints", stream_);
+  // ---- reduced parts -------------------------------------------------------------------
+  {
+    int np = 0;
+    for (int k = 0; k < nm; ++k) np += models[k]->npart;
+    d_.npartTot = np;
+    if (np > 0) {
+      std::vector<int> pModel, pN, pNtri, pNgen, pTriOff, pTri, pTriJoint, pRef, pGenFirst, pGenOff, pVecOff, pNx,
+          pXMat, pXVec;
+      std::vector<int64_t> pMatOff;
+      std::vector<double> pOffset, pSupTr, pRel, pTrUnd, pK, pM, pC, pFg, pSs, pKd, pGen;
+      std::vector<uint8_t> pHasC, pHasVld;
+      int64_t vecBase = 0, matBase = 0;
+      int genBase = 0;
+      for (int k = 0; k < nm; ++k) {
+        const HostModel& h = *models[k];
+        for (int p = 0; p < h.npart; ++p) {
+          const int n = 6 * h.pNtri[p] + h.pNgen[p];
+          pModel.push_back(k);
+          pN.push_back(n);
+          pNtri.push_back(h.pNtri[p]);
+          pNgen.push_back(h.pNgen[p]);
+          pTriOff.push_back((int)pTri.size());
+          for (int t = 0; t < h.pNtri[p]; ++t) {
+            const int tri = h.pTri[h.pTriOff[p] + t];
+            pTri.push_back(tri + modelTriOff_[k]);
+            const int dd = h.dofDep[h.triFirstDof[tri]];
+            pTriJoint.push_back(dd >= 0 ? dd / 6 + modelJointOff[k] : -1);
+            for (int q = 0; q < 12; ++q) pTrUnd.push_back(h.pTrUnd[12 * (size_t)(h.pTriOff[p] + t) + q]);
+          }
+          for (int j = 0; j < 3; ++j) pRef.push_back(h.pRef[3 * p + j]);
+          for (int q = 0; q < 9; ++q) pOffset.push_back(h.pOffset[9 * (size_t)p + q]);
+          for (int q = 0; q < 12; ++q) {
+            pSupTr.push_back(h.pSupTr[12 * (size_t)p + q]);
+            pRel.push_back(h.pTriRelSup[12 * (size_t)p + q]);
+          }
+          pGenFirst.push_back(h.pGenFirstDof[p] + modelDofOff_[k]);
+          pGenOff.push_back(genBase + h.pGenOff[p]);
+          pVecOff.push_back((int)(vecBase + h.pVecOff[p]));
+          pMatOff.push_back(matBase + h.pMatOff[p]);
+          pNx.push_back(h.pNx[p]);
+          pXMat.push_back((int)(cxMatBase[k] + h.pXMatOff[p]));
+          pXVec.push_back((int)(cxVecBase[k] + h.pXVecOff[p]));
+          pSs.push_back(h.pStifScl[p]);
+          pKd.push_back(h.pKDmp[p]);
+          pHasC.push_back(h.pHasC[p]);
+          pHasVld.push_back(h.pHasVld[p]);
+          d_.partMaxN = std::max(d_.partMaxN, n);
+          d_.partMaxNx = std::max(d_.partMaxNx, h.pNx[p]);
+        }
+        pK.insert(pK.end(), h.pK.begin(), h.pK.end());
+        pM.insert(pM.end(), h.pM.begin(), h.pM.end());
+        pC.insert(pC.end(), h.pC.begin(), h.pC.end());
+        pFg.insert(pFg.end(), h.pFg.begin(), h.pFg.end());
+        int ngen = 0, nvec = 0;
+        for (int p = 0; p < h.npart; ++p) {
+          ngen += h.pNgen[p];
+          nvec += 6 * h.pNtri[p] + h.pNgen[p];
+        }
+        genBase += ngen;
+        vecBase += nvec;
+        matBase += (int64_t)h.pK.size();
+      }
+      pGen.assign(genBase, 0.0);
+      partVecTot_ = (size_t)vecBase;
+      if (sizeof(double) * ((size_t)d_.partMaxN * std::max(d_.partMaxN, d_.partMaxNx) +
+                            (size_t)d_.partMaxN * d_.partMaxN) > 200 * 1024) {
+        err = "a part's expanded Newton matrix does not fit in shared memory";
+        return -905;
+      }
+      UPV(d_.pModel, int, pModel); UPV(d_.pN, int, pN); UPV(d_.pNtri, int, pNtri); UPV(d_.pNgen, int, pNgen);
+      UPV(d_.pTriOff, int, pTriOff); UPV(d_.pTri, int, pTri); UPV(d_.pTriJoint, int, pTriJoint);
+      UPV(d_.pRef, int, pRef); UPV(d_.pGenFirstDof, int, pGenFirst); UPV(d_.pGenOff, int, pGenOff);
+      UPV(d_.pVecOff, int, pVecOff); UPV(d_.pNx, int, pNx); UPV(d_.pXMatOff, int, pXMat);
+      UPV(d_.pXVecOff, int, pXVec); UPV(d_.pMatOff, int64_t, pMatOff);
+      UPV(d_.pOffset, double, pOffset); UPV(d_.pSupTr, double, pSupTr); UPV(d_.pTriRelSup, double, pRel);
+      UPV(d_.pTrUnd, double, pTrUnd); UPV(d_.pK, double, pK); UPV(d_.pM, double, pM); UPV(d_.pC, double, pC);
+      UPV(d_.pFg, double, pFg); UPV(d_.pStifScl, double, pSs); UPV(d_.pKDmp, double, pKd);
+      UPV(d_.pHasC, uint8_t, pHasC); UPV(d_.pHasVld, uint8_t, pHasVld); UPV(d_.pGen, double, pGen);
+      d_.pFinit = alloc<double>((size_t)std::max<int64_t>(vecBase, 1));
+      d_.pFinitPrev = alloc<double>((size_t)std::max<int64_t>(vecBase, 1));
+      cudaMemsetAsync(d_.pFinit, 0, sizeof(double) * (size_t)std::max<int64_t>(vecBase, 1), stream_);
+      cudaMemsetAsync(d_.pFinitPrev, 0, sizeof(double) * (size_t)std::max<int64_t>(vecBase, 1), stream_);
+      if (preparePartKernels(d_) != 0) { err = "part kernels: shared memory"; return -905; }
+    }
+  }
+  trace.mark("parts", stream_);
   // ---- CSR and gather maps -----------------------------------------------------------
   {
     if (ncontrib >= INT_MAX || 144LL * nel + 36LL * nax >= INT_MAX) {
@@ -1001,6 +1095,18 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     reg(d_.axLen, D * (size_t)d_.naxTot);
     reg(d_.FelA, D * 12 * (size_t)d_.naxTot);
   }
+  if (d_.npartTot > 0) {
+    size_t nv = 0, ng = 0;
+    for (int k = 0; k < nm; ++k)
+      for (int p = 0; p < models[k]->npart; ++p) {
+        nv += 6 * (size_t)models[k]->pNtri[p] + models[k]->pNgen[p];
+        ng += models[k]->pNgen[p];
+      }
+    reg(d_.pSupTr, D * 12 * (size_t)d_.npartTot);
+    reg(d_.pFinit, D * nv);
+    reg(d_.pFinitPrev, D * nv);
+    if (ng) reg(d_.pGen, D * ng);
+  }
   if (d_.njointTot > 0) {
     size_t nv = 0, xv = 0;
     for (int k = 0; k < nm; ++k) {
@@ -1355,6 +1461,9 @@ int Engine::initialState(std::string& err) {
   launchElements(d_, EM_FINAL, stream_);
   FG_CHECK(cudaMemcpyAsync(d_.finitPrev, d_.finit, sizeof(double) * 12 * (size_t)d_.nelTot,
                            cudaMemcpyDeviceToDevice, stream_));
+  if (d_.npartTot > 0)
+    FG_CHECK(cudaMemcpyAsync(d_.pFinitPrev, d_.pFinit, sizeof(double) * partVecTot_, cudaMemcpyDeviceToDevice,
+                             stream_));
   FG_CHECK(cudaMemsetAsync(d_.rinc, 0, sizeof(double) * (size_t)d_.ndofTot, stream_));
   if (d_.urQs) {
     // the state pure linear quasi-static steps restart from

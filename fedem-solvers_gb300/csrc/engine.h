@@ -173,6 +173,7 @@ class Engine {
   cudaEvent_t evRun_[2] = {nullptr, nullptr};
   double lastRunDevSec_ = 0.0;
   long long uploadedBytes_ = 0;
+  size_t partVecTot_ = 0;  // DOF-vector entries of all parts (pFinit, pFinitPrev)
   cudaEvent_t evChunk_ = nullptr;
   bool chunkPending_ = false;
   size_t deviceBytes_ = 0;

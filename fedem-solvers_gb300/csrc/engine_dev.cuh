@@ -178,6 +178,22 @@ struct DevData {
   int ncxTot = 0;
   int *cxEl, *cxNx, *cxMatOff, *cxVecOff, *cxNode;
   double *elMatX, *FelX;
+  // reduced parts (one thread block each): model, DOF count n (6 per triad,
+  // then the generalized DOFs), triad count, generalized DOF count, first entry
+  // of their triads (pTri: triad, pTriJoint: joint whose dependent triad it is
+  // or -1; pTrUnd: 12 per part triad), reference triads (3, local index),
+  // first generalized DOF (global), first generalized value (pGen), offsets of
+  // the DOF vectors (pFinit, pFinitPrev: n apart; pFg: 3 n at 3 * pVecOff) and
+  // of the matrices (pK, pM, pC: n^2 apart), the expanded DOF count and the
+  // expanded matrix and force offsets in elMatX / FelX.  12 per part: frame
+  // pSupTr, pTriRelSup; 9: reference-point offsets.
+  int npartTot = 0, partMaxN = 0, partMaxNx = 0;
+  int *pModel, *pN, *pNtri, *pNgen, *pTriOff, *pTri, *pTriJoint, *pRef, *pGenFirstDof, *pGenOff, *pVecOff, *pNx,
+      *pXMatOff, *pXVecOff;
+  int64_t* pMatOff;
+  double *pOffset, *pSupTr, *pTriRelSup, *pTrUnd, *pK, *pM, *pC, *pFg, *pStifScl, *pKDmp, *pFinit, *pFinitPrev,
+      *pGen;
+  uint8_t *pHasC, *pHasVld;
   // DOF chunks for the two-stage norm reduction (each chunk within one model)
   int nchunkTot = 0;
   int *chunkModel, *chunkStart, *chunkEnd, *modelChunkOff, *modelNchunk;

@@ -10,16 +10,20 @@
 //                      (BEAM31 :11, BELS31 :619, BEAM35 :396), src/Femlib/beamaux.f
 //   offsets/corot init src/vpmSolver/initiateSupElTypeModule.f90:354-371, supElTypeModule.f90:779-992
 //   SAM numbering      src/vpmSolver/samSolverModule.f90:95-250 (triads in input order, MSC = BC)
-//   damping/scaling    src/vpmSolver/initiateSupElTypeModule.f90:549-599, :785-811
+//   damping/scaling    src/vpmSolver/initiateSupElTypeModule.f90:549-599, :740-811
+//   reduced parts      src/vpmSolver/initiateSupElTypeModule.f90:140-700, 962-1033 (ReadSupEls,
+//                      ReadSupElMatrices), samSolverModule.f90:137-148 (generalized DOFs)
 
 #include "host_model.h"
 
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <array>
+#include <climits>
 #include <map>
 
 namespace fgpu {
@@ -119,6 +123,11 @@ struct Rec {
     auto it = r.vals.find(k);
     return (it == r.vals.end() || it->second.empty()) ? std::string() : lowerCase(it->second[0]);
   }
+  // every value as written (file names)
+  std::vector<std::string> strs(const char* k) const {
+    auto it = r.vals.find(k);
+    return it == r.vals.end() ? std::vector<std::string>() : it->second;
+  }
   // the value as written (quotes removed), for names compared case-sensitively
   std::string raw(const char* k) const {
     auto it = r.vals.find(k);
@@ -164,7 +173,48 @@ struct Opts {
     std::string v = lowerCase(it->second);
     return v == "true" || v == "1" || v == "t" || v == "yes" || v == "on";
   }
+  std::string s(const char* k) const {
+    auto it = kv.find(lowerCase(k));
+    return it == kv.end() ? std::string() : it->second;
+  }
 };
+
+// ---------------------------------------------------------------------------
+// Binary matrix files of reduced parts (ReadSupElMatrices,
+// initiateSupElTypeModule.f90:962-1033; readDoubleDBfile,
+// binaryDBInterface.f90:387-435; binaryDB.c:643-731): the file opens with the
+// tag text '#FEDEM <type>', its header ends with the version field ';1.0;\n'
+// and the values follow as raw little-endian doubles, column by column, to the
+// end of the file.  The bytes between the tag text and the version field (an
+// endian mark and checksum in the reference's tag layout) are not read.  A
+// relative name is taken relative to the directory of the model file
+// (-fsifile), else the working directory.
+// ---------------------------------------------------------------------------
+int readMatrixFile(const std::string& name, const std::string& fsiFile, const char* type, size_t nval,
+                   std::vector<double>& out, std::string& err) {
+  std::string path = name;
+  if (!path.empty() && path[0] != '/' && !fsiFile.empty()) {
+    const size_t slash = fsiFile.find_last_of('/');
+    if (slash != std::string::npos) path = fsiFile.substr(0, slash + 1) + path;
+  }
+  FILE* f = path.empty() ? nullptr : std::fopen(path.c_str(), "rb");
+  if (!f) { err = "cannot open the " + std::string(type) + " file '" + path + "'"; return -80; }
+  std::vector<char> buf;
+  char chunk[65536];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  std::fclose(f);
+  const std::string tag = std::string("#FEDEM ") + type, ver = ";1.0;\n";
+  const size_t bytes = 8 * nval;
+  if (buf.size() < tag.size() + ver.size() + bytes || std::memcmp(buf.data(), tag.data(), tag.size()) != 0 ||
+      std::memcmp(buf.data() + buf.size() - bytes - ver.size(), ver.data(), ver.size()) != 0) {
+    err = "'" + path + "' is not a " + type + " file of " + std::to_string(nval) + " values";
+    return -81;
+  }
+  out.resize(nval);
+  std::memcpy(out.data(), buf.data() + buf.size() - bytes, bytes);
+  return 0;
+}
 
 // ---------------------------------------------------------------------------
 // Small dense helpers. P34 is a 3x4 position matrix, column-major (12 doubles).
@@ -824,6 +874,31 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   m.dofDep.assign(m.ndof, -1);
   for (size_t j = 0; j < jin.size(); ++j)
     for (int k = 0; k < 6; ++k) m.dofDep[m.triFirstDof[jin[j].slave] + k] = 6 * (int)j + k;
+  // generalized DOFs of the reduced parts after the triad DOFs, part by part
+  // (initSAM_dofStatus, samSolverModule.f90:137-148, 191-197); status codes
+  // from the part's BC list (default free)
+  auto isPart = [](const Rec& r) {
+    auto f = r.strs("inputfiles");
+    return !f.empty() && !f[0].empty();
+  };
+  for (const NmlRecord& nr : recs) {
+    if (nr.name != "sup_el") continue;
+    Rec r{nr};
+    if (!isPart(r)) continue;
+    const int ng = r.inum("numgendofs", 0);
+    if (ng < 0) { err = "negative numGenDOFs"; return -10; }
+    auto bcg = r.nums("bc");
+    m.pGenFirstDof.push_back(m.ndof);
+    for (int g = 0; g < ng; ++g) {
+      int bc = g < (int)bcg.size() ? (int)std::lround(bcg[g]) : 1;
+      if (bc == 2 && !c.initEquilibrium) bc = 1;
+      if (bc != 0 && bc != 1) { err = "generalized DOF BC other than 0, 1 or 2"; return -30; }
+      m.meqn.push_back(bc == 1 ? m.neq++ : -1);
+      m.dofType.push_back(3);
+      m.dofDep.push_back(-1);
+    }
+    m.ndof += ng;
+  }
   // joint DOFs after all triad DOFs (initSAM_dofStatus, samSolverModule.f90:95-250)
   m.njoint = (int)jin.size();
   for (size_t j = 0; j < jin.size(); ++j) {
@@ -884,9 +959,96 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   std::vector<int> elProp;
   std::map<int, int> elIndex;
   m.qext.assign(m.neq, 0.0);
+  std::map<int, int> partIndex;
+  std::vector<std::array<std::string, 3>> partFiles;
+  std::vector<std::array<double, 4>> partScale;  // stiffScale, massScale, alpha1, alpha2
+  std::vector<std::vector<double>> partA3, partA4;
   for (const NmlRecord& nr : recs) {
     Rec r{nr};
-    if (nr.name == "sup_el") {
+    if (nr.name == "sup_el" && isPart(r)) {
+      // a reduced part (SUP_EL with inputFiles; ReadSupEls, initiateSupElTypeModule.f90:140-700)
+      const int p = m.npart++;
+      partIndex[r.inum("id", 0)] = p;
+      const int nt = r.inum("numtriads", 0), ng = r.inum("numgendofs", 0);
+      auto tids = r.nums("triadids");
+      if (nt < 2 || (int)tids.size() < nt) { err = "a part needs at least two triads"; return -10; }
+      // not on this path: nonlinear parts, part load cases, stress stiffening,
+      // mass-matrix correction, the shadowPosAlg 2 frame, time-dependent scaling
+      if (r.inum("numstates", 0) > 0 || r.inum("numloadcase", 0) > 0) {
+        err = "nonlinear parts and part load cases are not supported";
+        return -10;
+      }
+      for (double v : r.nums("stressstiffflag"))
+        if (v > 0.0) { err = "stress stiffening of parts is not supported"; return -10; }
+      if (r.inum("masscorrflag", -1) > 0) { err = "mass-matrix correction of parts is not supported"; return -10; }
+      if (r.inum("shadowposalg", 0) > 1) { err = "only the triangle frame (shadowPosAlg 1) is supported"; return -10; }
+      if (r.inum("stiffengineid", 0) > 0 || r.inum("strdmpengineid", 0) > 0) {
+        err = "time-dependent part stiffness or damping scaling is not supported";
+        return -10;
+      }
+      m.pNtri.push_back(nt);
+      m.pNgen.push_back(ng);
+      m.pTriOff.push_back((int)m.pTri.size());
+      for (int k = 0; k < nt; ++k) {
+        auto it = triIndex.find((int)std::lround(tids[k]));
+        if (it == triIndex.end()) { err = "part refers to unknown triad"; return -11; }
+        if (m.triNdof[it->second] != 6) { err = "part triads need 6 DOFs"; return -12; }
+        m.pTri.push_back(it->second);
+      }
+      auto sp = r.nums("suppos");
+      double S[12];
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 3; ++row) {
+          size_t k = (size_t)(4 * row + col);
+          S[row + 3 * col] = k < sp.size() ? sp[k] : 0.0;
+        }
+      const char* refKey[3] = {"reftriad1id", "reftriad2id", "reftriad3id"};
+      const char* offKey[3] = {"offset1", "offset2", "offset3"};
+      for (int j = 0; j < 3; ++j) {
+        int rid = r.inum(refKey[j], 0), node = -1;
+        for (int k = 0; k < nt; ++k)
+          if (m.triId[m.pTri[m.pTriOff[p] + k]] == rid) node = k;
+        if (node < 0) { err = "invalid reference triad"; return -13; }
+        m.pRef.push_back(node);
+        // offset in the reference triad's axes (TransformOffset, supElTypeModule.f90:779-789)
+        auto ov = r.nums(offKey[j]);
+        double off[3] = {0, 0, 0}, so[3];
+        for (size_t k = 0; k < 3 && k < ov.size(); ++k) off[k] = ov[k];
+        for (int q = 0; q < 3; ++q) so[q] = S[q] * off[0] + S[q + 3] * off[1] + S[q + 6] * off[2];
+        const double* U = &m.ur[12 * (size_t)m.pTri[m.pTriOff[p] + node]];
+        for (int col = 0; col < 3; ++col)
+          m.pOffset.push_back(so[0] * U[3 * col] + so[1] * U[3 * col + 1] + so[2] * U[3 * col + 2]);
+      }
+      for (double v : S) m.pSupTr.push_back(v);
+      m.pTrUnd.resize(12 * m.pTri.size(), 0.0);
+      auto files = r.strs("inputfiles");
+      std::array<std::string, 3> fl;
+      for (int k = 0; k < 3; ++k) fl[k] = k < (int)files.size() ? files[k] : std::string();
+      partFiles.push_back(fl);
+      partScale.push_back({r.num("stiffscale", 1.0), r.num("massscale", 1.0), r.num("alpha1", 0.0),
+                           r.num("alpha2", 0.0)});
+      auto a3 = r.nums("alpha3"), a4 = r.nums("alpha4");
+      a3.resize(ng, 0.0);
+      a4.resize(ng, 0.0);
+      partA3.push_back(a3);
+      partA4.push_back(a4);
+    } else if (nr.name == "triad_undpos" && partIndex.count(r.inum("supelid", 0))) {
+      const int p = partIndex[r.inum("supelid", 0)], tid = r.inum("triadid", 0);
+      int node = -1;
+      for (int k = 0; k < m.pNtri[p]; ++k)
+        if (m.triId[m.pTri[m.pTriOff[p] + k]] == tid) node = k;
+      if (node < 0) { err = "undeformed position for a triad not on the part"; return -16; }
+      for (const char* key : {"eccvec", "eccmass"})
+        for (double v : r.nums(key))
+          if (std::fabs(v) > 1.0e-16) { err = "eccentricity vectors of part triads are not supported"; return -16; }
+      auto u = r.nums("undposinsupelsystem");
+      double* T = &m.pTrUnd[12 * (size_t)(m.pTriOff[p] + node)];
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 3; ++row) {
+          size_t k = (size_t)(4 * row + col);
+          T[row + 3 * col] = k < u.size() ? u[k] : 0.0;
+        }
+    } else if (nr.name == "sup_el") {
       auto tids = r.nums("triadids");
       if (r.inum("numtriads", 2) != 2 || tids.size() < 2) { err = "only 2-noded beam superelements"; return -10; }
       int e = m.nel++;
@@ -1090,6 +1252,81 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     inverse34(tri, inv);
     compose34(inv, &m.supTr[12 * (size_t)e], &m.triRelSup[12 * (size_t)e]);
   }
+  // reduced parts: matrices from their files, structural damping with the
+  // generalized DOFs' own factors (computeStructDamping,
+  // initiateSupElTypeModule.f90:740-780) on the unscaled matrices, scaling,
+  // corotated frame initialisation
+  const std::string fsiFile = o.s("fsifile");
+  for (int p = 0; p < m.npart; ++p) {
+    const int nt = m.pNtri[p], ng = m.pNgen[p], n = 6 * nt + ng, nd = 6 * nt;
+    const size_t nn = (size_t)n * n;
+    if (n > 96) { err = "parts with more than 96 DOFs (6 per triad + generalized DOFs) are not supported"; return -10; }
+    m.pMatOff.push_back((int64_t)m.pK.size());
+    m.pVecOff.push_back(p == 0 ? 0 : m.pVecOff[p - 1] + 6 * m.pNtri[p - 1] + m.pNgen[p - 1]);
+    m.pGenOff.push_back(p == 0 ? 0 : m.pGenOff[p - 1] + m.pNgen[p - 1]);
+    std::vector<double> K, M, fg(3 * (size_t)n, 0.0), C(nn, 0.0);
+    if (int rc = readMatrixFile(partFiles[p][0], fsiFile, "stiffness matrix", nn, K, err)) return rc;
+    if (int rc = readMatrixFile(partFiles[p][1], fsiFile, "mass matrix", nn, M, err)) return rc;
+    if (!partFiles[p][2].empty())
+      if (int rc = readMatrixFile(partFiles[p][2], fsiFile, "gravity force vectors", 3 * (size_t)n, fg, err)) return rc;
+    const double ss = partScale[p][0], ms = partScale[p][1], a1 = partScale[p][2];
+    double a2 = partScale[p][3];
+    std::vector<double>& a3 = partA3[p];
+    std::vector<double>& a4 = partA4[p];
+    bool any3 = false, any4 = false;
+    for (int g = 0; g < ng; ++g) {
+      any3 = any3 || a3[g] > 0.0;
+      any4 = any4 || a4[g] > 0.0;
+    }
+    for (int g = 0; g < ng; ++g) {
+      if (!any3) a3[g] = a1;
+      if (!any4) a4[g] = a2;
+    }
+    const bool damp = a1 > 0.0 || a2 > 0.0 || any3 || any4;
+    if (damp) {
+      for (size_t k = 0; k < nn; ++k) C[k] = a1 * M[k] + a2 * K[k];
+      for (int g = 0; g < ng; ++g) {
+        const int j = nd + g;
+        const double d3 = a3[g] - a1, d4 = a4[g] - a2;
+        if (std::fabs(d3) > 1.0e-16) {
+          C[j + (size_t)n * j] += d3 * M[j + (size_t)n * j];
+          for (int i = 0; i < nd; ++i) C[i + (size_t)n * j] += d3 * M[i + (size_t)n * j];
+          for (int i = 0; i < nd; ++i) C[j + (size_t)n * i] += d3 * M[j + (size_t)n * i];
+        }
+        if (std::fabs(d4) > 1.0e-16) C[j + (size_t)n * j] += d4 * K[j + (size_t)n * j];
+      }
+    }
+    if (std::fabs(ss - 1.0) > 1.0e-16)
+      for (size_t k = 0; k < nn; ++k) K[k] *= ss;
+    if (std::fabs(ms - 1.0) > 1.0e-16) {
+      for (size_t k = 0; k < nn; ++k) M[k] *= ms;
+      for (double& v : fg) v *= ms;
+    }
+    if (damp && std::fabs(ss - 1.0) > 1.0e-16) a2 /= ss;
+    m.pK.insert(m.pK.end(), K.begin(), K.end());
+    m.pM.insert(m.pM.end(), M.begin(), M.end());
+    m.pC.insert(m.pC.end(), C.begin(), C.end());
+    m.pFg.insert(m.pFg.end(), fg.begin(), fg.end());
+    m.pStifScl.push_back(1.0);
+    m.pKDmp.push_back(a2);
+    m.pHasC.push_back(damp ? 1 : 0);
+    m.pHasVld.push_back((a2 > 0.0 && c.stiffDampFiltering > 0) ? 1 : 0);
+    double pts[3][3];
+    for (int j = 0; j < 3; ++j) {
+      const double* U = &m.ur[12 * (size_t)m.pTri[m.pTriOff[p] + m.pRef[3 * p + j]]];
+      const double* of = &m.pOffset[9 * (size_t)p + 3 * j];
+      for (int q = 0; q < 3; ++q) pts[j][q] = U[q] * of[0] + U[q + 3] * of[1] + U[q + 6] * of[2] + U[q + 9];
+    }
+    double tri[12], inv[12], rel[12];
+    if (frameFrom3Points(pts[0], pts[1], pts[2], tri)) { err = "cannot build a part's corotated frame"; return -22; }
+    inverse34(tri, inv);
+    compose34(inv, &m.pSupTr[12 * (size_t)p], rel);
+    for (double v : rel) m.pTriRelSup.push_back(v);
+  }
+  if (m.npart > 0 && c.tQStatic > c.tStart && c.fixedIt == -1) {
+    err = "parts together with pure linear quasi-static steps are not supported";
+    return -77;
+  }
   // element equation lists
   m.elEq.resize(12 * (size_t)m.nel);
   for (int e = 0; e < m.nel; ++e)
@@ -1126,6 +1363,28 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     m.cxVecSize += 4 * nx;
   }
   m.cxEqOff.push_back((int)m.cxEq.size());
+  // reduced parts in expanded form, after the beam elements above
+  for (int p = 0; p < m.npart; ++p) {
+    m.pXEqOff.push_back((int)m.cxEq.size());
+    for (int k = 0; k < m.pNtri[p]; ++k) {
+      const int t = m.pTri[m.pTriOff[p] + k], dd = m.dofDep[m.triFirstDof[t]];
+      if (dd >= 0) {
+        const int j = dd / 6;
+        for (int col = 0; col < m.jNM[j] + m.jNdof[j]; ++col) m.cxEq.push_back(m.jColEq[12 * j + col]);
+      } else {
+        for (int d = 0; d < 6; ++d) m.cxEq.push_back(m.meqn[m.triFirstDof[t] + d]);
+      }
+    }
+    for (int g = 0; g < m.pNgen[p]; ++g) m.cxEq.push_back(m.meqn[m.pGenFirstDof[p] + g]);
+    const int nx = (int)m.cxEq.size() - m.pXEqOff.back();
+    m.pNx.push_back(nx);
+    m.pXMatOff.push_back(m.cxMatSize);
+    m.pXVecOff.push_back(m.cxVecSize);
+    if ((int64_t)m.cxMatSize + (int64_t)nx * nx >= INT_MAX / 4) { err = "too many part matrix entries"; return -10; }
+    m.cxMatSize += nx * nx;
+    m.cxVecSize += 4 * nx;
+  }
+  m.pXEqOff.push_back((int)m.cxEq.size());
   const int xMatBase = 144 * m.nel + 36 * m.nax, xVecBase = 12 * m.nel + 6 * m.nax;
   // full symmetric CSR pattern (union of element cliques, diagonal always present)
   std::vector<std::vector<int>> rows(m.neq);
@@ -1142,6 +1401,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
     if (c < 0) clique(&m.elEq[12 * e], 12);
     else clique(&m.cxEq[m.cxEqOff[c]], m.cxNx[c]);
   }
+  for (int p = 0; p < m.npart; ++p) clique(&m.cxEq[m.pXEqOff[p]], m.pNx[p]);
   for (int a = 0; a < m.nax; ++a) clique(&m.axEq[6 * a], 6);
   m.rowPtr.assign(m.neq + 1, 0);
   for (int i = 0; i < m.neq; ++i) {
@@ -1165,6 +1425,20 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
         if (q[j] < 0) continue;
         int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
         slotList[slot].push_back(c < 0 ? 144 * e + i + 12 * j : xMatBase + m.cxMatOff[c] + i + n * j);
+      }
+    }
+  }
+  for (int p = 0; p < m.npart; ++p) {
+    const int n = m.pNx[p];
+    const int* q = &m.cxEq[m.pXEqOff[p]];
+    for (int i = 0; i < n; ++i) {
+      if (q[i] < 0) continue;
+      const int* b = &m.colInd[m.rowPtr[q[i]]];
+      const int* en = &m.colInd[0] + m.rowPtr[q[i] + 1];
+      for (int j = 0; j < n; ++j) {
+        if (q[j] < 0) continue;
+        int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
+        slotList[slot].push_back(xMatBase + m.pXMatOff[p] + i + n * j);
       }
     }
   }
@@ -1198,6 +1472,11 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       }
     }
   }
+  for (int p = 0; p < m.npart; ++p)
+    for (int i = 0; i < m.pNx[p]; ++i) {
+      const int q = m.cxEq[m.pXEqOff[p] + i];
+      if (q >= 0) eqList[q].push_back(xVecBase + m.pXVecOff[p] + 4 * i);
+    }
   for (int a = 0; a < m.nax; ++a)
     for (int i = 0; i < 6; ++i)
       if (m.axEq[6 * a + i] >= 0) eqList[m.axEq[6 * a + i]].push_back(12 * m.nel + 6 * a + i);
@@ -1213,6 +1492,15 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       if (q[i] > -2) continue;
       for (int j = 0; j < 12; ++j)
         if (q[j] >= 0) mrList[q[j]].push_back({144 * e + i + 12 * j, -2 - q[i]});
+    }
+  }
+  for (int p = 0; p < m.npart; ++p) {
+    const int n = m.pNx[p];
+    const int* q = &m.cxEq[m.pXEqOff[p]];
+    for (int i = 0; i < n; ++i) {
+      if (q[i] > -2) continue;
+      for (int j = 0; j < n; ++j)
+        if (q[j] >= 0) mrList[q[j]].push_back({xMatBase + m.pXMatOff[p] + i + n * j, -2 - q[i]});
     }
   }
   for (int a = 0; a < m.nax; ++a) {

@@ -123,6 +123,25 @@ struct HostModel {
   std::vector<int> cxEl, cxNx, cxEqOff, cxMatOff, cxVecOff, cxEq;
   std::vector<int> elCx;  // per element: its index in cxEl, or -1
   int cxMatSize = 0, cxVecSize = 0;
+  // reduced parts (superelements whose K, M and gravity force vectors come from
+  // binary matrix files; SupElType with genDOFs): nTri triads with six DOFs and
+  // nGen generalized (component-mode) DOFs each, n = 6 nTri + nGen, matrices
+  // n x n column-major in part axes.  Generalized DOFs follow all triad DOFs,
+  // part by part, and precede the joint DOFs (initSAM_dofStatus).  Per part:
+  // triad count, generalized DOF count, first entry in pTri (its triads), the
+  // three reference triads (local index), first generalized DOF, offsets of its
+  // matrices (n^2 apart), of its DOF vectors (n apart; gravity vectors 3n at
+  // 3 * pVecOff) and of its generalized DOF values (pGenOff).  A part's forces
+  // and Newton matrix reach the gather maps in expanded form, after the beam
+  // elements' in the expanded region: expanded DOFs per triad 6, or its joint's
+  // columns when it is dependent, then the generalized DOFs; pXEqOff into cxEq.
+  int npart = 0;
+  std::vector<int> pNtri, pNgen, pTriOff, pTri, pRef, pGenFirstDof, pGenOff, pVecOff, pXEqOff, pNx, pXMatOff,
+      pXVecOff;
+  std::vector<int64_t> pMatOff;
+  std::vector<double> pOffset, pSupTr, pTriRelSup, pTrUnd;  // 9, 12, 12 per part; 12 per part triad
+  std::vector<double> pK, pM, pC, pFg, pStifScl, pKDmp;
+  std::vector<uint8_t> pHasC, pHasVld;
   // full symmetric CSR pattern of the Newton matrix, equation order
   std::vector<int> rowPtr, colInd;
   // deterministic gather maps: CSR slot <- (element, entry); equation <- (element, local dof)

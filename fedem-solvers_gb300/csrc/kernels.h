@@ -70,6 +70,14 @@ void launchExpandElements(const DevData& d, cudaStream_t s);
 // expanded forces of those elements after an element pass of this mode
 void launchExpandForces(const DevData& d, int mode, cudaStream_t s);
 
+// reduced parts (part_kernels.cu): the element pass, the Newton matrices and
+// the end-of-step copy of the deformation; preparePartKernels sets the shared
+// memory the batch's largest part needs (0, or < 0 on error)
+int preparePartKernels(const DevData& d);
+void launchParts(const DevData& d, int mode, cudaStream_t s);
+void launchPartsNewton(const DevData& d, cudaStream_t s);
+void launchPartsStepEnd(const DevData& d, cudaStream_t s);
+
 // --- front_cascade.cu: one launch per phase over all fronts of all models ----
 struct PersistentPlan {
   const int* leaves;  // fronts without children, longest root path first (factorisation)

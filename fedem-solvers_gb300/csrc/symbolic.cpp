@@ -6,9 +6,10 @@
 // (src/vpmCommon/vpmLinAlg/asmExtensionModule.f90:227-893: SPRPRP, SPRSAS,
 // SPRRNM, SPRTRS, SPRSMB).  SPR's source is not part of the reference tree,
 // so the ordering here is our own, deterministic and documented:
-//   * equations are grouped by triad and by joint (all free DOFs of a triad, or
-//     all free DOFs of a joint, form one node); nodes are adjacent when the
-//     Newton matrix pattern couples them;
+//   * equations are grouped by triad, by part and by joint (all free DOFs of a
+//     triad, the free generalized DOFs of a part, or all free DOFs of a joint,
+//     form one node); nodes are adjacent when the Newton matrix pattern couples
+//     them;
 //   * nested dissection on the node graph: breadth-first level structures
 //     from a pseudo-peripheral node, the separator is the smallest level set
 //     in the middle third; components of at most LEAF_NODES nodes are leaves;
@@ -81,6 +82,7 @@ int symbolicAnalysis(HostModel& m, std::string& err) {
     }
   };
   for (int t = 0; t < m.ntri; ++t) addNode(m.triFirstDof[t], m.triNdof[t]);
+  for (int p = 0; p < m.npart; ++p) addNode(m.pGenFirstDof[p], m.pNgen[p]);  // a part's generalized DOFs
   for (int j = 0; j < m.njoint; ++j) addNode(m.jFirstDof[j], m.jNdof[j]);
   for (int e = 0; e < m.neq; ++e)
     if (eqNode[e] < 0) { err = "equation without a node"; return -43; }

@@ -492,15 +492,16 @@ def part_records(pid, triad_ids, origin, files, n_gen, undpos, R=None, alpha1=0.
            f"  refTriad3Id = {ta}, offset3 = 0.0 {_f(ref_offset)} 0.0\n"
            f"  alpha1 = {_f(alpha1)}\n  alpha2 = {_f(alpha2)}\n"
            f"  supPos = {_rows34(R, origin)}\n/\n"]
+    # a triad in global axes sits in the part axes R with orientation R
     for t, p in zip(triad_ids, undpos):
         out.append(f"&TRIAD_UNDPOS\n  supElId = {pid}\n  triadId = {t}\n"
-                   f"  undPosInSupElSystem = {_rows34(np.eye(3), p)}\n/\n")
+                   f"  undPosInSupElSystem = {_rows34(R, p)}\n/\n")
     return "".join(out)
 
 
 def superelement_chain_c3(directory, n_parts=16, n_modes=30, length=2.0, width=0.2, height=0.2, nx=40, ny=4,
                           nz=4, torque=500.0, freq=2.0, damping=0.01, damping_hz=10.0, steps=4000, dt=5.0e-4,
-                          g=9.81):
+                          g=9.81, axes=None):
     """Superelement chain: `n_parts` steel blocks (length x width x height,
     meshed with nx x ny x nz hexahedra) in series along global X, each reduced
     by the Craig-Bampton reducer to its two end-face triads plus `n_modes`
@@ -512,25 +513,27 @@ def superelement_chain_c3(directory, n_parts=16, n_modes=30, length=2.0, width=0
     the last one pinned (translations fixed).  Gravity -Z; a harmonic torque
     `torque` sin(2 pi freq t) about X at the last triad; Rayleigh damping
     `damping` at `damping_hz`, half mass- and half stiffness-proportional.
-    Returns (fsi, options, info)."""
+    `axes` (3 x 3 rotation, columns) turns the whole chain (not gravity) so
+    that its axis is axes[:, 0].  Returns (fsi, options, info)."""
     from . import reducer
 
     paths, (Kr, Mr, fg, w2) = reducer.block_part_files(directory, length, width, height, nx, ny, nz, n_modes)
     w0 = 2.0 * np.pi * damping_hz
     a1, a2 = damping * w0, damping / w0
     triads, joints, parts = [], [], []
-    rot = np.array([[0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])  # joint Z = global X
+    A = np.eye(3) if axes is None else np.asarray(axes, float)
+    rot = A @ np.array([[0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])  # joint Z = the chain axis
     for k in range(n_parts):
         ta, tb = 1 + 2 * k, 2 + 2 * k
         x0 = k * length
-        triads.append({"id": ta, "pos": (x0, 0.0, 0.0), "bc": [0] * 6 if k == 0 else None})
-        triads.append({"id": tb, "pos": (x0 + length, 0.0, 0.0),
-                       "bc": [0, 0, 0, 1, 1, 1] if k == n_parts - 1 else None})
-        parts.append(part_records(5000 + k, [ta, tb], (x0, 0.0, 0.0), paths, n_modes,
-                                  [(0.0, 0.0, 0.0), (length, 0.0, 0.0)], alpha1=a1, alpha2=a2,
+        pa, pb = A @ np.array([x0, 0.0, 0.0]), A @ np.array([x0 + length, 0.0, 0.0])
+        triads.append({"id": ta, "pos": tuple(pa), "bc": [0] * 6 if k == 0 else None})
+        triads.append({"id": tb, "pos": tuple(pb), "bc": [0, 0, 0, 1, 1, 1] if k == n_parts - 1 else None})
+        parts.append(part_records(5000 + k, [ta, tb], tuple(pa), paths, n_modes,
+                                  [(0.0, 0.0, 0.0), (length, 0.0, 0.0)], R=A, alpha1=a1, alpha2=a2,
                                   ref_offset=length))
         if k > 0:
-            joints.append({"id": 600 + k, "type": 1, "slave": ta, "master": ta - 1, "pos": (x0, 0.0, 0.0),
+            joints.append({"id": 600 + k, "type": 1, "slave": ta, "master": ta - 1, "pos": tuple(pa),
                            "rot": rot, "dofs": [(6, 1)]})
     fsi = frame_fsi(triads, [], [], joints=joints, gravity=(0.0, 0.0, -g), title="superelement chain")
     fsi += "".join(parts)
@@ -539,8 +542,8 @@ def superelement_chain_c3(directory, n_parts=16, n_modes=30, length=2.0, width=0
             f"  realData = {_f(freq)} 0.0 1.0 0.0\n/\n"
             f"&SENSOR\n  id = {eng + 2}\n  type = 'TIME'\n/\n"
             f"&ENGINE\n  id = {eng}\n  functionId = {eng + 1}\n  nArg = 1\n  argSensorId = {eng + 2}\n/\n"
-            f"&LOAD\n  id = 980000\n  triadId = {2 * n_parts}\n  lDof = 4\n  f0 = 0.0\n  f1 = {_f(torque)}\n"
-            f"  loadEngineId = {eng}\n/\n")
+            + "".join(f"&LOAD\n  id = {980000 + c}\n  triadId = {2 * n_parts}\n  lDof = {4 + c}\n  f0 = 0.0\n"
+                      f"  f1 = {_f(torque * A[c, 0])}\n  loadEngineId = {eng}\n/\n" for c in range(3) if A[c, 0] != 0.0))
     opts = ["-timeInc=%r" % dt, "-timeEnd=%r" % (steps * dt), "-alphaNewmark=0.1", "-tolDispNorm=1.0e-8"]
     info = {"Kr": Kr, "Mr": Mr, "fg": fg, "w2": w2, "files": paths, "tip": 2 * n_parts}
     return fsi, opts, info

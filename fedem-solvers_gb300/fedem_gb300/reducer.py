@@ -170,10 +170,13 @@ def craig_bampton_two_faces(K, M, coords, length, n_modes=30):
     Mii = Mq[i][:, i].tocsc()
     lu = sla.splu(Kii)
     Psi = -lu.solve(Kib)
-    w2, Phi = sla.eigsh(Kii, k=n_modes, M=Mii, sigma=0.0, which="LM")
-    order = np.argsort(w2)
-    w2, Phi = w2[order], Phi[:, order]
-    Phi = Phi / np.sqrt(np.einsum("ij,ij->j", Phi, Mii @ Phi))
+    if n_modes > 0:
+        w2, Phi = sla.eigsh(Kii, k=n_modes, M=Mii, sigma=0.0, which="LM")
+        order = np.argsort(w2)
+        w2, Phi = w2[order], Phi[:, order]
+        Phi = Phi / np.sqrt(np.einsum("ij,ij->j", Phi, Mii @ Phi))
+    else:  # static condensation alone (Guyan)
+        w2, Phi = np.zeros(0), np.zeros((n_int, 0))
     Tcb = np.zeros((12 + n_int, 12 + n_modes))
     Tcb[:12, :12] = np.eye(12)
     Tcb[12:, :12] = Psi

@@ -227,3 +227,38 @@ def test_result_changing_options_are_refused(gpu_lib, opt):
         Model(base, ["-timeInc=0.01", opt])
     Model(base, ["-timeInc=0.01", "-cutbackFactor=1.0", "-lineSearch-", "-NewmarkFlag=0",
                  "-tolUpdateFactor=0.0"]).close()
+
+
+def test_part_setup_matches_oracle(gpu_lib, oracle_lib, tmp_path):
+    """Reduced parts (matrix files, generalized DOFs, revolute joints between
+    them): the GPU host set-up numbers the generalized DOFs after the triads
+    and before the joint DOFs as the oracle does, with the same sparsity
+    pattern."""
+    from fedem_gb300 import models
+    from fedem_gb300.batch import Model
+    from oracle.oracle import OracleModel
+
+    fsi, opts, _ = models.superelement_chain_c3(str(tmp_path), n_parts=4, n_modes=8, nx=8, ny=2, nz=2, steps=10)
+    m = Model(fsi, opts)
+    o = OracleModel(fsi, opts)
+    assert (m.ntri, m.ndof, m.neq) == (o.ntri, o.ndof, o.neq)
+    assert np.array_equal(m.meqn(), o.meqn())
+    rp, ci = m.csr_pattern()
+    orp, oci = o.csr_upper_pattern()
+    for i in range(m.neq):
+        r = ci[rp[i]:rp[i + 1]]
+        assert np.array_equal(r[r >= i], oci[orp[i]:orp[i + 1]])
+
+
+def test_part_files_are_checked(gpu_lib, tmp_path):
+    """A missing or mistagged part matrix file fails model creation loudly."""
+    from fedem_gb300 import FedemException, models, reducer
+    from fedem_gb300.batch import Model
+
+    fsi, opts, info = models.superelement_chain_c3(str(tmp_path), n_parts=2, n_modes=4, nx=4, ny=2, nz=2, steps=10)
+    bad = str(tmp_path / "bad_M.fmx")
+    reducer.write_fmx(bad, "stiffness matrix", info["Mr"])
+    with pytest.raises(FedemException, match="mass matrix"):
+        Model(fsi.replace(info["files"]["M"], bad), opts)
+    with pytest.raises(FedemException, match="cannot open"):
+        Model(fsi.replace(info["files"]["K"], str(tmp_path / "none.fmx")), opts)
