@@ -16,7 +16,11 @@ e2e:   the same through the C ABI from host buffers, per step: model set-up
 Also reported: the batched plain FP64 path, the plain per-model FP64 GPU path
 on a sample of models, the mixed path's error against the FP64 path, the CPU
 oracle over the whole workload (cpu_baseline, and every model's final state
-compared with both GPU paths), phase rooflines, clocks, the served leg.
+compared with both GPU paths), phase rooflines, clocks, the served leg, and
+two single-model legs run to their end times in FP64 and mixed precision with
+the oracle beside them (parity of the final state and a one-thread CPU
+baseline): the space-frame tower (2,000 steps) and the superelement chain
+(4,000 steps).
 
 --impl reference: the CPU oracle (restatement of the reference algorithm; the
 reference itself does not build here) on the same workload and boundary: the
@@ -89,8 +93,10 @@ def parse():
     ap.add_argument("--no-oracle", action="store_true", help="skip the full CPU oracle run (parity + cpu_baseline)")
     ap.add_argument("--space-frame-steps", type=int, default=2000, help="time steps of the space-frame tower leg")
     ap.add_argument("--no-space-frame", action="store_true", help="skip the space-frame tower leg")
-    ap.add_argument("--space-frame-only", action="store_true",
-                    help="run only the space-frame tower leg (GPU) and print its JSON")
+    ap.add_argument("--superelement-steps", type=int, default=4000, help="time steps of the superelement chain leg")
+    ap.add_argument("--no-superelements", action="store_true", help="skip the superelement chain leg")
+    ap.add_argument("--single-models-only", action="store_true",
+                    help="run only the single-model legs (space frame, superelement chain) and print their JSON")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
@@ -307,14 +313,12 @@ def factor_flops(model):
     return tot
 
 
-def space_frame_oracle(steps):
-    """The oracle over the space-frame tower, single-threaded, set-up included.
-    Runs in a spawned process beside the GPU legs.  Returns (seconds, Newton
-    iterations, final triad matrices, largest displacement over the run)."""
-    from fedem_gb300 import models
+def single_model_oracle(fsi, opts):
+    """The oracle over one model, single-threaded, set-up included.  Runs in a
+    spawned process beside the GPU legs.  Returns (seconds, Newton iterations,
+    final triad matrices, largest displacement over the run)."""
     from oracle.oracle import OracleModel
 
-    fsi, opts = models.space_frame_c2(steps=steps)
     t0 = time.perf_counter()
     o = OracleModel(fsi, opts)
     o.run_all()
@@ -324,39 +328,62 @@ def space_frame_oracle(steps):
     return out
 
 
-def start_frame_oracle(args):
-    """(pool, pending result) of the space-frame oracle run in a spawned
-    process (a fresh interpreter: safe beside this process's CUDA context), or
-    (None, None) with --no-oracle."""
-    if args.no_oracle:
-        return None, None
+def single_model_workloads(args):
+    """The single-model legs: (key, fsi, options, steps, description).
+    space-frame tower: 12 storeys x 4 x 4 bays, 1,164 pipes, 40 revolute
+    joints, 40 spring/damper pairs, 10 kN at 2 Hz on the top floor, FP64.
+    superelement chain: 16 Craig-Bampton parts (40 x 4 x 4 hexahedra reduced to
+    2 triads + 30 modes, 42 x 42), 15 revolute joints, gravity, 500 N m at
+    2 Hz, Rayleigh 1 % at 10 Hz, dt 0.5 ms; its matrix files are written to a
+    temporary directory first."""
+    import tempfile
+
+    from fedem_gb300 import models
+
+    out = []
+    if not args.no_space_frame:
+        fsi, opts = models.space_frame_c2(steps=args.space_frame_steps)
+        out.append(("space_frame", fsi, opts, args.space_frame_steps,
+                    "space-frame tower, 12 storeys x 4 x 4 bays, 1164 beams, 40 revolute joints, 40 spring/damper "
+                    f"pairs, sinusoidal 10 kN top load at 2 Hz, {args.space_frame_steps} HHT-alpha steps of 1 ms"))
+    if not args.no_superelements:
+        d = tempfile.mkdtemp(prefix="fedem_parts_")
+        fsi, opts, _ = models.superelement_chain_c3(d, steps=args.superelement_steps)
+        out.append(("superelement_chain", fsi, opts, args.superelement_steps,
+                    "superelement chain, 16 parts (2 x 0.2 x 0.2 m steel blocks, 40 x 4 x 4 hexahedra reduced to 2 "
+                    "triads + 30 component modes, 42 x 42 K and M), 15 revolute joints, gravity + 500 N m "
+                    f"harmonic torque at 2 Hz, Rayleigh 1 % at 10 Hz, {args.superelement_steps} HHT-alpha steps "
+                    "of 0.5 ms"))
+    return out
+
+
+def start_single_oracles(args, workloads):
+    """(pool, {key: pending result}) of the oracle runs of the single-model
+    legs, each in its own spawned process (a fresh interpreter: safe beside
+    this process's CUDA context), or (None, {}) with --no-oracle."""
+    if args.no_oracle or not workloads:
+        return None, {}
     import multiprocessing
 
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    pool = multiprocessing.get_context("spawn").Pool(1)
-    return pool, pool.apply_async(space_frame_oracle, (args.space_frame_steps,))
+    pool = multiprocessing.get_context("spawn").Pool(len(workloads))
+    return pool, {key: pool.apply_async(single_model_oracle, (fsi, opts)) for key, fsi, opts, _, _ in workloads}
 
 
-def space_frame_leg(args, pending=None):
-    """The space-frame tower (12 storeys x 4 x 4 bays, 1,164 pipes, 40 revolute
-    joints, 40 spring/damper pairs, 10 kN at 2 Hz on the top floor) through
-    args.space_frame_steps time steps, one model per batch: plain FP64 and
-    mixed precision, device time of a full run after a warm-up run, phase
-    timings, the factorisation against the measured FP64 FMA rate, and, when
+def single_model_leg(fsi, opts, steps, desc, pending=None):
+    """One model per batch through its run: plain FP64 and mixed precision,
+    device time of a full run after a short warm-up run, phase timings, the
+    factorisation (timed alone) against the measured FP64 FMA rate, and, when
     `pending` (the oracle's run in a spawned process) is given, both final
     states against the oracle's and the oracle's time as the CPU baseline."""
     import numpy as np
 
-    from fedem_gb300 import models
     from fedem_gb300.batch import Batch, Model, measure_fp64_peak
 
-    fsi, opts = models.space_frame_c2(steps=args.space_frame_steps)
     m = Model(fsi, opts)
     flops = factor_flops(m)
     peak_tf, _ = measure_fp64_peak()
-    out = {"workload": f"space-frame tower, 12 storeys x 4 x 4 bays, {m.nel} beams, 40 revolute joints, 40 "
-                       f"spring/damper pairs, sinusoidal 10 kN top load at 2 Hz, {args.space_frame_steps} "
-                       f"HHT-alpha steps of 1 ms", "equations": m.neq, "unit": UNIT,
+    out = {"workload": desc, "equations": m.neq, "unit": UNIT,
            "factor_flops_per_factorisation": flops, "fp64_fma_peak_tflops": peak_tf,
            "fp64_peak_source": "measured (fgpu_measure_fp64_peak: 8 FMA chains per thread, 8 blocks per SM)"}
     finals = {}
@@ -372,7 +399,7 @@ def space_frame_leg(args, pending=None):
         finals[key] = b.triads(0).copy()
         its = b.info(0)["iterations"]
         if its != st["newton_iterations"]:
-            raise RuntimeError("space-frame run: iteration counts disagree")
+            raise RuntimeError("single-model run: iteration counts disagree")
         ph = (ms / max(n, 1)).tolist()
         leg = {"value": st["newton_iterations"] / (st["device_us"] * 1e-6),
                "time_steps_per_s": st["time_steps"] / (st["device_us"] * 1e-6),
@@ -390,7 +417,7 @@ def space_frame_leg(args, pending=None):
             achieved = flops / (f_ms * 1e-3) / 1e12
             leg["roofline_factor"] = {"bound": "fp64", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                                       "frac": achieved / peak_tf, "traffic": None,
-                                      "kernel": "kFactorForwardCascade<double> + kLargeFactorForward<double>",
+                                      "kernel": "kFactorForwardCascade<double> (+ kLargeFactorForward<double>)",
                                       "timing": "10 launches after the run, CUDA events on the engine stream"}
         else:
             leg["factor_gflops"] = flops / (f_ms * 1e-3) / 1e9
@@ -405,8 +432,8 @@ def space_frame_leg(args, pending=None):
             "definition": "final triad positions: max |gpu - oracle| / the largest triad displacement over "
                           "the run (oracle)"}
         out["cpu_baseline"] = {"value": c_it / c_dt, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"the full run ({args.space_frame_steps} steps, {c_it} Newton iterations, "
-                                         f"{c_dt:.1f} s), set-up included, one thread"}
+                               "sample": f"the full run ({steps} steps, {c_it} Newton iterations, {c_dt:.1f} s), "
+                                         "set-up included, one thread"}
     m.close()
     return out
 
@@ -509,12 +536,15 @@ def main():
     from fedem_gb300 import models
     from fedem_gb300.batch import Batch, create_models
 
-    want_frame = not args.no_space_frame and rank == 0 and not args.timed_only
+    want_single = rank == 0 and not args.timed_only
     lib = fedem_gb300.load_library()
     dev, bus = rank_device(local, lib)
-    if args.space_frame_only:
-        pool, pending = start_frame_oracle(args)
-        print(json.dumps({"space_frame": space_frame_leg(args, pending)}), flush=True)
+    if args.single_models_only:
+        work = single_model_workloads(args)
+        pool, pending = start_single_oracles(args, work)
+        out = {key: single_model_leg(fsi, opts, steps, desc, pending.get(key))
+               for key, fsi, opts, steps, desc in work}
+        print(json.dumps(out), flush=True)
         if pool is not None:
             pool.close()
         return
@@ -668,15 +698,17 @@ def main():
                                           "sample": f"{len(idx)} of {len(mods)} models run one at a time"}
         extras["speedup_vs_plain"] = value / plain_rate
         extras["speedup_vs_plain_time_steps"] = (tsteps_tot / dev_s_max) / (p_ts / p_s)
-        # the space-frame oracle starts here, after the c4 oracle leg (whose
-        # timing it would otherwise share cores with), and runs beside the GPU legs
-        pool, pending = start_frame_oracle(args) if want_frame else (None, None)
+        # the single-model oracle runs start here, after the batch oracle leg
+        # (whose timing they would otherwise share cores with), and run beside
+        # the GPU legs
+        work = single_model_workloads(args) if want_single else []
+        pool, pending = start_single_oracles(args, work)
         # ---- served: Poisson request stream with continuous batching ----------------------
         extras["served"] = served_leg(args)
-        if want_frame:
-            extras["space_frame"] = space_frame_leg(args, pending)
-            if pool is not None:
-                pool.close()
+        for key, fsi, opts, steps, desc in work:
+            extras[key] = single_model_leg(fsi, opts, steps, desc, pending.get(key))
+        if pool is not None:
+            pool.close()
 
     hbm_peak, peak_kind = measured_peaks()
     roof, roof_el = None, None
