@@ -330,6 +330,7 @@ def single_model_oracle(fsi, opts):
 
 def single_model_workloads(args):
     """The single-model legs: (key, fsi, options, steps, description).
+    cantilever: the reference's plain-method case, 20 beams, 1,000 steps.
     space-frame tower: 12 storeys x 4 x 4 bays, 1,164 pipes, 40 revolute
     joints, 40 spring/damper pairs, 10 kN at 2 Hz on the top floor, FP64.
     superelement chain: 16 Craig-Bampton parts (40 x 4 x 4 hexahedra reduced to
@@ -342,6 +343,10 @@ def single_model_workloads(args):
 
     out = []
     if not args.no_space_frame:
+        fsi, opts = models.cantilever_c1()
+        out.append(("cantilever", fsi, opts, 1000,
+                    "cantilever pipe, 5 m, 20 Euler-Bernoulli beams (120 free DOFs), 1 kN tip step load, 1000 "
+                    "HHT-alpha steps of 1 ms"))
         fsi, opts = models.space_frame_c2(steps=args.space_frame_steps)
         out.append(("space_frame", fsi, opts, args.space_frame_steps,
                     "space-frame tower, 12 storeys x 4 x 4 bays, 1164 beams, 40 revolute joints, 40 spring/damper "

@@ -1532,7 +1532,7 @@ int Engine::run(long long maxBatched, RunStats* stats) {
     float t0 = 0.f, t1 = 0.f, t2 = 0.f;
     if (cudaEventElapsedTime(&t0, ev_[3], ev_[4]) == cudaSuccess &&
         cudaEventElapsedTime(&t1, ev_[0], ev_[1]) == cudaSuccess &&
-        cudaEventElapsedTime(&t2, ev_[1], ev_[2]) == cudaSuccess && *hActiveEl_ > 0) {
+        cudaEventElapsedTime(&t2, ev_[1], ev_[2]) == cudaSuccess && (*hActiveEl_ > 0 || (active > 0 && d_.npartTot > 0))) {
       phaseMs_[0] += t0;
       phaseMs_[1] += t1;
       phaseMs_[2] += t2;
