@@ -149,6 +149,14 @@ def test_fedempy_symbol_set_is_exported(gpu_lib):
                "getBeamForcesFromDisp", "getStrainsFromDisp", "getRelDisp", "getRespVars", "getJointSprCoeff"]
     for name in fedempy:
         assert hasattr(gpu_lib, name), name
+    # with the reference tree at hand, the names fedempy's own source binds
+    ref = "/root/reference/PythonAPI/src/fedempy/solver.py"
+    if os.path.exists(ref):
+        with open(ref) as f:
+            bound = set(re.findall(r"self\._solver\.(\w+)\.restype", f.read()))
+        assert bound, "no bindings found in fedempy's solver.py"
+        missing = sorted(n for n in bound if not hasattr(gpu_lib, n))
+        assert not missing, missing
 
 
 def test_invalid_model_fails_loudly(gpu_lib):
