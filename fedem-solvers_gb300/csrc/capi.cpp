@@ -854,7 +854,7 @@ int fgpu_server_submit(fgpu_server* s, fgpu_model* m, int* id) {
 int fgpu_server_pump(fgpu_server* s) {
   if (!s) return fail(-1, "null server");
   int rc = s->srv.pump();
-  return rc < 0 ? fail(rc, "server pump failed") : rc;
+  return rc < 0 ? fail(rc, ("server pump failed (" + std::to_string(rc) + ")").c_str()) : rc;
 }
 
 int fgpu_server_status(fgpu_server* s, long long* st) {
@@ -863,6 +863,19 @@ int fgpu_server_status(fgpu_server* s, long long* st) {
   st[1] = s->srv.pending();
   st[2] = s->srv.liveEngines();
   st[3] = (long long)s->srv.bytesInUse();
+  return 0;
+}
+
+int fgpu_server_set_max_engines(fgpu_server* s, int n) {
+  if (!s) return fail(-1, "bad argument");
+  s->srv.setMaxEngines(n);
+  return 0;
+}
+
+int fgpu_server_slot_reuse(fgpu_server* s, double share, long long* rebatches) {
+  if (!s) return fail(-1, "bad argument");
+  if (share >= 0.0) s->srv.setSlotReuse(share);
+  if (rebatches) *rebatches = s->srv.rebatches();
   return 0;
 }
 

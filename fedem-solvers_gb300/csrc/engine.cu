@@ -1064,58 +1064,112 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   FG_CHECK(cudaMallocHost(&hActiveEl_, sizeof(long long)));
   for (cudaEvent_t& ev : ev_) FG_CHECK(cudaEventCreate(&ev));
   // mutable state for snapshot/restore (everything a run changes that is read
-  // before it is rewritten)
-  auto reg = [&](void* p, size_t bytes) { mutable_.push_back({p, bytes}); };
+  // before it is rewritten), with the layout of each array's per-model slices
+  {
+    // per model and kind: first object and object count
+    int64_t off[14] = {0};
+    for (auto& r : mRange_) r.assign(nm, {0, 0});
+    for (int k = 0; k < nm; ++k) {
+      const HostModel& h = *models[k];
+      int64_t cnt[14] = {0};
+      cnt[SK_TRIAD] = h.ntri;
+      cnt[SK_DOF] = h.ndof;
+      cnt[SK_EQ] = h.neq;
+      cnt[SK_MODEL] = 1;
+      cnt[SK_ELEM] = h.nel;
+      cnt[SK_AXIAL] = h.nax;
+      cnt[SK_MOTION] = (int64_t)h.motD0.size();
+      cnt[SK_EXT] = h.nExt;
+      cnt[SK_PART] = h.npart;
+      for (int p = 0; p < h.npart; ++p) {
+        cnt[SK_PARTVEC] += 6 * h.pNtri[p] + h.pNgen[p];
+        cnt[SK_PARTGEN] += h.pNgen[p];
+      }
+      cnt[SK_JVAR] = (int64_t)h.jLdof.size();
+      cnt[SK_JOINT] = h.njoint;
+      cnt[SK_XVEC] = h.cxVecSize;
+      for (int q = 0; q < 14; ++q) {
+        mRange_[q][k] = {off[q], cnt[q]};
+        off[q] += cnt[q];
+      }
+    }
+    stride_[SK_ELEM] = nel;
+    stride_[SK_AXIAL] = d_.naxTot;
+  }
   const size_t D = sizeof(double);
-  reg(d_.ur, D * 12 * (size_t)ntri);
-  for (double* p : {d_.urd, d_.urdd, d_.dk, d_.ak, d_.rinc, d_.sinc0, d_.sinc1, d_.sinc2}) reg(p, D * (size_t)ndof);
-  for (double* p : {d_.FSk, d_.FDk, d_.FIk, d_.Qk, d_.FIact, d_.res, d_.del, d_.extRhs}) reg(p, D * (size_t)neq);
-  reg(M.dt, D * nm);
-  reg(d_.supTr, D * 12 * (size_t)nel);
-  reg(d_.finit, D * 12 * (size_t)nel);
-  reg(d_.finitPrev, D * 12 * (size_t)nel);
-  reg(d_.Fel, D * 48 * (size_t)nel);
-  for (double* p : {M.time, M.sacc, M.svel, M.deln, M.staticScale}) reg(p, D * nm);
-  for (double* p : {M.scaleN, M.gravity}) reg(p, D * 3 * nm);
-  reg(M.pc, D * 4 * nm);
-  reg(M.normVal, D * 18 * nm);
-  for (int* p : {M.state, M.flags, M.status, M.iter, M.nSeqNoUpd, M.negPiv, M.staticIter, M.staticNinc,
-                 M.staticDone})
-    reg(p, sizeof(int) * nm);
-  for (long long* p : {M.nStep, M.nIter, M.stepLimit}) reg(p, sizeof(long long) * nm);
-  reg(M.qsCount, sizeof(int) * nm);
-  if (d_.nldTot > 0) reg(d_.qext, D * (size_t)neq);
-  if (d_.nextTot > 0) reg(d_.extVal, D * (size_t)d_.nextTot);
+  auto reg = [&](void* p, size_t elem, int kind, int width, size_t count, const char* tag) {
+    mutable_.push_back({p, elem * (size_t)width * count});
+    stateArrays_.push_back({static_cast<char*>(p), elem, kind, width, tag});
+  };
+  reg(d_.ur, D, SK_TRIAD, 12, ntri, "ur");
+  {
+    double* dofArr[8] = {d_.urd, d_.urdd, d_.dk, d_.ak, d_.rinc, d_.sinc0, d_.sinc1, d_.sinc2};
+    const char* dofTag[8] = {"urd", "urdd", "dk", "ak", "rinc", "sinc0", "sinc1", "sinc2"};
+    for (int q = 0; q < 8; ++q) reg(dofArr[q], D, SK_DOF, 1, ndof, dofTag[q]);
+    double* eqArr[8] = {d_.FSk, d_.FDk, d_.FIk, d_.Qk, d_.FIact, d_.res, d_.del, d_.extRhs};
+    const char* eqTag[8] = {"FSk", "FDk", "FIk", "Qk", "FIact", "res", "del", "extRhs"};
+    for (int q = 0; q < 8; ++q) reg(eqArr[q], D, SK_EQ, 1, neq, eqTag[q]);
+  }
+  reg(M.dt, D, SK_MODEL, 1, nm, "dt");
+  reg(d_.supTr, D, SK_ELEM, 12, nel, "supTr");
+  reg(d_.finit, D, SK_ELEM, 12, nel, "finit");
+  reg(d_.finitPrev, D, SK_ELEM, 12, nel, "finitPrev");
+  reg(d_.Fel, D, SK_ELEM, 48, nel, "Fel");
+  reg(M.time, D, SK_MODEL, 1, nm, "time");
+  reg(M.sacc, D, SK_MODEL, 1, nm, "sacc");
+  reg(M.svel, D, SK_MODEL, 1, nm, "svel");
+  reg(M.deln, D, SK_MODEL, 1, nm, "deln");
+  reg(M.staticScale, D, SK_MODEL, 1, nm, "staticScale");
+  reg(M.scaleN, D, SK_MODEL, 3, nm, "scaleN");
+  reg(M.gravity, D, SK_MODEL, 3, nm, "gravity");
+  reg(M.pc, D, SK_MODEL, 4, nm, "pc");
+  reg(M.normVal, D, SK_MODEL, 18, nm, "normVal");
+  {
+    int* ia[9] = {M.state, M.flags, M.status, M.iter, M.nSeqNoUpd, M.negPiv, M.staticIter, M.staticNinc,
+                  M.staticDone};
+    const char* it[9] = {"state", "flags", "status", "iter", "nSeqNoUpd", "negPiv", "staticIter", "staticNinc",
+                         "staticDone"};
+    for (int q = 0; q < 9; ++q) reg(ia[q], sizeof(int), SK_MODEL, 1, nm, it[q]);
+  }
+  reg(M.nStep, sizeof(long long), SK_MODEL, 1, nm, "nStep");
+  reg(M.nIter, sizeof(long long), SK_MODEL, 1, nm, "nIter");
+  reg(M.stepLimit, sizeof(long long), SK_MODEL, 1, nm, "stepLimit");
+  reg(M.qsCount, sizeof(int), SK_MODEL, 1, nm, "qsCount");
+  if (d_.nldTot > 0) reg(d_.qext, D, SK_EQ, 1, neq, "qext");
+  if (d_.nextTot > 0) reg(d_.extVal, D, SK_EXT, 1, d_.nextTot, "extVal");
   if (d_.nmotTot > 0) {
-    reg(d_.motD, D * (size_t)d_.nmotTot);
-    reg(d_.motCc, D * (size_t)d_.nmotTot);
+    reg(d_.motD, D, SK_MOTION, 1, d_.nmotTot, "motD");
+    reg(d_.motCc, D, SK_MOTION, 1, d_.nmotTot, "motCc");
+  }
+  if (d_.urQs) {  // the state pure linear quasi-static steps restart from
+    reg(d_.urQs, D, SK_TRIAD, 12, ntri, "urQs");
+    reg(d_.supTrQs, D, SK_ELEM, 12, nel, "supTrQs");
+    reg(d_.urdQs, D, SK_DOF, 1, ndof, "urdQs");
+    reg(d_.urddQs, D, SK_DOF, 1, ndof, "urddQs");
   }
   if (d_.naxTot > 0) {
-    reg(d_.axN, D * 3 * (size_t)d_.naxTot);
-    reg(d_.axLen, D * (size_t)d_.naxTot);
-    reg(d_.FelA, D * 12 * (size_t)d_.naxTot);
+    reg(d_.axN, D, SK_AXIAL, 3, d_.naxTot, "axN");
+    reg(d_.axLen, D, SK_AXIAL, 1, d_.naxTot, "axLen");
+    reg(d_.FelA, D, SK_AXIAL, 12, d_.naxTot, "FelA");
   }
   if (d_.npartTot > 0) {
-    size_t nv = 0, ng = 0;
-    for (int k = 0; k < nm; ++k)
-      for (int p = 0; p < models[k]->npart; ++p) {
-        nv += 6 * (size_t)models[k]->pNtri[p] + models[k]->pNgen[p];
-        ng += models[k]->pNgen[p];
-      }
-    reg(d_.pSupTr, D * 12 * (size_t)d_.npartTot);
-    reg(d_.pFinit, D * nv);
-    reg(d_.pFinitPrev, D * nv);
-    if (ng) reg(d_.pGen, D * ng);
+    reg(d_.pSupTr, D, SK_PART, 12, d_.npartTot, "pSupTr");
+    reg(d_.pFinit, D, SK_PARTVEC, 1, partVecTot_, "pFinit");
+    reg(d_.pFinitPrev, D, SK_PARTVEC, 1, partVecTot_, "pFinitPrev");
+    int64_t ng = 0;
+    for (int k = 0; k < nm; ++k) ng += mRange_[SK_PARTGEN][k][1];
+    if (ng) reg(d_.pGen, D, SK_PARTGEN, 1, (size_t)ng, "pGen");
   }
   if (d_.njointTot > 0) {
-    size_t nv = 0, xv = 0;
-    for (int k = 0; k < nm; ++k) {
-      nv += models[k]->jLdof.size();
-      xv += (size_t)models[k]->cxVecSize;
-    }
-    if (nv) reg(d_.jVar, D * nv);
-    reg(d_.jT, D * 72 * (size_t)d_.njointTot);
-    if (xv) reg(d_.FelX, D * xv);
+    int64_t nv = 0;
+    for (int k = 0; k < nm; ++k) nv += mRange_[SK_JVAR][k][1];
+    if (nv) reg(d_.jVar, D, SK_JVAR, 1, (size_t)nv, "jVar");
+    reg(d_.jT, D, SK_JOINT, 72, d_.njointTot, "jT");
+  }
+  {
+    int64_t xv = 0;
+    for (int k = 0; k < nm; ++k) xv += mRange_[SK_XVEC][k][1];
+    if (xv && d_.njointTot > 0) reg(d_.FelX, D, SK_XVEC, 1, (size_t)xv, "FelX");
   }
   uploadedBytes_ = t_putBytes;
   FG_CHECK(cudaStreamSynchronize(stream_));
@@ -1411,6 +1465,103 @@ int Engine::restoreStateFrom(const void* host) {
   }
   invalidateNewtonScales();
   return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -945;
+}
+
+// byte ranges of model m's share of a state array: one contiguous range for
+// the object-major kinds, one per row for the SoA kinds (elements, axial
+// elements: row c holds every object's value c)
+void Engine::modelSlices(const StateArray& a, int m, std::vector<std::pair<size_t, size_t>>& out) const {
+  out.clear();
+  const int64_t first = mRange_[a.kind][m][0], cnt = mRange_[a.kind][m][1];
+  if (cnt == 0) return;
+  if (a.kind == SK_ELEM || a.kind == SK_AXIAL) {
+    const int64_t stride = stride_[a.kind];
+    for (int c = 0; c < a.width; ++c)
+      out.push_back({(size_t)(c * stride + first) * a.elem, (size_t)cnt * a.elem});
+  } else {
+    out.push_back({(size_t)first * a.width * a.elem, (size_t)cnt * a.width * a.elem});
+  }
+}
+
+// A model's state blob: per state array holding a share of the model, its tag
+// (length byte + characters), the byte count (8 bytes) and the bytes of its
+// slices.  The arrays an engine registers depend on its batch (a batch without
+// prescribed motions has no motion state), so the blob names them; a receiving
+// engine takes the arrays it has and leaves the others as set up (the model
+// does not use them: an engine registers every array any of its models uses).
+int Engine::extractModelState(int m, std::vector<char>& out) {
+  if (m < 0 || m >= numModels()) return -1;
+  std::vector<std::pair<size_t, size_t>> sl;
+  out.clear();
+  struct Pending { size_t dst, src, n; char* base; };
+  std::vector<Pending> copies;
+  for (const StateArray& a : stateArrays_) {
+    modelSlices(a, m, sl);
+    uint64_t bytes = 0;
+    for (auto& r : sl) bytes += r.second;
+    if (bytes == 0) continue;
+    out.push_back((char)a.tag.size());
+    out.insert(out.end(), a.tag.begin(), a.tag.end());
+    const char* bp = reinterpret_cast<const char*>(&bytes);
+    out.insert(out.end(), bp, bp + sizeof(bytes));
+    for (auto& r : sl) {
+      copies.push_back({out.size(), r.first, r.second, a.p});
+      out.resize(out.size() + r.second);
+    }
+  }
+  for (auto& c : copies) cudaMemcpyAsync(out.data() + c.dst, c.base + c.src, c.n, cudaMemcpyDeviceToHost, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -946;
+}
+
+int Engine::injectModelState(int m, const std::vector<char>& in) {
+  if (m < 0 || m >= numModels()) return -1;
+  std::vector<std::pair<size_t, size_t>> sl;
+  size_t off = 0;
+  while (off < in.size()) {
+    const size_t tl = (unsigned char)in[off];
+    if (off + 1 + tl + sizeof(uint64_t) > in.size()) return -2;
+    const std::string tag(in.data() + off + 1, tl);
+    uint64_t bytes = 0;
+    std::memcpy(&bytes, in.data() + off + 1 + tl, sizeof(bytes));
+    off += 1 + tl + sizeof(bytes);
+    if (off + bytes > in.size()) return -2;
+    for (const StateArray& a : stateArrays_) {
+      if (a.tag != tag) continue;
+      modelSlices(a, m, sl);
+      uint64_t have = 0;
+      for (auto& r : sl) have += r.second;
+      if (have != bytes) return -2;  // a different model
+      size_t o = off;
+      for (auto& r : sl) {
+        cudaMemcpyAsync(a.p + r.first, in.data() + o, r.second, cudaMemcpyHostToDevice, stream_);
+        o += r.second;
+      }
+    }
+    off += bytes;
+  }
+  // this engine's element Newton matrices were not built with the scales the
+  // state records: rebuilt at the model's next tangent; no step limit
+  const double bad[3] = {-1.0, -1.0, -1.0};
+  const long long lim = LLONG_MAX;
+  cudaMemcpyAsync(d_.m.scaleN + 3 * m, bad, sizeof(bad), cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.stepLimit + m, &lim, sizeof(lim), cudaMemcpyHostToDevice, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -947;
+}
+
+int Engine::parkModels(const std::vector<int>& ms) {
+  const int nm = numModels();
+  std::vector<int> st(nm);
+  std::vector<long long> steps(nm), lim(nm);
+  cudaMemcpyAsync(st.data(), d_.m.state, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(steps.data(), d_.m.nStep, sizeof(long long) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(lim.data(), d_.m.stepLimit, sizeof(long long) * nm, cudaMemcpyDeviceToHost, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -948;
+  for (int m : ms) {
+    if (m < 0 || m >= nm) return -1;
+    lim[m] = steps[m] + (st[m] == ST_ITER ? 1 : 0);
+  }
+  cudaMemcpyAsync(d_.m.stepLimit, lim.data(), sizeof(long long) * nm, cudaMemcpyHostToDevice, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -949;
 }
 
 void Engine::enqueueIteration(cudaStream_t s) {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <array>
 #include <vector>
 
 #include "engine_dev.cuh"
@@ -106,6 +107,16 @@ class Engine {
   size_t stateBytes() const;
   int saveStateTo(void* host);
   int restoreStateFrom(const void* host);
+  // One model's share of the mutable state (its slices of every state array):
+  // a model built from the same host model in another engine takes it and
+  // continues from there bitwise as it would have here (continuous batching
+  // moves running models into a new engine with it).  Only between steps.
+  int extractModelState(int m, std::vector<char>& out);
+  int injectModelState(int m, const std::vector<char>& in);
+  // The models in `ms` stop at the end of their current step (a model between
+  // steps at once): their step limit becomes the current step count (+ 1 when a
+  // step is in progress).  Blocking.
+  int parkModels(const std::vector<int>& ms);
   // Saves / restores the mutable device state (device-to-device copies), so a
   // timed run can start again from the initial state already resident in HBM.
   int snapshot();
@@ -155,6 +166,21 @@ class Engine {
   bool allocFailed_ = false;
   // snapshot of mutable arrays: (device pointer, bytes) and the backup buffer
   std::vector<std::pair<void*, size_t>> mutable_;
+  // the same arrays with the layout their per-model slices follow
+  enum StateKind : int { SK_TRIAD, SK_DOF, SK_EQ, SK_MODEL, SK_ELEM, SK_AXIAL, SK_MOTION, SK_EXT, SK_PART,
+                         SK_PARTVEC, SK_PARTGEN, SK_JVAR, SK_JOINT, SK_XVEC };
+  struct StateArray {
+    char* p;
+    size_t elem;  // bytes of one value
+    int kind;
+    int width;    // values per object (per model for SK_MODEL; rows for the SoA kinds)
+    std::string tag;  // names the array in a model's state blob
+  };
+  std::vector<StateArray> stateArrays_;
+  // per model and kind: first object and object count (SK_MODEL: the model itself)
+  std::vector<std::array<int64_t, 2>> mRange_[14];
+  int64_t stride_[14] = {0};  // objects per SoA row (elements, axial elements)
+  void modelSlices(const StateArray& a, int m, std::vector<std::pair<size_t, size_t>>& out) const;
   std::vector<double> scaleSentinel_;
   std::vector<int> modelExtOff_, modelExtCnt_;
   std::vector<int> savedFlags_;

@@ -37,8 +37,28 @@ int Server::submit(const HostModel* m) {
   return (int)reqs_.size() - 1;
 }
 
+// Uploads the models of `ids` into a new engine for job j, computes their
+// initial state, and puts the carried state of the first carried->size() of
+// them back (models moved from another engine, between steps).
+int Server::startEngine(Job& j, const std::vector<int>& ids, const std::vector<std::vector<char>>* carried) {
+  j.engine = std::make_unique<Engine>();
+  std::vector<const HostModel*> ms;
+  for (int id : ids) ms.push_back(reqs_[id].model);
+  std::string err;
+  int rc = j.engine->upload(ms, opt_, err);
+  if (!rc) rc = j.engine->initialState(err);
+  if (!rc && carried)
+    for (size_t k = 0; k < carried->size() && !rc; ++k) rc = j.engine->injectModelState((int)k, (*carried)[k]);
+  if (rc) return rc;
+  j.ids = ids;
+  j.bytes = j.engine->deviceBytes();
+  j.parking = false;
+  return 0;
+}
+
 int Server::admit() {
   if (pending_.empty()) return 0;
+  if (maxEngines_ > 0 && (int)jobs_.size() >= maxEngines_) return 0;
   // batching window: wait for a few requests unless the device is idle
   bool idle = jobs_.empty();
   double waited = now() - reqs_[pending_.front()].arrival;
@@ -55,24 +75,65 @@ int Server::admit() {
   }
   if (take.empty()) return 0;
   Job j;
-  j.engine = std::make_unique<Engine>();
-  std::vector<const HostModel*> ms;
-  for (int id : take) ms.push_back(reqs_[id].model);
-  std::string err;
-  int rc = j.engine->upload(ms, opt_, err);
-  if (!rc) rc = j.engine->initialState(err);
-  double t = now();
+  const int rc = startEngine(j, take, nullptr);
+  const double t = now();
   if (rc) {
     for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
     return rc;
   }
   for (int id : take) { reqs_[id].state = 1; reqs_[id].admitted = t; }
-  j.ids = take;
-  j.bytes = j.engine->deviceBytes();
   inUse_ += j.bytes;
   if (j.engine->launchChunk(chunk_)) return -950;
   jobs_.push_back(std::move(j));
   return 1;
+}
+
+// Moves the running models of job k (all stopped between steps) into a new
+// engine together with the waiting requests that fit the memory the old engine
+// frees, and replaces the job.  Returns the number of requests admitted.
+int Server::rebatch(size_t k) {
+  Job& old = jobs_[k];
+  std::vector<int> keep;
+  std::vector<std::vector<char>> carried;
+  for (size_t q = 0; q < old.ids.size(); ++q) {
+    const int id = old.ids[q];
+    if (reqs_[id].state != 1) continue;
+    carried.emplace_back();
+    if (old.engine->extractModelState((int)q, carried.back())) return -954;
+    keep.push_back(id);
+  }
+  size_t bytes = 0;
+  for (int id : keep) bytes += estimateBytes(*reqs_[id].model, opt_);
+  std::vector<int> take = keep;
+  int added = 0;
+  while (!pending_.empty() && (int)take.size() < maxModels_) {
+    const int id = pending_.front();
+    const size_t b = estimateBytes(*reqs_[id].model, opt_);
+    if (inUse_ - old.bytes + bytes + b > budget_) break;
+    take.push_back(id);
+    bytes += b;
+    pending_.pop_front();
+    ++added;
+  }
+  inUse_ -= old.bytes;
+  old.engine.reset();  // the device memory of the old engine goes first
+  Job j;
+  const int rc = startEngine(j, take, &carried);
+  const double t = now();
+  if (rc) {
+    for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
+    jobs_.erase(jobs_.begin() + (long)k);
+    return rc;
+  }
+  for (size_t q = keep.size(); q < take.size(); ++q) {
+    reqs_[take[q]].state = 1;
+    reqs_[take[q]].admitted = t;
+  }
+  inUse_ += j.bytes;
+  ++rebatches_;
+  if (j.engine->launchChunk(chunk_)) return -950;
+  jobs_[k] = std::move(j);
+  return added;
 }
 
 // Completes the requests of a job whose models reached their end time (or
@@ -103,18 +164,42 @@ int Server::pump() {
   int finished = 0;
   // collect finished requests and engines, keep the others fed
   for (size_t k = 0; k < jobs_.size();) {
+    Job& j = jobs_[k];
     bool ready = false;
     int active = 1;
-    if (jobs_[k].engine->pollChunk(&ready, &active)) return -951;
+    if (j.engine->pollChunk(&ready, &active)) return -951;
+    if (ready && active == 0 && j.parking) {
+      // every running model stopped between steps: move them (and waiting requests)
+      finished += collect(j, false);
+      bool running = false;
+      for (int id : j.ids) running |= reqs_[id].state == 1;
+      if (running) {
+        const int a = rebatch(k);
+        if (a < 0) return a;
+        ++k;
+        continue;
+      }
+    }
     if (ready && active == 0) {
-      finished += collect(jobs_[k], true);
-      inUse_ -= jobs_[k].bytes;
+      finished += collect(j, true);
+      inUse_ -= j.bytes;
       jobs_.erase(jobs_.begin() + (long)k);
       continue;
     }
     if (ready) {
-      finished += collect(jobs_[k], false);
-      if (jobs_[k].engine->launchChunk(chunk_)) return -952;
+      finished += collect(j, false);
+      // slot reuse: enough of this engine's models finished and requests wait
+      if (!j.parking && reuseShare_ > 0.0 && !pending_.empty()) {
+        std::vector<int> running;
+        for (size_t q = 0; q < j.ids.size(); ++q)
+          if (reqs_[j.ids[q]].state == 1) running.push_back((int)q);
+        const size_t done = j.ids.size() - running.size();
+        if (!running.empty() && (double)done >= reuseShare_ * (double)j.ids.size()) {
+          if (j.engine->parkModels(running)) return -955;
+          j.parking = true;
+        }
+      }
+      if (j.engine->launchChunk(chunk_)) return -952;
     }
     ++k;
   }

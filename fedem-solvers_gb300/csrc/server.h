@@ -6,8 +6,12 @@
 // arrive while others run overlaps on the device.  Each request keeps its
 // state resident until it reaches its end time, when it is completed (results
 // and finish time) at the next chunk boundary although the other models of
-// its engine go on; finished engines release their memory for the next
-// admissions.
+// its engine go on.  Slots of finished requests are reused: when an engine
+// has finished a set share of its models and requests are waiting, its
+// running models stop at the end of their current step, their state moves
+// into a new engine together with the waiting requests that fit, and they
+// continue there exactly as they would have (the old engine's memory, finished
+// slots included, is released).  Finished engines release their memory.
 #pragma once
 
 #include <chrono>
@@ -48,10 +52,13 @@ class Server {
     std::unique_ptr<Engine> engine;
     std::vector<int> ids;
     size_t bytes = 0;
+    bool parking = false;  // running models stop at their next step end for a move
   };
   static size_t estimateBytes(const HostModel& m, const EngineOptions& opt);
   int admit();
   int collect(Job& j, bool all);
+  int startEngine(Job& j, const std::vector<int>& ids, const std::vector<std::vector<char>>* carried);
+  int rebatch(size_t k);
 
   size_t budget_, inUse_ = 0;
   int device_ = 0;
@@ -65,6 +72,15 @@ class Server {
     minBatch_ = minBatch > 0 ? minBatch : 1;
     maxWait_ = maxWaitSec;
   }
+  // Share of an engine's models that must have finished before its slots are
+  // reused for waiting requests (0: never; engines then end as a whole).
+  void setSlotReuse(double share) { reuseShare_ = share; }
+  // At most this many engines at a time (0: as many as memory allows).
+  void setMaxEngines(int n) { maxEngines_ = n > 0 ? n : 0; }
+  int maxEngines_ = 0;
+  long long rebatches() const { return rebatches_; }
+  double reuseShare_ = 0.25;
+  long long rebatches_ = 0;
   std::vector<Request> reqs_;
   std::deque<int> pending_;
   std::vector<Job> jobs_;

@@ -91,6 +91,8 @@ def load_library(path=None):
         "fgpu_server_pump": (c_int, [vp]),
         "fgpu_server_status": (c_int, [vp, P(c_ll)]),
         "fgpu_server_now": (c_dbl, [vp]),
+        "fgpu_server_slot_reuse": (c_int, [vp, c_dbl, P(c_ll)]),
+        "fgpu_server_set_max_engines": (c_int, [vp, c_int]),
         "fgpu_server_request": (c_int, [vp, c_int, P(c_int), P(c_dbl), P(c_ll), P(c_ll)]),
         "fgpu_server_result": (c_int, [vp, c_int, P(c_dbl)]),
         "fgpu_set_device": (c_int, [c_int]),

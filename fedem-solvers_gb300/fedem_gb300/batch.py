@@ -256,6 +256,18 @@ class Server:
     def now(self):
         return self._lib.fgpu_server_now(self._h)
 
+    def set_max_engines(self, n):
+        """At most n engines (GPU batches) run at a time (0: as memory allows)."""
+        self._lib.fgpu_server_set_max_engines(self._h, int(n))
+
+    def slot_reuse(self, share=-1.0):
+        """Sets the share of an engine's models that must have finished before
+        its running models move into a new engine with waiting requests (0:
+        never; < 0: unchanged); returns the number of such moves so far."""
+        n = ctypes.c_longlong(0)
+        self._lib.fgpu_server_slot_reuse(self._h, float(share), ctypes.byref(n))
+        return n.value
+
     def status(self):
         s = np.zeros(4, dtype=np.int64)
         self._lib.fgpu_server_status(self._h, _ptr(s, ctypes.c_longlong))

@@ -157,6 +157,15 @@ int fgpu_server_submit(fgpu_server* s, fgpu_model* m, int* request_id);
 int fgpu_server_pump(fgpu_server* s);
 /* counts: requests, pending, live batches; bytes in use */
 int fgpu_server_status(fgpu_server* s, long long* status4);
+/* Slot reuse: when this share (0..1) of an engine's models has finished and
+ * requests wait, the engine's running models stop at the end of their current
+ * step and move, with their whole state, into a new engine together with the
+ * waiting requests that fit the freed memory; they continue there exactly as
+ * they would have.  share < 0 leaves the setting (default 0.25), 0 disables
+ * it.  *rebatches: engines rebuilt this way so far. */
+int fgpu_server_slot_reuse(fgpu_server* s, double share, long long* rebatches);
+/* At most n engines run at a time (n <= 0: as many as the memory budget allows). */
+int fgpu_server_set_max_engines(fgpu_server* s, int n);
 double fgpu_server_now(fgpu_server* s);
 /* per request: state (0 pending, 1 running, 2 done, 3 failed), arrival, admitted,
  * finished times, Newton iterations, time steps */
