@@ -101,6 +101,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
+    ap.add_argument("--serve-slot-reuse", type=float, default=0.25,
+                    help="share of an engine's models finished before its slots are reused (0: never)")
     return ap.parse_args()
 
 
@@ -258,45 +260,70 @@ def rel_disp_error(a, c, x0, scale=None):
 
 
 def served_leg(args):
-    """Poisson request stream served with continuous batching; p50/p99 latency."""
+    """Poisson request stream served with continuous batching and slot reuse;
+    p50/p99 latency from each request's arrival (its model set-up from the
+    text on the host threads included) to its completion, throughput, and the
+    same requests run as one batch for comparison."""
     import numpy as np
 
     from fedem_gb300 import models
-    from fedem_gb300.batch import Model, Server
+    from fedem_gb300.batch import Batch, Model, Server
 
     pool = models.served_pool_c5(args.serve_pool, seed=5, steps_scale=args.serve_steps_scale)
-    mods = [Model(f, o) for f, o, _, _ in pool]
     rng = np.random.default_rng(55)
     n_req = max(1, int(round(args.serve_rate * args.serve_seconds)))
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n_req))
-    pick = rng.integers(0, len(mods), n_req)
+    pick = rng.integers(0, len(pool), n_req)
     srv = Server(budget_bytes=120e9, mixed=True, sweeps=args.sweeps, min_batch=8, max_wait=0.02)
+    srv.slot_reuse(args.serve_slot_reuse)
+    setup = ThreadPoolExecutor(max_workers=os.cpu_count() or 1)
     t0 = srv.now()
-    ids, k, overlap = [], 0, 0
+    futs, ids, k, overlap = [], [], 0, 0
+    kept = []
     while True:
         now = srv.now() - t0
         while k < n_req and arrivals[k] <= now:
-            ids.append(srv.submit(mods[pick[k]]))
+            f, o, _, _ = pool[pick[k]]
+            futs.append((k, setup.submit(Model, f, o)))
             k += 1
+        # requests whose set-up finished are submitted in arrival order
+        while futs and futs[0][1].done():
+            q, fut = futs.pop(0)
+            m = fut.result()
+            kept.append(m)
+            ids.append(srv.submit(m))
         srv.pump()
         st = srv.status()
         overlap = max(overlap, st["live_batches"])
-        if k == n_req and st["pending"] == 0 and st["live_batches"] == 0:
+        if k == n_req and not futs and st["pending"] == 0 and st["live_batches"] == 0:
             break
+    setup.shutdown()
     recs = [srv.request(i) for i in ids]
-    # latency from the scheduled arrival (a request submitted late, behind a
-    # blocking admission, still counts from when it arrived)
+    # latency from the scheduled arrival (set-up and any wait for admission included)
     lat = np.array([r["finished"] - (t0 + a) for r, a in zip(recs, arrivals)])
     its = sum(r["iterations"] for r in recs)
     span = max(r["finished"] for r in recs) - t0
     failed = sum(1 for r in recs if r["state"] != 2)
+    rebatches = srv.slot_reuse()
     srv.close()
-    return {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-            "throughput": its / span, "unit": UNIT, "requests": n_req, "failed": failed,
-            "arrival_rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
-            "max_concurrent_batches": overlap,
-            "pool": f"{len(mods)} models, 1k-200k DOF log-uniform, 100-2000 steps log-uniform x "
-                    f"{args.serve_steps_scale}"}
+    out = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+           "throughput": its / span, "unit": UNIT, "requests": n_req, "failed": failed,
+           "arrival_rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
+           "max_concurrent_batches": overlap, "slot_reuse_share": args.serve_slot_reuse,
+           "engines_rebuilt_for_slot_reuse": rebatches,
+           "latency_definition": "scheduled Poisson arrival -> completion; the request's model set-up from its "
+                                 "text (host threads) and any wait for admission included",
+           "pool": f"{len(pool)} models, 1k-200k DOF log-uniform, 100-2000 steps log-uniform x "
+                   f"{args.serve_steps_scale}"}
+    # the same requests as one batch (all present at once): device throughput
+    b = Batch(kept, mixed=True, sweeps=args.sweeps)
+    st = b.run()
+    out["batched_same_requests"] = {"value": st["newton_iterations"] / (st["device_us"] * 1e-6), "unit": UNIT,
+                                    "note": "the served requests' models in one batch, device time"}
+    b.close()
+    for m in kept:
+        m.close()
+    return out
 
 
 def factor_flops(model):
