@@ -259,11 +259,13 @@ def rel_disp_error(a, c, x0, scale=None):
     return float(np.abs(a - c).max()) / denom
 
 
-def served_leg(args):
-    """Poisson request stream served with continuous batching and slot reuse;
-    p50/p99 latency from each request's arrival (its model set-up from the
-    text on the host threads included) to its completion, throughput, and the
-    same requests run as one batch for comparison."""
+def served_leg(args, share, compare_batched=True):
+    """Poisson request stream served with continuous batching (slot reuse at
+    `share`); p50/p99 latency from each request's arrival to its completion,
+    throughput, and the same requests run as one batch for comparison.  A
+    request's model set-up from its text (host threads) is inside its latency;
+    requests for a model text already set up reuse it (the pool repeats
+    models), as a service keeps the set-up of the models it has seen."""
     import numpy as np
 
     from fedem_gb300 import models
@@ -275,29 +277,38 @@ def served_leg(args):
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n_req))
     pick = rng.integers(0, len(pool), n_req)
     srv = Server(budget_bytes=120e9, mixed=True, sweeps=args.sweeps, min_batch=8, max_wait=0.02)
-    srv.slot_reuse(args.serve_slot_reuse)
+    srv.slot_reuse(share)
     setup = ThreadPoolExecutor(max_workers=os.cpu_count() or 1)
     t0 = srv.now()
-    futs, ids, k, overlap = [], [], 0, 0
+    futs, ids, k, overlap = [], {}, 0, 0
+    cache = {}  # pool index -> model set-up (future)
     kept = []
     while True:
         now = srv.now() - t0
         while k < n_req and arrivals[k] <= now:
-            f, o, _, _ = pool[pick[k]]
-            futs.append((k, setup.submit(Model, f, o)))
+            q = int(pick[k])
+            if q not in cache:
+                f, o, _, _ = pool[q]
+                cache[q] = setup.submit(Model, f, o)
+            futs.append((k, cache[q]))
             k += 1
-        # requests whose set-up finished are submitted in arrival order
-        while futs and futs[0][1].done():
-            q, fut = futs.pop(0)
-            m = fut.result()
-            kept.append(m)
-            ids.append(srv.submit(m))
+        # requests whose model is set up are submitted
+        rest = []
+        for q, fut in futs:
+            if fut.done():
+                m = fut.result()
+                kept.append(m)
+                ids[q] = srv.submit(m)
+            else:
+                rest.append((q, fut))
+        futs = rest
         srv.pump()
         st = srv.status()
         overlap = max(overlap, st["live_batches"])
         if k == n_req and not futs and st["pending"] == 0 and st["live_batches"] == 0:
             break
     setup.shutdown()
+    ids = [ids[q] for q in range(n_req)]
     recs = [srv.request(i) for i in ids]
     # latency from the scheduled arrival (set-up and any wait for admission included)
     lat = np.array([r["finished"] - (t0 + a) for r, a in zip(recs, arrivals)])
@@ -309,20 +320,21 @@ def served_leg(args):
     out = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
            "throughput": its / span, "unit": UNIT, "requests": n_req, "failed": failed,
            "arrival_rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
-           "max_concurrent_batches": overlap, "slot_reuse_share": args.serve_slot_reuse,
-           "engines_rebuilt_for_slot_reuse": rebatches,
+           "max_concurrent_batches": overlap, "slot_reuse_share": share,
+           "engines_rebuilt_for_slot_reuse": rebatches, "distinct_models_set_up": len(cache),
            "latency_definition": "scheduled Poisson arrival -> completion; the request's model set-up from its "
                                  "text (host threads) and any wait for admission included",
            "pool": f"{len(pool)} models, 1k-200k DOF log-uniform, 100-2000 steps log-uniform x "
                    f"{args.serve_steps_scale}"}
-    # the same requests as one batch (all present at once): device throughput
-    b = Batch(kept, mixed=True, sweeps=args.sweeps)
-    st = b.run()
-    out["batched_same_requests"] = {"value": st["newton_iterations"] / (st["device_us"] * 1e-6), "unit": UNIT,
-                                    "note": "the served requests' models in one batch, device time"}
-    b.close()
-    for m in kept:
-        m.close()
+    if compare_batched:
+        # the same requests as one batch (all present at once): device throughput
+        b = Batch(kept, mixed=True, sweeps=args.sweeps)
+        st = b.run()
+        out["batched_same_requests"] = {"value": st["newton_iterations"] / (st["device_us"] * 1e-6),
+                                        "unit": UNIT, "note": "the served requests' models in one batch, device time"}
+        b.close()
+    for f in cache.values():
+        f.result().close()
     return out
 
 
@@ -736,7 +748,8 @@ def main():
         work = single_model_workloads(args) if want_single else []
         pool, pending = start_single_oracles(args, work)
         # ---- served: Poisson request stream with continuous batching ----------------------
-        extras["served"] = served_leg(args)
+        extras["served"] = served_leg(args, args.serve_slot_reuse)
+        extras["served_without_slot_reuse"] = served_leg(args, 0.0, compare_batched=False)
         for key, fsi, opts, steps, desc in work:
             extras[key] = single_model_leg(fsi, opts, steps, desc, pending.get(key))
         if pool is not None:
