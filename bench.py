@@ -95,6 +95,7 @@ def parse():
     ap.add_argument("--no-space-frame", action="store_true", help="skip the space-frame tower leg")
     ap.add_argument("--superelement-steps", type=int, default=4000, help="time steps of the superelement chain leg")
     ap.add_argument("--no-superelements", action="store_true", help="skip the superelement chain leg")
+    ap.add_argument("--no-cantilever", action="store_true", help="skip the cantilever leg")
     ap.add_argument("--single-models-only", action="store_true",
                     help="run only the single-model legs (space frame, superelement chain) and print their JSON")
     ap.add_argument("--serve-rate", type=float, default=200.0)
@@ -381,11 +382,12 @@ def single_model_workloads(args):
     from fedem_gb300 import models
 
     out = []
-    if not args.no_space_frame:
+    if not args.no_cantilever:
         fsi, opts = models.cantilever_c1()
         out.append(("cantilever", fsi, opts, 1000,
                     "cantilever pipe, 5 m, 20 Euler-Bernoulli beams (120 free DOFs), 1 kN tip step load, 1000 "
                     "HHT-alpha steps of 1 ms"))
+    if not args.no_space_frame:
         fsi, opts = models.space_frame_c2(steps=args.space_frame_steps)
         out.append(("space_frame", fsi, opts, args.space_frame_steps,
                     "space-frame tower, 12 storeys x 4 x 4 bays, 1164 beams, 40 revolute joints, 40 spring/damper "

@@ -20,7 +20,8 @@
 // pivots: each panel is factored in shared memory (its diagonal block by one
 // warp, the rows below it one per thread, no barrier inside), then the
 // trailing lower triangle is updated with it, C -= L_p D_p L_p^T, in 64 x 64
-// tiles with 4 x 4 register blocks, the tiles shared out over the blocks of a
+// tiles (FP32 fronts: mma.sync TF32 products on the tensor cores in the 3xTF32
+// split; FP64 fronts: 4 x 4 register blocks), the tiles shared out over the blocks of a
 // thread-block cluster (GB300's FP64 units are thin: one front's update on one
 // SM would set the pace).  Semantics as the warp kernels and the reference's
 // SPRFC1/SPRFS1/SPRBS1 seam (solExtensionModule.f90:153-505): no pivoting, a
@@ -31,6 +32,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.h"
 
@@ -75,6 +77,66 @@ __device__ inline void st(T* p, T v) {
 __device__ inline void clusterBarrier() {
   __threadfence();
   cg::this_cluster().sync();
+}
+
+// ---- FP32 trailing tiles on the tensor cores --------------------------------
+// C(64 x 64 tile) -= A B with A(m, k) = P(r0 + m, k) and B(k, n) = P(c0 + n, k) d_k
+// (k < kb <= 32, zero beyond kb), as mma.sync m16n8k8 TF32 products with FP32
+// accumulation in the 3xTF32 split (x = hi + lo, both TF32; a b = hi hi + hi lo
+// + lo hi), which keeps the FP32 accuracy of the update.  Warp w takes rows
+// 16 (w & 3) .. +15 and columns 32 (w >> 2) .. +31 of the tile (four 16 x 8
+// products); fragment layouts of m16n8k8.row.col: lane = 4 g + t holds
+// A(g, t), A(g + 8, t), A(g, t + 4), A(g + 8, t + 4); B(t, g), B(t + 4, g);
+// C(g, 2t), C(g, 2t + 1), C(g + 8, 2t), C(g + 8, 2t + 1).
+__device__ inline uint32_t tf32Of(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ inline void split3(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32Of(x);
+  lo = tf32Of(x - __uint_as_float(hi));
+}
+
+__device__ inline void mmaTf32(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// acc[j][q]: this thread's C fragment of the warp's j-th 16 x 8 product
+__device__ inline void tileUpdateMma(const float* P, int ldp, const float* dpan, int kb, int pr, int r0, int c0,
+                                     float acc[4][4]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int rb = r0 + 16 * (w & 3), cb = c0 + 32 * (w >> 2);
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[j][q] = 0.0f;
+  for (int k0 = 0; k0 < kb; k0 += 8) {
+    const int ka = k0 + t, kc = k0 + t + 4;
+    auto av = [&](int r, int k) { return (r < pr && k < kb) ? P[k * ldp + r] : 0.0f; };
+    uint32_t ah[4], al[4];
+    split3(av(rb + g, ka), ah[0], al[0]);
+    split3(av(rb + g + 8, ka), ah[1], al[1]);
+    split3(av(rb + g, kc), ah[2], al[2]);
+    split3(av(rb + g + 8, kc), ah[3], al[3]);
+    const float da = ka < kb ? dpan[ka] : 0.0f, dc = kc < kb ? dpan[kc] : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = cb + 8 * j + g;
+      uint32_t bh[2], bl[2];
+      split3(av(c, ka) * da, bh[0], bl[0]);
+      split3(av(c, kc) * dc, bh[1], bl[1]);
+      mmaTf32(acc[j], al, bh);
+      mmaTf32(acc[j], ah, bl);
+      mmaTf32(acc[j], ah, bh);
+    }
+  }
 }
 
 // Assembly (original entries, then the children's update matrices in child
@@ -193,39 +255,57 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
       for (int ti = tj; ti < ntiles; ++ti) {
         if (tcount++ % csize != crank) continue;  // this block's share of the tiles
         const int r0 = kb + ti * kTile, c0 = kb + tj * kTile;
-        T acc[4][4];
+        if constexpr (std::is_same<T, float>::value) {
+          // FP32 fronts: the tile's product on the tensor cores (3xTF32)
+          float acc[4][4];
+          tileUpdateMma(P, ldp, dpan, kb, pr, r0, c0, acc);
+          const int lane = tid & 31, w = tid >> 5, g = lane >> 2, t = lane & 3;
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+          for (int j = 0; j < 4; ++j)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
-        for (int kk = 0; kk < kb; ++kk) {
-          const T* Pk = P + kk * ldp;
-          const T dk = dpan[kk];
-          T av[4], bv[4];
+            for (int q = 0; q < 4; ++q) {
+              const int r = r0 + 16 * (w & 3) + g + 8 * (q >> 1), c = c0 + 32 * (w >> 2) + 8 * j + 2 * t + (q & 1);
+              if (r < pr && c < pr && r >= c) {
+                T* dst = F.at(k0 + r, k0 + c);
+                st(dst, ld(dst) - acc[j][q]);
+              }
+            }
+        } else {
+          // FP64 fronts: 4 x 4 register blocks on the FP64 units
+          T acc[4][4];
 #pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            const int r = r0 + lr + 16 * a;
-            av[a] = r < pr ? Pk[r] : T(0);
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+          for (int kk = 0; kk < kb; ++kk) {
+            const T* Pk = P + kk * ldp;
+            const T dk = dpan[kk];
+            T av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+              const int r = r0 + lr + 16 * a;
+              av[a] = r < pr ? Pk[r] : T(0);
+            }
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              const int c = c0 + lc + 16 * b;
+              bv[b] = c < pr ? Pk[c] * dk : T(0);
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+              for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
           }
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int c = c0 + lc + 16 * b;
-            bv[b] = c < pr ? Pk[c] * dk : T(0);
-          }
 #pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
-        }
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const int c = c0 + lc + 16 * b;
-#pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            const int r = r0 + lr + 16 * a;
-            if (r < pr && c < pr && r >= c) {
-              T* q = F.at(k0 + r, k0 + c);
-              st(q, ld(q) - acc[a][b]);
+            for (int a = 0; a < 4; ++a) {
+              const int r = r0 + lr + 16 * a;
+              if (r < pr && c < pr && r >= c) {
+                T* q = F.at(k0 + r, k0 + c);
+                st(q, ld(q) - acc[a][b]);
+              }
             }
           }
         }
