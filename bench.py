@@ -424,14 +424,18 @@ def single_model_leg(fsi, opts, steps, desc, pending=None):
     states against the oracle's and the oracle's time as the CPU baseline."""
     import numpy as np
 
-    from fedem_gb300.batch import Batch, Model, measure_fp64_peak
+    from fedem_gb300.batch import Batch, Model, measure_fp64_peak, measure_tf32_mma_peak
 
     m = Model(fsi, opts)
     flops = factor_flops(m)
     peak_tf, _ = measure_fp64_peak()
+    peak_tf32, _ = measure_tf32_mma_peak()
     out = {"workload": desc, "equations": m.neq, "unit": UNIT,
            "factor_flops_per_factorisation": flops, "fp64_fma_peak_tflops": peak_tf,
-           "fp64_peak_source": "measured (fgpu_measure_fp64_peak: 8 FMA chains per thread, 8 blocks per SM)"}
+           "fp64_peak_source": "measured (fgpu_measure_fp64_peak: 8 FMA chains per thread, 8 blocks per SM)",
+           "tf32_mma_peak_tflops": peak_tf32,
+           "tf32_peak_source": "measured (fgpu_measure_tf32_mma_peak: mma.sync m16n8k8, 8 fragments per warp, "
+                               "8 blocks per SM)"}
     finals = {}
     for mixed in (False, True):
         b = Batch([m], mixed=mixed)
@@ -467,6 +471,15 @@ def single_model_leg(fsi, opts, steps, desc, pending=None):
                                       "timing": "10 launches after the run, CUDA events on the engine stream"}
         else:
             leg["factor_gflops"] = flops / (f_ms * 1e-3) / 1e9
+            # FP32 fronts: large fronts' trailing tiles are 3xTF32 mma.sync products
+            # (three TF32 products per multiply-add), small fronts FP32 scalar
+            eff = peak_tf32 / 3.0
+            achieved = flops / (f_ms * 1e-3) / 1e12
+            leg["roofline_factor"] = {"bound": "tensor", "achieved": achieved, "peak": eff, "unit": "TFLOP/s",
+                                      "frac": achieved / eff, "traffic": None,
+                                      "peak_definition": "measured mma.sync TF32 rate / 3 (3xTF32 split)",
+                                      "kernel": "kFactorForwardCascade<float> (+ kLargeFactorForward<float>)",
+                                      "timing": "10 launches after the run, CUDA events on the engine stream"}
         out[key] = leg
         b.close()
     if pending is not None:
@@ -649,6 +662,7 @@ def main():
     iters_mixed = [b.info(k)["iterations"] for k in range(len(mods))]
     # the dominant kernel timed alone (every model factoring), after the timed runs
     fac_ms, fac_bytes = b.time_factor(reps=10) if mixed and not args.timed_only else (0.0, 0.0)
+    shape, probe_ms, _ = b.launch_shape()
     b.close()
 
     # ---- e2e through the C ABI from host buffers: set-up, upload, run, download --------
@@ -826,6 +840,10 @@ def main():
                 "wall_s_timed": wall_s, "clocks": clocks_info, "roofline": roof,
                 "roofline_elements": roof_el, "roofline_forward": roof_fwd, "roofline_backward": roof_bwd,
                 "phase_ms_per_iteration": phases,
+                "launch_shape": dict(shape, probe_ms=probe_ms,
+                                     how="autotuned before the first batched iteration: candidates timed on the "
+                                         "batch's own fronts, the fastest kept; every candidate gives the same "
+                                         "result bits"),
                 "value_definition": "Newton iterations of all models / device time of the batched mixed run, "
                                     "state resident in HBM (restored device-to-device between steps)"}
         line.update(extras)

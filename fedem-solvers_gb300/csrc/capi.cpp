@@ -826,6 +826,20 @@ int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2) {
   return b->engine.timeFactor(reps, out2, out2 + 1);
 }
 
+int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4) {
+  if (!b || !shape4) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  const int rc = b->engine.setLaunchShape(shape4);
+  if (rc == -1) return fail(-2, "launch shapes can only be set before the batch's first iteration");
+  if (rc < 0) return fail(-3, "launch shape out of range (panel 0/1, warps 4/8/16, cluster 2/4/8)");
+  return 0;
+}
+
+int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs) {
+  if (!b || !shape4) return fail(-1, "bad argument");
+  return b->engine.launchShape(shape4, probeMs);
+}
+
 int fgpu_server_create(double budget, int mixed, int sweeps, int maxModels, int minBatch, double maxWait,
                        fgpu_server** out) {
   if (!out) return fail(-1, "null output handle");

@@ -11,8 +11,13 @@
 // and replayed; models that are idle or in another phase early-exit on their
 // per-model flags, so models of uneven size and iteration count share launches.
 
+#include <array>
 #include <atomic>
 #include <chrono>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <string>
 #include <thread>
 #include <algorithm>
 #include <climits>
@@ -1250,6 +1255,190 @@ int Engine::timeFactor(int reps, double* msPerLaunch, double* bytes) {
   return 0;
 }
 
+// ---- autotuner ------------------------------------------------------------
+// Launch shapes are timed on the batch's own fronts before its first batched
+// iteration and the fastest kept.  Only shapes that give the same results to
+// the last bit are candidates (panel variant, warps per block, cluster size),
+// so the choice -- which depends on timing -- never changes a result.  Front
+// bucketing (which fronts go to warps, which to clusters) changes the
+// arithmetic and is therefore fixed (kLargeFrontRows), not tuned.
+// The probe runs while no model has started a step: the factors and solve
+// vectors it overwrites are scratch until the first iteration's
+// factorisation, which every model does (its first iteration updates the
+// tangent).  Its flags, status and pivot counters are restored.
+namespace {
+std::mutex g_shapeMutex;
+std::map<std::string, std::array<int, 4>> g_shapeCache;  // batch structure -> tuned shape
+}  // namespace
+
+int Engine::setLaunchShape(const int* sh) {
+  if (iterated_) return -1;
+  if (sh[0] < 0 || sh[0] > 1) return -2;
+  for (int k = 1; k <= 2; ++k)
+    if (sh[k] != 4 && sh[k] != 8 && sh[k] != 16) return -2;
+  if (sh[3] != 2 && sh[3] != 4 && sh[3] != 8) return -2;
+  pplan_.factorPanel = sh[0];
+  pplan_.forwardWarps = sh[1];
+  pplan_.backwardWarps = sh[2];
+  pplan_.largeCluster = sh[3];
+  shapeFixed_ = tuned_ = true;
+  probeMs_ = 0.0;
+  return 0;
+}
+
+int Engine::launchShape(int* sh, double* probeMs) const {
+  sh[0] = pplan_.factorPanel;
+  sh[1] = pplan_.forwardWarps;
+  sh[2] = pplan_.backwardWarps;
+  sh[3] = pplan_.largeCluster;
+  if (probeMs) *probeMs = probeMs_;
+  return tuned_ ? 1 : 0;
+}
+
+void Engine::ensureTuned() {
+  if (tuned_) return;
+  tuned_ = true;
+  if (iterated_ || d_.nfrontTot <= 0) return;
+  if (autotune() != 0) {  // keep the defaults
+    pplan_.factorPanel = 0;
+    pplan_.forwardWarps = pplan_.backwardWarps = pplan_.largeCluster = 8;
+  }
+}
+
+int Engine::autotune() {
+  const auto t0 = std::chrono::steady_clock::now();
+  char key[256];
+  snprintf(key, sizeof key, "dev%d f%d s%d r%d p%d L%d n%d l%d t%d", device_, opt_.fp32Factor ? 1 : 0,
+           opt_.refineSweeps, pplan_.maxRow, pplan_.maxNpiv, pplan_.maxRowLarge,
+           (int)std::lround(std::log2((double)d_.nfrontTot + 1.0)), (int)std::lround(std::log2(pplan_.nLeaves + 1.0)),
+           pplan_.nLargeTasks > 0 ? (int)std::lround(std::log2(pplan_.nLargeTasks + 1.0)) : -1);
+  {
+    std::lock_guard<std::mutex> lk(g_shapeMutex);
+    auto it = g_shapeCache.find(key);
+    if (it != g_shapeCache.end()) {
+      pplan_.factorPanel = it->second[0];
+      pplan_.forwardWarps = it->second[1];
+      pplan_.backwardWarps = it->second[2];
+      pplan_.largeCluster = it->second[3];
+      return 0;
+    }
+  }
+  const int nm = d_.m.n;
+  const bool f32 = opt_.fp32Factor;
+  std::vector<int> flags(nm), status(nm), neg(nm), all(nm, FL_ACTIVE | FL_TANGENT);
+  cudaMemcpyAsync(flags.data(), d_.m.flags, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(status.data(), d_.m.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(neg.data(), d_.m.negPiv, sizeof(int) * nm, cudaMemcpyDeviceToHost, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -1;
+  cudaMemcpyAsync(d_.m.flags, all.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  launchProbeEntries(d_, f32, stream_);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // mean milliseconds of `work` over 3 launches after one warm-up; `prep`
+  // (counters, queue seeds, inputs) is enqueued before each and not timed
+  auto timeIt = [&](const std::function<void()>& prep, const std::function<void()>& work) -> float {
+    float tot = 0.f;
+    for (int r = 0; r < 4; ++r) {
+      prep();
+      cudaEventRecord(e0, stream_);
+      work();
+      cudaEventRecord(e1, stream_);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r > 0) tot += ms;
+    }
+    return tot / 3.f;
+  };
+  const double* rhs = d_.del;
+  bool ok = true;
+  // 1. small-front factorisation: panel variant
+  {
+    float best = -1.f;
+    int pick = 0;
+    for (int pv = 0; pv <= 1; ++pv) {
+      pplan_.factorPanel = pv;
+      const float t = timeIt([&] { resetIterationCounters(stream_); },
+                             [&] { launchFactorForwardCascade(d_, pplan_, f32, rhs, stream_); });
+      if (t < 0.f) ok = false;
+      if (t >= 0.f && (best < 0.f || t < best)) best = t, pick = pv;
+    }
+    pplan_.factorPanel = pick;
+  }
+  // 2. large fronts: cluster size (the small cascade runs first, untimed)
+  if (ok && pplan_.nLargeTasks > 0) {
+    float best = -1.f;
+    int pick = 8;
+    for (int c : {8, 4, 2}) {
+      pplan_.largeCluster = c;
+      const float t = timeIt(
+          [&] {
+            resetIterationCounters(stream_);
+            launchFactorForwardCascade(d_, pplan_, f32, rhs, stream_);
+          },
+          [&] { launchLargeFactorForward(d_, pplan_, f32, rhs, stream_); });
+      if (t < 0.f) ok = false;
+      if (t >= 0.f && (best < 0.f || t < best)) best = t, pick = c;
+    }
+    pplan_.largeCluster = pick;
+  }
+  // 3. forward elimination of a refinement sweep: warps per block
+  if (ok && f32 && opt_.refineSweeps > 1) {
+    float best = -1.f;
+    int pick = 8;
+    for (int w : {8, 4, 16}) {
+      pplan_.forwardWarps = w;
+      const float t = timeIt([&] { resetIterationCounters(stream_); },
+                             [&] {
+                               launchForwardCascade(d_, pplan_, f32, rhs, 1, stream_);
+                               launchLargeForward(d_, pplan_, f32, rhs, 1, stream_);
+                             });
+      if (t < 0.f) ok = false;
+      if (t >= 0.f && (best < 0.f || t < best)) best = t, pick = w;
+    }
+    pplan_.forwardWarps = pick;
+  }
+  // 4. back substitution: warps per block (queues seeded for every model)
+  if (ok) {
+    float best = -1.f;
+    int pick = 8;
+    for (int w : {8, 4, 16}) {
+      pplan_.backwardWarps = w;
+      const float t = timeIt(
+          [&] {
+            resetIterationCounters(stream_);
+            launchSeedBackward(d_, seed_, stream_);
+          },
+          [&] {
+            launchLargeBackward(d_, pplan_, f32, 0, opt_.refineSweeps == 1, stream_);
+            launchBackward(d_, pplan_, f32, 0, opt_.refineSweeps == 1, stream_);
+          });
+      if (t < 0.f) ok = false;
+      if (t >= 0.f && (best < 0.f || t < best)) best = t, pick = w;
+    }
+    pplan_.backwardWarps = pick;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // a bounded wait that ran out in the probe would leave the error flag set
+  int errFlag = 0;
+  cudaMemcpyAsync(&errFlag, pplan_.errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(d_.m.flags, flags.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.status, status.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.negPiv, neg.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, stream_);
+  resetIterationCounters(stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess || !ok || errFlag) {
+    cudaMemsetAsync(pplan_.errFlag, 0, sizeof(int), stream_);
+    cudaStreamSynchronize(stream_);
+    return -1;
+  }
+  probeMs_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  std::lock_guard<std::mutex> lk(g_shapeMutex);
+  g_shapeCache[key] = {pplan_.factorPanel, pplan_.forwardWarps, pplan_.backwardWarps, pplan_.largeCluster};
+  return 0;
+}
+
 long long Engine::phaseTimings(double* ms, long long* elems, int n) {
   for (int k = 0; k < n && k < 5; ++k) ms[k] = phaseMs_[k];
   if (elems) *elems = phaseElems_;
@@ -1311,6 +1500,7 @@ void Engine::resetIterationCounters(cudaStream_t s) {
 // first half of a Newton iteration: step start (predictor) or the corrector's
 // right-hand side, and the Newton matrix when the tangent is updated
 void Engine::enqueueAssembly(cudaStream_t s) {
+  iterated_ = true;
   resetIterationCounters(s);
   launchBeginStep(d_, dActive_, dActiveEl_, seed_, s);
   launchQsRestore(d_, s);
@@ -1341,6 +1531,7 @@ void Engine::enqueueSolveUpdate(cudaStream_t s) {
 }
 
 int Engine::assembleIteration() {
+  ensureTuned();
   enqueueAssembly(stream_);
   return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -940;
 }
@@ -1653,6 +1844,7 @@ int Engine::probeWaitTimeout(long long spins, int* flag) {
 }
 
 int Engine::run(long long maxBatched, RunStats* stats) {
+  ensureTuned();
   if (opt_.useGraph && !graphExec_) {
     cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
     enqueueIteration(stream_);
@@ -1725,6 +1917,7 @@ int Engine::run(long long maxBatched, RunStats* stats) {
 }
 
 int Engine::launchChunk(int n) {
+  ensureTuned();
   if (opt_.useGraph && !graphExec_) {
     cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
     enqueueIteration(stream_);

@@ -137,6 +137,17 @@ class Engine {
   // Test hook: a bounded wait of `spins` polls that nothing ends (see engine.cu).
   int probeWaitTimeout(long long spins, int* flag);
 
+  // Launch shapes of the multifrontal kernels (PersistentPlan: factor panel
+  // variant, forward and backward warps per block, large-front cluster size).
+  // Before the first batched iteration the autotuner times the candidates on
+  // this batch's own fronts and keeps the fastest; shapes already tuned for a
+  // batch of the same structure are reused.  setLaunchShape (before the first
+  // iteration) fixes them instead.  No shape changes a result bit.
+  int setLaunchShape(const int* shape4);
+  // shape4 as above; *probeMs: wall time of this engine's probe (0 when the
+  // shapes came from setLaunchShape or the cache); returns 1 if tuned, 0 if not yet
+  int launchShape(int* shape4, double* probeMs) const;
+
  private:
   template <typename T>
   T* alloc(size_t n);
@@ -146,6 +157,11 @@ class Engine {
   void enqueueSolve(cudaStream_t s, bool timedForward = false);
   void enqueueFactor(cudaStream_t s);
   int readActive();
+  // the autotuner: runs once, before the first batched iteration
+  void ensureTuned();
+  int autotune();
+  bool tuned_ = false, shapeFixed_ = false, iterated_ = false;
+  double probeMs_ = 0.0;
 
   std::vector<const HostModel*> hm_;
   EngineOptions opt_;

@@ -25,6 +25,8 @@
 // Mixed precision: FP32 factor and correction solves; the FP64 refinement
 // residual is in front_kernels.cu.
 
+#include <atomic>
+
 #include "kernels.h"
 
 namespace fgpu {
@@ -44,36 +46,127 @@ namespace {
 __device__ inline bool singularPivot(float dk, float d0, double tol) { return !(fabsf(dk) > (float)tol * fabsf(d0)); }
 __device__ inline bool singularPivot(double dk, double d0, double tol) { return !(fabs(dk) > tol * fabs(d0)); }
 
-template <typename T>
+// Two panel factorisations of the small fronts, the same arithmetic in the
+// same order (so the same factor to the last bit), picked per batch by the
+// engine's autotuner: pivot by pivot with the multipliers passed by shuffles
+// and the rows kept in shared memory (few registers, high occupancy), or
+// register-blocked (fewer instructions and shared-memory accesses, more
+// registers).
+constexpr int kPanelShuffle = 0;
+constexpr int kPanelRegisters = 1;
+// pivot columns per block of the register-blocked panel factorisation
+constexpr int kPanelBlock = 8;
+
+template <typename T, int PANEL>
 __device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int lane, double tolFact, int& neg,
                               bool& sing, T* Uout) {
   if (np <= 32 && nr <= 64) {
-    // rows lane and lane + 32; the multipliers of the pivot rows (lanes below
-    // np) are passed by shuffles, one barrier per pivot
-    const int i0 = lane, i1 = lane + 32;
-    for (int k = 0; k < np; ++k) {
-      const T dk = F[k + nr * k];
-      const bool bad = singularPivot(dk, diag0[k], tolFact);
-      sing |= bad;
-      if (dk < T(0)) ++neg;
-      const T inv = bad ? T(0) : T(1) / dk;
-      const bool r0 = i0 > k && i0 < nr, r1 = i1 > k && i1 < nr;
-      const T f0 = r0 ? F[i0 + nr * k] : T(0), f1 = r1 ? F[i1 + nr * k] : T(0);
-      const T l0 = f0 * inv, l1 = f1 * inv;
-      for (int j = k + 1; j < np; ++j) {
-        const T lj = __shfl_sync(0xffffffffu, l0, j);
-        if (r0 && j <= i0) F[i0 + nr * j] -= f0 * lj;
-        if (r1) F[i1 + nr * j] -= f1 * lj;
+    if constexpr (PANEL == kPanelShuffle) {
+      // rows lane and lane + 32; the multipliers of the pivot rows (lanes below
+      // np) are passed by shuffles, one barrier per pivot
+      const int i0 = lane, i1 = lane + 32;
+      for (int k = 0; k < np; ++k) {
+        const T dk = F[k + nr * k];
+        const bool bad = singularPivot(dk, diag0[k], tolFact);
+        sing |= bad;
+        if (dk < T(0)) ++neg;
+        const T inv = bad ? T(0) : T(1) / dk;
+        const bool r0 = i0 > k && i0 < nr, r1 = i1 > k && i1 < nr;
+        const T f0 = r0 ? F[i0 + nr * k] : T(0), f1 = r1 ? F[i1 + nr * k] : T(0);
+        const T l0 = f0 * inv, l1 = f1 * inv;
+        for (int j = k + 1; j < np; ++j) {
+          const T lj = __shfl_sync(0xffffffffu, l0, j);
+          if (r0 && j <= i0) F[i0 + nr * j] -= f0 * lj;
+          if (r1) F[i1 + nr * j] -= f1 * lj;
+        }
+        if (r0) {
+          if (i0 >= np) F[k + nr * i0] = f0;
+          F[i0 + nr * k] = l0;
+        }
+        if (r1) {
+          if (i1 >= np) F[k + nr * i1] = f1;
+          F[i1 + nr * k] = l1;
+        }
+        __syncwarp();
       }
-      if (r0) {
-        if (i0 >= np) F[k + nr * i0] = f0;
-        F[i0 + nr * k] = l0;
+    } else {
+      // Register-blocked panel: lane r owns rows r and r + 32; the pivot columns
+      // are taken kPanelBlock at a time.  Inside a block the row values sit in
+      // registers and each multiplier l_jk is passed by a shuffle from the lane
+      // owning row j; the block's columns are then stored (l_ik below the
+      // diagonal, the unscaled value of an update row in its upper position),
+      // and the later pivot columns receive the block's updates all at once,
+      // l_jk read from shared memory (one broadcast load per value).  Every
+      // entry receives the same multiply-subtracts in the same order as in a
+      // right-looking elimination one pivot at a time, so the factor is the same
+      // to the last bit, with a fraction of the shared-memory traffic and no
+      // barrier per pivot.
+      const int i0 = lane, i1 = lane + 32;
+      const bool two = nr > 32;            // warp-uniform: a second row per lane
+      const bool h1 = two && i1 < nr;      // row i1 exists (it is below every pivot: np <= 32)
+      for (int k0 = 0; k0 < np; k0 += kPanelBlock) {
+        const int kb = min(kPanelBlock, np - k0);
+        const bool h0 = i0 >= k0 && i0 < nr;
+        T a0[kPanelBlock], a1[kPanelBlock];
+  #pragma unroll
+        for (int kk = 0; kk < kPanelBlock; ++kk) {
+          a0[kk] = (kk < kb && h0) ? F[i0 + nr * (k0 + kk)] : T(0);
+          a1[kk] = (kk < kb && h1) ? F[i1 + nr * (k0 + kk)] : T(0);
+        }
+  #pragma unroll
+        for (int kk = 0; kk < kPanelBlock; ++kk) {
+          if (kk >= kb) break;  // warp-uniform
+          const int k = k0 + kk;
+          const T dk = __shfl_sync(0xffffffffu, a0[kk], k);  // row k < 32 is lane k's first row
+          const bool bad = singularPivot(dk, diag0[k], tolFact);
+          sing |= bad;
+          if (dk < T(0)) ++neg;
+          const T inv = bad ? T(0) : T(1) / dk;
+          const bool r0 = i0 > k && i0 < nr;
+          const T f0 = r0 ? a0[kk] : T(0), f1 = h1 ? a1[kk] : T(0);
+          const T l0 = f0 * inv, l1 = f1 * inv;
+  #pragma unroll
+          for (int jj = kk + 1; jj < kPanelBlock; ++jj) {
+            if (jj >= kb) break;
+            const T lj = __shfl_sync(0xffffffffu, l0, k0 + jj);
+            if (r0 && k0 + jj <= i0) a0[jj] -= f0 * lj;
+            if (h1) a1[jj] -= f1 * lj;
+          }
+          if (i0 == k) F[k + nr * k] = dk;
+          if (r0) {
+            F[i0 + nr * k] = l0;
+            if (i0 >= np) F[k + nr * i0] = f0;
+            a0[kk] = f0;
+          }
+          if (h1) {
+            F[i1 + nr * k] = l1;
+            if (i1 >= np) F[k + nr * i1] = f1;
+            a1[kk] = f1;
+          }
+        }
+        __syncwarp();
+        // the later pivot columns j (row i >= j): C(i, j) -= f_i,k l_j,k over the block's k in order
+        for (int j = k0 + kb; j < np; ++j) {
+          T lj[kPanelBlock];
+  #pragma unroll
+          for (int kk = 0; kk < kPanelBlock; ++kk) lj[kk] = kk < kb ? F[j + nr * (k0 + kk)] : T(0);
+          if (i0 >= j && i0 < nr) {
+            T c = F[i0 + nr * j];
+  #pragma unroll
+            for (int kk = 0; kk < kPanelBlock; ++kk)
+              if (kk < kb) c -= a0[kk] * lj[kk];
+            F[i0 + nr * j] = c;
+          }
+          if (h1) {
+            T c = F[i1 + nr * j];
+  #pragma unroll
+            for (int kk = 0; kk < kPanelBlock; ++kk)
+              if (kk < kb) c -= a1[kk] * lj[kk];
+            F[i1 + nr * j] = c;
+          }
+        }
+        __syncwarp();
       }
-      if (r1) {
-        if (i1 >= np) F[k + nr * i1] = f1;
-        F[i1 + nr * k] = l1;
-      }
-      __syncwarp();
     }
   } else {
     for (int k = 0; k < np; ++k) {
@@ -117,7 +210,7 @@ __device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int
 constexpr int kFrontBatch = 4;
 // Uout: the front's packed update matrix (its place in the parent's
 // segment); segIn: the front's own children segment
-template <typename T>
+template <typename T, int PANEL>
 __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0, const T* asmVal, T* Lbase,
                                T* Uout, const T* segIn, double tolFact, int lane) {
   const int m = d.fModel[f];
@@ -161,7 +254,7 @@ __device__ void factorOneFront(const DevData& d, int f, T* F, T* lcol, T* diag0,
   }
   int neg = 0;
   bool sing = false;
-  factorBlocked<T>(F, lcol, diag0, nr, np, lane, tolFact, neg, sing, Uout);
+  factorBlocked<T, PANEL>(F, lcol, diag0, nr, np, lane, tolFact, neg, sing, Uout);
   T* Lout = Lbase + d.fLOff[f];
   for (int k = lane; k < nr * np; k += 32) Lout[k] = F[k];
   if (lane == 0) {
@@ -338,7 +431,7 @@ constexpr int kGroupBit = 1 << 30;
 // factorisation (models with a tangent update) fused with the forward
 // elimination of the first solve (all active models): one climb per front, and
 // the forward elimination reads L from the front still in shared memory
-template <typename T>
+template <typename T, int PANEL>
 __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow,
                                       const T* asmVal, T* Lbase, T* Ubase, double tolFact, const double* rhs, T* X,
                                       T* Wv, int* cnt) {
@@ -359,7 +452,7 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
     while ((fl & FL_ACTIVE) && f >= 0) {
       const T* Lres = nullptr;
       if (factor) {
-        factorOneFront<T>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase + d.fUOff[f], Ubase + d.fSegOff[f], tolFact,
+        factorOneFront<T, PANEL>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase + d.fUOff[f], Ubase + d.fSegOff[f], tolFact,
                           lane);
         __syncwarp();
         Lres = F;
@@ -538,12 +631,15 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
 }
 
 int smCountCached() {
-  static int n = 0;
+  // engines may be built on several host threads at once
+  static std::atomic<int> cached{0};
+  int n = cached.load(std::memory_order_relaxed);
   if (n == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (n <= 0) n = 1;
+    cached.store(n, std::memory_order_relaxed);
   }
   return n;
 }
@@ -562,12 +658,46 @@ void allowBigSmem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// one launch of a factor cascade kernel (either panel variant)
+template <typename T>
+void factorCascade(void (*kernel)(DevData, const int*, int, int, const T*, T*, T*, double, const double*, T*, T*,
+                                  int*),
+                   int wpb, size_t sm, const DevData& d, const PersistentPlan& p, const T* asmVal, T* L, T* U,
+                   double tol, const double* rhs, T* X, T* W, cudaStream_t s) {
+  allowBigSmem(kernel, sm);
+  const int blocks = occupancyBlocks(kernel, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
+  kernel<<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, asmVal, L, U, tol, rhs, X, W, p.cntFactor);
+}
+
 int factorWarpsPerBlock(size_t perWarpBytes) {
   int w = (int)(96 * 1024 / (perWarpBytes > 0 ? perWarpBytes : 1));
   return w > 8 ? 8 : (w < 1 ? 1 : w);
 }
 
+// Synthetic original entries for the autotuner's timing probe: a dominant
+// diagonal and small off-diagonal values of alternating sign (pivots stay
+// positive and far from singular, like a Newton matrix's), one thread per front.
+template <typename T>
+__global__ void kProbeEntries(DevData d, T* asmVal) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= d.nfrontTot) return;
+  const int nr = d.fNrow[f], na = d.fNasm[f];
+  const int64_t ao = d.fAsmOff[f];
+  for (int k = 0; k < na; ++k) {
+    const int pos = d.asmPos[ao + k];
+    const int i = pos % nr, j = pos / nr;
+    asmVal[ao + k] = i == j ? T(4 + nr) : (((i + j) & 1) ? T(0.01) : T(-0.01));
+  }
+}
+
 }  // namespace
+
+void launchProbeEntries(const DevData& d, bool fp32, cudaStream_t s) {
+  if (d.nfrontTot <= 0) return;
+  const int blocks = (d.nfrontTot + 127) / 128;
+  if (fp32) kProbeEntries<float><<<blocks, 128, 0, s>>>(d, d.asmVal32);
+  else kProbeEntries<double><<<blocks, 128, 0, s>>>(d, d.asmVal64);
+}
 
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
                                 cudaStream_t s) {
@@ -577,17 +707,21 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
   if (fp32) {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
     const size_t sm = (size_t)wpb * perWarp * sizeof(float);
-    allowBigSmem(kFactorForwardCascade<float>, sm);
-    const int blocks = occupancyBlocks(kFactorForwardCascade<float>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.asmVal32, d.L32,
-                                                             d.U32, tol, rhs, d.x32, d.w32, p.cntFactor);
+    if (p.factorPanel == kPanelRegisters)
+      factorCascade(kFactorForwardCascade<float, kPanelRegisters>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
+                    d.x32, d.w32, s);
+    else
+      factorCascade(kFactorForwardCascade<float, kPanelShuffle>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
+                    d.x32, d.w32, s);
   } else {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(double));
     const size_t sm = (size_t)wpb * perWarp * sizeof(double);
-    allowBigSmem(kFactorForwardCascade<double>, sm);
-    const int blocks = occupancyBlocks(kFactorForwardCascade<double>, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-    kFactorForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, d.asmVal64,
-                                                               d.L64, d.U64, tol, rhs, d.x64, d.w64, p.cntFactor);
+    if (p.factorPanel == kPanelRegisters)
+      factorCascade(kFactorForwardCascade<double, kPanelRegisters>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol,
+                    rhs, d.x64, d.w64, s);
+    else
+      factorCascade(kFactorForwardCascade<double, kPanelShuffle>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol, rhs,
+                    d.x64, d.w64, s);
   }
 }
 
@@ -601,7 +735,7 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
                           cudaStream_t s) {
   if (p.nTasks <= 0) return;
-  const int wpb = 8;
+  const int wpb = p.forwardWarps;
   int* cnt = p.cntForward + (size_t)(sweep - 1) * ((size_t)d.nfrontTot + 1);
   if (fp32) {
     const int capL = stagingCapacity(p, sizeof(float));
@@ -624,7 +758,7 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
   const int acc = !fp32 ? ACC_SET : (sweep == 0 ? ACC_FIRST : ACC_ADD);
   const int fin = (fp32 && last) ? 1 : 0;
   if (p.nLeaves <= 0) return;
-  const int wpb = 8;
+  const int wpb = p.backwardWarps;
   int* queue = p.bwQueue + (size_t)sweep * p.nLeaves;
   int* ctr = p.bwCtr + 4 * sweep;
   const int needed = (p.nLeaves + wpb - 1) / wpb;

@@ -34,6 +34,8 @@
 #include <algorithm>
 #include <type_traits>
 
+#include <atomic>
+
 #include "kernels.h"
 
 namespace fgpu {
@@ -42,7 +44,6 @@ namespace {
 namespace cg = cooperative_groups;
 
 constexpr int kLT = 256;         // threads per large-front block
-constexpr int kClusterCtas = 8;  // blocks of a cluster that factor one large front together
 constexpr int kTile = 64;        // trailing-update tile (rows and columns)
 
 // lower-triangle entry (ii >= jj) of an nu x nu matrix packed column by column
@@ -539,12 +540,15 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
 }
 
 int smCount() {
-  static int n = 0;
+  // engines may be built on several host threads at once
+  static std::atomic<int> cached{0};
+  int n = cached.load(std::memory_order_relaxed);
   if (n == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (n <= 0) n = 1;
+    cached.store(n, std::memory_order_relaxed);
   }
   return n;
 }
@@ -572,7 +576,7 @@ int panelWidth(int maxRow) {
   return kb;
 }
 
-// Factorisations run as clusters of kClusterCtas blocks per front (a grid of
+// Factorisations run as clusters of p.largeCluster blocks per front (a grid of
 // as many clusters as fit at once, at most one per start task); forward
 // eliminations alone as single blocks.
 template <typename T>
@@ -590,7 +594,8 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kClusterCtas;
+  const int csize = p.largeCluster;
+  attr[0].val.clusterDim.x = csize;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(kLT);
@@ -598,12 +603,12 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cfg.gridDim = dim3(kClusterCtas * p.nLargeTasks);
+  cfg.gridDim = dim3(csize * p.nLargeTasks);
   int clusters = 0;
   if (cudaOccupancyMaxActiveClusters(&clusters, kLargeFactorForward<T>, &cfg) != cudaSuccess || clusters < 1)
     clusters = 1;
   clusters = std::min(clusters, p.nLargeTasks);
-  cfg.gridDim = dim3(kClusterCtas * clusters);
+  cfg.gridDim = dim3(csize * clusters);
   cudaLaunchKernelEx(&cfg, kLargeFactorForward<T>, d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, 1, kb);
 }
 

@@ -118,6 +118,13 @@ struct PersistentPlan {
   int *cntLargeFactor = nullptr, *cntLargeForward = nullptr;
   int *bwLQueue = nullptr, *bwLCtr = nullptr;
   int largeStride = 0;
+  // Launch shapes, picked per batch by the engine's autotuner.  No choice
+  // changes a result bit: tasks are taken dynamically, and each front's
+  // arithmetic is the same whichever warp, block or cluster does it.
+  int factorPanel = 0;     // small-front panel factorisation: 0 shuffles, 1 register-blocked
+  int forwardWarps = 8;    // warps per block of the forward-elimination cascade
+  int backwardWarps = 8;   // warps per block of the back-substitution queue
+  int largeCluster = 8;    // blocks per cluster of the large-front factorisation (2, 4 or 8)
 };
 // fronts with more rows than this are factored and solved by a thread block
 // each (front_large.cu); smaller ones by one warp each in shared memory
@@ -153,6 +160,9 @@ void launchMotions(const DevData& d, cudaStream_t s);
 void launchLoads(const DevData& d, cudaStream_t s);
 void launchMotionRhs(const DevData& d, cudaStream_t s);
 void launchQsRestore(const DevData& d, cudaStream_t s);
+// synthetic, diagonally dominant original entries of every front (the
+// autotuner's timing probe, before the first iteration gathers the real ones)
+void launchProbeEntries(const DevData& d, bool fp32, cudaStream_t s);
 // FP64 refinement residual r = b - A x (front_kernels.cu)
 void launchRefineResidual(const DevData& d, cudaStream_t s);
 

@@ -116,6 +116,16 @@ def measure_fp64_peak(lib=None):
     return tf.value, ms.value
 
 
+def measure_tf32_mma_peak(lib=None):
+    """Measured TF32 rate of mma.sync m16n8k8 (FP32 accumulation) on the current
+    device: (TFLOP/s, ms of the best launch) from fgpu_measure_tf32_mma_peak."""
+    lib = lib or load_library()
+    tf, ms = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    if lib.fgpu_measure_tf32_mma_peak(ctypes.byref(tf), ctypes.byref(ms)) != 0:
+        raise FedemException("fgpu_measure_tf32_mma_peak failed")
+    return tf.value, ms.value
+
+
 class Batch:
     """Models resident on the GPU, advanced together (mixed or FP64)."""
 
@@ -211,6 +221,21 @@ class Batch:
         if self._lib.fgpu_batch_time_factor(self._h, int(reps), _ptr(out, ctypes.c_double)) != 0:
             raise FedemException("time_factor failed: " + self._lib.fgpu_last_error().decode())
         return float(out[0]), float(out[1])
+
+    def set_launch_shape(self, panel, forward_warps, backward_warps, large_cluster):
+        """Fixes the multifrontal launch shapes (before the first run) instead of
+        the autotuner's probe; no shape changes a result bit."""
+        sh = (ctypes.c_int * 4)(panel, forward_warps, backward_warps, large_cluster)
+        if self._lib.fgpu_batch_set_launch_shape(self._h, sh) != 0:
+            raise FedemException("set_launch_shape failed: " + self._lib.fgpu_last_error().decode())
+
+    def launch_shape(self):
+        """({panel, forward_warps, backward_warps, large_cluster}, probe ms, tuned)."""
+        sh = (ctypes.c_int * 4)()
+        ms = ctypes.c_double(0.0)
+        tuned = self._lib.fgpu_batch_launch_shape(self._h, sh, ctypes.byref(ms))
+        keys = ("panel", "forward_warps", "backward_warps", "large_cluster")
+        return dict(zip(keys, list(sh))), ms.value, tuned == 1
 
     def norms(self, model):
         v = np.zeros(18)

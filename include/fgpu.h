@@ -124,6 +124,22 @@ long long fgpu_batch_phase_timings_n(fgpu_batch* b, double* ms, int n, long long
  * snapshot before the next one.  Returns 0, or < 0 on error. */
 int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
 
+/* Launch shapes of the multifrontal kernels, shape4 = {small-front panel
+ * factorisation (0: pivot by pivot with shuffles, 1: register-blocked),
+ * warps per block of the forward-elimination cascade (4, 8 or 16), warps per
+ * block of the back-substitution queue (4, 8 or 16), blocks per cluster of the
+ * large-front factorisation (2, 4 or 8)}.  The autotuner picks them before a
+ * batch's first batched iteration by timing the candidates on the batch's own
+ * fronts (a few milliseconds; a batch of the same structure reuses the
+ * choice).  Every shape gives the same results to the last bit, so the
+ * timing-dependent choice never changes a result.  set: before the first
+ * iteration only, and it replaces the probe.  get: returns 1 once the shapes
+ * are chosen (0 before); *probeMs (may be NULL) = wall time of the batch's
+ * probe, 0 when set or reused.  No reference counterpart (the reference has
+ * no GPU kernels to shape). */
+int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4);
+int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs);
+
 /* Failure-path test hook: runs one warp of the back-substitution queue kernel
  * on a private queue whose only slot is never filled, with a wait limit of
  * `spins` polls (about 32 ns each), so the bounded wait runs out and sets the
@@ -140,6 +156,16 @@ int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag);
  * Returns 0, or < 0 on error.  The peak that FP64-bound kernels are quoted
  * against. */
 int fgpu_measure_fp64_peak(double* tflops, double* ms);
+
+/* Measured TF32 tensor rate of the warp-level mma.sync m16n8k8 instruction
+ * (FP32 accumulation) on the library's current device: eight independent
+ * accumulator fragments per warp, eight 256-thread blocks per SM, best of
+ * five timed launches after three warm-up launches.  *tflops: TF32 TFLOP/s
+ * (2 flops per multiply-add; a 3xTF32 split product costs three of them);
+ * *ms: the best launch's time.  Returns 0, or < 0 on error.  The peak that
+ * the FP32 large-front trailing tiles are quoted against.  No counterpart in
+ * the reference (a measurement helper). */
+int fgpu_measure_tf32_mma_peak(double* tflops, double* ms);
 
 /* ---- serving: continuous batching of simulation requests ------------------
  * Requests are admitted into new GPU batches (own stream each) as soon as the
