@@ -13,6 +13,11 @@ Server::Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBat
     : budget_(budgetBytes), device_(device), opt_(opt), maxModels_(maxModelsPerBatch > 0 ? maxModelsPerBatch : 1 << 30),
       chunk_(chunk > 0 ? chunk : 4), t0_(std::chrono::steady_clock::now()) {}
 
+Server::~Server() {
+  for (auto& st : starting_)
+    if (st.rc.valid()) st.rc.wait();  // engines being built finish before the server goes
+}
+
 double Server::now() const {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
 }
@@ -37,13 +42,13 @@ int Server::submit(const HostModel* m) {
   return (int)reqs_.size() - 1;
 }
 
-// Uploads the models of `ids` into a new engine for job j, computes their
-// initial state, and puts the carried state of the first carried->size() of
-// them back (models moved from another engine, between steps).
-int Server::startEngine(Job& j, const std::vector<int>& ids, const std::vector<std::vector<char>>* carried) {
+// Uploads the models `ms` (requests `ids`) into a new engine for job j,
+// computes their initial state, and puts the carried state of the first
+// carried->size() of them back (models moved from another engine, between
+// steps).  Touches only j and its arguments (it may run on its own thread).
+int Server::startEngine(Job& j, const std::vector<int>& ids, const std::vector<const HostModel*>& ms,
+                        const std::vector<std::vector<char>>* carried) {
   j.engine = std::make_unique<Engine>();
-  std::vector<const HostModel*> ms;
-  for (int id : ids) ms.push_back(reqs_[id].model);
   std::string err;
   int rc = j.engine->upload(ms, opt_, err);
   if (!rc) rc = j.engine->initialState(err);
@@ -58,9 +63,9 @@ int Server::startEngine(Job& j, const std::vector<int>& ids, const std::vector<s
 
 int Server::admit() {
   if (pending_.empty()) return 0;
-  if (maxEngines_ > 0 && (int)jobs_.size() >= maxEngines_) return 0;
+  if (maxEngines_ > 0 && liveEngines() >= maxEngines_) return 0;
   // batching window: wait for a few requests unless the device is idle
-  bool idle = jobs_.empty();
+  bool idle = liveEngines() == 0;
   double waited = now() - reqs_[pending_.front()].arrival;
   if (!idle && (int)pending_.size() < minBatch_ && waited < maxWait_) return 0;
   std::vector<int> take;
@@ -68,24 +73,61 @@ int Server::admit() {
   while (!pending_.empty() && (int)take.size() < maxModels_) {
     int id = pending_.front();
     size_t b = estimateBytes(*reqs_[id].model, opt_);
-    if (inUse_ + bytes + b > budget_ && !(take.empty() && jobs_.empty())) break;
+    if (inUse_ + bytes + b > budget_ && !(take.empty() && liveEngines() == 0)) break;
     take.push_back(id);
     bytes += b;
     pending_.pop_front();
   }
   if (take.empty()) return 0;
-  Job j;
-  const int rc = startEngine(j, take, nullptr);
+  // the engine is built on a host thread of its own; its requests count as
+  // running and its estimated memory as in use until finishStarts takes it
+  Starting st;
+  st.job = std::make_unique<Job>();
+  st.ids = take;
+  st.reserved = bytes;
   const double t = now();
-  if (rc) {
-    for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
-    return rc;
+  std::vector<const HostModel*> ms;
+  for (int id : take) {
+    reqs_[id].state = 1;
+    reqs_[id].admitted = t;
+    ms.push_back(reqs_[id].model);
   }
-  for (int id : take) { reqs_[id].state = 1; reqs_[id].admitted = t; }
-  inUse_ += j.bytes;
-  if (j.engine->launchChunk(chunk_)) return -950;
-  jobs_.push_back(std::move(j));
+  inUse_ += bytes;
+  Job* jp = st.job.get();
+  const int dev = device_, chunk = chunk_;
+  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk]() {
+    if (cudaSetDevice(dev) != cudaSuccess) return -953;
+    int rc = startEngine(*jp, take, ms, nullptr);
+    if (!rc && jp->engine->launchChunk(chunk)) rc = -950;
+    return rc;
+  });
+  starting_.push_back(std::move(st));
   return 1;
+}
+
+// Takes the engines whose build finished into the running jobs (or fails
+// their requests).  Returns the number of requests failed, < 0 never.
+int Server::finishStarts() {
+  int failed = 0;
+  for (size_t k = 0; k < starting_.size();) {
+    Starting& st = starting_[k];
+    if (st.rc.wait_for(std::chrono::seconds(0)) != std::future_status::ready) {
+      ++k;
+      continue;
+    }
+    const int rc = st.rc.get();
+    inUse_ -= st.reserved;
+    if (rc) {
+      const double t = now();
+      for (int id : st.ids) { reqs_[id].state = 3; reqs_[id].finished = t; }
+      failed += (int)st.ids.size();
+    } else {
+      inUse_ += st.job->bytes;
+      jobs_.push_back(std::move(*st.job));
+    }
+    starting_.erase(starting_.begin() + (long)k);
+  }
+  return failed;
 }
 
 // Moves the running models of job k (all stopped between steps) into a new
@@ -118,7 +160,9 @@ int Server::rebatch(size_t k) {
   inUse_ -= old.bytes;
   old.engine.reset();  // the device memory of the old engine goes first
   Job j;
-  const int rc = startEngine(j, take, &carried);
+  std::vector<const HostModel*> ms;
+  for (int id : take) ms.push_back(reqs_[id].model);
+  const int rc = startEngine(j, take, ms, &carried);
   const double t = now();
   if (rc) {
     for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
@@ -161,7 +205,7 @@ int Server::collect(Job& j, bool all) {
 
 int Server::pump() {
   if (cudaSetDevice(device_) != cudaSuccess) return -953;
-  int finished = 0;
+  int finished = finishStarts();
   // collect finished requests and engines, keep the others fed
   for (size_t k = 0; k < jobs_.size();) {
     Job& j = jobs_[k];

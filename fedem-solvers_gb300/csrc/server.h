@@ -12,10 +12,13 @@
 // into a new engine together with the waiting requests that fit, and they
 // continue there exactly as they would have (the old engine's memory, finished
 // slots included, is released).  Finished engines release their memory.
+// A new engine is built (upload, initial state, first chunk) on a host thread
+// of its own, so the engines already running stay fed meanwhile.
 #pragma once
 
 #include <chrono>
 #include <deque>
+#include <future>
 #include <memory>
 #include <vector>
 
@@ -44,7 +47,7 @@ class Server {
   const Request& request(int id) const { return reqs_[id]; }
   int numRequests() const { return (int)reqs_.size(); }
   int pending() const { return (int)pending_.size(); }
-  int liveEngines() const { return (int)jobs_.size(); }
+  int liveEngines() const { return (int)(jobs_.size() + starting_.size()); }
   size_t bytesInUse() const { return inUse_; }
 
  private:
@@ -54,10 +57,19 @@ class Server {
     size_t bytes = 0;
     bool parking = false;  // running models stop at their next step end for a move
   };
+  // an engine being built on its own host thread for admitted requests
+  struct Starting {
+    std::unique_ptr<Job> job;
+    std::vector<int> ids;
+    size_t reserved = 0;  // estimated bytes held in inUse_ until it is built
+    std::future<int> rc;
+  };
   static size_t estimateBytes(const HostModel& m, const EngineOptions& opt);
   int admit();
   int collect(Job& j, bool all);
-  int startEngine(Job& j, const std::vector<int>& ids, const std::vector<std::vector<char>>* carried);
+  int startEngine(Job& j, const std::vector<int>& ids, const std::vector<const HostModel*>& ms,
+                  const std::vector<std::vector<char>>* carried);
+  int finishStarts();
   int rebatch(size_t k);
 
   size_t budget_, inUse_ = 0;
@@ -84,7 +96,11 @@ class Server {
   std::vector<Request> reqs_;
   std::deque<int> pending_;
   std::vector<Job> jobs_;
+  std::vector<Starting> starting_;
   std::chrono::steady_clock::time_point t0_;
+
+ public:
+  ~Server();
 };
 
 }  // namespace fgpu
