@@ -330,18 +330,41 @@ __device__ void forwardOneFront(const DevData& d, int f, T* v, T* Ls, int capL, 
 // Wout: where the front's update vector goes; Win: the children's update
 // vectors concatenated in child order in shared memory (their gather list
 // order), or null to read them from W
+// Descriptors a solve of front f reads, loaded together in one round of
+// independent loads (every lane the same address: broadcasts).  The caller
+// loads them early, the parent's climb data right after (ParentLink), so that
+// neither costs a round trip of its own later.
+struct SolveDesc {
+  int f, nr, np, cg0, ncg, nch, parent;
+  int64_t lOff, rowOff, wOff;
+};
+__device__ inline SolveDesc solveDesc(const DevData& d, int f) {
+  SolveDesc q;
+  q.f = f;
+  q.nr = d.fNrow[f];
+  q.np = d.fNpiv[f];
+  q.cg0 = d.cgOff[f];
+  q.ncg = d.cgOff[f + 1] - q.cg0;
+  q.nch = d.fNchild[f];
+  q.parent = d.fParent[f];
+  q.lOff = d.fLOff[f];
+  q.rowOff = d.fRowOff[f];
+  q.wOff = d.fWOff[f];
+  return q;
+}
+
 template <typename T>
-__device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int capL, const T* Lbase,
+__device__ bool forwardOneFrontFast(const DevData& d, const SolveDesc& q, T* v, T* Ls, int capL, const T* Lbase,
                                     const double* rhs, T* X, const T* W, int lane, const T* Lres, T* Wout,
                                     const T* Win = nullptr) {
-  const int nr = d.fNrow[f], np = d.fNpiv[f];
-  const int cg0 = d.cgOff[f], ncg = d.cgOff[f + 1] - cg0, nch = d.fNchild[f];
+  const int nr = q.nr, np = q.np;
+  const int cg0 = q.cg0, ncg = q.ncg, nch = q.nch;
   const int cnt = nr * np;
   if (nr > 64 || ncg > 64 || (!Lres && cnt > capL)) return false;
-  const int* rows = d.frontRows + d.fRowOff[f];
+  const int* rows = d.frontRows + q.rowOff;
   // second round of loads: independent loads (the L block asynchronously into shared memory)
   if (!Lres) {
-    const T* Lg = Lbase + d.fLOff[f];
+    const T* Lg = Lbase + q.lOff;
     for (int k = lane; k < cnt; k += 32) copyAsync(Ls + k, Lg + k);
   }
   int row[2], src[2], dst[2];
@@ -390,27 +413,38 @@ __device__ bool forwardOneFrontFast(const DevData& d, int f, T* v, T* Ls, int ca
   return true;
 }
 
-// After a front is done: release its data and count it at the parent; returns
-// the parent if this warp completed the parent's count (and must go on), else -1
-// (also for a large parent: the large-front kernels take it up afterwards).
-// The warp barrier orders every lane's stores before lane 0's counter update,
-// a release-acquire RMW at GPU scope (no full fence): the warp that completes
-// the count acquires the children's stores, and its barrier passes them on to
-// its other lanes.
-__device__ inline int climb(const DevData& d, int f, int* cnt, int lane) {
-  __syncwarp();
-  int next = -1;
-  if (lane == 0) {
-    const int p = d.fParent[f];
-    if (p >= 0 && !d.fLarge[p]) {  // a large parent is left to the large-front kernels
-      int old;
-      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(cnt + p) : "memory");
-      if (old == d.fNchild[p] - 1) next = p;
-    }
+// After a front is done: release its data and count it at the parent; true
+// if this warp completed the parent's count (and must go on with the parent),
+// false otherwise (also for a large parent: the large-front kernels take it up
+// afterwards).  The parent's id, size class and child count (ParentLink) are
+// loaded while the front is still being processed, so the climb itself is one
+// atomic.  The warp barrier orders every lane's stores before lane 0's counter
+// update, a release-acquire RMW at GPU scope (no full fence): the warp that
+// completes the count acquires the children's stores, and its barrier passes
+// them on to its other lanes.
+struct ParentLink {
+  int p, nch;
+  bool large;
+};
+__device__ inline ParentLink parentLink(const DevData& d, int p) {
+  ParentLink l{p, 0, true};
+  if (p >= 0) {
+    l.large = d.fLarge[p] != 0;
+    l.nch = d.fNchild[p];
   }
-  next = __shfl_sync(0xffffffffu, next, 0);
+  return l;
+}
+__device__ inline bool climb(const ParentLink& l, int* cnt, int lane) {
   __syncwarp();
-  return next;
+  int go = 0;
+  if (lane == 0 && l.p >= 0 && !l.large) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(cnt + l.p) : "memory");
+    go = old == l.nch - 1;
+  }
+  go = __shfl_sync(0xffffffffu, go, 0);
+  __syncwarp();
+  return go != 0;
 }
 
 // Leaves are taken in their stored order (longest root paths first) from a
@@ -450,16 +484,18 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
     const int fl = d.m.flags[d.fModel[f]];
     const bool factor = fl & FL_TANGENT;
     while ((fl & FL_ACTIVE) && f >= 0) {
+      const SolveDesc q = solveDesc(d, f);
+      const ParentLink pl = parentLink(d, q.parent);
       const T* Lres = nullptr;
       if (factor) {
-        factorOneFront<T, PANEL>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase + d.fUOff[f], Ubase + d.fSegOff[f], tolFact,
-                          lane);
+        factorOneFront<T, PANEL>(d, f, F, lcol, diag0, asmVal, Lbase, Ubase + d.fUOff[f], Ubase + d.fSegOff[f],
+                                 tolFact, lane);
         __syncwarp();
         Lres = F;
       }
-      if (!forwardOneFrontFast<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres, Wv + d.fWOff[f]))
+      if (!forwardOneFrontFast<T>(d, q, v, F, capL, Lbase, rhs, X, Wv, lane, Lres, Wv + q.wOff))
         forwardOneFront<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres);
-      f = climb(d, f, cnt, lane);
+      f = climb(pl, cnt, lane) ? q.parent : -1;
     }
     idx = __shfl_sync(0xffffffffu, pending, 0);
   }
@@ -480,23 +516,35 @@ __global__ void kForwardCascade(DevData d, const int* __restrict__ tasks, int nT
     const int task = tasks[idx];
     int f = task & ~kGroupBit;
     const bool active = d.m.flags[d.fModel[f]] & FL_ACTIVE;
-    if (active && (task & kGroupBit)) {
-      const int nch = d.fNchild[f];
+    if (!active) f = -1;
+    SolveDesc q;
+    if (f >= 0) q = solveDesc(d, f);
+    if (f >= 0 && (task & kGroupBit)) {
+      const ParentLink pl = parentLink(d, q.parent);
       const int* ch = d.childList + d.fChildOff[f];
       int wo = 0;
-      for (int c = 0; c < nch; ++c) {
-        const int cf = ch[c];
-        forwardOneFrontFast<T>(d, cf, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, wsm + wo);
-        wo += d.fNrow[cf] - d.fNpiv[cf];
+      SolveDesc cq = solveDesc(d, ch[0]);
+      for (int c = 0; c < q.nch; ++c) {
+        // the next child's descriptors are loaded while this one is eliminated
+        const SolveDesc nq = solveDesc(d, ch[c + 1 < q.nch ? c + 1 : c]);
+        forwardOneFrontFast<T>(d, cq, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, wsm + wo);
+        wo += cq.nr - cq.np;
         __syncwarp();
+        cq = nq;
       }
-      forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + d.fWOff[f], wsm);
-      f = climb(d, f, cnt, lane);
+      forwardOneFrontFast<T>(d, q, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + q.wOff, wsm);
+      f = climb(pl, cnt, lane) ? q.parent : -1;
+      if (f >= 0) q = solveDesc(d, f);
     }
-    while (active && f >= 0) {
-      if (!forwardOneFrontFast<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + d.fWOff[f]))
+    while (f >= 0) {
+      // the parent's climb data and descriptors are loaded ahead of this
+      // front's elimination; they are used only if this warp goes on to it
+      const ParentLink pl = parentLink(d, q.parent);
+      const SolveDesc pq = solveDesc(d, q.parent >= 0 ? q.parent : f);
+      if (!forwardOneFrontFast<T>(d, q, v, Ls, capL, Lbase, rhs, X, W, lane, nullptr, W + q.wOff))
         forwardOneFront<T>(d, f, v, Ls, capL, Lbase, rhs, X, W, lane);
-      f = climb(d, f, cnt, lane);
+      f = climb(pl, cnt, lane) ? q.parent : -1;
+      q = pq;
     }
     idx = __shfl_sync(0xffffffffu, pending, 0);
   }
@@ -509,12 +557,33 @@ __global__ void kForwardCascade(DevData d, const int* __restrict__ tasks, int nT
 // xref = x, ACC_ADD xref += x (FP32 refinement sweeps); finalize: del = xref
 enum { ACC_SET = 0, ACC_FIRST = 1, ACC_ADD = 2 };
 
+// Descriptors of a back substitution, loaded together: the front's, and with
+// them those of its first child (the front the warp goes on to), so that the
+// next front starts without a descriptor round trip.
+struct BackDesc {
+  int f, nr, np, nch;
+  bool inl;  // children all leaves, solved by this warp
+  int64_t lOff, rowOff, childOff;
+};
+__device__ inline BackDesc backDesc(const DevData& d, const unsigned char* bwInline, int f) {
+  BackDesc q;
+  q.f = f;
+  q.nr = d.fNrow[f];
+  q.np = d.fNpiv[f];
+  q.nch = d.fNchild[f];
+  q.inl = bwInline[f] != 0;
+  q.lOff = d.fLOff[f];
+  q.rowOff = d.fRowOff[f];
+  q.childOff = d.fChildOff[f];
+  return q;
+}
+
 template <typename T>
-__device__ void backwardOneFront(const DevData& d, int f, T* xs, T* Ls, int capL, const T* Lbase, T* X, int acc,
-                                 bool finalize, int lane) {
-  const int nr = d.fNrow[f], np = d.fNpiv[f];
-  const int* rows = d.frontRows + d.fRowOff[f];
-  const T* L = stageL(Lbase + d.fLOff[f], nr * np, Ls, capL, lane);
+__device__ void backwardOneFront(const DevData& d, const BackDesc& q, T* xs, T* Ls, int capL, const T* Lbase, T* X,
+                                 int acc, bool finalize, int lane) {
+  const int nr = q.nr, np = q.np;
+  const int* rows = d.frontRows + q.rowOff;
+  const T* L = stageL(Lbase + q.lOff, nr * np, Ls, capL, lane);
   for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + __ldg(rows + r));
   copyAsyncWait();
   __syncwarp();
@@ -602,30 +671,38 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
     ok = __shfl_sync(0xffffffffu, ok, 0);
     __syncwarp();
     if (!ok) break;
+    BackDesc q = backDesc(d, bwInline, f);
     while (f >= 0) {
-      backwardOneFront<T>(d, f, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
+      // the first child and its descriptors are loaded ahead of this front's solve
+      const int* ch = d.childList + q.childOff;
+      const int c0 = q.nch > 0 ? ch[0] : -1;
+      const BackDesc cq = backDesc(d, bwInline, c0 >= 0 ? c0 : f);
+      backwardOneFront<T>(d, q, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
       __threadfence();
       __syncwarp();
-      const int nch = d.fNchild[f];
+      const int nch = q.nch;
       int next = -1;
       if (nch > 0) {
-        const int* ch = d.childList + d.fChildOff[f];
-        if (bwInline[f]) {
+        if (q.inl) {
           // children that are all leaves: solved here, one after the other
+          BackDesc lq = cq;
           for (int c = 0; c < nch; ++c) {
-            backwardOneFront<T>(d, ch[c], xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
+            const BackDesc nq = backDesc(d, bwInline, ch[c + 1 < nch ? c + 1 : c]);
+            backwardOneFront<T>(d, lq, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
             __syncwarp();
+            lq = nq;
           }
         } else {
-          next = ch[0];
+          next = c0;
           if (lane == 0 && nch > 1) {
             const int base = atomicAdd(ctr + 1, nch - 1);
-            for (int q = 1; q < nch; ++q) atomicExch(queue + base + q - 1, ch[q]);
+            for (int k = 1; k < nch; ++k) atomicExch(queue + base + k - 1, ch[k]);
           }
         }
       }
       __syncwarp();
       f = next;
+      q = cq;
     }
   }
 }

@@ -178,10 +178,23 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
     const int cu = d.fNrow[ch] - d.fNpiv[ch];
     const int64_t len = (int64_t)cu * (cu + 1) / 2;
     if (c > 0) clusterBarrier();
-    for (int64_t k = gtid; k < len; k += gstride) {
-      const int p = __ldg(spos + off + k) & 0xfffff;
-      T* q = F.at(p % nr, p / nr);
-      st(q, ld(q) + ld(seg + off + k));
+    // four entries per thread at a time, every load issued before the stores
+    // (positions are distinct within one child)
+    for (int64_t k0 = gtid; k0 < len; k0 += 4 * (int64_t)gstride) {
+      T* q[4];
+      T sv[4], cur[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t k = k0 + (int64_t)u * gstride;
+        const int p = k < len ? (__ldg(spos + off + k) & 0xfffff) : -1;
+        q[u] = p >= 0 ? F.at(p % nr, p / nr) : nullptr;
+        sv[u] = p >= 0 ? ld(seg + off + k) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) cur[u] = q[u] ? ld(q[u]) : T(0);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (q[u]) st(q[u], cur[u] + sv[u]);
     }
     off += len;
   }
@@ -261,16 +274,22 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
           float acc[4][4];
           tileUpdateMma(P, ldp, dpan, kb, pr, r0, c0, acc);
           const int lane = tid & 31, w = tid >> 5, g = lane >> 2, t = lane & 3;
+          // the tile's sixteen entries of this thread: every load before the stores
+          T* dst[4][4];
+          T cur[4][4];
 #pragma unroll
           for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               const int r = r0 + 16 * (w & 3) + g + 8 * (q >> 1), c = c0 + 32 * (w >> 2) + 8 * j + 2 * t + (q & 1);
-              if (r < pr && c < pr && r >= c) {
-                T* dst = F.at(k0 + r, k0 + c);
-                st(dst, ld(dst) - acc[j][q]);
-              }
+              dst[j][q] = (r < pr && c < pr && r >= c) ? F.at(k0 + r, k0 + c) : nullptr;
+              cur[j][q] = dst[j][q] ? ld(dst[j][q]) : T(0);
             }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (dst[j][q]) st(dst[j][q], cur[j][q] - acc[j][q]);
         } else {
           // FP64 fronts: 4 x 4 register blocks on the FP64 units
           T acc[4][4];
@@ -297,18 +316,23 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
 #pragma unroll
               for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
           }
+          T* dst[4][4];
+          T cur[4][4];
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int c = c0 + lc + 16 * b;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
               const int r = r0 + lr + 16 * a;
-              if (r < pr && c < pr && r >= c) {
-                T* q = F.at(k0 + r, k0 + c);
-                st(q, ld(q) - acc[a][b]);
-              }
+              dst[a][b] = (r < pr && c < pr && r >= c) ? F.at(k0 + r, k0 + c) : nullptr;
+              cur[a][b] = dst[a][b] ? ld(dst[a][b]) : T(0);
             }
           }
+#pragma unroll
+          for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+              if (dst[a][b]) st(dst[a][b], cur[a][b] - acc[a][b]);
         }
       }
   }
@@ -324,7 +348,8 @@ __device__ void factorLarge(const DevData& d, int f, const T* asmVal, T* Lbase, 
 // blocks of 32 pivots: warp 0 eliminates the block's unit lower triangle with
 // shuffles, then every thread updates its rows below the block with it
 template <typename T>
-__device__ void forwardLarge(const DevData& d, int f, const T* Lbase, const double* rhs, T* X, T* W, T* v) {
+__device__ void forwardLarge(const DevData& d, int f, const T* Lbase, const double* rhs, T* X, T* W, T* v,
+                             T* Ltri) {
   const int tid = threadIdx.x, lane = tid & 31;
   const int nr = d.fNrow[f], np = d.fNpiv[f], nu = nr - np;
   const T* L = Lbase + d.fLOff[f];
@@ -345,17 +370,37 @@ __device__ void forwardLarge(const DevData& d, int f, const T* Lbase, const doub
   for (int b0 = 0; b0 < np; b0 += 32) {
     const int bs = min(32, np - b0);
     if (tid < 32) {  // the block's triangle: lane r holds v[b0 + r]
+      // the triangle is staged in shared memory first (eight independent loads
+      // at a time), so that no step of the dependent chain below waits on a load
+      for (int k0 = 0; k0 < bs - 1; k0 += 8) {
+        T t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + u;
+          t[u] = (k < bs - 1 && lane > k && lane < bs) ? ld(L + (b0 + lane) + (int64_t)nr * (b0 + k)) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) Ltri[(k0 + u) * 32 + lane] = t[u];
+      }
+      __syncwarp();
       T x = lane < bs ? v[b0 + lane] : T(0);
       for (int k = 0; k < bs - 1; ++k) {
         const T yk = __shfl_sync(0xffffffffu, x, k);
-        if (lane > k && lane < bs) x -= ld(L + (b0 + lane) + (int64_t)nr * (b0 + k)) * yk;
+        if (lane > k && lane < bs) x -= Ltri[k * 32 + lane] * yk;
       }
       if (lane < bs) v[b0 + lane] = x;
     }
     __syncthreads();
     for (int i = b0 + bs + tid; i < nr; i += kLT) {
       T s = v[i];
-      for (int k = 0; k < bs; ++k) s -= ld(L + i + (int64_t)nr * (b0 + k)) * v[b0 + k];
+      for (int k0 = 0; k0 < bs; k0 += 8) {  // eight loads in flight, then the ordered updates
+        T t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t[u] = k0 + u < bs ? ld(L + i + (int64_t)nr * (b0 + k0 + u)) : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (k0 + u < bs) s -= t[u] * v[b0 + k0 + u];
+      }
       v[i] = s;
     }
     __syncthreads();
@@ -393,7 +438,8 @@ __global__ void __launch_bounds__(kLT) kLargeFactorForward(DevData d, Persistent
   T* v = reinterpret_cast<T*>(smraw);
   T* diag0 = v + ldp;
   T* dpan = diag0 + ldp;
-  T* P = dpan + 32;
+  T* Ltri = dpan + 32;  // 32 x 32 staging of a forward elimination's triangle
+  T* P = Ltri + 32 * 32;
   __shared__ int shIdx, shNext;
   cg::cluster_group cluster = cg::this_cluster();
   const int crank = (int)cluster.block_rank(), csize = (int)cluster.num_blocks();
@@ -411,7 +457,7 @@ __global__ void __launch_bounds__(kLT) kLargeFactorForward(DevData d, Persistent
     while ((fl & FL_ACTIVE) && f >= 0) {
       if (factor) factorLarge<T>(d, f, asmVal, Lbase, Ubase, tolFact, P, ldp, panel, diag0, dpan, crank, csize);
       if (crank == 0) {
-        forwardLarge<T>(d, f, Lbase, rhs, X, W, v);
+        forwardLarge<T>(d, f, Lbase, rhs, X, W, v, Ltri);
         f = climbLarge(d, p, f, cnt, &shNext);
       }
       cluster.sync();
@@ -431,6 +477,7 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
                                                        int* ctr, int* errFlag, int acc, int finalize) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* xs = reinterpret_cast<T*>(smraw);
+  T* Ltri = xs + ((p.maxRowLarge + 3) & ~3);  // 32 x 32 staging of a block's triangle
   __shared__ int shSlot, shF, shOk;
   const int tid = threadIdx.x;
   const int w = tid >> 5, lane = tid & 31;
@@ -481,10 +528,23 @@ __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan 
       for (int bEnd = np; bEnd > 0; bEnd -= 32) {
         const int b0 = bEnd > 32 ? bEnd - 32 : 0, bs = bEnd - b0;
         if (tid < 32) {
+          // lane r's column of the triangle staged first (rows j > r), eight
+          // independent loads at a time
+          for (int j0 = 0; j0 < bs; j0 += 8) {
+            T t[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int j = j0 + u;
+              t[u] = (j < bs && lane < j) ? ld(L + (b0 + j) + (int64_t)nr * (b0 + lane)) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) Ltri[(j0 + u) * 32 + lane] = t[u];
+          }
+          __syncwarp();
           T x = lane < bs ? xs[b0 + lane] : T(0);
           for (int j = bs - 1; j > 0; --j) {
             const T xj = __shfl_sync(0xffffffffu, x, j);
-            if (lane < j) x -= ld(L + (b0 + j) + (int64_t)nr * (b0 + lane)) * xj;
+            if (lane < j) x -= Ltri[j * 32 + lane] * xj;
           }
           if (lane < bs) xs[b0 + lane] = x;
         }
@@ -572,7 +632,7 @@ template <typename T>
 int panelWidth(int maxRow) {
   const size_t ldp = (size_t)((maxRow + 3) & ~3);
   int kb = 32;
-  while (kb > 4 && (2 * ldp + 32 + (size_t)kb * ldp) * sizeof(T) > 200 * 1024) kb -= 4;
+  while (kb > 4 && (2 * ldp + 32 + 32 * 32 + (size_t)kb * ldp) * sizeof(T) > 200 * 1024) kb -= 4;
   return kb;
 }
 
@@ -584,7 +644,7 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
                         T* X, T* W, int* cnt, bool factor, cudaStream_t s) {
   const size_t ldp = (size_t)((p.maxRowLarge + 3) & ~3);
   const int kb = panelWidth<T>(p.maxRowLarge);
-  const size_t sm = (2 * ldp + 32 + (factor ? (size_t)kb * ldp : 0)) * sizeof(T);
+  const size_t sm = (2 * ldp + 32 + 32 * 32 + (factor ? (size_t)kb * ldp : 0)) * sizeof(T);
   bigSmem(kLargeFactorForward<T>, sm);
   if (!factor) {
     const int grid = gridFor(kLargeFactorForward<T>, sm, p.nLargeTasks);
@@ -636,12 +696,12 @@ void launchLargeBackward(const DevData& d, const PersistentPlan& p, bool fp32, i
   int* queue = p.bwLQueue + (size_t)sweep * p.largeStride;
   int* ctr = p.bwLCtr + 4 * sweep;
   if (fp32) {
-    const size_t sm = (size_t)p.maxRowLarge * sizeof(float);
+    const size_t sm = ((size_t)((p.maxRowLarge + 3) & ~3) + 32 * 32) * sizeof(float);
     bigSmem(kLargeBackward<float>, sm);
     const int grid = gridFor(kLargeBackward<float>, sm, p.nLargeTasks);
     kLargeBackward<float><<<grid, kLT, sm, s>>>(d, p, d.L32, d.x32, queue, ctr, p.errFlag, acc, fin);
   } else {
-    const size_t sm = (size_t)p.maxRowLarge * sizeof(double);
+    const size_t sm = ((size_t)((p.maxRowLarge + 3) & ~3) + 32 * 32) * sizeof(double);
     bigSmem(kLargeBackward<double>, sm);
     const int grid = gridFor(kLargeBackward<double>, sm, p.nLargeTasks);
     kLargeBackward<double><<<grid, kLT, sm, s>>>(d, p, d.L64, d.x64, queue, ctr, p.errFlag, acc, fin);

@@ -16,6 +16,25 @@ Server::Server(size_t budgetBytes, const EngineOptions& opt, int maxModelsPerBat
 Server::~Server() {
   for (auto& st : starting_)
     if (st.rc.valid()) st.rc.wait();  // engines being built finish before the server goes
+  for (auto& r : retiring_)
+    if (r.valid()) r.wait();
+}
+
+// A finished engine is destroyed on a host thread of its own: freeing device
+// memory waits for the device, and the pump must keep the other engines fed.
+void Server::retire(std::unique_ptr<Engine> e) {
+  for (size_t k = 0; k < retiring_.size();) {
+    if (retiring_[k].wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+      retiring_.erase(retiring_.begin() + (long)k);
+    } else {
+      ++k;
+    }
+  }
+  const int dev = device_;
+  retiring_.push_back(std::async(std::launch::async, [dev, e = std::move(e)]() mutable {
+    cudaSetDevice(dev);
+    e.reset();
+  }));
 }
 
 double Server::now() const {
@@ -132,7 +151,8 @@ int Server::finishStarts() {
 
 // Moves the running models of job k (all stopped between steps) into a new
 // engine together with the waiting requests that fit the memory the old engine
-// frees, and replaces the job.  Returns the number of requests admitted.
+// frees: the job is removed and the new engine built on its own host thread.
+// Returns the number of requests admitted.
 int Server::rebatch(size_t k) {
   Job& old = jobs_[k];
   std::vector<int> keep;
@@ -158,25 +178,33 @@ int Server::rebatch(size_t k) {
     ++added;
   }
   inUse_ -= old.bytes;
-  old.engine.reset();  // the device memory of the old engine goes first
-  Job j;
-  std::vector<const HostModel*> ms;
-  for (int id : take) ms.push_back(reqs_[id].model);
-  const int rc = startEngine(j, take, ms, &carried);
+  std::unique_ptr<Engine> oldEngine = std::move(old.engine);
+  jobs_.erase(jobs_.begin() + (long)k);
+  // the new engine is built on a host thread of its own, as for an admission
   const double t = now();
-  if (rc) {
-    for (int id : take) { reqs_[id].state = 3; reqs_[id].finished = t; }
-    jobs_.erase(jobs_.begin() + (long)k);
-    return rc;
-  }
   for (size_t q = keep.size(); q < take.size(); ++q) {
     reqs_[take[q]].state = 1;
     reqs_[take[q]].admitted = t;
   }
-  inUse_ += j.bytes;
+  Starting st;
+  st.job = std::make_unique<Job>();
+  st.ids = take;
+  st.reserved = bytes;
+  inUse_ += bytes;
+  std::vector<const HostModel*> ms;
+  for (int id : take) ms.push_back(reqs_[id].model);
+  Job* jp = st.job.get();
+  const int dev = device_, chunk = chunk_;
+  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk, carried = std::move(carried),
+                                           oldEngine = std::move(oldEngine)]() mutable {
+    if (cudaSetDevice(dev) != cudaSuccess) return -953;
+    oldEngine.reset();  // the device memory of the old engine goes first
+    int rc = startEngine(*jp, take, ms, &carried);
+    if (!rc && jp->engine->launchChunk(chunk)) rc = -950;
+    return rc;
+  });
+  starting_.push_back(std::move(st));
   ++rebatches_;
-  if (j.engine->launchChunk(chunk_)) return -950;
-  jobs_[k] = std::move(j);
   return added;
 }
 
@@ -218,15 +246,15 @@ int Server::pump() {
       bool running = false;
       for (int id : j.ids) running |= reqs_[id].state == 1;
       if (running) {
-        const int a = rebatch(k);
+        const int a = rebatch(k);  // removes job k
         if (a < 0) return a;
-        ++k;
         continue;
       }
     }
     if (ready && active == 0) {
       finished += collect(j, true);
       inUse_ -= j.bytes;
+      retire(std::move(j.engine));
       jobs_.erase(jobs_.begin() + (long)k);
       continue;
     }

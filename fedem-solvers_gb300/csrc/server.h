@@ -12,8 +12,9 @@
 // into a new engine together with the waiting requests that fit, and they
 // continue there exactly as they would have (the old engine's memory, finished
 // slots included, is released).  Finished engines release their memory.
-// A new engine is built (upload, initial state, first chunk) on a host thread
-// of its own, so the engines already running stay fed meanwhile.
+// A new engine is built (upload, initial state, first chunk), and a finished
+// one destroyed, on a host thread of its own, so the engines already running
+// stay fed meanwhile.
 #pragma once
 
 #include <chrono>
@@ -70,6 +71,8 @@ class Server {
   int startEngine(Job& j, const std::vector<int>& ids, const std::vector<const HostModel*>& ms,
                   const std::vector<std::vector<char>>* carried);
   int finishStarts();
+  void retire(std::unique_ptr<Engine> e);
+  std::vector<std::future<void>> retiring_;
   int rebatch(size_t k);
 
   size_t budget_, inUse_ = 0;
