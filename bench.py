@@ -102,6 +102,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=48)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the served leg (with the --serve-* parameters) and print its JSON")
     ap.add_argument("--serve-slot-reuse", type=float, default=0.25,
                     help="share of an engine's models finished before its slots are reused (0: never)")
     return ap.parse_args()
@@ -598,6 +600,10 @@ def main():
     want_single = rank == 0 and not args.timed_only
     lib = fedem_gb300.load_library()
     dev, bus = rank_device(local, lib)
+    if args.served_only:
+        out = {"served": served_leg(args, args.serve_slot_reuse, compare_batched=False)}
+        print(json.dumps(out), flush=True)
+        return
     if args.single_models_only:
         work = single_model_workloads(args)
         pool, pending = start_single_oracles(args, work)

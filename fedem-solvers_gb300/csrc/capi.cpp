@@ -835,6 +835,22 @@ int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4) {
   return 0;
 }
 
+int fgpu_batch_results_open(fgpu_batch* b, const char* dir, int doublePrecision) {
+  if (!b || !dir) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  std::string err;
+  if (int rc = b->engine.resultsOpen(dir, doublePrecision != 0, err)) return fail(rc, err);
+  return 0;
+}
+
+int fgpu_batch_results_close(fgpu_batch* b) {
+  if (!b) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  std::string err;
+  if (int rc = b->engine.resultsClose(err)) return fail(rc, err);
+  return 0;
+}
+
 int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs) {
   if (!b || !shape4) return fail(-1, "bad argument");
   return b->engine.launchShape(shape4, probeMs);

@@ -41,6 +41,10 @@ namespace fgpu {
 
 Engine::~Engine() {
   cudaSetDevice(device_);
+  if (rec_.on) {
+    std::string err;
+    resultsClose(err);
+  }
   if (graphExec_) cudaGraphExecDestroy(graphExec_);
   if (graph_) cudaGraphDestroy(graph_);
   if (stream_) cudaStreamSynchronize(stream_);
@@ -1528,6 +1532,7 @@ void Engine::enqueueSolveUpdate(cudaStream_t s) {
   launchElements(d_, EM_INC, s);
   recordPhase(ev_[4], s);
   launchNormsControl(d_, s);
+  if (rec_.on) launchRecordStep(d_, rec_.plan, false, s);
 }
 
 int Engine::assembleIteration() {
@@ -1538,7 +1543,9 @@ int Engine::assembleIteration() {
 
 int Engine::solveUpdateIteration() {
   enqueueSolveUpdate(stream_);
-  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -941;
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -941;
+  std::string err;
+  return resultsDrain(err) ? -942 : 0;
 }
 
 void Engine::setStepLimitOf(int m, long long lim) {
@@ -1768,7 +1775,8 @@ void Engine::enqueueIteration(cudaStream_t s) {
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl * (pplan_.nLargeTasks > 0 ? 2 : 1) + solveLaunches +
                      (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +
-                     (d_.nldTot > 0 ? 1 : 0) + (d_.njointTot > 0 ? 2 : 0) + (d_.ncxTot > 0 ? 3 : 0);
+                     (d_.nldTot > 0 ? 1 : 0) + (d_.njointTot > 0 ? 2 : 0) + (d_.ncxTot > 0 ? 3 : 0) +
+                     (rec_.on ? 1 : 0);
 }
 
 int Engine::readActive() {
@@ -1887,6 +1895,10 @@ int Engine::run(long long maxBatched, RunStats* stats) {
       phaseElems_ += *hActiveEl_;
       ++phaseSamples_;
     }
+    if (rec_.on) {
+      std::string err;
+      if (resultsDrain(err)) return -924;
+    }
     if (active == 0) break;
   }
   cudaEventRecord(evRun_[1], stream_);
@@ -1949,6 +1961,10 @@ int Engine::pollChunk(bool* ready, int* active) {
   chunkPending_ = false;
   *ready = true;
   *active = *hActive_;
+  if (rec_.on) {
+    std::string err;
+    if (resultsDrain(err)) return -926;
+  }
   return 0;
 }
 

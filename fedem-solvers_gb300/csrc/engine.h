@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <string>
 #include <array>
 #include <vector>
@@ -148,6 +149,12 @@ class Engine {
   // shapes came from setLaunchShape or the cache); returns 1 if tuned, 0 if not yet
   int launchShape(int* shape4, double* probeMs) const;
 
+  // Results database of the primary response (results.cu): from now on every
+  // model appends one record per completed time step to <dir>/model<k>.res
+  // (a record of the current state first).  resultsClose flushes and closes.
+  int resultsOpen(const std::string& dir, bool asDouble, std::string& err);
+  int resultsClose(std::string& err);
+
  private:
   template <typename T>
   T* alloc(size_t n);
@@ -162,6 +169,16 @@ class Engine {
   int autotune();
   bool tuned_ = false, shapeFixed_ = false, iterated_ = false;
   double probeMs_ = 0.0;
+  // results database: ring plan, files and the records already written per model
+  struct Results {
+    bool on = false, asDouble = true;
+    RecordPlan plan;
+    std::vector<FILE*> files;
+    std::vector<int> vals;
+    std::vector<long long> off, written;
+    std::vector<double> host;
+  } rec_;
+  int resultsDrain(std::string& err);
 
   std::vector<const HostModel*> hm_;
   EngineOptions opt_;

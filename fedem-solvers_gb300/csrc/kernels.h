@@ -163,6 +163,24 @@ void launchQsRestore(const DevData& d, cudaStream_t s);
 // synthetic, diagonally dominant original entries of every front (the
 // autotuner's timing probe, before the first iteration gathers the real ones)
 void launchProbeEntries(const DevData& d, bool fp32, cudaStream_t s);
+// results database of the primary response (results.cu): per model a ring of
+// kRecordRing records (step, time, triad positions, superelement frames and
+// generalized DOFs, as doubles) in buf, written at each completed step
+struct RecordPlan {
+  double* buf = nullptr;       // the rings, model after model
+  long long* off = nullptr;    // per model: first value of its ring
+  int* vals = nullptr;         // per model: values per record (2 + data)
+  int* triRec = nullptr;       // per triad (global): offset of its values in its model's record
+  int* elRec = nullptr;        // per model: offset of its beam frames (12 per element)
+  int* partFirst = nullptr;    // per model, + 1: first reduced part (global)
+  int* partRec = nullptr;      // per part: offset of its frame and generalized DOFs
+  long long* count = nullptr;  // per model: records written so far
+  int ring = 0;
+};
+constexpr int kRecordRing = 8;
+// all: a record of every model's current state; otherwise of the models whose
+// step has just completed
+void launchRecordStep(const DevData& d, const RecordPlan& r, bool all, cudaStream_t s);
 // FP64 refinement residual r = b - A x (front_kernels.cu)
 void launchRefineResidual(const DevData& d, cudaStream_t s);
 

@@ -103,6 +103,8 @@ def load_library(path=None):
         "fgpu_measure_tf32_mma_peak": (c_int, [P(c_dbl), P(c_dbl)]),
         "fgpu_batch_set_launch_shape": (c_int, [vp, P(c_int)]),
         "fgpu_batch_launch_shape": (c_int, [vp, P(c_int), P(c_dbl)]),
+        "fgpu_batch_results_open": (c_int, [vp, ctypes.c_char_p, c_int]),
+        "fgpu_batch_results_close": (c_int, [vp]),
         "fgpu_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

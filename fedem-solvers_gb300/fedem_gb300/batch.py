@@ -237,6 +237,17 @@ class Batch:
         keys = ("panel", "forward_warps", "backward_warps", "large_cluster")
         return dict(zip(keys, list(sh))), ms.value, tuned == 1
 
+    def results_open(self, directory, double=True):
+        """Starts the results database: one file per model, <directory>/model<k>.res,
+        a record of the current state now and one per completed time step
+        (read it with fedem_gb300.results.read_results)."""
+        if self._lib.fgpu_batch_results_open(self._h, str(directory).encode(), 1 if double else 0) != 0:
+            raise FedemException("results_open failed: " + self._lib.fgpu_last_error().decode())
+
+    def results_close(self):
+        if self._lib.fgpu_batch_results_close(self._h) != 0:
+            raise FedemException("results_close failed: " + self._lib.fgpu_last_error().decode())
+
     def norms(self, model):
         v = np.zeros(18)
         self._lib.fgpu_batch_get_norms(self._h, model, _ptr(v, ctypes.c_double))

@@ -18,7 +18,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["engine.cu", "element_kernels.cu", "front_kernels.cu", "front_cascade.cu", "norms_noalloc.cu",
-              "joint_kernels.cu", "front_large.cu", "peaks.cu", "part_kernels.cu"]
+              "joint_kernels.cu", "front_large.cu", "peaks.cu", "part_kernels.cu", "results.cu"]
 CPP_SOURCES = ["host_model.cpp", "symbolic.cpp", "server.cpp", "eigen.cpp", "capi.cpp"]
 
 

@@ -140,6 +140,26 @@ int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
 int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4);
 int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs);
 
+/* Results database of the primary response (the reference's writeSolverDB1,
+ * src/vpmSolver/saveModule.f90:615-663, called for the initial configuration
+ * and after every time step, solverModule.f90:512-513, :929-931): every model
+ * of the batch writes <dir>/model<k>.res, a text header naming the record
+ * layout, then one binary record per saved state -- the step number (int32),
+ * the time (float64), each triad's position matrix (3 x 4, column by column;
+ * the translation only for three-DOF triads), each beam superelement's frame
+ * (3 x 4) and each reduced part's frame and generalized DOF values -- in
+ * double precision, or single precision when doublePrecision is 0 (the
+ * reference's -double1 option).  The first record is the models' current
+ * state; then one per completed time step.  Records are packed on the GPU at
+ * the end of each step into a small ring in device memory and appended to the
+ * files at the next synchronisation point of fgpu_batch_run, fgpu_batch_step
+ * or an externally driven iteration.  close flushes and closes the files
+ * (also done by fgpu_batch_destroy).  The header layout is this library's own
+ * (the reference's lives in a results-database library that is not part of
+ * its source tree); the record contents and order follow the reference. */
+int fgpu_batch_results_open(fgpu_batch* b, const char* dir, int doublePrecision);
+int fgpu_batch_results_close(fgpu_batch* b);
+
 /* Failure-path test hook: runs one warp of the back-substitution queue kernel
  * on a private queue whose only slot is never filled, with a wait limit of
  * `spins` polls (about 32 ns each), so the bounded wait runs out and sets the
