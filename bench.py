@@ -104,7 +104,7 @@ def parse():
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     ap.add_argument("--served-only", action="store_true",
                     help="run only the served leg (with the --serve-* parameters) and print its JSON")
-    ap.add_argument("--serve-slot-reuse", type=float, default=0.25,
+    ap.add_argument("--serve-slot-reuse", type=float, default=0.0,
                     help="share of an engine's models finished before its slots are reused (0: never)")
     return ap.parse_args()
 
@@ -771,7 +771,8 @@ def main():
         pool, pending = start_single_oracles(args, work)
         # ---- served: Poisson request stream with continuous batching ----------------------
         extras["served"] = served_leg(args, args.serve_slot_reuse)
-        extras["served_without_slot_reuse"] = served_leg(args, 0.0, compare_batched=False)
+        extras["served_with_slot_reuse"] = served_leg(args, 0.25 if args.serve_slot_reuse == 0.0 else 0.0,
+                                                      compare_batched=False)
         for key, fsi, opts, steps, desc in work:
             extras[key] = single_model_leg(fsi, opts, steps, desc, pending.get(key))
         if pool is not None:

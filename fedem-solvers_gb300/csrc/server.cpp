@@ -5,6 +5,7 @@
 
 #include "server.h"
 
+#include <array>
 #include <string>
 
 namespace fgpu {
@@ -83,6 +84,8 @@ int Server::startEngine(Job& j, const std::vector<int>& ids, const std::vector<c
 int Server::admit() {
   if (pending_.empty()) return 0;
   if (maxEngines_ > 0 && liveEngines() >= maxEngines_) return 0;
+  // one engine build at a time: requests arriving meanwhile join the next one
+  if (!starting_.empty()) return 0;
   // batching window: wait for a few requests unless the device is idle
   bool idle = liveEngines() == 0;
   double waited = now() - reqs_[pending_.front()].arrival;
@@ -114,9 +117,12 @@ int Server::admit() {
   inUse_ += bytes;
   Job* jp = st.job.get();
   const int dev = device_, chunk = chunk_;
-  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk]() {
+  const std::array<int, 4> shape = shape_;
+  const bool haveShape = haveShape_;
+  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk, shape, haveShape]() {
     if (cudaSetDevice(dev) != cudaSuccess) return -953;
     int rc = startEngine(*jp, take, ms, nullptr);
+    if (!rc && haveShape) jp->engine->setLaunchShape(shape.data());
     if (!rc && jp->engine->launchChunk(chunk)) rc = -950;
     return rc;
   });
@@ -142,6 +148,12 @@ int Server::finishStarts() {
       failed += (int)st.ids.size();
     } else {
       inUse_ += st.job->bytes;
+      if (!haveShape_) {
+        // the first engine's tuned launch shapes serve every later engine
+        // (no probe per engine; results do not depend on the shapes)
+        double ms = 0.0;
+        haveShape_ = st.job->engine->launchShape(shape_.data(), &ms) == 1;
+      }
       jobs_.push_back(std::move(*st.job));
     }
     starting_.erase(starting_.begin() + (long)k);
@@ -195,11 +207,14 @@ int Server::rebatch(size_t k) {
   for (int id : take) ms.push_back(reqs_[id].model);
   Job* jp = st.job.get();
   const int dev = device_, chunk = chunk_;
-  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk, carried = std::move(carried),
-                                           oldEngine = std::move(oldEngine)]() mutable {
+  const std::array<int, 4> shape = shape_;
+  const bool haveShape = haveShape_;
+  st.rc = std::async(std::launch::async, [this, jp, take, ms, dev, chunk, shape, haveShape,
+                                           carried = std::move(carried), oldEngine = std::move(oldEngine)]() mutable {
     if (cudaSetDevice(dev) != cudaSuccess) return -953;
     oldEngine.reset();  // the device memory of the old engine goes first
     int rc = startEngine(*jp, take, ms, &carried);
+    if (!rc && haveShape) jp->engine->setLaunchShape(shape.data());
     if (!rc && jp->engine->launchChunk(chunk)) rc = -950;
     return rc;
   });

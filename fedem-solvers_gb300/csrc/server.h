@@ -17,6 +17,7 @@
 // stay fed meanwhile.
 #pragma once
 
+#include <array>
 #include <chrono>
 #include <deque>
 #include <future>
@@ -72,6 +73,8 @@ class Server {
                   const std::vector<std::vector<char>>* carried);
   int finishStarts();
   void retire(std::unique_ptr<Engine> e);
+  std::array<int, 4> shape_{};  // launch shapes tuned by the first engine, for the later ones
+  bool haveShape_ = false;
   std::vector<std::future<void>> retiring_;
   int rebatch(size_t k);
 
