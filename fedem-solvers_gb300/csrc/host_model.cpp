@@ -25,6 +25,7 @@
 #include <array>
 #include <climits>
 #include <map>
+#include <string_view>
 
 namespace fgpu {
 namespace {
@@ -32,9 +33,42 @@ namespace {
 // ---------------------------------------------------------------------------
 // Namelist text -> records of key -> raw value tokens
 // ---------------------------------------------------------------------------
+// One namelist record, flat: its keys (lower case) in first-seen order and
+// the values of every key occurrence as segments of one value list (a key
+// given twice collects both segments, in order).  Values are views of the
+// model text as written (quotes of quoted strings removed; n*v repeats
+// expanded); the text outlives the records.
 struct NmlRecord {
   std::string name;
-  std::map<std::string, std::vector<std::string>> vals;
+  std::vector<std::string> keys;
+  std::vector<std::array<int, 3>> segs;  // key index, first value, value count
+  std::vector<std::string_view> vals;
+  int keyIndex(const char* k) const {
+    for (size_t i = 0; i < keys.size(); ++i)
+      if (keys[i] == k) return (int)i;
+    return -1;
+  }
+  // the values of key k, in order (false: no such key)
+  template <typename F>
+  bool each(const char* k, F f) const {
+    const int ki = keyIndex(k);
+    if (ki < 0) return false;
+    for (const auto& sg : segs)
+      if (sg[0] == ki)
+        for (int v = 0; v < sg[2]; ++v) f(vals[sg[1] + v]);
+    return true;
+  }
+  // the first value of key k (false: no such key or no value)
+  bool first(const char* k, std::string_view& out) const {
+    const int ki = keyIndex(k);
+    if (ki < 0) return false;
+    for (const auto& sg : segs)
+      if (sg[0] == ki && sg[2] > 0) {
+        out = vals[sg[1]];
+        return true;
+      }
+    return false;
+  }
 };
 
 std::string lowerCase(const std::string& s) {
@@ -43,7 +77,14 @@ std::string lowerCase(const std::string& s) {
   return r;
 }
 
-double toDouble(const std::string& tok) {
+double toDouble(std::string_view tok) {
+  // a Fortran exponent letter d/D reads as e
+  char buf[64];
+  if (tok.size() < sizeof buf) {
+    for (size_t k = 0; k < tok.size(); ++k) buf[k] = (tok[k] == 'd' || tok[k] == 'D') ? 'e' : tok[k];
+    buf[tok.size()] = '\0';
+    return std::strtod(buf, nullptr);
+  }
   std::string t(tok);
   for (char& c : t)
     if (c == 'd' || c == 'D') c = 'e';
@@ -54,52 +95,89 @@ std::vector<NmlRecord> readNamelists(const char* text) {
   std::vector<NmlRecord> out;
   const size_t n = std::strlen(text);
   size_t p = 0;
+  auto lowerIn = [](std::string& r) {
+    for (char& ch : r)
+      if (ch >= 'A' && ch <= 'Z') ch = (char)(ch - 'A' + 'a');
+  };
+  // ASCII classes (the model text is ASCII; no locale look-ups per character)
+  auto isSpace = [](char ch) { return ch == ' ' || ch == '\n' || ch == '\t' || ch == '\r' || ch == '\f' || ch == '\v'; };
+  auto isWordChar = [](char ch) {
+    return (ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || (ch >= '0' && ch <= '9') || ch == '_';
+  };
   while (p < n) {
-    while (p < n && text[p] != '&') ++p;
+    {
+      const void* amp = std::memchr(text + p, '&', n - p);
+      p = amp ? (size_t)((const char*)amp - text) : n;
+    }
     if (p >= n) break;
     size_t q = ++p;
-    while (q < n && (std::isalnum((unsigned char)text[q]) || text[q] == '_')) ++q;
+    while (q < n && isWordChar(text[q])) ++q;
     NmlRecord rec;
-    rec.name = lowerCase(std::string(text + p, q - p));
+    rec.name.assign(text + p, q - p);
+    lowerIn(rec.name);
     p = q;
-    struct Tok { std::string s; char kind; };  // 'w' word, '=' assign, 's' string
-    std::vector<Tok> toks;
+    // a word followed by '=' starts a key; words and quoted strings after a
+    // key are its values; a word is held back until the next token shows
+    // which of the two it is
+    int key = -1;
+    size_t pendS = 0, pendL = 0;
+    bool pend = false;
+    auto addValue = [&](const char* v, size_t len, bool word) {
+      if (key < 0) return;
+      const void* star = word ? std::memchr(v, '*', len) : nullptr;
+      if (star && star != v) {
+        const size_t sp = (size_t)((const char*)star - v);
+        const int rep = std::atoi(std::string(v, sp).c_str());
+        for (int r = 0; r < rep; ++r) rec.vals.emplace_back(v + sp + 1, len - sp - 1);  // views
+        rec.segs.back()[2] += rep > 0 ? rep : 0;
+      } else {
+        rec.vals.emplace_back(v, len);
+        rec.segs.back()[2] += 1;
+      }
+    };
+    auto flushPending = [&]() {
+      if (pend) addValue(text + pendS, pendL, true);
+      pend = false;
+    };
     while (p < n) {
-      char c = text[p];
-      if (c == '/') { ++p; break; }
-      if (std::isspace((unsigned char)c) || c == ',') { ++p; continue; }
-      if (c == '!') { while (p < n && text[p] != '\n') ++p; continue; }
-      if (c == '=') { toks.push_back({"=", '='}); ++p; continue; }
-      if (c == '\'' || c == '"') {
-        size_t s0 = ++p;
-        while (p < n && text[p] != c) ++p;
-        toks.push_back({std::string(text + s0, p - s0), 's'});
+      const char ch = text[p];
+      if (ch == '/') { ++p; break; }
+      if (isSpace(ch) || ch == ',') { ++p; continue; }
+      if (ch == '!') { while (p < n && text[p] != '\n') ++p; continue; }
+      if (ch == '=') {
+        ++p;
+        if (pend) {  // the held word is a key
+          std::string k(text + pendS, pendL);
+          lowerIn(k);
+          int ki = rec.keyIndex(k.c_str());
+          if (ki < 0) {
+            ki = (int)rec.keys.size();
+            rec.keys.push_back(std::move(k));
+          }
+          key = ki;
+          rec.segs.push_back({ki, (int)rec.vals.size(), 0});
+          pend = false;
+        }
+        continue;
+      }
+      if (ch == '\'' || ch == '"') {
+        flushPending();
+        const size_t s0 = ++p;
+        while (p < n && text[p] != ch) ++p;
+        addValue(text + s0, p - s0, false);
         if (p < n) ++p;
         continue;
       }
-      size_t s0 = p;
-      while (p < n && !std::isspace((unsigned char)text[p]) && text[p] != ',' && text[p] != '=' &&
+      flushPending();
+      const size_t s0 = p;
+      while (p < n && !isSpace(text[p]) && text[p] != ',' && text[p] != '=' &&
              text[p] != '/' && text[p] != '\'' && text[p] != '"')
         ++p;
-      toks.push_back({std::string(text + s0, p - s0), 'w'});
+      pendS = s0;
+      pendL = p - s0;
+      pend = true;
     }
-    std::string key;
-    for (size_t k = 0; k < toks.size(); ++k) {
-      if (toks[k].kind == 'w' && k + 1 < toks.size() && toks[k + 1].kind == '=') {
-        key = lowerCase(toks[k].s);
-        rec.vals[key];
-        ++k;
-      } else if (!key.empty()) {
-        const std::string& s = toks[k].s;
-        size_t star = toks[k].kind == 'w' ? s.find('*') : std::string::npos;
-        if (star != std::string::npos && star > 0) {
-          int rep = std::atoi(s.substr(0, star).c_str());
-          for (int r = 0; r < rep; ++r) rec.vals[key].push_back(s.substr(star + 1));
-        } else {
-          rec.vals[key].push_back(s);
-        }
-      }
-    }
+    flushPending();
     out.push_back(std::move(rec));
   }
   return out;
@@ -109,30 +187,29 @@ struct Rec {
   const NmlRecord& r;
   std::vector<double> nums(const char* k) const {
     std::vector<double> v;
-    auto it = r.vals.find(k);
-    if (it != r.vals.end())
-      for (const auto& s : it->second) v.push_back(toDouble(s));
+    r.each(k, [&](std::string_view x) { v.push_back(toDouble(x)); });
     return v;
   }
   double num(const char* k, double def) const {
-    auto v = nums(k);
-    return v.empty() ? def : v[0];
+    std::string_view x;
+    return r.first(k, x) ? toDouble(x) : def;
   }
   int inum(const char* k, int def) const { return (int)std::lround(num(k, (double)def)); }
   std::string str(const char* k) const {
-    auto it = r.vals.find(k);
-    return (it == r.vals.end() || it->second.empty()) ? std::string() : lowerCase(it->second[0]);
+    std::string_view x;
+    return r.first(k, x) ? lowerCase(std::string(x)) : std::string();
   }
   // every value as written (file names)
   std::vector<std::string> strs(const char* k) const {
-    auto it = r.vals.find(k);
-    return it == r.vals.end() ? std::vector<std::string>() : it->second;
+    std::vector<std::string> v;
+    r.each(k, [&](std::string_view x) { v.emplace_back(x); });
+    return v;
   }
   // the value as written (quotes removed), for names compared case-sensitively
   std::string raw(const char* k) const {
-    auto it = r.vals.find(k);
-    if (it == r.vals.end() || it->second.empty()) return std::string();
-    std::string v = it->second[0];
+    std::string_view x;
+    if (!r.first(k, x)) return std::string();
+    std::string v(x);
     if (v.size() >= 2 && (v.front() == '\'' || v.front() == '"') && v.back() == v.front()) v = v.substr(1, v.size() - 2);
     return v;
   }
@@ -1412,7 +1489,10 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
   m.colInd.reserve(m.rowPtr[m.neq]);
   for (int i = 0; i < m.neq; ++i) m.colInd.insert(m.colInd.end(), rows[i].begin(), rows[i].end());
   // slot <- (element, entry) lists, in element order (deterministic summation order)
-  std::vector<std::vector<int>> slotList(m.colInd.size());
+  // (slot, source) pairs in visiting order, then a stable counting sort by
+  // slot: each slot's list keeps the visiting order
+  std::vector<std::pair<int, int>> slotPairs;
+  slotPairs.reserve((size_t)144 * m.nel + (size_t)36 * m.nax);
   for (int e = 0; e < m.nel; ++e) {
     const int c = m.elCx[e];
     const int n = c < 0 ? 12 : m.cxNx[c];
@@ -1424,7 +1504,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       for (int j = 0; j < n; ++j) {
         if (q[j] < 0) continue;
         int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
-        slotList[slot].push_back(c < 0 ? 144 * e + i + 12 * j : xMatBase + m.cxMatOff[c] + i + n * j);
+        slotPairs.push_back({slot, c < 0 ? 144 * e + i + 12 * j : xMatBase + m.cxMatOff[c] + i + n * j});
       }
     }
   }
@@ -1438,7 +1518,7 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       for (int j = 0; j < n; ++j) {
         if (q[j] < 0) continue;
         int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
-        slotList[slot].push_back(xMatBase + m.pXMatOff[p] + i + n * j);
+        slotPairs.push_back({slot, xMatBase + m.pXMatOff[p] + i + n * j});
       }
     }
   }
@@ -1451,13 +1531,18 @@ int buildModel(const char* fsi, int argc, const char* const* argv, HostModel& m,
       for (int j = 0; j < 6; ++j) {
         if (q[j] < 0) continue;
         int slot = (int)(std::lower_bound(b, en, q[j]) - &m.colInd[0]);
-        slotList[slot].push_back(144 * m.nel + 36 * a + i + 6 * j);
+        slotPairs.push_back({slot, 144 * m.nel + 36 * a + i + 6 * j});
       }
     }
   }
   m.slotPtr.assign(m.colInd.size() + 1, 0);
-  for (size_t s = 0; s < slotList.size(); ++s) m.slotPtr[s + 1] = m.slotPtr[s] + (int)slotList[s].size();
-  for (auto& l : slotList) m.slotSrc.insert(m.slotSrc.end(), l.begin(), l.end());
+  for (const auto& sp : slotPairs) ++m.slotPtr[sp.first + 1];
+  for (size_t s = 0; s < m.colInd.size(); ++s) m.slotPtr[s + 1] += m.slotPtr[s];
+  m.slotSrc.assign(slotPairs.size(), 0);
+  {
+    std::vector<int> cur(m.slotPtr.begin(), m.slotPtr.end() - 1);
+    for (const auto& sp : slotPairs) m.slotSrc[cur[sp.first]++] = sp.second;
+  }
   // equation <- (element, local DOF) lists
   std::vector<std::vector<int>> eqList(m.neq);
   for (int e = 0; e < m.nel; ++e) {
