@@ -329,6 +329,18 @@ def served_leg(args, share, compare_batched=True):
                                  "text (host threads) and any wait for admission included",
            "pool": f"{len(pool)} models, 1k-200k DOF log-uniform, 100-2000 steps log-uniform x "
                    f"{args.serve_steps_scale}"}
+    if compare_batched and not args.no_oracle:
+        # the same requests on the CPU oracle, all host threads, one request per
+        # thread at a time (set-up inside the timed region), as a like-for-like
+        # CPU baseline of the served workload
+        threads = os.cpu_count() or 1
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        reqs = [(pool[int(q)][0], pool[int(q)][1], pool[int(q)][2]) for q in pick]
+        c_dt, c_its, _, _, _ = oracle_full_run(reqs, threads)
+        out["cpu_baseline_same_requests"] = {
+            "value": c_its / c_dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the {n_req} served requests, each from its text to its end time ({c_its} Newton "
+                      f"iterations, {c_dt:.1f} s), one request per thread at a time"}
     if compare_batched:
         # the same requests as one batch (all present at once): device throughput
         b = Batch(kept, mixed=True, sweeps=args.sweeps)
@@ -601,7 +613,7 @@ def main():
     lib = fedem_gb300.load_library()
     dev, bus = rank_device(local, lib)
     if args.served_only:
-        out = {"served": served_leg(args, args.serve_slot_reuse, compare_batched=False)}
+        out = {"served": served_leg(args, args.serve_slot_reuse)}
         print(json.dumps(out), flush=True)
         return
     if args.single_models_only:

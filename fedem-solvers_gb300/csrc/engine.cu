@@ -1277,7 +1277,7 @@ std::map<std::string, std::array<int, 4>> g_shapeCache;  // batch structure -> t
 
 int Engine::setLaunchShape(const int* sh) {
   if (iterated_) return -1;
-  if (sh[0] < 0 || sh[0] > 1) return -2;
+  if (sh[0] < 0 || sh[0] > 2) return -2;
   for (int k = 1; k <= 2; ++k)
     if (sh[k] != 4 && sh[k] != 8 && sh[k] != 16) return -2;
   if (sh[3] != 2 && sh[3] != 4 && sh[3] != 8) return -2;
@@ -1361,7 +1361,7 @@ int Engine::autotune() {
   {
     float best = -1.f;
     int pick = 0;
-    for (int pv = 0; pv <= 1; ++pv) {
+    for (int pv = 0; pv <= 2; ++pv) {
       pplan_.factorPanel = pv;
       const float t = timeIt([&] { resetIterationCounters(stream_); },
                              [&] { launchFactorForwardCascade(d_, pplan_, f32, rhs, stream_); });

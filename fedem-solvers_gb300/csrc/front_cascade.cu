@@ -46,127 +46,142 @@ namespace {
 __device__ inline bool singularPivot(float dk, float d0, double tol) { return !(fabsf(dk) > (float)tol * fabsf(d0)); }
 __device__ inline bool singularPivot(double dk, double d0, double tol) { return !(fabs(dk) > tol * fabs(d0)); }
 
-// Two panel factorisations of the small fronts, the same arithmetic in the
-// same order (so the same factor to the last bit), picked per batch by the
+// Panel factorisations of the small fronts, all with the same arithmetic in
+// the same order (so the same factor to the last bit), picked per batch by the
 // engine's autotuner: pivot by pivot with the multipliers passed by shuffles
 // and the rows kept in shared memory (few registers, high occupancy), or
 // register-blocked (fewer instructions and shared-memory accesses, more
-// registers).
+// registers) in blocks of 8 or 4 pivots.
 constexpr int kPanelShuffle = 0;
-constexpr int kPanelRegisters = 1;
-// pivot columns per block of the register-blocked panel factorisation
-constexpr int kPanelBlock = 8;
+constexpr int kPanelRegisters = 1;   // blocks of 8 pivots, fronts up to 64 rows
+constexpr int kPanelRegisters4 = 2;  // blocks of 4 pivots, one row per lane (fronts up to 32 rows)
+
+// pivot by pivot: rows lane and lane + 32 in shared memory; the multipliers of
+// the pivot rows (lanes below np) are passed by shuffles, one barrier per pivot
+template <typename T>
+__device__ void panelShuffle(T* F, const T* diag0, int nr, int np, int lane, double tolFact, int& neg, bool& sing) {
+  const int i0 = lane, i1 = lane + 32;
+  for (int k = 0; k < np; ++k) {
+    const T dk = F[k + nr * k];
+    const bool bad = singularPivot(dk, diag0[k], tolFact);
+    sing |= bad;
+    if (dk < T(0)) ++neg;
+    const T inv = bad ? T(0) : T(1) / dk;
+    const bool r0 = i0 > k && i0 < nr, r1 = i1 > k && i1 < nr;
+    const T f0 = r0 ? F[i0 + nr * k] : T(0), f1 = r1 ? F[i1 + nr * k] : T(0);
+    const T l0 = f0 * inv, l1 = f1 * inv;
+    for (int j = k + 1; j < np; ++j) {
+      const T lj = __shfl_sync(0xffffffffu, l0, j);
+      if (r0 && j <= i0) F[i0 + nr * j] -= f0 * lj;
+      if (r1) F[i1 + nr * j] -= f1 * lj;
+    }
+    if (r0) {
+      if (i0 >= np) F[k + nr * i0] = f0;
+      F[i0 + nr * k] = l0;
+    }
+    if (r1) {
+      if (i1 >= np) F[k + nr * i1] = f1;
+      F[i1 + nr * k] = l1;
+    }
+    __syncwarp();
+  }
+}
+
+// register-blocked in blocks of PB pivots (TWO: a second row per lane, fronts
+// of up to 64 rows; else at most 32 rows)
+template <typename T, int PB, bool TWO>
+__device__ void panelRegisters(T* F, const T* diag0, int nr, int np, int lane, double tolFact, int& neg,
+                               bool& sing) {
+  // Register-blocked panel: lane r owns rows r and r + 32; the pivot columns
+  // are taken PB at a time.  Inside a block the row values sit in
+  // registers and each multiplier l_jk is passed by a shuffle from the lane
+  // owning row j; the block's columns are then stored (l_ik below the
+  // diagonal, the unscaled value of an update row in its upper position),
+  // and the later pivot columns receive the block's updates all at once,
+  // l_jk read from shared memory (one broadcast load per value).  Every
+  // entry receives the same multiply-subtracts in the same order as in a
+  // right-looking elimination one pivot at a time, so the factor is the same
+  // to the last bit, with a fraction of the shared-memory traffic and no
+  // barrier per pivot.
+  const int i0 = lane, i1 = lane + 32;
+  const bool two = TWO && nr > 32;     // warp-uniform: a second row per lane
+  const bool h1 = two && i1 < nr;      // row i1 exists (it is below every pivot: np <= 32)
+  for (int k0 = 0; k0 < np; k0 += PB) {
+    const int kb = min(PB, np - k0);
+    const bool h0 = i0 >= k0 && i0 < nr;
+    T a0[PB], a1[PB];
+#pragma unroll
+    for (int kk = 0; kk < PB; ++kk) {
+      a0[kk] = (kk < kb && h0) ? F[i0 + nr * (k0 + kk)] : T(0);
+      a1[kk] = (kk < kb && h1) ? F[i1 + nr * (k0 + kk)] : T(0);
+    }
+#pragma unroll
+    for (int kk = 0; kk < PB; ++kk) {
+      if (kk >= kb) break;  // warp-uniform
+      const int k = k0 + kk;
+      const T dk = __shfl_sync(0xffffffffu, a0[kk], k);  // row k < 32 is lane k's first row
+      const bool bad = singularPivot(dk, diag0[k], tolFact);
+      sing |= bad;
+      if (dk < T(0)) ++neg;
+      const T inv = bad ? T(0) : T(1) / dk;
+      const bool r0 = i0 > k && i0 < nr;
+      const T f0 = r0 ? a0[kk] : T(0), f1 = h1 ? a1[kk] : T(0);
+      const T l0 = f0 * inv, l1 = f1 * inv;
+#pragma unroll
+      for (int jj = kk + 1; jj < PB; ++jj) {
+        if (jj >= kb) break;
+        const T lj = __shfl_sync(0xffffffffu, l0, k0 + jj);
+        if (r0 && k0 + jj <= i0) a0[jj] -= f0 * lj;
+        if (h1) a1[jj] -= f1 * lj;
+      }
+      if (i0 == k) F[k + nr * k] = dk;
+      if (r0) {
+        F[i0 + nr * k] = l0;
+        if (i0 >= np) F[k + nr * i0] = f0;
+        a0[kk] = f0;
+      }
+      if (h1) {
+        F[i1 + nr * k] = l1;
+        if (i1 >= np) F[k + nr * i1] = f1;
+        a1[kk] = f1;
+      }
+    }
+    __syncwarp();
+    // the later pivot columns j (row i >= j): C(i, j) -= f_i,k l_j,k over the block's k in order
+    for (int j = k0 + kb; j < np; ++j) {
+      T lj[PB];
+#pragma unroll
+      for (int kk = 0; kk < PB; ++kk) lj[kk] = kk < kb ? F[j + nr * (k0 + kk)] : T(0);
+      if (i0 >= j && i0 < nr) {
+        T c = F[i0 + nr * j];
+#pragma unroll
+        for (int kk = 0; kk < PB; ++kk)
+          if (kk < kb) c -= a0[kk] * lj[kk];
+        F[i0 + nr * j] = c;
+      }
+      if (h1) {
+        T c = F[i1 + nr * j];
+#pragma unroll
+        for (int kk = 0; kk < PB; ++kk)
+          if (kk < kb) c -= a1[kk] * lj[kk];
+        F[i1 + nr * j] = c;
+      }
+    }
+    __syncwarp();
+  }
+}
 
 template <typename T, int PANEL>
 __device__ void factorBlocked(T* F, T* lcol, const T* diag0, int nr, int np, int lane, double tolFact, int& neg,
                               bool& sing, T* Uout) {
   if (np <= 32 && nr <= 64) {
-    if constexpr (PANEL == kPanelShuffle) {
-      // rows lane and lane + 32; the multipliers of the pivot rows (lanes below
-      // np) are passed by shuffles, one barrier per pivot
-      const int i0 = lane, i1 = lane + 32;
-      for (int k = 0; k < np; ++k) {
-        const T dk = F[k + nr * k];
-        const bool bad = singularPivot(dk, diag0[k], tolFact);
-        sing |= bad;
-        if (dk < T(0)) ++neg;
-        const T inv = bad ? T(0) : T(1) / dk;
-        const bool r0 = i0 > k && i0 < nr, r1 = i1 > k && i1 < nr;
-        const T f0 = r0 ? F[i0 + nr * k] : T(0), f1 = r1 ? F[i1 + nr * k] : T(0);
-        const T l0 = f0 * inv, l1 = f1 * inv;
-        for (int j = k + 1; j < np; ++j) {
-          const T lj = __shfl_sync(0xffffffffu, l0, j);
-          if (r0 && j <= i0) F[i0 + nr * j] -= f0 * lj;
-          if (r1) F[i1 + nr * j] -= f1 * lj;
-        }
-        if (r0) {
-          if (i0 >= np) F[k + nr * i0] = f0;
-          F[i0 + nr * k] = l0;
-        }
-        if (r1) {
-          if (i1 >= np) F[k + nr * i1] = f1;
-          F[i1 + nr * k] = l1;
-        }
-        __syncwarp();
-      }
+    if constexpr (PANEL == kPanelRegisters) {
+      panelRegisters<T, 8, true>(F, diag0, nr, np, lane, tolFact, neg, sing);
+    } else if constexpr (PANEL == kPanelRegisters4) {
+      if (nr <= 32) panelRegisters<T, 4, false>(F, diag0, nr, np, lane, tolFact, neg, sing);
+      else panelShuffle<T>(F, diag0, nr, np, lane, tolFact, neg, sing);
     } else {
-      // Register-blocked panel: lane r owns rows r and r + 32; the pivot columns
-      // are taken kPanelBlock at a time.  Inside a block the row values sit in
-      // registers and each multiplier l_jk is passed by a shuffle from the lane
-      // owning row j; the block's columns are then stored (l_ik below the
-      // diagonal, the unscaled value of an update row in its upper position),
-      // and the later pivot columns receive the block's updates all at once,
-      // l_jk read from shared memory (one broadcast load per value).  Every
-      // entry receives the same multiply-subtracts in the same order as in a
-      // right-looking elimination one pivot at a time, so the factor is the same
-      // to the last bit, with a fraction of the shared-memory traffic and no
-      // barrier per pivot.
-      const int i0 = lane, i1 = lane + 32;
-      const bool two = nr > 32;            // warp-uniform: a second row per lane
-      const bool h1 = two && i1 < nr;      // row i1 exists (it is below every pivot: np <= 32)
-      for (int k0 = 0; k0 < np; k0 += kPanelBlock) {
-        const int kb = min(kPanelBlock, np - k0);
-        const bool h0 = i0 >= k0 && i0 < nr;
-        T a0[kPanelBlock], a1[kPanelBlock];
-  #pragma unroll
-        for (int kk = 0; kk < kPanelBlock; ++kk) {
-          a0[kk] = (kk < kb && h0) ? F[i0 + nr * (k0 + kk)] : T(0);
-          a1[kk] = (kk < kb && h1) ? F[i1 + nr * (k0 + kk)] : T(0);
-        }
-  #pragma unroll
-        for (int kk = 0; kk < kPanelBlock; ++kk) {
-          if (kk >= kb) break;  // warp-uniform
-          const int k = k0 + kk;
-          const T dk = __shfl_sync(0xffffffffu, a0[kk], k);  // row k < 32 is lane k's first row
-          const bool bad = singularPivot(dk, diag0[k], tolFact);
-          sing |= bad;
-          if (dk < T(0)) ++neg;
-          const T inv = bad ? T(0) : T(1) / dk;
-          const bool r0 = i0 > k && i0 < nr;
-          const T f0 = r0 ? a0[kk] : T(0), f1 = h1 ? a1[kk] : T(0);
-          const T l0 = f0 * inv, l1 = f1 * inv;
-  #pragma unroll
-          for (int jj = kk + 1; jj < kPanelBlock; ++jj) {
-            if (jj >= kb) break;
-            const T lj = __shfl_sync(0xffffffffu, l0, k0 + jj);
-            if (r0 && k0 + jj <= i0) a0[jj] -= f0 * lj;
-            if (h1) a1[jj] -= f1 * lj;
-          }
-          if (i0 == k) F[k + nr * k] = dk;
-          if (r0) {
-            F[i0 + nr * k] = l0;
-            if (i0 >= np) F[k + nr * i0] = f0;
-            a0[kk] = f0;
-          }
-          if (h1) {
-            F[i1 + nr * k] = l1;
-            if (i1 >= np) F[k + nr * i1] = f1;
-            a1[kk] = f1;
-          }
-        }
-        __syncwarp();
-        // the later pivot columns j (row i >= j): C(i, j) -= f_i,k l_j,k over the block's k in order
-        for (int j = k0 + kb; j < np; ++j) {
-          T lj[kPanelBlock];
-  #pragma unroll
-          for (int kk = 0; kk < kPanelBlock; ++kk) lj[kk] = kk < kb ? F[j + nr * (k0 + kk)] : T(0);
-          if (i0 >= j && i0 < nr) {
-            T c = F[i0 + nr * j];
-  #pragma unroll
-            for (int kk = 0; kk < kPanelBlock; ++kk)
-              if (kk < kb) c -= a0[kk] * lj[kk];
-            F[i0 + nr * j] = c;
-          }
-          if (h1) {
-            T c = F[i1 + nr * j];
-  #pragma unroll
-            for (int kk = 0; kk < kPanelBlock; ++kk)
-              if (kk < kb) c -= a1[kk] * lj[kk];
-            F[i1 + nr * j] = c;
-          }
-        }
-        __syncwarp();
-      }
+      panelShuffle<T>(F, diag0, nr, np, lane, tolFact, neg, sing);
     }
   } else {
     for (int k = 0; k < np; ++k) {
@@ -787,6 +802,9 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
     if (p.factorPanel == kPanelRegisters)
       factorCascade(kFactorForwardCascade<float, kPanelRegisters>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
                     d.x32, d.w32, s);
+    else if (p.factorPanel == kPanelRegisters4)
+      factorCascade(kFactorForwardCascade<float, kPanelRegisters4>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol,
+                    rhs, d.x32, d.w32, s);
     else
       factorCascade(kFactorForwardCascade<float, kPanelShuffle>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
                     d.x32, d.w32, s);
@@ -795,6 +813,9 @@ void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool 
     const size_t sm = (size_t)wpb * perWarp * sizeof(double);
     if (p.factorPanel == kPanelRegisters)
       factorCascade(kFactorForwardCascade<double, kPanelRegisters>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol,
+                    rhs, d.x64, d.w64, s);
+    else if (p.factorPanel == kPanelRegisters4)
+      factorCascade(kFactorForwardCascade<double, kPanelRegisters4>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol,
                     rhs, d.x64, d.w64, s);
     else
       factorCascade(kFactorForwardCascade<double, kPanelShuffle>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol, rhs,

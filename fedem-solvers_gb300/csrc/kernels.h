@@ -122,6 +122,7 @@ struct PersistentPlan {
   // changes a result bit: tasks are taken dynamically, and each front's
   // arithmetic is the same whichever warp, block or cluster does it.
   int factorPanel = 0;     // small-front panel factorisation: 0 shuffles, 1 register-blocked
+                           // (blocks of 8), 2 register-blocked (blocks of 4, fronts up to 32 rows)
   int forwardWarps = 8;    // warps per block of the forward-elimination cascade
   int backwardWarps = 8;   // warps per block of the back-substitution queue
   int largeCluster = 8;    // blocks per cluster of the large-front factorisation (2, 4 or 8)

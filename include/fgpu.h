@@ -125,7 +125,9 @@ long long fgpu_batch_phase_timings_n(fgpu_batch* b, double* ms, int n, long long
 int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
 
 /* Launch shapes of the multifrontal kernels, shape4 = {small-front panel
- * factorisation (0: pivot by pivot with shuffles, 1: register-blocked),
+ * factorisation (0: pivot by pivot with shuffles, 1: register-blocked in
+ * blocks of 8 pivots, 2: register-blocked in blocks of 4 for fronts of up to
+ * 32 rows),
  * warps per block of the forward-elimination cascade (4, 8 or 16), warps per
  * block of the back-substitution queue (4, 8 or 16), blocks per cluster of the
  * large-front factorisation (2, 4 or 8)}.  The autotuner picks them before a

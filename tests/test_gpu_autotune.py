@@ -2,17 +2,18 @@
 candidate shapes of the multifrontal kernels (panel variant of the small-front
 factorisation, warps per block of the forward and backward solves, cluster
 size of the large-front factorisation) on the batch's own fronts and keeps the
-fastest.  Only shapes that leave every result bit unchanged are candidates, so
-a batch run with the tuned shapes, with any fixed shape, or with the shapes
-reused from an earlier batch of the same structure gives bitwise the same
-results.  Checked on beam chains (small fronts only) and on the space-frame
+fastest.  Only shapes that leave every result bit unchanged are candidates
+(the three panel variants perform the same multiply-subtracts in the same
+order), so a batch run with the tuned shapes, with any fixed shape, or with
+the shapes reused from an earlier batch of the same structure gives bitwise
+the same results.  Checked on beam chains (small fronts only) and on the space-frame
 tower (large fronts on clusters), FP64 and mixed precision."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(1, 4, 16, 2), (0, 16, 4, 4), (1, 8, 8, 8)]
+SHAPES = [(1, 4, 16, 2), (0, 16, 4, 4), (2, 8, 8, 8)]
 
 
 def _cases(kind):
@@ -43,7 +44,7 @@ def test_every_shape_gives_the_same_bits(gpu, kind, mixed):
     cases = _cases(kind)
     ref, its, sh, ms, tuned = _run(cases, mixed)
     assert tuned
-    assert sh["panel"] in (0, 1) and sh["forward_warps"] in (4, 8, 16)
+    assert sh["panel"] in (0, 1, 2) and sh["forward_warps"] in (4, 8, 16)
     assert sh["backward_warps"] in (4, 8, 16) and sh["large_cluster"] in (2, 4, 8)
     for shape in SHAPES:
         x, it, sh2, ms2, tuned2 = _run(cases, mixed, shape)
