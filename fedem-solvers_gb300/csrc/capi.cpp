@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -90,6 +91,23 @@ std::string optionValue(int argc, char** argv, const char* key) {
   return std::string();
 }
 
+// a boolean option: -key, -key+ or -key=true/1 sets it, -key- or -key=false/0 clears it
+bool optionBool(int argc, char** argv, const char* key, bool def) {
+  const std::string k = std::string("-") + key;
+  bool v = def;
+  for (int a = 0; a < argc; ++a) {
+    if (!argv || !argv[a]) continue;
+    const std::string s(argv[a]);
+    if (s == k || s == k + "+") v = true;
+    else if (s == k + "-") v = false;
+    else if (s.compare(0, k.size() + 1, k + "=") == 0) {
+      const std::string w = s.substr(k.size() + 1);
+      v = !(w == "0" || w == "false" || w == "f" || w == "no" || w == "off");
+    }
+  }
+  return v;
+}
+
 bool hasFlag(int argc, char** argv, const char* key) {
   std::string k = std::string("-") + key;
   for (int a = 0; a < argc; ++a)
@@ -171,6 +189,16 @@ int solverInit(int argc, char** argv, const char* cfsi, const double* stateData,
   if (stateData && ndat > 0) {  // restart from an in-core state array (saveState of the same model)
     if ((size_t)ndat * sizeof(double) < s->engine->stateBytes()) return fail(-2, "state array too short");
     if (s->engine->restoreStateFrom(stateData)) return fail(-3, "restoring the state failed");
+  }
+  // primary response database (solverModule.f90:352, saveStep at :512-513 and
+  // after every step; -double1, -savestart as solverInterface.C:390-391)
+  const std::string frs1 = optionValue(argc, argv, "frs1file");
+  if (!frs1.empty()) {
+    const std::string ss = optionValue(argc, argv, "savestart");
+    const std::vector<std::string> paths{frs1};
+    if ((rc = s->engine->resultsOpen("", optionBool(argc, argv, "double1", true), err, &paths,
+                                     ss.empty() ? 0.0 : std::atof(ss.c_str()))))
+      return fail(rc, err);
   }
   g_core = std::move(s);
   return 0;

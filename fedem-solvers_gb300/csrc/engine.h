@@ -152,7 +152,10 @@ class Engine {
   // Results database of the primary response (results.cu): from now on every
   // model appends one record per completed time step to <dir>/model<k>.res
   // (a record of the current state first).  resultsClose flushes and closes.
-  int resultsOpen(const std::string& dir, bool asDouble, std::string& err);
+  // paths: one file per model instead of <dir>/model<k>.res; records of times
+  // before saveStart are not written (the reference's -savestart)
+  int resultsOpen(const std::string& dir, bool asDouble, std::string& err,
+                  const std::vector<std::string>* paths = nullptr, double saveStart = -1.0e300);
   int resultsClose(std::string& err);
 
  private:
@@ -172,6 +175,7 @@ class Engine {
   // results database: ring plan, files and the records already written per model
   struct Results {
     bool on = false, asDouble = true;
+    double saveStart = -1.0e300, epsT = 0.0;
     RecordPlan plan;
     std::vector<FILE*> files;
     std::vector<int> vals;

@@ -73,7 +73,8 @@ void launchRecordStep(const DevData& d, const RecordPlan& r, bool all, cudaStrea
   if (d.m.n > 0) kRecordStep<<<d.m.n, 128, 0, s>>>(d, r, all ? 1 : 0);
 }
 
-int Engine::resultsOpen(const std::string& dir, bool asDouble, std::string& err) {
+int Engine::resultsOpen(const std::string& dir, bool asDouble, std::string& err,
+                        const std::vector<std::string>* paths, double saveStart) {
   if (rec_.on) {
     err = "the results database is already open";
     return -1;
@@ -118,7 +119,8 @@ int Engine::resultsOpen(const std::string& dir, bool asDouble, std::string& err)
     vals[m] = v;
     off[m] = tot;
     tot += (long long)v * r.ring;
-    const std::string path = dir + "/model" + std::to_string(m) + ".res";
+    const std::string path =
+        paths && m < (int)paths->size() ? (*paths)[m] : dir + "/model" + std::to_string(m) + ".res";
     FILE* f = fopen(path.c_str(), "wb");
     if (!f) {
       err = "cannot open " + path;
@@ -171,6 +173,9 @@ int Engine::resultsOpen(const std::string& dir, bool asDouble, std::string& err)
   cudaMemcpyAsync(r.partRec, partRec.data(), sizeof(int) * partRec.size(), cudaMemcpyHostToDevice, stream_);
   rec_.vals = vals;
   rec_.off = off;
+  // no save before saveStart (solverRoutinesModule.f90:590-592: time + 0.1 minInc < saveStart)
+  rec_.saveStart = saveStart;
+  rec_.epsT = nm > 0 ? 0.1 * hm_[0]->ctl.minInc : 0.0;
   rec_.written.assign(nm, 0);
   rec_.on = true;
   // the batched iteration is captured again with the record kernel in it
@@ -217,6 +222,7 @@ int Engine::resultsDrain(std::string& err) {
     std::vector<float> fl(rec_.asDouble ? 0 : v - 2);
     for (long long k = 0; k < n; ++k) {
       const double* rec = rec_.host.data() + (size_t)k * v;
+      if (rec[1] + rec_.epsT < rec_.saveStart) continue;
       const int step = (int)rec[0];
       fwrite(&step, sizeof(int), 1, f);
       fwrite(rec + 1, sizeof(double), 1, f);

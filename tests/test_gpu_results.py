@@ -108,3 +108,34 @@ def test_reduced_parts_records(gpu, tmp_path):
             off += 3
     assert nt == tri.shape[0]
     b.close()
+
+
+def test_frs1file_through_the_solver_abi(gpu, tmp_path):
+    """The reference's own options on solverInit: -frs1file names the primary
+    response database, -savestart skips the states before that time
+    (solverModule.f90:352, solverRoutinesModule.f90:590-592); the records equal
+    the triad positions getStateVar reports after each step."""
+    from fedem_gb300 import models
+    from fedem_gb300.results import read_results
+    from fedem_gb300.solver import FedemSolver
+
+    n_el = 16
+    fsi = models.beam_chain_fsi(n_el, 0.25, 0.1, 0.01, clamp=0, load_node=n_el, load_dof=2, load=1500.0,
+                                **models.STEEL)
+    path = tmp_path / "primary.frs"
+    opts = ["-timeInc=0.001", "-timeEnd=0.03", "-alphaNewmark=0.1", "-tolDispNorm=1.0e-10",
+            f"-frs1file={path}", "-savestart=0.01"]
+    s = FedemSolver(solver_options=opts, fsi=fsi)
+    hist = []
+    while s.solve_next():
+        hist.append(np.array([s.get_state_var(t + 1) for t in range(n_el + 1)]))
+    hist.append(np.array([s.get_state_var(t + 1) for t in range(n_el + 1)]))
+    assert s.ierr.value == 0
+    s.solver_done()
+    r = read_results(path)
+    assert r["precision"] == "double"
+    np.testing.assert_array_equal(r["steps"], np.arange(10, 31))
+    assert abs(r["times"][0] - 0.01) < 1e-12
+    pos = r["triad_positions"][:, :, :, 3]
+    for k, step in enumerate(r["steps"]):
+        np.testing.assert_array_equal(pos[k], hist[step - 1])
