@@ -109,6 +109,7 @@ __device__ inline void seedBackward(const BackwardSeed& b, int i) {
 }
 
 __global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl, BackwardSeed bs) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
   int st = m.state[i], fl = 0;
@@ -168,6 +169,7 @@ __global__ void kBeginStep(DevModels m, int* activeCount, long long* activeEl, B
 
 // predicted velocity/acceleration increments and the actual inertia force
 __global__ void kPredictDofs(DevData d) {
+  pdlEntry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ndofTot) {
     int m = d.dofModel[i];
@@ -269,6 +271,7 @@ __device__ inline void rotateStore(const double* S, const double* f, double* out
 }
 
 __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
+  pdlEntry();
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int nel = d.nelTot;
   if (e >= nel) return;
@@ -454,6 +457,7 @@ __global__ void __launch_bounds__(128) kElements(DevData d, int mode) {
 // axial springs and dampers: direction, length, forces (UpdateSprings/UpdateDampers,
 // calcSpringForces, addInDampingForces, calcDamperForces); same pass gating as kElements
 __global__ void kAxial(DevData d, int mode) {
+  pdlEntry();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int nax = d.naxTot;
   if (a >= nax) return;
@@ -541,6 +545,7 @@ __global__ void kAxial(DevData d, int mode) {
 // spring (calcSpringStiffness, no geometric stiffness) or n n^T d0 sC for a damper
 // (addInDamperMat)
 __global__ void kAxialNewton(DevData d) {
+  pdlEntry();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int nax = d.naxTot;
   if (a >= nax) return;
@@ -577,6 +582,7 @@ __global__ void kAxialNewton(DevData d) {
 
 // residual: force predictor (7.53) or corrector (7.55); RHS del = residual
 __global__ void kResidual(DevData d) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
   // the list of the equation's first two contributions is read with the model's
@@ -652,6 +658,7 @@ __global__ void kResidual(DevData d) {
 
 // element Newton matrix N = sM*M + sC*stifScl*C + sK*stifScl*K (rebuilt when the scales change)
 __global__ void kBuildElementNewton(DevData d) {
+  pdlEntry();
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int nel = d.nelTot;
   if (e >= nel) return;
@@ -672,6 +679,7 @@ __global__ void kBuildElementNewton(DevData d) {
 
 // rotate the element Newton matrix to system axes: Ns = R N R^T blockwise
 __global__ void __launch_bounds__(128) kRotateElementNewton(DevData d) {
+  pdlEntry();
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int nel = d.nelTot;
   if (e >= nel) return;
@@ -743,6 +751,7 @@ __device__ inline void rotPair(const double* R, double p, double q, double* S) {
 }
 
 __global__ void __launch_bounds__(128) kNewtonBeam(DevData d) {
+  pdlEntry();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int nel = d.nelTot;
   if (e >= nel) return;
@@ -796,6 +805,7 @@ __device__ __forceinline__ double gatherEntry(const DevData& d, int src, int64_t
 // other models are skipped by a flag test (32 slot blocks per round of loads)
 // instead of a block launch each.
 __global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather(DevData d, int nSlotBlocks) {
+  pdlEntry();
   constexpr int R = kGatherSlotsPerThread;
   const int64_t lim = (int64_t)144 * d.nelTot;
   const int lane = threadIdx.x & 31;
@@ -862,6 +872,7 @@ __global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather
 
 // increment: expand the solution, update velocities/accelerations and triads
 __global__ void kIncrement(DevData d) {
+  pdlEntry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ndofTot) {
     int m = d.dofModel[i];
@@ -916,6 +927,7 @@ __global__ void kIncrement(DevData d) {
 // prescribed deflections at the start of a step (motionRoutinesModule.f90:58-193):
 // cc = D - Dprev, or the total D in a linear quasi-static step
 __global__ void kMotions(DevData d) {
+  pdlEntry();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.nmotTot) return;
   const int m = d.motModel[k], fl = d.m.flags[m];
@@ -928,6 +940,7 @@ __global__ void kMotions(DevData d) {
 
 // engine-driven point loads at the new time (forceRoutinesModule.f90:52-131)
 __global__ void kLoads(DevData d) {
+  pdlEntry();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.nldTot) return;
   const int eq = d.ldEq[k], m = d.eqModel[eq];
@@ -948,6 +961,7 @@ __global__ void kLoads(DevData d) {
 // columns of the prescribed DOFs, moved to the right-hand side (terms with
 // |cc| <= 1e-15 skipped, sysMatrixTypeModule.f90:2099-2259)
 __global__ void kMotionRhs(DevData d) {
+  pdlEntry();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.nmrTot) return;
   const int eq = d.mrEq[k];
@@ -964,6 +978,7 @@ __global__ void kMotionRhs(DevData d) {
 // a pure linear quasi-static step restarts from the state after the initial
 // configuration (restoreLastStep, solverRoutinesModule.f90:920-970)
 __global__ void kQsRestore(DevData d) {
+  pdlEntry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int want = FL_PRED | FL_QSTATIC | FL_LINEAR;
   if (i < d.ntriTot && (d.m.flags[d.triModel[i]] & want) == want)
@@ -1031,6 +1046,7 @@ __device__ inline unsigned long long absBits(double x) {
 __device__ inline unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
 __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
+  pdlEntry();
   __shared__ double sh[CHUNK_TPB / 32][NPART];
   const int c = blockIdx.x;
   const int m = d.chunkModel[c];
@@ -1126,6 +1142,7 @@ __global__ void __launch_bounds__(CHUNK_TPB) kNormsPartial(DevData d) {
 // one warp per model: lane k combines partial value k over the model's chunks
 // in chunk order, lane 0 evaluates the norms and the test
 __global__ void kControl(DevData d) {
+  pdlEntry();
   const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (m >= d.m.n) return;
@@ -1200,6 +1217,7 @@ __global__ void kControl(DevData d) {
 // terminateStep (solverRoutinesModule.f90:728-827): orthonormalise the triad
 // rotations of models that finished a step; keep their deformation for the next one
 __global__ void kStepEnd(DevData d) {
+  pdlEntry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ntriTot) {
     if ((d.m.flags[d.triModel[i]] & FL_STEPDONE) && d.triNdof[i] == 6) orthonormRot(d.ur + 12 * (size_t)i);
@@ -1220,11 +1238,13 @@ __global__ void kStepEnd(DevData d) {
 // ---------------------------------------------------------------------------
 // backward queues of the active models, for solves outside a step start
 __global__ void kSeedBackward(DevModels m, BackwardSeed bs) {
+  pdlEntry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < m.n && (m.flags[i] & FL_ACTIVE)) seedBackward(bs, i);
 }
 
 __global__ void kStaticBegin(DevModels m, int* activeCount, BackwardSeed bs) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
   if (m.staticDone[i] || m.state[i] == ST_ERROR) { m.flags[i] = 0; return; }
@@ -1240,6 +1260,7 @@ __global__ void kStaticBegin(DevModels m, int* activeCount, BackwardSeed bs) {
 }
 
 __global__ void kStaticResidual(DevData d) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
   int m = d.eqModel[i];
@@ -1267,6 +1288,7 @@ __global__ void kStaticResidual(DevData d) {
 }
 
 __global__ void __launch_bounds__(NTPB) kStaticNorm(DevData d) {
+  pdlEntry();
   __shared__ double sh[NTPB];
   int m = blockIdx.x;
   if (!(d.m.flags[m] & FL_STATIC)) return;
@@ -1292,6 +1314,7 @@ __global__ void __launch_bounds__(NTPB) kStaticNorm(DevData d) {
 }
 
 __global__ void kStaticIncrement(DevData d) {
+  pdlEntry();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < d.ndofTot) {
     int m = d.dofModel[i];
@@ -1329,6 +1352,7 @@ __global__ void kStaticIncrement(DevData d) {
 
 // convergence logic of the static iterations (staticEquilibriumModule.f90:262-371)
 __global__ void kStaticFinish(DevModels m) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.n) return;
   if (!(m.flags[i] & FL_STATIC)) return;
@@ -1353,30 +1377,30 @@ __global__ void kStaticFinish(DevModels m) {
 
 void launchBeginStep(const DevData& d, int* activeCount, long long* activeEl, const BackwardSeed& seed,
                      cudaStream_t s) {
-  kBeginStep<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, activeEl, seed);
+  pdlLaunch(kBeginStep, blocksFor(d.m.n, 128), 128, 0, s, d.m, activeCount, activeEl, seed);
 }
 void launchPredictDofs(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.neqTot ? d.ndofTot : d.neqTot;
-  kPredictDofs<<<blocksFor(n), TPB, 0, s>>>(d);
+  pdlLaunch(kPredictDofs, blocksFor(n), TPB, 0, s, d);
 }
 void launchElements(const DevData& d, int mode, cudaStream_t s) {
   launchJoints(d, mode, s);  // dependent triads first, as UpdateMechanism updates the joints first
-  if (d.nelTot > 0) kElements<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d, mode);
+  if (d.nelTot > 0) pdlLaunch(kElements, blocksFor(d.nelTot, 128), 128, 0, s, d, mode);
   launchParts(d, mode, s);
-  if (d.naxTot > 0) kAxial<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d, mode);
+  if (d.naxTot > 0) pdlLaunch(kAxial, blocksFor(d.naxTot, 128), 128, 0, s, d, mode);
   launchExpandForces(d, mode, s);
 }
 void launchResidual(const DevData& d, cudaStream_t s) {
-  if (d.neqTot > 0) kResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);
+  if (d.neqTot > 0) pdlLaunch(kResidual, blocksFor(d.neqTot), TPB, 0, s, d);
 }
 void launchBuildElementNewton(const DevData& d, cudaStream_t s) {
   // compressed beam batches build N inside kNewtonBeam
-  if (d.nelTot > 0 && !d.beamSparse) kBuildElementNewton<<<blocksFor(d.nelTot), TPB, 0, s>>>(d);
+  if (d.nelTot > 0 && !d.beamSparse) pdlLaunch(kBuildElementNewton, blocksFor(d.nelTot), TPB, 0, s, d);
 }
 void launchRotateElementNewton(const DevData& d, cudaStream_t s) {
-  if (d.nelTot > 0 && d.beamSparse) kNewtonBeam<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
-  else if (d.nelTot > 0) kRotateElementNewton<<<blocksFor(d.nelTot, 128), 128, 0, s>>>(d);
-  if (d.naxTot > 0) kAxialNewton<<<blocksFor(d.naxTot, 128), 128, 0, s>>>(d);
+  if (d.nelTot > 0 && d.beamSparse) pdlLaunch(kNewtonBeam, blocksFor(d.nelTot, 128), 128, 0, s, d);
+  else if (d.nelTot > 0) pdlLaunch(kRotateElementNewton, blocksFor(d.nelTot, 128), 128, 0, s, d);
+  if (d.naxTot > 0) pdlLaunch(kAxialNewton, blocksFor(d.naxTot, 128), 128, 0, s, d);
   launchExpandElements(d, s);
   launchPartsNewton(d, s);
 }
@@ -1398,49 +1422,49 @@ void launchCsrGather(const DevData& d, cudaStream_t s) {
   }
   const int nb = blocksFor(d.nslotTot, kSlotBlock);
   const int grid = bps > 0 && nsm > 0 ? std::min(nb, bps * nsm) : nb;
-  kCsrGather<<<grid, kSlotBlock / kGatherSlotsPerThread, 0, s>>>(d, nb);
+  pdlLaunch(kCsrGather, grid, kSlotBlock / kGatherSlotsPerThread, 0, s, d, nb);
 }
 void launchIncrement(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;
-  kIncrement<<<blocksFor(n), TPB, 0, s>>>(d);
+  pdlLaunch(kIncrement, blocksFor(n), TPB, 0, s, d);
 }
 void launchNormsControl(const DevData& d, cudaStream_t s) {
-  if (d.nchunkTot > 0) kNormsPartial<<<d.nchunkTot, CHUNK_TPB, 0, s>>>(d);
-  kControl<<<blocksFor(32LL * d.m.n, 128), 128, 0, s>>>(d);
+  if (d.nchunkTot > 0) pdlLaunch(kNormsPartial, d.nchunkTot, CHUNK_TPB, 0, s, d);
+  pdlLaunch(kControl, blocksFor(32LL * d.m.n, 128), 128, 0, s, d);
   long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
-  kStepEnd<<<blocksFor(n), TPB, 0, s>>>(d);
+  pdlLaunch(kStepEnd, blocksFor(n), TPB, 0, s, d);
   launchPartsStepEnd(d, s);
 }
 void launchLoads(const DevData& d, cudaStream_t s) {
-  if (d.nldTot > 0) kLoads<<<blocksFor(d.nldTot, 128), 128, 0, s>>>(d);
+  if (d.nldTot > 0) pdlLaunch(kLoads, blocksFor(d.nldTot, 128), 128, 0, s, d);
 }
 void launchMotions(const DevData& d, cudaStream_t s) {
-  if (d.nmotTot > 0) kMotions<<<blocksFor(d.nmotTot, 128), 128, 0, s>>>(d);
+  if (d.nmotTot > 0) pdlLaunch(kMotions, blocksFor(d.nmotTot, 128), 128, 0, s, d);
 }
 void launchMotionRhs(const DevData& d, cudaStream_t s) {
-  if (d.nmrTot > 0) kMotionRhs<<<blocksFor(d.nmrTot, 128), 128, 0, s>>>(d);
+  if (d.nmrTot > 0) pdlLaunch(kMotionRhs, blocksFor(d.nmrTot, 128), 128, 0, s, d);
 }
 void launchQsRestore(const DevData& d, cudaStream_t s) {
   if (!d.urQs) return;
   long long n = std::max<long long>(std::max<long long>(d.ntriTot, d.nelTot), d.ndofTot);
-  kQsRestore<<<blocksFor(n), TPB, 0, s>>>(d);
+  pdlLaunch(kQsRestore, blocksFor(n), TPB, 0, s, d);
 }
 void launchSeedBackward(const DevData& d, const BackwardSeed& seed, cudaStream_t s) {
-  kSeedBackward<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, seed);
+  pdlLaunch(kSeedBackward, blocksFor(d.m.n, 128), 128, 0, s, d.m, seed);
 }
 void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s) {
-  kStaticBegin<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m, activeCount, seed);
+  pdlLaunch(kStaticBegin, blocksFor(d.m.n, 128), 128, 0, s, d.m, activeCount, seed);
 }
 void launchStaticResidual(const DevData& d, cudaStream_t s) {
-  if (d.neqTot > 0) kStaticResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);
+  if (d.neqTot > 0) pdlLaunch(kStaticResidual, blocksFor(d.neqTot), TPB, 0, s, d);
 }
-void launchStaticNorm(const DevData& d, cudaStream_t s) { kStaticNorm<<<d.m.n, NTPB, 0, s>>>(d); }
+void launchStaticNorm(const DevData& d, cudaStream_t s) { pdlLaunch(kStaticNorm, d.m.n, NTPB, 0, s, d); }
 void launchStaticIncrement(const DevData& d, cudaStream_t s) {
   long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;
-  kStaticIncrement<<<blocksFor(n), TPB, 0, s>>>(d);
+  pdlLaunch(kStaticIncrement, blocksFor(n), TPB, 0, s, d);
 }
 void launchStaticFinish(const DevData& d, cudaStream_t s) {
-  kStaticFinish<<<blocksFor(d.m.n, 128), 128, 0, s>>>(d.m);
+  pdlLaunch(kStaticFinish, blocksFor(d.m.n, 128), 128, 0, s, d.m);
 }
 
 }  // namespace fgpu

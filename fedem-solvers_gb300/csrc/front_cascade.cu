@@ -484,6 +484,7 @@ template <typename T, int PANEL>
 __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow,
                                       const T* asmVal, T* Lbase, T* Ubase, double tolFact, const double* rhs, T* X,
                                       T* Wv, int* cnt) {
+  pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int capL = maxRow * maxRow;  // F doubles as the staging area of L
@@ -519,6 +520,7 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
 template <typename T>
 __global__ void kForwardCascade(DevData d, const int* __restrict__ tasks, int nTasks, int maxRow, int capL,
                                 const T* Lbase, const double* rhs, T* X, T* W, int* cnt) {
+  pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* v = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL + 64);
@@ -661,6 +663,7 @@ template <typename T>
 __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
                                const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize,
                                long long spinLimit) {
+  pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
@@ -758,7 +761,7 @@ void factorCascade(void (*kernel)(DevData, const int*, int, int, const T*, T*, T
                    double tol, const double* rhs, T* X, T* W, cudaStream_t s) {
   allowBigSmem(kernel, sm);
   const int blocks = occupancyBlocks(kernel, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-  kernel<<<blocks, 32 * wpb, sm, s>>>(d, p.leaves, p.nLeaves, p.maxRow, asmVal, L, U, tol, rhs, X, W, p.cntFactor);
+  pdlLaunch(kernel, blocks, 32 * wpb, sm, s, d, p.leaves, p.nLeaves, p.maxRow, asmVal, L, U, tol, rhs, X, W, p.cntFactor);
 }
 
 int factorWarpsPerBlock(size_t perWarpBytes) {
@@ -771,6 +774,7 @@ int factorWarpsPerBlock(size_t perWarpBytes) {
 // positive and far from singular, like a Newton matrix's), one thread per front.
 template <typename T>
 __global__ void kProbeEntries(DevData d, T* asmVal) {
+  pdlEntry();
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= d.nfrontTot) return;
   const int nr = d.fNrow[f], na = d.fNasm[f];
@@ -787,8 +791,8 @@ __global__ void kProbeEntries(DevData d, T* asmVal) {
 void launchProbeEntries(const DevData& d, bool fp32, cudaStream_t s) {
   if (d.nfrontTot <= 0) return;
   const int blocks = (d.nfrontTot + 127) / 128;
-  if (fp32) kProbeEntries<float><<<blocks, 128, 0, s>>>(d, d.asmVal32);
-  else kProbeEntries<double><<<blocks, 128, 0, s>>>(d, d.asmVal64);
+  if (fp32) pdlLaunch(kProbeEntries<float>, blocks, 128, 0, s, d, d.asmVal32);
+  else pdlLaunch(kProbeEntries<double>, blocks, 128, 0, s, d, d.asmVal64);
 }
 
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
@@ -840,14 +844,14 @@ void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, 
     const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(float);
     allowBigSmem(kForwardCascade<float>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<float>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
-    kForwardCascade<float><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L32, rhs, d.x32,
+    pdlLaunch(kForwardCascade<float>, blocks, 32 * wpb, sm, s, d, p.tasks, p.nTasks, p.maxRow, capL, d.L32, rhs, d.x32,
                                                        d.w32, cnt);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL + 64) * sizeof(double);
     allowBigSmem(kForwardCascade<double>, sm);
     const int blocks = occupancyBlocks(kForwardCascade<double>, 32 * wpb, sm, (p.nTasks + wpb - 1) / wpb);
-    kForwardCascade<double><<<blocks, 32 * wpb, sm, s>>>(d, p.tasks, p.nTasks, p.maxRow, capL, d.L64, rhs, d.x64,
+    pdlLaunch(kForwardCascade<double>, blocks, 32 * wpb, sm, s, d, p.tasks, p.nTasks, p.maxRow, capL, d.L64, rhs, d.x64,
                                                          d.w64, cnt);
   }
 }
@@ -865,14 +869,14 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(float);
     allowBigSmem(kBackwardQueue<float>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<float>, 32 * wpb, sm, needed);
-    kBackwardQueue<float><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L32, d.x32, queue, ctr, p.bwInline,
+    pdlLaunch(kBackwardQueue<float>, blocks, 32 * wpb, sm, s, d, p.maxRow, capL, d.L32, d.x32, queue, ctr, p.bwInline,
                                                       p.errFlag, acc, fin, p.spinLimit);
   } else {
     const int capL = stagingCapacity(p, sizeof(double));
     const size_t sm = (size_t)wpb * (p.maxRow + capL) * sizeof(double);
     allowBigSmem(kBackwardQueue<double>, sm);
     const int blocks = occupancyBlocks(kBackwardQueue<double>, 32 * wpb, sm, needed);
-    kBackwardQueue<double><<<blocks, 32 * wpb, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline,
+    pdlLaunch(kBackwardQueue<double>, blocks, 32 * wpb, sm, s, d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline,
                                                         p.errFlag, acc, fin, p.spinLimit);
   }
 }
@@ -883,7 +887,7 @@ void launchBackwardWaitProbe(const DevData& d, const PersistentPlan& p, int* que
   const int capL = stagingCapacity(p, sizeof(double));
   const size_t sm = (size_t)(p.maxRow + capL) * sizeof(double);
   allowBigSmem(kBackwardQueue<double>, sm);
-  kBackwardQueue<double><<<1, 32, sm, s>>>(d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline, p.errFlag,
+  pdlLaunch(kBackwardQueue<double>, 1, 32, sm, s, d, p.maxRow, capL, d.L64, d.x64, queue, ctr, p.bwInline, p.errFlag,
                                            ACC_SET, 0, spins);
 }
 

@@ -17,6 +17,7 @@ inline int blocksFor(long long n, int tpb = TPB) { return (int)((n + tpb - 1) / 
 
 // r = b - A x with the FP64 Newton matrix (full symmetric CSR), one row per thread
 __global__ void kRefineResidual(DevData d) {
+  pdlEntry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.neqTot) return;
   // the row's extent is read with the model index, before the activity test
@@ -30,7 +31,7 @@ __global__ void kRefineResidual(DevData d) {
 }  // namespace
 
 void launchRefineResidual(const DevData& d, cudaStream_t s) {
-  if (d.neqTot > 0) kRefineResidual<<<blocksFor(d.neqTot), TPB, 0, s>>>(d);
+  if (d.neqTot > 0) pdlLaunch(kRefineResidual, blocksFor(d.neqTot), TPB, 0, s, d);
 }
 
 }  // namespace fgpu

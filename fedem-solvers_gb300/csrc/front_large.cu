@@ -433,6 +433,7 @@ template <typename T>
 __global__ void __launch_bounds__(kLT) kLargeFactorForward(DevData d, PersistentPlan p, const T* asmVal, T* Lbase,
                                                             T* Ubase, double tolFact, const double* rhs, T* X, T* W,
                                                             int* cnt, int doFactor, int panel) {
+  pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ldp = (p.maxRowLarge + 3) & ~3;
   T* v = reinterpret_cast<T*>(smraw);
@@ -475,6 +476,7 @@ __global__ void __launch_bounds__(kLT) kLargeFactorForward(DevData d, Persistent
 template <typename T>
 __global__ void __launch_bounds__(kLT) kLargeBackward(DevData d, PersistentPlan p, const T* Lbase, T* X, int* queue,
                                                        int* ctr, int* errFlag, int acc, int finalize) {
+  pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   T* xs = reinterpret_cast<T*>(smraw);
   T* Ltri = xs + ((p.maxRowLarge + 3) & ~3);  // 32 x 32 staging of a block's triangle
@@ -648,21 +650,23 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
   bigSmem(kLargeFactorForward<T>, sm);
   if (!factor) {
     const int grid = gridFor(kLargeFactorForward<T>, sm, p.nLargeTasks);
-    kLargeFactorForward<T><<<grid, kLT, sm, s>>>(d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, 0, kb);
+    pdlLaunch(kLargeFactorForward<T>, grid, kLT, sm, s, d, p, asmVal, L, U, 1.0e-12, rhs, X, W, cnt, 0, kb);
     return;
   }
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   const int csize = p.largeCluster;
   attr[0].val.clusterDim.x = csize;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.blockDim = dim3(kLT);
   cfg.dynamicSmemBytes = sm;
   cfg.stream = s;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   cfg.gridDim = dim3(csize * p.nLargeTasks);
   int clusters = 0;
   if (cudaOccupancyMaxActiveClusters(&clusters, kLargeFactorForward<T>, &cfg) != cudaSuccess || clusters < 1)
@@ -699,12 +703,12 @@ void launchLargeBackward(const DevData& d, const PersistentPlan& p, bool fp32, i
     const size_t sm = ((size_t)((p.maxRowLarge + 3) & ~3) + 32 * 32) * sizeof(float);
     bigSmem(kLargeBackward<float>, sm);
     const int grid = gridFor(kLargeBackward<float>, sm, p.nLargeTasks);
-    kLargeBackward<float><<<grid, kLT, sm, s>>>(d, p, d.L32, d.x32, queue, ctr, p.errFlag, acc, fin);
+    pdlLaunch(kLargeBackward<float>, grid, kLT, sm, s, d, p, d.L32, d.x32, queue, ctr, p.errFlag, acc, fin);
   } else {
     const size_t sm = ((size_t)((p.maxRowLarge + 3) & ~3) + 32 * 32) * sizeof(double);
     bigSmem(kLargeBackward<double>, sm);
     const int grid = gridFor(kLargeBackward<double>, sm, p.nLargeTasks);
-    kLargeBackward<double><<<grid, kLT, sm, s>>>(d, p, d.L64, d.x64, queue, ctr, p.errFlag, acc, fin);
+    pdlLaunch(kLargeBackward<double>, grid, kLT, sm, s, d, p, d.L64, d.x64, queue, ctr, p.errFlag, acc, fin);
   }
 }
 

@@ -48,6 +48,7 @@ __device__ inline bool modeActive(int mode, int fl) {
 // One thread per joint: increment of the joint variables (after an increment
 // pass), the dependent triad on its kinematic position, the coefficients T.
 __global__ void kJoints(DevData d, int mode) {
+  pdlEntry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= d.njointTot) return;
   if (!modeActive(mode, d.m.flags[d.jModel[j]])) return;
@@ -151,6 +152,7 @@ __device__ inline void bColumn(const DevData& d, int c, int q, int& i0, double* 
 // Expanded Newton matrices B^T N B of the constrained elements of the models
 // that update their tangent: one block per element, thread q builds column q
 __global__ void kExpandElements(DevData d) {
+  pdlEntry();
   const int c = blockIdx.x, q = threadIdx.x;
   const int e = d.cxEl[c];
   if (!(d.m.flags[d.elModel[e]] & FL_TANGENT)) return;
@@ -190,6 +192,7 @@ __global__ void kExpandElements(DevData d) {
 // Expanded forces B^T F (FS, FD, FI, Q) of the constrained elements, with the
 // same model gating as the element pass of this mode
 __global__ void kExpandForces(DevData d, int mode) {
+  pdlEntry();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = t >> 5, p = t & 31;
   if (c >= d.ncxTot) return;
@@ -217,15 +220,15 @@ __global__ void kExpandForces(DevData d, int mode) {
 }  // namespace
 
 void launchJoints(const DevData& d, int mode, cudaStream_t s) {
-  if (d.njointTot > 0) kJoints<<<(d.njointTot + 63) / 64, 64, 0, s>>>(d, mode);
+  if (d.njointTot > 0) pdlLaunch(kJoints, (d.njointTot + 63) / 64, 64, 0, s, d, mode);
 }
 
 void launchExpandElements(const DevData& d, cudaStream_t s) {
-  if (d.ncxTot > 0) kExpandElements<<<d.ncxTot, 32, 0, s>>>(d);
+  if (d.ncxTot > 0) pdlLaunch(kExpandElements, d.ncxTot, 32, 0, s, d);
 }
 
 void launchExpandForces(const DevData& d, int mode, cudaStream_t s) {
-  if (d.ncxTot > 0) kExpandForces<<<(d.ncxTot * 32 + 127) / 128, 128, 0, s>>>(d, mode);
+  if (d.ncxTot > 0) pdlLaunch(kExpandForces, (d.ncxTot * 32 + 127) / 128, 128, 0, s, d, mode);
 }
 
 }  // namespace fgpu

@@ -9,6 +9,36 @@
 
 namespace fgpu {
 
+// Programmatic dependent launch.  Every kernel of the engine is launched with
+// programmatic stream serialization (pdlLaunch) and calls pdlEntry() first:
+// it waits until the previous kernel of its stream has completed and its
+// memory is visible (griddepcontrol.wait), then lets the next kernel's blocks
+// be scheduled (griddepcontrol.launch_dependents), which then wait the same
+// way.  Ordering and results are those of plain stream order; only the launch
+// of each kernel overlaps the end of the one before.
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdlEntry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline void pdlLaunch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                      Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
+
 // element pass modes
 enum ElemMode : int {
   EM_PRED = 0,         // predictor: velocities from dk/ak, no position update

@@ -67,6 +67,7 @@ __device__ inline void partColumn(const DevData& d, int p, int q, int& i0, doubl
 // generalized DOF increments, frame, deformation, local velocities, the four
 // force vectors rotated to system axes on the triad groups, expanded into FelX.
 __global__ void __launch_bounds__(kPartThreads) kParts(DevData d, int mode) {
+  pdlEntry();
   extern __shared__ double sh[];
   const int p = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
   const int m = d.pModel[p];
@@ -237,6 +238,7 @@ __global__ void __launch_bounds__(kPartThreads) kParts(DevData d, int mode) {
 // N = sM M + sC stifScl C + sK stifScl K, rotated to system axes on the triad
 // DOF groups, expanded B^T N B into elMatX (column-major nx x nx).
 __global__ void __launch_bounds__(kPartThreads) kPartsNewton(DevData d) {
+  pdlEntry();
   extern __shared__ double sh[];
   const int p = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
   const int m = d.pModel[p];
@@ -316,6 +318,7 @@ __global__ void __launch_bounds__(kPartThreads) kPartsNewton(DevData d) {
 // terminateStep: the deformation of a finished step becomes the previous one
 // (the rigid-body filtering of the next step measures from it)
 __global__ void kPartsStepEnd(DevData d) {
+  pdlEntry();
   const int p = blockIdx.x;
   const int fl = d.m.flags[d.pModel[p]];
   if (!(fl & FL_STEPDONE) || (fl & FL_LINEAR)) return;
@@ -343,15 +346,15 @@ int preparePartKernels(const DevData& d) {
 }
 
 void launchParts(const DevData& d, int mode, cudaStream_t s) {
-  if (d.npartTot > 0) kParts<<<d.npartTot, kPartThreads, partSmem(d), s>>>(d, mode);
+  if (d.npartTot > 0) pdlLaunch(kParts, d.npartTot, kPartThreads, partSmem(d), s, d, mode);
 }
 
 void launchPartsNewton(const DevData& d, cudaStream_t s) {
-  if (d.npartTot > 0) kPartsNewton<<<d.npartTot, kPartThreads, partNewtonSmem(d), s>>>(d);
+  if (d.npartTot > 0) pdlLaunch(kPartsNewton, d.npartTot, kPartThreads, partNewtonSmem(d), s, d);
 }
 
 void launchPartsStepEnd(const DevData& d, cudaStream_t s) {
-  if (d.npartTot > 0) kPartsStepEnd<<<d.npartTot, 64, 0, s>>>(d);
+  if (d.npartTot > 0) pdlLaunch(kPartsStepEnd, d.npartTot, 64, 0, s, d);
 }
 
 }  // namespace fgpu

@@ -31,6 +31,7 @@ namespace {
 // one block per model: the record of its current state when its step has just
 // completed (or unconditionally when all != 0), into ring slot count % ring
 __global__ void kRecordStep(DevData d, RecordPlan r, int all) {
+  pdlEntry();
   const int m = blockIdx.x;
   if (m >= d.m.n) return;
   if (!all && !(d.m.flags[m] & FL_STEPDONE)) return;
@@ -70,7 +71,7 @@ __global__ void kRecordStep(DevData d, RecordPlan r, int all) {
 }  // namespace
 
 void launchRecordStep(const DevData& d, const RecordPlan& r, bool all, cudaStream_t s) {
-  if (d.m.n > 0) kRecordStep<<<d.m.n, 128, 0, s>>>(d, r, all ? 1 : 0);
+  if (d.m.n > 0) pdlLaunch(kRecordStep, d.m.n, 128, 0, s, d, r, all ? 1 : 0);
 }
 
 int Engine::resultsOpen(const std::string& dir, bool asDouble, std::string& err,
