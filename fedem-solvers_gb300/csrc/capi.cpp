@@ -859,7 +859,7 @@ int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4) {
   OnDevice onDev(b->engine.device());
   const int rc = b->engine.setLaunchShape(shape4);
   if (rc == -1) return fail(-2, "launch shapes can only be set before the batch's first iteration");
-  if (rc < 0) return fail(-3, "launch shape out of range (panel 0/1/2, warps 4/8/16, cluster 2/4/8)");
+  if (rc < 0) return fail(-3, "launch shape out of range (panel 0/1/2, warps 4/8/16, cluster 2/4/8/16)");
   return 0;
 }
 

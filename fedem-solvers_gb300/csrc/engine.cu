@@ -1280,7 +1280,7 @@ int Engine::setLaunchShape(const int* sh) {
   if (sh[0] < 0 || sh[0] > 2) return -2;
   for (int k = 1; k <= 2; ++k)
     if (sh[k] != 4 && sh[k] != 8 && sh[k] != 16) return -2;
-  if (sh[3] != 2 && sh[3] != 4 && sh[3] != 8) return -2;
+  if (sh[3] != 2 && sh[3] != 4 && sh[3] != 8 && sh[3] != 16) return -2;
   pplan_.factorPanel = sh[0];
   pplan_.forwardWarps = sh[1];
   pplan_.backwardWarps = sh[2];
@@ -1374,7 +1374,8 @@ int Engine::autotune() {
   if (ok && pplan_.nLargeTasks > 0) {
     float best = -1.f;
     int pick = 8;
-    for (int c : {8, 4, 2}) {
+    for (int c : {8, 4, 2, 16}) {
+      if (c > 8 && largeClusterCapacity(pplan_, f32, c) < 1) continue;  // not on this device
       pplan_.largeCluster = c;
       const float t = timeIt(
           [&] {

@@ -638,6 +638,38 @@ int panelWidth(int maxRow) {
   return kb;
 }
 
+// clusters of csize blocks the device can hold at once with the factorisation's
+// shared memory (0: none; sizes above 8 need the non-portable cluster opt-in)
+template <typename T>
+int largeClusterCapacity(const PersistentPlan& p, int csize) {
+  const size_t ldp = (size_t)((p.maxRowLarge + 3) & ~3);
+  const int kb = panelWidth<T>(p.maxRowLarge);
+  const size_t sm = (2 * ldp + 32 + 32 * 32 + (size_t)kb * ldp) * sizeof(T);
+  bigSmem(kLargeFactorForward<T>, sm);
+  if (csize > 8 && cudaFuncSetAttribute(kLargeFactorForward<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                       cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kLT);
+  cfg.dynamicSmemBytes = sm;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(csize);
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, kLargeFactorForward<T>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return clusters;
+}
+
 // Factorisations run as clusters of p.largeCluster blocks per front (a grid of
 // as many clusters as fit at once, at most one per start task); forward
 // eliminations alone as single blocks.
@@ -656,7 +688,10 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  const int csize = p.largeCluster;
+  int csize = p.largeCluster;
+  // 16 blocks per cluster is beyond the portable size: allowed per kernel, and
+  // only taken when the device can hold such a cluster with this shared memory
+  if (csize > 8 && largeClusterCapacity<T>(p, csize) < 1) csize = 8;
   attr[0].val.clusterDim.x = csize;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
@@ -677,6 +712,11 @@ void factorForwardLarge(const DevData& d, const PersistentPlan& p, const T* asmV
 }
 
 }  // namespace
+
+int largeClusterCapacity(const PersistentPlan& p, bool fp32, int csize) {
+  if (p.nLargeTasks <= 0) return 0;
+  return fp32 ? largeClusterCapacity<float>(p, csize) : largeClusterCapacity<double>(p, csize);
+}
 
 void launchLargeFactorForward(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
                               cudaStream_t s) {

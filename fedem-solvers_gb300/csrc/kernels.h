@@ -155,7 +155,7 @@ struct PersistentPlan {
                            // (blocks of 8), 2 register-blocked (blocks of 4, fronts up to 32 rows)
   int forwardWarps = 8;    // warps per block of the forward-elimination cascade
   int backwardWarps = 8;   // warps per block of the back-substitution queue
-  int largeCluster = 8;    // blocks per cluster of the large-front factorisation (2, 4 or 8)
+  int largeCluster = 8;    // blocks per cluster of the large-front factorisation (2, 4, 8 or 16)
 };
 // fronts with more rows than this are factored and solved by a thread block
 // each (front_large.cu); smaller ones by one warp each in shared memory
@@ -165,6 +165,9 @@ constexpr int kLargeFrontRows = 96;
 // the back substitution of the large fronts (before the warp queue's)
 void launchLargeFactorForward(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
                               cudaStream_t s);
+// clusters of csize blocks (2 to 16) the device can hold at once for the
+// large-front factorisation of this plan (0: none)
+int largeClusterCapacity(const PersistentPlan& p, bool fp32, int csize);
 void launchLargeForward(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
                         cudaStream_t s);
 void launchLargeBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);

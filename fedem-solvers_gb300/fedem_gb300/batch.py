@@ -226,7 +226,7 @@ class Batch:
         """Fixes the multifrontal launch shapes (before the first run) instead of
         the autotuner's probe: panel 0 (shuffles), 1 (register-blocked, blocks of
         8) or 2 (blocks of 4, fronts up to 32 rows); warps 4, 8 or 16; cluster
-        2, 4 or 8.  No shape changes a result bit."""
+        2, 4, 8 or 16.  No shape changes a result bit."""
         sh = (ctypes.c_int * 4)(panel, forward_warps, backward_warps, large_cluster)
         if self._lib.fgpu_batch_set_launch_shape(self._h, sh) != 0:
             raise FedemException("set_launch_shape failed: " + self._lib.fgpu_last_error().decode())

@@ -130,7 +130,8 @@ int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
  * 32 rows),
  * warps per block of the forward-elimination cascade (4, 8 or 16), warps per
  * block of the back-substitution queue (4, 8 or 16), blocks per cluster of the
- * large-front factorisation (2, 4 or 8)}.  The autotuner picks them before a
+ * large-front factorisation (2, 4, 8, or 16 where the device holds such
+ * clusters; else 8 is used)}.  The autotuner picks them before a
  * batch's first batched iteration by timing the candidates on the batch's own
  * fronts (a few milliseconds; a batch of the same structure reuses the
  * choice).  Every shape gives the same results to the last bit, so the
