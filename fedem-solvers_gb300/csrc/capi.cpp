@@ -879,6 +879,32 @@ int fgpu_batch_results_close(fgpu_batch* b) {
   return 0;
 }
 
+int fgpu_batch_assemble_newton(fgpu_batch* b, int model, double sM, double sC, double sK) {
+  if (!b || model < 0 || model >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  const int rc = b->engine.seamAssemble(model, sM, sC, sK);
+  if (rc == -2) return fail(rc, "the model is inside a time step");
+  return rc ? fail(rc, "assembly failed") : 0;
+}
+
+int fgpu_batch_factor(fgpu_batch* b, int model) {
+  if (!b || model < 0 || model >= b->engine.numModels()) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  const int rc = b->engine.seamFactor(model);
+  if (rc == -3) return fail(rc, "singular Newton matrix");
+  if (rc == -2) return fail(rc, "the model is inside a time step");
+  return rc < 0 ? fail(rc, "factorisation failed") : rc;
+}
+
+int fgpu_batch_solve(fgpu_batch* b, int model, double* rhs, int nrhs) {
+  if (!b || !rhs || model < 0 || model >= b->engine.numModels() || nrhs < 0) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  const int rc = b->engine.seamSolve(model, rhs, nrhs);
+  if (rc == -2) return fail(rc, "the model is inside a time step");
+  if (rc == -5) return fail(rc, "a bounded wait of the back substitution ran out");
+  return rc ? fail(rc, "solve failed") : 0;
+}
+
 int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs) {
   if (!b || !shape4) return fail(-1, "bad argument");
   return b->engine.launchShape(shape4, probeMs);

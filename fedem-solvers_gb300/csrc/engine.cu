@@ -1554,6 +1554,75 @@ void Engine::setStepLimitOf(int m, long long lim) {
   cudaStreamSynchronize(stream_);
 }
 
+// ---- linear-solver seam of one model -------------------------------------
+namespace {
+// the flags of a seam call: model m alone, with `fl`
+void seamFlags(const DevData& d, int m, int fl, cudaStream_t s) {
+  std::vector<int> v((size_t)d.m.n, 0);
+  v[m] = fl;
+  cudaMemcpyAsync(d.m.flags, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice, s);
+  cudaStreamSynchronize(s);  // v goes out of scope
+}
+}  // namespace
+
+int Engine::seamAssemble(int m, double sM, double sC, double sK) {
+  if (m < 0 || m >= d_.m.n) return -1;
+  if (modelState(m) == ST_ITER) return -2;  // inside a step: its factor is in use
+  ensureTuned();
+  seamFlags(d_, m, FL_ACTIVE | FL_TANGENT | FL_REBUILD, stream_);
+  // scale factors as the element kernels read them: M, K, C
+  const double sc[3] = {sM, sK, sC};
+  cudaMemcpyAsync(d_.m.scaleN + 3 * (size_t)m, sc, sizeof sc, cudaMemcpyHostToDevice, stream_);
+  launchBuildElementNewton(d_, stream_);
+  launchRotateElementNewton(d_, stream_);
+  launchCsrGather(d_, stream_);
+  return cudaStreamSynchronize(stream_) == cudaSuccess ? 0 : -3;
+}
+
+int Engine::seamFactor(int m) {
+  if (m < 0 || m >= d_.m.n) return -1;
+  if (modelState(m) == ST_ITER) return -2;
+  int st0 = 0, neg0 = 0, st = 0, neg = 0;
+  cudaMemcpyAsync(&st0, d_.m.status + m, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(&neg0, d_.m.negPiv + m, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  const int zero = 0;
+  cudaMemcpyAsync(d_.m.status + m, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.negPiv + m, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  seamFlags(d_, m, FL_ACTIVE | FL_TANGENT, stream_);
+  resetIterationCounters(stream_);
+  enqueueFactor(stream_);
+  cudaMemcpyAsync(&st, d_.m.status + m, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(&neg, d_.m.negPiv + m, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -4;
+  // the model's own status and pivot count are its stepping's, not the seam's
+  cudaMemcpyAsync(d_.m.status + m, &st0, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  cudaMemcpyAsync(d_.m.negPiv + m, &neg0, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -4;
+  return (st & SS_SINGULAR) ? -3 : neg;
+}
+
+int Engine::seamSolve(int m, double* rhs, int nrhs) {
+  if (m < 0 || m >= d_.m.n || nrhs < 0) return -1;
+  if (modelState(m) == ST_ITER) return -2;
+  const int n = hm_[m]->neq;
+  seamFlags(d_, m, FL_ACTIVE, stream_);
+  for (int r = 0; r < nrhs; ++r) {
+    double* b = rhs + (size_t)r * n;
+    cudaMemcpyAsync(d_.del + modelEqOff_[m], b, sizeof(double) * n, cudaMemcpyHostToDevice, stream_);
+    resetIterationCounters(stream_);
+    launchSeedBackward(d_, seed_, stream_);
+    enqueueFactor(stream_);  // forward elimination only (no tangent flag)
+    enqueueSolve(stream_);
+    cudaMemcpyAsync(b, d_.del + modelEqOff_[m], sizeof(double) * n, cudaMemcpyDeviceToHost, stream_);
+    if (cudaStreamSynchronize(stream_) != cudaSuccess) return -4;
+  }
+  int err = 0;
+  cudaMemcpyAsync(&err, pplan_.errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return err ? -5 : 0;
+}
+
 int Engine::prepareStiffnessSolves() {
   const int nm = d_.m.n;
   savedFlags_.assign(nm, 0);

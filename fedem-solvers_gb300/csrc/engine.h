@@ -99,6 +99,15 @@ class Engine {
   int prepareStiffnessSolves();
   int solveStiffness(int m, const double* b, double* x);
   int endStiffnessSolves();
+  // The linear-solver seam of one model, between its steps (csAddEM + csSolve
+  // granularity): its Newton matrix N = sM M + sC C + sK K assembled on the GPU
+  // (element matrices, constraint expansion, CSR); factored (returns the
+  // number of negative pivots, -3 when a pivot is singular); solved for nrhs
+  // right-hand sides of its equations, in place.  The model's next batched
+  // iteration starts a step and so refactors its own tangent.
+  int seamAssemble(int m, double sM, double sC, double sK);
+  int seamFactor(int m);
+  int seamSolve(int m, double* rhs, int nrhs);
   // external function channel ch (0-based) of model m: its value for the next step
   int setExtValue(int m, int ch, double v);
   double extValue(int m, int ch);

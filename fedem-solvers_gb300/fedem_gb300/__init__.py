@@ -105,6 +105,9 @@ def load_library(path=None):
         "fgpu_batch_launch_shape": (c_int, [vp, P(c_int), P(c_dbl)]),
         "fgpu_batch_results_open": (c_int, [vp, ctypes.c_char_p, c_int]),
         "fgpu_batch_results_close": (c_int, [vp]),
+        "fgpu_batch_assemble_newton": (c_int, [vp, c_int, c_dbl, c_dbl, c_dbl]),
+        "fgpu_batch_factor": (c_int, [vp, c_int]),
+        "fgpu_batch_solve": (c_int, [vp, c_int, P(c_dbl), c_int]),
         "fgpu_last_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -239,6 +239,28 @@ class Batch:
         keys = ("panel", "forward_warps", "backward_warps", "large_cluster")
         return dict(zip(keys, list(sh))), ms.value, tuned == 1
 
+    def assemble_newton(self, model, sM, sC, sK):
+        """N = sM M + sC C + sK K of the model's current state, assembled on the
+        GPU (read it with newton_values); between the model's steps."""
+        if self._lib.fgpu_batch_assemble_newton(self._h, model, sM, sC, sK) != 0:
+            raise FedemException("assemble_newton failed: " + self._lib.fgpu_last_error().decode())
+
+    def factor(self, model):
+        """LDL^T of the assembled N: the number of negative pivots; raises on a
+        singular pivot (code -3) or an error."""
+        rc = self._lib.fgpu_batch_factor(self._h, model)
+        if rc < 0:
+            raise FedemException(f"factor failed ({rc}): " + self._lib.fgpu_last_error().decode())
+        return rc
+
+    def solve(self, model, rhs):
+        """Solutions of N x = b for b = rhs (neq values, or nrhs x neq)."""
+        b = np.ascontiguousarray(np.array(rhs, dtype=np.float64))
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        if self._lib.fgpu_batch_solve(self._h, model, _ptr(b, ctypes.c_double), nrhs) != 0:
+            raise FedemException("solve failed: " + self._lib.fgpu_last_error().decode())
+        return b
+
     def results_open(self, directory, double=True):
         """Starts the results database: one file per model, <directory>/model<k>.res,
         a record of the current state now and one per completed time step

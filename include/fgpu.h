@@ -143,6 +143,26 @@ int fgpu_batch_time_factor(fgpu_batch* b, int reps, double* out2);
 int fgpu_batch_set_launch_shape(fgpu_batch* b, const int* shape4);
 int fgpu_batch_launch_shape(fgpu_batch* b, int* shape4, double* probeMs);
 
+/* The linear-solver seam of one model, at the granularity of the reference's
+ * csAddEM + csSolve (src/vpmCommon/vpmLinAlg/asmExtensionModule.f90:1227,
+ * solExtensionModule.f90:153-505), for a host that drives its own Newton
+ * loop and wants the GPU's assembly and sparse LDL^T.  Between the model's
+ * time steps only (-2 inside one); the model's next batched iteration starts a
+ * step and refactors its own tangent.
+ * assemble_newton: N = sM M + sC C + sK K of the model's current state on the
+ *   GPU (element matrices in system axes, constraint expansion of joints and
+ *   prescribed DOFs as in the batched iteration, CSR in equation order);
+ *   fgpu_batch_get_newton_values reads it.
+ * factor: LDL^T of N (FP32 fronts for a mixed batch, FP64 otherwise); returns
+ *   the number of negative pivots (>= 0), -3 when a pivot is singular
+ *   (|d_k| <= 1e-12 |a_kk|, the reference's tolFactorize), < 0 on error.
+ * solve: N x = b for nrhs right-hand sides (each neq values in equation order,
+ *   overwritten by its solution); a mixed batch refines each solution against
+ *   the FP64 N (its solves-per-iteration count). */
+int fgpu_batch_assemble_newton(fgpu_batch* b, int model, double sM, double sC, double sK);
+int fgpu_batch_factor(fgpu_batch* b, int model);
+int fgpu_batch_solve(fgpu_batch* b, int model, double* rhs, int nrhs);
+
 /* Results database of the primary response (the reference's writeSolverDB1,
  * src/vpmSolver/saveModule.f90:615-663, called for the initial configuration
  * and after every time step, solverModule.f90:512-513, :929-931): every model
