@@ -221,18 +221,23 @@ int Engine::resultsDrain(std::string& err) {
     }
     FILE* f = rec_.files[m];
     std::vector<float> fl(rec_.asDouble ? 0 : v - 2);
+    bool ok = true;
     for (long long k = 0; k < n; ++k) {
       const double* rec = rec_.host.data() + (size_t)k * v;
       if (rec[1] + rec_.epsT < rec_.saveStart) continue;
       const int step = (int)rec[0];
-      fwrite(&step, sizeof(int), 1, f);
-      fwrite(rec + 1, sizeof(double), 1, f);
+      ok = ok && fwrite(&step, sizeof(int), 1, f) == 1;
+      ok = ok && fwrite(rec + 1, sizeof(double), 1, f) == 1;
       if (rec_.asDouble) {
-        fwrite(rec + 2, sizeof(double), v - 2, f);
+        ok = ok && fwrite(rec + 2, sizeof(double), v - 2, f) == (size_t)(v - 2);
       } else {
         for (int q = 0; q < v - 2; ++q) fl[q] = (float)rec[2 + q];
-        fwrite(fl.data(), sizeof(float), v - 2, f);
+        ok = ok && fwrite(fl.data(), sizeof(float), v - 2, f) == (size_t)(v - 2);
       }
+    }
+    if (!ok) {
+      err = "results: writing model " + std::to_string(m) + "'s file failed";
+      return -6;
     }
     rec_.written[m] = cnt[m];
   }
@@ -241,9 +246,15 @@ int Engine::resultsDrain(std::string& err) {
 
 int Engine::resultsClose(std::string& err) {
   if (!rec_.on) return 0;
-  const int rc = resultsDrain(err);
+  int rc = resultsDrain(err);
   for (FILE*& f : rec_.files)
-    if (f) fclose(f), f = nullptr;
+    if (f) {
+      if (fclose(f) != 0 && rc == 0) {
+        err = "results: closing a file failed";
+        rc = -7;
+      }
+      f = nullptr;
+    }
   rec_.on = false;
   if (graphExec_) cudaGraphExecDestroy(graphExec_), graphExec_ = nullptr;
   if (graph_) cudaGraphDestroy(graph_), graph_ = nullptr;
