@@ -56,6 +56,10 @@ Engine::~Engine() {
   for (void* p : allocs_) cudaFree(p);
   if (hActive_) cudaFreeHost(hActive_);
   if (hStates_) cudaFreeHost(hStates_);
+  if (side_) cudaStreamSynchronize(side_);
+  if (evFork_) cudaEventDestroy(evFork_);
+  if (evJoin_) cudaEventDestroy(evJoin_);
+  if (side_) cudaStreamDestroy(side_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -127,6 +131,8 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   if (opt_.refineSweeps < 1) opt_.refineSweeps = 1;
   FG_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   SetupTrace trace;
+  // the forked assembly is decided once the batch's object counts are known (below)
+  forkAssembly_ = false;
   const int nm = (int)models.size();
   // ---- global offsets --------------------------------------------------------
   modelTriOff_.assign(nm, 0);
@@ -1181,6 +1187,9 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
     if (xv && d_.njointTot > 0) reg(d_.FelX, D, SK_XVEC, 1, (size_t)xv, "FelX");
   }
   uploadedBytes_ = t_putBytes;
+  // beam elements only (no axial elements, joints or reduced parts, whose
+  // Newton matrices read state the element pass updates): forked assembly
+  forkAssembly_ = d_.nelTot > 0 && d_.naxTot == 0 && d_.njointTot == 0 && d_.npartTot == 0 && d_.ncxTot == 0;
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
   trace.mark("state registry", stream_);
@@ -1509,14 +1518,39 @@ void Engine::enqueueAssembly(cudaStream_t s) {
   resetIterationCounters(s);
   launchBeginStep(d_, dActive_, dActiveEl_, seed_, s);
   launchQsRestore(d_, s);
+  // Beam-only batches: the element Newton matrices and their CSR gather read
+  // the flags and scales of the step start, the element frames and the
+  // constant element matrices, none of which the predictor, the predictor's
+  // element pass (no frame update) or the residual write, and they write
+  // nothing those read -- so they run on the side stream beside them, joined
+  // before the prescribed-motion right-hand side that needs both.
+  if (forkAssembly_ && side_ == nullptr) {
+    if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&evFork_, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&evJoin_, cudaEventDisableTiming) != cudaSuccess)
+      forkAssembly_ = false;
+  }
+  const bool fork = forkAssembly_ && side_ != nullptr;
+  if (fork) {
+    cudaEventRecord(evFork_, s);
+    cudaStreamWaitEvent(side_, evFork_, 0);
+    launchBuildElementNewton(d_, side_);
+    launchRotateElementNewton(d_, side_);
+    launchCsrGather(d_, side_);
+    cudaEventRecord(evJoin_, side_);
+  }
   launchMotions(d_, s);
   launchLoads(d_, s);
   launchPredictDofs(d_, s);
   launchElements(d_, EM_PRED, s);
   launchResidual(d_, s);
-  launchBuildElementNewton(d_, s);
-  launchRotateElementNewton(d_, s);
-  launchCsrGather(d_, s);
+  if (fork) {
+    cudaStreamWaitEvent(s, evJoin_, 0);
+  } else {
+    launchBuildElementNewton(d_, s);
+    launchRotateElementNewton(d_, s);
+    launchCsrGather(d_, s);
+  }
   launchMotionRhs(d_, s);
 }
 

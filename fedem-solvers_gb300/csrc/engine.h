@@ -202,6 +202,12 @@ class Engine {
   int* hActive_ = nullptr;  // pinned
   int* hStates_ = nullptr;  // pinned: every model's state after the last chunk
   cudaStream_t stream_ = nullptr;
+  // beam-only batches: the Newton-matrix assembly (element matrices, CSR
+  // gather) runs on a second stream beside the predictor, element pass and
+  // residual, which it does not depend on; fork and join events
+  cudaStream_t side_ = nullptr;
+  cudaEvent_t evFork_ = nullptr, evJoin_ = nullptr;
+  bool forkAssembly_ = false;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graphExec_ = nullptr;
   std::vector<int> modelTriOff_, modelDofOff_, modelEqOff_, modelElOff_;
