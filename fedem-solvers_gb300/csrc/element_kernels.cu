@@ -1429,7 +1429,13 @@ void launchIncrement(const DevData& d, cudaStream_t s) {
   pdlLaunch(kIncrement, blocksFor(n), TPB, 0, s, d);
 }
 void launchNormsControl(const DevData& d, cudaStream_t s) {
+  launchNormsPartial(d, s);
+  launchControlStepEnd(d, s);
+}
+void launchNormsPartial(const DevData& d, cudaStream_t s) {
   if (d.nchunkTot > 0) pdlLaunch(kNormsPartial, d.nchunkTot, CHUNK_TPB, 0, s, d);
+}
+void launchControlStepEnd(const DevData& d, cudaStream_t s) {
   pdlLaunch(kControl, blocksFor(32LL * d.m.n, 128), 128, 0, s, d);
   long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
   pdlLaunch(kStepEnd, blocksFor(n), TPB, 0, s, d);

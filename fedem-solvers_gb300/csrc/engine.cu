@@ -59,6 +59,8 @@ Engine::~Engine() {
   if (side_) cudaStreamSynchronize(side_);
   if (evFork_) cudaEventDestroy(evFork_);
   if (evJoin_) cudaEventDestroy(evJoin_);
+  if (evFork2_) cudaEventDestroy(evFork2_);
+  if (evJoin2_) cudaEventDestroy(evJoin2_);
   if (side_) cudaStreamDestroy(side_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -1513,6 +1515,21 @@ void Engine::resetIterationCounters(cudaStream_t s) {
 
 // first half of a Newton iteration: step start (predictor) or the corrector's
 // right-hand side, and the Newton matrix when the tangent is updated
+// the side stream and its fork/join events, created at first use
+bool Engine::sideReady() {
+  if (side_) return true;
+  if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&evFork_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&evJoin_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&evFork2_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&evJoin2_, cudaEventDisableTiming) != cudaSuccess) {
+    if (side_) cudaStreamDestroy(side_);
+    side_ = nullptr;
+    return false;
+  }
+  return true;
+}
+
 void Engine::enqueueAssembly(cudaStream_t s) {
   iterated_ = true;
   resetIterationCounters(s);
@@ -1524,13 +1541,7 @@ void Engine::enqueueAssembly(cudaStream_t s) {
   // element pass (no frame update) or the residual write, and they write
   // nothing those read -- so they run on the side stream beside them, joined
   // before the prescribed-motion right-hand side that needs both.
-  if (forkAssembly_ && side_ == nullptr) {
-    if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&evFork_, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&evJoin_, cudaEventDisableTiming) != cudaSuccess)
-      forkAssembly_ = false;
-  }
-  const bool fork = forkAssembly_ && side_ != nullptr;
+  const bool fork = forkAssembly_ && sideReady();
   if (fork) {
     cudaEventRecord(evFork_, s);
     cudaStreamWaitEvent(side_, evFork_, 0);
@@ -1564,9 +1575,24 @@ void Engine::enqueueSolveUpdate(cudaStream_t s) {
   recordPhase(ev_[2], s);
   launchIncrement(d_, s);
   recordPhase(ev_[3], s);
+  // the partial norms read the increments and the residual, which the element
+  // pass does not touch; the convergence test after the join also sees every
+  // status bit the element pass set (a failed corotation)
+  const bool fork = sideReady();
+  if (fork) {
+    cudaEventRecord(evFork2_, s);
+    cudaStreamWaitEvent(side_, evFork2_, 0);
+    launchNormsPartial(d_, side_);
+    cudaEventRecord(evJoin2_, side_);
+  }
   launchElements(d_, EM_INC, s);
   recordPhase(ev_[4], s);
-  launchNormsControl(d_, s);
+  if (fork) {
+    cudaStreamWaitEvent(s, evJoin2_, 0);
+    launchControlStepEnd(d_, s);
+  } else {
+    launchNormsControl(d_, s);
+  }
   if (rec_.on) launchRecordStep(d_, rec_.plan, false, s);
 }
 

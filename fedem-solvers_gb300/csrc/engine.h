@@ -208,6 +208,10 @@ class Engine {
   cudaStream_t side_ = nullptr;
   cudaEvent_t evFork_ = nullptr, evJoin_ = nullptr;
   bool forkAssembly_ = false;
+  // every batch: the partial norms run on the side stream beside the element
+  // pass after the increment (they read the increments and the residual only)
+  cudaEvent_t evFork2_ = nullptr, evJoin2_ = nullptr;
+  bool sideReady();
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graphExec_ = nullptr;
   std::vector<int> modelTriOff_, modelDofOff_, modelEqOff_, modelElOff_;

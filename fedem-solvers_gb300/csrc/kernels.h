@@ -83,6 +83,10 @@ void launchRotateElementNewton(const DevData& d, cudaStream_t s);
 void launchCsrGather(const DevData& d, cudaStream_t s);
 void launchIncrement(const DevData& d, cudaStream_t s);
 void launchNormsControl(const DevData& d, cudaStream_t s);
+// the same in two parts: the per-chunk partial norms (reading the increments
+// and the residual only), then the convergence test and the step end
+void launchNormsPartial(const DevData& d, cudaStream_t s);
+void launchControlStepEnd(const DevData& d, cudaStream_t s);
 // static equilibrium helpers
 void launchStaticBegin(const DevData& d, int* activeCount, const BackwardSeed& seed, cudaStream_t s);
 void launchSeedBackward(const DevData& d, const BackwardSeed& seed, cudaStream_t s);
