@@ -797,7 +797,8 @@ def main():
         roof_el = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                    "frac": achieved / hbm_peak, "traffic": None,
                    "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
-                   "note": "bound by the FP64 rate (FP64 pipe 84-88 % busy), not by HBM",
+                   "note": "bound by the FP64 rate (FP64 pipe 84-88 % busy), not by HBM; the phase is sampled with "
+                               "the partial norms running beside it on a second stream",
                    "bytes_per_element": ELEM_BYTES, "samples": nsamp}
     E = 4 if mixed else 8
     roof_fwd = None
