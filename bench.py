@@ -51,11 +51,15 @@ UNIT = "Newton steps/s"
 #        K 208, M 208, triad position 96 + accelerations 48 + first DOF 4
 #   out: frame 96, deformation 96, FS, FI, FD, Q 4 x 96
 ELEM_BYTES = 1630
-# DRAM bytes (read + write) of one launch on this workload (256 models), from
-# ncu captures of kForwardCascade<float> and of kFactorForwardCascade<float>
-# in an iteration where every model factors (profiles/)
-FORWARD_TRAFFIC_256 = 153.6e6
-FACTOR_TRAFFIC_256 = 307.4e6
+# DRAM bytes (read + write) of one launch on this workload (256 models): the
+# mean of the first two Newton-iteration launches of each kernel captured by
+# ncu on the first 128 of these models, scaled by the ratio of algorithmic
+# bytes (fronts) or of elements (profiles/dram_traffic_beam_batch_128models.md)
+FACTOR_TRAFFIC_256 = 202.5e6
+FORWARD_TRAFFIC_256 = 152.1e6
+BACKWARD_TRAFFIC_256 = 133.2e6
+# DRAM bytes per element of the element pass after the increment (same capture)
+ELEM_TRAFFIC = 1238
 
 
 def forward_bytes(models, elem_bytes):
@@ -794,12 +798,14 @@ def main():
     roof, roof_el = None, None
     if nsamp > 0 and ms5[0] > 0:
         achieved = el_s * ELEM_BYTES / (ms5[0] * 1e-3) / 1e9
+        # per launch: the measured DRAM bytes per element x the sampled launches' mean active elements
         roof_el = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                   "frac": achieved / hbm_peak, "traffic": None,
+                   "frac": achieved / hbm_peak, "traffic": ELEM_TRAFFIC * el_s / nsamp,
                    "kernel": "kElements (element pass after the increment)", "peak_source": peak_kind,
                    "note": "bound by the FP64 rate (FP64 pipe 84-88 % busy), not by HBM; the phase is sampled with "
                                "the partial norms running beside it on a second stream",
-                   "bytes_per_element": ELEM_BYTES, "samples": nsamp}
+                   "bytes_per_element": ELEM_BYTES, "traffic_bytes_per_element": ELEM_TRAFFIC,
+                   "samples": nsamp}
     E = 4 if mixed else 8
     roof_fwd = None
     if nsamp > 0 and ms5[3] > 0:
@@ -818,8 +824,9 @@ def main():
         bb = backward_bytes(mods, E)
         t_bwd = ms5[4] * 1e-3 / nsamp
         achieved = bb / t_bwd / 1e9
+        traffic = BACKWARD_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
         roof_bwd = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": achieved / hbm_peak, "traffic": None,
+                    "frac": achieved / hbm_peak, "traffic": traffic,
                     "kernel": "kBackwardQueue (back substitution of the first solve, all fronts)",
                     "algorithmic_bytes_per_launch": bb, "launch_ms": t_bwd * 1e3, "peak_source": peak_kind,
                     "note": "latency-bound like the factor: queue hand-offs along the assembly trees",
