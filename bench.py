@@ -476,7 +476,7 @@ def single_model_leg(fsi, opts, steps, desc, pending=None):
                "ms_per_iteration": st["device_us"] * 1e-3 / max(st["batched_iterations"], 1),
                "phase_ms_per_iteration": {"elements": ph[0], "factor_and_first_forward": ph[1],
                                           "other_solve": ph[2], "second_forward": ph[3],
-                                          "first_backward": ph[4]}}
+                                          "back_substitution": ph[4]}}
         # the factorisation fused with the first forward elimination, timed alone
         # (10 launches, CUDA events on the engine stream) after the run
         f_ms, _ = b.time_factor(reps=10)
@@ -585,17 +585,20 @@ def run_reference(args, dist, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def backward_bytes(models, elem_bytes):
+def backward_bytes(models, elem_bytes, refinement=False):
     """Algorithmic bytes of one back substitution over all fronts: the L block
     (nrow x npiv), the row list, the solution values of all rows gathered, the
-    pivots' solution written in the solve precision and in FP64."""
+    pivots' solution written in the solve precision and in FP64 (the
+    refinement solve of the last sweep also reads the accumulated FP64
+    solution and writes the increment: 16 more bytes per pivot)."""
     import numpy as np
 
+    per_piv = elem_bytes + (24 if refinement else 8)
     total = 0
     for m in models:
         _, info = m.symbolic()
         npiv, nrow = info[:, 0].astype(np.int64), info[:, 1].astype(np.int64)
-        total += int((elem_bytes * nrow * npiv + 4 * nrow + elem_bytes * nrow + (elem_bytes + 8) * npiv).sum())
+        total += int((elem_bytes * nrow * npiv + 4 * nrow + elem_bytes * nrow + per_piv * npiv).sum())
     return total
 
 
@@ -820,14 +823,17 @@ def main():
                     "algorithmic_bytes_per_launch": fb, "launch_ms": t_fwd * 1e3, "peak_source": peak_kind,
                     "samples": nsamp}
     roof_bwd = None
-    if nsamp > 0 and ms5[4] > 0:
-        bb = backward_bytes(mods, E)
+    # the back substitution launched on its own: the refinement solve's (the
+    # first solve's runs inside the factorisation's launch in batches without
+    # large fronts); an FP64 batch of one solve per iteration has none
+    if nsamp > 0 and ms5[4] > 0.05 * ms5[1]:
+        bb = backward_bytes(mods, E, refinement=mixed)
         t_bwd = ms5[4] * 1e-3 / nsamp
         achieved = bb / t_bwd / 1e9
         traffic = BACKWARD_TRAFFIC_256 if len(mods) == 256 and args.models == 256 else None
         roof_bwd = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                     "frac": achieved / hbm_peak, "traffic": traffic,
-                    "kernel": "kBackwardQueue (back substitution of the first solve, all fronts)",
+                    "kernel": "kBackwardQueue (back substitution of the refinement solve, all fronts)",
                     "algorithmic_bytes_per_launch": bb, "launch_ms": t_bwd * 1e3, "peak_source": peak_kind,
                     "note": "latency-bound like the factor: queue hand-offs along the assembly trees",
                     "samples": nsamp}
@@ -851,7 +857,7 @@ def main():
     if nsamp > 0:
         phases = {"elements": ms5[0] / nsamp, "factor_and_first_forward": ms5[1] / nsamp,
                   "other_solve": ms5[2] / nsamp, "second_forward": ms5[3] / nsamp,
-                  "first_backward": ms5[4] / nsamp}
+                  "back_substitution": ms5[4] / nsamp}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,

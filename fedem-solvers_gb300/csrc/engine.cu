@@ -1466,10 +1466,10 @@ void Engine::resetPhaseTimings() {
   phaseSamples_ = phaseElems_ = 0;
 }
 
-void Engine::enqueueFactor(cudaStream_t s) {
+void Engine::enqueueFactor(cudaStream_t s, bool withBackward) {
   // factorisation and the first forward elimination in one cascade (small
   // fronts by warps, then the large fronts above them by thread blocks)
-  launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s);
+  launchFactorForwardCascade(d_, pplan_, opt_.fp32Factor, d_.del, s, withBackward, opt_.refineSweeps <= 1);
   launchLargeFactorForward(d_, pplan_, opt_.fp32Factor, d_.del, s);
 }
 
@@ -1485,9 +1485,12 @@ void Engine::recordPhase(cudaEvent_t ev, cudaStream_t s) {
     cudaEventRecord(ev, s);
 }
 
-void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
+void Engine::enqueueSolve(cudaStream_t s, bool timedForward, bool backwardDone) {
   const bool f32 = opt_.fp32Factor;
   const int sw = opt_.refineSweeps;
+  // the timed back substitution: the first solve's, or the second's when the
+  // first ran inside the factorisation's launch
+  const int timedBackward = backwardDone && sw > 1 ? 1 : 0;
   for (int sweep = 0; sweep < sw; ++sweep) {
     // the right-hand side is read and the solution stored inside the launches;
     // the first forward elimination ran with the factorisation
@@ -1498,10 +1501,12 @@ void Engine::enqueueSolve(cudaStream_t s, bool timedForward) {
       launchLargeForward(d_, pplan_, f32, f32 ? d_.rref : d_.del, sweep, s);
     }
     if (sweep == 1 && timedForward) recordPhase(ev_[6], s);
-    if (sweep == 0 && timedForward) recordPhase(ev_[7], s);
-    launchLargeBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
-    launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
-    if (sweep == 0 && timedForward) recordPhase(ev_[8], s);
+    if (sweep == timedBackward && timedForward) recordPhase(ev_[7], s);
+    if (!(sweep == 0 && backwardDone)) {
+      launchLargeBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
+      launchBackward(d_, pplan_, f32, sweep, sweep == sw - 1, s);
+    }
+    if (sweep == timedBackward && timedForward) recordPhase(ev_[8], s);
   }
 }
 
@@ -1568,10 +1573,14 @@ void Engine::enqueueAssembly(cudaStream_t s) {
 // second half: factorisation and solves, the increment, the element pass and
 // the convergence test
 void Engine::enqueueSolveUpdate(cudaStream_t s) {
+  // Batches without large fronts run the first solve's back substitution in
+  // the factorisation's launch: a model's back substitution starts as soon as
+  // its own elimination is done, beside the other models' factorisations.
+  const bool fuse = fusableBackward(pplan_, opt_.fp32Factor);
   recordPhase(ev_[0], s);
-  enqueueFactor(s);
+  enqueueFactor(s, fuse);
   recordPhase(ev_[1], s);
-  enqueueSolve(s, true);
+  enqueueSolve(s, true, fuse);
   recordPhase(ev_[2], s);
   launchIncrement(d_, s);
   recordPhase(ev_[3], s);
@@ -1900,8 +1909,10 @@ void Engine::enqueueIteration(cudaStream_t s) {
   // element Newton build + rotate (one fused kernel for compressed beams), CSR gather,
   // increment, norms partial + control, step end) + the factorisation with the first
   // forward elimination + per further solve a refinement residual and a forward
-  // elimination + a back substitution per solve
-  const int solveLaunches = (2 * sw - 1 + (sw - 1)) * (pplan_.nLargeTasks > 0 ? 2 : 1);
+  // elimination + a back substitution per solve (the first solve's inside the
+  // factorisation's launch when fused)
+  const int solveLaunches = (2 * sw - 1 + (sw - 1)) * (pplan_.nLargeTasks > 0 ? 2 : 1) -
+                            (fusableBackward(pplan_, opt_.fp32Factor) ? 1 : 0);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl * (pplan_.nLargeTasks > 0 ? 2 : 1) + solveLaunches +
                      (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +

@@ -173,8 +173,10 @@ class Engine {
   void enqueueIteration(cudaStream_t s);
   void enqueueAssembly(cudaStream_t s);
   void enqueueSolveUpdate(cudaStream_t s);
-  void enqueueSolve(cudaStream_t s, bool timedForward = false);
-  void enqueueFactor(cudaStream_t s);
+  // backwardDone: the first solve's back substitution already ran in the
+  // factorisation's launch (enqueueFactor with withBackward)
+  void enqueueSolve(cudaStream_t s, bool timedForward = false, bool backwardDone = false);
+  void enqueueFactor(cudaStream_t s, bool withBackward = false);
   int readActive();
   // the autotuner: runs once, before the first batched iteration
   void ensureTuned();

@@ -462,6 +462,21 @@ __device__ inline bool climb(const ParentLink& l, int* cnt, int lane) {
   return go != 0;
 }
 
+// A root's elimination is complete: its counter gets kRootDone added with
+// release semantics (after the warp barrier that orders every lane's stores),
+// which the fused back substitution acquires before it solves the root.
+constexpr int kRootDone = 1 << 24;
+__device__ inline void releaseRoot(int* cnt, int f, int lane) {
+  __syncwarp();
+  if (lane == 0) asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(cnt + f), "r"(kRootDone) : "memory");
+  __syncwarp();
+}
+__device__ inline int acquireCount(const int* c) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(c) : "memory");
+  return v;
+}
+
 // Leaves are taken in their stored order (longest root paths first) from a
 // launch-wide counter, cnt[nfrontTot]; lane 0 asks for the next leaf before
 // the current one is processed, so the request's latency is hidden.
@@ -480,10 +495,14 @@ constexpr int kGroupBit = 1 << 30;
 // factorisation (models with a tangent update) fused with the forward
 // elimination of the first solve (all active models): one climb per front, and
 // the forward elimination reads L from the front still in shared memory
+template <typename T>
+__device__ void backwardQueueLoop(const DevData& d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
+                                  const unsigned char* bwInline, int* errFlag, int acc, int finalize,
+                                  long long spinLimit, T* xs, T* Ls, int lane, const int* rootDone);
 template <typename T, int PANEL>
 __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves, int nLeaves, int maxRow,
                                       const T* asmVal, T* Lbase, T* Ubase, double tolFact, const double* rhs, T* X,
-                                      T* Wv, int* cnt) {
+                                      T* Wv, int* cnt, FusedBackward fb) {
   pdlEntry();
   extern __shared__ __align__(16) unsigned char smraw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -511,10 +530,18 @@ __global__ void kFactorForwardCascade(DevData d, const int* __restrict__ leaves,
       }
       if (!forwardOneFrontFast<T>(d, q, v, F, capL, Lbase, rhs, X, Wv, lane, Lres, Wv + q.wOff))
         forwardOneFront<T>(d, f, v, F, capL, Lbase, rhs, X, Wv, lane, Lres);
+      if (fb.queue && q.parent < 0) releaseRoot(cnt, f, lane);
       f = climb(pl, cnt, lane) ? q.parent : -1;
     }
     idx = __shfl_sync(0xffffffffu, pending, 0);
   }
+  // Fused first back substitution: once every leaf is taken, the warp serves
+  // the back-substitution queue.  Every front still to be eliminated belongs to
+  // a running warp that never waits, so a root the queue hands out completes;
+  // the warp waits for it (bounded) before solving it.
+  if (fb.queue)
+    backwardQueueLoop<T>(d, maxRow, fb.capL, Lbase, X, fb.queue, fb.ctr, fb.bwInline, fb.errFlag, fb.acc, fb.finalize,
+                         fb.spinLimit, v, F, lane, cnt);
 }
 
 template <typename T>
@@ -595,12 +622,28 @@ __device__ inline BackDesc backDesc(const DevData& d, const unsigned char* bwInl
   return q;
 }
 
+// l2Only: L was written in the same launch (fused back substitution), so it
+// is staged through L2 loads; an L1 line filled earlier in the launch by a
+// neighbouring front's solve could hold its old values (fusableBackward
+// guarantees that every block fits the staging area)
 template <typename T>
 __device__ void backwardOneFront(const DevData& d, const BackDesc& q, T* xs, T* Ls, int capL, const T* Lbase, T* X,
-                                 int acc, bool finalize, int lane) {
+                                 int acc, bool finalize, int lane, bool l2Only = false) {
   const int nr = q.nr, np = q.np;
   const int* rows = d.frontRows + q.rowOff;
-  const T* L = stageL(Lbase + q.lOff, nr * np, Ls, capL, lane);
+  const T* L;
+  if (l2Only) {
+    const T* Lg = Lbase + q.lOff;
+    const int cnt = nr * np;
+    if (cnt > capL) {
+      L = Lg;
+    } else {
+      for (int k = lane; k < cnt; k += 32) Ls[k] = __ldcg(Lg + k);
+      L = Ls;
+    }
+  } else {
+    L = stageL(Lbase + q.lOff, nr * np, Ls, capL, lane);
+  }
   for (int r = lane; r < nr; r += 32) xs[r] = __ldcg(X + __ldg(rows + r));
   copyAsyncWait();
   __syncwarp();
@@ -659,15 +702,12 @@ __device__ void backwardOneFront(const DevData& d, const BackDesc& q, T* xs, T* 
 // for is held by a running warp that solves without waiting, so each wait
 // ends; it is still bounded and sets errFlag when it runs out.
 // ctr: [0] next slot to take, [1] next free slot, [2] slot total.
+// rootDone: the fused factorisation's counters (a root may still be in
+// elimination in the same launch), or null when the roots are complete
 template <typename T>
-__global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
-                               const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize,
-                               long long spinLimit) {
-  pdlEntry();
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
-  T* Ls = xs + maxRow;
+__device__ void backwardQueueLoop(const DevData& d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
+                                  const unsigned char* bwInline, int* errFlag, int acc, int finalize,
+                                  long long spinLimit, T* xs, T* Ls, int lane, const int* rootDone) {
   const int total = *(volatile const int*)(ctr + 2);
   for (;;) {
     const int slot = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(ctr, 1) : 0, 0);
@@ -684,6 +724,17 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
         }
       }
       __threadfence();
+      // a root of an active model: wait until its elimination is released
+      if (ok && rootDone && d.fParent[f] < 0 && (d.m.flags[d.fModel[f]] & FL_ACTIVE)) {
+        while (acquireCount(rootDone + f) < kRootDone) {
+          __nanosleep(32);
+          if (++spins > spinLimit) {
+            atomicOr(errFlag, 1);
+            ok = 0;
+            break;
+          }
+        }
+      }
     }
     f = __shfl_sync(0xffffffffu, f, 0);
     ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -695,7 +746,7 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
       const int* ch = d.childList + q.childOff;
       const int c0 = q.nch > 0 ? ch[0] : -1;
       const BackDesc cq = backDesc(d, bwInline, c0 >= 0 ? c0 : f);
-      backwardOneFront<T>(d, q, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
+      backwardOneFront<T>(d, q, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane, rootDone != nullptr);
       __threadfence();
       __syncwarp();
       const int nch = q.nch;
@@ -706,7 +757,7 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
           BackDesc lq = cq;
           for (int c = 0; c < nch; ++c) {
             const BackDesc nq = backDesc(d, bwInline, ch[c + 1 < nch ? c + 1 : c]);
-            backwardOneFront<T>(d, lq, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane);
+            backwardOneFront<T>(d, lq, xs, Ls, capL, Lbase, X, acc, finalize != 0, lane, rootDone != nullptr);
             __syncwarp();
             lq = nq;
           }
@@ -723,6 +774,19 @@ __global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, 
       q = cq;
     }
   }
+}
+
+template <typename T>
+__global__ void kBackwardQueue(DevData d, int maxRow, int capL, const T* Lbase, T* X, int* queue, int* ctr,
+                               const unsigned char* __restrict__ bwInline, int* errFlag, int acc, int finalize,
+                               long long spinLimit) {
+  pdlEntry();
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* xs = reinterpret_cast<T*>(smraw) + (size_t)w * (maxRow + capL);
+  T* Ls = xs + maxRow;
+  backwardQueueLoop<T>(d, maxRow, capL, Lbase, X, queue, ctr, bwInline, errFlag, acc, finalize, spinLimit, xs, Ls,
+                       lane, nullptr);
 }
 
 int smCountCached() {
@@ -756,12 +820,13 @@ void allowBigSmem(K kernel, size_t bytes) {
 // one launch of a factor cascade kernel (either panel variant)
 template <typename T>
 void factorCascade(void (*kernel)(DevData, const int*, int, int, const T*, T*, T*, double, const double*, T*, T*,
-                                  int*),
+                                  int*, FusedBackward),
                    int wpb, size_t sm, const DevData& d, const PersistentPlan& p, const T* asmVal, T* L, T* U,
-                   double tol, const double* rhs, T* X, T* W, cudaStream_t s) {
+                   double tol, const double* rhs, T* X, T* W, const FusedBackward& fb, cudaStream_t s) {
   allowBigSmem(kernel, sm);
   const int blocks = occupancyBlocks(kernel, 32 * wpb, sm, (p.nLeaves + wpb - 1) / wpb);
-  pdlLaunch(kernel, blocks, 32 * wpb, sm, s, d, p.leaves, p.nLeaves, p.maxRow, asmVal, L, U, tol, rhs, X, W, p.cntFactor);
+  pdlLaunch(kernel, blocks, 32 * wpb, sm, s, d, p.leaves, p.nLeaves, p.maxRow, asmVal, L, U, tol, rhs, X, W, p.cntFactor,
+            fb);
 }
 
 int factorWarpsPerBlock(size_t perWarpBytes) {
@@ -796,34 +861,47 @@ void launchProbeEntries(const DevData& d, bool fp32, cudaStream_t s) {
 }
 
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
-                                cudaStream_t s) {
+                                cudaStream_t s, bool withBackward, bool lastSweep) {
   if (p.nLeaves <= 0) return;
   const double tol = 1.0e-12;
   const size_t perWarp = (size_t)p.maxRow * p.maxRow + 3 * p.maxRow;
+  // the fused back substitution of solve 0 (launchBackward's arguments); its
+  // solve vector and L staging reuse the warp's v and F areas
+  FusedBackward fb;
+  if (withBackward) {
+    fb.queue = p.bwQueue;
+    fb.ctr = p.bwCtr;
+    fb.bwInline = p.bwInline;
+    fb.errFlag = p.errFlag;
+    fb.spinLimit = p.spinLimit;
+    fb.acc = fp32 ? ACC_FIRST : ACC_SET;
+    fb.finalize = (fp32 && lastSweep) ? 1 : 0;
+    fb.capL = stagingCapacity(p, fp32 ? sizeof(float) : sizeof(double));
+  }
   if (fp32) {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(float));
     const size_t sm = (size_t)wpb * perWarp * sizeof(float);
     if (p.factorPanel == kPanelRegisters)
       factorCascade(kFactorForwardCascade<float, kPanelRegisters>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
-                    d.x32, d.w32, s);
+                    d.x32, d.w32, fb, s);
     else if (p.factorPanel == kPanelRegisters4)
       factorCascade(kFactorForwardCascade<float, kPanelRegisters4>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol,
-                    rhs, d.x32, d.w32, s);
+                    rhs, d.x32, d.w32, fb, s);
     else
       factorCascade(kFactorForwardCascade<float, kPanelShuffle>, wpb, sm, d, p, d.asmVal32, d.L32, d.U32, tol, rhs,
-                    d.x32, d.w32, s);
+                    d.x32, d.w32, fb, s);
   } else {
     const int wpb = factorWarpsPerBlock(perWarp * sizeof(double));
     const size_t sm = (size_t)wpb * perWarp * sizeof(double);
     if (p.factorPanel == kPanelRegisters)
       factorCascade(kFactorForwardCascade<double, kPanelRegisters>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol,
-                    rhs, d.x64, d.w64, s);
+                    rhs, d.x64, d.w64, fb, s);
     else if (p.factorPanel == kPanelRegisters4)
       factorCascade(kFactorForwardCascade<double, kPanelRegisters4>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol,
-                    rhs, d.x64, d.w64, s);
+                    rhs, d.x64, d.w64, fb, s);
     else
       factorCascade(kFactorForwardCascade<double, kPanelShuffle>, wpb, sm, d, p, d.asmVal64, d.L64, d.U64, tol, rhs,
-                    d.x64, d.w64, s);
+                    d.x64, d.w64, fb, s);
   }
 }
 
@@ -832,6 +910,11 @@ int stagingCapacity(const PersistentPlan& p, size_t elemBytes) {
   long long want = (long long)p.maxRow * p.maxNpiv;
   long long cap = (long long)(12 * 1024 / elemBytes);
   return (int)(want < cap ? want : cap);
+}
+
+bool fusableBackward(const PersistentPlan& p, bool fp32) {
+  return p.nLeaves > 0 && p.nLargeTasks == 0 &&
+         (long long)stagingCapacity(p, fp32 ? sizeof(float) : sizeof(double)) >= (long long)p.maxRow * p.maxNpiv;
 }
 
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,

@@ -177,10 +177,27 @@ void launchLargeForward(const DevData& d, const PersistentPlan& p, bool fp32, co
 void launchLargeBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sweep, bool last, cudaStream_t s);
 // values of one front's L block the solve kernels stage in shared memory
 int stagingCapacity(const PersistentPlan& p, size_t elemBytes);
+// The first solve's back substitution run by the factorisation's own launch
+// (its warps serve the solve's queue once every leaf is taken); queue null:
+// not fused.  Batches without large fronts only.
+struct FusedBackward {
+  int* queue = nullptr;
+  int* ctr = nullptr;
+  const unsigned char* bwInline = nullptr;
+  int* errFlag = nullptr;
+  long long spinLimit = 0;
+  int acc = 0, finalize = 0, capL = 0;
+};
+// whether the factorisation's launch can run the first back substitution: no
+// large fronts, and every front's L block fits the warp's staging area (the
+// fused solve reads L through L2 into shared memory)
+bool fusableBackward(const PersistentPlan& p, bool fp32);
 // factorisation of the models with a tangent update fused with the forward
-// elimination of rhs for every active model (first solve of an iteration)
+// elimination of rhs for every active model (first solve of an iteration);
+// withBackward: the back substitution of that solve too (lastSweep: it is the
+// iteration's last solve), in place of launchBackward for sweep 0
 void launchFactorForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs,
-                                cudaStream_t s);
+                                cudaStream_t s, bool withBackward = false, bool lastSweep = false);
 // forward elimination of the right-hand side rhs (FP64, rounded to the solve precision)
 void launchForwardCascade(const DevData& d, const PersistentPlan& p, bool fp32, const double* rhs, int sweep,
                           cudaStream_t s);

@@ -203,7 +203,10 @@ class Batch:
 
     def phase_timings(self, reset=False):
         """(samples, [element ms, factor + first forward ms, other solve ms, second forward ms,
-        first back substitution ms], active elements) sampled inside run()."""
+        back substitution ms], active elements) sampled inside run().  The back
+        substitution is the one launched on its own: the first solve's, or the
+        second solve's where the first runs inside the factorisation's launch
+        (batches without large fronts)."""
         ms = np.zeros(5)
         el = ctypes.c_longlong()
         n = self._lib.fgpu_batch_phase_timings_n(self._h, _ptr(ms, ctypes.c_double), 5, ctypes.byref(el),

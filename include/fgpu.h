@@ -107,14 +107,17 @@ int fgpu_batch_snapshot(fgpu_batch* b);
 int fgpu_batch_restore(fgpu_batch* b);
 /* CUDA-event samples of phases of the batched iteration, taken inside
  * fgpu_batch_run: ms4 = summed milliseconds of {element pass after the
- * increment, multifrontal factorisation with the first forward elimination,
- * the remaining solve launches incl. refinement, the forward elimination of
+ * increment, multifrontal factorisation with the first forward elimination
+ * (and the first back substitution in batches without large fronts), the
+ * remaining solve launches incl. refinement, the forward elimination of
  * the second solve (0 with one solve)}; elems = summed active elements of the
  * sampled iterations.  Returns the number of samples; reset != 0 clears the
  * accumulators afterwards. */
 long long fgpu_batch_phase_timings(fgpu_batch* b, double* ms4, long long* elems, int reset);
-/* The same with n (1..5) phases: the four above, then the back substitution of
- * the first solve of the iteration. */
+/* The same with n (1..5) phases: the four above, then the back substitution
+ * launched on its own -- the first solve's, or, in batches without large
+ * fronts (where the first solve's back substitution runs inside the
+ * factorisation's launch), the second solve's (0 with one solve). */
 long long fgpu_batch_phase_timings_n(fgpu_batch* b, double* ms, int n, long long* elems, int reset);
 /* Times reps launches of the factorisation fused with the first forward
  * elimination with every model factoring (CUDA events on the batch's stream).
