@@ -871,10 +871,13 @@ __global__ void __launch_bounds__(kSlotBlock / kGatherSlotsPerThread) kCsrGather
 }
 
 // increment: expand the solution, update velocities/accelerations and triads
+// threads [0, ntriTot) update a triad each (rotation increments: the heavier
+// work, in the first blocks), threads [ntriTot, ntriTot + ndofTot) a DOF each
 __global__ void kIncrement(DevData d) {
   pdlEntry();
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ndofTot) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = t - d.ntriTot;
+  if (t >= d.ntriTot && i < d.ndofTot) {
     int m = d.dofModel[i];
     const int fl = d.m.flags[m];
     if (fl & FL_ACTIVE) {
@@ -900,7 +903,8 @@ __global__ void kIncrement(DevData d) {
       }
     }
   }
-  if (i < d.ntriTot) {
+  if (t < d.ntriTot) {
+    const long long i = t;
     int m = d.triModel[i];
     if ((d.m.flags[m] & FL_ACTIVE) && d.triNdof[i] > 0) {
       double inc[6] = {0, 0, 0, 0, 0, 0};
@@ -1216,12 +1220,15 @@ __global__ void kControl(DevData d) {
 
 // terminateStep (solverRoutinesModule.f90:728-827): orthonormalise the triad
 // rotations of models that finished a step; keep their deformation for the next one
+// threads [0, ntriTot) a triad each, threads [ntriTot, ntriTot + nelTot) an element each
 __global__ void kStepEnd(DevData d) {
   pdlEntry();
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ntriTot) {
-    if ((d.m.flags[d.triModel[i]] & FL_STEPDONE) && d.triNdof[i] == 6) orthonormRot(d.ur + 12 * (size_t)i);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < d.ntriTot) {
+    if ((d.m.flags[d.triModel[t]] & FL_STEPDONE) && d.triNdof[t] == 6) orthonormRot(d.ur + 12 * (size_t)t);
+    return;
   }
+  const long long i = t - d.ntriTot;
   if (i < d.nelTot) {
     const int fl = d.m.flags[d.elModel[i]];
     if ((fl & FL_STEPDONE) && !(fl & FL_LINEAR))
@@ -1425,8 +1432,7 @@ void launchCsrGather(const DevData& d, cudaStream_t s) {
   pdlLaunch(kCsrGather, grid, kSlotBlock / kGatherSlotsPerThread, 0, s, d, nb);
 }
 void launchIncrement(const DevData& d, cudaStream_t s) {
-  long long n = d.ndofTot > d.ntriTot ? d.ndofTot : d.ntriTot;
-  pdlLaunch(kIncrement, blocksFor(n), TPB, 0, s, d);
+  pdlLaunch(kIncrement, blocksFor(d.ntriTot + d.ndofTot), TPB, 0, s, d);
 }
 void launchNormsControl(const DevData& d, cudaStream_t s) {
   launchNormsPartial(d, s);
@@ -1437,8 +1443,7 @@ void launchNormsPartial(const DevData& d, cudaStream_t s) {
 }
 void launchControlStepEnd(const DevData& d, cudaStream_t s) {
   pdlLaunch(kControl, blocksFor(32LL * d.m.n, 128), 128, 0, s, d);
-  long long n = d.ntriTot > d.nelTot ? d.ntriTot : d.nelTot;
-  pdlLaunch(kStepEnd, blocksFor(n), TPB, 0, s, d);
+  pdlLaunch(kStepEnd, blocksFor(d.ntriTot + d.nelTot), TPB, 0, s, d);
   launchPartsStepEnd(d, s);
 }
 void launchLoads(const DevData& d, cudaStream_t s) {
