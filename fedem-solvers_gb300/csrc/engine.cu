@@ -135,6 +135,7 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   SetupTrace trace;
   // the forked assembly is decided once the batch's object counts are known (below)
   forkAssembly_ = false;
+  fuseBackward_ = false;
   const int nm = (int)models.size();
   // ---- global offsets --------------------------------------------------------
   modelTriOff_.assign(nm, 0);
@@ -1192,6 +1193,10 @@ int Engine::upload(const std::vector<const HostModel*>& models, const EngineOpti
   // beam elements only (no axial elements, joints or reduced parts, whose
   // Newton matrices read state the element pass updates): forked assembly
   forkAssembly_ = d_.nelTot > 0 && d_.naxTot == 0 && d_.njointTot == 0 && d_.npartTot == 0 && d_.ncxTot == 0;
+  // the first solve's back substitution inside the factorisation's launch;
+  // FGPU_NO_FUSED_BACKWARD set at batch creation keeps it a launch of its own
+  // (the same results: tests compare the two)
+  fuseBackward_ = fusableBackward(pplan_, opt_.fp32Factor) && std::getenv("FGPU_NO_FUSED_BACKWARD") == nullptr;
   FG_CHECK(cudaStreamSynchronize(stream_));
   FG_CHECK(cudaGetLastError());
   trace.mark("state registry", stream_);
@@ -1576,7 +1581,7 @@ void Engine::enqueueSolveUpdate(cudaStream_t s) {
   // Batches without large fronts run the first solve's back substitution in
   // the factorisation's launch: a model's back substitution starts as soon as
   // its own elimination is done, beside the other models' factorisations.
-  const bool fuse = fusableBackward(pplan_, opt_.fp32Factor);
+  const bool fuse = fuseBackward_;
   recordPhase(ev_[0], s);
   enqueueFactor(s, fuse);
   recordPhase(ev_[1], s);
@@ -1912,7 +1917,7 @@ void Engine::enqueueIteration(cudaStream_t s) {
   // elimination + a back substitution per solve (the first solve's inside the
   // factorisation's launch when fused)
   const int solveLaunches = (2 * sw - 1 + (sw - 1)) * (pplan_.nLargeTasks > 0 ? 2 : 1) -
-                            (fusableBackward(pplan_, opt_.fp32Factor) ? 1 : 0);
+                            (fuseBackward_ ? 1 : 0);
   launchesPerIter_ = (d_.beamSparse ? 11 : 12) + nl * (pplan_.nLargeTasks > 0 ? 2 : 1) + solveLaunches +
                      (d_.urQs ? 1 : 0) +
                      (d_.nmotTot > 0 ? 1 : 0) + (d_.nmrTot > 0 ? 1 : 0) + (d_.naxTot > 0 ? 3 : 0) +

@@ -210,6 +210,7 @@ class Engine {
   cudaStream_t side_ = nullptr;
   cudaEvent_t evFork_ = nullptr, evJoin_ = nullptr;
   bool forkAssembly_ = false;
+  bool fuseBackward_ = false;  // first back substitution inside the factorisation's launch
   // every batch: the partial norms run on the side stream beside the element
   // pass after the increment (they read the increments and the residual only)
   cudaEvent_t evFork2_ = nullptr, evJoin2_ = nullptr;
