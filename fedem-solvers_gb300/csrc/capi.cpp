@@ -990,6 +990,13 @@ int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag) {
   return rc ? fail(rc, "wait probe failed") : 0;
 }
 
+int fgpu_batch_probe_root_wait_timeout(fgpu_batch* b, long long spins, int* flag) {
+  if (!b || spins < 1) return fail(-1, "bad argument");
+  OnDevice onDev(b->engine.device());
+  int rc = b->engine.probeRootWaitTimeout(spins, flag);
+  return rc ? fail(rc, "root wait probe failed") : 0;
+}
+
 int fgpu_set_device(int ordinal) {
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);

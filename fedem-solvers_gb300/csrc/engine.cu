@@ -1997,6 +1997,40 @@ int Engine::probeWaitTimeout(long long spins, int* flag) {
   return 0;
 }
 
+int Engine::probeRootWaitTimeout(long long spins, int* flag) {
+  const int nf = d_.nfrontTot;
+  if (nf <= 0 || d_.m.n <= 0) return -957;
+  // a root of model 0, marked active for the probe (its flags are put back)
+  std::vector<int> parent(nf), fmodel(nf);
+  cudaMemcpyAsync(parent.data(), d_.fParent, sizeof(int) * nf, cudaMemcpyDeviceToHost, stream_);
+  cudaMemcpyAsync(fmodel.data(), d_.fModel, sizeof(int) * nf, cudaMemcpyDeviceToHost, stream_);
+  int fl0 = 0;
+  cudaMemcpyAsync(&fl0, d_.m.flags, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -956;
+  int root = -1;
+  for (int f = 0; f < nf && root < 0; ++f)
+    if (parent[f] < 0 && fmodel[f] == 0) root = f;
+  if (root < 0) return -957;
+  // queue slot 0 = the root; ctr = {take 0, fill 1, total 1}; counters zero
+  const size_t ints = 8 + (size_t)nf + 1;
+  int* q = nullptr;
+  if (cudaMalloc(&q, sizeof(int) * ints) != cudaSuccess) return -955;
+  const int init[8] = {root, 0, 0, 0, 0, 1, 1, 0};
+  cudaMemsetAsync(q, 0, sizeof(int) * ints, stream_);
+  cudaMemcpyAsync(q, init, sizeof(init), cudaMemcpyHostToDevice, stream_);
+  const int act = fl0 | FL_ACTIVE;
+  cudaMemcpyAsync(d_.m.flags, &act, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  launchRootWaitProbe(d_, pplan_, q, q + 4, q + 8, spins, stream_);
+  cudaMemcpyAsync(d_.m.flags, &fl0, sizeof(int), cudaMemcpyHostToDevice, stream_);
+  int f = 0;
+  cudaMemcpyAsync(&f, pplan_.errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+  const cudaError_t e = cudaStreamSynchronize(stream_);
+  cudaFree(q);
+  if (e != cudaSuccess) return -956;
+  if (flag) *flag = f;
+  return 0;
+}
+
 int Engine::run(long long maxBatched, RunStats* stats) {
   ensureTuned();
   if (opt_.useGraph && !graphExec_) {

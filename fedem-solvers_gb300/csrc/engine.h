@@ -146,6 +146,8 @@ class Engine {
   void resetPhaseTimings();
   // Test hook: a bounded wait of `spins` polls that nothing ends (see engine.cu).
   int probeWaitTimeout(long long spins, int* flag);
+  // the same for the fused back substitution's wait for a root's elimination
+  int probeRootWaitTimeout(long long spins, int* flag);
 
   // Launch shapes of the multifrontal kernels (PersistentPlan: factor panel
   // variant, forward and backward warps per block, large-front cluster size).

@@ -974,4 +974,24 @@ void launchBackwardWaitProbe(const DevData& d, const PersistentPlan& p, int* que
                                            ACC_SET, 0, spins);
 }
 
+void launchRootWaitProbe(const DevData& d, const PersistentPlan& p, int* queue, int* ctr, int* cnt, long long spins,
+                         cudaStream_t s) {
+  // one warp of the fused factorisation with no leaf: it goes straight to the
+  // back substitution, takes slot 0 (a root) and waits for a release that no
+  // elimination makes (cnt is zero); the wait gives up before any front is touched
+  const size_t perWarp = (size_t)p.maxRow * p.maxRow + 3 * p.maxRow;
+  const size_t sm = perWarp * sizeof(double);
+  FusedBackward fb;
+  fb.queue = queue;
+  fb.ctr = ctr;
+  fb.bwInline = p.bwInline;
+  fb.errFlag = p.errFlag;
+  fb.spinLimit = spins;
+  fb.acc = ACC_SET;
+  fb.capL = stagingCapacity(p, sizeof(double));
+  allowBigSmem(kFactorForwardCascade<double, kPanelShuffle>, sm);
+  pdlLaunch(kFactorForwardCascade<double, kPanelShuffle>, 1, 32, sm, s, d, p.leaves, 0, p.maxRow,
+            (const double*)d.asmVal64, d.L64, d.U64, 1.0e-12, (const double*)d.del, d.x64, d.w64, cnt, fb);
+}
+
 }  // namespace fgpu

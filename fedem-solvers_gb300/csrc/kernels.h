@@ -209,6 +209,12 @@ void launchBackward(const DevData& d, const PersistentPlan& p, bool fp32, int sw
 // empty slot 0 and a slot total of 1 the wait runs out and sets p.errFlag.
 void launchBackwardWaitProbe(const DevData& d, const PersistentPlan& p, int* queue, int* ctr, long long spins,
                              cudaStream_t s);
+// One warp of the fused factorisation without leaves on a private queue whose
+// slot 0 holds a root of an active model and private counters cnt (zeroed,
+// nfrontTot + 1): the root's release never comes, so the bounded wait runs out
+// after `spins` polls and sets p.errFlag.
+void launchRootWaitProbe(const DevData& d, const PersistentPlan& p, int* queue, int* ctr, int* cnt, long long spins,
+                         cudaStream_t s);
 // prescribed deflections (step start), their predictor right-hand side (after the
 // element Newton matrices), and the restart state of pure linear quasi-static steps
 void launchMotions(const DevData& d, cudaStream_t s);

@@ -99,6 +99,7 @@ def load_library(path=None):
         "fgpu_get_device": (c_int, [P(c_int), ctypes.c_char_p, c_int]),
         "fgpu_batch_device": (c_int, [vp]),
         "fgpu_batch_probe_wait_timeout": (c_int, [vp, c_ll, P(c_int)]),
+        "fgpu_batch_probe_root_wait_timeout": (c_int, [vp, c_ll, P(c_int)]),
         "fgpu_measure_fp64_peak": (c_int, [P(c_dbl), P(c_dbl)]),
         "fgpu_measure_tf32_mma_peak": (c_int, [P(c_dbl), P(c_dbl)]),
         "fgpu_batch_set_launch_shape": (c_int, [vp, P(c_int)]),

@@ -194,6 +194,14 @@ int fgpu_batch_results_close(fgpu_batch* b);
  * still running then fails with status 16 (wait timed out) at its next
  * convergence test, as after a real wait that ran out. */
 int fgpu_batch_probe_wait_timeout(fgpu_batch* b, long long spins, int* flag);
+/* The same for the other bounded wait of the back substitution: where it runs
+ * inside the factorisation's launch, a warp waits for the elimination of the
+ * root it takes from the queue.  One warp of that launch, with no leaf to
+ * factor, takes a root of the batch's first model from a private queue and
+ * waits for a release that nothing makes; the wait runs out after `spins`
+ * polls and sets the wait-error flag (*flag = 1).  No front is touched; the
+ * running models then fail with status 16 as above. */
+int fgpu_batch_probe_root_wait_timeout(fgpu_batch* b, long long spins, int* flag);
 
 /* Measured FP64 fused multiply-add rate of the library's current device:
  * eight independent FMA chains per thread, eight 256-thread blocks per SM,

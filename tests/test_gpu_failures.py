@@ -150,6 +150,33 @@ def test_bounded_wait_runs_out_and_fails_the_models(gpu):
     m.close()
 
 
+def test_root_wait_runs_out_and_fails_the_models(gpu):
+    """The fused back substitution's wait for a root's elimination (a release
+    that nothing makes) gives up after its poll limit and sets the batch's wait
+    flag, like the queue-slot wait; the running models then fail with
+    SS_TIMEOUT and the context stays usable."""
+    import ctypes
+
+    from fedem_gb300 import load_library
+    from fedem_gb300.batch import Batch, Model
+
+    lib = load_library()
+    m = Model(*_good_cases()[0])
+    b = Batch([m])
+    flag = ctypes.c_int(0)
+    assert lib.fgpu_batch_probe_root_wait_timeout(b._h, 4096, ctypes.byref(flag)) == 0, lib.fgpu_last_error()
+    assert flag.value == 1
+    b.run()
+    info = b.info(0)
+    assert info["state"] == ST_ERROR and (info["status"] & SS_TIMEOUT)
+    b.close()
+    b2 = Batch([m])
+    st = b2.run()
+    assert st["models_done"] == 1 and st["models_failed"] == 0
+    b2.close()
+    m.close()
+
+
 def test_selected_device_is_honoured(gpu):
     """fgpu_set_device(0): the library's current device and the batch's device
     are ordinal 0, and the PCI bus id of that device is reported."""
