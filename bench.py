@@ -54,10 +54,11 @@ ELEM_BYTES = 1630
 # DRAM bytes (read + write) of one launch on this workload (256 models): the
 # mean of the first two Newton-iteration launches of each kernel captured by
 # ncu on the first 128 of these models, scaled by the ratio of algorithmic
-# bytes (fronts) or of elements (profiles/dram_traffic_beam_batch_128models.md)
+# bytes (fronts) or of elements (profiles/dram_traffic_beam_batch_128models.md);
+# for the back substitution the refinement solve's launch
 FACTOR_TRAFFIC_256 = 202.5e6
 FORWARD_TRAFFIC_256 = 152.1e6
-BACKWARD_TRAFFIC_256 = 133.2e6
+BACKWARD_TRAFFIC_256 = 137.4e6
 # DRAM bytes per element of the element pass after the increment (same capture)
 ELEM_TRAFFIC = 1238
 
